@@ -1,0 +1,386 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 state-vector engine on the 30-qubit gate sweep.
+
+Workload (one step): a seeded depth-40 random circuit on 30 qubits — each
+layer H/RX/RY/RZ on every qubit, then 15 disjoint CNOT/CZ/SWAP pairs, half
+nearest-neighbour, half long-range — applied to a resident complex64 state
+(8 GiB, larger than L2, so no flush is needed between steps). The metric is
+whole-job gates/s; the roofline is HBM bandwidth of the tile-pass kernel
+(2 * 2^30 * 8 bytes per pass). Also reported: end-to-end gates/s through the
+C ABI with host buffers (qf_run_circuit: upload f64 amplitudes, run, download),
+the CPU baseline (the oracle restating the reference's rayon path, on every
+host core, on a bounded sample of the same circuit), and 24-qubit VQE
+adjoint vs parameter-shift gradients/s.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "30q gates/s (HBM GB/s vs peak); adjoint vs param-shift grads/s at 1e-5 err"
+UNIT = "gates/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--qubits", type=int, default=30)
+    ap.add_argument("--depth", type=int, default=40)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--dtype", default="c64")
+    ap.add_argument("--tile", type=int, default=0)
+    ap.add_argument("--mode", default="auto", choices=["auto", "unfused", "fused"])
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extra", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def hbm_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    try:
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_sample_ops(ops):
+    """A bounded sample of the circuit keeping its 1q:2q mix: the first two
+    one-qubit gates, then the first two-qubit gate, repeated down the list."""
+    from quantumforge_gb300 import _abi as A
+
+    one = [i for i, r in enumerate(ops) if r["kind"] == A.OP_GATE]
+    two = [i for i, r in enumerate(ops) if r["kind"] != A.OP_GATE]
+    seq = []
+    for k in range(len(two)):
+        seq += one[2 * k: 2 * k + 2] + [two[k]]
+    return seq
+
+
+def time_cpu_oracle(n, ops, seconds, threads):
+    """The oracle's restatement of the reference CPU path (rayon clone/map/
+    collect for one-qubit gates on `threads` threads, single-threaded two-qubit
+    loops), timed on the same circuit until `seconds` have elapsed."""
+    import numpy as np
+
+    import oracle as O
+
+    a = np.zeros(1 << n, dtype=np.complex128)
+    a.view(np.float64)[::512] = 0.0  # touch every page before timing
+    a[0] = 1.0
+    seq = cpu_sample_ops(ops)
+    done = 0
+    t0 = time.perf_counter()
+    for idx in seq:
+        rec = ops[idx: idx + 1]
+        st = O.lib().qfo_run_ops(O._p(a), n, O._p(rec), 1, None, 0, None, 0, -1, 0.0, threads)
+        if st:
+            raise RuntimeError(f"oracle failed with status {st}")
+        done += 1
+        if time.perf_counter() - t0 >= seconds:
+            break
+    dt = time.perf_counter() - t0
+    n1 = sum(1 for i in seq[:done] if ops[i]["kind"] == 0)
+    return done / dt, f"first {done} gates ({n1} one-qubit, {done - n1} two-qubit, in circuit order, 1q:2q = 2:1) " \
+                      f"of the {n}-qubit circuit, complex128 as the reference, {dt:.1f} s"
+
+
+def reference_arm(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    from quantumforge_gb300 import workloads as W
+
+    ops = W.random_circuit(args.qubits, args.depth, args.seed, two_qubit="mixed")
+    threads = os.cpu_count() or 1
+    import numpy as np
+
+    import oracle as O
+
+    n = args.qubits
+    a = np.zeros(1 << n, dtype=np.complex128)
+    a.view(np.float64)[::512] = 0.0
+    a[0] = 1.0
+    seq = cpu_sample_ops(ops)
+    step_times = []
+    for s in range(args.warmup + args.steps):
+        idx = seq[s % len(seq)]
+        rec = ops[idx: idx + 1]
+        t0 = time.perf_counter()
+        st = O.lib().qfo_run_ops(O._p(a), n, O._p(rec), 1, None, 0, None, 0, -1, 0.0, threads)
+        dt = time.perf_counter() - t0
+        if st:
+            raise RuntimeError(f"oracle failed with status {st}")
+        if s >= args.warmup:
+            step_times.append(dt)
+    total = sum(step_times)
+    value = len(step_times) / total
+    sample = f"one gate per step, cycling the circuit's gates with its 1q:2q = 2:1 mix; {n} qubits complex128"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000 * total / len(step_times), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "complex128", "data": "synthetic",
+        "config": {"workload": f"{n}q depth-{args.depth} mixed random circuit (seed {args.seed})", "qubits": n,
+                   "depth": args.depth, "gates": len(ops)},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference is Rust (no toolchain on this box): its CPU path is timed through the oracle's C "
+                "restatement of StateVector::apply/apply_cnot/apply_cz/apply_swap",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import quantumforge_gb300 as qf
+    from quantumforge_gb300 import _abi as A
+    from quantumforge_gb300 import _native
+    from quantumforge_gb300 import workloads as W
+
+    n = args.qubits
+    backend = qf.CudaBackend(local)
+    ops = W.random_circuit(n, args.depth, args.seed, two_qubit="mixed")
+    n_gates = len(ops)
+    dcode = A.C64 if args.dtype in ("c64", "complex64") else A.C128
+    amp_bytes = 8 if dcode == A.C64 else 16
+    mode = {"auto": A.EXEC_AUTO, "unfused": A.EXEC_UNFUSED, "fused": A.EXEC_FUSED}[args.mode]
+    exec_opts = {"mode": args.mode, "tile_qubits": args.tile}
+    lib = _native.load()
+    npass, ngate = C.c_uint64(), C.c_uint64()
+    eo = A.ExecOpts(mode, args.tile, 0, 0)
+    _native.check(lib.qf_plan_stats(n, dcode, _native.ptr(ops), len(ops), None, 0, None, 0, C.byref(eo),
+                                    C.byref(npass), C.byref(ngate)))
+    n_passes = npass.value
+
+    sv = qf.StateVector.zero(n, dtype=args.dtype, backend=backend)
+    sp = C.c_void_p()
+    lib.qf_ctx_stream(backend.handle, C.byref(sp))
+    stream = torch.cuda.ExternalStream(sp.value, device=torch.device("cuda", local))
+
+    for _ in range(args.warmup):
+        sv.apply_ops(ops, exec_opts=exec_opts)
+    backend.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    backend.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    time.sleep(0.4)  # let the sampler attach before the timed region
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        sv.apply_ops(ops, exec_opts=exec_opts)
+    ev1.record(stream)
+    ev1.synchronize()
+    backend.synchronize()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    t = ev0.elapsed_time(ev1) / 1000.0
+    if world > 1:
+        tt = torch.tensor([t], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t = float(tt.item())
+    value = world * args.steps * n_gates / t
+    ms_per_step = 1000.0 * t / args.steps
+    # roofline of the dominant kernel (k_tile_pass): every launch is one full
+    # read + write sweep of the state
+    bytes_per_launch = 2 * (1 << n) * amp_bytes
+    launches = args.steps * n_passes
+    avg_launch_s = t / launches
+    achieved = bytes_per_launch / avg_launch_s / 1e9
+    peak, peak_kind = hbm_peak()
+    traffic = None
+    tf = ROOT / "profiles" / "tile_pass_traffic.json"
+    if tf.exists():
+        try:
+            traffic = json.loads(tf.read_text()).get(f"{n}q_{args.dtype}_bytes_per_launch")
+        except Exception:
+            traffic = None
+
+    # end to end through the C ABI with host buffers (pinned), copies timed
+    e2e = None
+    if args.e2e_steps > 0:
+        host_in = torch.zeros(2 << n, dtype=torch.float64, pin_memory=True)
+        host_in[0] = 1.0
+        host_out = torch.empty(2 << n, dtype=torch.float64, pin_memory=True)
+        eo2 = A.ExecOpts(mode, args.tile, 0, 0)
+        _native.check(lib.qf_run_circuit(backend.handle, n, dcode, _native.ptr(ops), len(ops),
+                                         C.c_void_p(host_in.data_ptr()), C.c_void_p(host_out.data_ptr()), 2 << n,
+                                         C.byref(eo2)))
+        if world > 1:
+            torch.distributed.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            _native.check(lib.qf_run_circuit(backend.handle, n, dcode, _native.ptr(ops), len(ops),
+                                             C.c_void_p(host_in.data_ptr()), C.c_void_p(host_out.data_ptr()), 2 << n,
+                                             C.byref(eo2)))
+        te = time.perf_counter() - t0
+        if world > 1:
+            tt = torch.tensor([te], device="cuda")
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            te = float(tt.item())
+        e2e = {"value": world * args.e2e_steps * n_gates / te, "unit": UNIT, "h2d_bytes_per_step": 16 << n,
+               "d2h_bytes_per_step": 16 << n,
+               "api": "qf_run_circuit (CudaBackend::run_circuit): f64 host amplitudes in and out, pinned"}
+        del host_in, host_out
+
+    extra = {}
+    cpu = None
+    if rank == 0 and not args.no_extra:
+        extra["vqe24"] = vqe_gradients(backend)
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, sample = time_cpu_oracle(n, ops, args.cpu_seconds, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "complex64" if dcode == A.C64 else "complex128", "data": "synthetic",
+            "config": {"workload": f"{n}q depth-{args.depth} mixed random circuit (seed {args.seed}), "
+                                   f"{args.dtype} state, {args.mode} execution",
+                       "qubits": n, "depth": args.depth, "gates": n_gates, "passes_per_step": n_passes,
+                       "tile_qubits": args.tile or "auto", "l2": "state larger than L2 (no flush needed)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic, "peak_kind": f"of {peak_kind}", "kernel": "k_tile_pass<float2,false>",
+                         "bytes_per_launch": bytes_per_launch, "avg_launch_ms": 1000 * avg_launch_s},
+            "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches,
+            "extra": extra,
+        }
+        print(json.dumps(line), flush=True)
+    backend.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def vqe_gradients(backend):
+    """24-qubit VQE (RY.RZ per qubit + CZ ring, 8 layers, 384 params, TFIM
+    ring h = 1): adjoint (checkpoint per layer) vs GPU parameter shift."""
+    import numpy as np
+
+    import quantumforge_gb300 as qf
+    from quantumforge_gb300 import workloads as W
+    from quantumforge_gb300.gradients import GradientOptions, GradientStrategy, gradient_with_inputs
+
+    n = 24
+    ops, params, H = W.vqe_tfim(n, 8, seed=3)
+    pc = qf.ParameterizedCircuit(params.size)
+    for r in ops:
+        pc.operations.append((int(r["kind"]), int(r["gate"]), int(r["q0"]), int(r["q1"]), int(r["param"]),
+                              float(r["theta"])))
+    kw = dict(dtype="c64", backend=backend, checkpoint_every=3 * n)
+    adj = gradient_with_inputs(pc, GradientOptions(strategy=GradientStrategy.Adjoint), [], params, n, H, **kw)
+    reps = 5
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        adj = gradient_with_inputs(pc, GradientOptions(strategy=GradientStrategy.Adjoint), [], params, n, H, **kw)
+    t_adj = (time.perf_counter() - t0) / reps
+    t0 = time.perf_counter()
+    sh = gradient_with_inputs(pc, GradientOptions(strategy=GradientStrategy.ParameterShift), [], params, n, H,
+                              dtype="c64", backend=backend)
+    t_sh = time.perf_counter() - t0
+    return {"qubits": n, "params": int(params.size), "ops": len(ops), "adjoint_grads_per_s": 1.0 / t_adj,
+            "param_shift_grads_per_s": 1.0 / t_sh, "ratio": t_sh / t_adj,
+            "max_abs_grad_diff_adjoint_vs_shift": float(np.abs(adj.gradient - sh.gradient).max()),
+            "energy_adjoint": adj.expectation, "energy_shift_run": sh.expectation, "dtype": "complex64"}
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

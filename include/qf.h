@@ -1,0 +1,338 @@
+/*
+ * qf.h — C ABI of the GB300 state-vector engine for QuantumForge.
+ *
+ * This header is the drop-in boundary for QuantumForge's dense state-vector
+ * path. Every entry point replaces one method of the reference's Rust API:
+ * the CPU `StateVector` / `Circuit` / `ParameterizedCircuit` / `gradients`
+ * path in `src/lib.rs` and `src/gradients.rs`, and the optional NVRTC backend
+ * `cuda::CudaBackend` / `CudaDeviceState` in `src/cuda.rs`. The comment above
+ * each declaration names the reference item it replaces (file:line in the
+ * reference crate).
+ *
+ * Conventions (mirroring the reference):
+ *   - Qubit q is bit q of the amplitude index; qubit 0 is the least
+ *     significant bit (src/lib.rs:672-679).
+ *   - Host amplitudes are interleaved (re, im) pairs of f64, the layout of the
+ *     reference's `#[repr(C)] Complex64` (src/lib.rs:437-446).
+ *   - Every call returns an `int` status: QF_OK (0) or one of the QF_ERR_*
+ *     codes, which mirror the reference's `QuantumError` and `CudaError`
+ *     variants (src/lib.rs:507-583, src/cuda.rs:3051-3078). Validation happens
+ *     before any launch, as in src/cuda.rs:2256-2285. `qf_last_error()`
+ *     returns a thread-local message for the last failing call on the thread.
+ *   - Handles are opaque. The caller owns host buffers; the library owns
+ *     device memory. A handle is used by one host thread at a time. Each
+ *     context owns one CUDA stream; all work of a context is ordered on it.
+ *   - Nothing in this header uses torch, C++ or CUDA types.
+ */
+#ifndef QF_H
+#define QF_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QF_ABI_VERSION 1
+
+/* ---------------------------------------------------------------------------
+ * Status codes. Mirror QuantumError (src/lib.rs:507-583) and CudaError
+ * (src/cuda.rs:3051-3078).
+ * ------------------------------------------------------------------------- */
+enum qf_status {
+    QF_OK = 0,
+    QF_ERR_ZERO_QUBITS = 1,                       /* QuantumError::ZeroQubits */
+    QF_ERR_MEMORY_BUDGET_EXCEEDED = 2,            /* QuantumError::MemoryBudgetExceeded */
+    QF_ERR_SIMULATION_SIZE_OVERFLOW = 3,          /* QuantumError::SimulationSizeOverflow */
+    QF_ERR_MEMORY_ALLOCATION_FAILED = 4,          /* QuantumError::MemoryAllocationFailed */
+    QF_ERR_STATE_SIZE_NOT_POWER_OF_TWO = 5,       /* QuantumError::StateSizeNotPowerOfTwo */
+    QF_ERR_QUBIT_OUT_OF_RANGE = 6,                /* QuantumError::QubitOutOfRange */
+    QF_ERR_INVALID_QUBIT_PAIR = 7,                /* QuantumError::InvalidQubitPair */
+    QF_ERR_INVALID_PROBABILITY = 8,               /* QuantumError::InvalidProbability */
+    QF_ERR_OPERATION_REQUIRES_DENSITY_MATRIX = 9, /* QuantumError::OperationRequiresDensityMatrix */
+    QF_ERR_OPERATION_REQUIRES_SHOT_EXECUTION = 10,/* QuantumError::OperationRequiresShotExecution */
+    QF_ERR_INVALID_SHOT_COUNT = 11,               /* QuantumError::InvalidShotCount */
+    QF_ERR_CLASSICAL_BIT_OUT_OF_RANGE = 12,       /* QuantumError::ClassicalBitOutOfRange */
+    QF_ERR_INVALID_PARAMETER_COUNT = 13,          /* QuantumError::InvalidParameterCount */
+    QF_ERR_INVALID_INPUT_COUNT = 14,              /* QuantumError::InvalidInputCount */
+    QF_ERR_NON_FINITE_PARAMETER = 15,             /* QuantumError::NonFiniteParameter, CudaError::NonFiniteAngle */
+    QF_ERR_INVALID_FINITE_DIFFERENCE_STEP = 16,   /* QuantumError::InvalidFiniteDifferenceStep */
+    QF_ERR_UNSUPPORTED_OPERATION = 17,            /* QuantumError::UnsupportedOperation */
+    QF_ERR_TIMEOUT = 18,                          /* QuantumError::Timeout */
+    QF_ERR_CUDA = 19,                             /* CudaError::Driver */
+    QF_ERR_INVALID_ARGUMENT = 20,                 /* null pointer, bad dtype/enum, length mismatch */
+    QF_ERR_EMPTY_BATCH = 21,                      /* CudaError::EmptyBatch */
+    QF_ERR_INCOMPATIBLE_BATCH = 22,               /* CudaError::IncompatibleBatch */
+    QF_ERR_STATE_TOO_LARGE = 23,                  /* CudaError::StateTooLarge */
+    QF_ERR_INCOMPATIBLE_DEVICE_STATE = 24         /* CudaError::IncompatibleDeviceState */
+};
+
+/* Gate codes, in the order of `enum Gate` (src/lib.rs:2239-2264). */
+enum qf_gate {
+    QF_GATE_I = 0, QF_GATE_X = 1, QF_GATE_Y = 2, QF_GATE_Z = 3, QF_GATE_H = 4,
+    QF_GATE_S = 5, QF_GATE_SDG = 6, QF_GATE_T = 7, QF_GATE_TDG = 8,
+    QF_GATE_RX = 9, QF_GATE_RY = 10, QF_GATE_RZ = 11
+};
+
+/* Single-qubit observables, in the order of `enum SingleQubitObservable`
+ * (src/lib.rs:2930-2938). Rotation axes reuse X/Y/Z = 0/1/2
+ * (`enum RotationAxis`, src/lib.rs:2919-2928). */
+enum qf_pauli1 { QF_PAULI_X = 0, QF_PAULI_Y = 1, QF_PAULI_Z = 2 };
+
+/* Operation kinds. One flat record covers both `CircuitOp`
+ * (src/lib.rs:2386-2440) and `ParameterizedOp` (src/lib.rs:2942-3006). */
+enum qf_op_kind {
+    QF_OP_GATE = 0,       /* CircuitOp::SingleQubit / ParameterizedOp::Fixed: gate on q0 (theta for RX/RY/RZ) */
+    QF_OP_CNOT = 1,       /* control q0, target q1 */
+    QF_OP_CZ = 2,         /* first q0, second q1 */
+    QF_OP_SWAP = 3,       /* first q0, second q1 */
+    QF_OP_CHANNEL = 4,    /* noise channel on q0: state-vector calls reject it like the reference */
+    QF_OP_MEASURE = 5,    /* measure q0 into classical bit `param` */
+    QF_OP_COND = 6,       /* if classical bit `param` == flags&1 apply gate on q0 */
+    QF_OP_ROTATION = 7,   /* ParameterizedOp::Rotation: axis in `gate` (QF_PAULI_*), q0, parameter index `param` */
+    QF_OP_ENCODING = 8    /* ParameterizedOp::EncodingRotation: axis in `gate`, q0, input index `param` */
+};
+
+/* One circuit operation: 24 bytes, no padding ambiguity. */
+typedef struct qf_op {
+    uint8_t kind;    /* enum qf_op_kind */
+    uint8_t gate;    /* enum qf_gate for GATE/COND, enum qf_pauli1 axis for ROTATION/ENCODING */
+    uint16_t flags;  /* COND: required classical value (bit 0) */
+    uint32_t q0;
+    uint32_t q1;
+    uint32_t param;  /* parameter / input / classical-bit index */
+    double theta;    /* fixed angle of a GATE/COND with RX/RY/RZ */
+} qf_op;
+
+/* One Pauli-string term c * P with P = (x-mask, z-mask): bit q set in both
+ * masks is Y on qubit q, only in xmask is X, only in zmask is Z. The action
+ * on a basis state follows PauliWord::apply_basis_index
+ * (src/analytic.rs:2629-2650). */
+typedef struct qf_pauli_term {
+    uint64_t xmask;
+    uint64_t zmask;
+    double coeff_re;
+    double coeff_im;
+} qf_pauli_term;
+
+/* Amplitude storage type on the device. */
+enum qf_dtype {
+    QF_C64 = 0,   /* complex64: f32 re/im; gate arithmetic in f32, reductions in f64 */
+    QF_C128 = 1   /* complex128: f64 re/im, the reference's precision */
+};
+
+/* Execution strategy for a gate list. */
+enum qf_exec_mode {
+    QF_EXEC_AUTO = 0,     /* tile-fused passes with autotuned tile width */
+    QF_EXEC_UNFUSED = 1,  /* one HBM sweep per gate (the reference's structure) */
+    QF_EXEC_FUSED = 2     /* tile-fused passes with the widths given below */
+};
+
+typedef struct qf_exec_opts {
+    int32_t mode;          /* enum qf_exec_mode */
+    int32_t tile_qubits;   /* qubits resident in shared memory per tile (0 = auto) */
+    int32_t block_qubits;  /* dense fused-block width k (0/1 = apply gates one by one, 2..5 = fuse into k-qubit blocks) */
+    int32_t reserved;
+} qf_exec_opts;
+
+/* Gradient strategies, in the order of `enum GradientStrategy`
+ * (src/gradients.rs:48-73). */
+enum qf_gradient_strategy {
+    QF_GRAD_PARAMETER_SHIFT = 0,
+    QF_GRAD_ADJOINT = 1,
+    QF_GRAD_BACKPROP = 2,
+    QF_GRAD_FINITE_DIFFERENCE = 3,
+    QF_GRAD_AUTO = 4
+};
+
+/* `GradientOptions` (src/gradients.rs:144-165) plus engine knobs. */
+typedef struct qf_gradient_opts {
+    int32_t strategy;              /* enum qf_gradient_strategy */
+    int32_t dtype;                 /* enum qf_dtype of the device state */
+    double finite_difference_step; /* default 1e-3 in the reference */
+    uint64_t shots;                /* >0 makes AUTO select parameter shift */
+    int32_t checkpoint_every;      /* adjoint: ops per checkpointed segment. The forward sweep stores
+                                      psi at every segment start; the backward sweep restores it there
+                                      instead of carrying the uncompute further (0 = pure uncompute). */
+    int32_t reserved;
+    qf_exec_opts exec;
+} qf_gradient_opts;
+
+/* `GradientEstimate` (src/gradients.rs:167-178). */
+typedef struct qf_gradient_info {
+    int32_t strategy;       /* the rule that ran (AUTO resolved) */
+    int32_t reserved;
+    uint64_t evaluations;   /* state-vector sweeps in the reference's accounting */
+} qf_gradient_info;
+
+typedef struct qf_ctx qf_ctx;  /* CudaBackend: device, stream, workspaces */
+typedef struct qf_sv qf_sv;    /* CudaDeviceState: one resident state vector */
+
+/* ---------------------------------------------------------------------------
+ * Errors and build information
+ * ------------------------------------------------------------------------- */
+
+/* Text of the last error on this thread (Display of QuantumError/CudaError,
+ * src/lib.rs:585-664, src/cuda.rs:3079-3104). Never NULL. */
+const char *qf_last_error(void);
+/* Name of a status code, e.g. "QF_ERR_QUBIT_OUT_OF_RANGE". */
+const char *qf_status_name(int status);
+/* ABI version this library was built with (QF_ABI_VERSION). */
+int qf_abi_version(void);
+
+/* ---------------------------------------------------------------------------
+ * Context — replaces CudaBackend::new (src/cuda.rs:556-790).
+ * ------------------------------------------------------------------------- */
+int qf_ctx_create(int device, qf_ctx **out);
+int qf_ctx_destroy(qf_ctx *ctx);
+/* CudaDeviceStateBatch::synchronize (src/cuda.rs:1792). */
+int qf_ctx_synchronize(qf_ctx *ctx);
+/* Raw stream handle (a cudaStream_t) of the context, for callers that order
+ * their own work after the engine's. */
+int qf_ctx_stream(qf_ctx *ctx, void **stream_out);
+
+/* ---------------------------------------------------------------------------
+ * Device state — replaces StateVector (src/lib.rs:928-1351) on the device and
+ * CudaDeviceState (src/cuda.rs:521-528, 1285-1484).
+ * ------------------------------------------------------------------------- */
+
+/* StateVector::zero_with_memory_budget (src/lib.rs:940-966): |0...0> on
+ * `qubits` qubits. `memory_budget_bytes` = 0 means no budget. */
+int qf_sv_create(qf_ctx *ctx, uint32_t qubits, int dtype, uint64_t memory_budget_bytes, qf_sv **out);
+int qf_sv_destroy(qf_sv *sv);
+int qf_sv_qubits(const qf_sv *sv, uint32_t *qubits_out);
+int qf_sv_dtype(const qf_sv *sv, int *dtype_out);
+/* Raw device pointer to the amplitudes (interleaved, dtype-typed). */
+int qf_sv_device_ptr(qf_sv *sv, void **ptr_out);
+/* Reset to |0...0>. */
+int qf_sv_set_zero(qf_sv *sv);
+/* CudaBackend::upload (src/cuda.rs:844-868): host f64 interleaved amplitudes,
+ * 2*2^qubits doubles; converted to the state's dtype on the device. */
+int qf_sv_upload(qf_sv *sv, const double *amps, uint64_t n_doubles);
+/* CudaDeviceState::download (src/cuda.rs:1459-1471): to host f64 interleaved. */
+int qf_sv_download(qf_sv *sv, double *amps_out, uint64_t n_doubles);
+/* Dtype-native host copies (f32 pairs for C64, f64 pairs for C128);
+ * `bytes` must equal the state size. Host memory may be pinned. */
+int qf_sv_upload_raw(qf_sv *sv, const void *host, uint64_t bytes);
+int qf_sv_download_raw(qf_sv *sv, void *host_out, uint64_t bytes);
+/* CudaDeviceStateBatch::copy_from_device (src/cuda.rs:1800-1817). */
+int qf_sv_copy_from(qf_sv *dst, const qf_sv *src);
+
+/* StateVector::apply (src/lib.rs:1017-1059), CudaDeviceState::apply_gate
+ * (src/cuda.rs:1296-1325). */
+int qf_sv_apply_gate(qf_sv *sv, int gate, double theta, uint32_t target);
+/* StateVector::apply_cnot / apply_cz / apply_swap (src/lib.rs:1062-1122),
+ * CudaDeviceState::apply_cnot/cz/swap (src/cuda.rs:1354-1384). */
+int qf_sv_apply_cnot(qf_sv *sv, uint32_t control, uint32_t target);
+int qf_sv_apply_cz(qf_sv *sv, uint32_t first, uint32_t second);
+int qf_sv_apply_swap(qf_sv *sv, uint32_t first, uint32_t second);
+
+/* Circuit::run (src/lib.rs:2786-2802) on a resident state, and
+ * ParameterizedCircuit::run_with_inputs (src/lib.rs:3097-3106) when the list
+ * holds ROTATION/ENCODING ops. `params`/`inputs` may be NULL when their
+ * counts are 0. `opts` may be NULL (AUTO). MEASURE/COND are rejected with
+ * QF_ERR_OPERATION_REQUIRES_SHOT_EXECUTION, CHANNEL with
+ * QF_ERR_OPERATION_REQUIRES_DENSITY_MATRIX, as in the reference. */
+int qf_sv_apply_ops(qf_sv *sv, const qf_op *ops, uint64_t n_ops,
+                    const double *params, uint64_t n_params,
+                    const double *inputs, uint64_t n_inputs,
+                    const qf_exec_opts *opts);
+
+/* StateVector::norm_sqr (src/lib.rs:998-1000), f64 accumulation. */
+int qf_sv_norm_sqr(qf_sv *sv, double *out);
+/* StateVector::probabilities (src/lib.rs:1144-1146): 2^qubits doubles to host. */
+int qf_sv_probabilities(qf_sv *sv, double *out, uint64_t n_out);
+/* StateVector::expectation_z (src/lib.rs:1149-1166) for every qubit in one
+ * HBM pass: out[q] = <Z_q>, `n_out` == qubits. */
+int qf_sv_expectation_z_all(qf_sv *sv, double *out, uint64_t n_out);
+/* StateVector::expectation (src/lib.rs:1304-1318) for X/Y/Z on one qubit. */
+int qf_sv_expectation(qf_sv *sv, int observable, uint32_t qubit, double *out);
+/* <psi|H|psi> for H = sum_t c_t P_t (PauliSum::expectation_ket,
+ * src/analytic.rs:2775). out[0] = Re, out[1] = Im. */
+int qf_sv_expectation_pauli_sum(qf_sv *sv, const qf_pauli_term *terms, uint64_t n_terms, double *out);
+/* StateVector::measure (src/lib.rs:1321-1351), CudaDeviceState::measure
+ * (src/cuda.rs:1386-1457): draws one uniform from the SmallRng whose state is
+ * *rng_state, collapses the state and returns the bit. */
+int qf_sv_measure(qf_sv *sv, uint32_t qubit, uint64_t *rng_state, uint8_t *outcome);
+
+/* ---------------------------------------------------------------------------
+ * Whole-circuit calls with host buffers.
+ * ------------------------------------------------------------------------- */
+
+/* CudaBackend::run_circuit (src/cuda.rs:1050-1083): upload `init_amps`
+ * (NULL = |0...0>), run, download into `out_amps` (NULL = no download). */
+int qf_run_circuit(qf_ctx *ctx, uint32_t qubits, int dtype,
+                   const qf_op *ops, uint64_t n_ops,
+                   const double *init_amps, double *out_amps, uint64_t n_doubles,
+                   const qf_exec_opts *opts);
+
+/* Circuit::run_shots (src/lib.rs:2822-2916) for circuits whose measurements
+ * all follow the last gate (the CLI `shots` form, src/bin/main.rs:574-602),
+ * sampled from the pre-measurement state with the reference's shot-major
+ * SmallRng stream. `outcomes` receives one packed classical register per shot
+ * (bit c = classical bit c, width <= 64); NULL skips it. `n_ties` counts
+ * decisions with |u - p_one| < tie_eps (outcomes that rounding could flip).
+ * Mid-circuit measurement or feed-forward returns QF_ERR_UNSUPPORTED_OPERATION. */
+int qf_run_shots(qf_ctx *ctx, uint32_t qubits, int dtype,
+                 const qf_op *ops, uint64_t n_ops, const double *init_amps,
+                 uint64_t shots, uint64_t seed, double tie_eps,
+                 uint64_t *outcomes, uint32_t *classical_width, uint64_t *n_ties,
+                 const qf_exec_opts *opts);
+
+/* Sampling on a resident state: measure `qubit_order[j]` into classical bit
+ * `classical_bits[j]` for j < m, for `shots` shots of the stream seeded by
+ * `seed`. Same semantics and outputs as qf_run_shots. */
+int qf_sv_sample(qf_sv *sv, const uint32_t *qubit_order, const uint32_t *classical_bits, uint32_t m,
+                 uint64_t shots, uint64_t seed, double tie_eps,
+                 uint64_t *outcomes, uint64_t *n_ties);
+
+/* ---------------------------------------------------------------------------
+ * Gradients — ParameterizedCircuit::gradient_with_inputs
+ * (src/gradients.rs:232-330), adjoint_gradient_with_inputs
+ * (src/lib.rs:3564-3704), parameter_shift_gradient_with_inputs
+ * (src/lib.rs:3516-3546), finite_difference_gradient_with_inputs
+ * (src/gradients.rs:344-375), backprop_gradient_with_inputs
+ * (src/gradients.rs:392-506).
+ *
+ * The observable is a Pauli sum; the reference's SingleQubitObservable is the
+ * one-term case. `expectation` receives <H> (may be NULL), `gradient`
+ * receives n_params values, `info` may be NULL.
+ * ------------------------------------------------------------------------- */
+int qf_gradient(qf_ctx *ctx, uint32_t qubits,
+                const qf_op *ops, uint64_t n_ops,
+                const double *params, uint64_t n_params,
+                const double *inputs, uint64_t n_inputs,
+                const qf_pauli_term *terms, uint64_t n_terms,
+                const qf_gradient_opts *opts,
+                double *expectation, double *gradient, qf_gradient_info *info);
+
+/* <H> of the circuit's output state: ParameterizedCircuit::run_with_inputs
+ * followed by the expectation (src/lib.rs:3097-3106, 3197-3226). */
+int qf_expectation(qf_ctx *ctx, uint32_t qubits, int dtype,
+                   const qf_op *ops, uint64_t n_ops,
+                   const double *params, uint64_t n_params,
+                   const double *inputs, uint64_t n_inputs,
+                   const qf_pauli_term *terms, uint64_t n_terms,
+                   const qf_exec_opts *opts, double *expectation);
+
+/* ---------------------------------------------------------------------------
+ * Plan inspection (host only, no device needed): the pass schedule the fused
+ * executor would use for a gate list. `n_passes` = HBM sweeps of the state,
+ * `n_gates` = gates after parameter binding. Used by tests and the autotuner.
+ * ------------------------------------------------------------------------- */
+int qf_plan_stats(uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops,
+                  const double *params, uint64_t n_params,
+                  const double *inputs, uint64_t n_inputs,
+                  const qf_exec_opts *opts, uint64_t *n_passes, uint64_t *n_gates);
+
+/* SmallRng::next_u64 (src/lib.rs:4898-4905) advanced `steps` times, computed
+ * by GF(2) matrix powers: the generator state from which the shot-major
+ * stream of run_shots_impl (src/lib.rs:2874-2912) draws its `steps`-th value.
+ * Host only; `state` is a SmallRng state (after SmallRng::seeded). */
+uint64_t qf_rng_jump(uint64_t state, uint64_t steps);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QF_H */

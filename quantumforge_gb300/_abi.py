@@ -1,0 +1,133 @@
+"""ctypes mirror of ``include/qf.h``: constants, record layouts and numpy dtypes.
+
+Only layouts live here; ``_native`` binds the functions.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+# status codes (QuantumError / CudaError variants)
+STATUS_NAMES = {
+    0: "Ok",
+    1: "ZeroQubits",
+    2: "MemoryBudgetExceeded",
+    3: "SimulationSizeOverflow",
+    4: "MemoryAllocationFailed",
+    5: "StateSizeNotPowerOfTwo",
+    6: "QubitOutOfRange",
+    7: "InvalidQubitPair",
+    8: "InvalidProbability",
+    9: "OperationRequiresDensityMatrix",
+    10: "OperationRequiresShotExecution",
+    11: "InvalidShotCount",
+    12: "ClassicalBitOutOfRange",
+    13: "InvalidParameterCount",
+    14: "InvalidInputCount",
+    15: "NonFiniteParameter",
+    16: "InvalidFiniteDifferenceStep",
+    17: "UnsupportedOperation",
+    18: "Timeout",
+    19: "Cuda",
+    20: "InvalidArgument",
+    21: "EmptyBatch",
+    22: "IncompatibleBatch",
+    23: "StateTooLarge",
+    24: "IncompatibleDeviceState",
+}
+STATUS_CODES = {v: k for k, v in STATUS_NAMES.items()}
+
+# enum qf_gate (order of `enum Gate`, src/lib.rs:2239-2264)
+GATE_I, GATE_X, GATE_Y, GATE_Z, GATE_H, GATE_S, GATE_SDG, GATE_T, GATE_TDG, GATE_RX, GATE_RY, GATE_RZ = range(12)
+GATE_NAMES = ["I", "X", "Y", "Z", "H", "S", "Sdg", "T", "Tdg", "Rx", "Ry", "Rz"]
+
+# enum qf_pauli1
+PAULI_X, PAULI_Y, PAULI_Z = 0, 1, 2
+
+# enum qf_op_kind
+OP_GATE, OP_CNOT, OP_CZ, OP_SWAP, OP_CHANNEL, OP_MEASURE, OP_COND, OP_ROTATION, OP_ENCODING = range(9)
+
+# enum qf_dtype
+C64, C128 = 0, 1
+
+# enum qf_exec_mode
+EXEC_AUTO, EXEC_UNFUSED, EXEC_FUSED = 0, 1, 2
+
+# enum qf_gradient_strategy
+GRAD_PARAMETER_SHIFT, GRAD_ADJOINT, GRAD_BACKPROP, GRAD_FINITE_DIFFERENCE, GRAD_AUTO = range(5)
+
+
+class Op(C.Structure):
+    _fields_ = [
+        ("kind", C.c_uint8),
+        ("gate", C.c_uint8),
+        ("flags", C.c_uint16),
+        ("q0", C.c_uint32),
+        ("q1", C.c_uint32),
+        ("param", C.c_uint32),
+        ("theta", C.c_double),
+    ]
+
+
+class PauliTerm(C.Structure):
+    _fields_ = [
+        ("xmask", C.c_uint64),
+        ("zmask", C.c_uint64),
+        ("coeff_re", C.c_double),
+        ("coeff_im", C.c_double),
+    ]
+
+
+class ExecOpts(C.Structure):
+    _fields_ = [
+        ("mode", C.c_int32),
+        ("tile_qubits", C.c_int32),
+        ("block_qubits", C.c_int32),
+        ("reserved", C.c_int32),
+    ]
+
+
+class GradientOpts(C.Structure):
+    _fields_ = [
+        ("strategy", C.c_int32),
+        ("dtype", C.c_int32),
+        ("finite_difference_step", C.c_double),
+        ("shots", C.c_uint64),
+        ("checkpoint_every", C.c_int32),
+        ("reserved", C.c_int32),
+        ("exec", ExecOpts),
+    ]
+
+
+class GradientInfo(C.Structure):
+    _fields_ = [("strategy", C.c_int32), ("reserved", C.c_int32), ("evaluations", C.c_uint64)]
+
+
+assert C.sizeof(Op) == 24, C.sizeof(Op)
+assert C.sizeof(PauliTerm) == 32
+
+OP_DTYPE = np.dtype(
+    [("kind", "u1"), ("gate", "u1"), ("flags", "<u2"), ("q0", "<u4"), ("q1", "<u4"), ("param", "<u4"), ("theta", "<f8")],
+    align=True,
+)
+TERM_DTYPE = np.dtype([("xmask", "<u8"), ("zmask", "<u8"), ("coeff_re", "<f8"), ("coeff_im", "<f8")])
+assert OP_DTYPE.itemsize == 24 and TERM_DTYPE.itemsize == 32
+
+
+def ops_array(records) -> np.ndarray:
+    """Build a contiguous ``qf_op`` array from (kind, gate, q0, q1, param, theta[, flags]) tuples."""
+    arr = np.zeros(len(records), dtype=OP_DTYPE)
+    for i, r in enumerate(records):
+        kind, gate, q0, q1, param, theta = r[:6]
+        arr[i] = (kind, gate, r[6] if len(r) > 6 else 0, q0, q1, param, theta)
+    return arr
+
+
+def terms_array(terms) -> np.ndarray:
+    """Build a ``qf_pauli_term`` array from (xmask, zmask, coeff) tuples (coeff real or complex)."""
+    arr = np.zeros(len(terms), dtype=TERM_DTYPE)
+    for i, (x, z, c) in enumerate(terms):
+        c = complex(c)
+        arr[i] = (x, z, c.real, c.imag)
+    return arr

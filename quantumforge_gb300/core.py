@@ -1,0 +1,654 @@
+"""Reference-shaped API over the GB300 engine.
+
+Names, argument meaning and errors follow the reference crate's
+``StateVector`` (src/lib.rs:928-1351), ``Gate`` (src/lib.rs:2239-2382),
+``Circuit`` (src/lib.rs:2384-2916), ``ParameterizedCircuit``
+(src/lib.rs:2919-3704, 4651-4740) and ``cuda::CudaBackend``
+(src/cuda.rs:515-1484). Every state lives in device memory; every operation
+is a call through the C ABI of include/qf.h.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _abi
+from ._native import QuantumError, check, load, ptr
+
+_DTYPES = {"c64": _abi.C64, "complex64": _abi.C64, "c128": _abi.C128, "complex128": _abi.C128,
+           _abi.C64: _abi.C64, _abi.C128: _abi.C128}
+
+
+def _dtype_code(dtype) -> int:
+    try:
+        return _DTYPES[dtype]
+    except KeyError:
+        raise QuantumError(_abi.STATUS_CODES["InvalidArgument"], f"unknown dtype {dtype!r}") from None
+
+
+# ---------------------------------------------------------------------------
+# SmallRng (src/lib.rs:4881-4911) — host generator for measure()
+# ---------------------------------------------------------------------------
+_M64 = (1 << 64) - 1
+
+
+class SmallRng:
+    """xorshift64 with a splitmix64 seed finaliser, bit-identical to the reference."""
+
+    __slots__ = ("state",)
+
+    def __init__(self, state: int):
+        self.state = state & _M64
+
+    @classmethod
+    def seeded(cls, seed: int) -> "SmallRng":
+        z = (seed + 0x9E3779B97F4A7C15) & _M64
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & _M64
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & _M64
+        z ^= z >> 31
+        return cls(z if z else 0x9E3779B97F4A7C15)
+
+    def next_u64(self) -> int:
+        x = self.state
+        x ^= (x << 13) & _M64
+        x ^= x >> 7
+        x ^= (x << 17) & _M64
+        self.state = x
+        return x
+
+    def next_f64(self) -> float:
+        return (self.next_u64() >> 11) * (1.0 / (1 << 53))
+
+
+# ---------------------------------------------------------------------------
+# Gates
+# ---------------------------------------------------------------------------
+class Gate:
+    """`enum Gate` (src/lib.rs:2239-2264): I X Y Z H S Sdg T Tdg, Rx/Ry/Rz(theta)."""
+
+    __slots__ = ("code", "theta")
+
+    def __init__(self, code: int, theta: float = 0.0):
+        self.code = int(code)
+        self.theta = float(theta)
+
+    @staticmethod
+    def Rx(theta: float) -> "Gate":
+        return Gate(_abi.GATE_RX, theta)
+
+    @staticmethod
+    def Ry(theta: float) -> "Gate":
+        return Gate(_abi.GATE_RY, theta)
+
+    @staticmethod
+    def Rz(theta: float) -> "Gate":
+        return Gate(_abi.GATE_RZ, theta)
+
+    def params(self) -> list[float]:
+        return [self.theta] if self.code >= _abi.GATE_RX else []
+
+    def matrix(self) -> np.ndarray:
+        """Gate::matrix (src/lib.rs:2267-2333) as a 2x2 complex128 array."""
+        s = 0.7071067811865476
+        c = self.code
+        t = self.theta
+        if c == _abi.GATE_RX:
+            co, si = math.cos(t * 0.5), math.sin(t * 0.5)
+            return np.array([[co, -1j * si], [-1j * si, co]])
+        if c == _abi.GATE_RY:
+            co, si = math.cos(t * 0.5), math.sin(t * 0.5)
+            return np.array([[co, -si], [si, co]], dtype=complex)
+        if c == _abi.GATE_RZ:
+            h = t * 0.5
+            return np.array([[complex(math.cos(h), -math.sin(h)), 0], [0, complex(math.cos(h), math.sin(h))]])
+        table = {
+            _abi.GATE_I: [[1, 0], [0, 1]], _abi.GATE_X: [[0, 1], [1, 0]], _abi.GATE_Y: [[0, -1j], [1j, 0]],
+            _abi.GATE_Z: [[1, 0], [0, -1]], _abi.GATE_H: [[s, s], [s, -s]], _abi.GATE_S: [[1, 0], [0, 1j]],
+            _abi.GATE_SDG: [[1, 0], [0, -1j]], _abi.GATE_T: [[1, 0], [0, complex(s, s)]],
+            _abi.GATE_TDG: [[1, 0], [0, complex(s, -s)]],
+        }
+        return np.array(table[c], dtype=complex)
+
+    def __eq__(self, other) -> bool:
+        return isinstance(other, Gate) and self.code == other.code and self.theta == other.theta
+
+    def __hash__(self) -> int:
+        return hash((self.code, self.theta))
+
+    def __repr__(self) -> str:
+        name = _abi.GATE_NAMES[self.code]
+        return f"{name}({self.theta})" if self.code >= _abi.GATE_RX else name
+
+
+for _i, _n in enumerate(_abi.GATE_NAMES[:9]):
+    setattr(Gate, _n, Gate(_i))
+
+
+class RotationAxis:
+    """`enum RotationAxis` (src/lib.rs:2919-2928)."""
+
+    X, Y, Z = _abi.PAULI_X, _abi.PAULI_Y, _abi.PAULI_Z
+
+
+class SingleQubitObservable:
+    """`enum SingleQubitObservable` (src/lib.rs:2930-2938)."""
+
+    X, Y, Z = _abi.PAULI_X, _abi.PAULI_Y, _abi.PAULI_Z
+
+
+# ---------------------------------------------------------------------------
+# Pauli sums (PauliWord / PauliSum semantics, src/analytic.rs:2547-2830)
+# ---------------------------------------------------------------------------
+class PauliSum:
+    """sum_t c_t P_t with P_t given by (x-mask, z-mask); Y = both bits set."""
+
+    def __init__(self, terms=None):
+        self.terms: list[tuple[int, int, complex]] = []
+        for t in terms or []:
+            self.add_term(*t)
+
+    def add_term(self, xmask: int, zmask: int, coeff) -> "PauliSum":
+        self.terms.append((int(xmask), int(zmask), complex(coeff)))
+        return self
+
+    def add_word(self, word: dict, coeff) -> "PauliSum":
+        """Add c * prod_q P_q for word = {qubit: 'X'|'Y'|'Z'}."""
+        x = z = 0
+        for q, p in word.items():
+            p = p.upper()
+            if p in ("X", "Y"):
+                x |= 1 << q
+            if p in ("Z", "Y"):
+                z |= 1 << q
+        return self.add_term(x, z, coeff)
+
+    @classmethod
+    def single(cls, observable: int, qubit: int) -> "PauliSum":
+        return cls().add_word({qubit: "XYZ"[observable]}, 1.0)
+
+    @classmethod
+    def tfim_ring(cls, n: int, h: float = 1.0) -> "PauliSum":
+        """-sum Z_i Z_{i+1 mod n} - h sum X_i."""
+        s = cls()
+        for i in range(n):
+            s.add_word({i: "Z", (i + 1) % n: "Z"}, -1.0)
+        for i in range(n):
+            s.add_word({i: "X"}, -h)
+        return s
+
+    @classmethod
+    def xxz_ring(cls, n: int, delta: float = 0.5) -> "PauliSum":
+        """sum (X_i X_{i+1} + Y_i Y_{i+1} + delta Z_i Z_{i+1}) on a ring."""
+        s = cls()
+        for i in range(n):
+            j = (i + 1) % n
+            s.add_word({i: "X", j: "X"}, 1.0)
+            s.add_word({i: "Y", j: "Y"}, 1.0)
+            s.add_word({i: "Z", j: "Z"}, delta)
+        return s
+
+    @classmethod
+    def maxcut(cls, edges) -> "PauliSum":
+        """sum_(u,v,w) w (1 - Z_u Z_v) / 2 — maxcut_expectation (src/qaoa_transfer.rs:199-218)."""
+        s = cls()
+        total = 0.0
+        for u, v, w in edges:
+            total += w
+            s.add_word({u: "Z", v: "Z"}, -0.5 * w)
+        s.add_term(0, 0, 0.5 * total)
+        return s
+
+    def array(self) -> np.ndarray:
+        return _abi.terms_array(self.terms)
+
+    def __len__(self) -> int:
+        return len(self.terms)
+
+
+def _as_terms(obs) -> np.ndarray:
+    if isinstance(obs, PauliSum):
+        return obs.array()
+    if isinstance(obs, np.ndarray) and obs.dtype == _abi.TERM_DTYPE:
+        return np.ascontiguousarray(obs)
+    return _abi.terms_array(list(obs))
+
+
+# ---------------------------------------------------------------------------
+# Backend / context
+# ---------------------------------------------------------------------------
+class CudaBackend:
+    """`cuda::CudaBackend::new(ordinal)` (src/cuda.rs:556-790): one device, one stream."""
+
+    def __init__(self, ordinal: int = 0):
+        lib = load()
+        h = C.c_void_p()
+        check(lib.qf_ctx_create(int(ordinal), C.byref(h)))
+        self._h = h
+        self.ordinal = ordinal
+
+    @property
+    def handle(self):
+        return self._h
+
+    def synchronize(self) -> None:
+        check(load().qf_ctx_synchronize(self._h))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            load().qf_ctx_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def device_ordinal(self) -> int:
+        return self.ordinal
+
+    # CudaBackend::upload / run_circuit / run_circuit_shots (src/cuda.rs:844, 1050, 1088)
+    def upload(self, amplitudes, dtype="c128") -> "StateVector":
+        return StateVector.from_amplitudes(amplitudes, dtype=dtype, backend=self)
+
+    def run_circuit(self, state: "StateVector | np.ndarray", circuit: "Circuit", dtype="c128", exec_opts=None) -> np.ndarray:
+        amps = state.amplitudes() if isinstance(state, StateVector) else np.asarray(state, dtype=np.complex128)
+        n = int(round(math.log2(amps.size)))
+        ops = circuit.ops()
+        src = np.ascontiguousarray(amps, dtype=np.complex128).view(np.float64)
+        out = np.empty(2 * amps.size, dtype=np.float64)
+        check(load().qf_run_circuit(self._h, n, _dtype_code(dtype), ptr(ops), len(ops), ptr(src), ptr(out), out.size,
+                                    _exec(exec_opts)))
+        return out.view(np.complex128)
+
+    def run_circuit_shots(self, initial_state, circuit: "Circuit", shots: int, seed: int, dtype="c128",
+                          tie_eps: float = 0.0) -> "ShotResult":
+        return circuit.run_shots(initial_state, shots, seed, dtype=dtype, backend=self, tie_eps=tie_eps)
+
+
+_default_backend: CudaBackend | None = None
+
+
+def default_backend() -> CudaBackend:
+    global _default_backend
+    if _default_backend is None:
+        _default_backend = CudaBackend(0)
+    return _default_backend
+
+
+def _exec(opts):
+    if opts is None:
+        return None
+    if isinstance(opts, _abi.ExecOpts):
+        return C.byref(opts)
+    mode = {"auto": _abi.EXEC_AUTO, "unfused": _abi.EXEC_UNFUSED, "fused": _abi.EXEC_FUSED}
+    o = _abi.ExecOpts(mode[opts.get("mode", "auto")], int(opts.get("tile_qubits", 0)), int(opts.get("block_qubits", 0)), 0)
+    return C.byref(o)
+
+
+# ---------------------------------------------------------------------------
+# StateVector (device resident)
+# ---------------------------------------------------------------------------
+class StateVector:
+    """A state vector resident in GPU memory (StateVector + CudaDeviceState)."""
+
+    def __init__(self, handle, qubits: int, dtype: int, backend: CudaBackend):
+        self._h = handle
+        self.qubits = qubits
+        self.dtype = dtype
+        self.backend = backend
+
+    @classmethod
+    def zero(cls, qubits: int, dtype="c128", memory_budget: int | None = None, backend: CudaBackend | None = None):
+        """StateVector::zero / zero_with_memory_budget (src/lib.rs:930-966)."""
+        backend = backend or default_backend()
+        h = C.c_void_p()
+        check(load().qf_sv_create(backend.handle, int(qubits), _dtype_code(dtype), int(memory_budget or 0), C.byref(h)))
+        return cls(h, int(qubits), _dtype_code(dtype), backend)
+
+    zero_with_memory_budget = zero
+
+    @classmethod
+    def from_amplitudes(cls, amplitudes, dtype="c128", backend: CudaBackend | None = None):
+        """StateVector::from_amplitudes (src/lib.rs:969-978)."""
+        a = np.ascontiguousarray(np.asarray(amplitudes, dtype=np.complex128))
+        if a.size < 2:
+            raise QuantumError(_abi.STATUS_CODES["ZeroQubits"], "a state vector must contain at least one qubit")
+        if a.size & (a.size - 1):
+            raise QuantumError(_abi.STATUS_CODES["StateSizeNotPowerOfTwo"], f"state vector length {a.size} is not a power of two")
+        sv = cls.zero(a.size.bit_length() - 1, dtype=dtype, backend=backend)
+        check(load().qf_sv_upload(sv._h, ptr(a.view(np.float64)), 2 * a.size))
+        return sv
+
+    def __del__(self):
+        try:
+            if self._h and self._h.value:
+                load().qf_sv_destroy(self._h)
+                self._h = C.c_void_p()
+        except Exception:
+            pass
+
+    def num_qubits(self) -> int:
+        return self.qubits
+
+    def copy(self) -> "StateVector":
+        other = StateVector.zero(self.qubits, dtype=self.dtype, backend=self.backend)
+        check(load().qf_sv_copy_from(other._h, self._h))
+        return other
+
+    def amplitudes(self) -> np.ndarray:
+        """Download as complex128 (CudaDeviceState::download, src/cuda.rs:1459-1471)."""
+        out = np.empty(2 << self.qubits, dtype=np.float64)
+        check(load().qf_sv_download(self._h, ptr(out), out.size))
+        return out.view(np.complex128)
+
+    # gates (src/lib.rs:1017-1122)
+    def apply(self, gate: Gate, qubit: int) -> "StateVector":
+        check(load().qf_sv_apply_gate(self._h, gate.code, gate.theta, int(qubit)))
+        return self
+
+    def apply_cnot(self, control: int, target: int) -> "StateVector":
+        check(load().qf_sv_apply_cnot(self._h, int(control), int(target)))
+        return self
+
+    def apply_cz(self, first: int, second: int) -> "StateVector":
+        check(load().qf_sv_apply_cz(self._h, int(first), int(second)))
+        return self
+
+    def apply_swap(self, first: int, second: int) -> "StateVector":
+        check(load().qf_sv_apply_swap(self._h, int(first), int(second)))
+        return self
+
+    def apply_ops(self, ops: np.ndarray, params=None, inputs=None, exec_opts=None) -> "StateVector":
+        p = None if params is None else np.ascontiguousarray(params, dtype=np.float64)
+        i = None if inputs is None else np.ascontiguousarray(inputs, dtype=np.float64)
+        check(load().qf_sv_apply_ops(self._h, ptr(ops), len(ops), ptr(p), 0 if p is None else p.size, ptr(i),
+                                     0 if i is None else i.size, _exec(exec_opts)))
+        return self
+
+    # reductions (src/lib.rs:998-1166, 1278-1318)
+    def norm_sqr(self) -> float:
+        v = C.c_double()
+        check(load().qf_sv_norm_sqr(self._h, C.byref(v)))
+        return v.value
+
+    def probabilities(self) -> np.ndarray:
+        out = np.empty(1 << self.qubits, dtype=np.float64)
+        check(load().qf_sv_probabilities(self._h, ptr(out), out.size))
+        return out
+
+    def expectation_z_all(self) -> np.ndarray:
+        out = np.empty(self.qubits, dtype=np.float64)
+        check(load().qf_sv_expectation_z_all(self._h, ptr(out), out.size))
+        return out
+
+    def expectation(self, observable: int, qubit: int) -> float:
+        v = C.c_double()
+        check(load().qf_sv_expectation(self._h, int(observable), int(qubit), C.byref(v)))
+        return v.value
+
+    def expectation_x(self, qubit: int) -> float:
+        return self.expectation(SingleQubitObservable.X, qubit)
+
+    def expectation_y(self, qubit: int) -> float:
+        return self.expectation(SingleQubitObservable.Y, qubit)
+
+    def expectation_z(self, qubit: int) -> float:
+        return self.expectation(SingleQubitObservable.Z, qubit)
+
+    def expectation_pauli_sum(self, hamiltonian) -> complex:
+        t = _as_terms(hamiltonian)
+        out = np.zeros(2, dtype=np.float64)
+        check(load().qf_sv_expectation_pauli_sum(self._h, ptr(t), len(t), ptr(out)))
+        return complex(out[0], out[1])
+
+    def measure(self, qubit: int, rng: SmallRng) -> int:
+        """StateVector::measure (src/lib.rs:1321-1351), advancing `rng`."""
+        st = C.c_uint64(rng.state)
+        o = C.c_uint8()
+        status = load().qf_sv_measure(self._h, int(qubit), C.byref(st), C.byref(o))
+        rng.state = st.value
+        check(status)
+        return int(o.value)
+
+    def sample(self, qubit_order, classical_bits, shots: int, seed: int, tie_eps: float = 0.0):
+        """Terminal measurements of a resident state: (packed outcomes, ties)."""
+        q = np.ascontiguousarray(qubit_order, dtype=np.uint32)
+        cb = np.ascontiguousarray(classical_bits, dtype=np.uint32)
+        out = np.empty(int(shots), dtype=np.uint64)
+        ties = C.c_uint64()
+        check(load().qf_sv_sample(self._h, ptr(q), ptr(cb), len(q), int(shots), int(seed), float(tie_eps), ptr(out),
+                                  C.byref(ties)))
+        return out, ties.value
+
+
+# ---------------------------------------------------------------------------
+# Circuits
+# ---------------------------------------------------------------------------
+@dataclass
+class ShotResult:
+    """`ShotResult` (src/lib.rs:2453-2464): counts keyed by LSB-first bit tuples."""
+
+    shots: int
+    counts: dict
+    ties: int = 0
+
+    @staticmethod
+    def from_packed(packed: np.ndarray, width: int, ties: int = 0) -> "ShotResult":
+        vals, cnts = np.unique(packed, return_counts=True)
+        counts = {tuple(int((int(v) >> b) & 1) for b in range(width)): int(c) for v, c in zip(vals, cnts)}
+        return ShotResult(int(packed.size), dict(sorted(counts.items())), ties)
+
+
+class Circuit:
+    """`Circuit` (src/lib.rs:2517-2916): an op list executed on a device state."""
+
+    def __init__(self):
+        self.operations: list[tuple] = []
+
+    @classmethod
+    def from_ops(cls, ops: np.ndarray) -> "Circuit":
+        """A circuit from a ``qf_op`` record array."""
+        c = cls()
+        for r in ops:
+            c.operations.append((int(r["kind"]), int(r["gate"]), int(r["q0"]), int(r["q1"]), int(r["param"]),
+                                 float(r["theta"]), int(r["flags"])))
+        return c
+
+    def push(self, gate: Gate, target: int) -> None:
+        self.operations.append((_abi.OP_GATE, gate.code, int(target), 0, 0, gate.theta))
+
+    def cnot(self, control: int, target: int) -> None:
+        self.operations.append((_abi.OP_CNOT, 0, int(control), int(target), 0, 0.0))
+
+    def cz(self, first: int, second: int) -> None:
+        self.operations.append((_abi.OP_CZ, 0, int(first), int(second), 0, 0.0))
+
+    def swap(self, first: int, second: int) -> None:
+        self.operations.append((_abi.OP_SWAP, 0, int(first), int(second), 0, 0.0))
+
+    def channel(self, target: int, channel=None) -> None:
+        self.operations.append((_abi.OP_CHANNEL, 0, int(target), 0, 0, 0.0))
+
+    def measure(self, target: int, classical_bit: int) -> None:
+        self.operations.append((_abi.OP_MEASURE, 0, int(target), 0, int(classical_bit), 0.0))
+
+    def if_classical_bit(self, classical_bit: int, value: int, gate: Gate, target: int) -> None:
+        self.operations.append((_abi.OP_COND, gate.code, int(target), 0, int(classical_bit), gate.theta, int(value) & 1))
+
+    def has_measurements(self) -> bool:
+        return any(op[0] == _abi.OP_MEASURE for op in self.operations)
+
+    def num_qubits(self) -> int:
+        m = -1
+        for op in self.operations:
+            m = max(m, op[2])
+            if op[0] in (_abi.OP_CNOT, _abi.OP_CZ, _abi.OP_SWAP):
+                m = max(m, op[3])
+        return m + 1
+
+    def ops(self) -> np.ndarray:
+        return _abi.ops_array(self.operations)
+
+    def run(self, state: StateVector, exec_opts=None) -> StateVector:
+        """Circuit::run (src/lib.rs:2786-2802), in place on the device state."""
+        return state.apply_ops(self.ops(), exec_opts=exec_opts)
+
+    def run_shots(self, initial_state, shots: int, seed: int, dtype="c128", backend: CudaBackend | None = None,
+                  tie_eps: float = 0.0, exec_opts=None) -> ShotResult:
+        """Circuit::run_shots (src/lib.rs:2822-2916) for terminal measurements."""
+        backend = backend or default_backend()
+        if isinstance(initial_state, StateVector):
+            amps = initial_state.amplitudes()
+        elif isinstance(initial_state, int):
+            amps = np.zeros(1 << initial_state, dtype=np.complex128)
+            amps[0] = 1
+        else:
+            amps = np.asarray(initial_state, dtype=np.complex128)
+        n = amps.size.bit_length() - 1
+        ops = self.ops()
+        src = np.ascontiguousarray(amps).view(np.float64)
+        out = np.empty(max(int(shots), 1), dtype=np.uint64)
+        width = C.c_uint32()
+        ties = C.c_uint64()
+        check(load().qf_run_shots(backend.handle, n, _dtype_code(dtype), ptr(ops), len(ops), ptr(src), int(shots), int(seed),
+                                  float(tie_eps), ptr(out), C.byref(width), C.byref(ties), _exec(exec_opts)))
+        return ShotResult.from_packed(out[: int(shots)], width.value, ties.value)
+
+
+class ParameterizedCircuit:
+    """`ParameterizedCircuit` (src/lib.rs:3008-3121, 3480-3704, 4651-4740)."""
+
+    def __init__(self, parameter_count: int, input_count: int = 0):
+        self.parameter_count_ = int(parameter_count)
+        self.input_count_ = int(input_count)
+        self.operations: list[tuple] = []
+
+    @classmethod
+    def new(cls, parameter_count: int) -> "ParameterizedCircuit":
+        return cls(parameter_count)
+
+    @classmethod
+    def with_inputs(cls, parameter_count: int, input_count: int) -> "ParameterizedCircuit":
+        return cls(parameter_count, input_count)
+
+    def parameter_count(self) -> int:
+        return self.parameter_count_
+
+    def input_count(self) -> int:
+        return self.input_count_
+
+    def push(self, gate: Gate, target: int) -> None:
+        self.operations.append((_abi.OP_GATE, gate.code, int(target), 0, 0, gate.theta))
+
+    def rotation(self, axis: int, target: int, parameter: int) -> None:
+        self.operations.append((_abi.OP_ROTATION, int(axis), int(target), 0, int(parameter), 0.0))
+
+    def encode_rotation(self, axis: int, target: int, input: int) -> None:  # noqa: A002 - reference name
+        self.operations.append((_abi.OP_ENCODING, int(axis), int(target), 0, int(input), 0.0))
+
+    def cnot(self, control: int, target: int) -> None:
+        self.operations.append((_abi.OP_CNOT, 0, int(control), int(target), 0, 0.0))
+
+    def cz(self, first: int, second: int) -> None:
+        self.operations.append((_abi.OP_CZ, 0, int(first), int(second), 0, 0.0))
+
+    def swap(self, first: int, second: int) -> None:
+        self.operations.append((_abi.OP_SWAP, 0, int(first), int(second), 0, 0.0))
+
+    def channel(self, target: int, channel=None) -> None:
+        self.operations.append((_abi.OP_CHANNEL, 0, int(target), 0, 0, 0.0))
+
+    def ops(self) -> np.ndarray:
+        return _abi.ops_array(self.operations)
+
+    # validate_parameters / validate_inputs (src/lib.rs:4651-4675)
+    def _values(self, inputs, parameters):
+        p = np.ascontiguousarray(parameters, dtype=np.float64).reshape(-1)
+        i = np.ascontiguousarray(inputs if inputs is not None else [], dtype=np.float64).reshape(-1)
+        if i.size != self.input_count_:
+            raise QuantumError(_abi.STATUS_CODES["InvalidInputCount"],
+                               f"expected {self.input_count_} encoded inputs, got {i.size}")
+        if not np.all(np.isfinite(i)):
+            raise QuantumError(_abi.STATUS_CODES["NonFiniteParameter"], "circuit parameters must be finite")
+        if p.size != self.parameter_count_:
+            raise QuantumError(_abi.STATUS_CODES["InvalidParameterCount"],
+                               f"expected {self.parameter_count_} circuit parameters, got {p.size}")
+        if not np.all(np.isfinite(p)):
+            raise QuantumError(_abi.STATUS_CODES["NonFiniteParameter"], "circuit parameters must be finite")
+        return i, p
+
+    def run_with_inputs(self, inputs, parameters, qubits: int, dtype="c128", backend=None, exec_opts=None) -> StateVector:
+        i, p = self._values(inputs, parameters)
+        sv = StateVector.zero(qubits, dtype=dtype, backend=backend)
+        return sv.apply_ops(self.ops(), params=p, inputs=i, exec_opts=exec_opts)
+
+    def run(self, parameters, qubits: int, dtype="c128", backend=None, exec_opts=None) -> StateVector:
+        return self.run_with_inputs([], parameters, qubits, dtype=dtype, backend=backend, exec_opts=exec_opts)
+
+    def expectation_pauli_sum(self, parameters, qubits: int, hamiltonian, inputs=None, dtype="c128", backend=None,
+                              exec_opts=None) -> float:
+        i, p = self._values(inputs, parameters)
+        backend = backend or default_backend()
+        t = _as_terms(hamiltonian)
+        ops = self.ops()
+        v = C.c_double()
+        check(load().qf_expectation(backend.handle, int(qubits), _dtype_code(dtype), ptr(ops), len(ops), ptr(p), p.size,
+                                    ptr(i), i.size, ptr(t), len(t), _exec(exec_opts), C.byref(v)))
+        return v.value
+
+    # gradients: thin wrappers over gradients.gradient_with_inputs
+    def circuit_profile(self):
+        from .gradients import CircuitProfile
+
+        prof = CircuitProfile(operations=len(self.operations), parameters=self.parameter_count_)
+        for op in self.operations:
+            if op[0] == _abi.OP_ROTATION:
+                prof.parameterized_operations += 1
+            elif op[0] == _abi.OP_CHANNEL:
+                prof.has_channel = True
+        return prof
+
+    def gradient_with_inputs(self, options, inputs, parameters, qubits, observable, observable_qubit, **kw):
+        from .gradients import gradient_with_inputs
+
+        return gradient_with_inputs(self, options, inputs, parameters, qubits,
+                                    PauliSum.single(observable, observable_qubit), **kw)
+
+    def gradient(self, options, parameters, qubits, observable, observable_qubit, **kw):
+        return self.gradient_with_inputs(options, [], parameters, qubits, observable, observable_qubit, **kw)
+
+    def gradient_auto(self, parameters, qubits, observable, observable_qubit, **kw):
+        from .gradients import GradientOptions
+
+        return self.gradient(GradientOptions(), parameters, qubits, observable, observable_qubit, **kw)
+
+    def _strategy_grad(self, strategy, inputs, parameters, qubits, observable, q, **kw):
+        from .gradients import GradientOptions
+
+        return self.gradient_with_inputs(GradientOptions(strategy=strategy), inputs, parameters, qubits, observable, q,
+                                         **kw).gradient
+
+    def parameter_shift_gradient_with_inputs(self, inputs, parameters, qubits, observable, observable_qubit, **kw):
+        from .gradients import GradientStrategy
+
+        return self._strategy_grad(GradientStrategy.ParameterShift, inputs, parameters, qubits, observable,
+                                   observable_qubit, **kw)
+
+    def parameter_shift_gradient_for(self, parameters, qubits, observable, observable_qubit, **kw):
+        return self.parameter_shift_gradient_with_inputs([], parameters, qubits, observable, observable_qubit, **kw)
+
+    def parameter_shift_gradient(self, parameters, qubits, observable_qubit, **kw):
+        return self.parameter_shift_gradient_for(parameters, qubits, SingleQubitObservable.Z, observable_qubit, **kw)
+
+    def adjoint_gradient_with_inputs(self, inputs, parameters, qubits, observable, observable_qubit, **kw):
+        from .gradients import GradientStrategy
+
+        return self._strategy_grad(GradientStrategy.Adjoint, inputs, parameters, qubits, observable, observable_qubit,
+                                   **kw)
+
+    def adjoint_gradient(self, parameters, qubits, observable, observable_qubit, **kw):
+        return self.adjoint_gradient_with_inputs([], parameters, qubits, observable, observable_qubit, **kw)

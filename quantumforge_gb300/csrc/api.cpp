@@ -1,0 +1,761 @@
+// api.cpp — the extern "C" boundary declared in include/qf.h. Validation and
+// error texts follow the reference's QuantumError / CudaError
+// (src/lib.rs:507-664, src/cuda.rs:3051-3104); all checks run before any
+// launch, and the device state is left untouched when a call is rejected.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "qf_internal.h"
+
+namespace qf {
+
+static thread_local std::string g_last_error = "";
+
+int fail(int status, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return status;
+}
+
+void clear_error() { g_last_error.clear(); }
+
+int cuda_fail(cudaError_t e, const char *what) {
+    return fail(QF_ERR_CUDA, "CUDA error %d (%s): %s in %s", (int)e, cudaGetErrorName(e), cudaGetErrorString(e), what);
+}
+
+int ensure_device(void **ptr, size_t *bytes, size_t need) {
+    if (*bytes >= need && *ptr) return QF_OK;
+    if (*ptr) {
+        cudaError_t e = cudaFree(*ptr);
+        *ptr = nullptr;
+        *bytes = 0;
+        if (e != cudaSuccess) return cuda_fail(e, "cudaFree(workspace)");
+    }
+    size_t want = std::max<size_t>(need, 1 << 16);
+    cudaError_t e = cudaMalloc(ptr, want);
+    if (e != cudaSuccess) {
+        *ptr = nullptr;
+        cudaGetLastError();
+        return fail(QF_ERR_MEMORY_ALLOCATION_FAILED, "could not reserve %zu bytes of device workspace", want);
+    }
+    *bytes = want;
+    return QF_OK;
+}
+
+int ensure_pinned(void **ptr, size_t *bytes, size_t need) {
+    if (*bytes >= need && *ptr) return QF_OK;
+    if (*ptr) cudaFreeHost(*ptr);
+    *ptr = nullptr;
+    *bytes = 0;
+    if (cudaMallocHost(ptr, need) != cudaSuccess) {
+        cudaGetLastError();
+        *ptr = nullptr;
+        return fail(QF_ERR_MEMORY_ALLOCATION_FAILED, "could not reserve %zu bytes of pinned host memory", need);
+    }
+    *bytes = need;
+    return QF_OK;
+}
+
+}  // namespace qf
+
+using namespace qf;
+
+namespace {
+
+int bind_device(qf_ctx *ctx) {
+    QF_CUDA(cudaSetDevice(ctx->device));
+    return QF_OK;
+}
+
+int check_sv(const qf_sv *sv) {
+    if (!sv || !sv->ctx || !sv->d) return fail(QF_ERR_INVALID_ARGUMENT, "state handle is NULL or released");
+    return QF_OK;
+}
+
+int check_dtype(int dtype) {
+    if (dtype != QF_C64 && dtype != QF_C128) return fail(QF_ERR_INVALID_ARGUMENT, "unknown dtype %d", dtype);
+    return QF_OK;
+}
+
+// StateVector::zero_with_memory_budget size checks (src/lib.rs:940-966).
+int alloc_state(qf_ctx *ctx, uint32_t qubits, int dtype, uint64_t budget, qf_sv **out) {
+    QF_TRY(check_dtype(dtype));
+    if (qubits == 0) return fail(QF_ERR_ZERO_QUBITS, "a state vector must contain at least one qubit");
+    if (qubits > 40) return fail(QF_ERR_SIMULATION_SIZE_OVERFLOW, "dense simulation size exceeds the supported addressable range");
+    const uint64_t dim = 1ULL << qubits;
+    const uint64_t bytes = dim * (dtype == QF_C64 ? 8ULL : 16ULL);
+    if (budget && bytes > budget)
+        return fail(QF_ERR_MEMORY_BUDGET_EXCEEDED, "dense state needs at least %llu bytes, exceeding the %llu-byte memory budget",
+                    (unsigned long long)bytes, (unsigned long long)budget);
+    qf_sv *sv = new qf_sv();
+    sv->ctx = ctx;
+    sv->n = qubits;
+    sv->dtype = dtype;
+    sv->dim = dim;
+    cudaError_t e = cudaMalloc(&sv->d, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        delete sv;
+        return fail(QF_ERR_MEMORY_ALLOCATION_FAILED, "could not reserve memory for the dense quantum state (%llu bytes)",
+                    (unsigned long long)bytes);
+    }
+    int st = fill_zero_state(sv);
+    if (st) {
+        cudaFree(sv->d);
+        delete sv;
+        return st;
+    }
+    *out = sv;
+    return QF_OK;
+}
+
+void free_state(qf_sv *sv) {
+    if (!sv) return;
+    if (sv->d) cudaFree(sv->d);
+    delete sv;
+}
+
+// A cached context-owned state of the requested shape (whole-circuit calls).
+int scratch_state(qf_ctx *ctx, qf_sv **slot, uint32_t n, int dtype, qf_sv **out) {
+    if (*slot && ((*slot)->n != n || (*slot)->dtype != dtype)) {
+        free_state(*slot);
+        *slot = nullptr;
+    }
+    if (!*slot) QF_TRY(alloc_state(ctx, n, dtype, 0, slot));
+    *out = *slot;
+    return QF_OK;
+}
+
+uint64_t classical_bit_check(const qf_op *ops, uint64_t n_ops, int *status) {
+    uint64_t width = 0;
+    *status = QF_OK;
+    for (uint64_t k = 0; k < n_ops; ++k)
+        if (ops[k].kind == QF_OP_MEASURE || ops[k].kind == QF_OP_COND) {
+            if (ops[k].param >= 4096) {
+                *status = fail(QF_ERR_CLASSICAL_BIT_OUT_OF_RANGE, "classical bit index %u exceeds the supported maximum of 4095",
+                               ops[k].param);
+                return 0;
+            }
+            width = std::max<uint64_t>(width, (uint64_t)ops[k].param + 1);
+        }
+    return width;
+}
+
+uint64_t count_rotations(const qf_op *ops, uint64_t n_ops) {
+    uint64_t c = 0;
+    for (uint64_t k = 0; k < n_ops; ++k) c += ops[k].kind == QF_OP_ROTATION;
+    return c;
+}
+
+bool has_channel(const qf_op *ops, uint64_t n_ops) {
+    for (uint64_t k = 0; k < n_ops; ++k)
+        if (ops[k].kind == QF_OP_CHANNEL) return true;
+    return false;
+}
+
+int check_terms_real(const qf_pauli_term *terms, uint64_t n_terms) {
+    if (n_terms && !terms) return fail(QF_ERR_INVALID_ARGUMENT, "terms is NULL");
+    for (uint64_t t = 0; t < n_terms; ++t) {
+        if (!std::isfinite(terms[t].coeff_re) || !std::isfinite(terms[t].coeff_im))
+            return fail(QF_ERR_NON_FINITE_PARAMETER, "observable coefficients must be finite");
+        if (terms[t].coeff_im != 0.0)
+            return fail(QF_ERR_INVALID_ARGUMENT, "gradient observables must be Hermitian (real coefficients)");
+    }
+    return QF_OK;
+}
+
+// Forward circuit + expectation on the context's scratch state.
+int forward_expectation(qf_ctx *ctx, uint32_t n, int dtype, const qf_op *ops, uint64_t n_ops, const double *params,
+                        uint64_t n_params, const double *inputs, uint64_t n_inputs, int64_t shift_op, double shift,
+                        const qf_pauli_term *terms, uint64_t n_terms, const qf_exec_opts *exec, double *e) {
+    std::vector<BGate> gates;
+    QF_TRY(bind_ops(n, ops, n_ops, params, n_params, inputs, n_inputs, shift_op, shift, gates));
+    qf_sv *sv;
+    QF_TRY(scratch_state(ctx, &ctx->scratch_sv, n, dtype, &sv));
+    QF_TRY(fill_zero_state(sv));
+    QF_TRY(execute_gates(sv, gates, exec));
+    double out[2];
+    QF_TRY(pauli_expectation(sv, terms, n_terms, out));
+    *e = out[0];
+    return QF_OK;
+}
+
+// Adjoint gradient on the device (the method of adjoint_gradient_with_inputs,
+// src/lib.rs:3564-3704, with O(2^n) memory): forward psi with optional
+// checkpoints at segment starts, lambda = H psi, then each segment backwards
+// in tile passes that carry psi and lambda together, accumulate
+// Im<lambda|P_k psi> per rotation occurrence in f64 and apply U_k^dagger to
+// both. With checkpoints, psi is restored from the stored forward state at
+// every segment boundary instead of carrying the uncompute drift further.
+int adjoint_device(qf_ctx *ctx, uint32_t n, const std::vector<BGate> &gates, const qf_pauli_term *terms, uint64_t n_terms,
+                   const qf_gradient_opts *o, uint64_t n_params, double *energy, double *grad) {
+    const int dtype = o->dtype;
+    const int every = std::max(0, o->checkpoint_every);
+    // segment boundaries by op index in the bound list
+    std::vector<size_t> seg_begin;
+    if (every > 0) {
+        for (size_t s = 0; s < gates.size(); s += (size_t)every) seg_begin.push_back(s);
+    } else {
+        seg_begin.push_back(0);
+    }
+    if (gates.empty()) seg_begin.assign(1, 0);
+    const size_t n_seg = seg_begin.size();
+    qf_sv *psi, *lam;
+    QF_TRY(scratch_state(ctx, &ctx->scratch_sv, n, dtype, &psi));
+    QF_TRY(scratch_state(ctx, &ctx->scratch_sv2, n, dtype, &lam));
+    std::vector<qf_sv *> ckpt;  // ckpt[s] = psi at the start of segment s+1
+    struct Guard {
+        std::vector<qf_sv *> *v;
+        ~Guard() {
+            for (qf_sv *s : *v) free_state(s);
+        }
+    } guard{&ckpt};
+    PlanOpts po;
+    default_tiling(n, dtype, o->exec.tile_qubits, &po.tile_qubits, &po.low_qubits);
+    QF_TRY(fill_zero_state(psi));
+    for (size_t s = 0; s < n_seg; ++s) {
+        const size_t b = seg_begin[s], e = s + 1 < n_seg ? seg_begin[s + 1] : gates.size();
+        std::vector<BGate> seg(gates.begin() + b, gates.begin() + e);
+        Plan plan;
+        po.backward = false;
+        QF_TRY(plan_passes(n, seg, po, plan));
+        QF_TRY(run_plan(psi, plan));
+        if (s + 1 < n_seg) {
+            qf_sv *c;
+            QF_TRY(alloc_state(ctx, n, dtype, 0, &c));
+            ckpt.push_back(c);
+            QF_CUDA(cudaMemcpyAsync(c->d, psi->d, psi->bytes(), cudaMemcpyDeviceToDevice, ctx->stream));
+        }
+    }
+    double e_val = 0.0;
+    QF_TRY(pauli_apply(psi, lam, terms, n_terms, &e_val));
+    if (energy) *energy = e_val;
+    std::vector<double> g(n_params, 0.0);
+    for (size_t s = n_seg; s-- > 0;) {
+        const size_t b = seg_begin[s], e = s + 1 < n_seg ? seg_begin[s + 1] : gates.size();
+        std::vector<BGate> seg(gates.begin() + b, gates.begin() + e);
+        Plan plan;
+        po.backward = true;
+        po.merge_1q = true;
+        QF_TRY(plan_passes(n, seg, po, plan));
+        if (plan.n_slots) {
+            double *d_sums;
+            const size_t bytes = sizeof(double) * plan.n_slots;
+            if (bytes > kSmallBytes) QF_TRY(ensure_device(&ctx->ws_tree, &ctx->ws_tree_bytes, bytes));
+            d_sums = bytes > kSmallBytes ? static_cast<double *>(ctx->ws_tree) : ctx->d_small;
+            QF_CUDA(cudaMemsetAsync(d_sums, 0, bytes, ctx->stream));
+            QF_TRY(run_plan_dual(psi, lam, plan, d_sums));
+            std::vector<double> sums(plan.n_slots);
+            QF_CUDA(cudaMemcpyAsync(sums.data(), d_sums, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+            QF_CUDA(cudaStreamSynchronize(ctx->stream));
+            for (uint32_t k = 0; k < plan.n_slots; ++k) g[(size_t)plan.slot_param[k]] += sums[k];
+        } else {
+            QF_TRY(run_plan_dual(psi, lam, plan, nullptr));
+        }
+        if (s > 0 && !ckpt.empty())
+            QF_CUDA(cudaMemcpyAsync(psi->d, ckpt[s - 1]->d, psi->bytes(), cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    QF_CUDA(cudaStreamSynchronize(ctx->stream));
+    std::copy(g.begin(), g.end(), grad);
+    return QF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *qf_last_error(void) { return g_last_error.c_str(); }
+
+const char *qf_status_name(int status) {
+    switch (status) {
+    case QF_OK: return "QF_OK";
+    case QF_ERR_ZERO_QUBITS: return "QF_ERR_ZERO_QUBITS";
+    case QF_ERR_MEMORY_BUDGET_EXCEEDED: return "QF_ERR_MEMORY_BUDGET_EXCEEDED";
+    case QF_ERR_SIMULATION_SIZE_OVERFLOW: return "QF_ERR_SIMULATION_SIZE_OVERFLOW";
+    case QF_ERR_MEMORY_ALLOCATION_FAILED: return "QF_ERR_MEMORY_ALLOCATION_FAILED";
+    case QF_ERR_STATE_SIZE_NOT_POWER_OF_TWO: return "QF_ERR_STATE_SIZE_NOT_POWER_OF_TWO";
+    case QF_ERR_QUBIT_OUT_OF_RANGE: return "QF_ERR_QUBIT_OUT_OF_RANGE";
+    case QF_ERR_INVALID_QUBIT_PAIR: return "QF_ERR_INVALID_QUBIT_PAIR";
+    case QF_ERR_INVALID_PROBABILITY: return "QF_ERR_INVALID_PROBABILITY";
+    case QF_ERR_OPERATION_REQUIRES_DENSITY_MATRIX: return "QF_ERR_OPERATION_REQUIRES_DENSITY_MATRIX";
+    case QF_ERR_OPERATION_REQUIRES_SHOT_EXECUTION: return "QF_ERR_OPERATION_REQUIRES_SHOT_EXECUTION";
+    case QF_ERR_INVALID_SHOT_COUNT: return "QF_ERR_INVALID_SHOT_COUNT";
+    case QF_ERR_CLASSICAL_BIT_OUT_OF_RANGE: return "QF_ERR_CLASSICAL_BIT_OUT_OF_RANGE";
+    case QF_ERR_INVALID_PARAMETER_COUNT: return "QF_ERR_INVALID_PARAMETER_COUNT";
+    case QF_ERR_INVALID_INPUT_COUNT: return "QF_ERR_INVALID_INPUT_COUNT";
+    case QF_ERR_NON_FINITE_PARAMETER: return "QF_ERR_NON_FINITE_PARAMETER";
+    case QF_ERR_INVALID_FINITE_DIFFERENCE_STEP: return "QF_ERR_INVALID_FINITE_DIFFERENCE_STEP";
+    case QF_ERR_UNSUPPORTED_OPERATION: return "QF_ERR_UNSUPPORTED_OPERATION";
+    case QF_ERR_TIMEOUT: return "QF_ERR_TIMEOUT";
+    case QF_ERR_CUDA: return "QF_ERR_CUDA";
+    case QF_ERR_INVALID_ARGUMENT: return "QF_ERR_INVALID_ARGUMENT";
+    case QF_ERR_EMPTY_BATCH: return "QF_ERR_EMPTY_BATCH";
+    case QF_ERR_INCOMPATIBLE_BATCH: return "QF_ERR_INCOMPATIBLE_BATCH";
+    case QF_ERR_STATE_TOO_LARGE: return "QF_ERR_STATE_TOO_LARGE";
+    case QF_ERR_INCOMPATIBLE_DEVICE_STATE: return "QF_ERR_INCOMPATIBLE_DEVICE_STATE";
+    default: return "QF_ERR_UNKNOWN";
+    }
+}
+
+int qf_abi_version(void) { return QF_ABI_VERSION; }
+
+int qf_ctx_create(int device, qf_ctx **out) {
+    clear_error();
+    if (!out) return fail(QF_ERR_INVALID_ARGUMENT, "out is NULL");
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceCount");
+    if (device < 0 || device >= count) return fail(QF_ERR_CUDA, "CUDA device %d does not exist (%d visible)", device, count);
+    QF_CUDA(cudaSetDevice(device));
+    qf_ctx *ctx = new qf_ctx();
+    ctx->device = device;
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device);
+    ctx->sm_count = v;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    ctx->smem_optin = (size_t)v;
+    if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaMalloc(&ctx->d_small, kSmallBytes)) != cudaSuccess ||
+        (e = cudaMallocHost(&ctx->h_small, kSmallBytes)) != cudaSuccess) {
+        int st = cuda_fail(e, "qf_ctx_create");
+        qf_ctx_destroy(ctx);
+        return st;
+    }
+    *out = ctx;
+    return QF_OK;
+}
+
+int qf_ctx_destroy(qf_ctx *ctx) {
+    if (!ctx) return QF_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    free_state(ctx->scratch_sv);
+    free_state(ctx->scratch_sv2);
+    if (ctx->ws_plan) cudaFree(ctx->ws_plan);
+    if (ctx->ws_red) cudaFree(ctx->ws_red);
+    if (ctx->ws_tree) cudaFree(ctx->ws_tree);
+    if (ctx->ws_stage) cudaFree(ctx->ws_stage);
+    if (ctx->d_small) cudaFree(ctx->d_small);
+    if (ctx->h_small) cudaFreeHost(ctx->h_small);
+    if (ctx->host_pinned) cudaFreeHost(ctx->host_pinned);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return QF_OK;
+}
+
+int qf_ctx_synchronize(qf_ctx *ctx) {
+    clear_error();
+    if (!ctx) return fail(QF_ERR_INVALID_ARGUMENT, "context is NULL");
+    QF_TRY(bind_device(ctx));
+    QF_CUDA(cudaStreamSynchronize(ctx->stream));
+    return QF_OK;
+}
+
+int qf_ctx_stream(qf_ctx *ctx, void **stream_out) {
+    if (!ctx || !stream_out) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    *stream_out = (void *)ctx->stream;
+    return QF_OK;
+}
+
+int qf_sv_create(qf_ctx *ctx, uint32_t qubits, int dtype, uint64_t memory_budget_bytes, qf_sv **out) {
+    clear_error();
+    if (!ctx || !out) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    QF_TRY(bind_device(ctx));
+    return alloc_state(ctx, qubits, dtype, memory_budget_bytes, out);
+}
+
+int qf_sv_destroy(qf_sv *sv) {
+    if (!sv) return QF_OK;
+    if (sv->ctx) {
+        cudaSetDevice(sv->ctx->device);
+        cudaStreamSynchronize(sv->ctx->stream);
+    }
+    free_state(sv);
+    return QF_OK;
+}
+
+int qf_sv_qubits(const qf_sv *sv, uint32_t *q) {
+    QF_TRY(check_sv(sv));
+    if (!q) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    *q = sv->n;
+    return QF_OK;
+}
+
+int qf_sv_dtype(const qf_sv *sv, int *d) {
+    QF_TRY(check_sv(sv));
+    if (!d) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    *d = sv->dtype;
+    return QF_OK;
+}
+
+int qf_sv_device_ptr(qf_sv *sv, void **p) {
+    QF_TRY(check_sv(sv));
+    if (!p) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    *p = sv->d;
+    return QF_OK;
+}
+
+int qf_sv_set_zero(qf_sv *sv) {
+    clear_error();
+    QF_TRY(check_sv(sv));
+    QF_TRY(bind_device(sv->ctx));
+    return fill_zero_state(sv);
+}
+
+int qf_sv_upload(qf_sv *sv, const double *amps, uint64_t n_doubles) {
+    clear_error();
+    QF_TRY(check_sv(sv));
+    if (!amps) return fail(QF_ERR_INVALID_ARGUMENT, "amplitudes are NULL");
+    if (n_doubles != 2 * sv->dim)
+        return fail(QF_ERR_STATE_SIZE_NOT_POWER_OF_TWO, "expected %llu doubles (2^%u complex amplitudes), got %llu",
+                    (unsigned long long)(2 * sv->dim), sv->n, (unsigned long long)n_doubles);
+    QF_TRY(bind_device(sv->ctx));
+    QF_TRY(convert_from_f64(sv, amps));
+    QF_CUDA(cudaStreamSynchronize(sv->ctx->stream));
+    return QF_OK;
+}
+
+int qf_sv_download(qf_sv *sv, double *amps_out, uint64_t n_doubles) {
+    clear_error();
+    QF_TRY(check_sv(sv));
+    if (!amps_out) return fail(QF_ERR_INVALID_ARGUMENT, "output is NULL");
+    if (n_doubles != 2 * sv->dim)
+        return fail(QF_ERR_INVALID_ARGUMENT, "expected %llu doubles, got %llu", (unsigned long long)(2 * sv->dim),
+                    (unsigned long long)n_doubles);
+    QF_TRY(bind_device(sv->ctx));
+    return convert_to_f64(sv, amps_out);
+}
+
+int qf_sv_upload_raw(qf_sv *sv, const void *host, uint64_t bytes) {
+    clear_error();
+    QF_TRY(check_sv(sv));
+    if (!host || bytes != sv->bytes()) return fail(QF_ERR_INVALID_ARGUMENT, "raw upload needs %zu bytes", sv->bytes());
+    QF_TRY(bind_device(sv->ctx));
+    QF_CUDA(cudaMemcpyAsync(sv->d, host, bytes, cudaMemcpyHostToDevice, sv->ctx->stream));
+    QF_CUDA(cudaStreamSynchronize(sv->ctx->stream));
+    return QF_OK;
+}
+
+int qf_sv_download_raw(qf_sv *sv, void *host_out, uint64_t bytes) {
+    clear_error();
+    QF_TRY(check_sv(sv));
+    if (!host_out || bytes != sv->bytes()) return fail(QF_ERR_INVALID_ARGUMENT, "raw download needs %zu bytes", sv->bytes());
+    QF_TRY(bind_device(sv->ctx));
+    QF_CUDA(cudaMemcpyAsync(host_out, sv->d, bytes, cudaMemcpyDeviceToHost, sv->ctx->stream));
+    QF_CUDA(cudaStreamSynchronize(sv->ctx->stream));
+    return QF_OK;
+}
+
+int qf_sv_copy_from(qf_sv *dst, const qf_sv *src) {
+    clear_error();
+    QF_TRY(check_sv(dst));
+    QF_TRY(check_sv(src));
+    if (dst->n != src->n || dst->dtype != src->dtype || dst->ctx != src->ctx)
+        return fail(QF_ERR_INCOMPATIBLE_DEVICE_STATE, "device states must share a backend and have equal dimensions");
+    QF_TRY(bind_device(dst->ctx));
+    QF_CUDA(cudaMemcpyAsync(dst->d, src->d, dst->bytes(), cudaMemcpyDeviceToDevice, dst->ctx->stream));
+    return QF_OK;
+}
+
+int qf_sv_apply_gate(qf_sv *sv, int gate, double theta, uint32_t target) {
+    clear_error();
+    QF_TRY(check_sv(sv));
+    if (target >= sv->n)
+        return fail(QF_ERR_QUBIT_OUT_OF_RANGE, "qubit index %u is out of range for %u qubits", target, sv->n);
+    BGate g;
+    QF_TRY(gate_matrix(gate, theta, g.m));
+    g.kind = BK_MAT1;
+    g.q0 = target;
+    g.diag = matrix_is_diag(g.m);
+    QF_TRY(bind_device(sv->ctx));
+    return launch_gate1(sv, g);
+}
+
+static int apply_2q(qf_sv *sv, BKind kind, uint32_t a, uint32_t b) {
+    clear_error();
+    QF_TRY(check_sv(sv));
+    if (a >= sv->n) return fail(QF_ERR_QUBIT_OUT_OF_RANGE, "qubit index %u is out of range for %u qubits", a, sv->n);
+    if (b >= sv->n) return fail(QF_ERR_QUBIT_OUT_OF_RANGE, "qubit index %u is out of range for %u qubits", b, sv->n);
+    if (a == b) return fail(QF_ERR_INVALID_QUBIT_PAIR, "two-qubit operation requires distinct qubits, got %u and %u", a, b);
+    BGate g;
+    g.kind = kind;
+    g.q0 = a;
+    g.q1 = b;
+    QF_TRY(bind_device(sv->ctx));
+    return launch_gate2(sv, g);
+}
+
+int qf_sv_apply_cnot(qf_sv *sv, uint32_t c, uint32_t t) { return apply_2q(sv, BK_CNOT, c, t); }
+int qf_sv_apply_cz(qf_sv *sv, uint32_t a, uint32_t b) { return apply_2q(sv, BK_CZ, a, b); }
+int qf_sv_apply_swap(qf_sv *sv, uint32_t a, uint32_t b) { return apply_2q(sv, BK_SWAP, a, b); }
+
+int qf_sv_apply_ops(qf_sv *sv, const qf_op *ops, uint64_t n_ops, const double *params, uint64_t n_params,
+                    const double *inputs, uint64_t n_inputs, const qf_exec_opts *opts) {
+    clear_error();
+    QF_TRY(check_sv(sv));
+    if ((n_params && !params) || (n_inputs && !inputs)) return fail(QF_ERR_INVALID_ARGUMENT, "parameter arrays are NULL");
+    std::vector<BGate> gates;
+    QF_TRY(bind_ops(sv->n, ops, n_ops, params, n_params, inputs, n_inputs, -1, 0.0, gates));
+    QF_TRY(bind_device(sv->ctx));
+    return execute_gates(sv, gates, opts);
+}
+
+int qf_sv_norm_sqr(qf_sv *sv, double *out) {
+    clear_error();
+    QF_TRY(check_sv(sv));
+    if (!out) return fail(QF_ERR_INVALID_ARGUMENT, "output is NULL");
+    QF_TRY(bind_device(sv->ctx));
+    return reduce_norm_sqr(sv, out);
+}
+
+int qf_sv_probabilities(qf_sv *sv, double *out, uint64_t n_out) {
+    clear_error();
+    QF_TRY(check_sv(sv));
+    if (!out || n_out != sv->dim) return fail(QF_ERR_INVALID_ARGUMENT, "probabilities need %llu outputs", (unsigned long long)sv->dim);
+    QF_TRY(bind_device(sv->ctx));
+    qf_ctx *ctx = sv->ctx;
+    QF_TRY(ensure_device(&ctx->ws_stage, &ctx->ws_stage_bytes, sizeof(double) * sv->dim));
+    QF_TRY(reduce_probabilities(sv, static_cast<double *>(ctx->ws_stage)));
+    QF_CUDA(cudaMemcpyAsync(out, ctx->ws_stage, sizeof(double) * sv->dim, cudaMemcpyDeviceToHost, ctx->stream));
+    QF_CUDA(cudaStreamSynchronize(ctx->stream));
+    return QF_OK;
+}
+
+int qf_sv_expectation_z_all(qf_sv *sv, double *out, uint64_t n_out) {
+    clear_error();
+    QF_TRY(check_sv(sv));
+    if (!out || n_out != sv->n) return fail(QF_ERR_INVALID_ARGUMENT, "expectation_z_all needs %u outputs", sv->n);
+    QF_TRY(bind_device(sv->ctx));
+    return reduce_expect_z_all(sv, out);
+}
+
+int qf_sv_expectation(qf_sv *sv, int observable, uint32_t qubit, double *out) {
+    clear_error();
+    QF_TRY(check_sv(sv));
+    if (!out) return fail(QF_ERR_INVALID_ARGUMENT, "output is NULL");
+    if (observable < QF_PAULI_X || observable > QF_PAULI_Z) return fail(QF_ERR_INVALID_ARGUMENT, "unknown observable %d", observable);
+    if (qubit >= sv->n) return fail(QF_ERR_QUBIT_OUT_OF_RANGE, "qubit index %u is out of range for %u qubits", qubit, sv->n);
+    QF_TRY(bind_device(sv->ctx));
+    return reduce_expect_1q(sv, observable, qubit, out);
+}
+
+int qf_sv_expectation_pauli_sum(qf_sv *sv, const qf_pauli_term *terms, uint64_t n_terms, double *out) {
+    clear_error();
+    QF_TRY(check_sv(sv));
+    if (!out || (n_terms && !terms)) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    QF_TRY(bind_device(sv->ctx));
+    return pauli_expectation(sv, terms, n_terms, out);
+}
+
+// StateVector::measure (src/lib.rs:1321-1351) with the uniform drawn on the
+// host from the caller's SmallRng state, as CudaDeviceState::measure does.
+int qf_sv_measure(qf_sv *sv, uint32_t qubit, uint64_t *rng_state, uint8_t *outcome) {
+    clear_error();
+    QF_TRY(check_sv(sv));
+    if (!rng_state || !outcome) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (qubit >= sv->n) return fail(QF_ERR_QUBIT_OUT_OF_RANGE, "qubit index %u is out of range for %u qubits", qubit, sv->n);
+    QF_TRY(bind_device(sv->ctx));
+    double p_one;
+    QF_TRY(reduce_p_one(sv, qubit, &p_one));
+    p_one = std::min(1.0, std::max(0.0, p_one));
+    uint64_t x = *rng_state;
+    x ^= x << 13;
+    x ^= x >> 7;
+    x ^= x << 17;
+    *rng_state = x;
+    const double u = (double)(x >> 11) * (1.0 / 9007199254740992.0);
+    const uint8_t o = u < p_one ? 1 : 0;
+    const double prob = o ? p_one : 1.0 - p_one;
+    if (prob <= 2.220446049250313e-16)
+        return fail(QF_ERR_INVALID_PROBABILITY, "measurement probability must be in [0, 1], got %g", prob);
+    QF_TRY(collapse(sv, qubit, o, std::sqrt(prob)));
+    *outcome = o;
+    return QF_OK;
+}
+
+int qf_run_circuit(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops, const double *init_amps,
+                   double *out_amps, uint64_t n_doubles, const qf_exec_opts *opts) {
+    clear_error();
+    if (!ctx) return fail(QF_ERR_INVALID_ARGUMENT, "context is NULL");
+    QF_TRY(check_dtype(dtype));
+    if (qubits == 0) return fail(QF_ERR_ZERO_QUBITS, "a state vector must contain at least one qubit");
+    if (qubits > 40) return fail(QF_ERR_SIMULATION_SIZE_OVERFLOW, "dense simulation size exceeds the supported addressable range");
+    if ((init_amps || out_amps) && n_doubles != (2ULL << qubits))
+        return fail(QF_ERR_STATE_SIZE_NOT_POWER_OF_TWO, "expected %llu doubles", (unsigned long long)(2ULL << qubits));
+    std::vector<BGate> gates;
+    QF_TRY(bind_ops(qubits, ops, n_ops, nullptr, 0, nullptr, 0, -1, 0.0, gates));
+    QF_TRY(bind_device(ctx));
+    qf_sv *sv;
+    QF_TRY(scratch_state(ctx, &ctx->scratch_sv, qubits, dtype, &sv));
+    if (init_amps) QF_TRY(convert_from_f64(sv, init_amps));
+    else QF_TRY(fill_zero_state(sv));
+    QF_TRY(execute_gates(sv, gates, opts));
+    if (out_amps) return convert_to_f64(sv, out_amps);
+    QF_CUDA(cudaStreamSynchronize(ctx->stream));
+    return QF_OK;
+}
+
+int qf_sv_sample(qf_sv *sv, const uint32_t *qubit_order, const uint32_t *classical_bits, uint32_t m, uint64_t shots,
+                 uint64_t seed, double tie_eps, uint64_t *outcomes, uint64_t *n_ties) {
+    clear_error();
+    QF_TRY(check_sv(sv));
+    if (shots == 0) return fail(QF_ERR_INVALID_SHOT_COUNT, "shot count must be greater than zero");
+    if (m && (!qubit_order || !classical_bits)) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    for (uint32_t j = 0; j < m; ++j)
+        if (classical_bits[j] >= 4096)
+            return fail(QF_ERR_CLASSICAL_BIT_OUT_OF_RANGE, "classical bit index %u exceeds the supported maximum of 4095", classical_bits[j]);
+    QF_TRY(bind_device(sv->ctx));
+    return sample_shots(sv, qubit_order, classical_bits, m, shots, seed, tie_eps, outcomes, n_ties);
+}
+
+int qf_run_shots(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops, const double *init_amps,
+                 uint64_t shots, uint64_t seed, double tie_eps, uint64_t *outcomes, uint32_t *classical_width,
+                 uint64_t *n_ties, const qf_exec_opts *opts) {
+    clear_error();
+    if (!ctx) return fail(QF_ERR_INVALID_ARGUMENT, "context is NULL");
+    QF_TRY(check_dtype(dtype));
+    if (shots == 0) return fail(QF_ERR_INVALID_SHOT_COUNT, "shot count must be greater than zero");
+    if (n_ops && !ops) return fail(QF_ERR_INVALID_ARGUMENT, "ops is NULL");
+    int st;
+    const uint64_t width = classical_bit_check(ops, n_ops, &st);
+    if (st) return st;
+    if (qubits == 0) return fail(QF_ERR_ZERO_QUBITS, "a state vector must contain at least one qubit");
+    // unitary prefix, then measurements only
+    uint64_t first = n_ops;
+    for (uint64_t k = 0; k < n_ops; ++k)
+        if (ops[k].kind == QF_OP_MEASURE) { first = k; break; }
+    std::vector<uint32_t> mq, mc;
+    for (uint64_t k = 0; k < n_ops; ++k) {
+        if (ops[k].kind == QF_OP_CHANNEL)
+            return fail(QF_ERR_OPERATION_REQUIRES_DENSITY_MATRIX, "this circuit operation requires density-matrix simulation");
+        if (ops[k].kind == QF_OP_COND || (k > first && ops[k].kind != QF_OP_MEASURE))
+            return fail(QF_ERR_UNSUPPORTED_OPERATION,
+                        "mid-circuit measurement and feed-forward need the per-shot engine; measurements must follow the last gate");
+        if (ops[k].kind == QF_OP_MEASURE) {
+            if (ops[k].q0 >= qubits)
+                return fail(QF_ERR_QUBIT_OUT_OF_RANGE, "qubit index %u is out of range for %u qubits", ops[k].q0, qubits);
+            mq.push_back(ops[k].q0);
+            mc.push_back(ops[k].param);
+        }
+    }
+    if (width > 64) return fail(QF_ERR_UNSUPPORTED_OPERATION, "classical registers wider than 64 bits are not packed");
+    std::vector<BGate> gates;
+    QF_TRY(bind_ops(qubits, ops, first, nullptr, 0, nullptr, 0, -1, 0.0, gates));
+    QF_TRY(bind_device(ctx));
+    qf_sv *sv;
+    QF_TRY(scratch_state(ctx, &ctx->scratch_sv, qubits, dtype, &sv));
+    if (init_amps) QF_TRY(convert_from_f64(sv, init_amps));
+    else QF_TRY(fill_zero_state(sv));
+    QF_TRY(execute_gates(sv, gates, opts));
+    if (classical_width) *classical_width = (uint32_t)width;
+    return sample_shots(sv, mq.data(), mc.data(), (uint32_t)mq.size(), shots, seed, tie_eps, outcomes, n_ties);
+}
+
+int qf_expectation(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops, const double *params,
+                   uint64_t n_params, const double *inputs, uint64_t n_inputs, const qf_pauli_term *terms, uint64_t n_terms,
+                   const qf_exec_opts *opts, double *expectation) {
+    clear_error();
+    if (!ctx || !expectation) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    QF_TRY(check_dtype(dtype));
+    if (qubits == 0) return fail(QF_ERR_ZERO_QUBITS, "a state vector must contain at least one qubit");
+    if (n_terms && !terms) return fail(QF_ERR_INVALID_ARGUMENT, "terms is NULL");
+    QF_TRY(bind_device(ctx));
+    return forward_expectation(ctx, qubits, dtype, ops, n_ops, params, n_params, inputs, n_inputs, -1, 0.0, terms, n_terms,
+                               opts, expectation);
+}
+
+// ParameterizedCircuit::gradient_with_inputs (src/gradients.rs:232-330).
+int qf_gradient(qf_ctx *ctx, uint32_t qubits, const qf_op *ops, uint64_t n_ops, const double *params, uint64_t n_params,
+                const double *inputs, uint64_t n_inputs, const qf_pauli_term *terms, uint64_t n_terms,
+                const qf_gradient_opts *opts, double *expectation, double *gradient, qf_gradient_info *info) {
+    clear_error();
+    if (!ctx || !opts || (n_params && !gradient)) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    if ((n_params && !params) || (n_inputs && !inputs)) return fail(QF_ERR_INVALID_ARGUMENT, "parameter arrays are NULL");
+    QF_TRY(check_dtype(opts->dtype));
+    QF_TRY(check_terms_real(terms, n_terms));
+    const uint64_t occurrences = count_rotations(ops, n_ops);
+    int strategy = opts->strategy;
+    if (strategy == QF_GRAD_AUTO) {
+        // GradientStrategy::select (src/gradients.rs:81-89)
+        if (has_channel(ops, n_ops))
+            return fail(QF_ERR_OPERATION_REQUIRES_DENSITY_MATRIX, "this circuit operation requires density-matrix simulation");
+        strategy = opts->shots > 0 ? QF_GRAD_PARAMETER_SHIFT : QF_GRAD_ADJOINT;
+    }
+    if (strategy < QF_GRAD_PARAMETER_SHIFT || strategy > QF_GRAD_FINITE_DIFFERENCE)
+        return fail(QF_ERR_INVALID_ARGUMENT, "unknown gradient strategy %d", opts->strategy);
+    if (strategy == QF_GRAD_FINITE_DIFFERENCE &&
+        (!std::isfinite(opts->finite_difference_step) || opts->finite_difference_step <= 0.0))
+        return fail(QF_ERR_INVALID_FINITE_DIFFERENCE_STEP, "finite-difference step must be positive and finite, got %g",
+                    opts->finite_difference_step);
+    if (qubits == 0) return fail(QF_ERR_ZERO_QUBITS, "a state vector must contain at least one qubit");
+    // validate the whole list once (also rejects channels/measurements)
+    std::vector<BGate> gates;
+    QF_TRY(bind_ops(qubits, ops, n_ops, params, n_params, inputs, n_inputs, -1, 0.0, gates));
+    {  // observable qubits in range
+        const uint64_t valid = qubits >= 64 ? ~0ULL : ((1ULL << qubits) - 1);
+        for (uint64_t t = 0; t < n_terms; ++t)
+            if ((terms[t].xmask | terms[t].zmask) & ~valid)
+                return fail(QF_ERR_QUBIT_OUT_OF_RANGE, "observable acts outside %u qubits", qubits);
+    }
+    QF_TRY(bind_device(ctx));
+    if (info) {
+        info->strategy = strategy;
+        info->reserved = 0;
+        info->evaluations = (strategy == QF_GRAD_ADJOINT || strategy == QF_GRAD_BACKPROP) ? 2 : 2 * occurrences;
+    }
+    const qf_exec_opts *exec = &opts->exec;
+    if (strategy == QF_GRAD_ADJOINT || strategy == QF_GRAD_BACKPROP)
+        return adjoint_device(ctx, qubits, gates, terms, n_terms, opts, n_params, expectation, gradient);
+
+    std::fill(gradient, gradient + n_params, 0.0);
+    if (expectation)
+        QF_TRY(forward_expectation(ctx, qubits, opts->dtype, ops, n_ops, params, n_params, inputs, n_inputs, -1, 0.0, terms,
+                                   n_terms, exec, expectation));
+    const bool shift_rule = strategy == QF_GRAD_PARAMETER_SHIFT;
+    const double h = shift_rule ? 1.57079632679489661923 : opts->finite_difference_step;
+    for (uint64_t k = 0; k < n_ops; ++k) {
+        if (ops[k].kind != QF_OP_ROTATION) continue;
+        double plus, minus;
+        QF_TRY(forward_expectation(ctx, qubits, opts->dtype, ops, n_ops, params, n_params, inputs, n_inputs, (int64_t)k, h,
+                                   terms, n_terms, exec, &plus));
+        QF_TRY(forward_expectation(ctx, qubits, opts->dtype, ops, n_ops, params, n_params, inputs, n_inputs, (int64_t)k, -h,
+                                   terms, n_terms, exec, &minus));
+        // parameter_shift_gradient_with_inputs (src/lib.rs:3541) / FD (src/gradients.rs:369)
+        gradient[ops[k].param] += shift_rule ? 0.5 * (plus - minus) : (plus - minus) / (2.0 * h);
+    }
+    return QF_OK;
+}
+
+uint64_t qf_rng_jump(uint64_t state, uint64_t steps) { return rng_jump(state, steps); }
+
+int qf_plan_stats(uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops, const double *params, uint64_t n_params,
+                  const double *inputs, uint64_t n_inputs, const qf_exec_opts *opts, uint64_t *n_passes, uint64_t *n_gates) {
+    clear_error();
+    QF_TRY(check_dtype(dtype));
+    if (!n_passes || !n_gates) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (qubits == 0) return fail(QF_ERR_ZERO_QUBITS, "a state vector must contain at least one qubit");
+    std::vector<BGate> gates;
+    QF_TRY(bind_ops(qubits, ops, n_ops, params, n_params, inputs, n_inputs, -1, 0.0, gates));
+    *n_gates = gates.size();
+    if (opts && opts->mode == QF_EXEC_UNFUSED) {
+        *n_passes = gates.size();
+        return QF_OK;
+    }
+    PlanOpts po;
+    default_tiling(qubits, dtype, opts ? opts->tile_qubits : 0, &po.tile_qubits, &po.low_qubits);
+    Plan plan;
+    QF_TRY(plan_passes(qubits, gates, po, plan));
+    *n_passes = plan.passes.size();
+    return QF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,393 @@
+// planner.cpp — host side of the engine: gate binding, tile-pass planning and
+// SmallRng jump-ahead. No device code; every function here also runs in the
+// CPU-only test-suite through qf_plan_stats / qf_rng_jump.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "qf_internal.h"
+
+namespace qf {
+
+// Gate::matrix (src/lib.rs:2267-2333). Host f64 with the C library's cos/sin,
+// as the reference's f64::cos/sin.
+int gate_matrix(int gate, double theta, double m[8]) {
+    const double s = 0.70710678118654752440;  // FRAC_1_SQRT_2
+    std::memset(m, 0, sizeof(double) * 8);
+    switch (gate) {
+    case QF_GATE_I: m[0] = 1; m[6] = 1; return QF_OK;
+    case QF_GATE_X: m[2] = 1; m[4] = 1; return QF_OK;
+    case QF_GATE_Y: m[3] = -1; m[5] = 1; return QF_OK;
+    case QF_GATE_Z: m[0] = 1; m[6] = -1; return QF_OK;
+    case QF_GATE_H: m[0] = s; m[2] = s; m[4] = s; m[6] = -s; return QF_OK;
+    case QF_GATE_S: m[0] = 1; m[7] = 1; return QF_OK;
+    case QF_GATE_SDG: m[0] = 1; m[7] = -1; return QF_OK;
+    case QF_GATE_T: m[0] = 1; m[6] = s; m[7] = s; return QF_OK;
+    case QF_GATE_TDG: m[0] = 1; m[6] = s; m[7] = -s; return QF_OK;
+    case QF_GATE_RX: {
+        double c = std::cos(theta * 0.5), si = std::sin(theta * 0.5);
+        m[0] = c; m[3] = -si; m[5] = -si; m[6] = c;
+        return QF_OK;
+    }
+    case QF_GATE_RY: {
+        double c = std::cos(theta * 0.5), si = std::sin(theta * 0.5);
+        m[0] = c; m[2] = -si; m[4] = si; m[6] = c;
+        return QF_OK;
+    }
+    case QF_GATE_RZ: {
+        double half = theta * 0.5;
+        m[0] = std::cos(half); m[1] = -std::sin(half);
+        m[6] = std::cos(half); m[7] = std::sin(half);
+        return QF_OK;
+    }
+    default:
+        return fail(QF_ERR_INVALID_ARGUMENT, "unknown gate code %d", gate);
+    }
+}
+
+bool matrix_is_diag(const double m[8]) { return m[2] == 0 && m[3] == 0 && m[4] == 0 && m[5] == 0; }
+
+static int rotation_gate(int axis) {
+    return axis == QF_PAULI_X ? QF_GATE_RX : axis == QF_PAULI_Y ? QF_GATE_RY : QF_GATE_RZ;
+}
+
+static int check_pair(uint32_t n, uint32_t a, uint32_t b) {
+    if (a >= n) return fail(QF_ERR_QUBIT_OUT_OF_RANGE, "qubit index %u is out of range for %u qubits", a, n);
+    if (b >= n) return fail(QF_ERR_QUBIT_OUT_OF_RANGE, "qubit index %u is out of range for %u qubits", b, n);
+    if (a == b)
+        return fail(QF_ERR_INVALID_QUBIT_PAIR, "two-qubit operation requires distinct qubits, got %u and %u", a, b);
+    return QF_OK;
+}
+
+// Validation mirrors Circuit::run (src/lib.rs:2786-2802) and
+// ParameterizedCircuit::run_with_shift (src/lib.rs:4677-4740), but is done for
+// the whole list before any launch (src/cuda.rs:2256-2285).
+int bind_ops(uint32_t n, const qf_op *ops, uint64_t n_ops, const double *params, uint64_t n_params,
+             const double *inputs, uint64_t n_inputs, int64_t shift_op, double shift,
+             std::vector<BGate> &out) {
+    out.clear();
+    out.reserve(n_ops);
+    if (n_ops && !ops) return fail(QF_ERR_INVALID_ARGUMENT, "ops is NULL");
+    for (uint64_t k = 0; k < n_inputs; ++k)
+        if (!std::isfinite(inputs[k])) return fail(QF_ERR_NON_FINITE_PARAMETER, "circuit parameters must be finite");
+    for (uint64_t k = 0; k < n_params; ++k)
+        if (!std::isfinite(params[k])) return fail(QF_ERR_NON_FINITE_PARAMETER, "circuit parameters must be finite");
+    for (uint64_t k = 0; k < n_ops; ++k) {
+        const qf_op &op = ops[k];
+        BGate g;
+        g.op_index = (int64_t)k;
+        switch (op.kind) {
+        case QF_OP_GATE:
+        case QF_OP_ROTATION:
+        case QF_OP_ENCODING: {
+            int gate;
+            double theta;
+            if (op.kind == QF_OP_GATE) {
+                gate = op.gate;
+                theta = op.theta;
+            } else {
+                if (op.gate > QF_PAULI_Z) return fail(QF_ERR_INVALID_ARGUMENT, "rotation axis %u is invalid", op.gate);
+                gate = rotation_gate(op.gate);
+                if (op.kind == QF_OP_ROTATION) {
+                    if (op.param >= n_params)
+                        return fail(QF_ERR_INVALID_PARAMETER_COUNT, "expected %llu circuit parameters, got %llu",
+                                    (unsigned long long)n_params, (unsigned long long)op.param + 1);
+                    theta = params[op.param];
+                    g.axis = op.gate;
+                    g.param = op.param;
+                } else {
+                    if (op.param >= n_inputs)
+                        return fail(QF_ERR_INVALID_INPUT_COUNT, "expected %llu encoded inputs, got %llu",
+                                    (unsigned long long)n_inputs, (unsigned long long)op.param + 1);
+                    theta = inputs[op.param];
+                }
+            }
+            if ((int64_t)k == shift_op) theta = theta + shift;
+            if (op.q0 >= n)
+                return fail(QF_ERR_QUBIT_OUT_OF_RANGE, "qubit index %u is out of range for %u qubits", op.q0, n);
+            g.kind = BK_MAT1;
+            g.q0 = op.q0;
+            QF_TRY(gate_matrix(gate, theta, g.m));
+            g.diag = matrix_is_diag(g.m);
+            break;
+        }
+        case QF_OP_CNOT:
+        case QF_OP_CZ:
+        case QF_OP_SWAP:
+            QF_TRY(check_pair(n, op.q0, op.q1));
+            g.kind = op.kind == QF_OP_CNOT ? BK_CNOT : op.kind == QF_OP_CZ ? BK_CZ : BK_SWAP;
+            g.q0 = op.q0;
+            g.q1 = op.q1;
+            break;
+        case QF_OP_CHANNEL:
+            return fail(QF_ERR_OPERATION_REQUIRES_DENSITY_MATRIX,
+                        "this circuit operation requires density-matrix simulation");
+        case QF_OP_MEASURE:
+        case QF_OP_COND:
+            return fail(QF_ERR_OPERATION_REQUIRES_SHOT_EXECUTION,
+                        "measurement and classically conditioned circuit operations require shot execution");
+        default:
+            return fail(QF_ERR_INVALID_ARGUMENT, "unknown op kind %u at index %llu", op.kind, (unsigned long long)k);
+        }
+        out.push_back(g);
+    }
+    return QF_OK;
+}
+
+// U^dagger: conjugate transpose of the 2x2 (adjoint_gate, src/lib.rs:2363-2382,
+// gives the same matrices); 2q gates are self-inverse.
+BGate inverse_gate(const BGate &g) {
+    BGate r = g;
+    if (g.kind == BK_MAT1) {
+        // (m00 m01; m10 m11)^dagger = (m00* m10*; m01* m11*)
+        r.m[0] = g.m[0]; r.m[1] = -g.m[1];
+        r.m[2] = g.m[4]; r.m[3] = -g.m[5];
+        r.m[4] = g.m[2]; r.m[5] = -g.m[3];
+        r.m[6] = g.m[6]; r.m[7] = -g.m[7];
+    }
+    return r;
+}
+
+// c = a * b for 2x2 complex (row-major, interleaved).
+static void mat_mul(const double a[8], const double b[8], double c[8]) {
+    for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j) {
+            double re = 0, im = 0;
+            for (int t = 0; t < 2; ++t) {
+                double ar = a[2 * (2 * i + t)], ai = a[2 * (2 * i + t) + 1];
+                double br = b[2 * (2 * t + j)], bi = b[2 * (2 * t + j) + 1];
+                re += ar * br - ai * bi;
+                im += ar * bi + ai * br;
+            }
+            c[2 * (2 * i + j)] = re;
+            c[2 * (2 * i + j) + 1] = im;
+        }
+}
+
+void default_tiling(uint32_t n, int dtype, int requested_tile, int *tile, int *low) {
+    int k = requested_tile > 0 ? requested_tile : (dtype == QF_C64 ? 12 : 11);
+    if (k > kMaxLocal + 5) k = kMaxLocal + 5;
+    int lo = dtype == QF_C64 ? 5 : 4;
+    if ((int)n <= k) { k = (int)n; lo = (int)n; }
+    if (lo > k) lo = k;
+    *tile = k;
+    *low = lo;
+}
+
+namespace {
+struct Item {
+    BGate g;
+    bool overlap = false;  // adjoint overlap marker for rotation g (axis in g.axis)
+    uint64_t touch = 0;    // qubits this item reads or writes
+    uint64_t need = 0;     // qubits that must be tile-resident
+};
+
+Item make_item(const BGate &g, bool overlap) {
+    Item it;
+    it.g = g;
+    it.overlap = overlap;
+    const uint64_t b0 = 1ULL << g.q0, b1 = 1ULL << g.q1;
+    if (overlap) {
+        it.touch = b0;
+        it.need = g.axis == QF_PAULI_Z ? 0 : b0;
+        return it;
+    }
+    switch (g.kind) {
+    case BK_MAT1: it.touch = b0; it.need = g.diag ? 0 : b0; break;
+    case BK_CNOT: it.touch = b0 | b1; it.need = b1; break;
+    case BK_CZ: it.touch = b0 | b1; it.need = 0; break;
+    default: it.touch = b0 | b1; it.need = b0 | b1; break;
+    }
+    return it;
+}
+
+int popc(uint64_t x) { return __builtin_popcountll(x); }
+}  // namespace
+
+// Greedy tile-pass planner. Walk the remaining items in circuit order; an item
+// joins the current pass when none of its qubits is blocked by an item left
+// behind and the qubits it needs resident still fit in the tile; otherwise its
+// qubits become blocked, so no later item on those qubits may move ahead of
+// it. Gates on different qubits commute, so the reordering is exact.
+// Diagonal gates, CZ and a CNOT's control never need residency: within a tile
+// their non-resident bits are constant and become per-tile scalars/conditions.
+int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, Plan &plan) {
+    plan = Plan();
+    plan.n = n;
+    const int k = std::min<int>(o.tile_qubits, (int)n);
+    const int low = std::min<int>(o.low_qubits, k);
+    if (k - low > kMaxLocal) return fail(QF_ERR_INVALID_ARGUMENT, "tile of %d qubits over %d low qubits is too wide", k, low);
+    const uint64_t all = n >= 64 ? ~0ULL : ((1ULL << n) - 1);
+    const uint64_t low_mask = (low >= 64) ? ~0ULL : ((1ULL << low) - 1);
+
+    std::vector<Item> items;
+    items.reserve(gates.size() * (o.backward ? 2 : 1));
+    if (!o.backward) {
+        for (const BGate &g : gates) items.push_back(make_item(g, false));
+    } else {
+        for (size_t i = gates.size(); i-- > 0;) {
+            if (gates[i].axis != 255) items.push_back(make_item(gates[i], true));
+            items.push_back(make_item(inverse_gate(gates[i]), false));
+        }
+    }
+
+    std::vector<int> remaining(items.size());
+    for (size_t i = 0; i < items.size(); ++i) remaining[i] = (int)i;
+
+    while (!remaining.empty()) {
+        uint64_t L = low_mask;
+        uint64_t blocked = 0;
+        std::vector<Item> taken;
+        std::vector<int> last_on(n, -1);  // index into taken of the last item touching q
+        std::vector<int> rest;
+        rest.reserve(remaining.size());
+        for (size_t r = 0; r < remaining.size(); ++r) {
+            const int idx = remaining[r];
+            const Item &it = items[idx];
+            if (blocked == all || taken.size() >= (size_t)o.max_items) { rest.push_back(idx); continue; }
+            if (it.touch & blocked) { blocked |= it.touch; rest.push_back(idx); continue; }
+            const uint64_t nl = L | it.need;
+            if (popc(nl) > k) { blocked |= it.touch; rest.push_back(idx); continue; }
+            L = nl;
+            // merge consecutive 1q gates on one qubit into one matrix
+            if (o.merge_1q && !it.overlap && it.g.kind == BK_MAT1) {
+                int prev = last_on[it.g.q0];
+                if (prev >= 0 && !taken[prev].overlap && taken[prev].g.kind == BK_MAT1) {
+                    double c[8];
+                    mat_mul(it.g.m, taken[prev].g.m, c);
+                    std::memcpy(taken[prev].g.m, c, sizeof c);
+                    taken[prev].g.diag = matrix_is_diag(c);
+                    taken[prev].g.op_index = -1;
+                    continue;
+                }
+            }
+            taken.push_back(it);
+            const int ti = (int)taken.size() - 1;
+            for (uint32_t q = 0; q < n; ++q)
+                if ((it.touch >> q) & 1ULL) last_on[q] = ti;
+        }
+        if (taken.empty()) return fail(QF_ERR_INVALID_ARGUMENT, "planner made no progress");
+        remaining.swap(rest);
+
+        // widen the tile with the lowest free qubits: longer contiguous runs
+        for (uint32_t q = 0; q < n && popc(L) < k; ++q) L |= 1ULL << q;
+        // lower to tile ops
+        Pass p;
+        uint32_t lo_eff = 0;
+        while (lo_eff < n && ((L >> lo_eff) & 1ULL)) ++lo_eff;
+        std::vector<int> local_bit(n, -1);
+        for (uint32_t q = 0; q < lo_eff; ++q) local_bit[q] = (int)q;
+        uint32_t r = 0;
+        std::memset(p.a.hi_q, 0, sizeof p.a.hi_q);
+        for (uint32_t q = lo_eff; q < n; ++q)
+            if ((L >> q) & 1ULL) {
+                if (r >= (uint32_t)kMaxLocal) return fail(QF_ERR_INVALID_ARGUMENT, "too many resident high qubits");
+                p.a.hi_q[r] = (uint8_t)q;
+                local_bit[q] = (int)(lo_eff + r);
+                ++r;
+            }
+        p.a.k = lo_eff + r;
+        p.a.low = lo_eff;
+        p.a.nonlocal_mask = all & ~L;
+        p.a.n_tiles = 1ULL << (n - p.a.k);
+        p.op_begin = (uint32_t)plan.ops.size();
+        p.mat_begin = (uint32_t)(plan.mats.size() / 8);
+        p.a.slot_base = plan.n_slots;
+        for (const Item &it : taken) {
+            TileOp t;
+            std::memset(&t, 0, sizeof t);
+            t.slot = -1;
+            const BGate &g = it.g;
+            const int lb0 = local_bit[g.q0];
+            const int lb1 = g.kind == BK_MAT1 ? -1 : local_bit[g.q1];
+            if (it.overlap) {
+                t.slot = (int32_t)plan.n_slots++;
+                plan.slot_param.push_back(g.param);
+                if (g.axis == QF_PAULI_X) { t.kind = T_OVL_X; t.b0 = (uint8_t)lb0; }
+                else if (g.axis == QF_PAULI_Y) { t.kind = T_OVL_Y; t.b0 = (uint8_t)lb0; }
+                else if (lb0 >= 0) { t.kind = T_OVL_ZL; t.b0 = (uint8_t)lb0; }
+                else { t.kind = T_OVL_ZG; t.g0 = g.q0; }
+                plan.ops.push_back(t);
+                continue;
+            }
+            switch (g.kind) {
+            case BK_MAT1: {
+                t.mat = (uint32_t)(plan.mats.size() / 8) - p.mat_begin;
+                plan.mats.insert(plan.mats.end(), g.m, g.m + 8);
+                if (!g.diag) { t.kind = T_MAT1; t.b0 = (uint8_t)lb0; }
+                else if (lb0 >= 0) { t.kind = T_DIAG1; t.b0 = (uint8_t)lb0; }
+                else { t.kind = T_GPHASE; t.g0 = g.q0; }
+                break;
+            }
+            case BK_CNOT:
+                if (lb0 >= 0) { t.kind = T_CNOT_LL; t.b0 = (uint8_t)lb0; t.b1 = (uint8_t)lb1; }
+                else { t.kind = T_CNOT_GL; t.g0 = g.q0; t.b1 = (uint8_t)lb1; }
+                break;
+            case BK_CZ:
+                if (lb0 >= 0 && lb1 >= 0) { t.kind = T_CZ_LL; t.b0 = (uint8_t)lb0; t.b1 = (uint8_t)lb1; }
+                else if (lb0 >= 0) { t.kind = T_CZ_GL; t.g0 = g.q1; t.b1 = (uint8_t)lb0; }
+                else if (lb1 >= 0) { t.kind = T_CZ_GL; t.g0 = g.q0; t.b1 = (uint8_t)lb1; }
+                else { t.kind = T_CZ_GG; t.g0 = g.q0; t.g1 = g.q1; }
+                break;
+            default:
+                t.kind = T_SWAP_LL; t.b0 = (uint8_t)lb0; t.b1 = (uint8_t)lb1;
+                break;
+            }
+            plan.ops.push_back(t);
+        }
+        p.a.n_ops = (uint32_t)plan.ops.size() - p.op_begin;
+        p.a.n_mats = (uint32_t)(plan.mats.size() / 8) - p.mat_begin;
+        p.a.n_slots = plan.n_slots - p.a.slot_base;
+        plan.passes.push_back(p);
+    }
+    return QF_OK;
+}
+
+// ---- SmallRng jump-ahead --------------------------------------------------
+// next_u64 (src/lib.rs:4898-4905) is linear over GF(2)^64: x -> T x. A 64x64
+// bit matrix is stored as its 64 columns (the image of each basis vector).
+static uint64_t xs_step(uint64_t x) {
+    x ^= x << 13;
+    x ^= x >> 7;
+    x ^= x << 17;
+    return x;
+}
+static uint64_t mat_apply(const uint64_t *cols, uint64_t x) {
+    uint64_t y = 0;
+    while (x) {
+        int c = __builtin_ctzll(x);
+        y ^= cols[c];
+        x &= x - 1;
+    }
+    return y;
+}
+static void mat_compose(const uint64_t *a, const uint64_t *b, uint64_t *out) {  // out = a . b
+    uint64_t tmp[64];
+    for (int c = 0; c < 64; ++c) tmp[c] = mat_apply(a, b[c]);
+    std::memcpy(out, tmp, sizeof tmp);
+}
+static void mat_power(uint64_t steps, uint64_t *out) {
+    uint64_t base[64], acc[64];
+    for (int c = 0; c < 64; ++c) { base[c] = xs_step(1ULL << c); acc[c] = 1ULL << c; }
+    while (steps) {
+        if (steps & 1ULL) mat_compose(base, acc, acc);
+        mat_compose(base, base, base);
+        steps >>= 1;
+    }
+    std::memcpy(out, acc, sizeof acc);
+}
+
+uint64_t rng_jump(uint64_t state, uint64_t steps) {
+    uint64_t m[64];
+    mat_power(steps, m);
+    return mat_apply(m, state);
+}
+
+// mats[j] = T^(stride * 2^j), j < count.
+void rng_jump_matrices(uint64_t stride, uint64_t (*mats)[64], int count) {
+    if (count <= 0) return;
+    mat_power(stride, mats[0]);
+    for (int j = 1; j < count; ++j) mat_compose(mats[j - 1], mats[j - 1], mats[j]);
+}
+
+}  // namespace qf

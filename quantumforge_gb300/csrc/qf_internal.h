@@ -1,0 +1,194 @@
+// qf_internal.h — internal declarations shared by the engine's translation
+// units. Nothing here crosses the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/qf.h"
+
+struct qf_ctx {
+    int device = 0;
+    int sm_count = 0;
+    size_t smem_optin = 0;
+    cudaStream_t stream = nullptr;
+    // Growable device workspaces owned by the context.
+    void *ws_plan = nullptr;      size_t ws_plan_bytes = 0;      // pass descriptors + matrices
+    void *ws_red = nullptr;       size_t ws_red_bytes = 0;       // reduction partials
+    void *ws_tree = nullptr;      size_t ws_tree_bytes = 0;      // sampler marginal tree
+    void *host_pinned = nullptr;  size_t host_pinned_bytes = 0;  // small pinned staging
+    void *ws_stage = nullptr;     size_t ws_stage_bytes = 0;     // f64 <-> dtype conversion staging
+    double *d_small = nullptr;    // 64 KiB device result area
+    double *h_small = nullptr;    // 64 KiB pinned host mirror
+    qf_sv *scratch_sv = nullptr;  // cached state for whole-circuit calls
+    qf_sv *scratch_sv2 = nullptr; // cached second state (adjoint costate)
+};
+constexpr size_t kSmallBytes = 64 * 1024;
+
+struct qf_sv {
+    qf_ctx *ctx = nullptr;
+    uint32_t n = 0;
+    int dtype = QF_C64;
+    uint64_t dim = 0;
+    void *d = nullptr;  // 2^n complex amplitudes, interleaved
+    size_t bytes() const { return dim * (dtype == QF_C64 ? 8u : 16u); }
+};
+
+namespace qf {
+
+// ---- errors -----------------------------------------------------------------
+int fail(int status, const char *fmt, ...);
+void clear_error();
+int cuda_fail(cudaError_t e, const char *what);
+#define QF_CUDA(expr)                                              \
+    do {                                                           \
+        cudaError_t qf_e_ = (expr);                                \
+        if (qf_e_ != cudaSuccess) return qf::cuda_fail(qf_e_, #expr); \
+    } while (0)
+#define QF_TRY(expr)                 \
+    do {                             \
+        int qf_s_ = (expr);          \
+        if (qf_s_ != QF_OK) return qf_s_; \
+    } while (0)
+
+// Grow-only device workspace.
+int ensure_device(void **ptr, size_t *bytes, size_t need);
+int ensure_pinned(void **ptr, size_t *bytes, size_t need);
+
+// ---- bound gates ------------------------------------------------------------
+// A gate list with parameters resolved to matrices (host, f64).
+enum BKind : uint8_t { BK_MAT1 = 0, BK_CNOT = 1, BK_CZ = 2, BK_SWAP = 3 };
+
+struct BGate {
+    uint8_t kind = BK_MAT1;
+    uint8_t diag = 0;        // MAT1 only: m01 == m10 == 0
+    uint8_t axis = 255;      // rotation occurrence: generator axis (QF_PAULI_*), else 255
+    uint8_t pad = 0;
+    uint32_t q0 = 0, q1 = 0;
+    int64_t op_index = -1;   // index into the caller's op list
+    int64_t param = -1;      // parameter index of a rotation occurrence
+    double m[8] = {0};       // m00, m01, m10, m11 as (re, im)
+};
+
+// Gate::matrix (src/lib.rs:2267-2333) evaluated on the host in f64.
+int gate_matrix(int gate, double theta, double m[8]);
+bool matrix_is_diag(const double m[8]);
+
+// Validate an op list for state-vector execution and bind it.
+// `shift_op`/`shift` add `shift` to the angle of op `shift_op` (parameter shift).
+int bind_ops(uint32_t n, const qf_op *ops, uint64_t n_ops, const double *params, uint64_t n_params,
+             const double *inputs, uint64_t n_inputs, int64_t shift_op, double shift,
+             std::vector<BGate> &out);
+// The inverse of a bound gate (U^dagger).
+BGate inverse_gate(const BGate &g);
+
+// ---- tile-pass plans --------------------------------------------------------
+enum TKind : uint8_t {
+    T_MAT1 = 0,     // dense 2x2 on local bit b0
+    T_DIAG1 = 1,    // diag(m00, m11) on local bit b0
+    T_GPHASE = 2,   // diag(m00, m11) on non-local qubit g0: scalar per tile
+    T_CNOT_LL = 3,  // control local b0, target local b1
+    T_CNOT_GL = 4,  // control non-local g0, target local b1
+    T_CZ_LL = 5,    // both local
+    T_CZ_GL = 6,    // g0 non-local, b1 local
+    T_CZ_GG = 7,    // both non-local
+    T_SWAP_LL = 8,  // both local
+    T_OVL_X = 9,    // adjoint overlap Im<lambda|X_b0 psi>, slot
+    T_OVL_Y = 10,   // adjoint overlap Im<lambda|Y_b0 psi>
+    T_OVL_ZL = 11,  // adjoint overlap Im<lambda|Z_b0 psi>, b0 local
+    T_OVL_ZG = 12   // adjoint overlap with Z on non-local g0
+};
+
+struct TileOp {
+    uint8_t kind;
+    uint8_t b0;
+    uint8_t b1;
+    uint8_t pad;
+    uint32_t g0;
+    uint32_t g1;
+    uint32_t mat;   // matrix index (4 complex entries)
+    int32_t slot;   // overlap slot
+};
+static_assert(sizeof(TileOp) == 20, "TileOp layout");
+
+constexpr int kMaxLocal = 16;
+
+// Kernel-side view of one pass: passed by value.
+struct PassArgs {
+    uint64_t nonlocal_mask;   // qubits not resident in the tile
+    uint64_t n_tiles;
+    uint32_t k;               // local qubits
+    uint32_t low;             // local bits 0..low-1 are global qubits 0..low-1
+    uint32_t n_ops;
+    uint32_t n_mats;
+    uint32_t slot_base;       // first overlap slot of this pass
+    uint32_t n_slots;         // overlap slots in this pass
+    uint8_t hi_q[kMaxLocal];  // global qubit of local bit low + r
+};
+
+struct Pass {
+    PassArgs a;
+    uint32_t op_begin = 0;    // into Plan::ops
+    uint32_t mat_begin = 0;   // into Plan::mats (matrix index)
+};
+
+struct Plan {
+    uint32_t n = 0;
+    std::vector<Pass> passes;
+    std::vector<TileOp> ops;
+    std::vector<double> mats;        // 8 doubles per matrix
+    std::vector<int64_t> slot_param; // overlap slot -> parameter index
+    uint32_t n_slots = 0;
+};
+
+struct PlanOpts {
+    int tile_qubits = 12;   // k
+    int low_qubits = 5;     // always-local contiguous low qubits
+    bool merge_1q = true;   // multiply consecutive 1q gates on one qubit
+    bool backward = false;  // adjoint reverse sweep: inverse gates + overlaps
+    int max_items = 768;    // bound on ops per pass (shared-memory budget)
+};
+
+int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, Plan &plan);
+// Default tile/low widths for a state.
+void default_tiling(uint32_t n, int dtype, int requested_tile, int *tile, int *low);
+
+// ---- launchers (kernels in *.cu) ------------------------------------------
+// Unfused single-gate sweeps.
+int launch_gate1(qf_sv *sv, const BGate &g);
+int launch_gate2(qf_sv *sv, const BGate &g);
+// Upload a plan's ops+matrices into the context workspace and run every pass.
+int run_plan(qf_sv *sv, const Plan &plan);
+// Backward adjoint passes on (psi, lambda); overlap partials per slot are
+// accumulated into d_slot_sums (f64, plan.n_slots entries, not cleared here).
+int run_plan_dual(qf_sv *psi, qf_sv *lambda, const Plan &plan, double *d_slot_sums);
+
+// Reductions (results to host unless noted).
+int reduce_norm_sqr(qf_sv *sv, double *out);
+int reduce_probabilities(qf_sv *sv, double *d_out);  // device output
+int reduce_expect_z_all(qf_sv *sv, double *out);     // n values
+int reduce_expect_1q(qf_sv *sv, int obs, uint32_t q, double *out);
+int reduce_p_one(qf_sv *sv, uint32_t q, double *out);
+int collapse(qf_sv *sv, uint32_t q, int outcome, double scale);
+// Pauli sums: <psi|H|psi> (complex), and lambda = H psi with <psi|lambda>.
+int pauli_expectation(qf_sv *sv, const qf_pauli_term *terms, uint64_t n_terms, double out[2]);
+int pauli_apply(qf_sv *psi, qf_sv *lambda, const qf_pauli_term *terms, uint64_t n_terms, double *energy);
+// Fill/convert.
+int fill_zero_state(qf_sv *sv);
+int convert_from_f64(qf_sv *sv, const double *d_src);
+int convert_to_f64(qf_sv *sv, double *d_dst);
+// Sampler.
+int sample_shots(qf_sv *sv, const uint32_t *qubits, const uint32_t *cbits, uint32_t m, uint64_t shots,
+                 uint64_t seed, double tie_eps, uint64_t *outcomes_host, uint64_t *n_ties);
+
+// SmallRng jump-ahead (host): state advanced by `steps` calls of next_u64.
+uint64_t rng_jump(uint64_t state, uint64_t steps);
+void rng_jump_matrices(uint64_t stride, uint64_t (*mats)[64], int count);
+
+// Dispatcher for a bound gate list on a resident state.
+int execute_gates(qf_sv *sv, const std::vector<BGate> &gates, const qf_exec_opts *opts);
+
+}  // namespace qf

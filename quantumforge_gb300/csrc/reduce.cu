@@ -1,0 +1,728 @@
+// reduce.cu — reductions over a resident state: norm, probabilities, <Z_q>
+// for every qubit in one pass, one-qubit X/Y/Z expectations, measurement
+// probability and collapse, Pauli-sum expectations and lambda = H psi.
+//
+// Every sum is accumulated in f64 from the first block-level partial on;
+// complex64 states form the per-thread partial over a short contiguous chunk
+// (8-16 amplitudes) in f32 first. Two-stage reductions write one partial per
+// block and sum the partials in block order, so results are deterministic.
+#include <algorithm>
+#include <cstring>
+#include <map>
+
+#include "qf_device.cuh"
+#include "qf_internal.h"
+
+namespace qf {
+
+constexpr int kRedThreads = 256;
+constexpr int kRedBlocks = 512;  // power of two: the <Z> kernel reads index bits from the thread id
+
+// Sum `n_vals` values per block over `n_blocks` blocks, in block order.
+__global__ void k_final_sum(const double *__restrict__ partials, uint32_t n_blocks, uint32_t n_vals,
+                            double *__restrict__ out) {
+    for (uint32_t v = threadIdx.x; v < n_vals; v += blockDim.x) {
+        double s = 0.0;
+        for (uint32_t b = 0; b < n_blocks; ++b) s += partials[(size_t)b * n_vals + v];
+        out[v] = s;
+    }
+}
+
+static int finish_sum(qf_ctx *ctx, const double *d_partials, uint32_t n_blocks, uint32_t n_vals, double *host_out) {
+    k_final_sum<<<1, 128, 0, ctx->stream>>>(d_partials, n_blocks, n_vals, ctx->d_small);
+    QF_CUDA(cudaGetLastError());
+    QF_CUDA(cudaMemcpyAsync(ctx->h_small, ctx->d_small, sizeof(double) * n_vals, cudaMemcpyDeviceToHost, ctx->stream));
+    QF_CUDA(cudaStreamSynchronize(ctx->stream));
+    std::copy(ctx->h_small, ctx->h_small + n_vals, host_out);
+    return QF_OK;
+}
+
+static int partials_buffer(qf_ctx *ctx, size_t doubles, double **out) {
+    QF_TRY(ensure_device(&ctx->ws_red, &ctx->ws_red_bytes, doubles * sizeof(double)));
+    *out = static_cast<double *>(ctx->ws_red);
+    return QF_OK;
+}
+
+template <typename C> __device__ __forceinline__ typename Real<C>::T nsq(C a) { return a.x * a.x + a.y * a.y; }
+
+// ---- state fill / conversion ---------------------------------------------
+template <typename C> __global__ void k_set_first_one(C *a) { a[0] = mk((typename Real<C>::T)1, (typename Real<C>::T)0); }
+
+int fill_zero_state(qf_sv *sv) {
+    QF_CUDA(cudaMemsetAsync(sv->d, 0, sv->bytes(), sv->ctx->stream));
+    if (sv->dtype == QF_C64) k_set_first_one<float2><<<1, 1, 0, sv->ctx->stream>>>(static_cast<float2 *>(sv->d));
+    else k_set_first_one<double2><<<1, 1, 0, sv->ctx->stream>>>(static_cast<double2 *>(sv->d));
+    QF_CUDA(cudaGetLastError());
+    return QF_OK;
+}
+
+__global__ void k_f64_to_c64(const double2 *__restrict__ src, float2 *__restrict__ dst, uint64_t count) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count; i += (uint64_t)gridDim.x * blockDim.x) {
+        const double2 v = src[i];
+        dst[i] = make_float2((float)v.x, (float)v.y);
+    }
+}
+__global__ void k_c64_to_f64(const float2 *__restrict__ src, double2 *__restrict__ dst, uint64_t count) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count; i += (uint64_t)gridDim.x * blockDim.x) {
+        const float2 v = src[i];
+        dst[i] = make_double2((double)v.x, (double)v.y);
+    }
+}
+
+// Host f64 amplitudes -> device state (chunked through a device staging buffer).
+int convert_from_f64(qf_sv *sv, const double *host) {
+    qf_ctx *ctx = sv->ctx;
+    if (sv->dtype == QF_C128) {
+        QF_CUDA(cudaMemcpyAsync(sv->d, host, sv->bytes(), cudaMemcpyHostToDevice, ctx->stream));
+        return QF_OK;
+    }
+    const uint64_t chunk = std::min<uint64_t>(sv->dim, 1ULL << 24);  // amplitudes per chunk (256 MiB staging)
+    QF_TRY(ensure_device(&ctx->ws_stage, &ctx->ws_stage_bytes, chunk * 16));
+    for (uint64_t off = 0; off < sv->dim; off += chunk) {
+        const uint64_t cnt = std::min(chunk, sv->dim - off);
+        QF_CUDA(cudaMemcpyAsync(ctx->ws_stage, host + 2 * off, cnt * 16, cudaMemcpyHostToDevice, ctx->stream));
+        k_f64_to_c64<<<std::max<uint64_t>(1, std::min<uint64_t>((cnt + 255) / 256, 4096)), 256, 0, ctx->stream>>>(
+            static_cast<const double2 *>(ctx->ws_stage), static_cast<float2 *>(sv->d) + off, cnt);
+        QF_CUDA(cudaGetLastError());
+    }
+    return QF_OK;
+}
+
+int convert_to_f64(qf_sv *sv, double *host) {
+    qf_ctx *ctx = sv->ctx;
+    if (sv->dtype == QF_C128) {
+        QF_CUDA(cudaMemcpyAsync(host, sv->d, sv->bytes(), cudaMemcpyDeviceToHost, ctx->stream));
+        QF_CUDA(cudaStreamSynchronize(ctx->stream));
+        return QF_OK;
+    }
+    const uint64_t chunk = std::min<uint64_t>(sv->dim, 1ULL << 24);
+    QF_TRY(ensure_device(&ctx->ws_stage, &ctx->ws_stage_bytes, chunk * 16));
+    for (uint64_t off = 0; off < sv->dim; off += chunk) {
+        const uint64_t cnt = std::min(chunk, sv->dim - off);
+        k_c64_to_f64<<<std::max<uint64_t>(1, std::min<uint64_t>((cnt + 255) / 256, 4096)), 256, 0, ctx->stream>>>(
+            static_cast<const float2 *>(sv->d) + off, static_cast<double2 *>(ctx->ws_stage), cnt);
+        QF_CUDA(cudaGetLastError());
+        QF_CUDA(cudaMemcpyAsync(host + 2 * off, ctx->ws_stage, cnt * 16, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    QF_CUDA(cudaStreamSynchronize(ctx->stream));
+    return QF_OK;
+}
+
+// ---- norm / probabilities --------------------------------------------------
+template <typename C>
+__global__ void k_norm(const C *__restrict__ a, uint64_t dim, double *__restrict__ partials) {
+    __shared__ double red[32];
+    double s = 0.0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < dim; i += (uint64_t)gridDim.x * blockDim.x)
+        s += (double)nsq(a[i]);
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+int reduce_norm_sqr(qf_sv *sv, double *out) {
+    qf_ctx *ctx = sv->ctx;
+    double *p;
+    QF_TRY(partials_buffer(ctx, kRedBlocks, &p));
+    if (sv->dtype == QF_C64) k_norm<float2><<<kRedBlocks, kRedThreads, 0, ctx->stream>>>(static_cast<float2 *>(sv->d), sv->dim, p);
+    else k_norm<double2><<<kRedBlocks, kRedThreads, 0, ctx->stream>>>(static_cast<double2 *>(sv->d), sv->dim, p);
+    QF_CUDA(cudaGetLastError());
+    return finish_sum(ctx, p, kRedBlocks, 1, out);
+}
+
+// StateVector::probabilities (src/lib.rs:1144-1146): |a_i|^2 per index.
+template <typename C>
+__global__ void k_probs(const C *__restrict__ a, uint64_t dim, double *__restrict__ out) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < dim; i += (uint64_t)gridDim.x * blockDim.x) {
+        const C v = a[i];
+        out[i] = (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+    }
+}
+
+int reduce_probabilities(qf_sv *sv, double *d_out) {
+    qf_ctx *ctx = sv->ctx;
+    const int grid = std::max(1, std::min<int>((int)((sv->dim + 255) / 256), ctx->sm_count * 8));
+    if (sv->dtype == QF_C64) k_probs<float2><<<grid, 256, 0, ctx->stream>>>(static_cast<float2 *>(sv->d), sv->dim, d_out);
+    else k_probs<double2><<<grid, 256, 0, ctx->stream>>>(static_cast<double2 *>(sv->d), sv->dim, d_out);
+    QF_CUDA(cudaGetLastError());
+    return QF_OK;
+}
+
+// ---- <Z_q> for every qubit in one HBM pass --------------------------------
+// Each thread takes chunks of 2^CH contiguous amplitudes. Inside a chunk the
+// per-bit sums of bits < CH are a small tree; bits CH..CH+S-1 (S = log2 of the
+// total thread count) are fixed by the thread id; the higher bits are fixed
+// per loop iteration and take the chunk total. partials[block][q] holds the
+// sum of p over indices with bit q set; partials[block][n] the total.
+template <typename C, int CH>
+__global__ void __launch_bounds__(kRedThreads)
+    k_expect_z_all(const C *__restrict__ a, uint32_t n, uint32_t s_log, double *__restrict__ partials) {
+    using R = typename Real<C>::T;
+    __shared__ double red[32];
+    const uint64_t gtid = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const uint64_t stride = 1ULL << s_log;
+    const uint64_t nchunks = 1ULL << (n - CH);
+    double tot = 0.0, lowsum[CH], hisum[64];
+#pragma unroll
+    for (int b = 0; b < CH; ++b) lowsum[b] = 0.0;
+    const uint32_t nhi = n > CH + s_log ? n - CH - s_log : 0;
+    for (uint32_t r = 0; r < nhi; ++r) hisum[r] = 0.0;
+    uint64_t it = 0;
+    for (uint64_t c = gtid; c < nchunks; c += stride, ++it) {
+        R p[1 << CH];
+        const C *src = a + (c << CH);
+#pragma unroll
+        for (int j = 0; j < (1 << CH); ++j) p[j] = nsq(src[j]);
+        R t = 0;
+#pragma unroll
+        for (int j = 0; j < (1 << CH); ++j) t += p[j];
+        tot += (double)t;
+#pragma unroll
+        for (int b = 0; b < CH; ++b) {
+            R s = 0;
+#pragma unroll
+            for (int j = 0; j < (1 << CH); ++j)
+                if ((j >> b) & 1) s += p[j];
+            lowsum[b] += (double)s;
+        }
+        for (uint32_t r = 0; r < nhi; ++r)
+            if ((it >> r) & 1ULL) hisum[r] += (double)t;
+    }
+    for (uint32_t q = 0; q <= n; ++q) {
+        double v;
+        if (q == n) v = tot;
+        else if (q < CH) v = lowsum[q];
+        else if (q < CH + s_log) v = ((gtid >> (q - CH)) & 1ULL) ? tot : 0.0;
+        else v = hisum[q - CH - s_log];
+        v = block_sum(v, red);
+        if (threadIdx.x == 0) partials[(size_t)blockIdx.x * (n + 1) + q] = v;
+    }
+}
+
+// Tiny states: one thread.
+template <typename C>
+__global__ void k_expect_z_small(const C *__restrict__ a, uint32_t n, double *__restrict__ partials) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double s[65];
+    for (uint32_t q = 0; q <= n; ++q) s[q] = 0.0;
+    for (uint64_t i = 0; i < (1ULL << n); ++i) {
+        const double p = (double)a[i].x * (double)a[i].x + (double)a[i].y * (double)a[i].y;
+        s[n] += p;
+        for (uint32_t q = 0; q < n; ++q)
+            if ((i >> q) & 1ULL) s[q] += p;
+    }
+    for (uint32_t q = 0; q <= n; ++q) partials[q] = s[q];
+}
+
+int reduce_expect_z_all(qf_sv *sv, double *out) {
+    qf_ctx *ctx = sv->ctx;
+    const uint32_t n = sv->n;
+    double *p;
+    QF_TRY(partials_buffer(ctx, (size_t)kRedBlocks * (n + 1), &p));
+    uint32_t blocks = 1;
+    const int ch = sv->dtype == QF_C64 ? 4 : 3;
+    if ((int)n < ch + 5) {
+        if (sv->dtype == QF_C64) k_expect_z_small<float2><<<1, 32, 0, ctx->stream>>>(static_cast<float2 *>(sv->d), n, p);
+        else k_expect_z_small<double2><<<1, 32, 0, ctx->stream>>>(static_cast<double2 *>(sv->d), n, p);
+    } else {
+        // threads = min(kRedBlocks * kRedThreads, chunks), a power of two
+        uint32_t s_log = 0;
+        const uint32_t max_log = 17;  // log2(kRedBlocks * kRedThreads)
+        s_log = std::min<uint32_t>(max_log, n - ch);
+        const uint32_t threads_total = 1u << s_log;
+        const uint32_t tpb = std::min<uint32_t>(kRedThreads, threads_total);
+        blocks = threads_total / tpb;
+        if (sv->dtype == QF_C64)
+            k_expect_z_all<float2, 4><<<blocks, tpb, 0, ctx->stream>>>(static_cast<float2 *>(sv->d), n, s_log, p);
+        else
+            k_expect_z_all<double2, 3><<<blocks, tpb, 0, ctx->stream>>>(static_cast<double2 *>(sv->d), n, s_log, p);
+    }
+    QF_CUDA(cudaGetLastError());
+    std::vector<double> sums(n + 1);
+    QF_TRY(finish_sum(ctx, p, blocks, n + 1, sums.data()));
+    for (uint32_t q = 0; q < n; ++q) out[q] = sums[n] - 2.0 * sums[q];
+    return QF_OK;
+}
+
+// ---- one-qubit expectations, P(q = 1), collapse --------------------------
+// mode 0: 2 sum Re(conj(a0) a1) (<X>), 1: 2 sum Im(conj(a0) a1) (<Y>),
+// 2: sum |a0|^2 - |a1|^2 (<Z>), 3: sum |a1|^2 (P(q=1)); a0/a1 = bit clear/set.
+template <typename C>
+__global__ void k_pair_reduce(const C *__restrict__ a, uint64_t n_pairs, uint32_t q, int mode,
+                              double *__restrict__ partials) {
+    __shared__ double red[32];
+    const uint64_t mask = 1ULL << q;
+    double s = 0.0;
+    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n_pairs; p += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t i0 = insert0(p, q);
+        const C a0 = a[i0], a1 = a[i0 | mask];
+        double v;
+        if (mode == 0) v = 2.0 * ((double)a0.x * a1.x + (double)a0.y * a1.y);
+        else if (mode == 1) v = 2.0 * ((double)a0.x * a1.y - (double)a0.y * a1.x);
+        else if (mode == 2) v = ((double)a0.x * a0.x + (double)a0.y * a0.y) - ((double)a1.x * a1.x + (double)a1.y * a1.y);
+        else v = (double)a1.x * a1.x + (double)a1.y * a1.y;
+        s += v;
+    }
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+static int pair_reduce(qf_sv *sv, uint32_t q, int mode, double *out) {
+    qf_ctx *ctx = sv->ctx;
+    double *p;
+    QF_TRY(partials_buffer(ctx, kRedBlocks, &p));
+    const uint64_t pairs = sv->dim / 2;
+    const uint32_t blocks = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(kRedBlocks, (pairs + 255) / 256));
+    if (sv->dtype == QF_C64)
+        k_pair_reduce<float2><<<blocks, kRedThreads, 0, ctx->stream>>>(static_cast<float2 *>(sv->d), pairs, q, mode, p);
+    else
+        k_pair_reduce<double2><<<blocks, kRedThreads, 0, ctx->stream>>>(static_cast<double2 *>(sv->d), pairs, q, mode, p);
+    QF_CUDA(cudaGetLastError());
+    return finish_sum(ctx, p, blocks, 1, out);
+}
+
+int reduce_expect_1q(qf_sv *sv, int obs, uint32_t q, double *out) {
+    const int mode = obs == QF_PAULI_X ? 0 : obs == QF_PAULI_Y ? 1 : 2;
+    return pair_reduce(sv, q, mode, out);
+}
+
+int reduce_p_one(qf_sv *sv, uint32_t q, double *out) { return pair_reduce(sv, q, 3, out); }
+
+// Collapse after measure (src/lib.rs:1341-1350): amplitudes whose bit differs
+// from the outcome become 0, the others are divided by `scale`.
+template <typename C>
+__global__ void k_collapse(C *__restrict__ a, uint64_t dim, uint32_t q, int outcome, double scale) {
+    using R = typename Real<C>::T;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < dim; i += (uint64_t)gridDim.x * blockDim.x) {
+        if ((int)((i >> q) & 1ULL) != outcome) a[i] = mk((R)0, (R)0);
+        else a[i] = mk((R)((double)a[i].x / scale), (R)((double)a[i].y / scale));
+    }
+}
+
+int collapse(qf_sv *sv, uint32_t q, int outcome, double scale) {
+    qf_ctx *ctx = sv->ctx;
+    const int grid = std::max(1, std::min<int>((int)((sv->dim + 255) / 256), ctx->sm_count * 8));
+    if (sv->dtype == QF_C64) k_collapse<float2><<<grid, 256, 0, ctx->stream>>>(static_cast<float2 *>(sv->d), sv->dim, q, outcome, scale);
+    else k_collapse<double2><<<grid, 256, 0, ctx->stream>>>(static_cast<double2 *>(sv->d), sv->dim, q, outcome, scale);
+    QF_CUDA(cudaGetLastError());
+    return QF_OK;
+}
+
+// ---- Pauli sums --------------------------------------------------------------
+// Terms are grouped by x-mask. For one group, G_x(i) = sum_t c_t * i^{ny_t} *
+// (-1)^{popcount(i & z_t)} is the phase PauliWord::apply_basis_index gives
+// basis state i (src/analytic.rs:2629-2650), so
+//   <psi|H_x|psi> = sum_i conj(psi_{i^x}) G_x(i) psi_i,  (H_x psi)_j = G_x(j^x) psi_{j^x}.
+// A pass keeps every x-bit of its groups tile-resident, so each partner
+// amplitude is in shared memory.
+struct PTerm {
+    uint64_t z;
+    double cre, cim;  // coefficient times i^{ny}
+};
+struct PGroup {
+    uint64_t x;        // global x-mask
+    uint32_t xl;       // the same mask in local tile bits
+    uint32_t t_begin;  // into the pass's term array
+    uint32_t t_count;
+    uint32_t pad;
+};
+struct PPassArgs {
+    uint64_t nonlocal_mask;
+    uint64_t n_tiles;
+    uint32_t k, low, n_groups, n_terms;
+    uint32_t mode;  // 0 = expectation, 1 = write lambda, 2 = accumulate lambda
+    uint32_t last;  // accumulate <psi|lambda> (mode 1/2)
+    uint8_t hi_q[kMaxLocal];
+};
+
+template <typename C>
+__global__ void __launch_bounds__(kRedThreads)
+    k_pauli_pass(const C *__restrict__ psi, C *__restrict__ lam, const PPassArgs pa, const PGroup *__restrict__ g_groups,
+                 const PTerm *__restrict__ g_terms, double *__restrict__ partials) {
+    using R = typename Real<C>::T;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t T = 1u << pa.k, nhi = pa.k - pa.low;
+    C *s = reinterpret_cast<C *>(smem);
+    uint64_t *hi_off = reinterpret_cast<uint64_t *>(smem + (size_t)T * sizeof(C));
+    PGroup *groups = reinterpret_cast<PGroup *>(hi_off + (1u << nhi));
+    PTerm *terms = reinterpret_cast<PTerm *>(groups + pa.n_groups);
+    __shared__ double red[32];
+    for (uint32_t h = threadIdx.x; h < (1u << nhi); h += blockDim.x) {
+        uint64_t off = 0;
+        for (uint32_t r = 0; r < nhi; ++r)
+            if ((h >> r) & 1u) off |= 1ULL << pa.hi_q[r];
+        hi_off[h] = off;
+    }
+    for (uint32_t g = threadIdx.x; g < pa.n_groups; g += blockDim.x) groups[g] = g_groups[g];
+    for (uint32_t t = threadIdx.x; t < pa.n_terms; t += blockDim.x) terms[t] = g_terms[t];
+    __syncthreads();
+    const uint32_t lowmask = (1u << pa.low) - 1;
+    double acc_re = 0.0, acc_im = 0.0;
+    for (uint64_t t = blockIdx.x; t < pa.n_tiles; t += gridDim.x) {
+        const uint64_t base = deposit(t, pa.nonlocal_mask);
+        for (uint32_t j = threadIdx.x; j < T; j += blockDim.x) s[j] = psi[base | hi_off[j >> pa.low] | (j & lowmask)];
+        __syncthreads();
+        for (uint32_t j = threadIdx.x; j < T; j += blockDim.x) {
+            const uint64_t gi = base | hi_off[j >> pa.low] | (j & lowmask);
+            R er = 0, ei = 0;
+            for (uint32_t g = 0; g < pa.n_groups; ++g) {
+                const PGroup G = groups[g];
+                // phase evaluated at the source index of the matrix element
+                const uint64_t src = pa.mode == 0 ? gi : (gi ^ G.x);
+                R gr = 0, gim = 0;
+                for (uint32_t q = 0; q < G.t_count; ++q) {
+                    const PTerm P = terms[G.t_begin + q];
+                    const R sg = (__popcll(src & P.z) & 1) ? R(-1) : R(1);
+                    gr += sg * (R)P.cre;
+                    gim += sg * (R)P.cim;
+                }
+                const C a = s[j ^ G.xl];
+                if (pa.mode == 0) {
+                    // conj(psi_{j^x}) * G * psi_j
+                    const C b = s[j];
+                    const R pr = gr * b.x - gim * b.y, pim = gr * b.y + gim * b.x;
+                    er += a.x * pr + a.y * pim;
+                    ei += a.x * pim - a.y * pr;
+                } else {
+                    er += gr * a.x - gim * a.y;
+                    ei += gr * a.y + gim * a.x;
+                }
+            }
+            if (pa.mode == 0) {
+                acc_re += (double)er;
+                acc_im += (double)ei;
+            } else {
+                if (pa.mode == 2) {
+                    const C old = lam[gi];
+                    er += old.x;
+                    ei += old.y;
+                }
+                lam[gi] = mk(er, ei);
+                if (pa.last) {
+                    const C b = s[j];  // conj(psi_j) * lambda_j
+                    acc_re += (double)b.x * (double)er + (double)b.y * (double)ei;
+                    acc_im += (double)b.x * (double)ei - (double)b.y * (double)er;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    acc_re = block_sum(acc_re, red);
+    if (threadIdx.x == 0) partials[2 * blockIdx.x] = acc_re;
+    acc_im = block_sum(acc_im, red);
+    if (threadIdx.x == 0) partials[2 * blockIdx.x + 1] = acc_im;
+}
+
+namespace {
+struct PPassHost {
+    PPassArgs a;
+    std::vector<PGroup> groups;
+    std::vector<PTerm> terms;
+};
+
+int plan_pauli(uint32_t n, int dtype, const qf_pauli_term *terms, uint64_t n_terms, std::vector<PPassHost> &passes) {
+    const uint64_t valid = n >= 64 ? ~0ULL : ((1ULL << n) - 1);
+    std::map<uint64_t, std::vector<PTerm>> by_x;
+    for (uint64_t t = 0; t < n_terms; ++t) {
+        const qf_pauli_term &P = terms[t];
+        if ((P.xmask | P.zmask) & ~valid)
+            return fail(QF_ERR_QUBIT_OUT_OF_RANGE, "Pauli term %llu acts outside %u qubits", (unsigned long long)t, n);
+        const int ny = __builtin_popcountll(P.xmask & P.zmask) & 3;
+        double re = P.coeff_re, im = P.coeff_im;
+        for (int r = 0; r < ny; ++r) {  // multiply by i
+            const double t2 = re;
+            re = -im;
+            im = t2;
+        }
+        by_x[P.xmask].push_back(PTerm{P.zmask, re, im});
+    }
+    int k, low;
+    default_tiling(n, dtype, 0, &k, &low);
+    const uint64_t low_mask = (1ULL << low) - 1;
+    std::vector<std::pair<uint64_t, std::vector<PTerm>>> groups(by_x.begin(), by_x.end());
+    std::vector<bool> done(groups.size(), false);
+    size_t left = groups.size();
+    while (left) {
+        uint64_t L = low_mask;
+        std::vector<size_t> sel;
+        for (size_t g = 0; g < groups.size(); ++g) {
+            if (done[g]) continue;
+            const uint64_t nl = L | groups[g].first;
+            if (__builtin_popcountll(nl) <= k) {
+                L = nl;
+                sel.push_back(g);
+            }
+        }
+        if (sel.empty()) return fail(QF_ERR_UNSUPPORTED_OPERATION, "Pauli term spans more than %d qubits", k);
+        for (uint32_t q = 0; q < n && __builtin_popcountll(L) < k; ++q) L |= 1ULL << q;
+        PPassHost P;
+        std::memset(&P.a, 0, sizeof P.a);
+        uint32_t lo_eff = 0;
+        while (lo_eff < n && ((L >> lo_eff) & 1ULL)) ++lo_eff;
+        std::vector<int> lbit(n, -1);
+        for (uint32_t q = 0; q < lo_eff; ++q) lbit[q] = (int)q;
+        uint32_t r = 0;
+        for (uint32_t q = lo_eff; q < n; ++q)
+            if ((L >> q) & 1ULL) {
+                if (r >= (uint32_t)kMaxLocal) return fail(QF_ERR_UNSUPPORTED_OPERATION, "Pauli pass too wide");
+                P.a.hi_q[r] = (uint8_t)q;
+                lbit[q] = (int)(lo_eff + r++);
+            }
+        P.a.k = lo_eff + r;
+        P.a.low = lo_eff;
+        P.a.nonlocal_mask = valid & ~L;
+        P.a.n_tiles = 1ULL << (n - P.a.k);
+        for (size_t g : sel) {
+            done[g] = true;
+            --left;
+            PGroup G;
+            G.x = groups[g].first;
+            G.xl = 0;
+            for (uint32_t q = 0; q < n; ++q)
+                if ((G.x >> q) & 1ULL) G.xl |= 1u << lbit[q];
+            G.t_begin = (uint32_t)P.terms.size();
+            G.t_count = (uint32_t)groups[g].second.size();
+            G.pad = 0;
+            P.terms.insert(P.terms.end(), groups[g].second.begin(), groups[g].second.end());
+            P.groups.push_back(G);
+        }
+        P.a.n_groups = (uint32_t)P.groups.size();
+        P.a.n_terms = (uint32_t)P.terms.size();
+        passes.push_back(std::move(P));
+    }
+    return QF_OK;
+}
+
+template <typename C>
+int run_pauli(qf_sv *psi, qf_sv *lam, std::vector<PPassHost> &passes, bool apply, double out[2]) {
+    qf_ctx *ctx = psi->ctx;
+    static bool attr_done[64] = {false};
+    if (!attr_done[ctx->device & 63]) {
+        QF_CUDA(cudaFuncSetAttribute(k_pauli_pass<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->smem_optin));
+        attr_done[ctx->device & 63] = true;
+    }
+    size_t meta = 0;
+    for (auto &P : passes) meta += P.groups.size() * sizeof(PGroup) + P.terms.size() * sizeof(PTerm) + 64;
+    QF_TRY(ensure_device(&ctx->ws_plan, &ctx->ws_plan_bytes, meta));
+    const uint32_t grid = (uint32_t)ctx->sm_count * 2;
+    double *partials;
+    QF_TRY(partials_buffer(ctx, (size_t)2 * grid * passes.size(), &partials));
+    unsigned char *dmeta = static_cast<unsigned char *>(ctx->ws_plan);
+    size_t off = 0;
+    for (size_t i = 0; i < passes.size(); ++i) {
+        PPassHost &P = passes[i];
+        P.a.mode = apply ? (i == 0 ? 1u : 2u) : 0u;
+        P.a.last = (apply && i + 1 == passes.size()) ? 1u : 0u;
+        PGroup *dg = reinterpret_cast<PGroup *>(dmeta + off);
+        QF_CUDA(cudaMemcpyAsync(dg, P.groups.data(), P.groups.size() * sizeof(PGroup), cudaMemcpyHostToDevice, ctx->stream));
+        off += (P.groups.size() * sizeof(PGroup) + 15) / 16 * 16;
+        PTerm *dt = reinterpret_cast<PTerm *>(dmeta + off);
+        QF_CUDA(cudaMemcpyAsync(dt, P.terms.data(), P.terms.size() * sizeof(PTerm), cudaMemcpyHostToDevice, ctx->stream));
+        off += (P.terms.size() * sizeof(PTerm) + 15) / 16 * 16;
+        const size_t smem = ((size_t)1 << P.a.k) * sizeof(C) + (8u << (P.a.k - P.a.low)) + P.groups.size() * sizeof(PGroup) +
+                            P.terms.size() * sizeof(PTerm);
+        if (smem > ctx->smem_optin) return fail(QF_ERR_UNSUPPORTED_OPERATION, "Pauli pass needs too much shared memory");
+        const uint32_t g = (uint32_t)std::min<uint64_t>(grid, P.a.n_tiles);
+        // unused partial slots of this pass stay zero
+        QF_CUDA(cudaMemsetAsync(partials + (size_t)2 * grid * i, 0, sizeof(double) * 2 * grid, ctx->stream));
+        k_pauli_pass<C><<<g, kRedThreads, smem, ctx->stream>>>(static_cast<const C *>(psi->d),
+                                                               lam ? static_cast<C *>(lam->d) : nullptr, P.a, dg, dt,
+                                                               partials + (size_t)2 * grid * i);
+        QF_CUDA(cudaGetLastError());
+    }
+    // expectation: sum over every pass; apply: only the last pass carries <psi|lambda>
+    const size_t first = apply ? passes.size() - 1 : 0;
+    const uint32_t nblk = (uint32_t)(grid * (passes.size() - first));
+    k_final_sum<<<1, 128, 0, ctx->stream>>>(partials + 2 * grid * first, nblk, 2, ctx->d_small);
+    QF_CUDA(cudaGetLastError());
+    QF_CUDA(cudaMemcpyAsync(ctx->h_small, ctx->d_small, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    QF_CUDA(cudaStreamSynchronize(ctx->stream));
+    out[0] = ctx->h_small[0];
+    out[1] = ctx->h_small[1];
+    return QF_OK;
+}
+}  // namespace
+
+int pauli_expectation(qf_sv *sv, const qf_pauli_term *terms, uint64_t n_terms, double out[2]) {
+    out[0] = out[1] = 0.0;
+    if (n_terms == 0) return QF_OK;
+    std::vector<PPassHost> passes;
+    QF_TRY(plan_pauli(sv->n, sv->dtype, terms, n_terms, passes));
+    if (sv->dtype == QF_C64) return run_pauli<float2>(sv, nullptr, passes, false, out);
+    return run_pauli<double2>(sv, nullptr, passes, false, out);
+}
+
+int pauli_apply(qf_sv *psi, qf_sv *lam, const qf_pauli_term *terms, uint64_t n_terms, double *energy) {
+    if (n_terms == 0) {
+        QF_CUDA(cudaMemsetAsync(lam->d, 0, lam->bytes(), psi->ctx->stream));
+        if (energy) *energy = 0.0;
+        return QF_OK;
+    }
+    std::vector<PPassHost> passes;
+    QF_TRY(plan_pauli(psi->n, psi->dtype, terms, n_terms, passes));
+    double out[2];
+    if (psi->dtype == QF_C64) QF_TRY(run_pauli<float2>(psi, lam, passes, true, out));
+    else QF_TRY(run_pauli<double2>(psi, lam, passes, true, out));
+    if (energy) *energy = out[0];
+    return QF_OK;
+}
+
+// ---- sampler -----------------------------------------------------------------
+// Terminal measurements of qubits q_0..q_{m-1} (distinct). J_m[b] is the
+// probability mass of the indices whose measured bits spell b (bit j = bit
+// q_j); level k of the tree sums level k+1 over the outcome of q_k. A shot
+// starts its SmallRng at draw s*m (the reference's shot-major order,
+// src/lib.rs:2874-2912) via jump matrices and descends the tree:
+// p_one = J_{k+1}(b | 1<<k) / D, D = product of the chosen branch
+// probabilities, which is the reference's successive renormalisation
+// (src/lib.rs:1329-1350) up to rounding; |u - p_one| < tie_eps is reported.
+template <typename C>
+__global__ void k_marginal(const C *__restrict__ a, uint32_t n, const uint32_t *__restrict__ mq, uint32_t m,
+                           uint64_t rest_mask, double *__restrict__ leaf) {
+    const uint64_t nb = 1ULL << m, nu = 1ULL << (n - m);
+    for (uint64_t b = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; b < nb; b += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t idx = 0;
+        for (uint32_t j = 0; j < m; ++j)
+            if ((b >> j) & 1ULL) idx |= 1ULL << mq[j];
+        double s = 0.0;
+        for (uint64_t u = 0; u < nu; ++u) {
+            const C v = a[idx | deposit(u, rest_mask)];
+            s += (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+        }
+        leaf[b] = s;
+    }
+}
+
+// level k (2^k entries at offset 2^k - 1) from level k+1
+__global__ void k_tree_level(double *tree, uint32_t k) {
+    const uint64_t cnt = 1ULL << k;
+    double *dst = tree + (cnt - 1), *src = tree + (2 * cnt - 1);
+    for (uint64_t b = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; b < cnt; b += (uint64_t)gridDim.x * blockDim.x)
+        dst[b] = src[b] + src[b | cnt];
+}
+
+__device__ __forceinline__ uint64_t gf2_apply(const uint64_t *cols, uint64_t x) {
+    uint64_t y = 0;
+    while (x) {
+        const int c = __ffsll((long long)x) - 1;
+        y ^= cols[c];
+        x &= x - 1;
+    }
+    return y;
+}
+
+__global__ void k_shots(const double *__restrict__ tree, uint32_t m, const uint32_t *__restrict__ cbits, uint64_t shots,
+                        uint64_t seed_state, const uint64_t *__restrict__ jump, double tie_eps,
+                        uint64_t *__restrict__ outcomes, unsigned long long *__restrict__ ties, int *__restrict__ err) {
+    for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < shots; s += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t x = seed_state;
+        for (int j = 0; j < 64; ++j)
+            if ((s >> j) & 1ULL) x = gf2_apply(jump + 64 * j, x);
+        uint64_t b = 0, reg = 0;
+        double D = 1.0;
+        unsigned long long nt = 0;
+        for (uint32_t k = 0; k < m; ++k) {
+            const double J1 = tree[((1ULL << (k + 1)) - 1) + (b | (1ULL << k))];
+            double p = J1 / D;
+            if (p < 0.0) p = 0.0;
+            if (p > 1.0) p = 1.0;
+            x ^= x << 13;
+            x ^= x >> 7;
+            x ^= x << 17;
+            const double u = (double)(x >> 11) * (1.0 / 9007199254740992.0);
+            const int o = u < p ? 1 : 0;
+            if (fabs(u - p) < tie_eps) ++nt;
+            const double prob = o ? p : 1.0 - p;
+            if (prob <= 2.220446049250313e-16) {
+                atomicOr(err, 1);
+                break;
+            }
+            D *= prob;
+            b |= (uint64_t)o << k;
+            reg = (reg & ~(1ULL << cbits[k])) | ((uint64_t)o << cbits[k]);
+        }
+        outcomes[s] = reg;
+        if (nt) atomicAdd(ties, nt);
+    }
+}
+
+int sample_shots(qf_sv *sv, const uint32_t *qubits, const uint32_t *cbits, uint32_t m, uint64_t shots, uint64_t seed,
+                 double tie_eps, uint64_t *outcomes_host, uint64_t *n_ties) {
+    qf_ctx *ctx = sv->ctx;
+    const uint32_t n = sv->n;
+    if (m > 30) return fail(QF_ERR_UNSUPPORTED_OPERATION, "at most 30 terminal measurements are supported, got %u", m);
+    uint64_t seen = 0;
+    for (uint32_t j = 0; j < m; ++j) {
+        if (qubits[j] >= n) return fail(QF_ERR_QUBIT_OUT_OF_RANGE, "qubit index %u is out of range for %u qubits", qubits[j], n);
+        if (cbits[j] >= 64) return fail(QF_ERR_UNSUPPORTED_OPERATION, "classical bit %u exceeds the packed 64-bit register", cbits[j]);
+        if ((seen >> qubits[j]) & 1ULL)
+            return fail(QF_ERR_UNSUPPORTED_OPERATION, "qubit %u is measured twice; repeated measurement needs the per-shot engine", qubits[j]);
+        seen |= 1ULL << qubits[j];
+    }
+    if (m == 0) {  // no measurement: every shot reads an empty register
+        if (outcomes_host) std::memset(outcomes_host, 0, sizeof(uint64_t) * shots);
+        if (n_ties) *n_ties = 0;
+        return QF_OK;
+    }
+    const uint64_t valid = n >= 64 ? ~0ULL : ((1ULL << n) - 1);
+    const uint64_t rest = valid & ~seen;
+    // workspace: tree (2^(m+1) doubles) | outcomes (shots u64) | jump (64*64 u64) | mq | cb | ties | err
+    const size_t tree_b = sizeof(double) * ((2ULL << m));
+    const size_t out_b = sizeof(uint64_t) * shots;
+    const size_t jump_b = sizeof(uint64_t) * 64 * 64;
+    const size_t meta_b = 2 * sizeof(uint32_t) * 32 + 64;
+    QF_TRY(ensure_device(&ctx->ws_tree, &ctx->ws_tree_bytes, tree_b + out_b + jump_b + meta_b));
+    unsigned char *w = static_cast<unsigned char *>(ctx->ws_tree);
+    double *tree = reinterpret_cast<double *>(w);
+    uint64_t *d_out = reinterpret_cast<uint64_t *>(w + tree_b);
+    uint64_t *d_jump = reinterpret_cast<uint64_t *>(w + tree_b + out_b);
+    uint32_t *d_mq = reinterpret_cast<uint32_t *>(w + tree_b + out_b + jump_b);
+    uint32_t *d_cb = d_mq + 32;
+    unsigned long long *d_ties = reinterpret_cast<unsigned long long *>(d_cb + 32);
+    int *d_err = reinterpret_cast<int *>(d_ties + 1);
+
+    static thread_local uint64_t jump[64][64];
+    rng_jump_matrices(m, jump, 64);
+    QF_CUDA(cudaMemcpyAsync(d_jump, jump, jump_b, cudaMemcpyHostToDevice, ctx->stream));
+    if (m) {
+        QF_CUDA(cudaMemcpyAsync(d_mq, qubits, sizeof(uint32_t) * m, cudaMemcpyHostToDevice, ctx->stream));
+        QF_CUDA(cudaMemcpyAsync(d_cb, cbits, sizeof(uint32_t) * m, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    QF_CUDA(cudaMemsetAsync(d_ties, 0, sizeof(unsigned long long) + sizeof(int) + 4, ctx->stream));
+    // leaves at offset 2^m - 1
+    double *leaf = tree + ((1ULL << m) - 1);
+    const uint64_t nb = 1ULL << m;
+    const int grid = std::max(1, std::min<int>((int)((nb + 255) / 256), ctx->sm_count * 8));
+    if (sv->dtype == QF_C64)
+        k_marginal<float2><<<grid, 256, 0, ctx->stream>>>(static_cast<float2 *>(sv->d), n, d_mq, m, rest, leaf);
+    else
+        k_marginal<double2><<<grid, 256, 0, ctx->stream>>>(static_cast<double2 *>(sv->d), n, d_mq, m, rest, leaf);
+    QF_CUDA(cudaGetLastError());
+    for (int k = (int)m - 1; k >= 0; --k) {
+        const uint64_t cnt = 1ULL << k;
+        k_tree_level<<<std::max(1, std::min<int>((int)((cnt + 255) / 256), ctx->sm_count * 8)), 256, 0, ctx->stream>>>(tree, (uint32_t)k);
+        QF_CUDA(cudaGetLastError());
+    }
+    const uint64_t seed_state = [&] {
+        uint64_t z = seed + 0x9E3779B97F4A7C15ULL;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+        z ^= z >> 31;
+        return z == 0 ? 0x9E3779B97F4A7C15ULL : z;
+    }();
+    const int sgrid = std::max(1, std::min<int>((int)((shots + 127) / 128), ctx->sm_count * 16));
+    k_shots<<<sgrid, 128, 0, ctx->stream>>>(tree, m, d_cb, shots, seed_state, d_jump, tie_eps, d_out, d_ties, d_err);
+    QF_CUDA(cudaGetLastError());
+    if (outcomes_host)
+        QF_CUDA(cudaMemcpyAsync(outcomes_host, d_out, out_b, cudaMemcpyDeviceToHost, ctx->stream));
+    QF_CUDA(cudaMemcpyAsync(ctx->h_small, d_ties, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    QF_CUDA(cudaStreamSynchronize(ctx->stream));
+    unsigned long long t;
+    int e;
+    std::memcpy(&t, ctx->h_small, sizeof t);
+    std::memcpy(&e, reinterpret_cast<unsigned char *>(ctx->h_small) + 8, sizeof e);
+    if (n_ties) *n_ties = t;
+    if (e) return fail(QF_ERR_INVALID_PROBABILITY, "a shot selected a measurement branch of probability <= f64::EPSILON");
+    return QF_OK;
+}
+
+}  // namespace qf

@@ -1,0 +1,127 @@
+"""C-ABI checks that need no GPU: the library loads, exports every symbol that
+include/qf.h declares, and its host-only logic (validation, planning,
+SmallRng jump-ahead) behaves."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle as O
+from quantumforge_gb300 import _abi as A
+from quantumforge_gb300 import _native
+from quantumforge_gb300 import workloads as W
+
+HEADER = Path(__file__).resolve().parent.parent / "include" / "qf.h"
+
+
+def header_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(qf_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_the_bound_signatures():
+    decl = header_functions()
+    assert decl, "no declarations parsed"
+    assert set(decl) == set(_native.SIGNATURES), set(decl) ^ set(_native.SIGNATURES)
+
+
+def test_library_exports_every_header_symbol(engine_lib):
+    lib = C.CDLL(str(_native.lib_path()))
+    for name in header_functions():
+        assert hasattr(lib, name), f"{name} missing from {_native.lib_path().name}"
+
+
+def test_abi_version_and_status_names(engine_lib):
+    assert engine_lib.qf_abi_version() == 1
+    for code, name in A.STATUS_NAMES.items():
+        got = engine_lib.qf_status_name(code).decode()
+        expect = "QF_OK" if code == 0 else "QF_ERR_" + re.sub(r"(?<!^)(?=[A-Z])", "_", name).upper()
+        assert got == expect, (code, got, expect)
+
+
+def test_struct_layouts_match_header():
+    assert C.sizeof(A.Op) == 24 and A.OP_DTYPE.itemsize == 24
+    assert C.sizeof(A.PauliTerm) == 32
+    assert A.Op.theta.offset == 16 and A.Op.param.offset == 12
+    assert C.sizeof(A.ExecOpts) == 16
+    assert C.sizeof(A.GradientOpts) == 48
+
+
+@pytest.mark.parametrize("seed,steps", [(0, 0), (1, 1), (42, 7), (721, 64), (991, 1000), (1234, 123457)])
+def test_rng_jump_equals_stepping(engine_lib, seed, steps):
+    r = O.Rng(seed)
+    start = r.state.value
+    for _ in range(steps):
+        r.next_u64()
+    assert engine_lib.qf_rng_jump(start, steps) == r.state.value
+
+
+def plan_stats(engine_lib, n, ops, params=None, tile=0, mode=A.EXEC_AUTO, dtype=A.C64):
+    p = None if params is None else np.ascontiguousarray(params, dtype=np.float64)
+    npass, ngate = C.c_uint64(), C.c_uint64()
+    o = A.ExecOpts(mode, tile, 0, 0)
+    st = engine_lib.qf_plan_stats(n, dtype, _native.ptr(ops), len(ops), _native.ptr(p), 0 if p is None else p.size,
+                                  None, 0, C.byref(o), C.byref(npass), C.byref(ngate))
+    return st, npass.value, ngate.value
+
+
+def test_plan_fuses_a_random_circuit(engine_lib):
+    ops = W.random_circuit(30, 40, 1, two_qubit="mixed")
+    st, npass, ngate = plan_stats(engine_lib, 30, ops)
+    assert st == 0 and ngate == len(ops)
+    st, unf, _ = plan_stats(engine_lib, 30, ops, mode=A.EXEC_UNFUSED)
+    assert unf == ngate
+    assert npass * 8 < ngate, (npass, ngate)
+    # wider tiles never need more passes
+    counts = [plan_stats(engine_lib, 30, ops, tile=k)[1] for k in (8, 10, 12, 14)]
+    assert counts == sorted(counts, reverse=True), counts
+
+
+def test_plan_small_state_is_one_pass(engine_lib):
+    ops = W.random_circuit(10, 20, 3, two_qubit="mixed")
+    st, npass, _ = plan_stats(engine_lib, 10, ops)
+    assert st == 0 and npass == 1
+
+
+def test_plan_diagonal_gates_need_no_residency(engine_lib):
+    # Rz and CZ on high qubits never force a new pass
+    recs = [(A.OP_GATE, A.GATE_RZ, q, 0, 0, 0.1 * q) for q in range(30)]
+    recs += [(A.OP_CZ, 0, q, 29 - q, 0, 0.0) for q in range(15)]
+    st, npass, _ = plan_stats(engine_lib, 30, A.ops_array(recs))
+    assert st == 0 and npass == 1
+
+
+@pytest.mark.parametrize(
+    "recs,params,kind",
+    [
+        ([(A.OP_GATE, A.GATE_H, 5, 0, 0, 0.0)], None, "QubitOutOfRange"),
+        ([(A.OP_CNOT, 0, 1, 1, 0, 0.0)], None, "InvalidQubitPair"),
+        ([(A.OP_CZ, 0, 0, 9, 0, 0.0)], None, "QubitOutOfRange"),
+        ([(A.OP_CHANNEL, 0, 0, 0, 0, 0.0)], None, "OperationRequiresDensityMatrix"),
+        ([(A.OP_MEASURE, 0, 0, 0, 0, 0.0)], None, "OperationRequiresShotExecution"),
+        ([(A.OP_ROTATION, A.PAULI_Y, 0, 0, 3, 0.0)], [0.1], "InvalidParameterCount"),
+        ([(A.OP_ROTATION, A.PAULI_Y, 0, 0, 0, 0.0)], [float("nan")], "NonFiniteParameter"),
+        ([(A.OP_GATE, 42, 0, 0, 0, 0.0)], None, "InvalidArgument"),
+    ],
+)
+def test_plan_validation_errors(engine_lib, recs, params, kind):
+    st, _, _ = plan_stats(engine_lib, 3, A.ops_array(recs), params=params)
+    assert A.STATUS_NAMES[st] == kind
+    assert engine_lib.qf_last_error().decode()
+
+
+def test_zero_qubits_rejected(engine_lib):
+    st, _, _ = plan_stats(engine_lib, 0, A.ops_array([]))
+    assert A.STATUS_NAMES[st] == "ZeroQubits"
+
+
+def test_context_creation_reports_missing_gpu_cleanly(engine_lib):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible; covered by the gpu tests")
+    h = C.c_void_p()
+    st = engine_lib.qf_ctx_create(0, C.byref(h))
+    assert A.STATUS_NAMES[st] == "Cuda" and not h.value

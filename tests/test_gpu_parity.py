@@ -1,0 +1,266 @@
+"""GPU parity: the engine's kernels against the CPU oracle on the same seeded
+inputs, through the C ABI. complex128 results must match within 1e-10 (the
+reference's own CUDA tests use 1e-12 for short circuits, kept where they
+apply); complex64 within the f32 bound stated per test; integer outcomes
+bit-exact unless a decision is reported as a tie."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle as O
+from quantumforge_gb300 import Circuit, Gate, PauliSum, QuantumError, SmallRng, StateVector
+from quantumforge_gb300 import _abi as A
+from quantumforge_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+C128_TOL = 1e-10
+C64_TOL = 2e-6  # max |amplitude error| of f32 sweeps over a few hundred gates
+
+
+def close(a, b, tol):
+    return np.abs(np.asarray(a) - np.asarray(b)).max() <= tol
+
+
+# ---- the reference's CUDA tests (tests/quantum_core.rs:401-731) ---------------
+def test_cuda_ry_matches_cpu_reference(backend):  # :401-421
+    sv = StateVector.zero(5, backend=backend)
+    sv.apply(Gate.H, 0).apply(Gate.Ry(-0.2), 3)
+    cpu = O.apply(O.apply(O.zero(5), A.GATE_H, 0, 0), A.GATE_RY, -0.2, 3)
+    for ax, q, th in ((A.GATE_RX, 2, 0.73), (A.GATE_RY, 4, -0.2), (A.GATE_RZ, 1, 1.1)):
+        sv.apply(Gate(ax, th), q)
+        O.apply(cpu, ax, th, q)
+    assert close(sv.amplitudes(), cpu, 1e-12)
+
+
+def test_cuda_entangling_gates_match_cpu_reference(backend):  # :446-486
+    cpu = O.zero(5)
+    for q in range(5):
+        O.apply(cpu, A.GATE_H, 0, q)
+    O.apply(cpu, A.GATE_RZ, 0.37, 2)
+    sv = StateVector.from_amplitudes(cpu, backend=backend)
+    sv.apply_cnot(0, 4)
+    O.cnot(cpu, 0, 4)
+    assert close(sv.amplitudes(), cpu, 1e-12)
+    sv.apply_cz(1, 3)
+    O.cz(cpu, 1, 3)
+    assert close(sv.amplitudes(), cpu, 1e-12)
+    sv.apply_swap(0, 2)
+    O.swap(cpu, 0, 2)
+    assert close(sv.amplitudes(), cpu, 1e-12)
+
+
+def test_cuda_executes_the_unitary_circuit_api(backend):  # :488-511
+    c = Circuit()
+    for gate, q in ((Gate.H, 0), (Gate.X, 1), (Gate.Y, 2), (Gate.Z, 3), (Gate.Rx(0.19), 0), (Gate.Ry(-0.57), 1),
+                    (Gate.Rz(1.03), 2)):
+        c.push(gate, q)
+    c.cnot(0, 3)
+    c.cz(1, 2)
+    c.swap(0, 1)
+    expected = O.run(c.ops(), 4)
+    for mode in ("unfused", "fused"):
+        got = backend.run_circuit(O.zero(4), c, exec_opts={"mode": mode})
+        assert close(got, expected, 1e-12)
+
+
+def test_cuda_batched_inputs_match_independent_cpu_runs(backend):  # :513-600 (states run one by one)
+    c = Circuit()
+    c.push(Gate.H, 0)
+    c.push(Gate.Rx(0.19), 2)
+    c.push(Gate.Ry(-0.53), 1)
+    c.cnot(0, 2)
+    c.cz(1, 2)
+    c.swap(0, 1)
+    c.push(Gate.Rz(math.pi / 2), 2)
+    inputs = [O.zero(3)]
+    s = O.apply(O.apply(O.zero(3), A.GATE_X, 0, 0), A.GATE_RY, 0.31, 2)
+    inputs.append(s)
+    inputs.append(O.apply(O.apply(O.zero(3), A.GATE_H, 0, 1), A.GATE_RZ, math.pi / 2, 2))
+    inputs.append(O.apply(O.apply(O.zero(3), A.GATE_X, 0, 1), A.GATE_H, 0, 2))
+    for st in inputs:
+        assert close(backend.run_circuit(st, c), O.run(c.ops(), 3, init=st), 1e-12)
+    # shared-RNG measurement of qubit 0 after H, in batch order (seed 7721)
+    rng_gpu, rng_cpu = SmallRng.seeded(7721), O.Rng(7721)
+    for st in inputs:
+        pre = O.apply(st.copy(), A.GATE_H, 0, 0)
+        sv = StateVector.from_amplitudes(pre, backend=backend)
+        cpu = pre.copy()
+        assert sv.measure(0, rng_gpu) == O.measure(cpu, 0, rng_cpu)
+        assert close(sv.amplitudes(), cpu, 1e-12)
+    assert rng_gpu.state == rng_cpu.state.value
+
+
+def test_cuda_resident_measurement_matches_the_cpu_reference(backend):  # :602-622
+    init = O.apply(O.zero(2), A.GATE_H, 0, 1)
+    cpu = init.copy()
+    expected = O.measure(cpu, 1, O.Rng(342))
+    sv = StateVector.from_amplitudes(init, backend=backend)
+    assert sv.measure(1, SmallRng.seeded(342)) == expected
+    assert close(sv.amplitudes(), cpu, 1e-12)
+
+
+def test_feedforward_circuit_is_rejected_by_the_terminal_sampler(backend):  # :649-676 circuit
+    c = Circuit()
+    c.push(Gate.H, 0)
+    c.push(Gate.H, 1)
+    c.measure(0, 0)
+    c.if_classical_bit(0, 1, Gate.X, 2)
+    c.measure(1, 1)
+    c.measure(2, 2)
+    with pytest.raises(QuantumError) as e:
+        c.run_shots(3, 64, 721, backend=backend)
+    assert e.value.kind == "UnsupportedOperation"
+
+
+# ---- random circuits -------------------------------------------------------------
+@pytest.mark.parametrize("n,depth,seed", [(3, 6, 1), (8, 12, 2), (12, 20, 3), (16, 20, 4), (20, 20, 5)])
+@pytest.mark.parametrize("mode", ["unfused", "fused"])
+def test_random_ladder_circuit_c128(backend, n, depth, seed, mode):
+    ops = W.random_circuit(n, depth, seed)
+    expected = O.run(ops, n)
+    sv = StateVector.zero(n, backend=backend)
+    sv.apply_ops(ops, exec_opts={"mode": mode})
+    assert close(sv.amplitudes(), expected, C128_TOL)
+
+
+@pytest.mark.parametrize("n,seed", [(10, 11), (14, 12), (18, 13)])
+@pytest.mark.parametrize("tile", [6, 8, 10, 11, 13])
+def test_mixed_circuit_fused_tiles_c128(backend, n, seed, tile):
+    ops = W.random_circuit(n, 12, seed, two_qubit="mixed")
+    expected = O.run(ops, n)
+    sv = StateVector.zero(n, backend=backend)
+    sv.apply_ops(ops, exec_opts={"mode": "fused", "tile_qubits": tile})
+    assert close(sv.amplitudes(), expected, C128_TOL)
+
+
+@pytest.mark.parametrize("n,seed", [(12, 21), (18, 22), (20, 23)])
+@pytest.mark.parametrize("mode", ["unfused", "fused"])
+def test_mixed_circuit_c64(backend, n, seed, mode):
+    ops = W.random_circuit(n, 20, seed, two_qubit="mixed")
+    expected = O.run(ops, n)
+    sv = StateVector.zero(n, dtype="c64", backend=backend)
+    sv.apply_ops(ops, exec_opts={"mode": mode})
+    got = sv.amplitudes()
+    assert close(got, expected, C64_TOL)
+    assert abs(sv.norm_sqr() - 1.0) < 1e-5
+
+
+def test_every_gate_kind_on_every_qubit_position(backend):
+    n = 7
+    recs = []
+    for gate in range(12):
+        for q in range(n):
+            recs.append((A.OP_GATE, gate, q, 0, 0, 0.3 + 0.1 * q if gate >= A.GATE_RX else 0.0))
+    for a in range(n):
+        for b in range(n):
+            if a != b:
+                recs.append((A.OP_CNOT, 0, a, b, 0, 0.0))
+                recs.append((A.OP_GATE, A.GATE_H, a, 0, 0, 0.0))
+                recs.append((A.OP_CZ, 0, a, b, 0, 0.0))
+                recs.append((A.OP_SWAP, 0, a, b, 0, 0.0))
+                recs.append((A.OP_GATE, A.GATE_RY, b, 0, 0, 0.2 * a))
+    ops = A.ops_array(recs)
+    expected = O.run(ops, n)
+    for mode, tile in (("unfused", 0), ("fused", 3), ("fused", 5), ("fused", 7)):
+        for dtype, tol in (("c128", C128_TOL), ("c64", C64_TOL)):
+            sv = StateVector.zero(n, dtype=dtype, backend=backend)
+            sv.apply_ops(ops, exec_opts={"mode": mode, "tile_qubits": tile})
+            assert close(sv.amplitudes(), expected, tol), (mode, tile, dtype)
+
+
+# ---- reductions ----------------------------------------------------------------
+@pytest.mark.parametrize("dtype,tol", [("c128", 1e-12), ("c64", 1e-6)])
+@pytest.mark.parametrize("n", [1, 2, 5, 9, 16, 21])
+def test_probabilities_and_expectations(backend, dtype, tol, n):
+    ops = W.random_circuit(n, 6, 40 + n, two_qubit="mixed" if n > 3 else "ladder")
+    a = O.run(ops, n)
+    sv = StateVector.from_amplitudes(a, dtype=dtype, backend=backend)
+    assert close(sv.probabilities(), O.probabilities(a), tol)
+    zs = sv.expectation_z_all()
+    for q in range(n):
+        assert abs(zs[q] - O.expectation(a, A.PAULI_Z, q)) < 10 * tol
+        for obs in (A.PAULI_X, A.PAULI_Y, A.PAULI_Z):
+            assert abs(sv.expectation(obs, q) - O.expectation(a, obs, q)) < 10 * tol
+    assert abs(sv.norm_sqr() - O.norm_sqr(a)) < 10 * tol
+
+
+@pytest.mark.parametrize("n", [4, 10, 17])
+def test_pauli_sum_expectations(backend, n):
+    ops = W.random_circuit(n, 5, 60 + n, two_qubit="mixed")
+    a = O.run(ops, n)
+    sv = StateVector.from_amplitudes(a, backend=backend)
+    r = np.random.default_rng(n)
+    rand = PauliSum()
+    for _ in range(12):
+        x = int(r.integers(0, 1 << n))
+        z = int(r.integers(0, 1 << n))
+        rand.add_term(x, z, complex(r.normal(), r.normal()))
+    for H in (PauliSum.tfim_ring(n, 0.8), PauliSum.xxz_ring(n, 0.5), rand):
+        got = sv.expectation_pauli_sum(H)
+        want = O.pauli_expectation(a, H.array())
+        assert abs(got - want) < 1e-10 * max(1.0, len(H))
+
+
+# ---- sampling ---------------------------------------------------------------------
+@pytest.mark.parametrize("n,seed", [(2, 991), (5, 721), (10, 42), (12, 43), (14, 44)])
+def test_terminal_shots_bit_exact(backend, n, seed):
+    ops = W.with_terminal_measurements(W.random_circuit(n, 10, seed), n)
+    shots = 4000
+    exp_packed, width = O.run_shots(ops, n, shots, seed)
+    c = Circuit.from_ops(ops)
+    assert np.array_equal(c.ops(), ops)
+    res = c.run_shots(n, shots, seed, backend=backend, tie_eps=1e-12)
+    assert res.ties == 0
+    assert res.counts == O.counts(exp_packed, width)
+    assert res.shots == shots
+
+
+def test_sample_on_resident_state_matches_literal_reference(backend):
+    n = 6
+    ops = W.random_circuit(n, 8, 17)
+    a = O.run(ops, n)
+    meas = A.ops_array([(A.OP_MEASURE, 0, q, 0, q, 0.0) for q in (3, 0, 5, 1, 4, 2)])
+    exp_packed, width = O.run_shots(meas, n, 2000, 5, init=a, literal=True)
+    sv = StateVector.from_amplitudes(a, backend=backend)
+    packed, ties = sv.sample([3, 0, 5, 1, 4, 2], [3, 0, 5, 1, 4, 2], 2000, 5, tie_eps=1e-12)
+    assert ties == 0
+    assert (packed == exp_packed).all()
+
+
+def test_shot_validation(backend):
+    c = Circuit()
+    c.push(Gate.H, 0)
+    c.measure(0, 0)
+    with pytest.raises(QuantumError) as e:
+        c.run_shots(1, 0, 1, backend=backend)
+    assert e.value.kind == "InvalidShotCount"
+    c.measure(0, 5000)
+    with pytest.raises(QuantumError) as e:
+        c.run_shots(1, 10, 1, backend=backend)
+    assert e.value.kind == "ClassicalBitOutOfRange"
+
+
+# ---- errors leave the state untouched ---------------------------------------------
+def test_errors_are_typed_and_state_is_untouched(backend):
+    sv = StateVector.zero(3, backend=backend)
+    sv.apply(Gate.H, 0)
+    before = sv.amplitudes().copy()
+    with pytest.raises(QuantumError) as e:
+        sv.apply(Gate.X, 3)
+    assert e.value.kind == "QubitOutOfRange"
+    with pytest.raises(QuantumError) as e:
+        sv.apply_cnot(1, 1)
+    assert e.value.kind == "InvalidQubitPair"
+    bad = A.ops_array([(A.OP_GATE, A.GATE_X, 1, 0, 0, 0.0), (A.OP_CHANNEL, 0, 0, 0, 0, 0.0)])
+    with pytest.raises(QuantumError) as e:
+        sv.apply_ops(bad)
+    assert e.value.kind == "OperationRequiresDensityMatrix"
+    assert np.array_equal(sv.amplitudes(), before)
+    with pytest.raises(QuantumError) as e:
+        StateVector.zero(0, backend=backend)
+    assert e.value.kind == "ZeroQubits"
+    with pytest.raises(QuantumError) as e:
+        StateVector.zero(20, memory_budget=1000, backend=backend)
+    assert e.value.kind == "MemoryBudgetExceeded"
