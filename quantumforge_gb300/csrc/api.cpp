@@ -114,12 +114,14 @@ int alloc_state(qf_ctx *ctx, uint32_t qubits, int dtype, uint64_t budget, qf_sv 
         delete sv;
         return st;
     }
+    ctx->states.insert(sv);
     *out = sv;
     return QF_OK;
 }
 
 void free_state(qf_sv *sv) {
     if (!sv) return;
+    if (sv->ctx) sv->ctx->states.erase(sv);
     if (sv->d) cudaFree(sv->d);
     delete sv;
 }
@@ -340,6 +342,14 @@ int qf_ctx_destroy(qf_ctx *ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     free_state(ctx->scratch_sv);
     free_state(ctx->scratch_sv2);
+    // states the caller still holds: free their memory, keep the handle as an
+    // orphan that qf_sv_destroy can release without the context
+    for (qf_sv *sv : ctx->states) {
+        if (sv->d) cudaFree(sv->d);
+        sv->d = nullptr;
+        sv->ctx = nullptr;
+    }
+    ctx->states.clear();
     if (ctx->ws_plan) cudaFree(ctx->ws_plan);
     if (ctx->ws_red) cudaFree(ctx->ws_red);
     if (ctx->ws_tree) cudaFree(ctx->ws_tree);
@@ -375,7 +385,11 @@ int qf_sv_create(qf_ctx *ctx, uint32_t qubits, int dtype, uint64_t memory_budget
 
 int qf_sv_destroy(qf_sv *sv) {
     if (!sv) return QF_OK;
-    if (sv->ctx) {
+    if (!sv->ctx) {  // orphaned by qf_ctx_destroy: memory already released
+        delete sv;
+        return QF_OK;
+    }
+    {
         cudaSetDevice(sv->ctx->device);
         cudaStreamSynchronize(sv->ctx->stream);
     }

@@ -214,7 +214,9 @@ int popc(uint64_t x) { return __builtin_popcountll(x); }
 int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, Plan &plan) {
     plan = Plan();
     plan.n = n;
-    const int k = std::min<int>(o.tile_qubits, (int)n);
+    // at least 3 resident qubits: any two-qubit op plus qubit 0 (which keeps
+    // complex64 tiles in 16-byte pairs) always fits
+    const int k = std::min<int>(std::max(o.tile_qubits, 3), (int)n);
     const int low = std::min<int>(o.low_qubits, k);
     if (k - low > kMaxLocal) return fail(QF_ERR_INVALID_ARGUMENT, "tile of %d qubits over %d low qubits is too wide", k, low);
     const uint64_t all = n >= 64 ? ~0ULL : ((1ULL << n) - 1);
@@ -235,7 +237,11 @@ int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, 
     for (size_t i = 0; i < items.size(); ++i) remaining[i] = (int)i;
 
     while (!remaining.empty()) {
+        // The first remaining item must fit: shrink the always-resident low
+        // block from the top until it does (qubit 0 stays resident, k >= 3).
         uint64_t L = low_mask;
+        const uint64_t first_need = items[remaining[0]].need;
+        for (int b = low - 1; b >= 1 && popc(L | first_need) > k; --b) L &= ~(1ULL << b);
         uint64_t blocked = 0;
         std::vector<Item> taken;
         std::vector<int> last_on(n, -1);  // index into taken of the last item touching q
@@ -288,6 +294,7 @@ int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, 
             }
         p.a.k = lo_eff + r;
         p.a.low = lo_eff;
+        if (lo_eff < 1 || p.a.k > 21) return fail(QF_ERR_INVALID_ARGUMENT, "invalid tile layout (low %u, k %u)", lo_eff, p.a.k);
         p.a.nonlocal_mask = all & ~L;
         p.a.n_tiles = 1ULL << (n - p.a.k);
         p.op_begin = (uint32_t)plan.ops.size();

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -25,6 +26,7 @@ struct qf_ctx {
     double *h_small = nullptr;    // 64 KiB pinned host mirror
     qf_sv *scratch_sv = nullptr;  // cached state for whole-circuit calls
     qf_sv *scratch_sv2 = nullptr; // cached second state (adjoint costate)
+    std::set<qf_sv *> states;     // live states; orphaned (memory freed) when the context is destroyed
 };
 constexpr size_t kSmallBytes = 64 * 1024;
 
@@ -53,6 +55,20 @@ int cuda_fail(cudaError_t e, const char *what);
         int qf_s_ = (expr);          \
         if (qf_s_ != QF_OK) return qf_s_; \
     } while (0)
+
+// Opt a kernel into the largest dynamic shared memory the device allows
+// (the opt-in limit minus the kernel's static shared memory); returns that
+// dynamic limit in *dyn_limit.
+template <typename F> int allow_max_dynamic_smem(F *func, const qf_ctx *ctx, size_t *dyn_limit) {
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, func);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncGetAttributes");
+    const size_t dyn = ctx->smem_optin > fa.sharedSizeBytes ? ctx->smem_optin - fa.sharedSizeBytes : 0;
+    e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaFuncSetAttribute(MaxDynamicSharedMemorySize)");
+    *dyn_limit = dyn;
+    return 0;
+}
 
 // Grow-only device workspace.
 int ensure_device(void **ptr, size_t *bytes, size_t need);

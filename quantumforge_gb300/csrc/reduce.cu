@@ -412,14 +412,84 @@ __global__ void __launch_bounds__(kRedThreads)
     if (threadIdx.x == 0) partials[2 * blockIdx.x + 1] = acc_im;
 }
 
+// A group whose x-mask does not fit in one tile: one grid-stride sweep over
+// the pairs (i, i ^ x) straight from global memory (coalesced runs on both
+// sides of the pair). mode 0 accumulates <psi|H_x|psi>; mode 2 adds H_x psi
+// into lambda.
+template <typename C>
+__global__ void k_pauli_wide(const C *__restrict__ psi, C *__restrict__ lam, uint64_t n_pairs, uint64_t x, uint32_t xb,
+                             const PTerm *__restrict__ terms, uint32_t nt, uint32_t mode, double *__restrict__ partials) {
+    using R = typename Real<C>::T;
+    __shared__ double red[32];
+    double acc_re = 0.0, acc_im = 0.0;
+    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n_pairs; p += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t i = insert0(p, xb), j = i ^ x;
+        R gir = 0, gii = 0, gjr = 0, gji = 0;
+        for (uint32_t t = 0; t < nt; ++t) {
+            const PTerm P = terms[t];
+            const R si = (__popcll(i & P.z) & 1) ? R(-1) : R(1);
+            const R sj = (__popcll(j & P.z) & 1) ? R(-1) : R(1);
+            gir += si * (R)P.cre;
+            gii += si * (R)P.cim;
+            gjr += sj * (R)P.cre;
+            gji += sj * (R)P.cim;
+        }
+        const C ai = psi[i], aj = psi[j];
+        // G_i a_i and G_j a_j
+        const R pir = gir * ai.x - gii * ai.y, pii = gir * ai.y + gii * ai.x;
+        const R pjr = gjr * aj.x - gji * aj.y, pji = gjr * aj.y + gji * aj.x;
+        if (mode == 0) {
+            // conj(a_j) G_i a_i + conj(a_i) G_j a_j
+            acc_re += (double)(aj.x * pir + aj.y * pii) + (double)(ai.x * pjr + ai.y * pji);
+            acc_im += (double)(aj.x * pii - aj.y * pir) + (double)(ai.x * pji - ai.y * pjr);
+        } else {
+            C lj = lam[j], li = lam[i];
+            lj.x += pir;
+            lj.y += pii;
+            li.x += pjr;
+            li.y += pji;
+            lam[j] = lj;
+            lam[i] = li;
+        }
+    }
+    acc_re = block_sum(acc_re, red);
+    if (threadIdx.x == 0) partials[2 * blockIdx.x] = acc_re;
+    acc_im = block_sum(acc_im, red);
+    if (threadIdx.x == 0) partials[2 * blockIdx.x + 1] = acc_im;
+}
+
+// sum_i conj(a_i) b_i
+template <typename C>
+__global__ void k_dot(const C *__restrict__ a, const C *__restrict__ b, uint64_t dim, double *__restrict__ partials) {
+    __shared__ double red[32];
+    double re = 0.0, im = 0.0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < dim; i += (uint64_t)gridDim.x * blockDim.x) {
+        const C u = a[i], v = b[i];
+        re += (double)u.x * v.x + (double)u.y * v.y;
+        im += (double)u.x * v.y - (double)u.y * v.x;
+    }
+    re = block_sum(re, red);
+    if (threadIdx.x == 0) partials[2 * blockIdx.x] = re;
+    im = block_sum(im, red);
+    if (threadIdx.x == 0) partials[2 * blockIdx.x + 1] = im;
+}
+
 namespace {
 struct PPassHost {
     PPassArgs a;
     std::vector<PGroup> groups;
     std::vector<PTerm> terms;
 };
+struct PWide {
+    uint64_t x;
+    std::vector<PTerm> terms;
+};
+struct PauliPlan {
+    std::vector<PPassHost> tiles;
+    std::vector<PWide> wide;
+};
 
-int plan_pauli(uint32_t n, int dtype, const qf_pauli_term *terms, uint64_t n_terms, std::vector<PPassHost> &passes) {
+int plan_pauli(uint32_t n, int dtype, const qf_pauli_term *terms, uint64_t n_terms, PauliPlan &plan) {
     const uint64_t valid = n >= 64 ? ~0ULL : ((1ULL << n) - 1);
     std::map<uint64_t, std::vector<PTerm>> by_x;
     for (uint64_t t = 0; t < n_terms; ++t) {
@@ -438,7 +508,11 @@ int plan_pauli(uint32_t n, int dtype, const qf_pauli_term *terms, uint64_t n_ter
     int k, low;
     default_tiling(n, dtype, 0, &k, &low);
     const uint64_t low_mask = (1ULL << low) - 1;
-    std::vector<std::pair<uint64_t, std::vector<PTerm>>> groups(by_x.begin(), by_x.end());
+    std::vector<std::pair<uint64_t, std::vector<PTerm>>> groups;
+    for (auto &kv : by_x) {
+        if (__builtin_popcountll(low_mask | kv.first) > k) plan.wide.push_back(PWide{kv.first, kv.second});
+        else groups.push_back(kv);
+    }
     std::vector<bool> done(groups.size(), false);
     size_t left = groups.size();
     while (left) {
@@ -452,7 +526,6 @@ int plan_pauli(uint32_t n, int dtype, const qf_pauli_term *terms, uint64_t n_ter
                 sel.push_back(g);
             }
         }
-        if (sel.empty()) return fail(QF_ERR_UNSUPPORTED_OPERATION, "Pauli term spans more than %d qubits", k);
         for (uint32_t q = 0; q < n && __builtin_popcountll(L) < k; ++q) L |= 1ULL << q;
         PPassHost P;
         std::memset(&P.a, 0, sizeof P.a);
@@ -487,31 +560,36 @@ int plan_pauli(uint32_t n, int dtype, const qf_pauli_term *terms, uint64_t n_ter
         }
         P.a.n_groups = (uint32_t)P.groups.size();
         P.a.n_terms = (uint32_t)P.terms.size();
-        passes.push_back(std::move(P));
+        plan.tiles.push_back(std::move(P));
     }
     return QF_OK;
 }
 
+// Expectation (apply == false): every launch adds its slice of partials.
+// Apply: lambda = sum of the launches; the energy <psi|lambda> comes from the
+// last tile pass, or from a separate dot product when wide groups follow.
 template <typename C>
-int run_pauli(qf_sv *psi, qf_sv *lam, std::vector<PPassHost> &passes, bool apply, double out[2]) {
+int run_pauli(qf_sv *psi, qf_sv *lam, PauliPlan &plan, bool apply, double out[2]) {
     qf_ctx *ctx = psi->ctx;
-    static bool attr_done[64] = {false};
-    if (!attr_done[ctx->device & 63]) {
-        QF_CUDA(cudaFuncSetAttribute(k_pauli_pass<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ctx->smem_optin));
-        attr_done[ctx->device & 63] = true;
-    }
+    static size_t dyn_limit[64] = {0};
+    if (!dyn_limit[ctx->device & 63]) QF_TRY(allow_max_dynamic_smem(k_pauli_pass<C>, ctx, &dyn_limit[ctx->device & 63]));
     size_t meta = 0;
-    for (auto &P : passes) meta += P.groups.size() * sizeof(PGroup) + P.terms.size() * sizeof(PTerm) + 64;
+    for (auto &P : plan.tiles) meta += P.groups.size() * sizeof(PGroup) + P.terms.size() * sizeof(PTerm) + 64;
+    for (auto &W : plan.wide) meta += W.terms.size() * sizeof(PTerm) + 32;
     QF_TRY(ensure_device(&ctx->ws_plan, &ctx->ws_plan_bytes, meta));
     const uint32_t grid = (uint32_t)ctx->sm_count * 2;
+    const bool need_dot = apply && !plan.wide.empty();
+    const size_t launches = plan.tiles.size() + plan.wide.size() + (need_dot ? 1 : 0);
     double *partials;
-    QF_TRY(partials_buffer(ctx, (size_t)2 * grid * passes.size(), &partials));
+    QF_TRY(partials_buffer(ctx, (size_t)2 * grid * launches, &partials));
+    QF_CUDA(cudaMemsetAsync(partials, 0, sizeof(double) * 2 * grid * launches, ctx->stream));
     unsigned char *dmeta = static_cast<unsigned char *>(ctx->ws_plan);
-    size_t off = 0;
-    for (size_t i = 0; i < passes.size(); ++i) {
-        PPassHost &P = passes[i];
+    size_t off = 0, slice = 0;
+    if (apply && plan.tiles.empty()) QF_CUDA(cudaMemsetAsync(lam->d, 0, lam->bytes(), ctx->stream));
+    for (size_t i = 0; i < plan.tiles.size(); ++i, ++slice) {
+        PPassHost &P = plan.tiles[i];
         P.a.mode = apply ? (i == 0 ? 1u : 2u) : 0u;
-        P.a.last = (apply && i + 1 == passes.size()) ? 1u : 0u;
+        P.a.last = (apply && !need_dot && i + 1 == plan.tiles.size()) ? 1u : 0u;
         PGroup *dg = reinterpret_cast<PGroup *>(dmeta + off);
         QF_CUDA(cudaMemcpyAsync(dg, P.groups.data(), P.groups.size() * sizeof(PGroup), cudaMemcpyHostToDevice, ctx->stream));
         off += (P.groups.size() * sizeof(PGroup) + 15) / 16 * 16;
@@ -520,18 +598,37 @@ int run_pauli(qf_sv *psi, qf_sv *lam, std::vector<PPassHost> &passes, bool apply
         off += (P.terms.size() * sizeof(PTerm) + 15) / 16 * 16;
         const size_t smem = ((size_t)1 << P.a.k) * sizeof(C) + (8u << (P.a.k - P.a.low)) + P.groups.size() * sizeof(PGroup) +
                             P.terms.size() * sizeof(PTerm);
-        if (smem > ctx->smem_optin) return fail(QF_ERR_UNSUPPORTED_OPERATION, "Pauli pass needs too much shared memory");
+        if (smem > dyn_limit[ctx->device & 63])
+            return fail(QF_ERR_UNSUPPORTED_OPERATION, "Pauli pass needs too much shared memory");
         const uint32_t g = (uint32_t)std::min<uint64_t>(grid, P.a.n_tiles);
-        // unused partial slots of this pass stay zero
-        QF_CUDA(cudaMemsetAsync(partials + (size_t)2 * grid * i, 0, sizeof(double) * 2 * grid, ctx->stream));
         k_pauli_pass<C><<<g, kRedThreads, smem, ctx->stream>>>(static_cast<const C *>(psi->d),
                                                                lam ? static_cast<C *>(lam->d) : nullptr, P.a, dg, dt,
-                                                               partials + (size_t)2 * grid * i);
+                                                               partials + (size_t)2 * grid * slice);
         QF_CUDA(cudaGetLastError());
     }
-    // expectation: sum over every pass; apply: only the last pass carries <psi|lambda>
-    const size_t first = apply ? passes.size() - 1 : 0;
-    const uint32_t nblk = (uint32_t)(grid * (passes.size() - first));
+    for (size_t w = 0; w < plan.wide.size(); ++w, ++slice) {
+        PWide &Wg = plan.wide[w];
+        PTerm *dt = reinterpret_cast<PTerm *>(dmeta + off);
+        QF_CUDA(cudaMemcpyAsync(dt, Wg.terms.data(), Wg.terms.size() * sizeof(PTerm), cudaMemcpyHostToDevice, ctx->stream));
+        off += (Wg.terms.size() * sizeof(PTerm) + 15) / 16 * 16;
+        const uint32_t xb = (uint32_t)__builtin_ctzll(Wg.x);
+        const uint64_t pairs = psi->dim / 2;
+        const uint32_t g = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(grid, (pairs + kRedThreads - 1) / kRedThreads));
+        k_pauli_wide<C><<<g, kRedThreads, 0, ctx->stream>>>(static_cast<const C *>(psi->d),
+                                                            lam ? static_cast<C *>(lam->d) : nullptr, pairs, Wg.x, xb, dt,
+                                                            (uint32_t)Wg.terms.size(), apply ? 2u : 0u,
+                                                            partials + (size_t)2 * grid * slice);
+        QF_CUDA(cudaGetLastError());
+    }
+    if (need_dot) {
+        k_dot<C><<<grid, kRedThreads, 0, ctx->stream>>>(static_cast<const C *>(psi->d), static_cast<const C *>(lam->d),
+                                                        psi->dim, partials + (size_t)2 * grid * slice);
+        QF_CUDA(cudaGetLastError());
+        ++slice;
+    }
+    // expectation: every slice; apply: only the slice carrying <psi|lambda>
+    const size_t first = apply ? slice - 1 : 0;
+    const uint32_t nblk = (uint32_t)(grid * (slice - first));
     k_final_sum<<<1, 128, 0, ctx->stream>>>(partials + 2 * grid * first, nblk, 2, ctx->d_small);
     QF_CUDA(cudaGetLastError());
     QF_CUDA(cudaMemcpyAsync(ctx->h_small, ctx->d_small, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
@@ -545,10 +642,10 @@ int run_pauli(qf_sv *psi, qf_sv *lam, std::vector<PPassHost> &passes, bool apply
 int pauli_expectation(qf_sv *sv, const qf_pauli_term *terms, uint64_t n_terms, double out[2]) {
     out[0] = out[1] = 0.0;
     if (n_terms == 0) return QF_OK;
-    std::vector<PPassHost> passes;
-    QF_TRY(plan_pauli(sv->n, sv->dtype, terms, n_terms, passes));
-    if (sv->dtype == QF_C64) return run_pauli<float2>(sv, nullptr, passes, false, out);
-    return run_pauli<double2>(sv, nullptr, passes, false, out);
+    PauliPlan plan;
+    QF_TRY(plan_pauli(sv->n, sv->dtype, terms, n_terms, plan));
+    if (sv->dtype == QF_C64) return run_pauli<float2>(sv, nullptr, plan, false, out);
+    return run_pauli<double2>(sv, nullptr, plan, false, out);
 }
 
 int pauli_apply(qf_sv *psi, qf_sv *lam, const qf_pauli_term *terms, uint64_t n_terms, double *energy) {
@@ -557,11 +654,11 @@ int pauli_apply(qf_sv *psi, qf_sv *lam, const qf_pauli_term *terms, uint64_t n_t
         if (energy) *energy = 0.0;
         return QF_OK;
     }
-    std::vector<PPassHost> passes;
-    QF_TRY(plan_pauli(psi->n, psi->dtype, terms, n_terms, passes));
+    PauliPlan plan;
+    QF_TRY(plan_pauli(psi->n, psi->dtype, terms, n_terms, plan));
     double out[2];
-    if (psi->dtype == QF_C64) QF_TRY(run_pauli<float2>(psi, lam, passes, true, out));
-    else QF_TRY(run_pauli<double2>(psi, lam, passes, true, out));
+    if (psi->dtype == QF_C64) QF_TRY(run_pauli<float2>(psi, lam, plan, true, out));
+    else QF_TRY(run_pauli<double2>(psi, lam, plan, true, out));
     if (energy) *energy = out[0];
     return QF_OK;
 }

@@ -480,21 +480,19 @@ __global__ void k_reduce_slots(const double *__restrict__ partials, uint32_t str
     }
 }
 
-template <typename C, bool DUAL> static int set_smem_attr(const qf_ctx *ctx) {
-    static bool done[64] = {false};
+template <typename C, bool DUAL> static int set_smem_attr(const qf_ctx *ctx, size_t *limit) {
+    static size_t dyn[64] = {0};
     const int dev = ctx->device & 63;
-    if (!done[dev]) {
-        QF_CUDA(cudaFuncSetAttribute(k_tile_pass<C, DUAL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)ctx->smem_optin));
-        done[dev] = true;
-    }
+    if (!dyn[dev]) QF_TRY(allow_max_dynamic_smem(k_tile_pass<C, DUAL>, ctx, &dyn[dev]));
+    *limit = dyn[dev];
     return QF_OK;
 }
 
 template <typename C, bool DUAL>
 static int launch_passes(qf_sv *psi, qf_sv *lam, const Plan &plan, double *d_slot_sums) {
     qf_ctx *ctx = psi->ctx;
-    QF_TRY((set_smem_attr<C, DUAL>(ctx)));
+    size_t smem_limit = 0;
+    QF_TRY((set_smem_attr<C, DUAL>(ctx, &smem_limit)));
     // upload ops then matrices
     const size_t ops_bytes = align_up((uint32_t)(plan.ops.size() * sizeof(TileOp)), 16);
     const size_t mats_bytes = plan.mats.size() * sizeof(double);
@@ -514,9 +512,9 @@ static int launch_passes(qf_sv *psi, qf_sv *lam, const Plan &plan, double *d_slo
         const TileSmem L = tile_smem(p.a.k, p.a.low, p.a.n_ops, p.a.n_mats, p.a.n_slots, DUAL, sizeof(C));
         max_smem = std::max(max_smem, L.total);
     }
-    if (max_smem > ctx->smem_optin)
+    if (max_smem > smem_limit)
         return fail(QF_ERR_UNSUPPORTED_OPERATION, "tile pass needs %u bytes of shared memory (limit %zu)", max_smem,
-                    ctx->smem_optin);
+                    smem_limit);
     int per_sm = 0;
     QF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile_pass<C, DUAL>, kThreads, max_smem));
     per_sm = std::max(per_sm, 1);

@@ -264,3 +264,16 @@ def test_errors_are_typed_and_state_is_untouched(backend):
     with pytest.raises(QuantumError) as e:
         StateVector.zero(20, memory_budget=1000, backend=backend)
     assert e.value.kind == "MemoryBudgetExceeded"
+
+
+def test_state_outliving_its_context_is_released_safely(engine_lib):
+    from quantumforge_gb300 import CudaBackend
+
+    b = CudaBackend(0)
+    sv = StateVector.zero(4, backend=b)
+    sv.apply(Gate.H, 0)
+    b.close()  # frees the state's memory and orphans the handle
+    with pytest.raises(QuantumError) as e:
+        sv.apply(Gate.X, 0)
+    assert e.value.kind == "InvalidArgument"
+    del sv  # qf_sv_destroy on an orphan must not touch the released context
