@@ -129,11 +129,14 @@ enum qf_exec_mode {
     QF_EXEC_FUSED = 2     /* tile-fused passes with the widths given below */
 };
 
+/* qf_exec_opts.flags */
+#define QF_EXEC_FLAG_SMEM_TILES 1  /* complex64: use the shared-memory tile kernel instead of register tiles */
+
 typedef struct qf_exec_opts {
     int32_t mode;          /* enum qf_exec_mode */
-    int32_t tile_qubits;   /* qubits resident in shared memory per tile (0 = auto) */
+    int32_t tile_qubits;   /* qubits resident per tile (0 = auto) */
     int32_t block_qubits;  /* dense fused-block width k (0/1 = apply gates one by one, 2..5 = fuse into k-qubit blocks) */
-    int32_t reserved;
+    int32_t flags;         /* QF_EXEC_FLAG_* */
 } qf_exec_opts;
 
 /* Gradient strategies, in the order of `enum GradientStrategy`

@@ -84,8 +84,22 @@ class ExecOpts(C.Structure):
         ("mode", C.c_int32),
         ("tile_qubits", C.c_int32),
         ("block_qubits", C.c_int32),
-        ("reserved", C.c_int32),
+        ("flags", C.c_int32),
     ]
+
+
+EXEC_FLAG_SMEM_TILES = 1
+_MODES = {"auto": EXEC_AUTO, "unfused": EXEC_UNFUSED, "fused": EXEC_FUSED}
+
+
+def exec_opts(opts) -> "ExecOpts":
+    """qf_exec_opts from a dict {mode, tile_qubits, block_qubits, smem_tiles}."""
+    if isinstance(opts, ExecOpts):
+        return opts
+    opts = opts or {}
+    flags = EXEC_FLAG_SMEM_TILES if opts.get("smem_tiles") else 0
+    return ExecOpts(_MODES[opts.get("mode", "auto")], int(opts.get("tile_qubits", 0)), int(opts.get("block_qubits", 0)),
+                    flags)
 
 
 class GradientOpts(C.Structure):

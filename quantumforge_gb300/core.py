@@ -282,11 +282,7 @@ def default_backend() -> CudaBackend:
 def _exec(opts):
     if opts is None:
         return None
-    if isinstance(opts, _abi.ExecOpts):
-        return C.byref(opts)
-    mode = {"auto": _abi.EXEC_AUTO, "unfused": _abi.EXEC_UNFUSED, "fused": _abi.EXEC_FUSED}
-    o = _abi.ExecOpts(mode[opts.get("mode", "auto")], int(opts.get("tile_qubits", 0)), int(opts.get("block_qubits", 0)), 0)
-    return C.byref(o)
+    return C.byref(_abi.exec_opts(opts))
 
 
 # ---------------------------------------------------------------------------

@@ -297,6 +297,9 @@ int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, 
         if (lo_eff < 1 || p.a.k > 21) return fail(QF_ERR_INVALID_ARGUMENT, "invalid tile layout (low %u, k %u)", lo_eff, p.a.k);
         p.a.nonlocal_mask = all & ~L;
         p.a.n_tiles = 1ULL << (n - p.a.k);
+        p.resident = L;
+        if (!o.backward)
+            for (const Item &it : taken) p.gates.push_back(it.g);
         p.op_begin = (uint32_t)plan.ops.size();
         p.mat_begin = (uint32_t)(plan.mats.size() / 8);
         p.a.slot_base = plan.n_slots;
@@ -346,6 +349,153 @@ int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, 
         p.a.n_mats = (uint32_t)(plan.mats.size() / 8) - p.mat_begin;
         p.a.n_slots = plan.n_slots - p.a.slot_base;
         plan.passes.push_back(p);
+    }
+    return QF_OK;
+}
+
+// ---- register-tiled lowering ----------------------------------------------
+static uint8_t matrix_kind(const double m[8]) {
+    if (m[1] == 0 && m[3] == 0 && m[5] == 0 && m[7] == 0) return 1;  // real
+    if (m[1] == 0 && m[7] == 0 && m[2] == 0 && m[4] == 0) return 2;  // real diagonal, imaginary off-diagonal
+    return 0;
+}
+
+int lower_rs(const Plan &plan, int wb, RsPlan &out) {
+    out = RsPlan();
+    out.wb = wb;
+    const uint32_t n = plan.n;
+    const int npos = 4 + wb;
+    const int k = 5 + npos;
+    for (const Pass &p : plan.passes) {
+        RsPass rp;
+        std::memset(&rp.a, 0, sizeof rp.a);
+        rp.op_begin = (uint32_t)out.ops.size();
+        rp.mat_begin = (uint32_t)(out.mats.size() / 8);
+        if ((int)n < k || popc(p.resident) != k || (p.resident & 31ULL) != 31ULL) {
+            rp.fallback = true;
+            out.passes.push_back(rp);
+            continue;
+        }
+        std::vector<uint32_t> freeq;
+        for (uint32_t q = 5; q < n; ++q)
+            if ((p.resident >> q) & 1ULL) freeq.push_back(q);
+        int slot_of[64];
+        for (int q = 0; q < 64; ++q) slot_of[q] = -1;
+        for (size_t s = 0; s < freeq.size(); ++s) slot_of[freeq[s]] = (int)s;
+        const std::vector<BGate> &G = p.gates;
+
+        // the qubit a gate needs in a register position (-1: none)
+        auto need_reg = [&](const BGate &g) -> int {
+            if (g.kind == BK_MAT1) return (!g.diag && g.q0 >= 5) ? (int)g.q0 : -1;
+            if (g.kind == BK_CNOT) return g.q1 >= 5 ? (int)g.q1 : -1;
+            if (g.kind == BK_SWAP) {
+                const bool f0 = g.q0 >= 5, f1 = g.q1 >= 5;
+                if (f0 != f1) return f0 ? (int)g.q0 : (int)g.q1;
+            }
+            return -1;
+        };
+        uint32_t label[8];
+        auto pos_of = [&](uint32_t q) -> int {
+            for (int s = 0; s < npos; ++s)
+                if (label[s] == q) return s;
+            return -1;
+        };
+        // register set for the gates from `from` on: the next four distinct
+        // qubits they need in registers, then free qubits already in registers
+        auto relayout = [&](size_t from, bool have_current) {
+            std::vector<uint32_t> regs;
+            for (size_t i = from; i < G.size() && regs.size() < 4; ++i) {
+                const int q = need_reg(G[i]);
+                if (q >= 0 && std::find(regs.begin(), regs.end(), (uint32_t)q) == regs.end()) regs.push_back((uint32_t)q);
+            }
+            if (have_current)
+                for (int s = 0; s < 4 && regs.size() < 4; ++s)
+                    if (std::find(regs.begin(), regs.end(), label[s]) == regs.end()) regs.push_back(label[s]);
+            for (uint32_t q : freeq)
+                if (regs.size() < 4 && std::find(regs.begin(), regs.end(), q) == regs.end()) regs.push_back(q);
+            uint32_t nl[8];
+            for (int s = 0; s < 4; ++s) nl[s] = regs[s];
+            int w = 4;
+            for (uint32_t q : freeq)
+                if (std::find(regs.begin(), regs.end(), q) == regs.end()) nl[w++] = q;
+            std::memcpy(label, nl, sizeof nl);
+        };
+        auto pack = [&]() {
+            uint32_t v = 0;
+            for (int s = 0; s < npos; ++s) v |= (uint32_t)slot_of[label[s]] << (3 * s);
+            return v;
+        };
+        auto desc = [&](uint32_t q) -> uint8_t {
+            if (q < 5) return (uint8_t)q;
+            const int s = pos_of(q);
+            if (s >= 0) return (uint8_t)(s < 4 ? 8 + s : 16 + (s - 4));
+            return (uint8_t)(64 + q);
+        };
+        auto add_mat = [&](const double *m) {
+            out.mats.insert(out.mats.end(), m, m + 8);
+            return (uint32_t)(out.mats.size() / 8 - 1) - rp.mat_begin;
+        };
+        relayout(0, false);
+        for (int s = 0; s < npos; ++s) rp.a.load_q[s] = (uint8_t)label[s];
+        for (size_t gi = 0; gi < G.size(); ++gi) {
+            const BGate &g = G[gi];
+            const int nq = need_reg(g);
+            if (nq >= 0 && pos_of((uint32_t)nq) >= 4) {
+                RsOp r{};
+                r.kind = RS_REMAP;
+                r.a = pack();
+                relayout(gi, true);
+                r.b = pack();
+                out.ops.push_back(r);
+            }
+            RsOp r{};
+            switch (g.kind) {
+            case BK_MAT1:
+                r.mat = add_mat(g.m);
+                r.mk = matrix_kind(g.m);
+                if (g.diag) { r.kind = RS_DIAG; r.p0 = desc(g.q0); }
+                else if (g.q0 < 5) { r.kind = RS_MLANE; r.p0 = (uint8_t)g.q0; }
+                else { r.kind = RS_MREG; r.p0 = (uint8_t)pos_of(g.q0); }
+                out.ops.push_back(r);
+                break;
+            case BK_CNOT:
+                r.kind = RS_CNOT;
+                r.p0 = desc(g.q0);
+                r.p1 = desc(g.q1);
+                out.ops.push_back(r);
+                break;
+            case BK_CZ:
+                r.kind = RS_CZ;
+                r.p0 = desc(g.q0);
+                r.p1 = desc(g.q1);
+                out.ops.push_back(r);
+                break;
+            default: {  // SWAP
+                const bool f0 = g.q0 >= 5, f1 = g.q1 >= 5;
+                if (f0 && f1) {  // relabel: the positions now hold each other's qubit
+                    const int a = pos_of(g.q0), b = pos_of(g.q1);
+                    std::swap(label[a], label[b]);
+                } else if (!f0 && !f1) {
+                    r.kind = RS_SWAP_LL;
+                    r.p0 = (uint8_t)g.q0;
+                    r.p1 = (uint8_t)g.q1;
+                    out.ops.push_back(r);
+                } else {
+                    r.kind = RS_SWAP_LR;
+                    r.p0 = (uint8_t)(f0 ? g.q1 : g.q0);
+                    r.p1 = (uint8_t)pos_of(f0 ? g.q0 : g.q1);
+                    out.ops.push_back(r);
+                }
+                break;
+            }
+            }
+        }
+        for (int s = 0; s < npos; ++s) rp.a.store_q[s] = (uint8_t)label[s];
+        rp.a.nonlocal_mask = p.a.nonlocal_mask;
+        rp.a.n_tiles = p.a.n_tiles;
+        rp.a.n_ops = (uint32_t)out.ops.size() - rp.op_begin;
+        rp.a.n_mats = (uint32_t)(out.mats.size() / 8) - rp.mat_begin;
+        out.passes.push_back(rp);
     }
     return QF_OK;
 }

@@ -149,6 +149,62 @@ struct Pass {
     PassArgs a;
     uint32_t op_begin = 0;    // into Plan::ops
     uint32_t mat_begin = 0;   // into Plan::mats (matrix index)
+    uint64_t resident = 0;    // qubits resident in the tile
+    std::vector<BGate> gates; // the pass's gates in order (after 1q merging), global qubits; forward plans only
+};
+
+// ---- register-tiled passes (complex64) -------------------------------------
+// A CTA of 32 << WB threads holds a 2^(9+WB)-amplitude tile: lane bits are
+// qubits 0..4 (so every warp access is 256 contiguous bytes), each thread
+// keeps 16 amplitudes in registers (4 register qubits) and the warp index
+// spans WB more resident qubits. Gates on register qubits run in registers,
+// on lane qubits through warp shuffles; a warp-qubit gate first exchanges
+// register and warp qubits through shared memory (a remap). SWAPs among
+// register/warp qubits relabel positions and move no data.
+enum RsKind : uint8_t {
+    RS_MREG = 0,    // dense 2x2 on register position p0
+    RS_MLANE = 1,   // dense 2x2 on lane bit p0
+    RS_DIAG = 2,    // diag(m00, m11) on bit descriptor p0
+    RS_CNOT = 3,    // control descriptor p0, target descriptor p1 (lane or register)
+    RS_CZ = 4,      // descriptors p0, p1
+    RS_SWAP_LR = 5, // lane bit p0 <-> register position p1
+    RS_SWAP_LL = 6, // lane bits p0 <-> p1
+    RS_REMAP = 7    // a = old layout slots, b = new layout slots (3 bits per position)
+};
+// Bit descriptors: 0..4 lane bit, 8+r register position, 16+w warp position,
+// 64+q qubit q outside the tile.
+struct RsOp {
+    uint8_t kind;
+    uint8_t p0;
+    uint8_t p1;
+    uint8_t mk;    // matrix structure: 0 general, 1 real, 2 real diagonal + imaginary off-diagonal
+    uint32_t a;
+    uint32_t b;
+    uint32_t mat;  // matrix index
+};
+static_assert(sizeof(RsOp) == 16, "RsOp layout");
+
+struct RsPassArgs {
+    uint64_t nonlocal_mask;
+    uint64_t n_tiles;
+    uint32_t n_ops;
+    uint32_t n_mats;
+    uint8_t load_q[8];   // qubit at register positions 0..3 then warp positions 0..WB-1, at load
+    uint8_t store_q[8];  // the same at store (after relabels and remaps)
+};
+
+struct RsPass {
+    RsPassArgs a;
+    bool fallback = false;  // run this pass with the shared-memory tile kernel
+    uint32_t op_begin = 0;
+    uint32_t mat_begin = 0;
+};
+
+struct RsPlan {
+    int wb = 3;
+    std::vector<RsPass> passes;
+    std::vector<RsOp> ops;
+    std::vector<double> mats;
 };
 
 struct Plan {
@@ -169,6 +225,9 @@ struct PlanOpts {
 };
 
 int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, Plan &plan);
+// Lower a forward plan to register-tiled passes; passes whose tile is not
+// {qubits 0..4} plus 4 + wb more qubits are marked fallback.
+int lower_rs(const Plan &plan, int wb, RsPlan &out);
 // Default tile/low widths for a state.
 void default_tiling(uint32_t n, int dtype, int requested_tile, int *tile, int *low);
 
@@ -176,8 +235,11 @@ void default_tiling(uint32_t n, int dtype, int requested_tile, int *tile, int *l
 // Unfused single-gate sweeps.
 int launch_gate1(qf_sv *sv, const BGate &g);
 int launch_gate2(qf_sv *sv, const BGate &g);
-// Upload a plan's ops+matrices into the context workspace and run every pass.
-int run_plan(qf_sv *sv, const Plan &plan);
+// Upload a plan's ops+matrices into the context workspace and run every pass
+// (register-tiled for complex64 where the tile fits, shared memory otherwise).
+int run_plan(qf_sv *sv, const Plan &plan, int flags = 0);
+int run_plan_smem(qf_sv *sv, const Plan &plan);
+int run_plan_rs(qf_sv *sv, const Plan &plan, int wb);
 // Backward adjoint passes on (psi, lambda); overlap partials per slot are
 // accumulated into d_slot_sums (f64, plan.n_slots entries, not cleared here).
 int run_plan_dual(qf_sv *psi, qf_sv *lambda, const Plan &plan, double *d_slot_sums);

@@ -541,10 +541,21 @@ static int launch_passes(qf_sv *psi, qf_sv *lam, const Plan &plan, double *d_slo
     return QF_OK;
 }
 
-int run_plan(qf_sv *sv, const Plan &plan) {
+int run_plan_smem(qf_sv *sv, const Plan &plan) {
     if (plan.passes.empty()) return QF_OK;
     if (sv->dtype == QF_C64) return launch_passes<float2, false>(sv, nullptr, plan, nullptr);
     return launch_passes<double2, false>(sv, nullptr, plan, nullptr);
+}
+
+// complex64 plans with 12- or 13-qubit tiles run register-tiled; the rest
+// (complex128, small states, QF_EXEC_FLAG_SMEM_TILES) in shared memory.
+int run_plan(qf_sv *sv, const Plan &plan, int flags) {
+    if (plan.passes.empty()) return QF_OK;
+    if (sv->dtype == QF_C64 && !(flags & QF_EXEC_FLAG_SMEM_TILES) && sv->n >= 12) {
+        const uint32_t k = plan.passes[0].a.k;
+        if (k == 12 || k == 13) return run_plan_rs(sv, plan, (int)k - 9);
+    }
+    return run_plan_smem(sv, plan);
 }
 
 int run_plan_dual(qf_sv *psi, qf_sv *lambda, const Plan &plan, double *d_slot_sums) {
@@ -571,7 +582,7 @@ int execute_gates(qf_sv *sv, const std::vector<BGate> &gates, const qf_exec_opts
     default_tiling(sv->n, sv->dtype, opts ? opts->tile_qubits : 0, &po.tile_qubits, &po.low_qubits);
     Plan plan;
     QF_TRY(plan_passes(sv->n, gates, po, plan));
-    return run_plan(sv, plan);
+    return run_plan(sv, plan, opts ? opts->flags : 0);
 }
 
 }  // namespace qf

@@ -98,8 +98,7 @@ def gradient_with_inputs(circuit, options: GradientOptions, inputs, parameters, 
     o.shots = int(options.shots)
     o.checkpoint_every = int(checkpoint_every)
     if exec_opts:
-        mode = {"auto": _abi.EXEC_AUTO, "unfused": _abi.EXEC_UNFUSED, "fused": _abi.EXEC_FUSED}
-        o.exec = _abi.ExecOpts(mode[exec_opts.get("mode", "auto")], int(exec_opts.get("tile_qubits", 0)), 0, 0)
+        o.exec = _abi.exec_opts(exec_opts)
     grad = np.zeros(p.size, dtype=np.float64)
     e = C.c_double(float("nan"))
     info = _abi.GradientInfo()

@@ -266,6 +266,47 @@ def test_errors_are_typed_and_state_is_untouched(backend):
     assert e.value.kind == "MemoryBudgetExceeded"
 
 
+def _all_kinds_circuit(n, seed):
+    """Every gate kind on every qubit and every ordered pair of a spread of
+    qubits (lane, register and warp positions of the register-tiled pass)."""
+    r = np.random.default_rng(seed)
+    recs = []
+    for gate in range(12):
+        for q in range(n):
+            recs.append((A.OP_GATE, gate, q, 0, 0, float(r.uniform(-3, 3)) if gate >= A.GATE_RX else 0.0))
+    picks = sorted(set([0, 1, 3, 4, 5, 7, n // 2, n - 2, n - 1]))
+    for a in picks:
+        for b in picks:
+            if a != b:
+                for kind in (A.OP_CNOT, A.OP_CZ, A.OP_SWAP):
+                    recs.append((kind, 0, a, b, 0, 0.0))
+                    recs.append((A.OP_GATE, int(r.integers(4, 12)), int(r.integers(0, n)), 0, 0, float(r.uniform(-3, 3))))
+    return A.ops_array(recs)
+
+
+@pytest.mark.parametrize("n,tile", [(12, 12), (14, 12), (15, 13), (17, 12), (17, 13)])
+def test_register_tiled_passes_match_oracle_and_smem_kernel(backend, n, tile):
+    ops = _all_kinds_circuit(n, n * 31 + tile)
+    expected = O.run(ops, n)
+    sv = StateVector.zero(n, dtype="c64", backend=backend)
+    sv.apply_ops(ops, exec_opts={"tile_qubits": tile})
+    rs = sv.amplitudes()
+    sv2 = StateVector.zero(n, dtype="c64", backend=backend)
+    sv2.apply_ops(ops, exec_opts={"tile_qubits": tile, "smem_tiles": True})
+    sm = sv2.amplitudes()
+    assert close(rs, expected, C64_TOL)
+    assert close(sm, expected, C64_TOL)
+
+
+@pytest.mark.parametrize("n,seed,tile", [(12, 5, 12), (16, 6, 12), (21, 7, 12), (22, 8, 13)])
+def test_register_tiled_mixed_circuits(backend, n, seed, tile):
+    ops = W.random_circuit(n, 24, seed, two_qubit="mixed")
+    expected = O.run(ops, n, threads=8)
+    sv = StateVector.zero(n, dtype="c64", backend=backend)
+    sv.apply_ops(ops, exec_opts={"tile_qubits": tile})
+    assert close(sv.amplitudes(), expected, C64_TOL)
+
+
 def test_state_outliving_its_context_is_released_safely(engine_lib):
     from quantumforge_gb300 import CudaBackend
 
