@@ -364,6 +364,7 @@ def vqe_gradients(backend):
     for _ in range(reps):
         adj = gradient_with_inputs(pc, GradientOptions(strategy=GradientStrategy.Adjoint), [], params, n, H, **kw)
     t_adj = (time.perf_counter() - t0) / reps
+    pc.expectation_pauli_sum(params, n, H, dtype="c64", backend=backend)  # warm: compiles the forward passes
     t0 = time.perf_counter()
     sh = gradient_with_inputs(pc, GradientOptions(strategy=GradientStrategy.ParameterShift), [], params, n, H,
                               dtype="c64", backend=backend)

@@ -131,6 +131,8 @@ enum qf_exec_mode {
 
 /* qf_exec_opts.flags */
 #define QF_EXEC_FLAG_SMEM_TILES 1  /* complex64: use the shared-memory tile kernel instead of register tiles */
+#define QF_EXEC_FLAG_JIT 2         /* complex64: compile the plan's passes (NVRTC) even for small states */
+#define QF_EXEC_FLAG_NO_JIT 4      /* complex64: never compile passes; interpret them */
 
 typedef struct qf_exec_opts {
     int32_t mode;          /* enum qf_exec_mode */

@@ -89,15 +89,21 @@ class ExecOpts(C.Structure):
 
 
 EXEC_FLAG_SMEM_TILES = 1
+EXEC_FLAG_JIT = 2
+EXEC_FLAG_NO_JIT = 4
 _MODES = {"auto": EXEC_AUTO, "unfused": EXEC_UNFUSED, "fused": EXEC_FUSED}
 
 
 def exec_opts(opts) -> "ExecOpts":
-    """qf_exec_opts from a dict {mode, tile_qubits, block_qubits, smem_tiles}."""
+    """qf_exec_opts from a dict {mode, tile_qubits, block_qubits, smem_tiles, jit}."""
     if isinstance(opts, ExecOpts):
         return opts
     opts = opts or {}
     flags = EXEC_FLAG_SMEM_TILES if opts.get("smem_tiles") else 0
+    if opts.get("jit") is True:
+        flags |= EXEC_FLAG_JIT
+    elif opts.get("jit") is False:
+        flags |= EXEC_FLAG_NO_JIT
     return ExecOpts(_MODES[opts.get("mode", "auto")], int(opts.get("tile_qubits", 0)), int(opts.get("block_qubits", 0)),
                     flags)
 

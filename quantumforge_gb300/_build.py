@@ -19,7 +19,7 @@ LIBDIR = PKG / "_lib"
 LIB = LIBDIR / "libqf_gb300.so"
 INCLUDE = PKG.parent / "include"
 
-SOURCES = ["api.cpp", "planner.cpp", "sweep.cu", "reduce.cu", "rspass.cu"]
+SOURCES = ["api.cpp", "planner.cpp", "sweep.cu", "reduce.cu", "rspass.cu", "jit.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O3", "--expt-relaxed-constexpr",
               "-Xptxas", "-O3", f"-I{INCLUDE}"]
@@ -65,7 +65,7 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
             for f in futs:
                 f.result()
     if force or jobs or not LIB.exists():
-        cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs)]
+        cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-ldl"]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")

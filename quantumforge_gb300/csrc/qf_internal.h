@@ -240,6 +240,14 @@ int launch_gate2(qf_sv *sv, const BGate &g);
 int run_plan(qf_sv *sv, const Plan &plan, int flags = 0);
 int run_plan_smem(qf_sv *sv, const Plan &plan);
 int run_plan_rs(qf_sv *sv, const Plan &plan, int wb);
+// Compiled register-tiled passes (jit.cpp); states of at least kJitMinQubits
+// qubits use them by default.
+constexpr uint32_t kJitMinQubits = 24;
+bool jit_available();
+int run_plan_jit(qf_sv *sv, const Plan &plan, int wb);
+// Generate the plan's pass kernels and compile them with NVRTC without
+// loading them (no GPU needed); for tests of the code generator.
+int jit_check_compile(const Plan &plan, int wb, std::string *source, std::string *err);
 // Backward adjoint passes on (psi, lambda); overlap partials per slot are
 // accumulated into d_slot_sums (f64, plan.n_slots entries, not cleared here).
 int run_plan_dual(qf_sv *psi, qf_sv *lambda, const Plan &plan, double *d_slot_sums);

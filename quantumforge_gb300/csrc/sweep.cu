@@ -553,6 +553,11 @@ int run_plan(qf_sv *sv, const Plan &plan, int flags) {
     if (plan.passes.empty()) return QF_OK;
     if (sv->dtype == QF_C64 && !(flags & QF_EXEC_FLAG_SMEM_TILES) && sv->n >= 12) {
         const uint32_t k = plan.passes[0].a.k;
+        // compiled passes for large states (the compile is amortised over many
+        // sweeps of the state), interpreted register tiles otherwise
+        const bool jit = k == 12 && !(flags & QF_EXEC_FLAG_NO_JIT) &&
+                         ((flags & QF_EXEC_FLAG_JIT) || sv->n >= kJitMinQubits) && jit_available();
+        if (jit) return run_plan_jit(sv, plan, 3);
         if (k == 12 || k == 13) return run_plan_rs(sv, plan, (int)k - 9);
     }
     return run_plan_smem(sv, plan);

@@ -307,6 +307,21 @@ def test_register_tiled_mixed_circuits(backend, n, seed, tile):
     assert close(sv.amplitudes(), expected, C64_TOL)
 
 
+@pytest.mark.parametrize("n,seed,kinds", [(14, 3, True), (17, 4, False), (20, 9, False)])
+def test_compiled_passes_match_oracle(backend, n, seed, kinds):
+    """Passes compiled by the pass compiler (NVRTC) against the oracle, and
+    a second run of the same structure with new angles (cached kernels)."""
+    ops = _all_kinds_circuit(n, seed) if kinds else W.random_circuit(n, 16, seed, two_qubit="mixed")
+    for trial in range(2):
+        if trial == 1:  # same structure, new angles: reuses the compiled kernels
+            ops = ops.copy()
+            ops["theta"] = ops["theta"] * 0.7 + 0.1
+        expected = O.run(ops, n, threads=8)
+        sv = StateVector.zero(n, dtype="c64", backend=backend)
+        sv.apply_ops(ops, exec_opts={"jit": True})
+        assert close(sv.amplitudes(), expected, C64_TOL), trial
+
+
 def test_state_outliving_its_context_is_released_safely(engine_lib):
     from quantumforge_gb300 import CudaBackend
 
