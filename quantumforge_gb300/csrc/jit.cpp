@@ -88,6 +88,7 @@ struct Gen {
     std::complex<double> gphase{1.0, 0.0};
     bool any_diag = false;
     int wb = 3;
+    bool prefetch = true;  // double-buffered cp.async tile loads
 
     std::string R(int i) const { return "r" + std::to_string(v[i]); }
     int slot(const std::complex<double> a, const std::complex<double> b, const std::complex<double> c,
@@ -181,9 +182,9 @@ void gen_pass(Gen &g, const RsPlan &rp, const RsPass &p, int index) {
     for (int i = 0; i < kR; ++i) g.v[i] = i;
     bool has_remap = false;
     for (uint32_t o = 0; o < p.a.n_ops; ++o) has_remap |= rp.ops[p.op_begin + o].kind == RS_REMAP;
-    s << "extern \"C\" __global__ void __launch_bounds__(" << (32 << wb) << ", " << (wb == 3 ? 2 : 1) << ") p" << index
+    const int nt_threads = 32 << wb, tile = kR * nt_threads;
+    s << "extern \"C\" __global__ void __launch_bounds__(" << nt_threads << ", " << (wb == 3 ? 2 : 1) << ") p" << index
       << "(float2* __restrict__ A, unsigned long long nt) {\n";
-    if (has_remap) s << "__shared__ float2 S[" << kR * (32 << wb) << "];\n";
     s << "const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;\n";
     auto warp_off = [&](const uint8_t *qs) {
         std::ostringstream o;
@@ -192,10 +193,55 @@ void gen_pass(Gen &g, const RsPlan &rp, const RsPass &p, int index) {
         return o.str();
     };
     s << "const unsigned long long lw = " << warp_off(p.a.load_q) << ", sw = " << warp_off(p.a.store_q) << ";\n";
-    s << "for (unsigned long long t = blockIdx.x; t < nt; t += gridDim.x) {\n";
-    s << "const unsigned long long tb = " << deposit_code(p.a.nonlocal_mask) << ";\n";
-    s << "const unsigned long long b0 = tb | lane | lw;\n";
-    for (int i = 0; i < kR; ++i) s << "float2 r" << i << " = A[b0 | " << layout_offset(p.a.load_q, i) << "];\n";
+    const std::string dep = deposit_code(p.a.nonlocal_mask);
+    if (g.prefetch) {
+        // Double-buffered asynchronous tile loads: tile t+1 streams into shared
+        // memory (16-byte cp.async) while tile t is computed. Shared index j of
+        // a tile: bits 0..4 = qubits 0..4, bits 5..8 = register positions,
+        // bits 9.. = warp positions (load layout). Thread tid copies chunks
+        // tid + nthreads*k (two amplitudes each).
+        s << "extern __shared__ __align__(16) float2 SB[];\n";
+        s << "const unsigned tid = threadIdx.x, sbase = (unsigned)__cvta_generic_to_shared(SB);\n";
+        s << "const unsigned long long toff = (unsigned long long)((2u * tid) & 31u)";
+        for (int b = 0; b < 4; ++b) s << " | ((tid & " << (16u << b) << "u) ? (1ull << " << (int)p.a.load_q[b] << ") : 0ull)";
+        s << ";\n";
+        const int chunks = tile / 2 / nt_threads;  // per thread
+        auto issue = [&](const std::string &tq, const std::string &buf) {
+            for (int k = 0; k < chunks; ++k) {
+                uint64_t kk = 0;  // warp-position bits of chunk k (j >> 9 == k)
+                for (int w = 0; w < wb; ++w)
+                    if ((k >> w) & 1) kk |= 1ULL << p.a.load_q[4 + w];
+                s << "qf_cpa16(sbase + ((" << buf << ") * " << tile << "u + 2u * (tid + " << nt_threads * k << "u)) * 8u, A + (" << tq
+                  << " | toff | 0x" << std::hex << kk << std::dec << "ull));\n";
+            }
+        };
+        s << "unsigned long long t = blockIdx.x;\n";
+        s << "if (t < nt) {const unsigned long long tq = " << dep << ";\n";
+        issue("tq", "0u");
+        s << "}\nasm volatile(\"cp.async.commit_group;\\n\" ::: \"memory\");\n";
+        s << "for (unsigned it = 0; t < nt; t += gridDim.x, ++it) {\n";
+        s << "const unsigned cur = it & 1u;\n";
+        // prefetch the CTA's next tile (the deposit expression reads `t`; substitute t2)
+        s << "{const unsigned long long t2 = t + gridDim.x; if (t2 < nt) {const unsigned long long tq = ";
+        {
+            std::string d2 = dep;
+            for (size_t pos = 0; (pos = d2.find("(t >>", pos)) != std::string::npos; pos += 6) d2.replace(pos, 5, "(t2 >>");
+            s << d2 << ";\n";
+        }
+        issue("tq", "cur ^ 1u");
+        s << "}}\nasm volatile(\"cp.async.commit_group;\\n\" ::: \"memory\");\n";
+        s << "asm volatile(\"cp.async.wait_group 1;\\n\" ::: \"memory\");\n__syncthreads();\n";
+        s << "float2* S = SB + cur * " << tile << "u;\n";
+        s << "const unsigned long long tb = " << dep << ";\n";
+        for (int i = 0; i < kR; ++i) s << "float2 r" << i << " = S[lane | " << (i << 5) << "u | (warp << 9)];\n";
+        s << "__syncthreads();\n";
+    } else {
+        if (has_remap) s << "__shared__ float2 S[" << tile << "];\n";
+        s << "for (unsigned long long t = blockIdx.x; t < nt; t += gridDim.x) {\n";
+        s << "const unsigned long long tb = " << dep << ";\n";
+        s << "const unsigned long long b0 = tb | lane | lw;\n";
+        for (int i = 0; i < kR; ++i) s << "float2 r" << i << " = A[b0 | " << layout_offset(p.a.load_q, i) << "];\n";
+    }
     const double *mats = rp.mats.data() + 8 * (size_t)p.mat_begin;
     for (uint32_t o = 0; o < p.a.n_ops; ++o) {
         const RsOp &op = rp.ops[p.op_begin + o];
@@ -360,7 +406,7 @@ JitCache &cache() {
     return c;
 }
 
-int compile_module(const std::string &src, int n_kernels, JitModule &out, std::string &err) {
+int compile_module(const std::string &src, int n_kernels, size_t dyn_smem, int device, JitModule &out, std::string &err) {
     Nvrtc &nv = nvrtc();
     if (!nv.ok) {
         err = nv.why;
@@ -404,6 +450,13 @@ int compile_module(const std::string &src, int n_kernels, JitModule &out, std::s
         err = std::string("cudaLibraryGetGlobal: ") + cudaGetErrorString(e);
         return QF_ERR_CUDA;
     }
+    if (dyn_smem > 48 * 1024)
+        for (int k = 0; k < n_kernels; ++k)
+            if ((e = cudaKernelSetAttributeForDevice(out.kernels[k], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)dyn_smem, device)) != cudaSuccess) {
+                err = std::string("cudaKernelSetAttributeForDevice: ") + cudaGetErrorString(e);
+                return QF_ERR_CUDA;
+            }
     return QF_OK;
 }
 
@@ -411,6 +464,7 @@ struct ModulePlan {
     std::string src;
     std::vector<float> consts;  // interleaved float2
     std::vector<int> pass_index;
+    size_t dyn_smem = 0;        // dynamic shared memory per CTA (prefetch buffers)
 };
 
 }  // namespace
@@ -418,9 +472,15 @@ struct ModulePlan {
 bool jit_available() { return nvrtc().ok; }
 
 // group passes into modules: at most 8 passes and 56 KB of constants each
+static bool jit_prefetch_enabled() {
+    const char *e = std::getenv("QF_JIT_PREFETCH");
+    return !(e && e[0] == '0');
+}
+
 static void gen_modules(const RsPlan &rp, int wb, std::vector<ModulePlan> &mods) {
     Gen g;
     g.wb = wb;
+    g.prefetch = jit_prefetch_enabled();
     const size_t npass = rp.passes.size();
     size_t pi = 0;
     while (pi < npass) {
@@ -447,7 +507,10 @@ static void gen_modules(const RsPlan &rp, int wb, std::vector<ModulePlan> &mods)
         }
         std::ostringstream head;
         head << "__constant__ float2 M[" << std::max<size_t>(1, g.consts.size()) << "];\n";
+        head << "__device__ __forceinline__ void qf_cpa16(unsigned s, const float2* g) {"
+                " asm volatile(\"cp.async.cg.shared.global [%0], [%1], 16;\\n\" :: \"r\"(s), \"l\"(g) : \"memory\"); }\n";
         mp.src = head.str() + body.str();
+        mp.dyn_smem = g.prefetch ? 2u * kR * (32u << wb) * sizeof(float) * 2 : 0;
         mp.consts.reserve(g.consts.size() * 2);
         for (auto &c : g.consts) {
             mp.consts.push_back((float)c.real());
@@ -517,7 +580,8 @@ int run_plan_jit(qf_sv *sv, const Plan &plan, int wb) {
             built[k] = std::make_shared<JitModule>();
             th.emplace_back([&, k, dev] {
                 cudaSetDevice(dev);
-                st[k] = compile_module(mods[todo[k]].src, (int)mods[todo[k]].pass_index.size(), *built[k], errs[k]);
+                st[k] = compile_module(mods[todo[k]].src, (int)mods[todo[k]].pass_index.size(), mods[todo[k]].dyn_smem, dev,
+                                       *built[k], errs[k]);
             });
         }
         for (auto &t : th) t.join();
@@ -539,13 +603,14 @@ int run_plan_jit(qf_sv *sv, const Plan &plan, int wb) {
         for (size_t k = 0; k < mods[m].pass_index.size(); ++k) {
             const RsPass &p = rp.passes[mods[m].pass_index[k]];
             int per_sm = 0;
-            QF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)jm.kernels[k], threads, 0));
+            const size_t dyn = mods[m].dyn_smem;
+            QF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)jm.kernels[k], threads, dyn));
             per_sm = std::max(per_sm, 1);
             const uint64_t grid = std::min<uint64_t>((uint64_t)per_sm * ctx->sm_count, p.a.n_tiles);
             float2 *amps = static_cast<float2 *>(sv->d);
             unsigned long long nt = p.a.n_tiles;
             void *args[] = {&amps, &nt};
-            QF_CUDA(cudaLaunchKernel((const void *)jm.kernels[k], dim3((unsigned)grid), dim3(threads), args, 0, ctx->stream));
+            QF_CUDA(cudaLaunchKernel((const void *)jm.kernels[k], dim3((unsigned)grid), dim3(threads), args, dyn, ctx->stream));
         }
     }
     return QF_OK;
