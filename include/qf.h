@@ -337,6 +337,29 @@ int qf_plan_stats(uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops,
  * Host only; `state` is a SmallRng state (after SmallRng::seeded). */
 uint64_t qf_rng_jump(uint64_t state, uint64_t steps);
 
+/* ---------------------------------------------------------------------------
+ * Allocation-free reduction. This entry point has no counterpart in the
+ * reference; it serves callers that cannot let a library allocate device
+ * memory: a host framework whose device memory all comes from its own pool
+ * allocator, or a latency-bound loop where cudaMalloc/cudaFree (which
+ * synchronise the device) are not acceptable.
+ *
+ * out[q] = <Z_q> for every qubit of the state at `d_amps` (caller-owned device
+ * memory on `device`: 2^qubits complex64 or complex128 amplitudes,
+ * interleaved, 8- or 16-byte aligned), the same values as
+ * qf_sv_expectation_z_all. The library calls no cudaMalloc, cudaFree or other
+ * allocating routine: its only scratch is a fixed array in the library's
+ * device image (about 84 KB, held on every GPU that loads the library until
+ * the process exits), which limits `qubits` to 1..40 (QF_ERR_STATE_TOO_LARGE
+ * beyond). `stream` is a cudaStream_t (NULL = the legacy default stream); the
+ * call returns after the result is on the host. The first call on a device
+ * looks up the scratch array's device address, so make it before any stream
+ * capture. Every call reuses the same scratch, so calls that overlap on the
+ * GPU race: serialise them.
+ * ------------------------------------------------------------------------- */
+int qf_expectation_z_all_noalloc(int device, const void *d_amps, uint32_t qubits, int dtype, void *stream,
+                                 double *out, uint64_t n_out);
+
 #ifdef __cplusplus
 }
 #endif

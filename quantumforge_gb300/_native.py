@@ -71,6 +71,7 @@ SIGNATURES = {
     "qf_expectation": [P, U32, C.c_int, P, U64, P, U64, P, U64, P, U64, P, PF64],
     "qf_plan_stats": [U32, C.c_int, P, U64, P, U64, P, U64, P, PU64, PU64],
     "qf_rng_jump": [U64, U64],
+    "qf_expectation_z_all_noalloc": [C.c_int, P, U32, C.c_int, P, P, U64],
 }
 RESTYPES = {"qf_last_error": C.c_char_p, "qf_status_name": C.c_char_p, "qf_rng_jump": U64}
 
