@@ -316,6 +316,7 @@ def run_ours(args):
     cpu = None
     if rank == 0 and not args.no_extra:
         extra["vqe24"] = vqe_gradients(backend)
+        extra["qaoa4096"] = qaoa_batch(backend, cpu=not args.no_cpu_baseline)
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, sample = time_cpu_oracle(n, ops, args.cpu_seconds, threads)
@@ -340,6 +341,62 @@ def run_ours(args):
     backend.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def qaoa_batch(backend, cpu: bool):
+    """4096 random 3-regular MaxCut instances, n uniform in {12..20}, p = 4:
+    cost and 8-parameter adjoint gradient per instance in one persistent
+    launch replayed from a CUDA graph, tiles autotuned per n."""
+    import numpy as np
+
+    from quantumforge_gb300 import workloads as W
+    from quantumforge_gb300.qaoa import QaoaBatch, autotune_tiles
+
+    problems, gam, bet = W.qaoa_batch_problems(4096)
+    tiles = autotune_tiles(problems, 4, candidates=(9, 10, 11, 12), reps=1, backend=backend)
+    batch = QaoaBatch(problems, 4, tile_qubits=tiles, backend=backend, use_graph=True)
+    batch.run(gam, bet)
+    reps = 3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        cost, grad = batch.run(gam, bet)
+    dt = (time.perf_counter() - t0) / reps
+    out = {"instances": len(problems), "sizes": [12, 14, 16, 18, 20], "p": 4, "batch_s": dt,
+           "instances_per_s": len(problems) / dt, "gradient_params_per_instance": 8, "tiles": tiles,
+           "dtype": "complex64", "host_copies_in_timing": True, "mean_cost": float(np.mean(cost))}
+    if cpu:
+        out["cpu_estimate"] = qaoa_cpu_estimate(problems)
+    return out
+
+
+def qaoa_cpu_estimate(problems):
+    """The reference's per-instance route — run qaoa_maxcut and
+    maxcut_expectation, central finite differences for 8 parameters (17
+    circuit evaluations) — with the oracle on every host core: one evaluation
+    timed per n in {12, 14, 16}, n = 18 and 20 extrapolated by the observed
+    per-qubit growth; averaged over the batch's size mix."""
+    import numpy as np
+
+    import oracle as O
+    from quantumforge_gb300 import workloads as W
+
+    threads = os.cpu_count() or 1
+    t_eval = {}
+    for n in (12, 14, 16):
+        edges = W.random_3_regular(n, 1)
+        ops = W.qaoa_maxcut(n, edges, 4, [0.3] * 4, [0.5] * 4)
+        t0 = time.perf_counter()
+        a = O.run(ops, n, threads=threads)
+        O.maxcut_expectation(a, edges)
+        t_eval[n] = time.perf_counter() - t0
+    growth = (t_eval[16] / t_eval[12]) ** (1 / 4)  # per qubit
+    t_eval[18] = t_eval[16] * growth ** 2
+    t_eval[20] = t_eval[16] * growth ** 4
+    per_inst = np.mean([17 * t_eval[n] for n, _ in problems])
+    return {"instances_per_s": 1.0 / per_inst, "cores": threads, "kind": "port",
+            "sample": "one circuit evaluation timed at n = 12, 14, 16 (18, 20 extrapolated); 17 evaluations per "
+                      "instance (cost + 8-parameter central differences)",
+            "eval_s": {str(k): v for k, v in t_eval.items()}}
 
 
 def vqe_gradients(backend):

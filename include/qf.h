@@ -322,6 +322,35 @@ int qf_expectation(qf_ctx *ctx, uint32_t qubits, int dtype,
                    const qf_exec_opts *opts, double *expectation);
 
 /* ---------------------------------------------------------------------------
+ * Batched QAOA MaxCut — replaces calling maxcut_qaoa_expectation
+ * (src/qaoa_transfer.rs:221-236) per instance, and its central
+ * finite-difference gradient (the `adagrad` optimiser, same file), for a batch
+ * of instances of uneven qubit counts: one persistent launch computes every
+ * instance's cost <C> (maxcut_expectation, src/qaoa_transfer.rs:199-218) and
+ * its exact adjoint gradient for the circuit algorithms::qaoa_maxcut
+ * (src/algorithms.rs:110-137) with unit edge weights. complex64 states,
+ * f64 accumulation.
+ * ------------------------------------------------------------------------- */
+typedef struct qf_qaoa_instance {
+    uint32_t qubits;       /* 2..30 */
+    uint32_t edge_begin;   /* first (u, v) pair in edges_uv */
+    uint32_t edge_count;   /* at most 96 */
+    uint32_t tile_qubits;  /* 0 = from qf_qaoa_opts.tile_qubits[qubits] (autotuned) */
+} qf_qaoa_instance;
+
+typedef struct qf_qaoa_opts {
+    int32_t use_graph;         /* capture the launch in a CUDA graph once per batch layout, then replay */
+    int32_t tile_qubits[33];   /* tile width per qubit count (0 = default) */
+} qf_qaoa_opts;
+
+/* gammas/betas: n_inst x p (row = instance). cost_out: n_inst values;
+ * grad_out: n_inst x 2p rows [dC/dγ_0..dC/dγ_{p-1}, dC/dβ_0..dC/dβ_{p-1}]. */
+int qf_qaoa_maxcut_batch(qf_ctx *ctx, const qf_qaoa_instance *inst, uint64_t n_inst,
+                         const uint32_t *edges_uv, uint64_t n_edges, uint32_t p,
+                         const double *gammas, const double *betas,
+                         double *cost_out, double *grad_out, const qf_qaoa_opts *opts);
+
+/* ---------------------------------------------------------------------------
  * Plan inspection (host only, no device needed): the pass schedule the fused
  * executor would use for a gate list. `n_passes` = HBM sweeps of the state,
  * `n_gates` = gates after parameter binding. Used by tests and the autotuner.

@@ -138,6 +138,34 @@ def random_3_regular(n: int, seed: int):
     raise RuntimeError("failed to sample a 3-regular graph")
 
 
+def qaoa_param_circuit(n: int, edges, p: int) -> np.ndarray:
+    """qaoa_maxcut as a parameterised op list for unit weights: parameter l is
+    theta_l = 2*gamma_l (every Rz of layer l), parameter p + l is
+    phi_l = 2*beta_l (every Rx of layer l); so dC/dgamma_l = 2 dC/dtheta_l."""
+    recs = [(_abi.OP_GATE, _abi.GATE_H, q, 0, 0, 0.0) for q in range(n)]
+    for layer in range(p):
+        for u, v, _w in edges:
+            recs.append((_abi.OP_CNOT, 0, u, v, 0, 0.0))
+            recs.append((_abi.OP_ROTATION, _abi.PAULI_Z, v, 0, layer, 0.0))
+            recs.append((_abi.OP_CNOT, 0, u, v, 0, 0.0))
+        for q in range(n):
+            recs.append((_abi.OP_ROTATION, _abi.PAULI_X, q, 0, p + layer, 0.0))
+    return _abi.ops_array(recs)
+
+
+def qaoa_batch_problems(count: int = 4096, sizes=(12, 14, 16, 18, 20), p: int = 4, seed: int = 11):
+    """Batched QAOA workload: `count` random 3-regular MaxCut instances with n
+    uniform over `sizes`, depth p, gamma uniform in [0, pi], beta in [0, pi/2]."""
+    rng = SmallRng.seeded(seed)
+    problems, gam, bet = [], [], []
+    for i in range(count):
+        n = sizes[rng.next_u64() % len(sizes)]
+        problems.append((n, random_3_regular(n, seed * 1_000_003 + i)))
+        gam.append([math.pi * rng.next_f64() for _ in range(p)])
+        bet.append([0.5 * math.pi * rng.next_f64() for _ in range(p)])
+    return problems, np.array(gam), np.array(bet)
+
+
 def qaoa_maxcut(n: int, edges, p: int, betas, gammas) -> np.ndarray:
     """algorithms::qaoa_maxcut (src/algorithms.rs:110-137): H on all; per layer
     CNOT(u,v), Rz(2*gamma*w) on v, CNOT(u,v) for every edge, then Rx(2*beta)

@@ -1,0 +1,69 @@
+"""Batched QAOA MaxCut against the oracle: the cost is maxcut_expectation of
+the qaoa_maxcut circuit; the gradient is the oracle's parameter shift on the
+same circuit with shared parameters theta_l = 2 gamma_l, phi_l = 2 beta_l.
+complex64 state: cost within 1e-5 relative, gradient within 1e-4."""
+import numpy as np
+import pytest
+
+import oracle as O
+from quantumforge_gb300 import PauliSum
+from quantumforge_gb300 import workloads as W
+from quantumforge_gb300.qaoa import QaoaBatch, autotune_tiles
+
+pytestmark = pytest.mark.gpu
+
+
+def oracle_cost_grad(n, edges, gam, bet):
+    p = len(gam)
+    ops = W.qaoa_param_circuit(n, edges, p)
+    params = np.concatenate([2 * np.asarray(gam), 2 * np.asarray(bet)])
+    H = PauliSum.maxcut(edges).array()
+    e, g = O.adjoint_uncompute(ops, n, params, H)
+    return e, 2 * g
+
+
+def test_param_circuit_matches_the_reference_builder():
+    edges = O.random_3_regular(8, 3)
+    gam, bet = [0.3, 1.1], [0.7, 0.2]
+    a = O.run(W.qaoa_maxcut(8, edges, 2, bet, gam), 8)
+    b = O.run(W.qaoa_param_circuit(8, edges, 2), 8, params=np.concatenate([2 * np.array(gam), 2 * np.array(bet)]))
+    assert np.abs(a - b).max() < 1e-12
+    assert abs(O.maxcut_expectation(a, edges) - O.pauli_expectation(a, PauliSum.maxcut(edges).array()).real) < 1e-12
+
+
+@pytest.mark.parametrize("tiles", [None, {4: 4, 6: 4, 8: 5, 10: 6, 12: 7}])
+@pytest.mark.parametrize("graph", [False, True])
+def test_batch_matches_oracle(backend, tiles, graph):
+    rng = np.random.default_rng(4)
+    problems = []
+    for i, n in enumerate([4, 6, 8, 10, 12, 12, 10, 8, 6, 4]):
+        problems.append((n, O.random_3_regular(n, 100 + i)))
+    p = 3
+    gam = rng.uniform(0, np.pi, (len(problems), p))
+    bet = rng.uniform(0, np.pi / 2, (len(problems), p))
+    batch = QaoaBatch(problems, p, tile_qubits=tiles, backend=backend, use_graph=graph)
+    cost, grad = batch.run(gam, bet)
+    for i, (n, edges) in enumerate(problems):
+        e_ref, g_ref = oracle_cost_grad(n, edges, gam[i], bet[i])
+        assert abs(cost[i] - e_ref) < 1e-5 * max(1.0, abs(e_ref)), (i, cost[i], e_ref)
+        assert np.abs(grad[i] - g_ref).max() < 1e-4, (i, grad[i], g_ref)
+    # a second call with new angles (the graph is replayed)
+    cost2, grad2 = batch.run(gam * 0.5, bet * 0.5)
+    e_ref, g_ref = oracle_cost_grad(problems[3][0], problems[3][1], gam[3] * 0.5, bet[3] * 0.5)
+    assert abs(cost2[3] - e_ref) < 1e-5 * max(1.0, abs(e_ref))
+    assert np.abs(grad2[3] - g_ref).max() < 1e-4
+
+
+def test_uniform_superposition_cuts_half_the_edges(backend):
+    # gamma = beta = 0: the state is H^n |0>, every edge is cut with probability 1/2
+    problems = [(n, O.random_3_regular(n, n)) for n in (12, 14, 16)]
+    batch = QaoaBatch(problems, 2, backend=backend)
+    cost, grad = batch.run(np.zeros((3, 2)), np.zeros((3, 2)))
+    for (n, edges), c in zip(problems, cost):
+        assert abs(c - 0.5 * len(edges)) < 1e-5
+
+
+def test_autotune_returns_a_tile_per_size(backend):
+    problems = [(n, O.random_3_regular(n, n + 7)) for n in (12, 14) for _ in range(8)]
+    best = autotune_tiles(problems, 2, candidates=(8, 10, 12), reps=1, backend=backend)
+    assert set(best) == {12, 14} and all(k in (8, 10, 12) for k in best.values())
