@@ -317,6 +317,7 @@ def run_ours(args):
     if rank == 0 and not args.no_extra:
         extra["vqe24"] = vqe_gradients(backend)
         extra["qaoa4096"] = qaoa_batch(backend, cpu=not args.no_cpu_baseline)
+        extra["shots20"] = shots20(backend, cpu=not args.no_cpu_baseline)
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, sample = time_cpu_oracle(n, ops, args.cpu_seconds, threads)
@@ -341,6 +342,47 @@ def run_ours(args):
     backend.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def shots20(backend, cpu: bool):
+    """20 qubits complex128, depth-20 random circuit with CNOT ladders:
+    probabilities, <Z_i> for all i and 10^5 seeded shots (measure(q, q) for
+    every qubit), checked against the oracle's exact memoised sampler."""
+    import numpy as np
+
+    import oracle as O
+    import quantumforge_gb300 as qf
+    from quantumforge_gb300 import workloads as W
+
+    n, shots, seed = 20, 100_000, 42
+    ops = W.random_circuit(n, 20, 7)
+    mops = W.with_terminal_measurements(ops, n)
+    circ = qf.Circuit.from_ops(mops)
+    res = circ.run_shots(n, shots, seed, dtype="c128", backend=backend, tie_eps=1e-12)  # warm
+    t0 = time.perf_counter()
+    sv = qf.StateVector.zero(n, dtype="c128", backend=backend)
+    sv.apply_ops(ops)
+    probs = sv.probabilities()
+    zs = sv.expectation_z_all()
+    t_state = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    res = circ.run_shots(n, shots, seed, dtype="c128", backend=backend, tie_eps=1e-12)
+    t_shots = time.perf_counter() - t0
+    out = {"qubits": n, "gates": len(ops), "shots": shots, "seed": seed, "run_probs_z_s": t_state,
+           "shots_call_s": t_shots, "shots_per_s": shots / t_shots, "ties": res.ties, "distinct_outcomes": len(res.counts)}
+    exp_packed, width = O.run_shots(mops, n, shots, seed, threads=os.cpu_count() or 1)
+    out["counts_bit_exact_vs_oracle"] = res.counts == O.counts(exp_packed, width)
+    a = O.run(ops, n, threads=os.cpu_count() or 1)
+    out["max_prob_err_vs_oracle"] = float(np.abs(probs - O.probabilities(a)).max())
+    out["max_z_err_vs_oracle"] = float(max(abs(zs[q] - O.expectation(a, 2, q)) for q in range(n)))
+    if cpu:
+        # the reference re-simulates every shot (run_shots_impl); 2 shots timed
+        t0 = time.perf_counter()
+        O.run_shots(mops, n, 2, seed, literal=True)
+        t2 = time.perf_counter() - t0
+        out["cpu_literal_shots_per_s"] = 2 / t2
+        out["cpu_sample"] = "2 shots of the literal per-shot re-simulation (oracle restating run_shots_impl, one thread)"
+    return out
 
 
 def qaoa_batch(backend, cpu: bool):
