@@ -1,21 +1,33 @@
-// jit.cpp — pass compiler for complex64 register-tiled sweeps.
+// jit.cpp — pass compiler for complex64 tile sweeps.
 //
-// A register-tiled plan (lower_rs) is turned into CUDA C with one kernel per
-// pass: register positions, lane bits, layouts, remaps and the tile-address
-// deposit are compile-time constants; CNOTs and SWAPs whose qubits are all in
-// register positions become renames of the register variables and emit no
-// code; matrix entries are read from __constant__ memory, so a structurally
-// identical circuit with new angles reuses the compiled kernels. Diagonal
-// gates are applied as diag(1, m11/m00) and the product of the m00 factors is
-// applied once at the end of the plan (a global phase).
+// Each pass of a forward plan (a run of gates on 12 resident qubits) becomes
+// one straight-line CUDA kernel. A CTA of 256 threads handles a 4096-amplitude
+// tile per loop iteration: the tile streams into shared memory one iteration
+// ahead (16-byte cp.async, double buffered), is read into 16 registers per
+// thread in a layout that assigns the 12 resident qubits to 5 lane bits, 4
+// register bits and 3 warp bits, and every dense gate runs on a register
+// qubit: when a gate's qubit is not in a register position the tile is
+// re-read from shared memory in a new layout (a remap). Diagonal gates, CZ and
+// CNOT controls read their qubit's bit wherever it lives; CNOTs inside the
+// register positions are renames of the register variables and SWAPs of
+// resident qubits are relabels, neither emits an instruction. Shared memory
+// is XOR-swizzled on bits 1..3 so that warp accesses in any layout are
+// (nearly) conflict-free while 16-byte chunks stay contiguous. The tile is
+// stored straight from registers when the lanes hold qubits 0..4, otherwise
+// through shared memory in coalesced 16-byte chunks.
 //
+// Matrices are read from __constant__ memory (real ones as packed f32x2
+// pairs), so a structurally identical circuit with new angles reuses the
+// compiled kernels; diagonal gates are applied as diag(1, m11/m00) and the
+// product of the m00 factors once at the end of the plan (a global phase).
 // Kernels are compiled with NVRTC (loaded with dlopen) for sm_103a, loaded
-// with cudaLibraryLoadData and cached per context by source text.
+// with cudaLibraryLoadData and cached by source text.
 #include <dlfcn.h>
 #include <nvrtc.h>
 
 #include <algorithm>
 #include <complex>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -79,41 +91,44 @@ Nvrtc &nvrtc() {
 }
 
 // ---- code generation ---------------------------------------------------------
-constexpr int kR = 16;
+constexpr int kR = 16;        // amplitudes per thread
+constexpr int kPos = 12;      // positions: 0..4 lane bits, 5..8 register bits, 9..11 warp bits
+constexpr int kTile = 4096;   // amplitudes per tile
+constexpr int kThreads = 256;
+constexpr int kChunks = kTile / 2 / kThreads;  // 16-byte chunks per thread
+
+uint32_t swz(uint32_t j) { return ((j >> 4) ^ (j >> 7) ^ (j >> 10)) & 7u; }
+uint32_t physj(uint32_t j) { return j ^ (swz(j) << 1); }
 
 struct Gen {
     std::ostringstream s;
-    int v[kR];  // logical register -> variable number
+    int v[kR];                                 // logical register -> variable number
     std::vector<std::complex<double>> consts;  // 4 complex per matrix slot (float2 M[...])
     std::complex<double> gphase{1.0, 0.0};
     bool any_diag = false;
-    int wb = 3;
-    bool prefetch = true;  // double-buffered cp.async tile loads
+    int tmp = 0;
 
     std::string R(int i) const { return "r" + std::to_string(v[i]); }
-    int slot(const std::complex<double> a, const std::complex<double> b, const std::complex<double> c,
-             const std::complex<double> d) {
+    std::string fresh(const char *stem) { return std::string(stem) + std::to_string(tmp++); }
+    int slot(std::complex<double> a, std::complex<double> b, std::complex<double> c, std::complex<double> d) {
         consts.push_back(a);
         consts.push_back(b);
         consts.push_back(c);
         consts.push_back(d);
         return (int)consts.size() / 4 - 1;
     }
-    // thread-constant bit expression of a descriptor (lane/warp/outside)
-    static std::string cbit(uint8_t d) {
-        if (d < 8) return "((lane >> " + std::to_string(d) + ") & 1u)";
-        if (d >= 16 && d < 64) return "((warp >> " + std::to_string(d - 16) + ") & 1u)";
-        return "((unsigned)(tb >> " + std::to_string(d - 64) + ") & 1u)";
-    }
-    static bool is_reg(uint8_t d) { return d >= 8 && d < 16; }
 };
-
-std::complex<double> cx(const double *m, int k) { return {m[2 * k], m[2 * k + 1]}; }
 
 std::string Mref(int slot, int e) { return "M[" + std::to_string(4 * slot + e) + "]"; }
 
-// deposit of the tile index t onto the outside qubits, as runs of shifts
-std::string deposit_code(uint64_t mask) {
+std::string hex64(uint64_t v) {
+    std::ostringstream o;
+    o << "0x" << std::hex << v << "ull";
+    return o.str();
+}
+
+// deposit of the tile index `var` onto the outside qubits, as runs of shifts
+std::string deposit_code(uint64_t mask, const std::string &var) {
     std::ostringstream o;
     o << "0ull";
     int consumed = 0;
@@ -125,30 +140,37 @@ std::string deposit_code(uint64_t mask) {
         int e = q;
         while (e < 64 && ((mask >> e) & 1ULL)) ++e;
         const int len = e - q;
-        o << " | (((t >> " << consumed << ") & 0x" << std::hex << ((len >= 64) ? ~0ULL : ((1ULL << len) - 1)) << std::dec
-          << "ull) << " << q << ")";
+        o << " | (((" << var << " >> " << consumed << ") & " << hex64(len >= 64 ? ~0ULL : ((1ULL << len) - 1)) << ") << "
+          << q << ")";
         consumed += len;
         q = e;
     }
     return o.str();
 }
 
-std::string layout_offset(const uint8_t *qs, int i) {
-    uint64_t off = 0;
-    for (int b = 0; b < 4; ++b)
-        if ((i >> b) & 1) off |= 1ULL << qs[b];
-    std::ostringstream o;
-    o << "0x" << std::hex << off << "ull";
-    return o.str();
+uint8_t matrix_kind_of(const std::complex<double> m[4]) {
+    bool real = true;
+    for (int k = 0; k < 4; ++k) real = real && m[k].imag() == 0.0;
+    if (real) return 1;
+    if (m[0].imag() == 0 && m[3].imag() == 0 && m[1].real() == 0 && m[2].real() == 0) return 2;
+    return 0;
 }
 
+void emit_cmul_const(Gen &g, const std::string &R, int slot, int e) {
+    const std::string f = Mref(slot, e);
+    g.s << "{const float2 x=" << R << ";" << R << ".x=" << f << ".x*x.x-" << f << ".y*x.y;" << R << ".y=" << f
+        << ".x*x.y+" << f << ".y*x.x;}\n";
+}
+
+// A dense 2x2 on the pair (A, B); real matrices use packed f32x2 FMA with
+// splatted constants.
 void emit_mat2(Gen &g, int slot, int mk, const std::string &A, const std::string &B) {
     const std::string m00 = Mref(slot, 0), m01 = Mref(slot, 1), m10 = Mref(slot, 2), m11 = Mref(slot, 3);
     auto &s = g.s;
     s << "{const float2 x=" << A << ",y=" << B << ";";
     if (mk == 1) {
-        s << A << ".x=" << m00 << ".x*x.x+" << m01 << ".x*y.x;" << A << ".y=" << m00 << ".x*x.y+" << m01 << ".x*y.y;";
-        s << B << ".x=" << m10 << ".x*x.x+" << m11 << ".x*y.x;" << B << ".y=" << m10 << ".x*x.y+" << m11 << ".x*y.y;";
+        s << A << "=qf_ffma2(" << m01 << ",y,qf_fmul2(" << m00 << ",x));";
+        s << B << "=qf_ffma2(" << m11 << ",y,qf_fmul2(" << m10 << ",x));";
     } else if (mk == 2) {
         s << A << ".x=" << m00 << ".x*x.x-" << m01 << ".y*y.y;" << A << ".y=" << m00 << ".x*x.y+" << m01 << ".y*y.x;";
         s << B << ".x=" << m11 << ".x*y.x-" << m10 << ".y*x.y;" << B << ".y=" << m11 << ".x*y.y+" << m10 << ".y*x.x;";
@@ -161,233 +183,433 @@ void emit_mat2(Gen &g, int slot, int mk, const std::string &A, const std::string
     s << "}\n";
 }
 
-void emit_cmul_const(Gen &g, const std::string &R, int slot, int e) {
-    const std::string f = Mref(slot, e);
-    g.s << "{const float2 x=" << R << ";" << R << ".x=" << f << ".x*x.x-" << f << ".y*x.y;" << R << ".y=" << f
-        << ".x*x.y+" << f << ".y*x.x;}\n";
-}
+// One pass -> one kernel.
+struct PassGen {
+    Gen &g;
+    const Pass &p;
+    uint32_t n;
+    int slot_of[64];
+    uint32_t slot_q[kPos];
+    uint32_t L[kPos];  // position -> qubit
 
-uint8_t matrix_kind_of(const std::complex<double> m[4]) {
-    bool real = true;
-    for (int k = 0; k < 4; ++k) real = real && m[k].imag() == 0.0;
-    if (real) return 1;
-    if (m[0].imag() == 0 && m[3].imag() == 0 && m[1].real() == 0 && m[2].real() == 0) return 2;
-    return 0;
-}
-
-// one pass -> kernel body
-void gen_pass(Gen &g, const RsPlan &rp, const RsPass &p, int index) {
-    auto &s = g.s;
-    const int wb = rp.wb;
-    for (int i = 0; i < kR; ++i) g.v[i] = i;
-    bool has_remap = false;
-    for (uint32_t o = 0; o < p.a.n_ops; ++o) has_remap |= rp.ops[p.op_begin + o].kind == RS_REMAP;
-    const int nt_threads = 32 << wb, tile = kR * nt_threads;
-    s << "extern \"C\" __global__ void __launch_bounds__(" << nt_threads << ", " << (wb == 3 ? 2 : 1) << ") p" << index
-      << "(float2* __restrict__ A, unsigned long long nt) {\n";
-    s << "const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;\n";
-    auto warp_off = [&](const uint8_t *qs) {
-        std::ostringstream o;
-        o << "0ull";
-        for (int w = 0; w < wb; ++w) o << " | ((warp & " << (1 << w) << "u) ? (1ull << " << (int)qs[4 + w] << ") : 0ull)";
-        return o.str();
-    };
-    s << "const unsigned long long lw = " << warp_off(p.a.load_q) << ", sw = " << warp_off(p.a.store_q) << ";\n";
-    const std::string dep = deposit_code(p.a.nonlocal_mask);
-    if (g.prefetch) {
-        // Double-buffered asynchronous tile loads: tile t+1 streams into shared
-        // memory (16-byte cp.async) while tile t is computed. Shared index j of
-        // a tile: bits 0..4 = qubits 0..4, bits 5..8 = register positions,
-        // bits 9.. = warp positions (load layout). Thread tid copies chunks
-        // tid + nthreads*k (two amplitudes each).
-        s << "extern __shared__ __align__(16) float2 SB[];\n";
-        s << "const unsigned tid = threadIdx.x, sbase = (unsigned)__cvta_generic_to_shared(SB);\n";
-        s << "const unsigned long long toff = (unsigned long long)((2u * tid) & 31u)";
-        for (int b = 0; b < 4; ++b) s << " | ((tid & " << (16u << b) << "u) ? (1ull << " << (int)p.a.load_q[b] << ") : 0ull)";
-        s << ";\n";
-        const int chunks = tile / 2 / nt_threads;  // per thread
-        auto issue = [&](const std::string &tq, const std::string &buf) {
-            for (int k = 0; k < chunks; ++k) {
-                uint64_t kk = 0;  // warp-position bits of chunk k (j >> 9 == k)
-                for (int w = 0; w < wb; ++w)
-                    if ((k >> w) & 1) kk |= 1ULL << p.a.load_q[4 + w];
-                s << "qf_cpa16(sbase + ((" << buf << ") * " << tile << "u + 2u * (tid + " << nt_threads * k << "u)) * 8u, A + (" << tq
-                  << " | toff | 0x" << std::hex << kk << std::dec << "ull));\n";
+    PassGen(Gen &gen, const Pass &pass, uint32_t nq) : g(gen), p(pass), n(nq) {
+        for (int q = 0; q < 64; ++q) slot_of[q] = -1;
+        int s = 0;
+        for (uint32_t q = 0; q < n; ++q)
+            if ((p.resident >> q) & 1ULL) {
+                slot_of[q] = s;
+                slot_q[s++] = q;
             }
+    }
+    int pos_of(uint32_t q) const {
+        for (int i = 0; i < kPos; ++i)
+            if (L[i] == q) return i;
+        return -1;
+    }
+    // bit descriptor of qubit q in the current layout
+    uint8_t desc(uint32_t q) const {
+        const int ps = pos_of(q);
+        if (ps < 0) return (uint8_t)(64 + q);
+        if (ps < 5) return (uint8_t)ps;
+        if (ps < 9) return (uint8_t)(8 + ps - 5);
+        return (uint8_t)(16 + ps - 9);
+    }
+    static bool is_reg(uint8_t d) { return d >= 8 && d < 16; }
+    static std::string cbit(uint8_t d) {
+        if (d < 8) return "((lane >> " + std::to_string(d) + ") & 1u)";
+        if (d >= 16 && d < 64) return "((warp >> " + std::to_string(d - 16) + ") & 1u)";
+        return "((unsigned)(tb >> " + std::to_string(d - 64) + ") & 1u)";
+    }
+    // ---- gate scheduling inside the pass ----
+    // Gates commute unless they share a qubit on which one of them is not
+    // diagonal (a diagonal 1q gate, both CZ qubits and a CNOT control are
+    // diagonal on their qubit). A gate runs once every earlier gate it does
+    // not commute with has run and, for a dense gate or a CNOT target, once
+    // its qubit sits in a register position. Diagonal 1q gates wait for their
+    // qubit to reach a register too (half the multiplies) unless only they
+    // are left.
+    std::vector<std::vector<int>> preds;
+    std::vector<char> done;
+    std::vector<int> order;  // gate indices in emission order
+    bool failed = false;
+
+    static bool diag_on(const BGate &x, uint32_t q) {
+        switch (x.kind) {
+        case BK_MAT1: return x.diag != 0;
+        case BK_CNOT: return q == x.q0;
+        case BK_CZ: return true;
+        default: return false;
+        }
+    }
+    static int arity(const BGate &x) { return x.kind == BK_MAT1 ? 1 : 2; }
+    static uint32_t qubit(const BGate &x, int k) { return k ? x.q1 : x.q0; }
+    void build_deps() {
+        const auto &G = p.gates;
+        preds.assign(G.size(), {});
+        done.assign(G.size(), 0);
+        for (size_t j = 0; j < G.size(); ++j)
+            for (size_t i = 0; i < j; ++i) {
+                bool conflict = false;
+                for (int a = 0; a < arity(G[i]) && !conflict; ++a)
+                    for (int b = 0; b < arity(G[j]) && !conflict; ++b) {
+                        const uint32_t q = qubit(G[i], a);
+                        if (q == qubit(G[j], b) && !(diag_on(G[i], q) && diag_on(G[j], q))) conflict = true;
+                    }
+                if (conflict) preds[j].push_back((int)i);
+            }
+    }
+    bool ready(size_t j, const std::vector<char> &d) const {
+        for (int i : preds[j])
+            if (!d[i]) return false;
+        return true;
+    }
+    static bool strict_need(const BGate &x) { return (x.kind == BK_MAT1 && !x.diag) || x.kind == BK_CNOT; }
+    bool runnable(const BGate &x, uint64_t regs, bool force_diag) const {
+        if (x.kind == BK_MAT1)  // a diagonal gate on a qubit outside the tile never reaches a register
+            return ((regs >> x.q0) & 1ULL) || (x.diag && (force_diag || !((p.resident >> x.q0) & 1ULL)));
+        if (x.kind == BK_CNOT) return (regs >> x.q1) & 1ULL;
+        return true;
+    }
+    // gates that would run with `regs` in register positions, from state `d`
+    // (updated); SWAPs move register membership with the labels
+    int simulate(uint64_t regs, std::vector<char> &d, bool force_diag, int *strict) const {
+        const auto &G = p.gates;
+        int count = 0, st = 0;
+        for (bool progress = true; progress;) {
+            progress = false;
+            for (size_t j = 0; j < G.size(); ++j) {
+                if (d[j] || !ready(j, d) || !runnable(G[j], regs, force_diag)) continue;
+                d[j] = 1;
+                ++count;
+                st += strict_need(G[j]);
+                if (G[j].kind == BK_SWAP) {
+                    const uint64_t a = (regs >> G[j].q0) & 1ULL, b = (regs >> G[j].q1) & 1ULL;
+                    if (a != b) regs ^= (1ULL << G[j].q0) | (1ULL << G[j].q1);
+                }
+                progress = true;
+            }
+        }
+        if (strict) *strict = st;
+        return count;
+    }
+    // register qubits for the next layout: greedily the qubits that let the
+    // most dense gates (then gates) run
+    std::vector<uint32_t> choose_regs() const {
+        std::vector<uint32_t> S;
+        uint64_t mask = 0;
+        int best_dense = -1, best_all = -1;
+        {
+            std::vector<char> d = done;
+            best_all = simulate(0, d, false, &best_dense);
+        }
+        for (int k = 0; k < 4; ++k) {
+            int pick = -1, pd = best_dense, pa = best_all;
+            for (int s = kPos - 1; s >= 0; --s) {  // ties keep qubits 0..4 for the lanes
+                const uint32_t q = slot_q[s];
+                if ((mask >> q) & 1ULL) continue;
+                std::vector<char> d = done;
+                int dn = 0;
+                const int all = simulate(mask | (1ULL << q), d, false, &dn);
+                if (dn > pd || (dn == pd && all > pa)) {
+                    pick = (int)q;
+                    pd = dn;
+                    pa = all;
+                }
+            }
+            if (pick < 0) break;
+            S.push_back((uint32_t)pick);
+            mask |= 1ULL << pick;
+            best_dense = pd;
+            best_all = pa;
+        }
+        return S;
+    }
+    uint64_t reg_mask() const {
+        uint64_t m = 0;
+        for (int i = 5; i < 9; ++i) m |= 1ULL << L[i];
+        return m;
+    }
+    // layout with `want` (up to four qubits) in the register positions, lanes
+    // chosen for conflict-free shared-memory access
+    void relayout(const std::vector<uint32_t> &want) {
+        std::vector<uint32_t> regs(want.begin(), want.begin() + std::min<size_t>(want.size(), 4));
+        for (int s = kPos - 1; s >= 0 && regs.size() < 4; --s)  // prefer high slots: keep 0..4 for the lanes
+            if (std::find(regs.begin(), regs.end(), slot_q[s]) == regs.end()) regs.push_back(slot_q[s]);
+        std::vector<int> free_slots;
+        for (int s = 0; s < kPos; ++s)
+            if (std::find(regs.begin(), regs.end(), slot_q[s]) == regs.end()) free_slots.push_back(s);
+        uint32_t nl[kPos];
+        std::vector<bool> used(kPos, false);
+        auto take = [&](int s) {
+            used[s] = true;
+            return slot_q[s];
+        };
+        bool natural = true;
+        for (int s = 0; s < 5; ++s) natural = natural && std::find(free_slots.begin(), free_slots.end(), s) != free_slots.end();
+        if (natural) {
+            for (int ps = 0; ps < 5; ++ps) nl[ps] = take(ps);
+        } else {
+            // lane positions 0..3 (a half warp): slots whose swizzled images are independent
+            static const int cls[4][4] = {{0, -1, -1, -1}, {1, 4, 7, 10}, {2, 5, 8, 11}, {3, 6, 9, -1}};
+            for (int c = 0; c < 4; ++c) {
+                int pick = -1;
+                for (int k = 0; k < 4 && pick < 0; ++k) {
+                    const int s = cls[c][k];
+                    if (s >= 0 && !used[s] && std::find(free_slots.begin(), free_slots.end(), s) != free_slots.end()) pick = s;
+                }
+                if (pick < 0)
+                    for (int s : free_slots)
+                        if (!used[s]) {
+                            pick = s;
+                            break;
+                        }
+                nl[c] = take(pick);
+            }
+            int pick = -1;
+            for (int s : free_slots)
+                if (!used[s]) {
+                    pick = s;
+                    break;
+                }
+            nl[4] = take(pick);
+        }
+        for (int r = 0; r < 4; ++r) nl[5 + r] = regs[r];
+        int w = 9;
+        for (int s : free_slots)
+            if (!used[s]) {
+                nl[w++] = take(s);
+            }
+        std::memcpy(L, nl, sizeof nl);
+    }
+    // shared-memory index of the thread part (lane and warp bits), as code
+    std::string thread_index() const {
+        std::ostringstream o;
+        o << "(0u";
+        for (int ps = 0; ps < 5; ++ps) o << " | (((lane >> " << ps << ") & 1u) << " << slot_of[L[ps]] << ")";
+        for (int w = 0; w < 3; ++w) o << " | (((warp >> " << w << ") & 1u) << " << slot_of[L[9 + w]] << ")";
+        o << ")";
+        return o.str();
+    }
+    uint32_t reg_index(int i) const {
+        uint32_t j = 0;
+        for (int r = 0; r < 4; ++r)
+            if ((i >> r) & 1) j |= 1u << slot_of[L[5 + r]];
+        return j;
+    }
+    // read all registers from shared memory S in the current layout
+    void emit_read() {
+        const std::string pt = g.fresh("pt");
+        g.s << "const unsigned " << pt << " = qf_phys(" << thread_index() << ");\n";
+        for (int i = 0; i < kR; ++i) g.s << g.R(i) << " = S[" << pt << " ^ " << physj(reg_index(i)) << "u];\n";
+    }
+    void emit_write() {
+        const std::string pt = g.fresh("pt");
+        g.s << "const unsigned " << pt << " = qf_phys(" << thread_index() << ");\n";
+        for (int i = 0; i < kR; ++i) g.s << "S[" << pt << " ^ " << physj(reg_index(i)) << "u] = " << g.R(i) << ";\n";
+    }
+    // global byte-free address bits of canonical shared index j's register+warp part
+    uint64_t chunk_k_bits(int k) const {  // canonical j = 2*tid + 512*k: bits 9..11 = k -> slots 9..11
+        uint64_t a = 0;
+        for (int b = 0; b < 3; ++b)
+            if ((k >> b) & 1) a |= 1ULL << slot_q[9 + b];
+        return a;
+    }
+
+    void emit_kernel(int index, bool last_pass) {
+        auto &s = g.s;
+        for (int i = 0; i < kR; ++i) g.v[i] = i;
+        const std::string dep_t = deposit_code(p.a.nonlocal_mask, "t");
+        const std::string dep_t2 = deposit_code(p.a.nonlocal_mask, "t2");
+        s << "extern \"C\" __global__ void __launch_bounds__(" << kThreads << ", 3) p" << index
+          << "(float2* __restrict__ A, unsigned long long nt) {\n";
+        s << "extern __shared__ __align__(16) float2 SB[];\n";
+        s << "const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, tid = threadIdx.x;\n";
+        s << "const unsigned sbase = (unsigned)__cvta_generic_to_shared(SB);\n";
+        // canonical shared index j = 2*tid + 512*k: bits 0..4 = qubits 0..4,
+        // bits 5..8 = slots 5..8 (from tid >> 4), bits 9..11 = slots 9..11 (k)
+        s << "const unsigned long long toff = (unsigned long long)((2u * tid) & 31u)";
+        for (int b = 0; b < 4; ++b) s << " | ((tid & " << (16u << b) << "u) ? (1ull << " << slot_q[5 + b] << ") : 0ull)";
+        s << ";\n";
+        s << "const unsigned pt2 = qf_phys(2u * tid);\n";
+        auto issue = [&](const std::string &tq, const std::string &buf) {
+            for (int k = 0; k < kChunks; ++k)
+                s << "qf_cpa16(sbase + ((" << buf << ") * " << kTile << "u + (pt2 ^ " << physj(512u * k) << "u)) * 8u, A + (" << tq
+                  << " | toff | " << hex64(chunk_k_bits(k)) << "));\n";
         };
         s << "unsigned long long t = blockIdx.x;\n";
-        s << "if (t < nt) {const unsigned long long tq = " << dep << ";\n";
+        s << "if (t < nt) {const unsigned long long tq = " << dep_t << ";\n";
         issue("tq", "0u");
         s << "}\nasm volatile(\"cp.async.commit_group;\\n\" ::: \"memory\");\n";
         s << "for (unsigned it = 0; t < nt; t += gridDim.x, ++it) {\n";
         s << "const unsigned cur = it & 1u;\n";
-        // prefetch the CTA's next tile (the deposit expression reads `t`; substitute t2)
-        s << "{const unsigned long long t2 = t + gridDim.x; if (t2 < nt) {const unsigned long long tq = ";
-        {
-            std::string d2 = dep;
-            for (size_t pos = 0; (pos = d2.find("(t >>", pos)) != std::string::npos; pos += 6) d2.replace(pos, 5, "(t2 >>");
-            s << d2 << ";\n";
-        }
+        s << "{const unsigned long long t2 = t + gridDim.x; if (t2 < nt) {const unsigned long long tq = " << dep_t2 << ";\n";
         issue("tq", "cur ^ 1u");
         s << "}}\nasm volatile(\"cp.async.commit_group;\\n\" ::: \"memory\");\n";
         s << "asm volatile(\"cp.async.wait_group 1;\\n\" ::: \"memory\");\n__syncthreads();\n";
-        s << "float2* S = SB + cur * " << tile << "u;\n";
-        s << "const unsigned long long tb = " << dep << ";\n";
-        for (int i = 0; i < kR; ++i) s << "float2 r" << i << " = S[lane | " << (i << 5) << "u | (warp << 9)];\n";
+        s << "float2* S = SB + cur * " << kTile << "u;\n";
+        s << "const unsigned long long tb = " << dep_t << ";\n";
+        for (int i = 0; i < kR; ++i) s << "float2 r" << i << ";\n";
+        build_deps();
+        relayout(choose_regs());
+        emit_read();
         s << "__syncthreads();\n";
-    } else {
-        if (has_remap) s << "__shared__ float2 S[" << tile << "];\n";
-        s << "for (unsigned long long t = blockIdx.x; t < nt; t += gridDim.x) {\n";
-        s << "const unsigned long long tb = " << dep << ";\n";
-        s << "const unsigned long long b0 = tb | lane | lw;\n";
-        for (int i = 0; i < kR; ++i) s << "float2 r" << i << " = A[b0 | " << layout_offset(p.a.load_q, i) << "];\n";
+        const auto &G = p.gates;
+        size_t left = G.size();
+        bool remapped = false;
+        while (left) {
+            bool progress = false;
+            for (size_t j = 0; j < G.size() && left; ++j) {
+                if (done[j] || !ready(j, done) || !runnable(G[j], reg_mask(), false)) continue;
+                emit_gate(G[j]);
+                order.push_back((int)j);
+                done[j] = 1;
+                --left;
+                progress = true;
+                j = (size_t)-1;  // rescan: the gate may have released earlier ones
+            }
+            if (progress) remapped = false;
+            if (!left || progress) continue;
+            bool dense_left = false;
+            for (size_t j = 0; j < G.size(); ++j) dense_left = dense_left || (!done[j] && strict_need(G[j]));
+            if (!dense_left || remapped) {  // only diagonal gates hold things up: run one where its qubit is
+                bool ran = false;
+                for (size_t j = 0; j < G.size(); ++j)
+                    if (!done[j] && ready(j, done) && runnable(G[j], reg_mask(), true)) {
+                        emit_gate(G[j]);
+                        order.push_back((int)j);
+                        done[j] = 1;
+                        --left;
+                        ran = true;
+                        break;
+                    }
+                if (!ran) {  // cannot happen for a planned pass: every dense target is resident
+                    failed = true;
+                    return;
+                }
+                remapped = false;
+                continue;
+            }
+            s << "{\n";  // remap: a new layout with the chosen qubits in register positions
+            emit_write();
+            s << "__syncthreads();\n";
+            relayout(choose_regs());
+            emit_read();
+            s << "__syncthreads();\n}\n";
+            remapped = true;
+        }
+        finish(last_pass);
     }
-    const double *mats = rp.mats.data() + 8 * (size_t)p.mat_begin;
-    for (uint32_t o = 0; o < p.a.n_ops; ++o) {
-        const RsOp &op = rp.ops[p.op_begin + o];
-        std::complex<double> m[4];
-        if (op.kind == RS_MREG || op.kind == RS_MLANE || op.kind == RS_DIAG)
-            for (int k = 0; k < 4; ++k) m[k] = cx(mats + 8 * (size_t)op.mat, k);
-        switch (op.kind) {
-        case RS_MREG: {
-            const int mk = matrix_kind_of(m);
-            const int sl = g.slot(m[0], m[1], m[2], m[3]);
-            for (int i = 0; i < kR; ++i)
-                if (!(i & (1 << op.p0))) emit_mat2(g, sl, mk, g.R(i), g.R(i | (1 << op.p0)));
-            break;
-        }
-        case RS_MLANE: {
-            const int mk = matrix_kind_of(m);
-            const int sl = g.slot(m[0], m[1], m[2], m[3]);
-            const int b = op.p0;
-            s << "{const unsigned hb = (lane >> " << b << ") & 1u; const float2 cs = hb ? " << Mref(sl, 3) << " : "
-              << Mref(sl, 0) << ", co = hb ? " << Mref(sl, 2) << " : " << Mref(sl, 1) << ";\n";
-            for (int i = 0; i < kR; ++i) {
-                const std::string Ri = g.R(i);
-                s << "{float2 q; q.x = __shfl_xor_sync(0xffffffffu, " << Ri << ".x, " << (1 << b) << "); q.y = __shfl_xor_sync(0xffffffffu, "
-                  << Ri << ".y, " << (1 << b) << "); const float2 x=" << Ri << ";";
-                if (mk == 1)
-                    s << Ri << ".x=cs.x*x.x+co.x*q.x;" << Ri << ".y=cs.x*x.y+co.x*q.y;}\n";
-                else
-                    s << Ri << ".x=cs.x*x.x-cs.y*x.y+co.x*q.x-co.y*q.y;" << Ri << ".y=cs.x*x.y+cs.y*x.x+co.x*q.y+co.y*q.x;}\n";
-            }
-            s << "}\n";
-            break;
-        }
-        case RS_DIAG: {
-            // diag(m00, m11) = m00 * diag(1, m11/m00)
-            g.any_diag = true;
-            g.gphase *= m[0];
-            const std::complex<double> f = m[3] / m[0];
-            const int sl = g.slot(f, 0.0, 0.0, f);
-            if (Gen::is_reg(op.p0)) {
-                const int rb = op.p0 - 8;
-                for (int i = 0; i < kR; ++i)
-                    if ((i >> rb) & 1) emit_cmul_const(g, g.R(i), sl, 0);
-            } else {
-                s << "if (" << Gen::cbit(op.p0) << ") {\n";
-                for (int i = 0; i < kR; ++i) emit_cmul_const(g, g.R(i), sl, 0);
-                s << "}\n";
-            }
-            break;
-        }
-        case RS_CNOT: {
-            const bool creg = Gen::is_reg(op.p0);
-            if (Gen::is_reg(op.p1)) {
-                const int tb = op.p1 - 8;
-                if (creg) {  // rename only
-                    const int cb = op.p0 - 8;
-                    for (int i = 0; i < kR; ++i)
-                        if (((i >> cb) & 1) && !((i >> tb) & 1)) std::swap(g.v[i], g.v[i | (1 << tb)]);
+
+    void emit_gate(const BGate &x) {
+        auto &s = g.s;
+        {
+            switch (x.kind) {
+            case BK_MAT1: {
+                std::complex<double> m[4] = {{x.m[0], x.m[1]}, {x.m[2], x.m[3]}, {x.m[4], x.m[5]}, {x.m[6], x.m[7]}};
+                if (x.diag) {  // diag(m00, m11) = m00 * diag(1, m11/m00)
+                    g.any_diag = true;
+                    g.gphase *= m[0];
+                    const std::complex<double> f = m[3] / m[0];
+                    const int sl = g.slot(f, 0.0, 0.0, f);
+                    const uint8_t d = desc(x.q0);
+                    if (is_reg(d)) {
+                        const int rb = d - 8;
+                        for (int i = 0; i < kR; ++i)
+                            if ((i >> rb) & 1) emit_cmul_const(g, g.R(i), sl, 0);
+                    } else {
+                        s << "if (" << cbit(d) << ") {\n";
+                        for (int i = 0; i < kR; ++i) emit_cmul_const(g, g.R(i), sl, 0);
+                        s << "}\n";
+                    }
                 } else {
-                    s << "if (" << Gen::cbit(op.p0) << ") {\n";
+                    const int mk = matrix_kind_of(m);
+                    int sl;
+                    if (mk == 1)  // splatted real entries for packed f32x2 arithmetic
+                        sl = g.slot({m[0].real(), m[0].real()}, {m[1].real(), m[1].real()}, {m[2].real(), m[2].real()},
+                                    {m[3].real(), m[3].real()});
+                    else
+                        sl = g.slot(m[0], m[1], m[2], m[3]);
+                    const int rb = pos_of(x.q0) - 5;
                     for (int i = 0; i < kR; ++i)
-                        if (!((i >> tb) & 1)) {
-                            const std::string A = g.R(i), B = g.R(i | (1 << tb));
-                            s << "{const float2 x=" << A << "; " << A << "=" << B << "; " << B << "=x;}\n";
+                        if (!((i >> rb) & 1)) emit_mat2(g, sl, mk, g.R(i), g.R(i | (1 << rb)));
+                }
+                break;
+            }
+            case BK_CNOT: {
+                const uint8_t dc = desc(x.q0);
+                const int tb_ = pos_of(x.q1) - 5;
+                if (is_reg(dc)) {  // rename only
+                    const int cb = dc - 8;
+                    for (int i = 0; i < kR; ++i)
+                        if (((i >> cb) & 1) && !((i >> tb_) & 1)) std::swap(g.v[i], g.v[i | (1 << tb_)]);
+                } else {
+                    s << "if (" << cbit(dc) << ") {\n";
+                    for (int i = 0; i < kR; ++i)
+                        if (!((i >> tb_) & 1)) {
+                            const std::string A_ = g.R(i), B_ = g.R(i | (1 << tb_));
+                            s << "{const float2 x=" << A_ << "; " << A_ << "=" << B_ << "; " << B_ << "=x;}\n";
                         }
                     s << "}\n";
                 }
-            } else {  // lane target
-                const int b = op.p1;
-                if (!creg) s << "{const unsigned cc = " << Gen::cbit(op.p0) << ";\n";
-                for (int i = 0; i < kR; ++i) {
-                    if (creg && !((i >> (op.p0 - 8)) & 1)) continue;
-                    const std::string Ri = g.R(i);
-                    s << "{float2 q; q.x = __shfl_xor_sync(0xffffffffu, " << Ri << ".x, " << (1 << b)
-                      << "); q.y = __shfl_xor_sync(0xffffffffu, " << Ri << ".y, " << (1 << b) << ");";
-                    if (creg) s << Ri << " = q;}\n";
-                    else s << "if (cc) " << Ri << " = q;}\n";
-                }
-                if (!creg) s << "}\n";
+                break;
             }
-            break;
-        }
-        case RS_CZ: {
-            const bool ra = Gen::is_reg(op.p0), rb = Gen::is_reg(op.p1);
-            if (ra && rb) {
-                const int a = op.p0 - 8, b = op.p1 - 8;
-                for (int i = 0; i < kR; ++i)
-                    if (((i >> a) & 1) && ((i >> b) & 1)) s << g.R(i) << ".x = -" << g.R(i) << ".x; " << g.R(i) << ".y = -" << g.R(i) << ".y;\n";
-            } else if (ra || rb) {
-                const int a = (ra ? op.p0 : op.p1) - 8;
-                const uint8_t other = ra ? op.p1 : op.p0;
-                s << "if (" << Gen::cbit(other) << ") {\n";
-                for (int i = 0; i < kR; ++i)
-                    if ((i >> a) & 1) s << g.R(i) << ".x = -" << g.R(i) << ".x; " << g.R(i) << ".y = -" << g.R(i) << ".y;\n";
-                s << "}\n";
-            } else {
-                s << "if (" << Gen::cbit(op.p0) << " & " << Gen::cbit(op.p1) << ") {\n";
-                for (int i = 0; i < kR; ++i) s << g.R(i) << ".x = -" << g.R(i) << ".x; " << g.R(i) << ".y = -" << g.R(i) << ".y;\n";
-                s << "}\n";
-            }
-            break;
-        }
-        case RS_SWAP_LR: {
-            const int a = op.p0, rb = op.p1;
-            s << "{const unsigned la = (lane >> " << a << ") & 1u;\n";
-            for (int i = 0; i < kR; ++i)
-                if (!((i >> rb) & 1)) {
-                    const std::string Ri = g.R(i), Rj = g.R(i | (1 << rb));
-                    s << "{const float2 snd = la ? " << Ri << " : " << Rj << "; float2 q; q.x = __shfl_xor_sync(0xffffffffu, snd.x, "
-                      << (1 << a) << "); q.y = __shfl_xor_sync(0xffffffffu, snd.y, " << (1 << a) << "); if (la) " << Ri
-                      << " = q; else " << Rj << " = q;}\n";
+            case BK_CZ: {
+                const uint8_t da = desc(x.q0), db = desc(x.q1);
+                auto neg = [&](int i) { s << g.R(i) << ".x = -" << g.R(i) << ".x; " << g.R(i) << ".y = -" << g.R(i) << ".y;\n"; };
+                if (is_reg(da) && is_reg(db)) {
+                    for (int i = 0; i < kR; ++i)
+                        if (((i >> (da - 8)) & 1) && ((i >> (db - 8)) & 1)) neg(i);
+                } else if (is_reg(da) || is_reg(db)) {
+                    const int a = (is_reg(da) ? da : db) - 8;
+                    s << "if (" << cbit(is_reg(da) ? db : da) << ") {\n";
+                    for (int i = 0; i < kR; ++i)
+                        if ((i >> a) & 1) neg(i);
+                    s << "}\n";
+                } else {
+                    s << "if (" << cbit(da) << " & " << cbit(db) << ") {\n";
+                    for (int i = 0; i < kR; ++i) neg(i);
+                    s << "}\n";
                 }
-            s << "}\n";
-            break;
-        }
-        case RS_SWAP_LL: {
-            const int a = op.p0, b = op.p1;
-            s << "{const unsigned ba = (lane >> " << a << ") & 1u, bb = (lane >> " << b << ") & 1u; const unsigned src = (lane & ~"
-              << ((1u << a) | (1u << b)) << "u) | (ba << " << b << ") | (bb << " << a << ");\n";
-            for (int i = 0; i < kR; ++i)
-                s << g.R(i) << ".x = __shfl_sync(0xffffffffu, " << g.R(i) << ".x, src); " << g.R(i)
-                  << ".y = __shfl_sync(0xffffffffu, " << g.R(i) << ".y, src);\n";
-            s << "}\n";
-            break;
-        }
-        default: {  // RS_REMAP
-            auto slots = [&](uint32_t packed, int pos) { return (packed >> (3 * pos)) & 7u; };
-            auto idx = [&](uint32_t packed, int i) {
-                std::ostringstream o;
-                uint32_t regbits = 0;
-                for (int b = 0; b < 4; ++b)
-                    if ((i >> b) & 1) regbits |= 1u << slots(packed, b);
-                o << "lane + 32u * (" << regbits << "u";
-                for (int w = 0; w < wb; ++w) o << " | ((warp & " << (1 << w) << "u) ? " << (1u << slots(packed, 4 + w)) << "u : 0u)";
-                o << ")";
-                return o.str();
-            };
-            for (int i = 0; i < kR; ++i) s << "S[" << idx(op.a, i) << "] = " << g.R(i) << ";\n";
-            s << "__syncthreads();\n";
-            for (int i = 0; i < kR; ++i) s << g.R(i) << " = S[" << idx(op.b, i) << "];\n";
-            s << "__syncthreads();\n";
-            break;
-        }
+                break;
+            }
+            default: {  // SWAP of two resident qubits: relabel
+                const int a = pos_of(x.q0), b = pos_of(x.q1);
+                std::swap(L[a], L[b]);
+                break;
+            }
+            }
         }
     }
-    (void)index;
-}
+
+    void finish(bool last_pass) {
+        auto &s = g.s;
+        if (last_pass && g.any_diag) {  // the plan's global phase, once, at the very end
+            const int sl = g.slot(g.gphase, 0.0, 0.0, 0.0);
+            for (int i = 0; i < kR; ++i) emit_cmul_const(g, g.R(i), sl, 0);
+        }
+        bool natural = true;
+        for (int ps = 0; ps < 5; ++ps) natural = natural && L[ps] == (uint32_t)ps;
+        if (natural) {  // lanes hold qubits 0..4: store straight from registers
+            s << "const unsigned long long sw = 0ull";
+            for (int w = 0; w < 3; ++w) s << " | ((warp & " << (1 << w) << "u) ? (1ull << " << L[9 + w] << ") : 0ull)";
+            s << ";\n";
+            for (int i = 0; i < kR; ++i) {
+                uint64_t off = 0;
+                for (int r = 0; r < 4; ++r)
+                    if ((i >> r) & 1) off |= 1ULL << L[5 + r];
+                s << "A[(tb | lane | sw) | " << hex64(off) << "] = " << g.R(i) << ";\n";
+            }
+        } else {  // through shared memory, 16-byte coalesced stores
+            emit_write();
+            s << "__syncthreads();\n";
+            for (int k = 0; k < kChunks; ++k)
+                s << "*reinterpret_cast<float4*>(A + (tb | toff | " << hex64(chunk_k_bits(k))
+                  << ")) = *reinterpret_cast<const float4*>(S + (pt2 ^ " << physj(512u * k) << "u));\n";
+            s << "__syncthreads();\n";
+        }
+        s << "}\n}\n";
+    }
+};
 
 struct JitModule {
     cudaLibrary_t lib = nullptr;
@@ -406,7 +628,24 @@ JitCache &cache() {
     return c;
 }
 
-int compile_module(const std::string &src, int n_kernels, size_t dyn_smem, int device, JitModule &out, std::string &err) {
+constexpr size_t kDynSmem = 2u * kTile * sizeof(float) * 2;  // two tile buffers of float2
+
+const char *kPrelude =
+    "__device__ __forceinline__ void qf_cpa16(unsigned s, const float2* g) {"
+    " asm volatile(\"cp.async.cg.shared.global [%0], [%1], 16;\\n\" :: \"r\"(s), \"l\"(g) : \"memory\"); }\n"
+    "__device__ __forceinline__ unsigned qf_phys(unsigned j) { return j ^ ((((j >> 4) ^ (j >> 7) ^ (j >> 10)) & 7u) << 1); }\n"
+    "__device__ __forceinline__ unsigned long long qf_pk(float2 v) { unsigned long long r;"
+    " asm(\"mov.b64 %0, {%1, %2};\" : \"=l\"(r) : \"f\"(v.x), \"f\"(v.y)); return r; }\n"
+    "__device__ __forceinline__ float2 qf_upk(unsigned long long r) { float2 v;"
+    " asm(\"mov.b64 {%0, %1}, %2;\" : \"=f\"(v.x), \"=f\"(v.y) : \"l\"(r)); return v; }\n"
+    "__device__ __forceinline__ float2 qf_ffma2(float2 a, float2 b, float2 c) { unsigned long long d;"
+    " asm(\"fma.rn.f32x2 %0, %1, %2, %3;\" : \"=l\"(d) : \"l\"(qf_pk(a)), \"l\"(qf_pk(b)), \"l\"(qf_pk(c))); return qf_upk(d); }\n"
+    "__device__ __forceinline__ float2 qf_fmul2(float2 a, float2 b) { unsigned long long d;"
+    " asm(\"mul.rn.f32x2 %0, %1, %2;\" : \"=l\"(d) : \"l\"(qf_pk(a)), \"l\"(qf_pk(b))); return qf_upk(d); }\n";
+
+const char *kNvrtcOpts[] = {"--gpu-architecture=sm_103a", "--std=c++17", "-default-device", "-lineinfo"};
+
+int compile_module(const std::string &src, int n_kernels, int device, JitModule &out, std::string &err) {
     Nvrtc &nv = nvrtc();
     if (!nv.ok) {
         err = nv.why;
@@ -417,8 +656,7 @@ int compile_module(const std::string &src, int n_kernels, size_t dyn_smem, int d
         err = "nvrtcCreateProgram failed";
         return QF_ERR_CUDA;
     }
-    const char *opts[] = {"--gpu-architecture=sm_103a", "--std=c++17", "-default-device", "-lineinfo"};
-    nvrtcResult r = nv.compile(prog, 4, opts);
+    nvrtcResult r = nv.compile(prog, 4, kNvrtcOpts);
     if (r != NVRTC_SUCCESS) {
         size_t ls = 0;
         nv.log_size(prog, &ls);
@@ -445,18 +683,16 @@ int compile_module(const std::string &src, int n_kernels, size_t dyn_smem, int d
             err = std::string("cudaLibraryGetKernel: ") + cudaGetErrorString(e);
             return QF_ERR_CUDA;
         }
+        if ((e = cudaKernelSetAttributeForDevice(out.kernels[k], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)kDynSmem, device)) != cudaSuccess) {
+            err = std::string("cudaKernelSetAttributeForDevice: ") + cudaGetErrorString(e);
+            return QF_ERR_CUDA;
+        }
     }
     if ((e = cudaLibraryGetGlobal(&out.consts, &out.consts_bytes, out.lib, "M")) != cudaSuccess) {
         err = std::string("cudaLibraryGetGlobal: ") + cudaGetErrorString(e);
         return QF_ERR_CUDA;
     }
-    if (dyn_smem > 48 * 1024)
-        for (int k = 0; k < n_kernels; ++k)
-            if ((e = cudaKernelSetAttributeForDevice(out.kernels[k], cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                     (int)dyn_smem, device)) != cudaSuccess) {
-                err = std::string("cudaKernelSetAttributeForDevice: ") + cudaGetErrorString(e);
-                return QF_ERR_CUDA;
-            }
     return QF_OK;
 }
 
@@ -464,24 +700,15 @@ struct ModulePlan {
     std::string src;
     std::vector<float> consts;  // interleaved float2
     std::vector<int> pass_index;
-    size_t dyn_smem = 0;        // dynamic shared memory per CTA (prefetch buffers)
 };
 
-}  // namespace
-
-bool jit_available() { return nvrtc().ok; }
+// a pass the compiled kernels can run: 12 resident qubits including 0..4
+bool pass_fits(const Pass &p) { return __builtin_popcountll(p.resident) == kPos && (p.resident & 31ULL) == 31ULL; }
 
 // group passes into modules: at most 8 passes and 56 KB of constants each
-static bool jit_prefetch_enabled() {
-    const char *e = std::getenv("QF_JIT_PREFETCH");
-    return !(e && e[0] == '0');
-}
-
-static void gen_modules(const RsPlan &rp, int wb, std::vector<ModulePlan> &mods) {
+bool gen_modules(const Plan &plan, std::vector<ModulePlan> &mods) {
     Gen g;
-    g.wb = wb;
-    g.prefetch = jit_prefetch_enabled();
-    const size_t npass = rp.passes.size();
+    const size_t npass = plan.passes.size();
     size_t pi = 0;
     while (pi < npass) {
         ModulePlan mp;
@@ -491,26 +718,17 @@ static void gen_modules(const RsPlan &rp, int wb, std::vector<ModulePlan> &mods)
         while (pi < npass && local < 8 && g.consts.size() * 8 < 56 * 1024) {
             g.s.str("");
             g.s.clear();
-            gen_pass(g, rp, rp.passes[pi], local);
-            if (pi + 1 == npass && g.any_diag) {  // the plan's global phase, once, at the very end
-                const int sl = g.slot(g.gphase, 0.0, 0.0, 0.0);
-                for (int i = 0; i < kR; ++i) emit_cmul_const(g, g.R(i), sl, 0);
-            }
-            // stores with the final register names
-            for (int i = 0; i < kR; ++i)
-                g.s << "A[(tb | lane | sw) | " << layout_offset(rp.passes[pi].a.store_q, i) << "] = " << g.R(i) << ";\n";
-            g.s << "}\n}\n";
+            PassGen pg(g, plan.passes[pi], plan.n);
+            pg.emit_kernel(local, pi + 1 == npass);
+            if (pg.failed) return false;
             body << g.s.str();
             mp.pass_index.push_back((int)pi);
             ++pi;
             ++local;
         }
         std::ostringstream head;
-        head << "__constant__ float2 M[" << std::max<size_t>(1, g.consts.size()) << "];\n";
-        head << "__device__ __forceinline__ void qf_cpa16(unsigned s, const float2* g) {"
-                " asm volatile(\"cp.async.cg.shared.global [%0], [%1], 16;\\n\" :: \"r\"(s), \"l\"(g) : \"memory\"); }\n";
+        head << "__constant__ float2 M[" << std::max<size_t>(1, g.consts.size()) << "];\n" << kPrelude;
         mp.src = head.str() + body.str();
-        mp.dyn_smem = g.prefetch ? 2u * kR * (32u << wb) * sizeof(float) * 2 : 0;
         mp.consts.reserve(g.consts.size() * 2);
         for (auto &c : g.consts) {
             mp.consts.push_back((float)c.real());
@@ -518,24 +736,32 @@ static void gen_modules(const RsPlan &rp, int wb, std::vector<ModulePlan> &mods)
         }
         mods.push_back(std::move(mp));
     }
+    return true;
+}
+
+}  // namespace
+
+bool jit_available() { return nvrtc().ok; }
+
+bool jit_plan_fits(const Plan &plan) {
+    if (plan.n < (uint32_t)kPos) return false;
+    for (const Pass &p : plan.passes)
+        if (!pass_fits(p)) return false;
+    return true;
 }
 
 // Generated sources and an NVRTC compile without loading (needs no GPU).
-int jit_check_compile(const Plan &plan, int wb, std::string *source, std::string *err) {
-    RsPlan rp;
-    QF_TRY(lower_rs(plan, wb, rp));
-    for (const RsPass &p : rp.passes)
-        if (p.fallback) return fail(QF_ERR_UNSUPPORTED_OPERATION, "plan has a pass outside the register layout");
+int jit_check_compile(const Plan &plan, int, std::string *source, std::string *err) {
+    if (!jit_plan_fits(plan)) return fail(QF_ERR_UNSUPPORTED_OPERATION, "plan has a pass outside the compiled layout");
     std::vector<ModulePlan> mods;
-    gen_modules(rp, wb, mods);
+    if (!gen_modules(plan, mods)) return fail(QF_ERR_UNSUPPORTED_OPERATION, "pass compiler could not schedule a pass");
     Nvrtc &nv = nvrtc();
     if (!nv.ok) return fail(QF_ERR_UNSUPPORTED_OPERATION, "%s", nv.why.c_str());
     for (auto &m : mods) {
         if (source) *source += m.src;
         nvrtcProgram prog;
         nv.create(&prog, m.src.c_str(), "qf_pass.cu", 0, nullptr, nullptr);
-        const char *opts[] = {"--gpu-architecture=sm_103a", "--std=c++17", "-default-device"};
-        nvrtcResult r = nv.compile(prog, 3, opts);
+        nvrtcResult r = nv.compile(prog, 3, kNvrtcOpts);
         if (r != NVRTC_SUCCESS) {
             size_t ls = 0;
             nv.log_size(prog, &ls);
@@ -551,15 +777,11 @@ int jit_check_compile(const Plan &plan, int wb, std::string *source, std::string
 }
 
 // Generate, compile (or fetch) and launch the plan's passes.
-int run_plan_jit(qf_sv *sv, const Plan &plan, int wb) {
-    RsPlan rp;
-    QF_TRY(lower_rs(plan, wb, rp));
-    for (const RsPass &p : rp.passes)
-        if (p.fallback) return run_plan_smem(sv, plan);
+int run_plan_jit(qf_sv *sv, const Plan &plan, int) {
+    if (!jit_plan_fits(plan)) return run_plan_rs(sv, plan, 3);  // interpreted (falls back to shared memory)
     qf_ctx *ctx = sv->ctx;
     std::vector<ModulePlan> mods;
-    gen_modules(rp, wb, mods);
-    // compile what is not cached (in parallel)
+    if (!gen_modules(plan, mods)) return run_plan_rs(sv, plan, 3);
     std::vector<std::shared_ptr<JitModule>> handles(mods.size());
     std::vector<size_t> todo;
     {
@@ -570,18 +792,17 @@ int run_plan_jit(qf_sv *sv, const Plan &plan, int wb) {
             else todo.push_back(m);
         }
     }
-    if (!todo.empty()) {
+    if (!todo.empty()) {  // compile the missing modules in parallel
         std::vector<int> st(todo.size(), QF_OK);
         std::vector<std::string> errs(todo.size());
         std::vector<std::shared_ptr<JitModule>> built(todo.size());
         std::vector<std::thread> th;
-        int dev = ctx->device;
+        const int dev = ctx->device;
         for (size_t k = 0; k < todo.size(); ++k) {
             built[k] = std::make_shared<JitModule>();
             th.emplace_back([&, k, dev] {
                 cudaSetDevice(dev);
-                st[k] = compile_module(mods[todo[k]].src, (int)mods[todo[k]].pass_index.size(), mods[todo[k]].dyn_smem, dev,
-                                       *built[k], errs[k]);
+                st[k] = compile_module(mods[todo[k]].src, (int)mods[todo[k]].pass_index.size(), dev, *built[k], errs[k]);
             });
         }
         for (auto &t : th) t.join();
@@ -593,24 +814,22 @@ int run_plan_jit(qf_sv *sv, const Plan &plan, int wb) {
             handles[todo[k]] = built[k];
         }
     }
-    // launch
-    const int threads = 32 << wb;
     for (size_t m = 0; m < mods.size(); ++m) {
         JitModule &jm = *handles[m];
         const size_t bytes = mods[m].consts.size() * sizeof(float);
         if (bytes > jm.consts_bytes) return fail(QF_ERR_CUDA, "pass compiler: constant bank size mismatch");
         if (bytes) QF_CUDA(cudaMemcpyAsync(jm.consts, mods[m].consts.data(), bytes, cudaMemcpyHostToDevice, ctx->stream));
         for (size_t k = 0; k < mods[m].pass_index.size(); ++k) {
-            const RsPass &p = rp.passes[mods[m].pass_index[k]];
+            const Pass &p = plan.passes[mods[m].pass_index[k]];
             int per_sm = 0;
-            const size_t dyn = mods[m].dyn_smem;
-            QF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)jm.kernels[k], threads, dyn));
+            QF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)jm.kernels[k], kThreads, kDynSmem));
             per_sm = std::max(per_sm, 1);
             const uint64_t grid = std::min<uint64_t>((uint64_t)per_sm * ctx->sm_count, p.a.n_tiles);
             float2 *amps = static_cast<float2 *>(sv->d);
             unsigned long long nt = p.a.n_tiles;
             void *args[] = {&amps, &nt};
-            QF_CUDA(cudaLaunchKernel((const void *)jm.kernels[k], dim3((unsigned)grid), dim3(threads), args, dyn, ctx->stream));
+            QF_CUDA(cudaLaunchKernel((const void *)jm.kernels[k], dim3((unsigned)grid), dim3(kThreads), args, kDynSmem,
+                                     ctx->stream));
         }
     }
     return QF_OK;
