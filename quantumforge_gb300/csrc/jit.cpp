@@ -346,15 +346,25 @@ struct PassGen {
         };
         bool natural = true;
         for (int s = 0; s < 5; ++s) natural = natural && std::find(free_slots.begin(), free_slots.end(), s) != free_slots.end();
+        // qubit 0 in a register goes to register bit 0: register pairs are
+        // then adjacent in shared memory and move as 16-byte accesses
+        const auto q0 = std::find(regs.begin(), regs.end(), slot_q[0]);
+        if (q0 != regs.end()) std::iter_swap(regs.begin(), q0);
         if (natural) {
             for (int ps = 0; ps < 5; ++ps) nl[ps] = take(ps);
         } else {
-            // lane positions 0..3 (a half warp): slots whose swizzled images are independent
+            // Lane positions of one access phase take slots whose swizzled
+            // images are independent in the bank bits: slot 0 gives bit 0,
+            // the classes {1,4,7,10}, {2,5,8,11}, {3,6,9} bits 1, 2, 3. An
+            // 8-byte access has half-warp phases (lane bits 0..3), a 16-byte
+            // one quarter-warp phases (lane bits 0..2, bank bits 1..3).
             static const int cls[4][4] = {{0, -1, -1, -1}, {1, 4, 7, 10}, {2, 5, 8, 11}, {3, 6, 9, -1}};
+            const int c0 = q0 != regs.end() ? 1 : 0;
             for (int c = 0; c < 4; ++c) {
+                const int cc = c + c0 < 4 ? c + c0 : -1;
                 int pick = -1;
-                for (int k = 0; k < 4 && pick < 0; ++k) {
-                    const int s = cls[c][k];
+                for (int k = 0; k < 4 && pick < 0 && cc >= 0; ++k) {
+                    const int s = cls[cc][k];
                     if (s >= 0 && !used[s] && std::find(free_slots.begin(), free_slots.end(), s) != free_slots.end()) pick = s;
                 }
                 if (pick < 0)
@@ -396,15 +406,28 @@ struct PassGen {
             if ((i >> r) & 1) j |= 1u << slot_of[L[5 + r]];
         return j;
     }
+    bool pairs() const { return L[5] == slot_q[0]; }
     // read all registers from shared memory S in the current layout
     void emit_read() {
         const std::string pt = g.fresh("pt");
         g.s << "const unsigned " << pt << " = qf_phys(" << thread_index() << ");\n";
+        if (pairs()) {
+            for (int i = 0; i < kR; i += 2)
+                g.s << "{const float4 t = *reinterpret_cast<const float4*>(S + (" << pt << " ^ " << physj(reg_index(i)) << "u)); "
+                    << g.R(i) << " = make_float2(t.x, t.y); " << g.R(i + 1) << " = make_float2(t.z, t.w);}\n";
+            return;
+        }
         for (int i = 0; i < kR; ++i) g.s << g.R(i) << " = S[" << pt << " ^ " << physj(reg_index(i)) << "u];\n";
     }
     void emit_write() {
         const std::string pt = g.fresh("pt");
         g.s << "const unsigned " << pt << " = qf_phys(" << thread_index() << ");\n";
+        if (pairs()) {
+            for (int i = 0; i < kR; i += 2)
+                g.s << "*reinterpret_cast<float4*>(S + (" << pt << " ^ " << physj(reg_index(i)) << "u)) = make_float4(" << g.R(i)
+                    << ".x, " << g.R(i) << ".y, " << g.R(i + 1) << ".x, " << g.R(i + 1) << ".y);\n";
+            return;
+        }
         for (int i = 0; i < kR; ++i) g.s << "S[" << pt << " ^ " << physj(reg_index(i)) << "u] = " << g.R(i) << ";\n";
     }
     // global byte-free address bits of canonical shared index j's register+warp part
