@@ -97,8 +97,21 @@ constexpr int kTile = 4096;   // amplitudes per tile
 constexpr int kThreads = 256;
 constexpr int kChunks = kTile / 2 / kThreads;  // 16-byte chunks per thread
 
-uint32_t swz(uint32_t j) { return ((j >> 4) ^ (j >> 7) ^ (j >> 10)) & 7u; }
+// Shared-memory swizzle: tile index bits 4..11 are folded into bits 1..3
+// (the bank bits of a 16-byte chunk) with the columns 1,2,4,3,6,5,7,1, so
+// that the slots 1..11 reach every nonzero combination of bank bits and any
+// four register slots leave a bank basis for the lanes. Bit 0 is never
+// swizzled: 16-byte chunks stay whole.
+constexpr uint32_t kSwzMask[3] = {0xE9u, 0x5Au, 0x74u};
+uint32_t swz(uint32_t j) {
+    const uint32_t h = (j >> 4) & 0xFFu;
+    uint32_t r = 0;
+    for (int b = 0; b < 3; ++b) r |= (uint32_t)(__builtin_popcount(h & kSwzMask[b]) & 1) << b;
+    return r;
+}
 uint32_t physj(uint32_t j) { return j ^ (swz(j) << 1); }
+// bank vector (bits 0..3 of the swizzled index) contributed by slot s
+uint32_t bank_vec(int s) { return physj(1u << s) & 15u; }
 
 struct Gen {
     std::ostringstream s;
@@ -353,26 +366,31 @@ struct PassGen {
         if (natural) {
             for (int ps = 0; ps < 5; ++ps) nl[ps] = take(ps);
         } else {
-            // Lane positions of one access phase take slots whose swizzled
-            // images are independent in the bank bits: slot 0 gives bit 0,
-            // the classes {1,4,7,10}, {2,5,8,11}, {3,6,9} bits 1, 2, 3. An
-            // 8-byte access has half-warp phases (lane bits 0..3), a 16-byte
-            // one quarter-warp phases (lane bits 0..2, bank bits 1..3).
-            static const int cls[4][4] = {{0, -1, -1, -1}, {1, 4, 7, 10}, {2, 5, 8, 11}, {3, 6, 9, -1}};
-            const int c0 = q0 != regs.end() ? 1 : 0;
+            // The lanes of one access phase take slots whose bank vectors are
+            // independent: an 8-byte access has half-warp phases (lane bits
+            // 0..3 must reach all four bank bits, so slot 0 goes first), a
+            // 16-byte one quarter-warp phases (lane bits 0..2, bank bits 1..3).
+            const int phase_lanes = q0 != regs.end() ? 3 : 4;
+            std::vector<uint32_t> basis;
+            auto reduce = [&](uint32_t v) {
+                for (uint32_t b : basis) v = std::min(v, v ^ b);
+                return v;
+            };
             for (int c = 0; c < 4; ++c) {
-                const int cc = c + c0 < 4 ? c + c0 : -1;
                 int pick = -1;
-                for (int k = 0; k < 4 && pick < 0 && cc >= 0; ++k) {
-                    const int s = cls[cc][k];
-                    if (s >= 0 && !used[s] && std::find(free_slots.begin(), free_slots.end(), s) != free_slots.end()) pick = s;
-                }
+                if (c < phase_lanes)
+                    for (int s : free_slots)
+                        if (!used[s] && reduce(bank_vec(s))) {
+                            pick = s;
+                            break;
+                        }
                 if (pick < 0)
                     for (int s : free_slots)
                         if (!used[s]) {
                             pick = s;
                             break;
                         }
+                if (const uint32_t r = reduce(bank_vec(pick))) basis.push_back(r);
                 nl[c] = take(pick);
             }
             int pick = -1;
@@ -406,15 +424,22 @@ struct PassGen {
             if ((i >> r) & 1) j |= 1u << slot_of[L[5 + r]];
         return j;
     }
-    bool pairs() const { return L[5] == slot_q[0]; }
+    // register bit holding qubit 0 (the registers i and i | 1 << bit are then
+    // adjacent in shared memory), or -1
+    int pair_bit() const {
+        for (int r = 0; r < 4; ++r)
+            if (L[5 + r] == slot_q[0]) return r;
+        return -1;
+    }
     // read all registers from shared memory S in the current layout
     void emit_read() {
         const std::string pt = g.fresh("pt");
         g.s << "const unsigned " << pt << " = qf_phys(" << thread_index() << ");\n";
-        if (pairs()) {
-            for (int i = 0; i < kR; i += 2)
-                g.s << "{const float4 t = *reinterpret_cast<const float4*>(S + (" << pt << " ^ " << physj(reg_index(i)) << "u)); "
-                    << g.R(i) << " = make_float2(t.x, t.y); " << g.R(i + 1) << " = make_float2(t.z, t.w);}\n";
+        if (const int pb = pair_bit(); pb >= 0) {
+            for (int i = 0; i < kR; ++i)
+                if (!((i >> pb) & 1))
+                    g.s << "{const float4 t = *reinterpret_cast<const float4*>(S + (" << pt << " ^ " << physj(reg_index(i))
+                        << "u)); " << g.R(i) << " = make_float2(t.x, t.y); " << g.R(i | (1 << pb)) << " = make_float2(t.z, t.w);}\n";
             return;
         }
         for (int i = 0; i < kR; ++i) g.s << g.R(i) << " = S[" << pt << " ^ " << physj(reg_index(i)) << "u];\n";
@@ -422,10 +447,13 @@ struct PassGen {
     void emit_write() {
         const std::string pt = g.fresh("pt");
         g.s << "const unsigned " << pt << " = qf_phys(" << thread_index() << ");\n";
-        if (pairs()) {
-            for (int i = 0; i < kR; i += 2)
-                g.s << "*reinterpret_cast<float4*>(S + (" << pt << " ^ " << physj(reg_index(i)) << "u)) = make_float4(" << g.R(i)
-                    << ".x, " << g.R(i) << ".y, " << g.R(i + 1) << ".x, " << g.R(i + 1) << ".y);\n";
+        if (const int pb = pair_bit(); pb >= 0) {
+            for (int i = 0; i < kR; ++i)
+                if (!((i >> pb) & 1)) {
+                    const std::string A_ = g.R(i), B_ = g.R(i | (1 << pb));
+                    g.s << "*reinterpret_cast<float4*>(S + (" << pt << " ^ " << physj(reg_index(i)) << "u)) = make_float4(" << A_
+                        << ".x, " << A_ << ".y, " << B_ << ".x, " << B_ << ".y);\n";
+                }
             return;
         }
         for (int i = 0; i < kR; ++i) g.s << "S[" << pt << " ^ " << physj(reg_index(i)) << "u] = " << g.R(i) << ";\n";
@@ -656,7 +684,8 @@ constexpr size_t kDynSmem = 2u * kTile * sizeof(float) * 2;  // two tile buffers
 const char *kPrelude =
     "__device__ __forceinline__ void qf_cpa16(unsigned s, const float2* g) {"
     " asm volatile(\"cp.async.cg.shared.global [%0], [%1], 16;\\n\" :: \"r\"(s), \"l\"(g) : \"memory\"); }\n"
-    "__device__ __forceinline__ unsigned qf_phys(unsigned j) { return j ^ ((((j >> 4) ^ (j >> 7) ^ (j >> 10)) & 7u) << 1); }\n"
+    "__device__ __forceinline__ unsigned qf_phys(unsigned j) { const unsigned h = (j >> 4) & 0xFFu;"
+    " return j ^ ((__popc(h & 0xE9u) & 1u) << 1) ^ ((__popc(h & 0x5Au) & 1u) << 2) ^ ((__popc(h & 0x74u) & 1u) << 3); }\n"
     "__device__ __forceinline__ unsigned long long qf_pk(float2 v) { unsigned long long r;"
     " asm(\"mov.b64 %0, {%1, %2};\" : \"=l\"(r) : \"f\"(v.x), \"f\"(v.y)); return r; }\n"
     "__device__ __forceinline__ float2 qf_upk(unsigned long long r) { float2 v;"
