@@ -5,8 +5,8 @@ Workload (one step): a seeded depth-40 random circuit on 30 qubits — each
 layer H/RX/RY/RZ on every qubit, then 15 disjoint CNOT/CZ/SWAP pairs, half
 nearest-neighbour, half long-range — applied to a resident complex64 state
 (8 GiB, larger than L2, so no flush is needed between steps). The metric is
-whole-job gates/s; the roofline is HBM bandwidth of the tile-pass kernel
-(2 * 2^30 * 8 bytes per pass). Also reported: end-to-end gates/s through the
+whole-job gates/s; the roofline is HBM bandwidth of the tile-pass kernels
+(2 * 2^30 * 8 bytes per pass, one kernel launch per pass). Also reported: end-to-end gates/s through the
 C ABI with host buffers (qf_run_circuit: upload f64 amplitudes, run, download),
 the CPU baseline (the oracle restating the reference's rayon path, on every
 host core, on a bounded sample of the same circuit), and 24-qubit VQE
@@ -49,6 +49,8 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true")
+    ap.add_argument("--extras", default="vqe24,qaoa4096,shots20,vqe32",
+                    help="comma-separated extra workloads to run after the headline")
     return ap.parse_args()
 
 
@@ -270,18 +272,25 @@ def run_ours(args):
         t = float(tt.item())
     value = world * args.steps * n_gates / t
     ms_per_step = 1000.0 * t / args.steps
-    # roofline of the dominant kernel (k_tile_pass): every launch is one full
-    # read + write sweep of the state
+    # roofline of the dominant kernels (one launch per tile pass): every launch
+    # is one full read + write sweep of the state
     bytes_per_launch = 2 * (1 << n) * amp_bytes
     launches = args.steps * n_passes
     avg_launch_s = t / launches
     achieved = bytes_per_launch / avg_launch_s / 1e9
     peak, peak_kind = hbm_peak()
+    if dcode == A.C64 and n >= 24:
+        kernel = f"compiled tile passes p0..p{n_passes - 1} (one NVRTC sm_103a kernel per pass)"
+    elif dcode == A.C64 and n >= 12:
+        kernel = "k_rs_pass (register-tiled pass interpreter)"
+    else:
+        kernel = "k_tile_pass<double2,false>" if dcode == A.C128 else "k_tile_pass<float2,false>"
+    # DRAM bytes per launch from one ncu capture of this workload (see profiles/)
     traffic = None
     tf = ROOT / "profiles" / "tile_pass_traffic.json"
     if tf.exists():
         try:
-            traffic = json.loads(tf.read_text()).get(f"{n}q_{args.dtype}_bytes_per_launch")
+            traffic = json.loads(tf.read_text()).get(f"{n}q_d{args.depth}_s{args.seed}_{args.dtype}_bytes_per_launch")
         except Exception:
             traffic = None
 
@@ -315,9 +324,15 @@ def run_ours(args):
     extra = {}
     cpu = None
     if rank == 0 and not args.no_extra:
-        extra["vqe24"] = vqe_gradients(backend)
-        extra["qaoa4096"] = qaoa_batch(backend, cpu=not args.no_cpu_baseline)
-        extra["shots20"] = shots20(backend, cpu=not args.no_cpu_baseline)
+        wanted = set(args.extras.split(","))
+        if "vqe24" in wanted:
+            extra["vqe24"] = vqe_gradients(backend)
+        if "qaoa4096" in wanted:
+            extra["qaoa4096"] = qaoa_batch(backend, cpu=not args.no_cpu_baseline)
+        if "shots20" in wanted:
+            extra["shots20"] = shots20(backend, cpu=not args.no_cpu_baseline)
+        if "vqe32" in wanted:
+            extra["vqe32"] = vqe32_checkpointed(backend)
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, sample = time_cpu_oracle(n, ops, args.cpu_seconds, threads)
@@ -333,7 +348,7 @@ def run_ours(args):
                        "tile_qubits": args.tile or "auto", "l2": "state larger than L2 (no flush needed)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": traffic, "peak_kind": f"of {peak_kind}", "kernel": "k_tile_pass<float2,false>",
+                         "traffic": traffic, "peak_kind": f"of {peak_kind}", "kernel": kernel,
                          "bytes_per_launch": bytes_per_launch, "avg_launch_ms": 1000 * avg_launch_s},
             "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches,
             "extra": extra,
@@ -472,6 +487,43 @@ def vqe_gradients(backend):
             "param_shift_grads_per_s": 1.0 / t_sh, "ratio": t_sh / t_adj,
             "max_abs_grad_diff_adjoint_vs_shift": float(np.abs(adj.gradient - sh.gradient).max()),
             "energy_adjoint": adj.expectation, "energy_shift_run": sh.expectation, "dtype": "complex64"}
+
+
+def vqe32_checkpointed(backend):
+    """32-qubit XXZ-ring VQE (RX.RY per qubit + CNOT ring, 4 layers, 256
+    params, H = sum XX + YY + 0.5 ZZ, 96 terms): complex64 adjoint gradient
+    with a checkpoint per layer (psi, lambda + 3 checkpoints = 160 GiB) and
+    with pure uncompute (64 GiB), both against a complex128 uncompute run
+    (128 GiB) of the same circuit."""
+    import numpy as np
+
+    import quantumforge_gb300 as qf
+    from quantumforge_gb300 import workloads as W
+    from quantumforge_gb300.gradients import GradientOptions, GradientStrategy, gradient_with_inputs
+
+    n, layers = 32, 4
+    ops, params, H = W.vqe_xxz(n, layers, seed=5)
+    pc = qf.ParameterizedCircuit(params.size)
+    for r in ops:
+        pc.operations.append((int(r["kind"]), int(r["gate"]), int(r["q0"]), int(r["q1"]), int(r["param"]),
+                              float(r["theta"])))
+    opts = GradientOptions(strategy=GradientStrategy.Adjoint)
+    runs = {}
+    for name, every in (("checkpoint_per_layer", 3 * n), ("uncompute", 0)):
+        gradient_with_inputs(pc, opts, [], params, n, H, dtype="c64", checkpoint_every=every, backend=backend)
+        t0 = time.perf_counter()
+        est = gradient_with_inputs(pc, opts, [], params, n, H, dtype="c64", checkpoint_every=every, backend=backend)
+        runs[name] = (time.perf_counter() - t0, est)
+    t0 = time.perf_counter()
+    ref = gradient_with_inputs(pc, opts, [], params, n, H, dtype="c128", checkpoint_every=0, backend=backend)
+    t_ref = time.perf_counter() - t0
+    out = {"qubits": n, "params": int(params.size), "ops": len(ops), "terms": len(H.terms),
+           "energy_c128": ref.expectation, "c128_uncompute_s_per_gradient": t_ref}
+    for name, (t, est) in runs.items():
+        out[name] = {"s_per_gradient": t, "gradients_per_s": 1.0 / t,
+                     "max_abs_grad_err_vs_c128": float(np.abs(np.asarray(est.gradient) - np.asarray(ref.gradient)).max()),
+                     "energy_err_vs_c128": abs(est.expectation - ref.expectation), "dtype": "complex64"}
+    return out
 
 
 def main():

@@ -230,7 +230,7 @@ int adjoint_device(qf_ctx *ctx, uint32_t n, const std::vector<BGate> &gates, con
         Plan plan;
         po.backward = false;
         QF_TRY(plan_passes(n, seg, po, plan));
-        QF_TRY(run_plan(psi, plan));
+        QF_TRY(run_plan(psi, plan, o->exec.flags));
         if (s + 1 < n_seg) {
             qf_sv *c;
             QF_TRY(alloc_state(ctx, n, dtype, 0, &c));
@@ -255,13 +255,13 @@ int adjoint_device(qf_ctx *ctx, uint32_t n, const std::vector<BGate> &gates, con
             if (bytes > kSmallBytes) QF_TRY(ensure_device(&ctx->ws_tree, &ctx->ws_tree_bytes, bytes));
             d_sums = bytes > kSmallBytes ? static_cast<double *>(ctx->ws_tree) : ctx->d_small;
             QF_CUDA(cudaMemsetAsync(d_sums, 0, bytes, ctx->stream));
-            QF_TRY(run_plan_dual(psi, lam, plan, d_sums));
+            QF_TRY(run_plan_dual(psi, lam, plan, d_sums, o->exec.flags));
             std::vector<double> sums(plan.n_slots);
             QF_CUDA(cudaMemcpyAsync(sums.data(), d_sums, bytes, cudaMemcpyDeviceToHost, ctx->stream));
             QF_CUDA(cudaStreamSynchronize(ctx->stream));
             for (uint32_t k = 0; k < plan.n_slots; ++k) g[(size_t)plan.slot_param[k]] += sums[k];
         } else {
-            QF_TRY(run_plan_dual(psi, lam, plan, nullptr));
+            QF_TRY(run_plan_dual(psi, lam, plan, nullptr, o->exec.flags));
         }
         if (s > 0 && !ckpt.empty())
             QF_CUDA(cudaMemcpyAsync(psi->d, ckpt[s - 1]->d, psi->bytes(), cudaMemcpyDeviceToDevice, ctx->stream));

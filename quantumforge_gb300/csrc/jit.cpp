@@ -121,7 +121,8 @@ struct Gen {
     bool any_diag = false;
     int tmp = 0;
 
-    std::string R(int i) const { return "r" + std::to_string(v[i]); }
+    std::string pfx = "r";  // register array: r = psi, l = lambda (backward passes)
+    std::string R(int i) const { return pfx + std::to_string(v[i]); }
     std::string fresh(const char *stem) { return std::string(stem) + std::to_string(tmp++); }
     int slot(std::complex<double> a, std::complex<double> b, std::complex<double> c, std::complex<double> d) {
         consts.push_back(a);
@@ -205,7 +206,9 @@ struct PassGen {
     uint32_t slot_q[kPos];
     uint32_t L[kPos];  // position -> qubit
 
-    PassGen(Gen &gen, const Pass &pass, uint32_t nq) : g(gen), p(pass), n(nq) {
+    bool dual;  // backward pass: psi (A, r*) and lambda (B, l*) with overlap slots
+
+    PassGen(Gen &gen, const Pass &pass, uint32_t nq, bool dual_ = false) : g(gen), p(pass), n(nq), dual(dual_) {
         for (int q = 0; q < 64; ++q) slot_of[q] = -1;
         int s = 0;
         for (uint32_t q = 0; q < n; ++q)
@@ -246,15 +249,18 @@ struct PassGen {
     std::vector<int> order;  // gate indices in emission order
     bool failed = false;
 
+    // An overlap Im<lambda|P_q psi> commutes with every gate that commutes
+    // with P_q: it is diagonal on q for P = Z.
     static bool diag_on(const BGate &x, uint32_t q) {
         switch (x.kind) {
         case BK_MAT1: return x.diag != 0;
         case BK_CNOT: return q == x.q0;
         case BK_CZ: return true;
+        case BK_OVL: return x.axis == QF_PAULI_Z;
         default: return false;
         }
     }
-    static int arity(const BGate &x) { return x.kind == BK_MAT1 ? 1 : 2; }
+    static int arity(const BGate &x) { return (x.kind == BK_MAT1 || x.kind == BK_OVL) ? 1 : 2; }
     static uint32_t qubit(const BGate &x, int k) { return k ? x.q1 : x.q0; }
     void build_deps() {
         const auto &G = p.gates;
@@ -276,11 +282,14 @@ struct PassGen {
             if (!d[i]) return false;
         return true;
     }
-    static bool strict_need(const BGate &x) { return (x.kind == BK_MAT1 && !x.diag) || x.kind == BK_CNOT; }
+    static bool strict_need(const BGate &x) {
+        return (x.kind == BK_MAT1 && !x.diag) || x.kind == BK_CNOT || (x.kind == BK_OVL && x.axis != QF_PAULI_Z);
+    }
     bool runnable(const BGate &x, uint64_t regs, bool force_diag) const {
         if (x.kind == BK_MAT1)  // a diagonal gate on a qubit outside the tile never reaches a register
             return ((regs >> x.q0) & 1ULL) || (x.diag && (force_diag || !((p.resident >> x.q0) & 1ULL)));
         if (x.kind == BK_CNOT) return (regs >> x.q1) & 1ULL;
+        if (x.kind == BK_OVL) return x.axis == QF_PAULI_Z || ((regs >> x.q0) & 1ULL);
         return true;
     }
     // gates that would run with `regs` in register positions, from state `d`
@@ -431,32 +440,52 @@ struct PassGen {
             if (L[5 + r] == slot_q[0]) return r;
         return -1;
     }
-    // read all registers from shared memory S in the current layout
+    // arrays: 0 = psi (registers r*, shared S, global A), 1 = lambda (l*, SL, B)
+    int n_arrays() const { return dual ? 2 : 1; }
+    static const char *reg_pfx(int a) { return a ? "l" : "r"; }
+    static const char *smem_of(int a) { return a ? "SL" : "S"; }
+    static const char *glob_of(int a) { return a ? "B" : "A"; }
+    // read all registers from shared memory in the current layout
     void emit_read() {
         const std::string pt = g.fresh("pt");
         g.s << "const unsigned " << pt << " = qf_phys(" << thread_index() << ");\n";
-        if (const int pb = pair_bit(); pb >= 0) {
-            for (int i = 0; i < kR; ++i)
-                if (!((i >> pb) & 1))
-                    g.s << "{const float4 t = *reinterpret_cast<const float4*>(S + (" << pt << " ^ " << physj(reg_index(i))
-                        << "u)); " << g.R(i) << " = make_float2(t.x, t.y); " << g.R(i | (1 << pb)) << " = make_float2(t.z, t.w);}\n";
-            return;
+        const int pb = pair_bit();
+        for (int a = 0; a < n_arrays(); ++a) {
+            g.pfx = reg_pfx(a);
+            const char *S_ = smem_of(a);
+            if (pb >= 0) {
+                for (int i = 0; i < kR; ++i)
+                    if (!((i >> pb) & 1))
+                        g.s << "{const float4 t = *reinterpret_cast<const float4*>(" << S_ << " + (" << pt << " ^ "
+                            << physj(reg_index(i)) << "u)); " << g.R(i) << " = make_float2(t.x, t.y); " << g.R(i | (1 << pb))
+                            << " = make_float2(t.z, t.w);}\n";
+            } else {
+                for (int i = 0; i < kR; ++i)
+                    g.s << g.R(i) << " = " << S_ << "[" << pt << " ^ " << physj(reg_index(i)) << "u];\n";
+            }
         }
-        for (int i = 0; i < kR; ++i) g.s << g.R(i) << " = S[" << pt << " ^ " << physj(reg_index(i)) << "u];\n";
+        g.pfx = "r";
     }
     void emit_write() {
         const std::string pt = g.fresh("pt");
         g.s << "const unsigned " << pt << " = qf_phys(" << thread_index() << ");\n";
-        if (const int pb = pair_bit(); pb >= 0) {
-            for (int i = 0; i < kR; ++i)
-                if (!((i >> pb) & 1)) {
-                    const std::string A_ = g.R(i), B_ = g.R(i | (1 << pb));
-                    g.s << "*reinterpret_cast<float4*>(S + (" << pt << " ^ " << physj(reg_index(i)) << "u)) = make_float4(" << A_
-                        << ".x, " << A_ << ".y, " << B_ << ".x, " << B_ << ".y);\n";
-                }
-            return;
+        const int pb = pair_bit();
+        for (int a = 0; a < n_arrays(); ++a) {
+            g.pfx = reg_pfx(a);
+            const char *S_ = smem_of(a);
+            if (pb >= 0) {
+                for (int i = 0; i < kR; ++i)
+                    if (!((i >> pb) & 1)) {
+                        const std::string A_ = g.R(i), B_ = g.R(i | (1 << pb));
+                        g.s << "*reinterpret_cast<float4*>(" << S_ << " + (" << pt << " ^ " << physj(reg_index(i))
+                            << "u)) = make_float4(" << A_ << ".x, " << A_ << ".y, " << B_ << ".x, " << B_ << ".y);\n";
+                    }
+            } else {
+                for (int i = 0; i < kR; ++i)
+                    g.s << S_ << "[" << pt << " ^ " << physj(reg_index(i)) << "u] = " << g.R(i) << ";\n";
+            }
         }
-        for (int i = 0; i < kR; ++i) g.s << "S[" << pt << " ^ " << physj(reg_index(i)) << "u] = " << g.R(i) << ";\n";
+        g.pfx = "r";
     }
     // global byte-free address bits of canonical shared index j's register+warp part
     uint64_t chunk_k_bits(int k) const {  // canonical j = 2*tid + 512*k: bits 9..11 = k -> slots 9..11
@@ -466,13 +495,35 @@ struct PassGen {
         return a;
     }
 
+    // slots of this pass held as f64 accumulators, one per lane and 32 slots
+    static constexpr int kMaxAcc = 4;
+    int n_acc() const { return ((int)p.a.n_slots + 31) / 32; }
+    std::streamoff prefetch_mark = -1;  // backward passes: where the next tile's load is spliced in
+
+    void emit_issue(const std::string &tq) {
+        auto &s = g.s;
+        for (int a = 0; a < n_arrays(); ++a)
+            for (int k = 0; k < kChunks; ++k)
+                s << "qf_cpa16(sbase + (" << (a ? "4096u + " : "") << "(pt2 ^ " << physj(512u * k) << "u)) * 8u, "
+                  << glob_of(a) << " + (" << tq << " | toff | " << hex64(chunk_k_bits(k)) << "));\n";
+    }
+
     void emit_kernel(int index, bool last_pass) {
         auto &s = g.s;
         for (int i = 0; i < kR; ++i) g.v[i] = i;
         const std::string dep_t = deposit_code(p.a.nonlocal_mask, "t");
         const std::string dep_t2 = deposit_code(p.a.nonlocal_mask, "t2");
-        s << "extern \"C\" __global__ void __launch_bounds__(" << kThreads << ", 3) p" << index
-          << "(float2* __restrict__ A, unsigned long long nt) {\n";
+        if (dual && n_acc() > kMaxAcc) {
+            failed = true;
+            return;
+        }
+        if (!dual)
+            s << "extern \"C\" __global__ void __launch_bounds__(" << kThreads << ", 3) p" << index
+              << "(float2* __restrict__ A, unsigned long long nt) {\n";
+        else
+            s << "extern \"C\" __global__ void __launch_bounds__(" << kThreads << ", 2) p" << index
+              << "(float2* __restrict__ A, float2* __restrict__ B, unsigned long long nt, double* __restrict__ partials, "
+                 "unsigned stride) {\n";
         s << "extern __shared__ __align__(16) float2 SB[];\n";
         s << "const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, tid = threadIdx.x;\n";
         s << "const unsigned sbase = (unsigned)__cvta_generic_to_shared(SB);\n";
@@ -488,22 +539,36 @@ struct PassGen {
                   << " | toff | " << hex64(chunk_k_bits(k)) << "));\n";
         };
         s << "unsigned long long t = blockIdx.x;\n";
-        s << "if (t < nt) {const unsigned long long tq = " << dep_t << ";\n";
-        issue("tq", "0u");
-        s << "}\nasm volatile(\"cp.async.commit_group;\\n\" ::: \"memory\");\n";
-        s << "for (unsigned it = 0; t < nt; t += gridDim.x, ++it) {\n";
-        s << "const unsigned cur = it & 1u;\n";
-        s << "{const unsigned long long t2 = t + gridDim.x; if (t2 < nt) {const unsigned long long tq = " << dep_t2 << ";\n";
-        issue("tq", "cur ^ 1u");
-        s << "}}\nasm volatile(\"cp.async.commit_group;\\n\" ::: \"memory\");\n";
-        s << "asm volatile(\"cp.async.wait_group 1;\\n\" ::: \"memory\");\n__syncthreads();\n";
-        s << "float2* S = SB + cur * " << kTile << "u;\n";
+        if (!dual) {
+            s << "if (t < nt) {const unsigned long long tq = " << dep_t << ";\n";
+            issue("tq", "0u");
+            s << "}\nasm volatile(\"cp.async.commit_group;\\n\" ::: \"memory\");\n";
+            s << "for (unsigned it = 0; t < nt; t += gridDim.x, ++it) {\n";
+            s << "const unsigned cur = it & 1u;\n";
+            s << "{const unsigned long long t2 = t + gridDim.x; if (t2 < nt) {const unsigned long long tq = " << dep_t2 << ";\n";
+            issue("tq", "cur ^ 1u");
+            s << "}}\nasm volatile(\"cp.async.commit_group;\\n\" ::: \"memory\");\n";
+            s << "asm volatile(\"cp.async.wait_group 1;\\n\" ::: \"memory\");\n__syncthreads();\n";
+            s << "float2* S = SB + cur * " << kTile << "u;\n";
+        } else {
+            // one psi + lambda buffer; the next tile streams in after the last
+            // shared-memory read of the current one
+            for (int a = 0; a < n_acc(); ++a) s << "double acc" << a << " = 0.0;\n";
+            s << "if (t < nt) {const unsigned long long tq = " << dep_t << ";\n";
+            emit_issue("tq");
+            s << "}\nasm volatile(\"cp.async.commit_group;\\n\" ::: \"memory\");\n";
+            s << "for (; t < nt; t += gridDim.x) {\n";
+            s << "asm volatile(\"cp.async.wait_group 0;\\n\" ::: \"memory\");\n__syncthreads();\n";
+            s << "float2* S = SB;\nfloat2* SL = SB + " << kTile << "u;\n";
+        }
         s << "const unsigned long long tb = " << dep_t << ";\n";
-        for (int i = 0; i < kR; ++i) s << "float2 r" << i << ";\n";
+        for (int a = 0; a < n_arrays(); ++a)
+            for (int i = 0; i < kR; ++i) s << "float2 " << reg_pfx(a) << i << ";\n";
         build_deps();
         relayout(choose_regs());
         emit_read();
         s << "__syncthreads();\n";
+        prefetch_mark = (std::streamoff)s.tellp();
         const auto &G = p.gates;
         size_t left = G.size();
         bool remapped = false;
@@ -546,23 +611,63 @@ struct PassGen {
             relayout(choose_regs());
             emit_read();
             s << "__syncthreads();\n}\n";
+            prefetch_mark = (std::streamoff)s.tellp();
             remapped = true;
         }
-        finish(last_pass);
+        finish(last_pass, dep_t2);
+    }
+
+    // Im<lambda|P_q psi> over the thread's amplitudes (the adjoint term of
+    // src/lib.rs:3648-3664, summed as the shared-memory kernel does), reduced
+    // over the warp in f32 and added to the slot's f64 accumulator (held by
+    // lane slot % 32).
+    void emit_overlap(const BGate &x) {
+        auto &s = g.s;
+        const int ls = (int)x.op_index - (int)p.a.slot_base;
+        auto R_ = [&](int i) { return "r" + std::to_string(g.v[i]); };
+        auto L_ = [&](int i) { return "l" + std::to_string(g.v[i]); };
+        s << "{float ov = 0.f;\n";
+        const uint8_t d = desc(x.q0);
+        if (x.axis == QF_PAULI_Z) {
+            const int rb = is_reg(d) ? d - 8 : -1;
+            for (int i = 0; i < kR; ++i) {
+                const bool neg = rb >= 0 && ((i >> rb) & 1);
+                s << "ov " << (neg ? "-" : "+") << "= " << L_(i) << ".x * " << R_(i) << ".y - " << L_(i) << ".y * " << R_(i)
+                  << ".x;\n";
+            }
+            if (rb < 0) s << "if (" << cbit(d) << ") ov = -ov;\n";
+        } else {
+            const int rb = d - 8;
+            const bool y = x.axis == QF_PAULI_Y;
+            for (int i = 0; i < kR; ++i) {
+                if ((i >> rb) & 1) continue;
+                const int j = i | (1 << rb);
+                const std::string l0 = L_(i), l1 = L_(j), p0 = R_(i), p1 = R_(j);
+                if (!y)
+                    s << "ov += (" << l0 << ".x * " << p1 << ".y - " << l0 << ".y * " << p1 << ".x) + (" << l1 << ".x * " << p0
+                      << ".y - " << l1 << ".y * " << p0 << ".x);\n";
+                else
+                    s << "ov += -(" << l0 << ".x * " << p1 << ".x + " << l0 << ".y * " << p1 << ".y) + (" << l1 << ".x * " << p0
+                      << ".x + " << l1 << ".y * " << p0 << ".y);\n";
+            }
+        }
+        for (int o = 16; o >= 1; o >>= 1) s << "ov += __shfl_xor_sync(0xffffffffu, ov, " << o << ");\n";
+        s << "if (lane == " << (ls & 31) << "u) acc" << (ls >> 5) << " += (double)ov;}\n";
     }
 
     void emit_gate(const BGate &x) {
         auto &s = g.s;
-        {
-            switch (x.kind) {
-            case BK_MAT1: {
-                std::complex<double> m[4] = {{x.m[0], x.m[1]}, {x.m[2], x.m[3]}, {x.m[4], x.m[5]}, {x.m[6], x.m[7]}};
-                if (x.diag) {  // diag(m00, m11) = m00 * diag(1, m11/m00)
-                    g.any_diag = true;
-                    g.gphase *= m[0];
-                    const std::complex<double> f = m[3] / m[0];
-                    const int sl = g.slot(f, 0.0, 0.0, f);
-                    const uint8_t d = desc(x.q0);
+        switch (x.kind) {
+        case BK_MAT1: {
+            std::complex<double> m[4] = {{x.m[0], x.m[1]}, {x.m[2], x.m[3]}, {x.m[4], x.m[5]}, {x.m[6], x.m[7]}};
+            if (x.diag) {  // diag(m00, m11) = m00 * diag(1, m11/m00)
+                g.any_diag = true;
+                g.gphase *= m[0];
+                const std::complex<double> f = m[3] / m[0];
+                const int sl = g.slot(f, 0.0, 0.0, f);
+                const uint8_t d = desc(x.q0);
+                for (int a = 0; a < n_arrays(); ++a) {
+                    g.pfx = reg_pfx(a);
                     if (is_reg(d)) {
                         const int rb = d - 8;
                         for (int i = 0; i < kR; ++i)
@@ -572,93 +677,145 @@ struct PassGen {
                         for (int i = 0; i < kR; ++i) emit_cmul_const(g, g.R(i), sl, 0);
                         s << "}\n";
                     }
-                } else {
-                    const int mk = matrix_kind_of(m);
-                    int sl;
-                    if (mk == 1)  // splatted real entries for packed f32x2 arithmetic
-                        sl = g.slot({m[0].real(), m[0].real()}, {m[1].real(), m[1].real()}, {m[2].real(), m[2].real()},
-                                    {m[3].real(), m[3].real()});
-                    else
-                        sl = g.slot(m[0], m[1], m[2], m[3]);
-                    const int rb = pos_of(x.q0) - 5;
+                }
+            } else {
+                const int mk = matrix_kind_of(m);
+                int sl;
+                if (mk == 1)  // splatted real entries for packed f32x2 arithmetic
+                    sl = g.slot({m[0].real(), m[0].real()}, {m[1].real(), m[1].real()}, {m[2].real(), m[2].real()},
+                                {m[3].real(), m[3].real()});
+                else
+                    sl = g.slot(m[0], m[1], m[2], m[3]);
+                const int rb = pos_of(x.q0) - 5;
+                for (int a = 0; a < n_arrays(); ++a) {
+                    g.pfx = reg_pfx(a);
                     for (int i = 0; i < kR; ++i)
                         if (!((i >> rb) & 1)) emit_mat2(g, sl, mk, g.R(i), g.R(i | (1 << rb)));
                 }
-                break;
             }
-            case BK_CNOT: {
-                const uint8_t dc = desc(x.q0);
-                const int tb_ = pos_of(x.q1) - 5;
-                if (is_reg(dc)) {  // rename only
-                    const int cb = dc - 8;
-                    for (int i = 0; i < kR; ++i)
-                        if (((i >> cb) & 1) && !((i >> tb_) & 1)) std::swap(g.v[i], g.v[i | (1 << tb_)]);
-                } else {
-                    s << "if (" << cbit(dc) << ") {\n";
+            break;
+        }
+        case BK_CNOT: {
+            const uint8_t dc = desc(x.q0);
+            const int tb_ = pos_of(x.q1) - 5;
+            if (is_reg(dc)) {  // rename only (the same for both arrays)
+                const int cb = dc - 8;
+                for (int i = 0; i < kR; ++i)
+                    if (((i >> cb) & 1) && !((i >> tb_) & 1)) std::swap(g.v[i], g.v[i | (1 << tb_)]);
+            } else {
+                s << "if (" << cbit(dc) << ") {\n";
+                for (int a = 0; a < n_arrays(); ++a) {
+                    g.pfx = reg_pfx(a);
                     for (int i = 0; i < kR; ++i)
                         if (!((i >> tb_) & 1)) {
                             const std::string A_ = g.R(i), B_ = g.R(i | (1 << tb_));
                             s << "{const float2 x=" << A_ << "; " << A_ << "=" << B_ << "; " << B_ << "=x;}\n";
                         }
-                    s << "}\n";
                 }
-                break;
+                s << "}\n";
             }
-            case BK_CZ: {
-                const uint8_t da = desc(x.q0), db = desc(x.q1);
-                auto neg = [&](int i) { s << g.R(i) << ".x = -" << g.R(i) << ".x; " << g.R(i) << ".y = -" << g.R(i) << ".y;\n"; };
+            break;
+        }
+        case BK_CZ: {
+            const uint8_t da = desc(x.q0), db = desc(x.q1);
+            auto neg = [&](int i) { s << g.R(i) << ".x = -" << g.R(i) << ".x; " << g.R(i) << ".y = -" << g.R(i) << ".y;\n"; };
+            for (int a = 0; a < n_arrays(); ++a) {
+                g.pfx = reg_pfx(a);
                 if (is_reg(da) && is_reg(db)) {
                     for (int i = 0; i < kR; ++i)
                         if (((i >> (da - 8)) & 1) && ((i >> (db - 8)) & 1)) neg(i);
                 } else if (is_reg(da) || is_reg(db)) {
-                    const int a = (is_reg(da) ? da : db) - 8;
+                    const int b = (is_reg(da) ? da : db) - 8;
                     s << "if (" << cbit(is_reg(da) ? db : da) << ") {\n";
                     for (int i = 0; i < kR; ++i)
-                        if ((i >> a) & 1) neg(i);
+                        if ((i >> b) & 1) neg(i);
                     s << "}\n";
                 } else {
                     s << "if (" << cbit(da) << " & " << cbit(db) << ") {\n";
                     for (int i = 0; i < kR; ++i) neg(i);
                     s << "}\n";
                 }
-                break;
             }
-            default: {  // SWAP of two resident qubits: relabel
-                const int a = pos_of(x.q0), b = pos_of(x.q1);
-                std::swap(L[a], L[b]);
-                break;
-            }
-            }
+            break;
         }
+        case BK_OVL: emit_overlap(x); break;
+        default: {  // SWAP of two resident qubits: relabel
+            const int a = pos_of(x.q0), b = pos_of(x.q1);
+            std::swap(L[a], L[b]);
+            break;
+        }
+        }
+        g.pfx = "r";
     }
 
-    void finish(bool last_pass) {
+    void finish(bool last_pass, const std::string &dep_t2) {
         auto &s = g.s;
         if (last_pass && g.any_diag) {  // the plan's global phase, once, at the very end
             const int sl = g.slot(g.gphase, 0.0, 0.0, 0.0);
-            for (int i = 0; i < kR; ++i) emit_cmul_const(g, g.R(i), sl, 0);
+            for (int a = 0; a < n_arrays(); ++a) {
+                g.pfx = reg_pfx(a);
+                for (int i = 0; i < kR; ++i) emit_cmul_const(g, g.R(i), sl, 0);
+            }
+            g.pfx = "r";
         }
+        const std::string prefetch = "{const unsigned long long t2 = t + gridDim.x; if (t2 < nt) {const unsigned long long tq = " +
+                                     dep_t2 + ";\n";
         bool natural = true;
         for (int ps = 0; ps < 5; ++ps) natural = natural && L[ps] == (uint32_t)ps;
         if (natural) {  // lanes hold qubits 0..4: store straight from registers
+            if (dual) {  // shared memory is free from the last read on: start the next tile there
+                std::string txt = s.str();
+                std::ostringstream keep;
+                std::swap(keep, g.s);  // emit the copy code into a fresh stream
+                emit_issue("tq");
+                const std::string issue_code = g.s.str();
+                std::swap(keep, g.s);
+                txt.insert((size_t)prefetch_mark,
+                           prefetch + issue_code + "}}\nasm volatile(\"cp.async.commit_group;\\n\" ::: \"memory\");\n");
+                s.str("");
+                s.clear();
+                s << txt;
+            }
             s << "const unsigned long long sw = 0ull";
             for (int w = 0; w < 3; ++w) s << " | ((warp & " << (1 << w) << "u) ? (1ull << " << L[9 + w] << ") : 0ull)";
             s << ";\n";
-            for (int i = 0; i < kR; ++i) {
-                uint64_t off = 0;
-                for (int r = 0; r < 4; ++r)
-                    if ((i >> r) & 1) off |= 1ULL << L[5 + r];
-                s << "A[(tb | lane | sw) | " << hex64(off) << "] = " << g.R(i) << ";\n";
+            for (int a = 0; a < n_arrays(); ++a) {
+                g.pfx = reg_pfx(a);
+                for (int i = 0; i < kR; ++i) {
+                    uint64_t off = 0;
+                    for (int r = 0; r < 4; ++r)
+                        if ((i >> r) & 1) off |= 1ULL << L[5 + r];
+                    s << glob_of(a) << "[(tb | lane | sw) | " << hex64(off) << "] = " << g.R(i) << ";\n";
+                }
             }
+            g.pfx = "r";
         } else {  // through shared memory, 16-byte coalesced stores
             emit_write();
             s << "__syncthreads();\n";
-            for (int k = 0; k < kChunks; ++k)
-                s << "*reinterpret_cast<float4*>(A + (tb | toff | " << hex64(chunk_k_bits(k))
-                  << ")) = *reinterpret_cast<const float4*>(S + (pt2 ^ " << physj(512u * k) << "u));\n";
+            for (int a = 0; a < n_arrays(); ++a)
+                for (int k = 0; k < kChunks; ++k)
+                    s << "*reinterpret_cast<float4*>(" << glob_of(a) << " + (tb | toff | " << hex64(chunk_k_bits(k))
+                      << ")) = *reinterpret_cast<const float4*>(" << smem_of(a) << " + (pt2 ^ " << physj(512u * k) << "u));\n";
             s << "__syncthreads();\n";
+            if (dual) {
+                s << prefetch;
+                emit_issue("tq");
+                s << "}}\nasm volatile(\"cp.async.commit_group;\\n\" ::: \"memory\");\n";
+            }
         }
-        s << "}\n}\n";
+        s << "}\n";  // tile loop
+        if (dual) {  // per-CTA slot sums, warps in order
+            s << "asm volatile(\"cp.async.wait_group 0;\\n\" ::: \"memory\");\n__syncthreads();\n";
+            s << "double* RD = reinterpret_cast<double*>(SB);\n";
+            for (int a = 0; a < n_acc(); ++a)
+                s << "if (lane + " << 32 * a << "u < " << p.a.n_slots << "u) RD[(lane + " << 32 * a << "u) * 8u + warp] = acc" << a
+                  << ";\n";
+            s << "__syncthreads();\n";
+            s << "for (unsigned k = tid; k < " << p.a.n_slots << "u; k += " << kThreads << "u) {double v = 0.0;"
+              << " for (unsigned w = 0; w < 8u; ++w) v += RD[k * 8u + w];"
+              << " partials[(size_t)(" << p.a.slot_base << "u + k) * stride + blockIdx.x] = v;}\n";
+        }
+        s << "}\n";  // kernel
     }
 };
 
@@ -758,7 +915,7 @@ struct ModulePlan {
 bool pass_fits(const Pass &p) { return __builtin_popcountll(p.resident) == kPos && (p.resident & 31ULL) == 31ULL; }
 
 // group passes into modules: at most 8 passes and 56 KB of constants each
-bool gen_modules(const Plan &plan, std::vector<ModulePlan> &mods) {
+bool gen_modules(const Plan &plan, std::vector<ModulePlan> &mods, bool dual = false) {
     Gen g;
     const size_t npass = plan.passes.size();
     size_t pi = 0;
@@ -770,7 +927,7 @@ bool gen_modules(const Plan &plan, std::vector<ModulePlan> &mods) {
         while (pi < npass && local < 8 && g.consts.size() * 8 < 56 * 1024) {
             g.s.str("");
             g.s.clear();
-            PassGen pg(g, plan.passes[pi], plan.n);
+            PassGen pg(g, plan.passes[pi], plan.n, dual);
             pg.emit_kernel(local, pi + 1 == npass);
             if (pg.failed) return false;
             body << g.s.str();
@@ -803,10 +960,10 @@ bool jit_plan_fits(const Plan &plan) {
 }
 
 // Generated sources and an NVRTC compile without loading (needs no GPU).
-int jit_check_compile(const Plan &plan, int, std::string *source, std::string *err) {
+int jit_check_compile(const Plan &plan, int, std::string *source, std::string *err, bool dual) {
     if (!jit_plan_fits(plan)) return fail(QF_ERR_UNSUPPORTED_OPERATION, "plan has a pass outside the compiled layout");
     std::vector<ModulePlan> mods;
-    if (!gen_modules(plan, mods)) return fail(QF_ERR_UNSUPPORTED_OPERATION, "pass compiler could not schedule a pass");
+    if (!gen_modules(plan, mods, dual)) return fail(QF_ERR_UNSUPPORTED_OPERATION, "pass compiler could not schedule a pass");
     Nvrtc &nv = nvrtc();
     if (!nv.ok) return fail(QF_ERR_UNSUPPORTED_OPERATION, "%s", nv.why.c_str());
     for (auto &m : mods) {
@@ -828,13 +985,10 @@ int jit_check_compile(const Plan &plan, int, std::string *source, std::string *e
     return QF_OK;
 }
 
-// Generate, compile (or fetch) and launch the plan's passes.
-int run_plan_jit(qf_sv *sv, const Plan &plan, int) {
-    if (!jit_plan_fits(plan)) return run_plan_rs(sv, plan, 3);  // interpreted (falls back to shared memory)
-    qf_ctx *ctx = sv->ctx;
-    std::vector<ModulePlan> mods;
-    if (!gen_modules(plan, mods)) return run_plan_rs(sv, plan, 3);
-    std::vector<std::shared_ptr<JitModule>> handles(mods.size());
+namespace {
+// Compiled modules for `mods`, from the cache or compiled in parallel.
+int fetch_modules(qf_ctx *ctx, const std::vector<ModulePlan> &mods, std::vector<std::shared_ptr<JitModule>> &handles) {
+    handles.assign(mods.size(), nullptr);
     std::vector<size_t> todo;
     {
         std::lock_guard<std::mutex> lk(cache().mu);
@@ -844,39 +998,61 @@ int run_plan_jit(qf_sv *sv, const Plan &plan, int) {
             else todo.push_back(m);
         }
     }
-    if (!todo.empty()) {  // compile the missing modules in parallel
-        std::vector<int> st(todo.size(), QF_OK);
-        std::vector<std::string> errs(todo.size());
-        std::vector<std::shared_ptr<JitModule>> built(todo.size());
-        std::vector<std::thread> th;
-        const int dev = ctx->device;
-        for (size_t k = 0; k < todo.size(); ++k) {
-            built[k] = std::make_shared<JitModule>();
-            th.emplace_back([&, k, dev] {
-                cudaSetDevice(dev);
-                st[k] = compile_module(mods[todo[k]].src, (int)mods[todo[k]].pass_index.size(), dev, *built[k], errs[k]);
-            });
-        }
-        for (auto &t : th) t.join();
-        for (size_t k = 0; k < todo.size(); ++k)
-            if (st[k]) return fail(st[k], "pass compiler: %s", errs[k].c_str());
-        std::lock_guard<std::mutex> lk(cache().mu);
-        for (size_t k = 0; k < todo.size(); ++k) {
-            cache().mods[mods[todo[k]].src] = built[k];
-            handles[todo[k]] = built[k];
-        }
+    if (todo.empty()) return QF_OK;
+    std::vector<int> st(todo.size(), QF_OK);
+    std::vector<std::string> errs(todo.size());
+    std::vector<std::shared_ptr<JitModule>> built(todo.size());
+    std::vector<std::thread> th;
+    const int dev = ctx->device;
+    for (size_t k = 0; k < todo.size(); ++k) {
+        built[k] = std::make_shared<JitModule>();
+        th.emplace_back([&, k, dev] {
+            cudaSetDevice(dev);
+            st[k] = compile_module(mods[todo[k]].src, (int)mods[todo[k]].pass_index.size(), dev, *built[k], errs[k]);
+        });
     }
+    for (auto &t : th) t.join();
+    for (size_t k = 0; k < todo.size(); ++k)
+        if (st[k]) return fail(st[k], "pass compiler: %s", errs[k].c_str());
+    std::lock_guard<std::mutex> lk(cache().mu);
+    for (size_t k = 0; k < todo.size(); ++k) {
+        cache().mods[mods[todo[k]].src] = built[k];
+        handles[todo[k]] = built[k];
+    }
+    return QF_OK;
+}
+
+int upload_consts(qf_ctx *ctx, JitModule &jm, const ModulePlan &mp) {
+    const size_t bytes = mp.consts.size() * sizeof(float);
+    if (bytes > jm.consts_bytes) return fail(QF_ERR_CUDA, "pass compiler: constant bank size mismatch");
+    if (bytes) QF_CUDA(cudaMemcpyAsync(jm.consts, mp.consts.data(), bytes, cudaMemcpyHostToDevice, ctx->stream));
+    return QF_OK;
+}
+
+int grid_of(qf_ctx *ctx, cudaKernel_t k, uint64_t n_tiles, uint64_t *grid) {
+    int per_sm = 0;
+    QF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)k, kThreads, kDynSmem));
+    per_sm = std::min(std::max(per_sm, 1), 4);
+    *grid = std::min<uint64_t>((uint64_t)per_sm * ctx->sm_count, n_tiles);
+    return QF_OK;
+}
+}  // namespace
+
+// Generate, compile (or fetch) and launch the plan's passes.
+int run_plan_jit(qf_sv *sv, const Plan &plan, int) {
+    if (!jit_plan_fits(plan)) return run_plan_rs(sv, plan, 3);  // interpreted (falls back to shared memory)
+    qf_ctx *ctx = sv->ctx;
+    std::vector<ModulePlan> mods;
+    if (!gen_modules(plan, mods)) return run_plan_rs(sv, plan, 3);
+    std::vector<std::shared_ptr<JitModule>> handles;
+    QF_TRY(fetch_modules(ctx, mods, handles));
     for (size_t m = 0; m < mods.size(); ++m) {
         JitModule &jm = *handles[m];
-        const size_t bytes = mods[m].consts.size() * sizeof(float);
-        if (bytes > jm.consts_bytes) return fail(QF_ERR_CUDA, "pass compiler: constant bank size mismatch");
-        if (bytes) QF_CUDA(cudaMemcpyAsync(jm.consts, mods[m].consts.data(), bytes, cudaMemcpyHostToDevice, ctx->stream));
+        QF_TRY(upload_consts(ctx, jm, mods[m]));
         for (size_t k = 0; k < mods[m].pass_index.size(); ++k) {
             const Pass &p = plan.passes[mods[m].pass_index[k]];
-            int per_sm = 0;
-            QF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)jm.kernels[k], kThreads, kDynSmem));
-            per_sm = std::max(per_sm, 1);
-            const uint64_t grid = std::min<uint64_t>((uint64_t)per_sm * ctx->sm_count, p.a.n_tiles);
+            uint64_t grid;
+            QF_TRY(grid_of(ctx, jm.kernels[k], p.a.n_tiles, &grid));
             float2 *amps = static_cast<float2 *>(sv->d);
             unsigned long long nt = p.a.n_tiles;
             void *args[] = {&amps, &nt};
@@ -884,6 +1060,44 @@ int run_plan_jit(qf_sv *sv, const Plan &plan, int) {
                                      ctx->stream));
         }
     }
+    return QF_OK;
+}
+
+// Backward adjoint passes: psi and lambda in registers, the overlap slots
+// reduced per CTA into partials[slot * stride + block] and then summed in
+// block order into d_slot_sums.
+int run_plan_jit_dual(qf_sv *psi, qf_sv *lam, const Plan &plan, double *d_slot_sums) {
+    if (!jit_plan_fits(plan)) return run_plan_dual_smem(psi, lam, plan, d_slot_sums);
+    qf_ctx *ctx = psi->ctx;
+    std::vector<ModulePlan> mods;
+    if (!gen_modules(plan, mods, true)) return run_plan_dual_smem(psi, lam, plan, d_slot_sums);
+    std::vector<std::shared_ptr<JitModule>> handles;
+    QF_TRY(fetch_modules(ctx, mods, handles));
+    const uint32_t stride = 4u * (uint32_t)std::max(1, ctx->sm_count);
+    double *d_partials = nullptr;
+    if (plan.n_slots) {
+        const size_t bytes = sizeof(double) * (size_t)plan.n_slots * stride;
+        QF_TRY(ensure_device(&ctx->ws_red, &ctx->ws_red_bytes, bytes));
+        d_partials = static_cast<double *>(ctx->ws_red);
+        QF_CUDA(cudaMemsetAsync(d_partials, 0, bytes, ctx->stream));
+    }
+    for (size_t m = 0; m < mods.size(); ++m) {
+        JitModule &jm = *handles[m];
+        QF_TRY(upload_consts(ctx, jm, mods[m]));
+        for (size_t k = 0; k < mods[m].pass_index.size(); ++k) {
+            const Pass &p = plan.passes[mods[m].pass_index[k]];
+            uint64_t grid;
+            QF_TRY(grid_of(ctx, jm.kernels[k], p.a.n_tiles, &grid));
+            float2 *a = static_cast<float2 *>(psi->d), *b = static_cast<float2 *>(lam->d);
+            unsigned long long nt = p.a.n_tiles;
+            double *parts = d_partials;
+            unsigned str = stride;
+            void *args[] = {&a, &b, &nt, &parts, &str};
+            QF_CUDA(cudaLaunchKernel((const void *)jm.kernels[k], dim3((unsigned)grid), dim3(kThreads), args, kDynSmem,
+                                     ctx->stream));
+        }
+    }
+    if (plan.n_slots && d_slot_sums) QF_TRY(reduce_slots(ctx, d_partials, stride, plan.n_slots, d_slot_sums));
     return QF_OK;
 }
 

@@ -298,8 +298,6 @@ int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, 
         p.a.nonlocal_mask = all & ~L;
         p.a.n_tiles = 1ULL << (n - p.a.k);
         p.resident = L;
-        if (!o.backward)
-            for (const Item &it : taken) p.gates.push_back(it.g);
         p.op_begin = (uint32_t)plan.ops.size();
         p.mat_begin = (uint32_t)(plan.mats.size() / 8);
         p.a.slot_base = plan.n_slots;
@@ -318,8 +316,13 @@ int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, 
                 else if (lb0 >= 0) { t.kind = T_OVL_ZL; t.b0 = (uint8_t)lb0; }
                 else { t.kind = T_OVL_ZG; t.g0 = g.q0; }
                 plan.ops.push_back(t);
+                BGate ov = g;
+                ov.kind = BK_OVL;
+                ov.op_index = t.slot;
+                p.gates.push_back(ov);
                 continue;
             }
+            p.gates.push_back(g);
             switch (g.kind) {
             case BK_MAT1: {
                 t.mat = (uint32_t)(plan.mats.size() / 8) - p.mat_begin;

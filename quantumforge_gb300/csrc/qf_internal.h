@@ -76,7 +76,9 @@ int ensure_pinned(void **ptr, size_t *bytes, size_t need);
 
 // ---- bound gates ------------------------------------------------------------
 // A gate list with parameters resolved to matrices (host, f64).
-enum BKind : uint8_t { BK_MAT1 = 0, BK_CNOT = 1, BK_CZ = 2, BK_SWAP = 3 };
+// BK_OVL marks an adjoint overlap Im<lambda|P_q0 psi> in a backward pass:
+// P = X/Y/Z from `axis`, op_index = the overlap slot.
+enum BKind : uint8_t { BK_MAT1 = 0, BK_CNOT = 1, BK_CZ = 2, BK_SWAP = 3, BK_OVL = 4 };
 
 struct BGate {
     uint8_t kind = BK_MAT1;
@@ -150,7 +152,7 @@ struct Pass {
     uint32_t op_begin = 0;    // into Plan::ops
     uint32_t mat_begin = 0;   // into Plan::mats (matrix index)
     uint64_t resident = 0;    // qubits resident in the tile
-    std::vector<BGate> gates; // the pass's gates in order (after 1q merging), global qubits; forward plans only
+    std::vector<BGate> gates; // the pass's gates in order (after 1q merging, overlaps as BK_OVL), global qubits
 };
 
 // ---- register-tiled passes (complex64) -------------------------------------
@@ -246,11 +248,21 @@ constexpr uint32_t kJitMinQubits = 24;
 bool jit_available();
 int run_plan_jit(qf_sv *sv, const Plan &plan, int wb);
 // Generate the plan's pass kernels and compile them with NVRTC without
-// loading them (no GPU needed); for tests of the code generator.
-int jit_check_compile(const Plan &plan, int wb, std::string *source, std::string *err);
+// loading them (no GPU needed); for tests of the code generator. `dual`
+// generates the backward (psi, lambda) kernels of an adjoint plan.
+int jit_check_compile(const Plan &plan, int wb, std::string *source, std::string *err, bool dual = false);
 // Backward adjoint passes on (psi, lambda); overlap partials per slot are
 // accumulated into d_slot_sums (f64, plan.n_slots entries, not cleared here).
-int run_plan_dual(qf_sv *psi, qf_sv *lambda, const Plan &plan, double *d_slot_sums);
+// Complex64 states use compiled dual passes (by default from kJitMinQubits
+// qubits, or with QF_EXEC_FLAG_JIT; QF_EXEC_FLAG_SMEM_TILES forces the
+// shared-memory kernel).
+int run_plan_dual(qf_sv *psi, qf_sv *lambda, const Plan &plan, double *d_slot_sums, int flags = 0);
+int run_plan_dual_smem(qf_sv *psi, qf_sv *lambda, const Plan &plan, double *d_slot_sums);
+// Compiled backward passes; falls back to run_plan_dual_smem for plans the
+// compiled layout does not cover.
+int run_plan_jit_dual(qf_sv *psi, qf_sv *lambda, const Plan &plan, double *d_slot_sums);
+// slot_sums[s] += sum over b < stride of partials[s * stride + b] (block order)
+int reduce_slots(qf_ctx *ctx, const double *partials, uint32_t stride, uint32_t n_slots, double *d_slot_sums);
 
 // Reductions (results to host unless noted).
 int reduce_norm_sqr(qf_sv *sv, double *out);

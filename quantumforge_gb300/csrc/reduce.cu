@@ -318,6 +318,13 @@ struct PTerm {
     uint64_t z;
     double cre, cim;  // coefficient times i^{ny}
 };
+// a term staged in shared memory with its coefficient in the state's real
+// type: converted once per CTA, not once per amplitude
+template <typename R>
+struct PTermR {
+    uint64_t z;
+    R cre, cim;
+};
 struct PGroup {
     uint64_t x;        // global x-mask
     uint32_t xl;       // the same mask in local tile bits
@@ -344,7 +351,7 @@ __global__ void __launch_bounds__(kRedThreads)
     C *s = reinterpret_cast<C *>(smem);
     uint64_t *hi_off = reinterpret_cast<uint64_t *>(smem + (size_t)T * sizeof(C));
     PGroup *groups = reinterpret_cast<PGroup *>(hi_off + (1u << nhi));
-    PTerm *terms = reinterpret_cast<PTerm *>(groups + pa.n_groups);
+    PTermR<R> *terms = reinterpret_cast<PTermR<R> *>(groups + pa.n_groups);
     __shared__ double red[32];
     for (uint32_t h = threadIdx.x; h < (1u << nhi); h += blockDim.x) {
         uint64_t off = 0;
@@ -353,7 +360,8 @@ __global__ void __launch_bounds__(kRedThreads)
         hi_off[h] = off;
     }
     for (uint32_t g = threadIdx.x; g < pa.n_groups; g += blockDim.x) groups[g] = g_groups[g];
-    for (uint32_t t = threadIdx.x; t < pa.n_terms; t += blockDim.x) terms[t] = g_terms[t];
+    for (uint32_t t = threadIdx.x; t < pa.n_terms; t += blockDim.x)
+        terms[t] = PTermR<R>{g_terms[t].z, (R)g_terms[t].cre, (R)g_terms[t].cim};
     __syncthreads();
     const uint32_t lowmask = (1u << pa.low) - 1;
     double acc_re = 0.0, acc_im = 0.0;
@@ -361,6 +369,7 @@ __global__ void __launch_bounds__(kRedThreads)
         const uint64_t base = deposit(t, pa.nonlocal_mask);
         for (uint32_t j = threadIdx.x; j < T; j += blockDim.x) s[j] = psi[base | hi_off[j >> pa.low] | (j & lowmask)];
         __syncthreads();
+        R tile_re = 0, tile_im = 0;  // this thread's share of the tile, then one f64 add per tile
         for (uint32_t j = threadIdx.x; j < T; j += blockDim.x) {
             const uint64_t gi = base | hi_off[j >> pa.low] | (j & lowmask);
             R er = 0, ei = 0;
@@ -370,10 +379,14 @@ __global__ void __launch_bounds__(kRedThreads)
                 const uint64_t src = pa.mode == 0 ? gi : (gi ^ G.x);
                 R gr = 0, gim = 0;
                 for (uint32_t q = 0; q < G.t_count; ++q) {
-                    const PTerm P = terms[G.t_begin + q];
-                    const R sg = (__popcll(src & P.z) & 1) ? R(-1) : R(1);
-                    gr += sg * (R)P.cre;
-                    gim += sg * (R)P.cim;
+                    const PTermR<R> P = terms[G.t_begin + q];
+                    if (__popcll(src & P.z) & 1) {
+                        gr -= P.cre;
+                        gim -= P.cim;
+                    } else {
+                        gr += P.cre;
+                        gim += P.cim;
+                    }
                 }
                 const C a = s[j ^ G.xl];
                 if (pa.mode == 0) {
@@ -388,8 +401,8 @@ __global__ void __launch_bounds__(kRedThreads)
                 }
             }
             if (pa.mode == 0) {
-                acc_re += (double)er;
-                acc_im += (double)ei;
+                tile_re += er;
+                tile_im += ei;
             } else {
                 if (pa.mode == 2) {
                     const C old = lam[gi];
@@ -399,11 +412,13 @@ __global__ void __launch_bounds__(kRedThreads)
                 lam[gi] = mk(er, ei);
                 if (pa.last) {
                     const C b = s[j];  // conj(psi_j) * lambda_j
-                    acc_re += (double)b.x * (double)er + (double)b.y * (double)ei;
-                    acc_im += (double)b.x * (double)ei - (double)b.y * (double)er;
+                    tile_re += b.x * er + b.y * ei;
+                    tile_im += b.x * ei - b.y * er;
                 }
             }
         }
+        acc_re += (double)tile_re;
+        acc_im += (double)tile_im;
         __syncthreads();
     }
     acc_re = block_sum(acc_re, red);
@@ -418,21 +433,26 @@ __global__ void __launch_bounds__(kRedThreads)
 // into lambda.
 template <typename C>
 __global__ void k_pauli_wide(const C *__restrict__ psi, C *__restrict__ lam, uint64_t n_pairs, uint64_t x, uint32_t xb,
-                             const PTerm *__restrict__ terms, uint32_t nt, uint32_t mode, double *__restrict__ partials) {
+                             const PTerm *__restrict__ g_terms, uint32_t nt, uint32_t mode, double *__restrict__ partials) {
     using R = typename Real<C>::T;
     __shared__ double red[32];
+    extern __shared__ __align__(16) unsigned char wsmem[];
+    PTermR<R> *terms = reinterpret_cast<PTermR<R> *>(wsmem);
+    for (uint32_t t = threadIdx.x; t < nt; t += blockDim.x)
+        terms[t] = PTermR<R>{g_terms[t].z, (R)g_terms[t].cre, (R)g_terms[t].cim};
+    __syncthreads();
     double acc_re = 0.0, acc_im = 0.0;
     for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n_pairs; p += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t i = insert0(p, xb), j = i ^ x;
         R gir = 0, gii = 0, gjr = 0, gji = 0;
         for (uint32_t t = 0; t < nt; ++t) {
-            const PTerm P = terms[t];
+            const PTermR<R> P = terms[t];
             const R si = (__popcll(i & P.z) & 1) ? R(-1) : R(1);
             const R sj = (__popcll(j & P.z) & 1) ? R(-1) : R(1);
-            gir += si * (R)P.cre;
-            gii += si * (R)P.cim;
-            gjr += sj * (R)P.cre;
-            gji += sj * (R)P.cim;
+            gir += si * P.cre;
+            gii += si * P.cim;
+            gjr += sj * P.cre;
+            gji += sj * P.cim;
         }
         const C ai = psi[i], aj = psi[j];
         // G_i a_i and G_j a_j
@@ -577,7 +597,7 @@ int run_pauli(qf_sv *psi, qf_sv *lam, PauliPlan &plan, bool apply, double out[2]
     for (auto &P : plan.tiles) meta += P.groups.size() * sizeof(PGroup) + P.terms.size() * sizeof(PTerm) + 64;
     for (auto &W : plan.wide) meta += W.terms.size() * sizeof(PTerm) + 32;
     QF_TRY(ensure_device(&ctx->ws_plan, &ctx->ws_plan_bytes, meta));
-    const uint32_t grid = (uint32_t)ctx->sm_count * 2;
+    const uint32_t grid = (uint32_t)ctx->sm_count * 8;  // upper bound; tile passes use their occupancy
     const bool need_dot = apply && !plan.wide.empty();
     const size_t launches = plan.tiles.size() + plan.wide.size() + (need_dot ? 1 : 0);
     double *partials;
@@ -597,10 +617,13 @@ int run_pauli(qf_sv *psi, qf_sv *lam, PauliPlan &plan, bool apply, double out[2]
         QF_CUDA(cudaMemcpyAsync(dt, P.terms.data(), P.terms.size() * sizeof(PTerm), cudaMemcpyHostToDevice, ctx->stream));
         off += (P.terms.size() * sizeof(PTerm) + 15) / 16 * 16;
         const size_t smem = ((size_t)1 << P.a.k) * sizeof(C) + (8u << (P.a.k - P.a.low)) + P.groups.size() * sizeof(PGroup) +
-                            P.terms.size() * sizeof(PTerm);
+                            P.terms.size() * sizeof(PTermR<typename Real<C>::T>);
         if (smem > dyn_limit[ctx->device & 63])
             return fail(QF_ERR_UNSUPPORTED_OPERATION, "Pauli pass needs too much shared memory");
-        const uint32_t g = (uint32_t)std::min<uint64_t>(grid, P.a.n_tiles);
+        int per_sm = 0;
+        QF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pauli_pass<C>, kRedThreads, smem));
+        const uint32_t g = (uint32_t)std::min<uint64_t>(std::min<uint64_t>(grid, (uint64_t)std::max(per_sm, 1) * ctx->sm_count),
+                                                        P.a.n_tiles);
         k_pauli_pass<C><<<g, kRedThreads, smem, ctx->stream>>>(static_cast<const C *>(psi->d),
                                                                lam ? static_cast<C *>(lam->d) : nullptr, P.a, dg, dt,
                                                                partials + (size_t)2 * grid * slice);
@@ -614,7 +637,9 @@ int run_pauli(qf_sv *psi, qf_sv *lam, PauliPlan &plan, bool apply, double out[2]
         const uint32_t xb = (uint32_t)__builtin_ctzll(Wg.x);
         const uint64_t pairs = psi->dim / 2;
         const uint32_t g = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(grid, (pairs + kRedThreads - 1) / kRedThreads));
-        k_pauli_wide<C><<<g, kRedThreads, 0, ctx->stream>>>(static_cast<const C *>(psi->d),
+        const size_t wsm = Wg.terms.size() * sizeof(PTermR<typename Real<C>::T>);
+        if (wsm > 48 * 1024) return fail(QF_ERR_UNSUPPORTED_OPERATION, "too many Pauli terms share one x-mask");
+        k_pauli_wide<C><<<g, kRedThreads, wsm, ctx->stream>>>(static_cast<const C *>(psi->d),
                                                             lam ? static_cast<C *>(lam->d) : nullptr, pairs, Wg.x, xb, dt,
                                                             (uint32_t)Wg.terms.size(), apply ? 2u : 0u,
                                                             partials + (size_t)2 * grid * slice);

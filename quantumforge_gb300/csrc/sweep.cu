@@ -563,12 +563,26 @@ int run_plan(qf_sv *sv, const Plan &plan, int flags) {
     return run_plan_smem(sv, plan);
 }
 
-int run_plan_dual(qf_sv *psi, qf_sv *lambda, const Plan &plan, double *d_slot_sums) {
+int run_plan_dual_smem(qf_sv *psi, qf_sv *lambda, const Plan &plan, double *d_slot_sums) {
+    if (psi->dtype == QF_C64) return launch_passes<float2, true>(psi, lambda, plan, d_slot_sums);
+    return launch_passes<double2, true>(psi, lambda, plan, d_slot_sums);
+}
+
+int run_plan_dual(qf_sv *psi, qf_sv *lambda, const Plan &plan, double *d_slot_sums, int flags) {
     if (plan.passes.empty()) return QF_OK;
     if (psi->dtype != lambda->dtype || psi->n != lambda->n)
         return fail(QF_ERR_INCOMPATIBLE_DEVICE_STATE, "device states must have equal dimensions and dtype");
-    if (psi->dtype == QF_C64) return launch_passes<float2, true>(psi, lambda, plan, d_slot_sums);
-    return launch_passes<double2, true>(psi, lambda, plan, d_slot_sums);
+    if (psi->dtype == QF_C64 && !(flags & QF_EXEC_FLAG_SMEM_TILES) && !(flags & QF_EXEC_FLAG_NO_JIT) &&
+        ((flags & QF_EXEC_FLAG_JIT) || psi->n >= kJitMinQubits) && jit_available())
+        return run_plan_jit_dual(psi, lambda, plan, d_slot_sums);
+    return run_plan_dual_smem(psi, lambda, plan, d_slot_sums);
+}
+
+int reduce_slots(qf_ctx *ctx, const double *partials, uint32_t stride, uint32_t n_slots, double *d_slot_sums) {
+    if (!n_slots) return QF_OK;
+    k_reduce_slots<<<(n_slots + 127) / 128, 128, 0, ctx->stream>>>(partials, stride, n_slots, d_slot_sums);
+    QF_CUDA(cudaGetLastError());
+    return QF_OK;
 }
 
 // Bound gate list on a resident state: unfused sweeps or tile passes.

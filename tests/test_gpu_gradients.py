@@ -177,16 +177,35 @@ def test_vqe_adjoint_c128_matches_oracle(backend, n, layers, tile):
         assert np.abs(est.gradient - g_ref).max() < 1e-10, every
 
 
+@pytest.mark.parametrize("compiled", [False, True])
 @pytest.mark.parametrize("n,layers", [(12, 4), (18, 3)])
-def test_vqe_adjoint_c64_error_bound(backend, n, layers):
+def test_vqe_adjoint_c64_error_bound(backend, n, layers, compiled):
+    """compiled: forward and backward passes as generated register-tiled
+    kernels (the default from 24 qubits), else the shared-memory kernels."""
     ops, params, H = W.vqe_xxz(n, layers, seed=n)
     pc = pc_from_ops(ops, params.size)
     e_ref, g_ref = O.adjoint_uncompute(ops, n, params, H.array(), threads=8)
+    eo = {"jit": True} if compiled else {"smem_tiles": True}
     for every in (0, 3 * n):
         est = gradient_with_inputs(pc, GradientOptions(strategy=GradientStrategy.Adjoint), [], params, n, H,
-                                   dtype="c64", checkpoint_every=every, backend=backend)
+                                   dtype="c64", checkpoint_every=every, exec_opts=eo, backend=backend)
         assert abs(est.expectation - e_ref) < 1e-5
         assert np.abs(est.gradient - g_ref).max() < 1e-5
+
+
+@pytest.mark.parametrize("n,layers,every", [(13, 3, 0), (14, 8, 42), (16, 2, 0)])
+def test_vqe_adjoint_compiled_passes_match_shared_memory_passes(backend, n, layers, every):
+    """TFIM (RY.RZ + CZ ring) and XXZ (RX.RY + CNOT ring) circuits: the
+    compiled dual passes give the shared-memory kernels' gradient (c64)."""
+    for wl in (W.vqe_tfim(n, layers, seed=n), W.vqe_xxz(n, layers, seed=n + 1)):
+        ops, params, H = wl
+        pc = pc_from_ops(ops, params.size)
+        res = []
+        for eo in ({"jit": True}, {"smem_tiles": True}):
+            res.append(gradient_with_inputs(pc, GradientOptions(strategy=GradientStrategy.Adjoint), [], params, n, H,
+                                            dtype="c64", checkpoint_every=every, exec_opts=eo, backend=backend))
+        assert abs(res[0].expectation - res[1].expectation) < 2e-6
+        assert np.abs(res[0].gradient - res[1].gradient).max() < 2e-6
 
 
 def test_vqe_adjoint_equals_gpu_parameter_shift_c64(backend):
