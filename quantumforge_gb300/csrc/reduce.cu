@@ -317,6 +317,9 @@ int collapse(qf_sv *sv, uint32_t q, int outcome, double scale) {
 struct PTerm {
     uint64_t z;
     double cre, cim;  // coefficient times i^{ny}
+    uint64_t zo;      // z on the pass's non-resident qubits
+    uint32_t zl;      // z on the resident qubits, in tile-local bits
+    uint32_t q;       // bit r: parity of r & (zl >> 8) (the register part of a thread's amplitudes)
 };
 // a term staged in shared memory with its coefficient in the state's real
 // type: converted once per CTA, not once per amplitude
@@ -325,12 +328,18 @@ struct PTermR {
     uint64_t z;
     R cre, cim;
 };
+template <typename R>
+struct PTermT {
+    uint64_t zo;
+    uint32_t zl, q;
+    R cre, cim;
+};
 struct PGroup {
     uint64_t x;        // global x-mask
     uint32_t xl;       // the same mask in local tile bits
     uint32_t t_begin;  // into the pass's term array
     uint32_t t_count;
-    uint32_t pad;
+    uint32_t real;     // every coefficient of the group is real
 };
 struct PPassArgs {
     uint64_t nonlocal_mask;
@@ -414,6 +423,118 @@ __global__ void __launch_bounds__(kRedThreads)
                     const C b = s[j];  // conj(psi_j) * lambda_j
                     tile_re += b.x * er + b.y * ei;
                     tile_im += b.x * ei - b.y * er;
+                }
+            }
+        }
+        acc_re += (double)tile_re;
+        acc_im += (double)tile_im;
+        __syncthreads();
+    }
+    acc_re = block_sum(acc_re, red);
+    if (threadIdx.x == 0) partials[2 * blockIdx.x] = acc_re;
+    acc_im = block_sum(acc_im, red);
+    if (threadIdx.x == 0) partials[2 * blockIdx.x + 1] = acc_im;
+}
+
+// The same pass for tiles of 256 * NR amplitudes: thread tid owns the
+// amplitudes j = tid + 256 r (r < NR), processed RC at a time. A term's sign
+// at j (or j ^ x) is parity(tid & zl) ^ parity(tile base & zo) ^ parity(x & zl)
+// ^ bit r of the precomputed q, so each term costs one select-add per
+// amplitude and the NR sums are independent.
+template <typename C, int NR, int RC>
+__global__ void __launch_bounds__(kRedThreads)
+    k_pauli_pass_r(const C *__restrict__ psi, C *__restrict__ lam, const PPassArgs pa, const PGroup *__restrict__ g_groups,
+                   const PTerm *__restrict__ g_terms, double *__restrict__ partials) {
+    using R = typename Real<C>::T;
+    extern __shared__ __align__(16) unsigned char smem[];
+    constexpr uint32_t T = 256u * NR;
+    const uint32_t nhi = pa.k - pa.low, tid = threadIdx.x;
+    C *s = reinterpret_cast<C *>(smem);
+    uint64_t *hi_off = reinterpret_cast<uint64_t *>(smem + (size_t)T * sizeof(C));
+    PGroup *groups = reinterpret_cast<PGroup *>(hi_off + (1u << nhi));
+    PTermT<R> *terms = reinterpret_cast<PTermT<R> *>(groups + pa.n_groups);
+    __shared__ double red[32];
+    for (uint32_t h = tid; h < (1u << nhi); h += blockDim.x) {
+        uint64_t off = 0;
+        for (uint32_t r = 0; r < nhi; ++r)
+            if ((h >> r) & 1u) off |= 1ULL << pa.hi_q[r];
+        hi_off[h] = off;
+    }
+    for (uint32_t g = tid; g < pa.n_groups; g += blockDim.x) groups[g] = g_groups[g];
+    for (uint32_t t = tid; t < pa.n_terms; t += blockDim.x) {
+        const PTerm P = g_terms[t];
+        terms[t] = PTermT<R>{P.zo, P.zl, P.q, (R)P.cre, (R)P.cim};
+    }
+    __syncthreads();
+    const uint32_t lowmask = (1u << pa.low) - 1;
+    double acc_re = 0.0, acc_im = 0.0;
+    for (uint64_t t = blockIdx.x; t < pa.n_tiles; t += gridDim.x) {
+        const uint64_t base = deposit(t, pa.nonlocal_mask);
+        for (uint32_t j = tid; j < T; j += blockDim.x) s[j] = psi[base | hi_off[j >> pa.low] | (j & lowmask)];
+        __syncthreads();
+        R tile_re = 0, tile_im = 0;
+#pragma unroll 1
+        for (uint32_t rc = 0; rc < (uint32_t)NR; rc += RC) {
+            R er[RC], ei[RC];
+#pragma unroll
+            for (int r = 0; r < RC; ++r) er[r] = ei[r] = 0;
+            for (uint32_t g = 0; g < pa.n_groups; ++g) {
+                const PGroup G = groups[g];
+                const uint32_t xo = pa.mode == 0 ? 0u : G.xl;  // phase at the source index of the element
+                R gr[RC], gim[RC];
+#pragma unroll
+                for (int r = 0; r < RC; ++r) gr[r] = gim[r] = 0;
+                for (uint32_t q = 0; q < G.t_count; ++q) {
+                    const PTermT<R> P = terms[G.t_begin + q];
+                    const uint32_t par = (__popc((tid ^ xo) & P.zl & 0xFFu) + __popc(xo & P.zl & ~0xFFu) + __popcll(base & P.zo)) & 1u;
+                    const uint32_t m = (P.q >> rc) ^ (0u - par);
+                    if (G.real) {
+#pragma unroll
+                        for (int r = 0; r < RC; ++r) gr[r] += ((m >> r) & 1u) ? -P.cre : P.cre;
+                    } else {
+#pragma unroll
+                        for (int r = 0; r < RC; ++r) {
+                            const bool odd = (m >> r) & 1u;
+                            gr[r] += odd ? -P.cre : P.cre;
+                            gim[r] += odd ? -P.cim : P.cim;
+                        }
+                    }
+                }
+#pragma unroll
+                for (int r = 0; r < RC; ++r) {
+                    const uint32_t j = tid + 256u * (rc + r);
+                    const C a = s[j ^ G.xl];
+                    if (pa.mode == 0) {  // conj(psi_{j^x}) * G * psi_j
+                        const C b = s[j];
+                        const R pr = gr[r] * b.x - gim[r] * b.y, pim = gr[r] * b.y + gim[r] * b.x;
+                        er[r] += a.x * pr + a.y * pim;
+                        ei[r] += a.x * pim - a.y * pr;
+                    } else {
+                        er[r] += gr[r] * a.x - gim[r] * a.y;
+                        ei[r] += gr[r] * a.y + gim[r] * a.x;
+                    }
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < RC; ++r) {
+                const uint32_t j = tid + 256u * (rc + r);
+                if (pa.mode == 0) {
+                    tile_re += er[r];
+                    tile_im += ei[r];
+                } else {
+                    const uint64_t gi = base | hi_off[j >> pa.low] | (j & lowmask);
+                    R vr = er[r], vi = ei[r];
+                    if (pa.mode == 2) {
+                        const C old = lam[gi];
+                        vr += old.x;
+                        vi += old.y;
+                    }
+                    lam[gi] = mk(vr, vi);
+                    if (pa.last) {
+                        const C b = s[j];  // conj(psi_j) * lambda_j
+                        tile_re += b.x * vr + b.y * vi;
+                        tile_im += b.x * vi - b.y * vr;
+                    }
                 }
             }
         }
@@ -523,7 +644,7 @@ int plan_pauli(uint32_t n, int dtype, const qf_pauli_term *terms, uint64_t n_ter
             re = -im;
             im = t2;
         }
-        by_x[P.xmask].push_back(PTerm{P.zmask, re, im});
+        by_x[P.xmask].push_back(PTerm{P.zmask, re, im, 0, 0, 0});
     }
     int k, low;
     default_tiling(n, dtype, 0, &k, &low);
@@ -574,8 +695,19 @@ int plan_pauli(uint32_t n, int dtype, const qf_pauli_term *terms, uint64_t n_ter
                 if ((G.x >> q) & 1ULL) G.xl |= 1u << lbit[q];
             G.t_begin = (uint32_t)P.terms.size();
             G.t_count = (uint32_t)groups[g].second.size();
-            G.pad = 0;
-            P.terms.insert(P.terms.end(), groups[g].second.begin(), groups[g].second.end());
+            G.real = 1;
+            for (PTerm T : groups[g].second) {
+                // the term's z on the resident qubits in tile bits, on the rest as is
+                T.zo = T.z & P.a.nonlocal_mask;
+                T.zl = 0;
+                for (uint32_t q = 0; q < n; ++q)
+                    if (((T.z >> q) & 1ULL) && lbit[q] >= 0) T.zl |= 1u << lbit[q];
+                T.q = 0;
+                const uint32_t nr = P.a.k > 8 ? 1u << (P.a.k - 8) : 1u;
+                for (uint32_t r = 0; r < nr && r < 32; ++r) T.q |= (uint32_t)(__builtin_popcount(r & (T.zl >> 8)) & 1) << r;
+                if (T.cim != 0.0) G.real = 0;
+                P.terms.push_back(T);
+            }
             P.groups.push_back(G);
         }
         P.a.n_groups = (uint32_t)P.groups.size();
@@ -588,11 +720,34 @@ int plan_pauli(uint32_t n, int dtype, const qf_pauli_term *terms, uint64_t n_ter
 // Expectation (apply == false): every launch adds its slice of partials.
 // Apply: lambda = sum of the launches; the energy <psi|lambda> comes from the
 // last tile pass, or from a separate dot product when wide groups follow.
+// the register-blocked pass for a tile of 2^k = 256 * NR amplitudes
+template <typename C>
+struct PauliRKernel {
+    using Fn = void (*)(const C *, C *, const PPassArgs, const PGroup *, const PTerm *, double *);
+    static Fn get(uint32_t k) {
+        switch (k) {
+        case 9: return k_pauli_pass_r<C, 2, 2>;
+        case 10: return k_pauli_pass_r<C, 4, 4>;
+        case 11: return k_pauli_pass_r<C, 8, 8>;
+        case 12: return k_pauli_pass_r<C, 16, 8>;
+        case 13: return k_pauli_pass_r<C, 32, 8>;
+        default: return nullptr;
+        }
+    }
+};
+
 template <typename C>
 int run_pauli(qf_sv *psi, qf_sv *lam, PauliPlan &plan, bool apply, double out[2]) {
     qf_ctx *ctx = psi->ctx;
+    using R = typename Real<C>::T;
     static size_t dyn_limit[64] = {0};
-    if (!dyn_limit[ctx->device & 63]) QF_TRY(allow_max_dynamic_smem(k_pauli_pass<C>, ctx, &dyn_limit[ctx->device & 63]));
+    if (!dyn_limit[ctx->device & 63]) {
+        QF_TRY(allow_max_dynamic_smem(k_pauli_pass<C>, ctx, &dyn_limit[ctx->device & 63]));
+        for (uint32_t k = 9; k <= 13; ++k) {
+            size_t lim = 0;
+            QF_TRY(allow_max_dynamic_smem(PauliRKernel<C>::get(k), ctx, &lim));
+        }
+    }
     size_t meta = 0;
     for (auto &P : plan.tiles) meta += P.groups.size() * sizeof(PGroup) + P.terms.size() * sizeof(PTerm) + 64;
     for (auto &W : plan.wide) meta += W.terms.size() * sizeof(PTerm) + 32;
@@ -616,17 +771,23 @@ int run_pauli(qf_sv *psi, qf_sv *lam, PauliPlan &plan, bool apply, double out[2]
         PTerm *dt = reinterpret_cast<PTerm *>(dmeta + off);
         QF_CUDA(cudaMemcpyAsync(dt, P.terms.data(), P.terms.size() * sizeof(PTerm), cudaMemcpyHostToDevice, ctx->stream));
         off += (P.terms.size() * sizeof(PTerm) + 15) / 16 * 16;
-        const size_t smem = ((size_t)1 << P.a.k) * sizeof(C) + (8u << (P.a.k - P.a.low)) + P.groups.size() * sizeof(PGroup) +
-                            P.terms.size() * sizeof(PTermR<typename Real<C>::T>);
+        auto rk = PauliRKernel<C>::get(P.a.k);
+        const size_t head = ((size_t)1 << P.a.k) * sizeof(C) + (8u << (P.a.k - P.a.low)) + P.groups.size() * sizeof(PGroup);
+        const size_t smem = head + P.terms.size() * (rk ? sizeof(PTermT<R>) : sizeof(PTermR<R>));
         if (smem > dyn_limit[ctx->device & 63])
             return fail(QF_ERR_UNSUPPORTED_OPERATION, "Pauli pass needs too much shared memory");
         int per_sm = 0;
-        QF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pauli_pass<C>, kRedThreads, smem));
+        if (rk) QF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rk, kRedThreads, smem));
+        else QF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pauli_pass<C>, kRedThreads, smem));
         const uint32_t g = (uint32_t)std::min<uint64_t>(std::min<uint64_t>(grid, (uint64_t)std::max(per_sm, 1) * ctx->sm_count),
                                                         P.a.n_tiles);
-        k_pauli_pass<C><<<g, kRedThreads, smem, ctx->stream>>>(static_cast<const C *>(psi->d),
-                                                               lam ? static_cast<C *>(lam->d) : nullptr, P.a, dg, dt,
-                                                               partials + (size_t)2 * grid * slice);
+        if (rk)
+            rk<<<g, kRedThreads, smem, ctx->stream>>>(static_cast<const C *>(psi->d), lam ? static_cast<C *>(lam->d) : nullptr,
+                                                      P.a, dg, dt, partials + (size_t)2 * grid * slice);
+        else
+            k_pauli_pass<C><<<g, kRedThreads, smem, ctx->stream>>>(static_cast<const C *>(psi->d),
+                                                                   lam ? static_cast<C *>(lam->d) : nullptr, P.a, dg, dt,
+                                                                   partials + (size_t)2 * grid * slice);
         QF_CUDA(cudaGetLastError());
     }
     for (size_t w = 0; w < plan.wide.size(); ++w, ++slice) {
