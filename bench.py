@@ -51,6 +51,7 @@ def parse_args():
     ap.add_argument("--no-extra", action="store_true")
     ap.add_argument("--extras", default="vqe24,qaoa4096,shots20,vqe32",
                     help="comma-separated extra workloads to run after the headline")
+    ap.add_argument("--vqe-qubits", type=int, default=32, help="qubits of the checkpointed-adjoint extra (vqe32)")
     return ap.parse_args()
 
 
@@ -332,7 +333,7 @@ def run_ours(args):
         if "shots20" in wanted:
             extra["shots20"] = shots20(backend, cpu=not args.no_cpu_baseline)
         if "vqe32" in wanted:
-            extra["vqe32"] = vqe32_checkpointed(backend)
+            extra["vqe32"] = vqe32_checkpointed(backend, args.vqe_qubits)
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, sample = time_cpu_oracle(n, ops, args.cpu_seconds, threads)
@@ -489,24 +490,21 @@ def vqe_gradients(backend):
             "energy_adjoint": adj.expectation, "energy_shift_run": sh.expectation, "dtype": "complex64"}
 
 
-def vqe32_checkpointed(backend):
-    """32-qubit XXZ-ring VQE (RX.RY per qubit + CNOT ring, 4 layers, 256
-    params, H = sum XX + YY + 0.5 ZZ, 96 terms): complex64 adjoint gradient
-    with a checkpoint per layer (psi, lambda + 3 checkpoints = 160 GiB) and
-    with pure uncompute (64 GiB), both against a complex128 uncompute run
-    (128 GiB) of the same circuit."""
+def vqe32_checkpointed(backend, n=32):
+    """n-qubit (default 32) XXZ-ring VQE (RX.RY per qubit + CNOT ring, 4
+    layers, 8n params, H = sum XX + YY + 0.5 ZZ, 3n terms): complex64 adjoint
+    gradient with a checkpoint per layer (psi, lambda + 3 checkpoints = 160 GiB
+    at 32 qubits) and with pure uncompute (64 GiB), both against a complex128
+    uncompute run (128 GiB) of the same circuit."""
     import numpy as np
 
     import quantumforge_gb300 as qf
     from quantumforge_gb300 import workloads as W
     from quantumforge_gb300.gradients import GradientOptions, GradientStrategy, gradient_with_inputs
 
-    n, layers = 32, 4
+    layers = 4
     ops, params, H = W.vqe_xxz(n, layers, seed=5)
-    pc = qf.ParameterizedCircuit(params.size)
-    for r in ops:
-        pc.operations.append((int(r["kind"]), int(r["gate"]), int(r["q0"]), int(r["q1"]), int(r["param"]),
-                              float(r["theta"])))
+    pc = qf.ParameterizedCircuit.from_ops(ops, params.size)
     opts = GradientOptions(strategy=GradientStrategy.Adjoint)
     runs = {}
     for name, every in (("checkpoint_per_layer", 3 * n), ("uncompute", 0)):

@@ -531,6 +531,15 @@ class ParameterizedCircuit:
     def with_inputs(cls, parameter_count: int, input_count: int) -> "ParameterizedCircuit":
         return cls(parameter_count, input_count)
 
+    @classmethod
+    def from_ops(cls, ops: np.ndarray, parameter_count: int, input_count: int = 0) -> "ParameterizedCircuit":
+        """A parameterized circuit from a ``qf_op`` record array."""
+        c = cls(parameter_count, input_count)
+        for r in ops:
+            c.operations.append((int(r["kind"]), int(r["gate"]), int(r["q0"]), int(r["q1"]), int(r["param"]),
+                                 float(r["theta"])))
+        return c
+
     def parameter_count(self) -> int:
         return self.parameter_count_
 

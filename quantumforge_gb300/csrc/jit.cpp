@@ -521,7 +521,7 @@ struct PassGen {
             s << "extern \"C\" __global__ void __launch_bounds__(" << kThreads << ", 3) p" << index
               << "(float2* __restrict__ A, unsigned long long nt) {\n";
         else
-            s << "extern \"C\" __global__ void __launch_bounds__(" << kThreads << ", 2) p" << index
+            s << "extern \"C\" __global__ void __launch_bounds__(" << kThreads << ", 2) b" << index
               << "(float2* __restrict__ A, float2* __restrict__ B, unsigned long long nt, double* __restrict__ partials, "
                  "unsigned stride) {\n";
         s << "extern __shared__ __align__(16) float2 SB[];\n";
@@ -854,7 +854,8 @@ const char *kPrelude =
 
 const char *kNvrtcOpts[] = {"--gpu-architecture=sm_103a", "--std=c++17", "-default-device", "-lineinfo"};
 
-int compile_module(const std::string &src, int n_kernels, int device, JitModule &out, std::string &err) {
+// kernels p0, p1, ... (forward passes) or b0, b1, ... (backward passes)
+int compile_module(const std::string &src, int n_kernels, int device, JitModule &out, std::string &err, char prefix) {
     Nvrtc &nv = nvrtc();
     if (!nv.ok) {
         err = nv.why;
@@ -887,7 +888,7 @@ int compile_module(const std::string &src, int n_kernels, int device, JitModule 
     }
     out.kernels.resize(n_kernels);
     for (int k = 0; k < n_kernels; ++k) {
-        const std::string nm = "p" + std::to_string(k);
+        const std::string nm = std::string(1, prefix) + std::to_string(k);
         if ((e = cudaLibraryGetKernel(&out.kernels[k], out.lib, nm.c_str())) != cudaSuccess) {
             err = std::string("cudaLibraryGetKernel: ") + cudaGetErrorString(e);
             return QF_ERR_CUDA;
@@ -906,6 +907,7 @@ int compile_module(const std::string &src, int n_kernels, int device, JitModule 
 }
 
 struct ModulePlan {
+    char prefix = 'p';  // kernel names: p<k> forward, b<k> backward
     std::string src;
     std::vector<float> consts;  // interleaved float2
     std::vector<int> pass_index;
@@ -921,6 +923,7 @@ bool gen_modules(const Plan &plan, std::vector<ModulePlan> &mods, bool dual = fa
     size_t pi = 0;
     while (pi < npass) {
         ModulePlan mp;
+        mp.prefix = dual ? 'b' : 'p';
         std::ostringstream body;
         g.consts.clear();
         int local = 0;
@@ -1008,7 +1011,8 @@ int fetch_modules(qf_ctx *ctx, const std::vector<ModulePlan> &mods, std::vector<
         built[k] = std::make_shared<JitModule>();
         th.emplace_back([&, k, dev] {
             cudaSetDevice(dev);
-            st[k] = compile_module(mods[todo[k]].src, (int)mods[todo[k]].pass_index.size(), dev, *built[k], errs[k]);
+            st[k] = compile_module(mods[todo[k]].src, (int)mods[todo[k]].pass_index.size(), dev, *built[k], errs[k],
+                                   mods[todo[k]].prefix);
         });
     }
     for (auto &t : th) t.join();
