@@ -307,7 +307,8 @@ def test_register_tiled_mixed_circuits(backend, n, seed, tile):
     assert close(sv.amplitudes(), expected, C64_TOL)
 
 
-@pytest.mark.parametrize("n,seed,kinds", [(14, 3, True), (17, 4, False), (20, 9, False)])
+@pytest.mark.parametrize("n,seed,kinds", [(14, 3, True), (17, 4, False), (20, 9, False), (13, 21, True), (15, 22, True),
+                                          (16, 23, True), (18, 24, True), (19, 25, False)])
 def test_compiled_passes_match_oracle(backend, n, seed, kinds):
     """Passes compiled by the pass compiler (NVRTC) against the oracle, and
     a second run of the same structure with new angles (cached kernels)."""
