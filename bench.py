@@ -382,10 +382,17 @@ def shots20(backend, cpu: bool):
     zs = sv.expectation_z_all()
     t_state = time.perf_counter() - t0
     t0 = time.perf_counter()
+    circ.run_shots_packed(n, shots, seed, dtype="c128", backend=backend, tie_eps=1e-12)
+    t_engine = time.perf_counter() - t0
+    t0 = time.perf_counter()
     res = circ.run_shots(n, shots, seed, dtype="c128", backend=backend, tie_eps=1e-12)
     t_shots = time.perf_counter() - t0
     out = {"qubits": n, "gates": len(ops), "shots": shots, "seed": seed, "run_probs_z_s": t_state,
-           "shots_call_s": t_shots, "shots_per_s": shots / t_shots, "ties": res.ties, "distinct_outcomes": len(res.counts)}
+           "engine_call_s": t_engine, "engine_shots_per_s": shots / t_engine,
+           "api_call_s": t_shots, "api_shots_per_s": shots / t_shots,
+           "api": "engine: qf_run_shots (simulate, sample, packed outcomes to host); api: Circuit.run_shots incl. the "
+                  "counts map keyed by bit tuples",
+           "ties": res.ties, "distinct_outcomes": len(res.counts)}
     exp_packed, width = O.run_shots(mops, n, shots, seed, threads=os.cpu_count() or 1)
     out["counts_bit_exact_vs_oracle"] = res.counts == O.counts(exp_packed, width)
     a = O.run(ops, n, threads=os.cpu_count() or 1)

@@ -434,9 +434,13 @@ class ShotResult:
 
     @staticmethod
     def from_packed(packed: np.ndarray, width: int, ties: int = 0) -> "ShotResult":
-        vals, cnts = np.unique(packed, return_counts=True)
-        counts = {tuple(int((int(v) >> b) & 1) for b in range(width)): int(c) for v, c in zip(vals, cnts)}
-        return ShotResult(int(packed.size), dict(sorted(counts.items())), ties)
+        """Counts keyed by LSB-first bit tuples, in the BTreeMap<Vec<u8>, usize>
+        order of the reference (lexicographic from classical bit 0)."""
+        vals, cnts = np.unique(np.asarray(packed, dtype=np.uint64), return_counts=True)
+        bits = ((vals[:, None] >> np.arange(width, dtype=np.uint64)[None, :]) & np.uint64(1)).astype(np.uint8)
+        order = np.lexsort(bits.T[::-1]) if width else np.arange(vals.size)
+        counts = dict(zip(map(tuple, bits[order].tolist()), cnts[order].tolist()))
+        return ShotResult(int(np.asarray(packed).size), counts, ties)
 
 
 class Circuit:
@@ -496,6 +500,12 @@ class Circuit:
     def run_shots(self, initial_state, shots: int, seed: int, dtype="c128", backend: CudaBackend | None = None,
                   tie_eps: float = 0.0, exec_opts=None) -> ShotResult:
         """Circuit::run_shots (src/lib.rs:2822-2916) for terminal measurements."""
+        return ShotResult.from_packed(*self.run_shots_packed(initial_state, shots, seed, dtype, backend, tie_eps, exec_opts))
+
+    def run_shots_packed(self, initial_state, shots: int, seed: int, dtype="c128", backend: CudaBackend | None = None,
+                         tie_eps: float = 0.0, exec_opts=None):
+        """The engine's qf_run_shots result: (packed outcomes, one u64 per shot
+        with classical bit c at bit c; register width; ties)."""
         backend = backend or default_backend()
         if isinstance(initial_state, StateVector):
             amps = initial_state.amplitudes()
@@ -512,7 +522,7 @@ class Circuit:
         ties = C.c_uint64()
         check(load().qf_run_shots(backend.handle, n, _dtype_code(dtype), ptr(ops), len(ops), ptr(src), int(shots), int(seed),
                                   float(tie_eps), ptr(out), C.byref(width), C.byref(ties), _exec(exec_opts)))
-        return ShotResult.from_packed(out[: int(shots)], width.value, ties.value)
+        return out[: int(shots)], width.value, ties.value
 
 
 class ParameterizedCircuit:
