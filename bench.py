@@ -52,6 +52,7 @@ def parse_args():
     ap.add_argument("--extras", default="vqe24,qaoa4096,shots20,vqe32",
                     help="comma-separated extra workloads to run after the headline")
     ap.add_argument("--vqe-qubits", type=int, default=32, help="qubits of the checkpointed-adjoint extra (vqe32)")
+    ap.add_argument("--qaoa-instances", type=int, default=4096, help="instances of the batched QAOA extra (qaoa4096)")
     return ap.parse_args()
 
 
@@ -329,7 +330,7 @@ def run_ours(args):
         if "vqe24" in wanted:
             extra["vqe24"] = vqe_gradients(backend)
         if "qaoa4096" in wanted:
-            extra["qaoa4096"] = qaoa_batch(backend, cpu=not args.no_cpu_baseline)
+            extra["qaoa4096"] = qaoa_batch(backend, cpu=not args.no_cpu_baseline, count=args.qaoa_instances)
         if "shots20" in wanted:
             extra["shots20"] = shots20(backend, cpu=not args.no_cpu_baseline)
         if "vqe32" in wanted:
@@ -408,16 +409,17 @@ def shots20(backend, cpu: bool):
     return out
 
 
-def qaoa_batch(backend, cpu: bool):
-    """4096 random 3-regular MaxCut instances, n uniform in {12..20}, p = 4:
-    cost and 8-parameter adjoint gradient per instance in one persistent
-    launch replayed from a CUDA graph, tiles autotuned per n."""
+def qaoa_batch(backend, cpu: bool, count: int = 4096):
+    """`count` (4096) random 3-regular MaxCut instances, n uniform in
+    {12..20}, p = 4: cost and 8-parameter adjoint gradient per instance,
+    replayed from a CUDA graph (batched tile passes per qubit count above 12
+    qubits, one CTA per instance up to 12 qubits, tiles autotuned there)."""
     import numpy as np
 
     from quantumforge_gb300 import workloads as W
     from quantumforge_gb300.qaoa import QaoaBatch, autotune_tiles
 
-    problems, gam, bet = W.qaoa_batch_problems(4096)
+    problems, gam, bet = W.qaoa_batch_problems(count)
     tiles = autotune_tiles(problems, 4, candidates=(9, 10, 11, 12), reps=1, backend=backend)
     batch = QaoaBatch(problems, 4, tile_qubits=tiles, backend=backend, use_graph=True)
     batch.run(gam, bet)

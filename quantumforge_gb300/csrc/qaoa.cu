@@ -38,6 +38,8 @@ struct QDesc {
     uint64_t psi;       // float2 offset of psi in the arena
     uint64_t lam;       // float2 offset of lambda
     uint64_t cost;      // byte offset of the C(x) table in the cost arena
+    uint64_t ptab;      // batched instances: float2 offset of the per-layer phase tables
+    uint64_t part;      // batched instances: double offset of the per-tile partial sums
     uint32_t n;
     uint32_t k;         // tile qubits
     uint32_t e_begin;
@@ -281,6 +283,359 @@ __global__ void __launch_bounds__(kQThreads)
     }
 }
 
+// ---- batched passes for instances of 13..24 qubits ---------------------------
+// All instances of one qubit count n are advanced together, one tile pass per
+// launch over every (instance, tile) pair, so a pass streams at the rate of the
+// whole GPU. Tiles hold 2^12 amplitudes: pass A the low 12 qubits (contiguous;
+// cost phase and mixer on qubits 0..11), pass B the high n-12 qubits plus the
+// low L = 24-n (mixer on qubits 12..n-1). A forward layer is A then B; the last
+// B also writes lambda = C psi and the energy. A reverse layer undoes B then A
+// on psi and lambda, with the dE/dbeta terms of both and the dE/dgamma term
+// (after the mixer is undone) written per (instance, tile) and summed in tile
+// order by k_qaoa_reduce.
+constexpr int kQBTile = 12;
+constexpr uint32_t kQBT = 1u << kQBTile;
+
+struct QBArgs {
+    uint32_t r0, m;  // descriptor rows [r0, r0 + m): one qubit count
+    uint32_t n, L;   // qubits; low bits of a pass-B tile (24 - n)
+    uint32_t p, layer;
+    uint64_t tiles;  // tiles per instance: 2^(n-12)
+};
+
+// part slots per tile: 0 energy, 1+l dE/dbeta (pass A), 1+p+l dE/dbeta
+// (pass B), 1+2p+l dE/dgamma
+__device__ __forceinline__ uint64_t qb_index(bool pass_b, uint32_t L, uint64_t t, uint32_t j) {
+    if (!pass_b) return (t << kQBTile) | j;
+    return (uint64_t)(j & ((1u << L) - 1)) | (t << L) | ((uint64_t)(j >> L) << kQBTile);
+}
+
+__device__ __forceinline__ void qb_cp16(void *dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void qb_cp_wait() {
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+// Shared-memory position of tile amplitude j: bits 1..3 XOR bits 4..6, so
+// that the mixer round on tile bits 0..3 (16-byte pair accesses, 8 lanes per
+// phase) and the rounds on higher bits (8-byte accesses, 16 lanes per phase)
+// are bank-conflict free; bit 0 is kept, so 16-byte pairs stay whole.
+__device__ __forceinline__ uint32_t qb_phys(uint32_t j) { return j ^ (((j >> 4) & 7u) << 1); }
+// a tile of 2^12 amplitudes into shared memory: 16-byte copies of amplitude
+// pairs (pass B with L = 0 has no adjacent pair: plain loads)
+__device__ __forceinline__ void qb_load(float2 *dst, const float2 *src, bool pass_b, uint32_t L, uint64_t t) {
+    if (pass_b && L == 0) {
+        for (uint32_t j = threadIdx.x; j < kQBT; j += blockDim.x) dst[qb_phys(j)] = src[qb_index(true, 0, t, j)];
+        return;
+    }
+    for (uint32_t c = threadIdx.x; c < kQBT / 2; c += blockDim.x)
+        qb_cp16(dst + qb_phys(2 * c), src + qb_index(pass_b, L, t, 2 * c));
+}
+// the 16 amplitudes base | (i << b0) of a mixer round, and back
+__device__ __forceinline__ void qb_read(const float2 *tile, uint32_t base, uint32_t b0, float2 (&v)[16]) {
+    if (b0 == 0) {
+#pragma unroll
+        for (uint32_t i = 0; i < 16; i += 2) {
+            const float4 t = *reinterpret_cast<const float4 *>(tile + qb_phys(base | i));
+            v[i] = make_float2(t.x, t.y);
+            v[i + 1] = make_float2(t.z, t.w);
+        }
+    } else {
+#pragma unroll
+        for (uint32_t i = 0; i < 16; ++i) v[i] = tile[qb_phys(base | (i << b0))];
+    }
+}
+__device__ __forceinline__ void qb_write(float2 *tile, uint32_t base, uint32_t b0, const float2 (&v)[16]) {
+    if (b0 == 0) {
+#pragma unroll
+        for (uint32_t i = 0; i < 16; i += 2)
+            *reinterpret_cast<float4 *>(tile + qb_phys(base | i)) = make_float4(v[i].x, v[i].y, v[i + 1].x, v[i + 1].y);
+    } else {
+#pragma unroll
+        for (uint32_t i = 0; i < 16; ++i) tile[qb_phys(base | (i << b0))] = v[i];
+    }
+}
+// the cost bytes of a pass-A tile (contiguous)
+__device__ __forceinline__ void qb_load_cost(uint8_t *dst, const uint8_t *src, uint64_t t) {
+    for (uint32_t c = threadIdx.x; c < kQBT / 16; c += blockDim.x) qb_cp16(dst + 16 * c, src + (t << kQBTile) + 16 * c);
+}
+
+// C(x) for every amplitude of every instance of the class; per-layer phases
+// exp(-i gamma (W - 2c)) and mixer (cos beta, sin beta) as the per-instance
+// kernel computes them
+__global__ void __launch_bounds__(kQThreads)
+    k_qaoa_costs(const QBArgs a, const QDesc *__restrict__ desc, const uint64_t *__restrict__ emasks, uint8_t *__restrict__ costs) {
+    __shared__ uint64_t em[kQMaxEdges];
+    const uint64_t items = (uint64_t)a.m * a.tiles;
+    for (uint64_t w = blockIdx.x; w < items; w += gridDim.x) {
+        const uint32_t ci = (uint32_t)(w / a.tiles);
+        const uint64_t t = w % a.tiles;
+        const QDesc D = desc[a.r0 + ci];
+        __syncthreads();
+        for (uint32_t e = threadIdx.x; e < D.e_count; e += blockDim.x) em[e] = emasks[D.e_begin + e];
+        __syncthreads();
+        uint8_t *cost = costs + D.cost;
+        for (uint32_t j = threadIdx.x; j < kQBT; j += blockDim.x) {
+            const uint64_t x = (t << kQBTile) | j;
+            cost[x] = (uint8_t)cut_value(x, em, D.e_count);
+        }
+    }
+}
+
+__global__ void k_qaoa_tables(const QDesc *__restrict__ desc, uint32_t rows, const double *__restrict__ gammas,
+                              const double *__restrict__ betas, uint32_t p, float2 *__restrict__ ptab, float2 *__restrict__ mtab) {
+    const uint32_t span = kQMaxEdges + 1;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < (uint64_t)rows * p * span;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t r = (uint32_t)(i / ((uint64_t)p * span)), l = (uint32_t)((i / span) % p), c = (uint32_t)(i % span);
+        const QDesc D = desc[r];
+        const double gm = gammas[(size_t)D.out * p + l];
+        if (c <= D.e_count) {
+            const double ang = -gm * ((double)D.e_count - 2.0 * (double)c);
+            ptab[D.ptab + (uint64_t)l * span + c] = make_float2((float)cos(ang), (float)sin(ang));
+        }
+        if (c == 0) {
+            const double bt = betas[(size_t)D.out * p + l];
+            mtab[(uint64_t)r * p + l] = make_float2((float)cos(bt), (float)sin(bt));
+        }
+    }
+}
+
+// Mixer rounds of a batched pass: a round applies exp(-i beta X) to the bits
+// of a 4-bit window [b0, b0 + 4) selected by `mask`, with the 16 amplitudes
+// j = base(tid) | (i << b0) of each thread in registers; pass A has windows
+// 0, 4, 8, pass B the windows at and above its first high bit L (top first).
+struct QBRounds {
+    uint32_t n;
+    uint32_t b0[3];
+    uint32_t mask[3];
+};
+__device__ __forceinline__ QBRounds qb_rounds(bool pass_b, uint32_t L) {
+    QBRounds R;
+    R.n = 0;
+    if (!pass_b) {
+        for (uint32_t w = 0; w < 3; ++w) {
+            R.b0[R.n] = 4 * w;
+            R.mask[R.n++] = 0xFu;
+        }
+    } else {
+        for (int w = 2; w >= 0; --w) {
+            const uint32_t b0 = 4u * (uint32_t)w;
+            if (b0 + 4 <= L) break;
+            uint32_t m = 0;
+            for (uint32_t b = 0; b < 4; ++b)
+                if (b0 + b >= L) m |= 1u << b;
+            R.b0[R.n] = b0;
+            R.mask[R.n++] = m;
+        }
+    }
+    return R;
+}
+__device__ __forceinline__ uint32_t qb_base(uint32_t b0) {  // thread's group with the window bits cleared
+    const uint32_t g = threadIdx.x;
+    return (g & ((1u << b0) - 1)) | ((g >> b0) << (b0 + 4));
+}
+// exp(-i beta X) (c = cos, s = sin) on the window bits in `mask`; dual: the
+// same on l, with 2 Im<l|X_b|a> before each gate added to gsum
+template <bool DUAL>
+__device__ __forceinline__ void qb_mix(float2 (&a)[16], float2 (&l)[16], uint32_t mask, float c, float s, float &gsum) {
+#pragma unroll
+    for (uint32_t b = 0; b < 4; ++b) {
+        if (!((mask >> b) & 1u)) continue;
+#pragma unroll
+        for (uint32_t i = 0; i < 16; ++i) {
+            if (i & (1u << b)) continue;
+            const uint32_t j = i | (1u << b);
+            if (DUAL) gsum += (l[i].x * a[j].y - l[i].y * a[j].x) + (l[j].x * a[i].y - l[j].y * a[i].x);
+            const float2 x = a[i], y = a[j];
+            a[i] = make_float2(c * x.x + s * y.y, c * x.y - s * y.x);
+            a[j] = make_float2(c * y.x + s * x.y, c * y.y - s * x.x);
+            if (DUAL) {
+                const float2 u = l[i], v = l[j];
+                l[i] = make_float2(c * u.x + s * v.y, c * u.y - s * v.x);
+                l[j] = make_float2(c * v.x + s * u.y, c * v.y - s * u.x);
+            }
+        }
+    }
+}
+__device__ __forceinline__ void qb_issue(bool dual, bool pass_b, bool with_cost, const QBArgs &a, const QDesc *desc,
+                                         float2 *arena, const uint8_t *costs, uint64_t w, float2 *tp, float2 *tl,
+                                         uint8_t *tc) {
+    const uint32_t ci = (uint32_t)(w / a.tiles);
+    const uint64_t t = w % a.tiles;
+    const QDesc D = desc[a.r0 + ci];
+    const bool load_psi = pass_b || dual || a.layer > 0;
+    if (load_psi) qb_load(tp, arena + D.psi, pass_b, a.L, t);
+    if (dual) qb_load(tl, arena + D.lam, pass_b, a.L, t);
+    if (with_cost) qb_load_cost(tc, costs + D.cost, t);
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+
+// forward pass: [pass A: cost phase] + mixer; the last pass B of the last
+// layer also writes lambda = C psi and the per-tile energy
+template <bool PASS_B>
+__global__ void __launch_bounds__(kQThreads)
+    k_qaoa_fwd(const QBArgs a, const QDesc *__restrict__ desc, float2 *__restrict__ arena, const uint8_t *__restrict__ costs,
+               const float2 *__restrict__ ptab, const float2 *__restrict__ mtab, double *__restrict__ part) {
+    extern __shared__ __align__(16) float2 qb_tile[];
+    uint8_t *tc = reinterpret_cast<uint8_t *>(qb_tile + kQBT);
+    __shared__ double red[32];
+    const uint64_t items = (uint64_t)a.m * a.tiles;
+    const bool last = PASS_B && a.layer + 1 == a.p;
+    const QBRounds R = qb_rounds(PASS_B, a.L);
+    const float amp0 = (float)(1.0 / sqrt((double)(1ULL << a.n)));
+    uint64_t w = blockIdx.x;
+    if (w < items) qb_issue(false, PASS_B, !PASS_B, a, desc, arena, costs, w, qb_tile, nullptr, tc);
+    for (; w < items; w += gridDim.x) {
+        const uint32_t ci = (uint32_t)(w / a.tiles);
+        const uint64_t t = w % a.tiles;
+        const uint32_t r = a.r0 + ci;
+        const QDesc D = desc[r];
+        const float2 *ph = ptab + D.ptab + (uint64_t)a.layer * (kQMaxEdges + 1);
+        const float2 cs = mtab[(uint64_t)r * a.p + a.layer];
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        __syncthreads();
+        float2 v[16], dummy[16];
+        float gs = 0.f;
+        uint32_t base = 0;
+        for (uint32_t k = 0; k < R.n; ++k) {
+            base = qb_base(R.b0[k]);
+            if (!PASS_B && k == 0) {  // the cost layer (layer 0 starts from H on every qubit of |0>); window 0..3
+                if (a.layer > 0) qb_read(qb_tile, base, 0, v);
+                const uint4 cb = *reinterpret_cast<const uint4 *>(tc + base);
+                const uint32_t cw[4] = {cb.x, cb.y, cb.z, cb.w};
+#pragma unroll
+                for (uint32_t i = 0; i < 16; ++i)
+                    v[i] = cm(a.layer == 0 ? make_float2(amp0, 0.f) : v[i], ph[(cw[i >> 2] >> (8 * (i & 3))) & 0xFFu]);
+            } else {
+                qb_read(qb_tile, base, R.b0[k], v);
+            }
+            qb_mix<false>(v, dummy, R.mask[k], cs.x, cs.y, gs);
+            if (k + 1 < R.n) {
+                qb_write(qb_tile, base, R.b0[k], v);
+                __syncthreads();
+            }
+        }
+        const uint32_t b0 = R.b0[R.n - 1];
+        __syncthreads();  // every read of this tile is done: stream the next one in
+        if (w + gridDim.x < items) qb_issue(false, PASS_B, !PASS_B, a, desc, arena, costs, w + gridDim.x, qb_tile, nullptr, tc);
+        float2 *psi = arena + D.psi;
+        float e = 0.f;
+#pragma unroll
+        for (uint32_t i = 0; i < 16; ++i) {
+            const uint64_t x = qb_index(PASS_B, a.L, t, base | (i << b0));
+            psi[x] = v[i];
+            if (last) {  // lambda = C psi and <C>
+                const float cv = (float)costs[D.cost + x];
+                arena[D.lam + x] = make_float2(cv * v[i].x, cv * v[i].y);
+                e += cv * (v[i].x * v[i].x + v[i].y * v[i].y);
+            }
+        }
+        if (last) {
+            const double et = block_sum((double)e, red);
+            if (threadIdx.x == 0) part[D.part + t] = et;
+        }
+    }
+}
+
+// reverse pass: the inverse mixer on psi and lambda with the dE/dbeta terms;
+// pass A then the cost layer's dE/dgamma term and the inverse phase
+template <bool PASS_B>
+__global__ void __launch_bounds__(kQThreads)
+    k_qaoa_rev(const QBArgs a, const QDesc *__restrict__ desc, float2 *__restrict__ arena, const uint8_t *__restrict__ costs,
+               const float2 *__restrict__ ptab, const float2 *__restrict__ mtab, double *__restrict__ part) {
+    extern __shared__ __align__(16) float2 qb_tile[];
+    float2 *tp = qb_tile, *tl = qb_tile + kQBT;
+    uint8_t *tc = reinterpret_cast<uint8_t *>(qb_tile + 2 * kQBT);
+    __shared__ double red[32];
+    const uint64_t items = (uint64_t)a.m * a.tiles;
+    const QBRounds R = qb_rounds(PASS_B, a.L);
+    uint64_t w = blockIdx.x;
+    if (w < items) qb_issue(true, PASS_B, !PASS_B, a, desc, arena, costs, w, tp, tl, tc);
+    for (; w < items; w += gridDim.x) {
+        const uint32_t ci = (uint32_t)(w / a.tiles);
+        const uint64_t t = w % a.tiles;
+        const uint32_t r = a.r0 + ci;
+        const QDesc D = desc[r];
+        const float2 *ph = ptab + D.ptab + (uint64_t)a.layer * (kQMaxEdges + 1);
+        const float2 cs = mtab[(uint64_t)r * a.p + a.layer];
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        __syncthreads();
+        float2 v[16], l[16];
+        uint8_t cv[16];
+        float gb = 0.f;
+        uint32_t base = 0;
+        for (uint32_t k = 0; k < R.n; ++k) {
+            base = qb_base(R.b0[k]);
+            qb_read(tp, base, R.b0[k], v);
+            qb_read(tl, base, R.b0[k], l);
+            if (!PASS_B && k + 1 == R.n)
+#pragma unroll
+                for (uint32_t i = 0; i < 16; ++i) cv[i] = tc[base | (i << R.b0[k])];
+            qb_mix<true>(v, l, R.mask[k], cs.x, -cs.y, gb);  // the inverse mixer, gradient before each gate
+            if (k + 1 < R.n) {
+                qb_write(tp, base, R.b0[k], v);
+                qb_write(tl, base, R.b0[k], l);
+                __syncthreads();
+            }
+        }
+        const uint32_t b0 = R.b0[R.n - 1];
+        __syncthreads();  // every read of this tile is done: stream the next one in
+        if (w + gridDim.x < items) qb_issue(true, PASS_B, !PASS_B, a, desc, arena, costs, w + gridDim.x, tp, tl, tc);
+        float2 *psi = arena + D.psi, *lam = arena + D.lam;
+        const float W = (float)D.e_count;
+        float gg = 0.f;
+#pragma unroll
+        for (uint32_t i = 0; i < 16; ++i) {
+            const uint64_t x = qb_index(PASS_B, a.L, t, base | (i << b0));
+            float2 pv = v[i], lv = l[i];
+            if (!PASS_B) {  // the cost layer: its gradient term, then undo its phase
+                const float2 f = ph[cv[i]];
+                gg += (W - 2.f * (float)cv[i]) * (lv.x * pv.y - lv.y * pv.x);
+                pv = cmc(pv, f);
+                lv = cmc(lv, f);
+            }
+            psi[x] = pv;
+            lam[x] = lv;
+        }
+        const double gbt = block_sum((double)gb, red);
+        if (threadIdx.x == 0) part[D.part + (uint64_t)(1 + (PASS_B ? a.p : 0) + a.layer) * a.tiles + t] = gbt;
+        if (!PASS_B) {
+            const double ggt = block_sum((double)gg, red);
+            if (threadIdx.x == 0) part[D.part + (uint64_t)(1 + 2 * a.p + a.layer) * a.tiles + t] = ggt;
+        }
+    }
+}
+
+// energy and gradients of the batched instances: per-tile partials in order
+__global__ void k_qaoa_reduce(const QBArgs a, const QDesc *__restrict__ desc, const double *__restrict__ part,
+                              double *__restrict__ out_cost, double *__restrict__ out_grad) {
+    const uint32_t slots = 1 + 2 * a.p;  // energy, dE/dgamma_l, dE/dbeta_l
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < (uint64_t)a.m * slots;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t ci = (uint32_t)(i / slots), sl = (uint32_t)(i % slots);
+        const QDesc D = desc[a.r0 + ci];
+        const double *P = part + D.part;
+        double v = 0.0;
+        if (sl == 0) {
+            for (uint64_t t = 0; t < a.tiles; ++t) v += P[t];
+            out_cost[D.out] = v;
+        } else if (sl <= a.p) {  // dE/dgamma_l
+            const uint32_t l = sl - 1;
+            for (uint64_t t = 0; t < a.tiles; ++t) v += P[(uint64_t)(1 + 2 * a.p + l) * a.tiles + t];
+            out_grad[(size_t)D.out * 2 * a.p + l] = 2.0 * v;
+        } else {  // dE/dbeta_l: pass A then pass B terms
+            const uint32_t l = sl - 1 - a.p;
+            double vb = 0.0;
+            for (uint64_t t = 0; t < a.tiles; ++t) v += P[(uint64_t)(1 + l) * a.tiles + t];
+            for (uint64_t t = 0; t < a.tiles; ++t) vb += P[(uint64_t)(1 + a.p + l) * a.tiles + t];
+            out_grad[(size_t)D.out * 2 * a.p + a.p + l] = 2.0 * (v + vb);
+        }
+    }
+}
+
 }  // namespace
 
 struct QaoaGraph {
@@ -320,16 +675,29 @@ extern "C" int qf_qaoa_maxcut_batch(qf_ctx *ctx, const qf_qaoa_instance *inst, u
     for (uint64_t i = 0; i < n_inst * p; ++i)
         if (!std::isfinite(gammas[i]) || !std::isfinite(betas[i])) return fail(QF_ERR_NON_FINITE_PARAMETER, "circuit parameters must be finite");
     std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return inst[a].qubits > inst[b].qubits; });
-    uint64_t amp_off = 0, cost_off = 0;
+    // rows [0, r_small): batched passes per qubit count (13..24 qubits); the
+    // rest: one CTA per instance
+    uint64_t amp_off = 0, cost_off = 0, ptab_off = 0, part_off = 0;
+    uint32_t r_small = 0;
     for (uint64_t r = 0; r < n_inst; ++r) {
         const qf_qaoa_instance &I = inst[order[r]];
         QDesc &D = desc[r];
+        std::memset(&D, 0, sizeof D);
         D.n = I.qubits;
-        const int kt = I.tile_qubits ? (int)I.tile_qubits : (opts && opts->tile_qubits[I.qubits] ? opts->tile_qubits[I.qubits] : 10);
-        D.k = (uint32_t)std::max(4, std::min(kQMaxTile, kt));
-        if (D.n > D.k && D.n - D.k > D.k - 1) D.k = (D.n + 1) / 2 + 1;  // pass B needs n-k+1 <= k
-        D.k = std::min<uint32_t>(D.k, (uint32_t)kQMaxTile);
-        if (D.n > D.k && D.n - D.k + 1 > D.k) return fail(QF_ERR_UNSUPPORTED_OPERATION, "instance of %u qubits needs tiles above %d qubits", D.n, kQMaxTile);
+        if (D.n > 24) return fail(QF_ERR_UNSUPPORTED_OPERATION, "batched QAOA supports up to 24 qubits, got %u", D.n);
+        if (D.n > (uint32_t)kQBTile) {
+            r_small = (uint32_t)r + 1;
+            D.k = kQBTile;
+            D.ptab = ptab_off;
+            ptab_off += (uint64_t)p * (kQMaxEdges + 1);
+            D.part = part_off;
+            part_off += (uint64_t)(1 + 3 * p) << (D.n - kQBTile);
+        } else {
+            const int kt = I.tile_qubits ? (int)I.tile_qubits : (opts && opts->tile_qubits[I.qubits] ? opts->tile_qubits[I.qubits] : 10);
+            D.k = (uint32_t)std::max(4, std::min(kQMaxTile, kt));
+            if (D.n > D.k && D.n - D.k > D.k - 1) D.k = (D.n + 1) / 2 + 1;  // pass B needs n-k+1 <= k
+            D.k = std::min<uint32_t>(D.k, (uint32_t)kQMaxTile);
+        }
         D.e_begin = I.edge_begin;
         D.e_count = I.edge_count;
         D.out = order[r];
@@ -348,7 +716,9 @@ extern "C" int qf_qaoa_maxcut_batch(qf_ctx *ctx, const qf_qaoa_instance *inst, u
     const size_t b_desc = al(sizeof(QDesc) * n_inst), b_mask = al(8 * std::max<uint64_t>(1, n_edges));
     const size_t b_par = al(8 * n_inst * p), b_cost = al(8 * n_inst), b_grad = al(16 * n_inst * p), b_cnt = 256;
     const size_t b_arena = al(8 * amp_off), b_costs = al(cost_off);
-    const size_t total = b_desc + b_mask + 2 * b_par + b_cost + b_grad + b_cnt + b_arena + b_costs;
+    const size_t b_ptab = al(8 * std::max<uint64_t>(1, ptab_off)), b_mtab = al(8 * std::max<uint64_t>(1, (uint64_t)r_small * p));
+    const size_t b_part = al(8 * std::max<uint64_t>(1, part_off));
+    const size_t total = b_desc + b_mask + 2 * b_par + b_cost + b_grad + b_cnt + b_arena + b_costs + b_ptab + b_mtab + b_part;
     QF_TRY(ensure_device(&ctx->ws_tree, &ctx->ws_tree_bytes, total));
     unsigned char *w = static_cast<unsigned char *>(ctx->ws_tree);
     QDesc *d_desc = reinterpret_cast<QDesc *>(w);
@@ -360,6 +730,10 @@ extern "C" int qf_qaoa_maxcut_batch(qf_ctx *ctx, const qf_qaoa_instance *inst, u
     unsigned *d_cnt = reinterpret_cast<unsigned *>(w + b_desc + b_mask + 2 * b_par + b_cost + b_grad);
     float2 *d_arena = reinterpret_cast<float2 *>(w + b_desc + b_mask + 2 * b_par + b_cost + b_grad + b_cnt);
     uint8_t *d_costs = reinterpret_cast<uint8_t *>(w + b_desc + b_mask + 2 * b_par + b_cost + b_grad + b_cnt + b_arena);
+    unsigned char *w2 = w + b_desc + b_mask + 2 * b_par + b_cost + b_grad + b_cnt + b_arena + b_costs;
+    float2 *d_ptab = reinterpret_cast<float2 *>(w2);
+    float2 *d_mtab = reinterpret_cast<float2 *>(w2 + b_ptab);
+    double *d_part = reinterpret_cast<double *>(w2 + b_ptab + b_mtab);
     cudaStream_t st = ctx->stream;
     QF_CUDA(cudaMemcpyAsync(d_desc, desc.data(), sizeof(QDesc) * n_inst, cudaMemcpyHostToDevice, st));
     if (n_edges) QF_CUDA(cudaMemcpyAsync(d_mask, masks.data(), 8 * n_edges, cudaMemcpyHostToDevice, st));
@@ -367,25 +741,81 @@ extern "C" int qf_qaoa_maxcut_batch(qf_ctx *ctx, const qf_qaoa_instance *inst, u
     QF_CUDA(cudaMemcpyAsync(d_bet, betas, 8 * n_inst * p, cudaMemcpyHostToDevice, st));
     static bool attr[64] = {false};
     const size_t smem = sizeof(QShared);
+    const size_t smem_f = sizeof(float2) * kQBT + kQBT, smem_r = 2 * sizeof(float2) * kQBT + kQBT;  // tiles + cost bytes
     if (!attr[ctx->device & 63]) {
         QF_CUDA(cudaFuncSetAttribute(k_qaoa_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        QF_CUDA(cudaFuncSetAttribute(k_qaoa_rev<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r));
+        QF_CUDA(cudaFuncSetAttribute(k_qaoa_rev<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r));
+        QF_CUDA(cudaFuncSetAttribute(k_qaoa_fwd<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_f));
+        QF_CUDA(cudaFuncSetAttribute(k_qaoa_fwd<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_f));
         attr[ctx->device & 63] = true;
     }
+    const uint32_t n_small = (uint32_t)n_inst - r_small;
     int per_sm = 0;
     QF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_qaoa_batch, kQThreads, smem));
-    const uint32_t grid = (uint32_t)std::min<uint64_t>(n_inst, (uint64_t)std::max(1, per_sm) * ctx->sm_count);
+    const uint32_t grid = (uint32_t)std::min<uint64_t>(std::max(1u, n_small), (uint64_t)std::max(1, per_sm) * ctx->sm_count);
+    int occ_f = 0, occ_r = 0;
+    QF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, k_qaoa_fwd<false>, kQThreads, smem_f));
+    QF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_r, k_qaoa_rev<false>, kQThreads, smem_r));
+    const uint64_t cap_f = (uint64_t)std::max(1, occ_f) * ctx->sm_count, cap_r = (uint64_t)std::max(1, occ_r) * ctx->sm_count;
     auto enqueue = [&](cudaStream_t s) -> int {
-        QF_CUDA(cudaMemsetAsync(d_cnt, 0, sizeof(unsigned), s));
-        k_qaoa_batch<<<grid, kQThreads, smem, s>>>(d_desc, (uint32_t)n_inst, d_arena, d_costs, d_mask, d_gam, d_bet, p,
-                                                   d_cost, d_grad, d_cnt);
-        QF_CUDA(cudaGetLastError());
+        if (r_small) {
+            k_qaoa_tables<<<(unsigned)std::min<uint64_t>(4096, ((uint64_t)r_small * p * (kQMaxEdges + 1) + 255) / 256), 256, 0, s>>>(
+                d_desc, r_small, d_gam, d_bet, p, d_ptab, d_mtab);
+            QF_CUDA(cudaGetLastError());
+        }
+        for (uint32_t r0 = 0; r0 < r_small;) {  // one launch sequence per qubit count
+            uint32_t r1 = r0;
+            while (r1 < r_small && desc[r1].n == desc[r0].n) ++r1;
+            QBArgs A;
+            A.r0 = r0;
+            A.m = r1 - r0;
+            A.n = desc[r0].n;
+            A.L = 24 - A.n;
+            A.p = p;
+            A.tiles = 1ULL << (A.n - kQBTile);
+            const uint64_t items = (uint64_t)A.m * A.tiles;
+            const unsigned gf = (unsigned)std::min(items, cap_f), gr = (unsigned)std::min(items, cap_r);
+            A.layer = 0;
+            k_qaoa_costs<<<gf, kQThreads, 0, s>>>(A, d_desc, d_mask, d_costs);
+            for (uint32_t l = 0; l < p; ++l) {
+                A.layer = l;
+                k_qaoa_fwd<false><<<gf, kQThreads, smem_f, s>>>(A, d_desc, d_arena, d_costs, d_ptab, d_mtab, d_part);
+                k_qaoa_fwd<true><<<gf, kQThreads, smem_f, s>>>(A, d_desc, d_arena, d_costs, d_ptab, d_mtab, d_part);
+            }
+            for (uint32_t l = p; l-- > 0;) {
+                A.layer = l;
+                k_qaoa_rev<true><<<gr, kQThreads, smem_r, s>>>(A, d_desc, d_arena, d_costs, d_ptab, d_mtab, d_part);
+                k_qaoa_rev<false><<<gr, kQThreads, smem_r, s>>>(A, d_desc, d_arena, d_costs, d_ptab, d_mtab, d_part);
+            }
+            k_qaoa_reduce<<<(unsigned)std::max<uint64_t>(1, ((uint64_t)A.m * (1 + 2 * p) + 127) / 128), 128, 0, s>>>(
+                A, d_desc, d_part, d_cost, d_grad);
+            QF_CUDA(cudaGetLastError());
+            r0 = r1;
+        }
+        if (n_small) {
+            QF_CUDA(cudaMemsetAsync(d_cnt, 0, sizeof(unsigned), s));
+            k_qaoa_batch<<<grid, kQThreads, smem, s>>>(d_desc + r_small, n_small, d_arena, d_costs, d_mask, d_gam, d_bet, p,
+                                                       d_cost, d_grad, d_cnt);
+            QF_CUDA(cudaGetLastError());
+        }
         return QF_OK;
     };
     if (opts && opts->use_graph) {
         // capture the memset + persistent launch once per layout and replay it
         static thread_local cudaGraphExec_t exec = nullptr;
         static thread_local uint64_t key = 0;
-        const uint64_t k2 = (uint64_t)(uintptr_t)w ^ (n_inst * 1315423911ULL) ^ ((uint64_t)p << 56) ^ (amp_off << 7) ^ grid;
+        uint64_t k2 = 1469598103934665603ULL;  // FNV-1a over everything the captured launches depend on
+        auto mix = [&](uint64_t v) {
+            for (int b = 0; b < 8; ++b) k2 = (k2 ^ ((v >> (8 * b)) & 0xFF)) * 1099511628211ULL;
+        };
+        mix((uint64_t)(uintptr_t)w);
+        mix(n_inst);
+        mix(p);
+        mix(amp_off);
+        mix(grid);
+        mix(r_small);
+        for (uint32_t r = 0; r < r_small; ++r) mix(desc[r].n);
         if (!exec || key != k2) {
             if (exec) cudaGraphExecDestroy(exec);
             exec = nullptr;

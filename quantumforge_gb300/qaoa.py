@@ -1,11 +1,13 @@
 """Batched QAOA MaxCut on the GPU.
 
-``QaoaBatch`` evaluates, for many MaxCut instances of uneven qubit counts in
-one persistent launch, the expected cut of the QAOA state
+``QaoaBatch`` evaluates, for many MaxCut instances of uneven qubit counts, the
+expected cut of the QAOA state
 (``maxcut_qaoa_expectation``, src/qaoa_transfer.rs:221-236, on the circuit of
 ``algorithms::qaoa_maxcut``, src/algorithms.rs:110-137, unit weights) and its
-exact gradient with respect to every gamma_l and beta_l. ``autotune_tiles``
-picks the shared-memory tile width per qubit count by timing sub-batches.
+exact gradient with respect to every gamma_l and beta_l: instances of up to 12
+qubits one CTA each, larger ones (up to 24) as tile passes batched over all
+instances of a qubit count. ``autotune_tiles`` picks the shared-memory tile
+width of the small instances per qubit count by timing sub-batches.
 """
 from __future__ import annotations
 
@@ -79,12 +81,15 @@ class QaoaBatch:
 
 
 def autotune_tiles(problems, p: int, candidates=(8, 9, 10, 11, 12), reps: int = 2, backend=None) -> dict:
-    """Best tile width per qubit count, timed on the sub-batch of that count."""
+    """Best tile width per qubit count (up to 12 qubits: larger instances run as
+    batched passes with fixed 12-qubit tiles), timed on the sub-batch of that
+    count."""
     rng = np.random.default_rng(0)
     best = {}
     by_n: dict[int, list] = {}
     for prob in problems:
-        by_n.setdefault(int(prob[0]), []).append(prob)
+        if int(prob[0]) <= 12:
+            by_n.setdefault(int(prob[0]), []).append(prob)
     for n, probs in sorted(by_n.items()):
         probs = probs[: max(8, min(len(probs), 256))]
         g = rng.uniform(0, np.pi, (len(probs), p))

@@ -54,16 +54,43 @@ def test_batch_matches_oracle(backend, tiles, graph):
     assert np.abs(grad2[3] - g_ref).max() < 1e-4
 
 
+@pytest.mark.parametrize("graph", [False, True])
+def test_batched_passes_match_oracle(backend, graph):
+    """Instances above 12 qubits run as batched tile passes per qubit count
+    (several instances per count, mixed with per-CTA small instances)."""
+    rng = np.random.default_rng(9)
+    sizes = [14, 16, 18, 14, 10, 16, 12, 14]
+    problems = [(n, O.random_3_regular(n, 300 + i)) for i, n in enumerate(sizes)]
+    p = 2
+    gam = rng.uniform(0, np.pi, (len(problems), p))
+    bet = rng.uniform(0, np.pi / 2, (len(problems), p))
+    batch = QaoaBatch(problems, p, backend=backend, use_graph=graph)
+    for scale in (1.0, 0.6):  # the second call replays the graph with new angles
+        cost, grad = batch.run(gam * scale, bet * scale)
+        for i, (n, edges) in enumerate(problems):
+            e_ref, g_ref = oracle_cost_grad(n, edges, gam[i] * scale, bet[i] * scale)
+            assert abs(cost[i] - e_ref) < 1e-5 * max(1.0, abs(e_ref)), (i, n, cost[i], e_ref)
+            assert np.abs(grad[i] - g_ref).max() < 1e-4 * max(1.0, np.abs(g_ref).max()), (i, n, grad[i], g_ref)
+
+
 def test_uniform_superposition_cuts_half_the_edges(backend):
     # gamma = beta = 0: the state is H^n |0>, every edge is cut with probability 1/2
-    problems = [(n, O.random_3_regular(n, n)) for n in (12, 14, 16)]
+    problems = [(n, O.random_3_regular(n, n)) for n in (12, 14, 16, 20, 22, 24)]
     batch = QaoaBatch(problems, 2, backend=backend)
-    cost, grad = batch.run(np.zeros((3, 2)), np.zeros((3, 2)))
+    cost, grad = batch.run(np.zeros((len(problems), 2)), np.zeros((len(problems), 2)))
     for (n, edges), c in zip(problems, cost):
-        assert abs(c - 0.5 * len(edges)) < 1e-5
+        assert abs(c - 0.5 * len(edges)) < 1e-5 * len(edges), (n, c)
 
 
-def test_autotune_returns_a_tile_per_size(backend):
-    problems = [(n, O.random_3_regular(n, n + 7)) for n in (12, 14) for _ in range(8)]
+def test_more_than_24_qubits_is_rejected(backend):
+    from quantumforge_gb300 import QuantumError
+
+    with pytest.raises(QuantumError):
+        QaoaBatch([(26, O.random_3_regular(26, 1))], 1, backend=backend).run(np.zeros((1, 1)), np.zeros((1, 1)))
+
+
+def test_autotune_returns_a_tile_per_small_size(backend):
+    # instances above 12 qubits run as batched passes with fixed tiles: not tuned
+    problems = [(n, O.random_3_regular(n, n + 7)) for n in (10, 12, 14) for _ in range(8)]
     best = autotune_tiles(problems, 2, candidates=(8, 10, 12), reps=1, backend=backend)
-    assert set(best) == {12, 14} and all(k in (8, 10, 12) for k in best.values())
+    assert set(best) == {10, 12} and all(k in (8, 10, 12) for k in best.values())
