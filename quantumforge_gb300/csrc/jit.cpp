@@ -908,7 +908,7 @@ int compile_module(const std::string &src, int n_kernels, int device, JitModule 
 
 struct ModulePlan {
     char prefix = 'p';  // kernel names: p<k> forward, b<k> backward
-    std::string src;
+    std::shared_ptr<const std::string> src;
     std::vector<float> consts;  // interleaved float2
     std::vector<int> pass_index;
 };
@@ -917,9 +917,92 @@ struct ModulePlan {
 bool pass_fits(const Pass &p) { return __builtin_popcountll(p.resident) == kPos && (p.resident & 31ULL) == 31ULL; }
 
 // group passes into modules: at most 8 passes and 56 KB of constants each
-bool gen_modules(const Plan &plan, std::vector<ModulePlan> &mods, bool dual = false) {
+// Everything of a plan that shapes its generated source: per pass the
+// resident qubits and, per gate, kind, qubits, diagonal flag, matrix kind,
+// overlap axis and slot. Matrix values only enter the constant banks.
+std::string plan_key(const Plan &plan, bool dual) {
+    std::string k;
+    auto put = [&](uint64_t v, int bytes) {
+        for (int b = 0; b < bytes; ++b) k.push_back((char)((v >> (8 * b)) & 0xFF));
+    };
+    put(plan.n, 1);
+    put(dual, 1);
+    put(plan.passes.size(), 4);
+    for (const Pass &p : plan.passes) {
+        put(p.resident, 8);
+        put(p.gates.size(), 4);
+        for (const BGate &x : p.gates) {
+            uint8_t mk = 0;
+            if (x.kind == BK_MAT1 && !x.diag) {
+                const std::complex<double> m[4] = {{x.m[0], x.m[1]}, {x.m[2], x.m[3]}, {x.m[4], x.m[5]}, {x.m[6], x.m[7]}};
+                mk = matrix_kind_of(m);
+            }
+            put(x.kind | (x.diag << 3) | (mk << 4), 1);
+            put(x.q0, 1);
+            put(x.q1, 1);
+            if (x.kind == BK_OVL) {
+                put(x.axis, 1);
+                put((uint64_t)x.op_index, 4);
+            }
+        }
+    }
+    return k;
+}
+
+// The constant banks of modules generated for `plan`, rebuilt from the gates
+// in each pass's emission order exactly as emit_gate / finish allocate them.
+void replay_consts(const Plan &plan, const std::vector<std::vector<int>> &orders, std::vector<ModulePlan> &mods) {
     Gen g;
     const size_t npass = plan.passes.size();
+    for (ModulePlan &mp : mods) {
+        g.consts.clear();
+        for (int pi : mp.pass_index) {
+            const Pass &p = plan.passes[pi];
+            for (int j : orders[pi]) {
+                const BGate &x = p.gates[j];
+                if (x.kind != BK_MAT1) continue;
+                const std::complex<double> m[4] = {{x.m[0], x.m[1]}, {x.m[2], x.m[3]}, {x.m[4], x.m[5]}, {x.m[6], x.m[7]}};
+                if (x.diag) {
+                    g.any_diag = true;
+                    g.gphase *= m[0];
+                    const std::complex<double> f = m[3] / m[0];
+                    g.slot(f, 0.0, 0.0, f);
+                } else if (matrix_kind_of(m) == 1) {
+                    g.slot({m[0].real(), m[0].real()}, {m[1].real(), m[1].real()}, {m[2].real(), m[2].real()},
+                           {m[3].real(), m[3].real()});
+                } else {
+                    g.slot(m[0], m[1], m[2], m[3]);
+                }
+            }
+            if ((size_t)pi + 1 == npass && g.any_diag) g.slot(g.gphase, 0.0, 0.0, 0.0);
+        }
+        mp.consts.clear();
+        mp.consts.reserve(g.consts.size() * 2);
+        for (auto &c : g.consts) {
+            mp.consts.push_back((float)c.real());
+            mp.consts.push_back((float)c.imag());
+        }
+    }
+}
+
+struct GenEntry {
+    std::vector<ModulePlan> mods;        // sources; constants refilled per use
+    std::vector<std::vector<int>> orders;  // per pass: gate indices in emission order
+};
+struct GenCache {
+    std::mutex mu;
+    std::map<std::string, std::shared_ptr<const GenEntry>> entries;
+};
+GenCache &gen_cache() {
+    static GenCache c;
+    return c;
+}
+
+bool gen_modules_uncached(const Plan &plan, std::vector<ModulePlan> &mods, std::vector<std::vector<int>> &orders,
+                          bool dual) {
+    Gen g;
+    const size_t npass = plan.passes.size();
+    orders.assign(npass, {});
     size_t pi = 0;
     while (pi < npass) {
         ModulePlan mp;
@@ -934,13 +1017,14 @@ bool gen_modules(const Plan &plan, std::vector<ModulePlan> &mods, bool dual = fa
             pg.emit_kernel(local, pi + 1 == npass);
             if (pg.failed) return false;
             body << g.s.str();
+            orders[pi] = pg.order;
             mp.pass_index.push_back((int)pi);
             ++pi;
             ++local;
         }
         std::ostringstream head;
         head << "__constant__ float2 M[" << std::max<size_t>(1, g.consts.size()) << "];\n" << kPrelude;
-        mp.src = head.str() + body.str();
+        mp.src = std::make_shared<const std::string>(head.str() + body.str());
         mp.consts.reserve(g.consts.size() * 2);
         for (auto &c : g.consts) {
             mp.consts.push_back((float)c.real());
@@ -948,6 +1032,29 @@ bool gen_modules(const Plan &plan, std::vector<ModulePlan> &mods, bool dual = fa
         }
         mods.push_back(std::move(mp));
     }
+    return true;
+}
+
+// Modules of a plan: generated once per structure, constants per call.
+bool gen_modules(const Plan &plan, std::vector<ModulePlan> &mods, bool dual = false) {
+    const std::string key = plan_key(plan, dual);
+    std::shared_ptr<const GenEntry> hit;
+    {
+        std::lock_guard<std::mutex> lk(gen_cache().mu);
+        auto it = gen_cache().entries.find(key);
+        if (it != gen_cache().entries.end()) hit = it->second;
+    }
+    if (hit) {
+        mods = hit->mods;
+        replay_consts(plan, hit->orders, mods);
+        return true;
+    }
+    auto e = std::make_shared<GenEntry>();
+    if (!gen_modules_uncached(plan, e->mods, e->orders, dual)) return false;
+    mods = e->mods;
+    std::lock_guard<std::mutex> lk(gen_cache().mu);
+    if (gen_cache().entries.size() > 256) gen_cache().entries.clear();  // bound the host memory of the cache
+    gen_cache().entries[key] = e;
     return true;
 }
 
@@ -970,9 +1077,9 @@ int jit_check_compile(const Plan &plan, int, std::string *source, std::string *e
     Nvrtc &nv = nvrtc();
     if (!nv.ok) return fail(QF_ERR_UNSUPPORTED_OPERATION, "%s", nv.why.c_str());
     for (auto &m : mods) {
-        if (source) *source += m.src;
+        if (source) *source += *m.src;
         nvrtcProgram prog;
-        nv.create(&prog, m.src.c_str(), "qf_pass.cu", 0, nullptr, nullptr);
+        nv.create(&prog, m.src->c_str(), "qf_pass.cu", 0, nullptr, nullptr);
         nvrtcResult r = nv.compile(prog, 3, kNvrtcOpts);
         if (r != NVRTC_SUCCESS) {
             size_t ls = 0;
@@ -996,7 +1103,7 @@ int fetch_modules(qf_ctx *ctx, const std::vector<ModulePlan> &mods, std::vector<
     {
         std::lock_guard<std::mutex> lk(cache().mu);
         for (size_t m = 0; m < mods.size(); ++m) {
-            auto it = cache().mods.find(mods[m].src);
+            auto it = cache().mods.find(*mods[m].src);
             if (it != cache().mods.end()) handles[m] = it->second;
             else todo.push_back(m);
         }
@@ -1011,7 +1118,7 @@ int fetch_modules(qf_ctx *ctx, const std::vector<ModulePlan> &mods, std::vector<
         built[k] = std::make_shared<JitModule>();
         th.emplace_back([&, k, dev] {
             cudaSetDevice(dev);
-            st[k] = compile_module(mods[todo[k]].src, (int)mods[todo[k]].pass_index.size(), dev, *built[k], errs[k],
+            st[k] = compile_module(*mods[todo[k]].src, (int)mods[todo[k]].pass_index.size(), dev, *built[k], errs[k],
                                    mods[todo[k]].prefix);
         });
     }
@@ -1020,7 +1127,7 @@ int fetch_modules(qf_ctx *ctx, const std::vector<ModulePlan> &mods, std::vector<
         if (st[k]) return fail(st[k], "pass compiler: %s", errs[k].c_str());
     std::lock_guard<std::mutex> lk(cache().mu);
     for (size_t k = 0; k < todo.size(); ++k) {
-        cache().mods[mods[todo[k]].src] = built[k];
+        cache().mods[*mods[todo[k]].src] = built[k];
         handles[todo[k]] = built[k];
     }
     return QF_OK;
