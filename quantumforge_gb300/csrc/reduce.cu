@@ -69,11 +69,32 @@ __global__ void k_c64_to_f64(const float2 *__restrict__ src, double2 *__restrict
     }
 }
 
-// Host f64 amplitudes -> device state (chunked through a device staging buffer).
+// Device address of a page-locked host buffer (the kernels then read or write
+// it directly over the host link, no staging), or nullptr for pageable memory.
+static const void *pinned_device_ptr(const void *host) {
+    cudaPointerAttributes pa;
+    if (cudaPointerGetAttributes(&pa, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return pa.type == cudaMemoryTypeHost ? pa.devicePointer : nullptr;
+}
+
+// Host f64 amplitudes -> device state: a conversion kernel reading a pinned
+// host buffer directly, else chunks through a device staging buffer.
 int convert_from_f64(qf_sv *sv, const double *host) {
     qf_ctx *ctx = sv->ctx;
+    // the caller may reuse `host` once this returns: finish reading it first
     if (sv->dtype == QF_C128) {
         QF_CUDA(cudaMemcpyAsync(sv->d, host, sv->bytes(), cudaMemcpyHostToDevice, ctx->stream));
+        QF_CUDA(cudaStreamSynchronize(ctx->stream));
+        return QF_OK;
+    }
+    if (const void *dp = pinned_device_ptr(host)) {
+        k_f64_to_c64<<<(unsigned)std::max(1, ctx->sm_count) * 8, 256, 0, ctx->stream>>>(static_cast<const double2 *>(dp),
+                                                                                        static_cast<float2 *>(sv->d), sv->dim);
+        QF_CUDA(cudaGetLastError());
+        QF_CUDA(cudaStreamSynchronize(ctx->stream));
         return QF_OK;
     }
     const uint64_t chunk = std::min<uint64_t>(sv->dim, 1ULL << 24);  // amplitudes per chunk (256 MiB staging)
@@ -92,6 +113,13 @@ int convert_to_f64(qf_sv *sv, double *host) {
     qf_ctx *ctx = sv->ctx;
     if (sv->dtype == QF_C128) {
         QF_CUDA(cudaMemcpyAsync(host, sv->d, sv->bytes(), cudaMemcpyDeviceToHost, ctx->stream));
+        QF_CUDA(cudaStreamSynchronize(ctx->stream));
+        return QF_OK;
+    }
+    if (void *dp = const_cast<void *>(pinned_device_ptr(host))) {
+        k_c64_to_f64<<<(unsigned)std::max(1, ctx->sm_count) * 8, 256, 0, ctx->stream>>>(static_cast<const float2 *>(sv->d),
+                                                                                        static_cast<double2 *>(dp), sv->dim);
+        QF_CUDA(cudaGetLastError());
         QF_CUDA(cudaStreamSynchronize(ctx->stream));
         return QF_OK;
     }

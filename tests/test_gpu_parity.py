@@ -334,3 +334,35 @@ def test_state_outliving_its_context_is_released_safely(engine_lib):
         sv.apply(Gate.X, 0)
     assert e.value.kind == "InvalidArgument"
     del sv  # qf_sv_destroy on an orphan must not touch the released context
+
+
+@pytest.mark.parametrize("dtype", ["c64", "c128"])
+def test_run_circuit_with_pinned_host_buffers(backend, dtype):
+    """qf_run_circuit with page-locked f64 host amplitudes (read and written in
+    place by the conversion kernels) against the oracle, and the pageable path."""
+    import ctypes as C
+
+    torch = pytest.importorskip("torch")
+    from quantumforge_gb300 import _native
+
+    n = 14
+    ops = W.random_circuit(n, 8, 31, two_qubit="mixed")
+    rng = np.random.default_rng(3)
+    init = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    init /= np.linalg.norm(init)
+    expected = O.run(ops, n, init=init)
+    lib = _native.load()
+    code = A.C64 if dtype == "c64" else A.C128
+    tol = C64_TOL if dtype == "c64" else C128_TOL
+    h_in = torch.from_numpy(init.view(np.float64).copy()).pin_memory()
+    h_out = torch.empty(2 << n, dtype=torch.float64).pin_memory()
+    eo = A.exec_opts(None)
+    _native.check(lib.qf_run_circuit(backend.handle, n, code, _native.ptr(ops), len(ops), C.c_void_p(h_in.data_ptr()),
+                                     C.c_void_p(h_out.data_ptr()), 2 << n, C.byref(eo)))
+    got = h_out.numpy().view(np.complex128)
+    assert close(got, expected, tol)
+    out2 = np.empty(2 << n, dtype=np.float64)  # pageable buffers: staged copies
+    src = np.ascontiguousarray(init).view(np.float64)
+    _native.check(lib.qf_run_circuit(backend.handle, n, code, _native.ptr(ops), len(ops), _native.ptr(src),
+                                     _native.ptr(out2), 2 << n, C.byref(eo)))
+    assert np.array_equal(out2, h_out.numpy())
