@@ -765,7 +765,7 @@ int qf_plan_stats(uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops, 
         return QF_OK;
     }
     PlanOpts po;
-    default_tiling(qubits, dtype, opts ? opts->tile_qubits : 0, &po.tile_qubits, &po.low_qubits);
+    forward_tiling(qubits, dtype, opts ? opts->tile_qubits : 0, opts ? opts->flags : 0, &po.tile_qubits, &po.low_qubits);
     Plan plan;
     QF_TRY(plan_passes(qubits, gates, po, plan));
     *n_passes = plan.passes.size();

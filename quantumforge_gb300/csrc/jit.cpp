@@ -92,19 +92,23 @@ Nvrtc &nvrtc() {
 
 // ---- code generation ---------------------------------------------------------
 constexpr int kR = 16;        // amplitudes per thread
-constexpr int kPos = 12;      // positions: 0..4 lane bits, 5..8 register bits, 9..11 warp bits
-constexpr int kTile = 4096;   // amplitudes per tile
-constexpr int kThreads = 256;
-constexpr int kChunks = kTile / 2 / kThreads;  // 16-byte chunks per thread
+// A pass tile holds K = 12 or 13 resident qubits (forward passes may use 13,
+// backward passes 12) in K positions: 0..4 lane bits, 5..8 register bits,
+// 9..K-1 warp bits; 16 amplitudes per thread, so 2^(K-4) threads per CTA.
+constexpr int kPosMax = 13;
+constexpr int kChunks = 8;  // 16-byte chunks per thread per tile (2^K / 2 / 2^(K-4))
+int tile_of(int K) { return 1 << K; }
+int threads_of(int K) { return 1 << (K - 4); }
+size_t dyn_smem_of(int K) { return 2u * (size_t)tile_of(K) * 8u; }  // two tile buffers of float2
 
-// Shared-memory swizzle: tile index bits 4..11 are folded into bits 1..3
-// (the bank bits of a 16-byte chunk) with the columns 1,2,4,3,6,5,7,1, so
-// that the slots 1..11 reach every nonzero combination of bank bits and any
+// Shared-memory swizzle: tile index bits 4..12 are folded into bits 1..3
+// (the bank bits of a 16-byte chunk) with the columns 1,2,4,3,6,5,7,1,2, so
+// that the slots 1..12 reach every nonzero combination of bank bits and any
 // four register slots leave a bank basis for the lanes. Bit 0 is never
 // swizzled: 16-byte chunks stay whole.
-constexpr uint32_t kSwzMask[3] = {0xE9u, 0x5Au, 0x74u};
+constexpr uint32_t kSwzMask[3] = {0xE9u, 0x15Au, 0x74u};
 uint32_t swz(uint32_t j) {
-    const uint32_t h = (j >> 4) & 0xFFu;
+    const uint32_t h = (j >> 4) & 0x1FFu;
     uint32_t r = 0;
     for (int b = 0; b < 3; ++b) r |= (uint32_t)(__builtin_popcount(h & kSwzMask[b]) & 1) << b;
     return r;
@@ -203,8 +207,10 @@ struct PassGen {
     const Pass &p;
     uint32_t n;
     int slot_of[64];
-    uint32_t slot_q[kPos];
-    uint32_t L[kPos];  // position -> qubit
+    uint32_t slot_q[kPosMax];
+    uint32_t L[kPosMax];  // position -> qubit
+    int K = 12;           // resident qubits (positions)
+    int WB = 3;           // warp bits: K - 9
 
     bool dual;  // backward pass: psi (A, r*) and lambda (B, l*) with overlap slots
 
@@ -216,9 +222,11 @@ struct PassGen {
                 slot_of[q] = s;
                 slot_q[s++] = q;
             }
+        K = s;
+        WB = K - 9;
     }
     int pos_of(uint32_t q) const {
-        for (int i = 0; i < kPos; ++i)
+        for (int i = 0; i < K; ++i)
             if (L[i] == q) return i;
         return -1;
     }
@@ -326,7 +334,7 @@ struct PassGen {
         }
         for (int k = 0; k < 4; ++k) {
             int pick = -1, pd = best_dense, pa = best_all;
-            for (int s = kPos - 1; s >= 0; --s) {  // ties keep qubits 0..4 for the lanes
+            for (int s = K - 1; s >= 0; --s) {  // ties keep qubits 0..4 for the lanes
                 const uint32_t q = slot_q[s];
                 if ((mask >> q) & 1ULL) continue;
                 std::vector<char> d = done;
@@ -355,13 +363,13 @@ struct PassGen {
     // chosen for conflict-free shared-memory access
     void relayout(const std::vector<uint32_t> &want) {
         std::vector<uint32_t> regs(want.begin(), want.begin() + std::min<size_t>(want.size(), 4));
-        for (int s = kPos - 1; s >= 0 && regs.size() < 4; --s)  // prefer high slots: keep 0..4 for the lanes
+        for (int s = K - 1; s >= 0 && regs.size() < 4; --s)  // prefer high slots: keep 0..4 for the lanes
             if (std::find(regs.begin(), regs.end(), slot_q[s]) == regs.end()) regs.push_back(slot_q[s]);
         std::vector<int> free_slots;
-        for (int s = 0; s < kPos; ++s)
+        for (int s = 0; s < K; ++s)
             if (std::find(regs.begin(), regs.end(), slot_q[s]) == regs.end()) free_slots.push_back(s);
-        uint32_t nl[kPos];
-        std::vector<bool> used(kPos, false);
+        uint32_t nl[kPosMax];
+        std::vector<bool> used(K, false);
         auto take = [&](int s) {
             used[s] = true;
             return slot_q[s];
@@ -416,14 +424,14 @@ struct PassGen {
             if (!used[s]) {
                 nl[w++] = take(s);
             }
-        std::memcpy(L, nl, sizeof nl);
+        std::memcpy(L, nl, sizeof(uint32_t) * K);
     }
     // shared-memory index of the thread part (lane and warp bits), as code
     std::string thread_index() const {
         std::ostringstream o;
         o << "(0u";
         for (int ps = 0; ps < 5; ++ps) o << " | (((lane >> " << ps << ") & 1u) << " << slot_of[L[ps]] << ")";
-        for (int w = 0; w < 3; ++w) o << " | (((warp >> " << w << ") & 1u) << " << slot_of[L[9 + w]] << ")";
+        for (int w = 0; w < WB; ++w) o << " | (((warp >> " << w << ") & 1u) << " << slot_of[L[9 + w]] << ")";
         o << ")";
         return o.str();
     }
@@ -487,11 +495,14 @@ struct PassGen {
         }
         g.pfx = "r";
     }
-    // global byte-free address bits of canonical shared index j's register+warp part
-    uint64_t chunk_k_bits(int k) const {  // canonical j = 2*tid + 512*k: bits 9..11 = k -> slots 9..11
+    // Canonical shared index of 16-byte chunk k of thread tid: j = 2*tid +
+    // (tile/8)*k, so bits 0..4 are qubits 0..4, bits 5..K-4 slots 5..K-4 (tid
+    // bits 4..), bits K-3..K-1 the chunk index (the top three slots).
+    uint32_t chunk_j(int k) const { return (uint32_t)(tile_of(K) / 8) * (uint32_t)k; }
+    uint64_t chunk_k_bits(int k) const {
         uint64_t a = 0;
         for (int b = 0; b < 3; ++b)
-            if ((k >> b) & 1) a |= 1ULL << slot_q[9 + b];
+            if ((k >> b) & 1) a |= 1ULL << slot_q[K - 3 + b];
         return a;
     }
 
@@ -504,7 +515,7 @@ struct PassGen {
         auto &s = g.s;
         for (int a = 0; a < n_arrays(); ++a)
             for (int k = 0; k < kChunks; ++k)
-                s << "qf_cpa16(sbase + (" << (a ? "4096u + " : "") << "(pt2 ^ " << physj(512u * k) << "u)) * 8u, "
+                s << "qf_cpa16(sbase + (" << (a ? std::to_string(tile_of(K)) + "u + " : std::string()) << "(pt2 ^ " << physj(chunk_j(k)) << "u)) * 8u, "
                   << glob_of(a) << " + (" << tq << " | toff | " << hex64(chunk_k_bits(k)) << "));\n";
     }
 
@@ -518,10 +529,10 @@ struct PassGen {
             return;
         }
         if (!dual)
-            s << "extern \"C\" __global__ void __launch_bounds__(" << kThreads << ", 3) p" << index
+            s << "extern \"C\" __global__ void __launch_bounds__(" << threads_of(K) << ", " << (K == 12 ? 3 : 1) << ") p" << index
               << "(float2* __restrict__ A, unsigned long long nt) {\n";
         else
-            s << "extern \"C\" __global__ void __launch_bounds__(" << kThreads << ", 2) b" << index
+            s << "extern \"C\" __global__ void __launch_bounds__(" << threads_of(K) << ", 2) b" << index
               << "(float2* __restrict__ A, float2* __restrict__ B, unsigned long long nt, double* __restrict__ partials, "
                  "unsigned stride) {\n";
         s << "extern __shared__ __align__(16) float2 SB[];\n";
@@ -530,12 +541,12 @@ struct PassGen {
         // canonical shared index j = 2*tid + 512*k: bits 0..4 = qubits 0..4,
         // bits 5..8 = slots 5..8 (from tid >> 4), bits 9..11 = slots 9..11 (k)
         s << "const unsigned long long toff = (unsigned long long)((2u * tid) & 31u)";
-        for (int b = 0; b < 4; ++b) s << " | ((tid & " << (16u << b) << "u) ? (1ull << " << slot_q[5 + b] << ") : 0ull)";
+        for (int b = 0; b < K - 8; ++b) s << " | ((tid & " << (16u << b) << "u) ? (1ull << " << slot_q[5 + b] << ") : 0ull)";
         s << ";\n";
         s << "const unsigned pt2 = qf_phys(2u * tid);\n";
         auto issue = [&](const std::string &tq, const std::string &buf) {
             for (int k = 0; k < kChunks; ++k)
-                s << "qf_cpa16(sbase + ((" << buf << ") * " << kTile << "u + (pt2 ^ " << physj(512u * k) << "u)) * 8u, A + (" << tq
+                s << "qf_cpa16(sbase + ((" << buf << ") * " << tile_of(K) << "u + (pt2 ^ " << physj(chunk_j(k)) << "u)) * 8u, A + (" << tq
                   << " | toff | " << hex64(chunk_k_bits(k)) << "));\n";
         };
         s << "unsigned long long t = blockIdx.x;\n";
@@ -549,7 +560,7 @@ struct PassGen {
             issue("tq", "cur ^ 1u");
             s << "}}\nasm volatile(\"cp.async.commit_group;\\n\" ::: \"memory\");\n";
             s << "asm volatile(\"cp.async.wait_group 1;\\n\" ::: \"memory\");\n__syncthreads();\n";
-            s << "float2* S = SB + cur * " << kTile << "u;\n";
+            s << "float2* S = SB + cur * " << tile_of(K) << "u;\n";
         } else {
             // one psi + lambda buffer; the next tile streams in after the last
             // shared-memory read of the current one
@@ -559,7 +570,7 @@ struct PassGen {
             s << "}\nasm volatile(\"cp.async.commit_group;\\n\" ::: \"memory\");\n";
             s << "for (; t < nt; t += gridDim.x) {\n";
             s << "asm volatile(\"cp.async.wait_group 0;\\n\" ::: \"memory\");\n__syncthreads();\n";
-            s << "float2* S = SB;\nfloat2* SL = SB + " << kTile << "u;\n";
+            s << "float2* S = SB;\nfloat2* SL = SB + " << tile_of(K) << "u;\n";
         }
         s << "const unsigned long long tb = " << dep_t << ";\n";
         for (int a = 0; a < n_arrays(); ++a)
@@ -777,7 +788,7 @@ struct PassGen {
                 s << txt;
             }
             s << "const unsigned long long sw = 0ull";
-            for (int w = 0; w < 3; ++w) s << " | ((warp & " << (1 << w) << "u) ? (1ull << " << L[9 + w] << ") : 0ull)";
+            for (int w = 0; w < WB; ++w) s << " | ((warp & " << (1 << w) << "u) ? (1ull << " << L[9 + w] << ") : 0ull)";
             s << ";\n";
             for (int a = 0; a < n_arrays(); ++a) {
                 g.pfx = reg_pfx(a);
@@ -795,7 +806,7 @@ struct PassGen {
             for (int a = 0; a < n_arrays(); ++a)
                 for (int k = 0; k < kChunks; ++k)
                     s << "*reinterpret_cast<float4*>(" << glob_of(a) << " + (tb | toff | " << hex64(chunk_k_bits(k))
-                      << ")) = *reinterpret_cast<const float4*>(" << smem_of(a) << " + (pt2 ^ " << physj(512u * k) << "u));\n";
+                      << ")) = *reinterpret_cast<const float4*>(" << smem_of(a) << " + (pt2 ^ " << physj(chunk_j(k)) << "u));\n";
             s << "__syncthreads();\n";
             if (dual) {
                 s << prefetch;
@@ -811,7 +822,7 @@ struct PassGen {
                 s << "if (lane + " << 32 * a << "u < " << p.a.n_slots << "u) RD[(lane + " << 32 * a << "u) * 8u + warp] = acc" << a
                   << ";\n";
             s << "__syncthreads();\n";
-            s << "for (unsigned k = tid; k < " << p.a.n_slots << "u; k += " << kThreads << "u) {double v = 0.0;"
+            s << "for (unsigned k = tid; k < " << p.a.n_slots << "u; k += " << threads_of(K) << "u) {double v = 0.0;"
               << " for (unsigned w = 0; w < 8u; ++w) v += RD[k * 8u + w];"
               << " partials[(size_t)(" << p.a.slot_base << "u + k) * stride + blockIdx.x] = v;}\n";
         }
@@ -836,13 +847,12 @@ JitCache &cache() {
     return c;
 }
 
-constexpr size_t kDynSmem = 2u * kTile * sizeof(float) * 2;  // two tile buffers of float2
 
 const char *kPrelude =
     "__device__ __forceinline__ void qf_cpa16(unsigned s, const float2* g) {"
     " asm volatile(\"cp.async.cg.shared.global [%0], [%1], 16;\\n\" :: \"r\"(s), \"l\"(g) : \"memory\"); }\n"
-    "__device__ __forceinline__ unsigned qf_phys(unsigned j) { const unsigned h = (j >> 4) & 0xFFu;"
-    " return j ^ ((__popc(h & 0xE9u) & 1u) << 1) ^ ((__popc(h & 0x5Au) & 1u) << 2) ^ ((__popc(h & 0x74u) & 1u) << 3); }\n"
+    "__device__ __forceinline__ unsigned qf_phys(unsigned j) { const unsigned h = (j >> 4) & 0x1FFu;"
+    " return j ^ ((__popc(h & 0xE9u) & 1u) << 1) ^ ((__popc(h & 0x15Au) & 1u) << 2) ^ ((__popc(h & 0x74u) & 1u) << 3); }\n"
     "__device__ __forceinline__ unsigned long long qf_pk(float2 v) { unsigned long long r;"
     " asm(\"mov.b64 %0, {%1, %2};\" : \"=l\"(r) : \"f\"(v.x), \"f\"(v.y)); return r; }\n"
     "__device__ __forceinline__ float2 qf_upk(unsigned long long r) { float2 v;"
@@ -894,7 +904,7 @@ int compile_module(const std::string &src, int n_kernels, int device, JitModule 
             return QF_ERR_CUDA;
         }
         if ((e = cudaKernelSetAttributeForDevice(out.kernels[k], cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)kDynSmem, device)) != cudaSuccess) {
+                                                 (int)dyn_smem_of(kPosMax), device)) != cudaSuccess) {
             err = std::string("cudaKernelSetAttributeForDevice: ") + cudaGetErrorString(e);
             return QF_ERR_CUDA;
         }
@@ -914,7 +924,13 @@ struct ModulePlan {
 };
 
 // a pass the compiled kernels can run: 12 resident qubits including 0..4
-bool pass_fits(const Pass &p) { return __builtin_popcountll(p.resident) == kPos && (p.resident & 31ULL) == 31ULL; }
+// a pass the compiled kernels can run: 12 resident qubits (or 13 forward)
+// including 0..4
+bool pass_fits(const Pass &p, bool dual) {
+    const int K = __builtin_popcountll(p.resident);
+    return (K == 12 || (!dual && K == 13)) && (p.resident & 31ULL) == 31ULL;
+}
+int pass_k(const Pass &p) { return __builtin_popcountll(p.resident); }
 
 // group passes into modules: at most 8 passes and 56 KB of constants each
 // Everything of a plan that shapes its generated source: per pass the
@@ -1062,16 +1078,16 @@ bool gen_modules(const Plan &plan, std::vector<ModulePlan> &mods, bool dual = fa
 
 bool jit_available() { return nvrtc().ok; }
 
-bool jit_plan_fits(const Plan &plan) {
-    if (plan.n < (uint32_t)kPos) return false;
+bool jit_plan_fits(const Plan &plan, bool dual = false) {
+    if (plan.n < 12 || plan.passes.empty()) return false;
     for (const Pass &p : plan.passes)
-        if (!pass_fits(p)) return false;
+        if (!pass_fits(p, dual) || pass_k(p) != pass_k(plan.passes[0])) return false;
     return true;
 }
 
 // Generated sources and an NVRTC compile without loading (needs no GPU).
 int jit_check_compile(const Plan &plan, int, std::string *source, std::string *err, bool dual) {
-    if (!jit_plan_fits(plan)) return fail(QF_ERR_UNSUPPORTED_OPERATION, "plan has a pass outside the compiled layout");
+    if (!jit_plan_fits(plan, dual)) return fail(QF_ERR_UNSUPPORTED_OPERATION, "plan has a pass outside the compiled layout");
     std::vector<ModulePlan> mods;
     if (!gen_modules(plan, mods, dual)) return fail(QF_ERR_UNSUPPORTED_OPERATION, "pass compiler could not schedule a pass");
     Nvrtc &nv = nvrtc();
@@ -1140,9 +1156,9 @@ int upload_consts(qf_ctx *ctx, JitModule &jm, const ModulePlan &mp) {
     return QF_OK;
 }
 
-int grid_of(qf_ctx *ctx, cudaKernel_t k, uint64_t n_tiles, uint64_t *grid) {
+int grid_of(qf_ctx *ctx, cudaKernel_t k, int K, uint64_t n_tiles, uint64_t *grid) {
     int per_sm = 0;
-    QF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)k, kThreads, kDynSmem));
+    QF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)k, threads_of(K), dyn_smem_of(K)));
     per_sm = std::min(std::max(per_sm, 1), 4);
     *grid = std::min<uint64_t>((uint64_t)per_sm * ctx->sm_count, n_tiles);
     return QF_OK;
@@ -1151,10 +1167,11 @@ int grid_of(qf_ctx *ctx, cudaKernel_t k, uint64_t n_tiles, uint64_t *grid) {
 
 // Generate, compile (or fetch) and launch the plan's passes.
 int run_plan_jit(qf_sv *sv, const Plan &plan, int) {
-    if (!jit_plan_fits(plan)) return run_plan_rs(sv, plan, 3);  // interpreted (falls back to shared memory)
+    const int wb = (int)plan.passes[0].a.k - 9;
+    if (!jit_plan_fits(plan)) return run_plan_rs(sv, plan, wb);  // interpreted (falls back to shared memory)
     qf_ctx *ctx = sv->ctx;
     std::vector<ModulePlan> mods;
-    if (!gen_modules(plan, mods)) return run_plan_rs(sv, plan, 3);
+    if (!gen_modules(plan, mods)) return run_plan_rs(sv, plan, wb);
     std::vector<std::shared_ptr<JitModule>> handles;
     QF_TRY(fetch_modules(ctx, mods, handles));
     for (size_t m = 0; m < mods.size(); ++m) {
@@ -1163,11 +1180,12 @@ int run_plan_jit(qf_sv *sv, const Plan &plan, int) {
         for (size_t k = 0; k < mods[m].pass_index.size(); ++k) {
             const Pass &p = plan.passes[mods[m].pass_index[k]];
             uint64_t grid;
-            QF_TRY(grid_of(ctx, jm.kernels[k], p.a.n_tiles, &grid));
+            const int K = pass_k(p);
+            QF_TRY(grid_of(ctx, jm.kernels[k], K, p.a.n_tiles, &grid));
             float2 *amps = static_cast<float2 *>(sv->d);
             unsigned long long nt = p.a.n_tiles;
             void *args[] = {&amps, &nt};
-            QF_CUDA(cudaLaunchKernel((const void *)jm.kernels[k], dim3((unsigned)grid), dim3(kThreads), args, kDynSmem,
+            QF_CUDA(cudaLaunchKernel((const void *)jm.kernels[k], dim3((unsigned)grid), dim3(threads_of(K)), args, dyn_smem_of(K),
                                      ctx->stream));
         }
     }
@@ -1178,7 +1196,7 @@ int run_plan_jit(qf_sv *sv, const Plan &plan, int) {
 // reduced per CTA into partials[slot * stride + block] and then summed in
 // block order into d_slot_sums.
 int run_plan_jit_dual(qf_sv *psi, qf_sv *lam, const Plan &plan, double *d_slot_sums) {
-    if (!jit_plan_fits(plan)) return run_plan_dual_smem(psi, lam, plan, d_slot_sums);
+    if (!jit_plan_fits(plan, true)) return run_plan_dual_smem(psi, lam, plan, d_slot_sums);
     qf_ctx *ctx = psi->ctx;
     std::vector<ModulePlan> mods;
     if (!gen_modules(plan, mods, true)) return run_plan_dual_smem(psi, lam, plan, d_slot_sums);
@@ -1198,13 +1216,14 @@ int run_plan_jit_dual(qf_sv *psi, qf_sv *lam, const Plan &plan, double *d_slot_s
         for (size_t k = 0; k < mods[m].pass_index.size(); ++k) {
             const Pass &p = plan.passes[mods[m].pass_index[k]];
             uint64_t grid;
-            QF_TRY(grid_of(ctx, jm.kernels[k], p.a.n_tiles, &grid));
+            const int K = pass_k(p);
+            QF_TRY(grid_of(ctx, jm.kernels[k], K, p.a.n_tiles, &grid));
             float2 *a = static_cast<float2 *>(psi->d), *b = static_cast<float2 *>(lam->d);
             unsigned long long nt = p.a.n_tiles;
             double *parts = d_partials;
             unsigned str = stride;
             void *args[] = {&a, &b, &nt, &parts, &str};
-            QF_CUDA(cudaLaunchKernel((const void *)jm.kernels[k], dim3((unsigned)grid), dim3(kThreads), args, kDynSmem,
+            QF_CUDA(cudaLaunchKernel((const void *)jm.kernels[k], dim3((unsigned)grid), dim3(threads_of(K)), args, dyn_smem_of(K),
                                      ctx->stream));
         }
     }

@@ -232,6 +232,7 @@ int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, 
 int lower_rs(const Plan &plan, int wb, RsPlan &out);
 // Default tile/low widths for a state.
 void default_tiling(uint32_t n, int dtype, int requested_tile, int *tile, int *low);
+void forward_tiling(uint32_t n, int dtype, int requested_tile, int flags, int *tile, int *low);
 
 // ---- launchers (kernels in *.cu) ------------------------------------------
 // Unfused single-gate sweeps.

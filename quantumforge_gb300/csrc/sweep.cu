@@ -555,7 +555,7 @@ int run_plan(qf_sv *sv, const Plan &plan, int flags) {
         const uint32_t k = plan.passes[0].a.k;
         // compiled passes for large states (the compile is amortised over many
         // sweeps of the state), interpreted register tiles otherwise
-        const bool jit = k == 12 && !(flags & QF_EXEC_FLAG_NO_JIT) &&
+        const bool jit = (k == 12 || k == 13) && !(flags & QF_EXEC_FLAG_NO_JIT) &&
                          ((flags & QF_EXEC_FLAG_JIT) || sv->n >= kJitMinQubits) && jit_available();
         if (jit) return run_plan_jit(sv, plan, 3);
         if (k == 12 || k == 13) return run_plan_rs(sv, plan, (int)k - 9);
@@ -598,7 +598,7 @@ int execute_gates(qf_sv *sv, const std::vector<BGate> &gates, const qf_exec_opts
     if (mode != QF_EXEC_AUTO && mode != QF_EXEC_FUSED)
         return fail(QF_ERR_INVALID_ARGUMENT, "unknown execution mode %d", mode);
     PlanOpts po;
-    default_tiling(sv->n, sv->dtype, opts ? opts->tile_qubits : 0, &po.tile_qubits, &po.low_qubits);
+    forward_tiling(sv->n, sv->dtype, opts ? opts->tile_qubits : 0, opts ? opts->flags : 0, &po.tile_qubits, &po.low_qubits);
     Plan plan;
     QF_TRY(plan_passes(sv->n, gates, po, plan));
     return run_plan(sv, plan, opts ? opts->flags : 0);

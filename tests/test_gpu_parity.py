@@ -323,6 +323,21 @@ def test_compiled_passes_match_oracle(backend, n, seed, kinds):
         assert close(sv.amplitudes(), expected, C64_TOL), trial
 
 
+@pytest.mark.parametrize("n,seed,kinds", [(14, 41, True), (16, 42, True), (17, 43, False), (20, 44, False)])
+def test_compiled_13_qubit_tiles_match_oracle(backend, n, seed, kinds):
+    """Compiled forward passes on 13-qubit tiles (512 threads, 4 warp bits; the
+    default for large complex64 states), with new angles on a second run."""
+    ops = _all_kinds_circuit(n, seed) if kinds else W.random_circuit(n, 16, seed, two_qubit="mixed")
+    for trial in range(2):
+        if trial == 1:
+            ops = ops.copy()
+            ops["theta"] = ops["theta"] * 0.7 + 0.1
+        expected = O.run(ops, n, threads=8)
+        sv = StateVector.zero(n, dtype="c64", backend=backend)
+        sv.apply_ops(ops, exec_opts={"jit": True, "tile_qubits": 13})
+        assert close(sv.amplitudes(), expected, C64_TOL), trial
+
+
 def test_state_outliving_its_context_is_released_safely(engine_lib):
     from quantumforge_gb300 import CudaBackend
 
