@@ -271,6 +271,177 @@ int adjoint_device(qf_ctx *ctx, uint32_t n, const std::vector<BGate> &gates, con
     return QF_OK;
 }
 
+// Circuit::run_shots (src/lib.rs:2842-2916) for circuits with mid-circuit
+// measurements, repeated measurements or ConditionalSingleQubit feed-forward.
+// Shots walk a tree of measurement branches: a branch is one device state
+// with its classical register; unitary segments (with the conditionals that
+// fire for the branch's register) run through the fused engine once per
+// branch; at a measurement every shot of a branch draws its own next uniform
+// (shot s starts at draw s * measurements of SmallRng::seeded(seed), the
+// reference's shot-major stream) against the branch's P(1) and moves to the
+// collapsed child (src/lib.rs:1321-1351). The trailing measurements of
+// distinct qubits use the prefix-tree sampler per branch. Decisions equal the
+// reference's except where |u - P(1)| < tie_eps (counted); complex64 states
+// take P(1) relative to their own norm.
+int run_shots_branching(qf_ctx *ctx, uint32_t n, int dtype, const qf_op *ops, uint64_t n_ops, const double *init,
+                        uint64_t shots, uint64_t seed, double tie_eps, uint64_t *outcomes, uint64_t *n_ties,
+                        const qf_exec_opts *opts) {
+    // terminal block: the trailing measurements of distinct qubits
+    uint64_t T = n_ops, seen = 0;
+    while (T > 0 && ops[T - 1].kind == QF_OP_MEASURE && !((seen >> ops[T - 1].q0) & 1ULL)) {
+        seen |= 1ULL << ops[T - 1].q0;
+        --T;
+    }
+    uint64_t m_total = 0;
+    for (uint64_t k = 0; k < n_ops; ++k) m_total += ops[k].kind == QF_OP_MEASURE;
+    // every shot's generator state at its first draw
+    std::vector<uint64_t> st(shots);
+    {
+        uint64_t z = seed + 0x9E3779B97F4A7C15ULL;  // SmallRng::seeded (src/lib.rs:4881-4897)
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+        z ^= z >> 31;
+        uint64_t x = z == 0 ? 0x9E3779B97F4A7C15ULL : z;
+        for (uint64_t s = 0; s < shots; ++s) {
+            st[s] = x;
+            for (uint64_t k = 0; k < m_total; ++k) {
+                x ^= x << 13;
+                x ^= x >> 7;
+                x ^= x << 17;
+            }
+        }
+    }
+    struct Branch {
+        qf_sv *sv;
+        uint64_t reg;
+        std::vector<uint32_t> shots;
+    };
+    std::vector<Branch> br, next;
+    struct Guard {  // the device states of every live branch, on every exit
+        std::vector<Branch> *v, *w;
+        ~Guard() {
+            for (std::vector<Branch> *x : {v, w})
+                for (Branch &b : *x)
+                    if (b.sv) free_state(b.sv);
+        }
+    } guard{&br, &next};
+    {
+        qf_sv *root;
+        QF_TRY(alloc_state(ctx, n, dtype, 0, &root));
+        br.push_back(Branch{root, 0, {}});
+        br[0].shots.resize(shots);
+        for (uint64_t s = 0; s < shots; ++s) br[0].shots[s] = (uint32_t)s;
+        if (init) QF_TRY(convert_from_f64(root, init));
+    }
+    std::vector<qf_op> seg;  // pending gates and conditionals
+    auto flush = [&]() -> int {
+        if (seg.empty()) return QF_OK;
+        for (Branch &b : br) {
+            std::vector<qf_op> run;
+            run.reserve(seg.size());
+            for (const qf_op &o : seg) {
+                if (o.kind == QF_OP_COND) {  // ConditionalSingleQubit: apply when classical[bit] == value
+                    if (((b.reg >> o.param) & 1ULL) != (uint64_t)(o.flags & 1)) continue;
+                    qf_op g = o;
+                    g.kind = QF_OP_GATE;
+                    g.param = 0;
+                    g.flags = 0;
+                    run.push_back(g);
+                } else {
+                    run.push_back(o);
+                }
+            }
+            std::vector<BGate> gates;
+            QF_TRY(bind_ops(n, run.data(), run.size(), nullptr, 0, nullptr, 0, -1, 0.0, gates));
+            QF_TRY(execute_gates(b.sv, gates, opts));
+        }
+        seg.clear();
+        return QF_OK;
+    };
+    uint64_t ties = 0;
+    for (uint64_t k = 0; k < T; ++k) {
+        const qf_op &o = ops[k];
+        if (o.kind != QF_OP_MEASURE) {
+            seg.push_back(o);
+            continue;
+        }
+        QF_TRY(flush());
+        next.clear();
+        for (Branch &b : br) {
+            double p1;
+            QF_TRY(reduce_p_one(b.sv, o.q0, &p1));
+            if (dtype == QF_C64) {  // relative to the state's own norm, which f32 rounding moves off 1
+                double nrm;
+                QF_TRY(reduce_norm_sqr(b.sv, &nrm));
+                if (nrm > 0.0) p1 /= nrm;
+            }
+            p1 = std::min(1.0, std::max(0.0, p1));
+            std::vector<uint32_t> go[2];
+            for (uint32_t s : b.shots) {
+                uint64_t x = st[s];
+                x ^= x << 13;
+                x ^= x >> 7;
+                x ^= x << 17;
+                st[s] = x;
+                const double u = (double)(x >> 11) * (1.0 / 9007199254740992.0);
+                const int out = u < p1 ? 1 : 0;
+                if (std::fabs(u - p1) < tie_eps) ++ties;
+                go[out].push_back(s);
+            }
+            double prob[2] = {1.0 - p1, p1};
+            for (int out = 0; out < 2; ++out)
+                if (!go[out].empty() && prob[out] <= 2.220446049250313e-16)
+                    return fail(QF_ERR_INVALID_PROBABILITY, "measurement probability must be in [0, 1], got %g", prob[out]);
+            const int reuse = go[1].empty() ? 0 : 1;  // the branch's own state goes to this child
+            for (int out = 0; out < 2; ++out) {
+                if (go[out].empty()) continue;
+                qf_sv *c = b.sv;
+                if (out != reuse) {  // a copy taken before the shared state is collapsed
+                    QF_TRY(alloc_state(ctx, n, dtype, 0, &c));
+                    next.push_back(Branch{c, 0, {}});
+                    QF_CUDA(cudaMemcpyAsync(c->d, b.sv->d, b.sv->bytes(), cudaMemcpyDeviceToDevice, ctx->stream));
+                } else {
+                    next.push_back(Branch{c, 0, {}});
+                    b.sv = nullptr;
+                }
+                QF_TRY(collapse(c, o.q0, out, std::sqrt(prob[out])));
+                next.back().reg = (b.reg & ~(1ULL << o.param)) | ((uint64_t)out << o.param);
+                next.back().shots = std::move(go[out]);
+            }
+        }
+        for (Branch &b : br)
+            if (b.sv) free_state(b.sv);
+        br.swap(next);
+        next.clear();
+    }
+    QF_TRY(flush());
+    if (T < n_ops) {  // terminal measurements: the prefix-tree sampler per branch
+        std::vector<uint32_t> tq, tc;
+        uint64_t tmask = 0;
+        for (uint64_t k = T; k < n_ops; ++k) {
+            tq.push_back(ops[k].q0);
+            tc.push_back(ops[k].param);
+            tmask |= 1ULL << ops[k].param;
+        }
+        for (Branch &b : br) {
+            std::vector<uint64_t> starts(b.shots.size()), out(b.shots.size());
+            for (size_t i = 0; i < b.shots.size(); ++i) starts[i] = st[b.shots[i]];
+            uint64_t t = 0;
+            QF_TRY(sample_shots(b.sv, tq.data(), tc.data(), (uint32_t)tq.size(), b.shots.size(), seed, tie_eps, out.data(), &t,
+                                starts.data()));
+            ties += t;
+            if (outcomes)
+                for (size_t i = 0; i < b.shots.size(); ++i) outcomes[b.shots[i]] = (b.reg & ~tmask) | out[i];
+        }
+    } else if (outcomes) {
+        for (Branch &b : br)
+            for (uint32_t s : b.shots) outcomes[s] = b.reg;
+    }
+    QF_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (n_ties) *n_ties = ties;
+    return QF_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -643,25 +814,37 @@ int qf_run_shots(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint
     const uint64_t width = classical_bit_check(ops, n_ops, &st);
     if (st) return st;
     if (qubits == 0) return fail(QF_ERR_ZERO_QUBITS, "a state vector must contain at least one qubit");
-    // unitary prefix, then measurements only
+    // a unitary prefix then measurements of distinct qubits: one state, the
+    // prefix-tree sampler; anything else (feed-forward, a measurement followed
+    // by gates, a qubit measured twice): the branching engine
     uint64_t first = n_ops;
     for (uint64_t k = 0; k < n_ops; ++k)
         if (ops[k].kind == QF_OP_MEASURE) { first = k; break; }
     std::vector<uint32_t> mq, mc;
+    bool branching = false;
+    uint64_t measured = 0;
     for (uint64_t k = 0; k < n_ops; ++k) {
         if (ops[k].kind == QF_OP_CHANNEL)
             return fail(QF_ERR_OPERATION_REQUIRES_DENSITY_MATRIX, "this circuit operation requires density-matrix simulation");
-        if (ops[k].kind == QF_OP_COND || (k > first && ops[k].kind != QF_OP_MEASURE))
-            return fail(QF_ERR_UNSUPPORTED_OPERATION,
-                        "mid-circuit measurement and feed-forward need the per-shot engine; measurements must follow the last gate");
-        if (ops[k].kind == QF_OP_MEASURE) {
+        if (ops[k].kind == QF_OP_COND || (k > first && ops[k].kind != QF_OP_MEASURE)) branching = true;
+        if (ops[k].kind == QF_OP_MEASURE || ops[k].kind == QF_OP_COND) {
             if (ops[k].q0 >= qubits)
                 return fail(QF_ERR_QUBIT_OUT_OF_RANGE, "qubit index %u is out of range for %u qubits", ops[k].q0, qubits);
+        }
+        if (ops[k].kind == QF_OP_MEASURE) {
+            if ((measured >> ops[k].q0) & 1ULL) branching = true;
+            measured |= 1ULL << ops[k].q0;
             mq.push_back(ops[k].q0);
             mc.push_back(ops[k].param);
         }
     }
     if (width > 64) return fail(QF_ERR_UNSUPPORTED_OPERATION, "classical registers wider than 64 bits are not packed");
+    if (qubits > 63 && !mq.empty()) return fail(QF_ERR_UNSUPPORTED_OPERATION, "measurement masks cover at most 63 qubits");
+    if (branching) {
+        QF_TRY(bind_device(ctx));
+        if (classical_width) *classical_width = (uint32_t)width;
+        return run_shots_branching(ctx, qubits, dtype, ops, n_ops, init_amps, shots, seed, tie_eps, outcomes, n_ties, opts);
+    }
     std::vector<BGate> gates;
     QF_TRY(bind_ops(qubits, ops, first, nullptr, 0, nullptr, 0, -1, 0.0, gates));
     QF_TRY(bind_device(ctx));

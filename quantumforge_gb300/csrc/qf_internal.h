@@ -280,8 +280,12 @@ int fill_zero_state(qf_sv *sv);
 int convert_from_f64(qf_sv *sv, const double *d_src);
 int convert_to_f64(qf_sv *sv, double *d_dst);
 // Sampler.
+// start_states: optional per-shot generator states (host, `shots` entries)
+// replacing the shot-major jump from `seed`.
 int sample_shots(qf_sv *sv, const uint32_t *qubits, const uint32_t *cbits, uint32_t m, uint64_t shots,
-                 uint64_t seed, double tie_eps, uint64_t *outcomes_host, uint64_t *n_ties);
+                 uint64_t seed, double tie_eps, uint64_t *outcomes_host, uint64_t *n_ties,
+                 const uint64_t *start_states = nullptr);
+
 
 // SmallRng jump-ahead (host): state advanced by `steps` calls of next_u64.
 uint64_t rng_jump(uint64_t state, uint64_t steps);

@@ -922,14 +922,19 @@ __device__ __forceinline__ uint64_t gf2_apply(const uint64_t *cols, uint64_t x) 
 }
 
 __global__ void k_shots(const double *__restrict__ tree, uint32_t m, const uint32_t *__restrict__ cbits, uint64_t shots,
-                        uint64_t seed_state, const uint64_t *__restrict__ jump, double tie_eps,
-                        uint64_t *__restrict__ outcomes, unsigned long long *__restrict__ ties, int *__restrict__ err) {
+                        uint64_t seed_state, const uint64_t *__restrict__ jump, const uint64_t *__restrict__ starts,
+                        int normalize, double tie_eps, uint64_t *__restrict__ outcomes, unsigned long long *__restrict__ ties,
+                        int *__restrict__ err) {
     for (uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; s < shots; s += (uint64_t)gridDim.x * blockDim.x) {
         uint64_t x = seed_state;
-        for (int j = 0; j < 64; ++j)
-            if ((s >> j) & 1ULL) x = gf2_apply(jump + 64 * j, x);
+        if (starts) {  // the shot's generator state given (shots of one branch of a feed-forward circuit)
+            x = starts[s];
+        } else {
+            for (int j = 0; j < 64; ++j)
+                if ((s >> j) & 1ULL) x = gf2_apply(jump + 64 * j, x);
+        }
         uint64_t b = 0, reg = 0;
-        double D = 1.0;
+        double D = normalize ? tree[0] : 1.0;  // complex64: probabilities relative to the state's own norm
         unsigned long long nt = 0;
         for (uint32_t k = 0; k < m; ++k) {
             const double J1 = tree[((1ULL << (k + 1)) - 1) + (b | (1ULL << k))];
@@ -957,7 +962,7 @@ __global__ void k_shots(const double *__restrict__ tree, uint32_t m, const uint3
 }
 
 int sample_shots(qf_sv *sv, const uint32_t *qubits, const uint32_t *cbits, uint32_t m, uint64_t shots, uint64_t seed,
-                 double tie_eps, uint64_t *outcomes_host, uint64_t *n_ties) {
+                 double tie_eps, uint64_t *outcomes_host, uint64_t *n_ties, const uint64_t *start_states) {
     qf_ctx *ctx = sv->ctx;
     const uint32_t n = sv->n;
     if (m > 30) return fail(QF_ERR_UNSUPPORTED_OPERATION, "at most 30 terminal measurements are supported, got %u", m);
@@ -976,12 +981,13 @@ int sample_shots(qf_sv *sv, const uint32_t *qubits, const uint32_t *cbits, uint3
     }
     const uint64_t valid = n >= 64 ? ~0ULL : ((1ULL << n) - 1);
     const uint64_t rest = valid & ~seen;
-    // workspace: tree (2^(m+1) doubles) | outcomes (shots u64) | jump (64*64 u64) | mq | cb | ties | err
+    // workspace: tree (2^(m+1) doubles) | outcomes (shots u64) | jump (64*64 u64) | mq | cb | ties | err | starts
     const size_t tree_b = sizeof(double) * ((2ULL << m));
     const size_t out_b = sizeof(uint64_t) * shots;
     const size_t jump_b = sizeof(uint64_t) * 64 * 64;
     const size_t meta_b = 2 * sizeof(uint32_t) * 32 + 64;
-    QF_TRY(ensure_device(&ctx->ws_tree, &ctx->ws_tree_bytes, tree_b + out_b + jump_b + meta_b));
+    const size_t start_b = start_states ? sizeof(uint64_t) * shots : 0;
+    QF_TRY(ensure_device(&ctx->ws_tree, &ctx->ws_tree_bytes, tree_b + out_b + jump_b + meta_b + start_b));
     unsigned char *w = static_cast<unsigned char *>(ctx->ws_tree);
     double *tree = reinterpret_cast<double *>(w);
     uint64_t *d_out = reinterpret_cast<uint64_t *>(w + tree_b);
@@ -990,6 +996,8 @@ int sample_shots(qf_sv *sv, const uint32_t *qubits, const uint32_t *cbits, uint3
     uint32_t *d_cb = d_mq + 32;
     unsigned long long *d_ties = reinterpret_cast<unsigned long long *>(d_cb + 32);
     int *d_err = reinterpret_cast<int *>(d_ties + 1);
+    uint64_t *d_starts = start_states ? reinterpret_cast<uint64_t *>(w + tree_b + out_b + jump_b + meta_b) : nullptr;
+    if (d_starts) QF_CUDA(cudaMemcpyAsync(d_starts, start_states, start_b, cudaMemcpyHostToDevice, ctx->stream));
 
     static thread_local uint64_t jump[64][64];
     rng_jump_matrices(m, jump, 64);
@@ -1021,7 +1029,8 @@ int sample_shots(qf_sv *sv, const uint32_t *qubits, const uint32_t *cbits, uint3
         return z == 0 ? 0x9E3779B97F4A7C15ULL : z;
     }();
     const int sgrid = std::max(1, std::min<int>((int)((shots + 127) / 128), ctx->sm_count * 16));
-    k_shots<<<sgrid, 128, 0, ctx->stream>>>(tree, m, d_cb, shots, seed_state, d_jump, tie_eps, d_out, d_ties, d_err);
+    k_shots<<<sgrid, 128, 0, ctx->stream>>>(tree, m, d_cb, shots, seed_state, d_jump, d_starts, sv->dtype == QF_C64 ? 1 : 0,
+                                            tie_eps, d_out, d_ties, d_err);
     QF_CUDA(cudaGetLastError());
     if (outcomes_host)
         QF_CUDA(cudaMemcpyAsync(outcomes_host, d_out, out_b, cudaMemcpyDeviceToHost, ctx->stream));

@@ -101,7 +101,18 @@ def test_cuda_resident_measurement_matches_the_cpu_reference(backend):  # :602-6
     assert close(sv.amplitudes(), cpu, 1e-12)
 
 
-def test_feedforward_circuit_is_rejected_by_the_terminal_sampler(backend):  # :649-676 circuit
+def _shots_vs_oracle(backend, c, n, shots, seed, dtype="c128", tie_eps=1e-12):
+    """Per-shot outcomes of the branching engine against the oracle's literal
+    per-shot re-simulation (run_shots_impl); a shot may differ only where a
+    decision fell within tie_eps of P(1) (counted by the engine)."""
+    got, width, ties = c.run_shots_packed(n, shots, seed, dtype=dtype, backend=backend, tie_eps=tie_eps)
+    want, w2 = O.run_shots(c.ops(), n, shots, seed, literal=True)
+    assert width == w2
+    assert int((got != want).sum()) <= ties, (int((got != want).sum()), ties)
+    return got, width, ties
+
+
+def test_feedforward_circuit_matches_the_reference_engine(backend):  # tests/quantum_core.rs:649-676, seed 721
     c = Circuit()
     c.push(Gate.H, 0)
     c.push(Gate.H, 1)
@@ -109,9 +120,57 @@ def test_feedforward_circuit_is_rejected_by_the_terminal_sampler(backend):  # :6
     c.if_classical_bit(0, 1, Gate.X, 2)
     c.measure(1, 1)
     c.measure(2, 2)
-    with pytest.raises(QuantumError) as e:
-        c.run_shots(3, 64, 721, backend=backend)
-    assert e.value.kind == "UnsupportedOperation"
+    got, width, ties = _shots_vs_oracle(backend, c, 3, 64, 721)
+    assert ties == 0
+    res = c.run_shots(3, 64, 721, backend=backend)
+    assert sum(res.counts.values()) == 64
+    assert set(res.counts) == {(0, 0, 0), (1, 1, 1), (0, 1, 0), (1, 0, 1)}
+
+
+def test_classical_condition_circuit_matches_the_reference_engine(backend):  # tests/quantum_core.rs:747-766
+    c = Circuit()
+    c.push(Gate.H, 0)
+    c.measure(0, 0)
+    c.if_classical_bit(0, 1, Gate.X, 1)
+    c.measure(1, 1)
+    got, width, ties = _shots_vs_oracle(backend, c, 2, 512, 991)
+    assert ties == 0 and set(c.run_shots(2, 512, 991, backend=backend).counts) == {(0, 0), (1, 1)}
+
+
+def _mid_circuit(n, seed):
+    r = np.random.default_rng(seed)
+    c = Circuit.from_ops(W.random_circuit(n, 3, seed, two_qubit="mixed"))
+    for k in range(4):  # a measurement, conditionals on it, more gates
+        q = int(r.integers(0, n))
+        c.measure(q, k)
+        for _ in range(2):
+            c.if_classical_bit(k, int(r.integers(0, 2)), Gate(int(r.integers(1, 12)), float(r.uniform(-3, 3))),
+                               int(r.integers(0, n)))
+        for op in W.random_circuit(n, 1, seed + 10 * k, two_qubit="ladder"):
+            c.operations.append((int(op["kind"]), int(op["gate"]), int(op["q0"]), int(op["q1"]), 0, float(op["theta"]), 0))
+    c.measure(0, 4)  # qubit 0 may already have been measured: a repeated measurement
+    for q in range(1, min(n, 6)):  # a terminal block of distinct qubits
+        c.measure(q, 4 + q)
+    return c
+
+
+# complex128 decisions equal the reference's except within 1e-12 of P(1);
+# complex64 states carry f32 rounding through the collapses: window 2e-5
+@pytest.mark.parametrize("n,seed,dtype,tie", [(6, 1, "c128", 1e-12), (9, 2, "c128", 1e-12), (10, 3, "c64", 2e-5),
+                                              (8, 4, "c64", 2e-5)])
+def test_mid_circuit_measurement_and_feed_forward_match_the_reference_engine(backend, n, seed, dtype, tie):
+    c = _mid_circuit(n, seed)
+    got, width, ties = _shots_vs_oracle(backend, c, n, 1500, 100 + seed, dtype=dtype, tie_eps=tie)
+    assert len(set(got.tolist())) > 1
+
+
+def test_repeated_measurement_repeats_the_outcome(backend):
+    c = Circuit()
+    c.push(Gate.H, 0)
+    c.measure(0, 0)
+    c.measure(0, 1)
+    got, width, ties = _shots_vs_oracle(backend, c, 1, 256, 5)
+    assert set(got.tolist()) <= {0, 3}
 
 
 # ---- random circuits -------------------------------------------------------------
