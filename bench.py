@@ -26,6 +26,8 @@ import threading
 import time
 from pathlib import Path
 
+import numpy as np
+
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
@@ -49,7 +51,7 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true")
-    ap.add_argument("--extras", default="vqe24,qaoa4096,shots20,vqe32",
+    ap.add_argument("--extras", default="vqe24,qaoa4096,shots20,shots_ff,vqe32",
                     help="comma-separated extra workloads to run after the headline")
     ap.add_argument("--vqe-qubits", type=int, default=32, help="qubits of the checkpointed-adjoint extra (vqe32)")
     ap.add_argument("--qaoa-instances", type=int, default=4096, help="instances of the batched QAOA extra (qaoa4096)")
@@ -333,6 +335,8 @@ def run_ours(args):
             extra["qaoa4096"] = qaoa_batch(backend, cpu=not args.no_cpu_baseline, count=args.qaoa_instances)
         if "shots20" in wanted:
             extra["shots20"] = shots20(backend, cpu=not args.no_cpu_baseline)
+        if "shots_ff" in wanted:
+            extra["shots_ff"] = shots_feedforward(backend, cpu=not args.no_cpu_baseline)
         if "vqe32" in wanted:
             extra["vqe32"] = vqe32_checkpointed(backend, args.vqe_qubits)
     if rank == 0 and not args.no_cpu_baseline:
@@ -406,6 +410,58 @@ def shots20(backend, cpu: bool):
         t2 = time.perf_counter() - t0
         out["cpu_literal_shots_per_s"] = 2 / t2
         out["cpu_sample"] = "2 shots of the literal per-shot re-simulation (oracle restating run_shots_impl, one thread)"
+    return out
+
+
+def feedforward_circuit(n=20, seed=7):
+    """C1's circuit (depth-20 random H/RX/RY/RZ + CNOT ladders) cut into four
+    parts by three mid-circuit measurements, each followed by classically
+    conditioned corrections (X, H, Rz) on other qubits, then measure(q, q) for
+    every qubit."""
+    import quantumforge_gb300 as qf
+    from quantumforge_gb300 import workloads as W
+
+    body = W.random_circuit(n, 20, seed)
+    c = qf.Circuit()
+    parts = np.array_split(np.arange(len(body)), 4)
+    for k, idx in enumerate(parts):
+        for i in idx:
+            r = body[i]
+            c.operations.append((int(r["kind"]), int(r["gate"]), int(r["q0"]), int(r["q1"]), 0, float(r["theta"]), 0))
+        if k < 3:
+            q = (5 * k + 3) % n
+            c.measure(q, q)
+            c.if_classical_bit(q, 1, qf.Gate.X, (q + 1) % n)
+            c.if_classical_bit(q, 0, qf.Gate.H, (q + 7) % n)
+            c.if_classical_bit(q, 1, qf.Gate.Rz(0.7), (q + 11) % n)
+    for q in range(n):
+        c.measure(q, q)
+    return c
+
+
+def shots_feedforward(backend, cpu: bool):
+    """10^5 seeded shots of a 20-qubit complex128 circuit with three mid-circuit
+    measurements and feed-forward: the branching shot engine, its first shots
+    against the oracle's literal per-shot engine (run_shots_impl)."""
+    import oracle as O
+
+    n, shots, seed = 20, 100_000, 42
+    c = feedforward_circuit(n)
+    c.run_shots_packed(n, shots, seed, dtype="c128", backend=backend, tie_eps=1e-12)  # warm (compiles nothing; allocs)
+    t0 = time.perf_counter()
+    got, width, ties = c.run_shots_packed(n, shots, seed, dtype="c128", backend=backend, tie_eps=1e-12)
+    dt = time.perf_counter() - t0
+    out = {"qubits": n, "ops": len(c.operations), "mid_circuit_measurements": 3, "shots": shots, "seed": seed,
+           "engine_call_s": dt, "engine_shots_per_s": shots / dt, "ties": int(ties),
+           "distinct_outcomes": int(len(np.unique(got)))}
+    k = 3  # the literal engine re-simulates every shot: compare the first shots
+    t0 = time.perf_counter()
+    want, _ = O.run_shots(c.ops(), n, k, seed, literal=True)
+    tl = time.perf_counter() - t0
+    out["first_shots_equal_oracle"] = bool(np.array_equal(got[:k], want))
+    if cpu:
+        out["cpu_literal_shots_per_s"] = k / tl
+        out["cpu_sample"] = f"{k} shots of the literal per-shot re-simulation (oracle restating run_shots_impl, one thread)"
     return out
 
 

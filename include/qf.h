@@ -272,13 +272,17 @@ int qf_run_circuit(qf_ctx *ctx, uint32_t qubits, int dtype,
                    const double *init_amps, double *out_amps, uint64_t n_doubles,
                    const qf_exec_opts *opts);
 
-/* Circuit::run_shots (src/lib.rs:2822-2916) for circuits whose measurements
- * all follow the last gate (the CLI `shots` form, src/bin/main.rs:574-602),
- * sampled from the pre-measurement state with the reference's shot-major
- * SmallRng stream. `outcomes` receives one packed classical register per shot
- * (bit c = classical bit c, width <= 64); NULL skips it. `n_ties` counts
- * decisions with |u - p_one| < tie_eps (outcomes that rounding could flip).
- * Mid-circuit measurement or feed-forward returns QF_ERR_UNSUPPORTED_OPERATION. */
+/* Circuit::run_shots (src/lib.rs:2822-2916) with the reference's shot-major
+ * SmallRng stream (one draw per Measure). Circuits whose measurements all
+ * follow the last gate (the CLI `shots` form, src/bin/main.rs:574-602) are
+ * sampled from the one pre-measurement state; mid-circuit measurements,
+ * repeated measurements and ConditionalSingleQubit feed-forward (QF_OP_COND)
+ * run as a tree of measurement branches, one device state per branch reached.
+ * `outcomes` receives one packed classical register per shot (bit c =
+ * classical bit c, width <= 64); NULL skips it. `n_ties` counts decisions with
+ * |u - p_one| < tie_eps (outcomes that rounding could flip). Channels return
+ * QF_ERR_OPERATION_REQUIRES_DENSITY_MATRIX as the reference's noiseless
+ * run_shots does. */
 int qf_run_shots(qf_ctx *ctx, uint32_t qubits, int dtype,
                  const qf_op *ops, uint64_t n_ops, const double *init_amps,
                  uint64_t shots, uint64_t seed, double tie_eps,
