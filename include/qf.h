@@ -29,6 +29,7 @@
 
 #include <stddef.h>
 #include <stdint.h>
+#include <string.h>
 
 #ifdef __cplusplus
 extern "C" {
@@ -87,7 +88,9 @@ enum qf_op_kind {
     QF_OP_CNOT = 1,       /* control q0, target q1 */
     QF_OP_CZ = 2,         /* first q0, second q1 */
     QF_OP_SWAP = 3,       /* first q0, second q1 */
-    QF_OP_CHANNEL = 4,    /* noise channel on q0: state-vector calls reject it like the reference */
+    QF_OP_CHANNEL = 4,    /* noise channel `gate` (enum qf_channel) on q0, theta = probability / rate;
+                             state-vector calls reject it like the reference; trajectories in
+                             qf_run_shots_with_noise */
     QF_OP_MEASURE = 5,    /* measure q0 into classical bit `param` */
     QF_OP_COND = 6,       /* if classical bit `param` == flags&1 apply gate on q0 */
     QF_OP_ROTATION = 7,   /* ParameterizedOp::Rotation: axis in `gate` (QF_PAULI_*), q0, parameter index `param` */
@@ -104,6 +107,32 @@ typedef struct qf_op {
     uint32_t param;  /* parameter / input / classical-bit index */
     double theta;    /* fixed angle of a GATE/COND with RX/RY/RZ */
 } qf_op;
+
+/* Noise channels (`enum NoiseChannel`, src/lib.rs:1561-1600), in the `gate`
+ * field of a QF_OP_CHANNEL record: Depolarizing { probability = theta },
+ * AmplitudeDamping { gamma = theta }, PhaseDamping { gamma = theta },
+ * ThermalDamping { gamma_down = theta, beta_delta = qf_op_aux(op) }. */
+enum qf_channel {
+    QF_CHANNEL_DEPOLARIZING = 0,
+    QF_CHANNEL_AMPLITUDE_DAMPING = 1,
+    QF_CHANNEL_PHASE_DAMPING = 2,
+    QF_CHANNEL_THERMAL_DAMPING = 3
+};
+
+/* A channel's second parameter: the double whose bits are
+ * ((uint64_t)param << 32) | q1 (both unused by one-qubit channels). */
+static inline double qf_op_aux(const qf_op *op) {
+    const uint64_t bits = ((uint64_t)op->param << 32) | (uint64_t)op->q1;
+    double v;
+    memcpy(&v, &bits, sizeof v);
+    return v;
+}
+static inline void qf_op_set_aux(qf_op *op, double v) {
+    uint64_t bits;
+    memcpy(&bits, &v, sizeof bits);
+    op->q1 = (uint32_t)(bits & 0xFFFFFFFFu);
+    op->param = (uint32_t)(bits >> 32);
+}
 
 /* One Pauli-string term c * P with P = (x-mask, z-mask): bit q set in both
  * masks is Y on qubit q, only in xmask is X, only in zmask is Z. The action
@@ -288,6 +317,16 @@ int qf_run_shots(qf_ctx *ctx, uint32_t qubits, int dtype,
                  uint64_t shots, uint64_t seed, double tie_eps,
                  uint64_t *outcomes, uint32_t *classical_width, uint64_t *n_ties,
                  const qf_exec_opts *opts);
+
+/* Circuit::run_shots_with_noise (src/lib.rs:2829-2840): run_shots with
+ * channel trajectories (apply_channel_trajectory, src/lib.rs:1356-1506, one
+ * draw per channel from the shot's stream) and the initial state normalized.
+ * Same arguments and results as qf_run_shots. */
+int qf_run_shots_with_noise(qf_ctx *ctx, uint32_t qubits, int dtype,
+                             const qf_op *ops, uint64_t n_ops, const double *init_amps,
+                             uint64_t shots, uint64_t seed, double tie_eps,
+                             uint64_t *outcomes, uint32_t *classical_width, uint64_t *n_ties,
+                             const qf_exec_opts *opts);
 
 /* Sampling on a resident state: measure `qubit_order[j]` into classical bit
  * `classical_bits[j]` for j < m, for `shots` shots of the stream seeded by

@@ -49,6 +49,9 @@ def lib():
             "qfo_sv_expectation_pauli_sum": ([P, U32, P, U64, P], C.c_int),
             "qfo_run_ops": ([P, U32, P, U64, P, U64, P, U64, I64, F64, C.c_int], C.c_int),
             "qfo_run_shots_literal": ([P, U32, P, U64, U64, U64, P, C.POINTER(U32)], C.c_int),
+            "qfo_run_shots_noisy_literal": ([P, U32, P, U64, U64, U64, P, C.POINTER(U32)], C.c_int),
+            "qfo_sv_normalize": ([P, U32], C.c_int),
+            "qfo_sv_channel_trajectory": ([P, U32, C.c_int, F64, F64, U32, C.POINTER(U64)], C.c_int),
             "qfo_run_shots_tree": ([P, U32, P, U64, U64, U64, P, C.POINTER(U32), C.c_int], C.c_int),
             "qfo_parameter_shift_gradient": ([U32, P, U64, P, U64, P, U64, P, U64, P, C.c_int], C.c_int),
             "qfo_finite_difference_gradient": ([U32, P, U64, P, U64, P, U64, P, U64, F64, P, C.c_int], C.c_int),
@@ -164,17 +167,30 @@ def measure(a, q: int, rng: Rng) -> int:
     return o.value
 
 
+def channel_trajectory(a, kind: int, p: float, q: int, rng: Rng, beta_delta: float = 0.0) -> None:
+    """apply_channel_trajectory in place on `a` (one draw from `rng`)."""
+    _chk(lib().qfo_sv_channel_trajectory(_p(a), a.size.bit_length() - 1, kind, p, beta_delta, q, C.byref(rng.state)))
+
+
+def normalize(a) -> None:
+    _chk(lib().qfo_sv_normalize(_p(a), a.size.bit_length() - 1))
+
+
 def pauli_expectation(a, terms: np.ndarray) -> complex:
     out = np.zeros(2)
     _chk(lib().qfo_sv_expectation_pauli_sum(_p(a), a.size.bit_length() - 1, _p(terms), len(terms), _p(out)))
     return complex(out[0], out[1])
 
 
-def run_shots(ops, n, shots, seed, init=None, literal=False, threads=0):
+def run_shots(ops, n, shots, seed, init=None, literal=False, threads=0, noise=False):
+    """Circuit::run_shots (noise=False) or run_shots_with_noise (noise=True,
+    always the literal per-shot form): (packed outcomes, register width)."""
     a = zero(n) if init is None else np.ascontiguousarray(init, dtype=np.complex128)
     out = np.zeros(shots, dtype=np.uint64)
     w = U32()
-    if literal:
+    if noise:
+        _chk(lib().qfo_run_shots_noisy_literal(_p(a), n, _p(ops), len(ops), shots, seed, _p(out), C.byref(w)))
+    elif literal:
         _chk(lib().qfo_run_shots_literal(_p(a), n, _p(ops), len(ops), shots, seed, _p(out), C.byref(w)))
     else:
         _chk(lib().qfo_run_shots_tree(_p(a), n, _p(ops), len(ops), shots, seed, _p(out), C.byref(w), threads))

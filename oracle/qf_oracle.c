@@ -274,6 +274,126 @@ int qfo_sv_measure(double *amps, uint32_t n, uint32_t qubit, uint64_t *rng_state
     return 0;
 }
 
+/* StateVector::normalize (src/lib.rs:1005-1014): divide by sqrt(norm_sqr). */
+int qfo_sv_normalize(double *amps, uint32_t n) {
+    const double norm = sqrt(qfo_sv_norm_sqr(amps, n));
+    if (norm == 0.0 || !isfinite(norm)) return QF_ERR_INVALID_PROBABILITY;
+    cplx *a = (cplx *)amps;
+    const uint64_t dim = 1ULL << n;
+    for (uint64_t i = 0; i < dim; ++i) a[i] = c_divf(a[i], norm);
+    return 0;
+}
+
+/* validate_probability (src/lib.rs:2229-2235). */
+static int valid_probability(double p) { return isfinite(p) && p >= 0.0 && p <= 1.0; }
+
+/* Sequential index-order sum of norm_sqr over the amplitudes whose `mask` bit
+ * is set (the probability_one of src/lib.rs:1390-1396 and :1449-1455). */
+static double p_one_sum(const cplx *a, uint64_t dim, uint64_t mask) {
+    double s = SUM_INIT;
+    for (uint64_t i = 0; i < dim; ++i)
+        if (i & mask) s += c_norm_sqr(a[i]);
+    return s;
+}
+
+static double clamp01(double x) { return x < 0.0 ? 0.0 : (x > 1.0 ? 1.0 : x); }
+
+/* StateVector::apply_channel_trajectory (src/lib.rs:1356-1506): one uniform
+ * from the shot's stream selects a Kraus branch, which is applied and
+ * renormalised. Thermal rates follow NoiseChannel::thermal_rates
+ * (src/lib.rs:1611-1626): gamma_up = gamma_down * exp(-beta_delta). */
+int qfo_sv_channel_trajectory(double *amps, uint32_t n, int channel, double p, double beta_delta, uint32_t qubit,
+                              uint64_t *rng_state) {
+    if (qubit >= n) return QF_ERR_QUBIT_OUT_OF_RANGE;
+    cplx *a = (cplx *)amps;
+    const uint64_t mask = 1ULL << qubit, dim = 1ULL << n;
+    if (channel == QF_CHANNEL_DEPOLARIZING) {
+        if (!valid_probability(p)) return QF_ERR_INVALID_PROBABILITY;
+        const double sample = qfo_rng_next_f64(rng_state);
+        if (sample >= 1.0 - p && p > 0.0) {
+            double b = floor((sample - (1.0 - p)) * (3.0 / p));
+            unsigned branch = b >= 255.0 ? 255u : (unsigned)b; /* `as u8` saturates */
+            const int gate = branch == 0 ? QF_GATE_X : (branch == 1 ? QF_GATE_Y : QF_GATE_Z);
+            return qfo_sv_apply(amps, n, gate, 0.0, qubit, 0);
+        }
+        return 0;
+    }
+    if (channel == QF_CHANNEL_AMPLITUDE_DAMPING || channel == QF_CHANNEL_PHASE_DAMPING) {
+        const double gamma = p;
+        if (!valid_probability(gamma)) return QF_ERR_INVALID_PROBABILITY;
+        const double norm = qfo_sv_norm_sqr(amps, n);
+        if (!isfinite(norm) || norm <= DBL_EPSILON) return QF_ERR_INVALID_PROBABILITY;
+        const double probability_one = p_one_sum(a, dim, mask);
+        const double jump_probability = clamp01(gamma * probability_one / norm);
+        const int jump = qfo_rng_next_f64(rng_state) < jump_probability;
+        const double branch_norm = jump ? gamma * probability_one : norm - gamma * probability_one;
+        if (!isfinite(branch_norm) || branch_norm <= DBL_EPSILON) return QF_ERR_INVALID_PROBABILITY;
+        const double inverse_norm = 1.0 / sqrt(branch_norm);
+        if (jump) {
+            const double scale = sqrt(gamma) * inverse_norm;
+            for (uint64_t base = 0; base < dim; ++base) {
+                if (base & mask) continue;
+                const uint64_t excited = base | mask;
+                const cplx value = c_mulf(a[excited], scale);
+                if (channel == QF_CHANNEL_AMPLITUDE_DAMPING) {
+                    a[base] = value;
+                    a[excited] = c_new(0.0, 0.0);
+                } else {
+                    a[base] = c_new(0.0, 0.0);
+                    a[excited] = value;
+                }
+            }
+        } else {
+            const double excited_scale = sqrt(1.0 - gamma) * inverse_norm;
+            for (uint64_t i = 0; i < dim; ++i) a[i] = c_mulf(a[i], (i & mask) == 0 ? inverse_norm : excited_scale);
+        }
+        return 0;
+    }
+    if (channel == QF_CHANNEL_THERMAL_DAMPING) {
+        const double gamma_down = p;
+        if (!valid_probability(gamma_down)) return QF_ERR_INVALID_PROBABILITY;
+        if (!isfinite(beta_delta) || beta_delta < 0.0) return QF_ERR_INVALID_PROBABILITY;
+        const double gamma_up = gamma_down * exp(-beta_delta);
+        const double norm = qfo_sv_norm_sqr(amps, n);
+        if (!isfinite(norm) || norm <= DBL_EPSILON) return QF_ERR_INVALID_PROBABILITY;
+        const double probability_one = p_one_sum(a, dim, mask);
+        const double p1 = clamp01(probability_one / norm);
+        const double p0 = 1.0 - p1;
+        const double down = p1 * gamma_down;
+        const double up = p0 * gamma_up;
+        const double stay = p0 * (1.0 - gamma_up) + p1 * (1.0 - gamma_down);
+        const double sample = qfo_rng_next_f64(rng_state);
+        double branch_norm;
+        int branch;
+        if (sample < down) { branch_norm = down; branch = 1; }
+        else if (sample < down + up) { branch_norm = up; branch = 2; }
+        else { branch_norm = stay; branch = 0; }
+        if (!isfinite(branch_norm) || branch_norm <= DBL_EPSILON) return QF_ERR_INVALID_PROBABILITY;
+        const double inverse_norm = 1.0 / sqrt(branch_norm);
+        if (branch == 1) {
+            const double scale = sqrt(gamma_down) * inverse_norm;
+            for (uint64_t base = 0; base < dim; ++base) {
+                if (base & mask) continue;
+                a[base] = c_mulf(a[base | mask], scale);
+                a[base | mask] = c_new(0.0, 0.0);
+            }
+        } else if (branch == 2) {
+            const double scale = sqrt(gamma_up) * inverse_norm;
+            for (uint64_t base = 0; base < dim; ++base) {
+                if (base & mask) continue;
+                a[base | mask] = c_mulf(a[base], scale);
+                a[base] = c_new(0.0, 0.0);
+            }
+        } else {
+            const double ground_scale = sqrt(1.0 - gamma_up) * inverse_norm;
+            const double excited_scale = sqrt(1.0 - gamma_down) * inverse_norm;
+            for (uint64_t i = 0; i < dim; ++i) a[i] = c_mulf(a[i], (i & mask) == 0 ? ground_scale : excited_scale);
+        }
+        return 0;
+    }
+    return QF_ERR_INVALID_ARGUMENT;
+}
+
 /* PauliWord::apply_basis_index (src/analytic.rs:2629-2650): P|i> = phase |i'>.
  * Qubits are visited in increasing order; phases are exact (+-1, +-i). */
 static uint64_t pauli_apply_basis_index(uint64_t xmask, uint64_t zmask, uint32_t n, uint64_t index, cplx *phase) {
@@ -417,12 +537,14 @@ static int classical_width(const qf_op *ops, uint64_t n_ops, uint32_t *width) {
     return 0;
 }
 
-/* Circuit::run_shots_impl without noise (src/lib.rs:2842-2916): every shot
- * clones the initial state and re-runs every op; all measurements draw from
- * one SmallRng in shot-major order. outcomes[s] packs classical bit c at bit c
- * (registers wider than 64 bits are rejected here). */
-int qfo_run_shots_literal(const double *init_amps, uint32_t n, const qf_op *ops, uint64_t n_ops,
-                          uint64_t shots, uint64_t seed, uint64_t *outcomes, uint32_t *width) {
+/* Circuit::run_shots_impl (src/lib.rs:2842-2916): every shot clones the
+ * initial state (normalised first when allow_noise) and re-runs every op;
+ * measurements and channel trajectories draw from one SmallRng in shot-major
+ * order. Without allow_noise a channel is rejected as density-matrix work.
+ * outcomes[s] packs classical bit c at bit c (registers wider than 64 bits
+ * are rejected here). */
+static int run_shots_literal(const double *init_amps, uint32_t n, const qf_op *ops, uint64_t n_ops, uint64_t shots,
+                             uint64_t seed, int allow_noise, uint64_t *outcomes, uint32_t *width) {
     if (shots == 0) return QF_ERR_INVALID_SHOT_COUNT;
     uint32_t w;
     int st = classical_width(ops, n_ops, &w);
@@ -430,11 +552,19 @@ int qfo_run_shots_literal(const double *init_amps, uint32_t n, const qf_op *ops,
     if (w > 64) return QF_ERR_UNSUPPORTED_OPERATION;
     *width = w;
     const uint64_t dim = 1ULL << n;
+    double *start = (double *)malloc(sizeof(double) * 2 * dim);
     double *state = (double *)malloc(sizeof(double) * 2 * dim);
-    if (!state) return QF_ERR_MEMORY_ALLOCATION_FAILED;
+    if (!start || !state) {
+        free(start);
+        free(state);
+        return QF_ERR_MEMORY_ALLOCATION_FAILED;
+    }
+    memcpy(start, init_amps, sizeof(double) * 2 * dim);
+    /* normalize() gives the same state in every shot: done once */
+    if (allow_noise) st = qfo_sv_normalize(start, n);
     uint64_t rng = qfo_rng_seeded(seed);
     for (uint64_t s = 0; s < shots && !st; ++s) {
-        memcpy(state, init_amps, sizeof(double) * 2 * dim);
+        memcpy(state, start, sizeof(double) * 2 * dim);
         uint64_t classical = 0;
         for (uint64_t k = 0; k < n_ops && !st; ++k) {
             const qf_op *op = &ops[k];
@@ -445,14 +575,28 @@ int qfo_run_shots_literal(const double *init_amps, uint32_t n, const qf_op *ops,
             } else if (op->kind == QF_OP_COND) {
                 if (((classical >> op->param) & 1ULL) == (uint64_t)(op->flags & 1))
                     st = qfo_sv_apply(state, n, op->gate, op->theta, op->q0, 0);
+            } else if (op->kind == QF_OP_CHANNEL && allow_noise) {
+                st = qfo_sv_channel_trajectory(state, n, op->gate, op->theta, qf_op_aux(op), op->q0, &rng);
             } else {
                 st = apply_op(state, n, op, NULL, 0, NULL, 0, (int64_t)k, -1, 0.0, 0);
             }
         }
         outcomes[s] = classical;
     }
+    free(start);
     free(state);
     return st;
+}
+
+int qfo_run_shots_literal(const double *init_amps, uint32_t n, const qf_op *ops, uint64_t n_ops,
+                          uint64_t shots, uint64_t seed, uint64_t *outcomes, uint32_t *width) {
+    return run_shots_literal(init_amps, n, ops, n_ops, shots, seed, 0, outcomes, width);
+}
+
+/* Circuit::run_shots_with_noise (src/lib.rs:2829-2840). */
+int qfo_run_shots_noisy_literal(const double *init_amps, uint32_t n, const qf_op *ops, uint64_t n_ops,
+                                uint64_t shots, uint64_t seed, uint64_t *outcomes, uint32_t *width) {
+    return run_shots_literal(init_amps, n, ops, n_ops, shots, seed, 1, outcomes, width);
 }
 
 /* Memoised exact form of run_shots_impl for circuits whose measurements all

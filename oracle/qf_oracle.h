@@ -47,6 +47,11 @@ double qfo_sv_norm_sqr(const double *amps, uint32_t n);
 void qfo_sv_probabilities(const double *amps, uint32_t n, double *out);
 int qfo_sv_expectation(const double *amps, uint32_t n, int observable, uint32_t qubit, double *out);
 int qfo_sv_measure(double *amps, uint32_t n, uint32_t qubit, uint64_t *rng_state, uint8_t *outcome);
+int qfo_sv_normalize(double *amps, uint32_t n);
+/* apply_channel_trajectory: `channel` is enum qf_channel, p the probability /
+ * gamma / gamma_down, beta_delta the thermal channel's second parameter. */
+int qfo_sv_channel_trajectory(double *amps, uint32_t n, int channel, double p, double beta_delta, uint32_t qubit,
+                              uint64_t *rng_state);
 int qfo_sv_expectation_pauli_sum(const double *amps, uint32_t n, const qf_pauli_term *terms,
                                  uint64_t n_terms, double out[2]);
 
@@ -58,6 +63,10 @@ int qfo_run_ops(double *amps, uint32_t n, const qf_op *ops, uint64_t n_ops,
 /* Circuit::run_shots_impl, literal per-shot re-simulation (src/lib.rs:2842-2916). */
 int qfo_run_shots_literal(const double *init_amps, uint32_t n, const qf_op *ops, uint64_t n_ops,
                           uint64_t shots, uint64_t seed, uint64_t *outcomes, uint32_t *width);
+/* Circuit::run_shots_with_noise: the same with channel trajectories and the
+ * initial state normalised (src/lib.rs:2829-2840, 1356-1506). */
+int qfo_run_shots_noisy_literal(const double *init_amps, uint32_t n, const qf_op *ops, uint64_t n_ops,
+                                uint64_t shots, uint64_t seed, uint64_t *outcomes, uint32_t *width);
 /* Exact memoised form of the same for a unitary prefix followed by measures. */
 int qfo_run_shots_tree(const double *init_amps, uint32_t n, const qf_op *ops, uint64_t n_ops,
                        uint64_t shots, uint64_t seed, uint64_t *outcomes, uint32_t *width, int threads);

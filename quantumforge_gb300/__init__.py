@@ -12,6 +12,7 @@ from .core import (
     Circuit,
     CudaBackend,
     Gate,
+    NoiseChannel,
     ParameterizedCircuit,
     PauliSum,
     RotationAxis,
@@ -24,7 +25,7 @@ from .core import (
 from . import gradients
 
 __all__ = [
-    "Circuit", "CudaBackend", "Gate", "ParameterizedCircuit", "PauliSum", "QuantumError", "RotationAxis",
+    "Circuit", "CudaBackend", "Gate", "NoiseChannel", "ParameterizedCircuit", "PauliSum", "QuantumError", "RotationAxis",
     "ShotResult", "SingleQubitObservable", "SmallRng", "StateVector", "default_backend", "gradients",
     "load_library",
 ]

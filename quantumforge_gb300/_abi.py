@@ -48,6 +48,9 @@ PAULI_X, PAULI_Y, PAULI_Z = 0, 1, 2
 # enum qf_op_kind
 OP_GATE, OP_CNOT, OP_CZ, OP_SWAP, OP_CHANNEL, OP_MEASURE, OP_COND, OP_ROTATION, OP_ENCODING = range(9)
 
+# enum qf_channel (order of `enum NoiseChannel`, src/lib.rs:1561-1600)
+CHANNEL_DEPOLARIZING, CHANNEL_AMPLITUDE_DAMPING, CHANNEL_PHASE_DAMPING, CHANNEL_THERMAL_DAMPING = range(4)
+
 # enum qf_dtype
 C64, C128 = 0, 1
 
@@ -142,6 +145,20 @@ def ops_array(records) -> np.ndarray:
         kind, gate, q0, q1, param, theta = r[:6]
         arr[i] = (kind, gate, r[6] if len(r) > 6 else 0, q0, q1, param, theta)
     return arr
+
+
+def aux_fields(value: float) -> tuple[int, int]:
+    """(q1, param) of a channel record whose second parameter is `value`:
+    the float64 bits split as q1 = low 32, param = high 32 (qf_op_set_aux)."""
+    bits = int(np.float64(value).view(np.uint64))
+    return bits & 0xFFFFFFFF, bits >> 32
+
+
+def channel_record(kind: int, target: int, p: float, beta_delta: float = 0.0) -> tuple:
+    """A QF_OP_CHANNEL record: channel `kind` on `target`, theta = probability
+    / gamma / gamma_down, beta_delta (thermal channel) in the aux fields."""
+    q1, param = aux_fields(beta_delta)
+    return (OP_CHANNEL, int(kind), int(target), q1, param, float(p))
 
 
 def terms_array(terms) -> np.ndarray:

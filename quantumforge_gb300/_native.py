@@ -66,6 +66,7 @@ SIGNATURES = {
     "qf_sv_measure": [P, U32, PU64, C.POINTER(C.c_uint8)],
     "qf_run_circuit": [P, U32, C.c_int, P, U64, P, P, U64, P],
     "qf_run_shots": [P, U32, C.c_int, P, U64, P, U64, U64, F64, P, PU32, PU64, P],
+    "qf_run_shots_with_noise": [P, U32, C.c_int, P, U64, P, U64, U64, F64, P, PU32, PU64, P],
     "qf_sv_sample": [P, P, P, U32, U64, U64, F64, P, PU64],
     "qf_gradient": [P, U32, P, U64, P, U64, P, U64, P, U64, P, P, P, P],
     "qf_expectation": [P, U32, C.c_int, P, U64, P, U64, P, U64, P, U64, P, PF64],

@@ -268,6 +268,15 @@ class CudaBackend:
                           tie_eps: float = 0.0) -> "ShotResult":
         return circuit.run_shots(initial_state, shots, seed, dtype=dtype, backend=self, tie_eps=tie_eps)
 
+    def run_circuit_shots_batched(self, initial_state, circuit: "Circuit", shots: int, seed: int, dtype="c128",
+                                  tie_eps: float = 0.0) -> "ShotResult":
+        """CudaBackend::run_circuit_shots_batched (src/cuda.rs:1157-1266): the
+        noise-trajectory semantics when the circuit holds a channel (initial
+        state normalised), plain run_shots otherwise."""
+        noisy = any(op[0] == _abi.OP_CHANNEL for op in circuit.operations)
+        return ShotResult.from_packed(*circuit.run_shots_packed(initial_state, shots, seed, dtype, self, tie_eps,
+                                                                noise=noisy))
+
 
 _default_backend: CudaBackend | None = None
 
@@ -443,6 +452,51 @@ class ShotResult:
         return ShotResult(int(np.asarray(packed).size), counts, ties)
 
 
+class NoiseChannel:
+    """`enum NoiseChannel` (src/lib.rs:1561-1627): a local channel on one qubit.
+    Shots sample one Kraus trajectory per channel (run_shots_with_noise)."""
+
+    __slots__ = ("kind", "p", "beta_delta")
+
+    def __init__(self, kind: int, p: float, beta_delta: float = 0.0):
+        self.kind, self.p, self.beta_delta = int(kind), float(p), float(beta_delta)
+
+    @staticmethod
+    def Depolarizing(probability: float) -> "NoiseChannel":
+        return NoiseChannel(_abi.CHANNEL_DEPOLARIZING, probability)
+
+    @staticmethod
+    def AmplitudeDamping(gamma: float) -> "NoiseChannel":
+        return NoiseChannel(_abi.CHANNEL_AMPLITUDE_DAMPING, gamma)
+
+    @staticmethod
+    def PhaseDamping(gamma: float) -> "NoiseChannel":
+        return NoiseChannel(_abi.CHANNEL_PHASE_DAMPING, gamma)
+
+    @staticmethod
+    def ThermalDamping(gamma_down: float, beta_delta: float) -> "NoiseChannel":
+        return NoiseChannel(_abi.CHANNEL_THERMAL_DAMPING, gamma_down, beta_delta)
+
+    def thermal_rates(self):
+        """(gamma_up, gamma_down) of a thermal channel, else None (src/lib.rs:1611-1626)."""
+        if self.kind != _abi.CHANNEL_THERMAL_DAMPING:
+            return None
+        if not (math.isfinite(self.p) and 0.0 <= self.p <= 1.0) or not (math.isfinite(self.beta_delta) and self.beta_delta >= 0):
+            raise ValueError("invalid thermal damping parameters")
+        return self.p * math.exp(-self.beta_delta), self.p
+
+    def record(self, target: int) -> tuple:
+        return _abi.channel_record(self.kind, target, self.p, self.beta_delta)
+
+    def __eq__(self, other) -> bool:
+        return isinstance(other, NoiseChannel) and (self.kind, self.p, self.beta_delta) == (other.kind, other.p, other.beta_delta)
+
+    def __repr__(self) -> str:
+        names = ["Depolarizing", "AmplitudeDamping", "PhaseDamping", "ThermalDamping"]
+        extra = f", beta_delta={self.beta_delta}" if self.kind == _abi.CHANNEL_THERMAL_DAMPING else ""
+        return f"NoiseChannel.{names[self.kind]}({self.p}{extra})"
+
+
 class Circuit:
     """`Circuit` (src/lib.rs:2517-2916): an op list executed on a device state."""
 
@@ -470,8 +524,8 @@ class Circuit:
     def swap(self, first: int, second: int) -> None:
         self.operations.append((_abi.OP_SWAP, 0, int(first), int(second), 0, 0.0))
 
-    def channel(self, target: int, channel=None) -> None:
-        self.operations.append((_abi.OP_CHANNEL, 0, int(target), 0, 0, 0.0))
+    def channel(self, target: int, channel: NoiseChannel) -> None:
+        self.operations.append(channel.record(int(target)))
 
     def measure(self, target: int, classical_bit: int) -> None:
         self.operations.append((_abi.OP_MEASURE, 0, int(target), 0, int(classical_bit), 0.0))
@@ -502,10 +556,18 @@ class Circuit:
         """Circuit::run_shots (src/lib.rs:2822-2916) for terminal measurements."""
         return ShotResult.from_packed(*self.run_shots_packed(initial_state, shots, seed, dtype, backend, tie_eps, exec_opts))
 
+    def run_shots_with_noise(self, initial_state, shots: int, seed: int, dtype="c128", backend: CudaBackend | None = None,
+                             tie_eps: float = 0.0, exec_opts=None) -> ShotResult:
+        """Circuit::run_shots_with_noise (src/lib.rs:2829-2840): channel
+        trajectories, measurements and feed-forward per shot."""
+        return ShotResult.from_packed(*self.run_shots_packed(initial_state, shots, seed, dtype, backend, tie_eps, exec_opts,
+                                                             noise=True))
+
     def run_shots_packed(self, initial_state, shots: int, seed: int, dtype="c128", backend: CudaBackend | None = None,
-                         tie_eps: float = 0.0, exec_opts=None):
-        """The engine's qf_run_shots result: (packed outcomes, one u64 per shot
-        with classical bit c at bit c; register width; ties)."""
+                         tie_eps: float = 0.0, exec_opts=None, noise: bool = False):
+        """The engine's qf_run_shots (qf_run_shots_with_noise when `noise`)
+        result: (packed outcomes, one u64 per shot with classical bit c at
+        bit c; register width; ties)."""
         backend = backend or default_backend()
         if isinstance(initial_state, StateVector):
             amps = initial_state.amplitudes()
@@ -520,8 +582,9 @@ class Circuit:
         out = np.empty(max(int(shots), 1), dtype=np.uint64)
         width = C.c_uint32()
         ties = C.c_uint64()
-        check(load().qf_run_shots(backend.handle, n, _dtype_code(dtype), ptr(ops), len(ops), ptr(src), int(shots), int(seed),
-                                  float(tie_eps), ptr(out), C.byref(width), C.byref(ties), _exec(exec_opts)))
+        fn = load().qf_run_shots_with_noise if noise else load().qf_run_shots
+        check(fn(backend.handle, n, _dtype_code(dtype), ptr(ops), len(ops), ptr(src), int(shots), int(seed), float(tie_eps),
+                 ptr(out), C.byref(width), C.byref(ties), _exec(exec_opts)))
         return out[: int(shots)], width.value, ties.value
 
 
@@ -574,8 +637,8 @@ class ParameterizedCircuit:
     def swap(self, first: int, second: int) -> None:
         self.operations.append((_abi.OP_SWAP, 0, int(first), int(second), 0, 0.0))
 
-    def channel(self, target: int, channel=None) -> None:
-        self.operations.append((_abi.OP_CHANNEL, 0, int(target), 0, 0, 0.0))
+    def channel(self, target: int, channel: NoiseChannel) -> None:
+        self.operations.append(channel.record(int(target)))
 
     def ops(self) -> np.ndarray:
         return _abi.ops_array(self.operations)

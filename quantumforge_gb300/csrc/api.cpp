@@ -271,29 +271,72 @@ int adjoint_device(qf_ctx *ctx, uint32_t n, const std::vector<BGate> &gates, con
     return QF_OK;
 }
 
-// Circuit::run_shots (src/lib.rs:2842-2916) for circuits with mid-circuit
-// measurements, repeated measurements or ConditionalSingleQubit feed-forward.
-// Shots walk a tree of measurement branches: a branch is one device state
-// with its classical register; unitary segments (with the conditionals that
-// fire for the branch's register) run through the fused engine once per
-// branch; at a measurement every shot of a branch draws its own next uniform
-// (shot s starts at draw s * measurements of SmallRng::seeded(seed), the
-// reference's shot-major stream) against the branch's P(1) and moves to the
-// collapsed child (src/lib.rs:1321-1351). The trailing measurements of
-// distinct qubits use the prefix-tree sampler per branch. Decisions equal the
-// reference's except where |u - P(1)| < tie_eps (counted); complex64 states
-// take P(1) relative to their own norm.
+// One uniform of SmallRng (src/lib.rs:4899-4911) from a shot's state.
+inline double next_uniform(uint64_t *x) {
+    uint64_t v = *x;
+    v ^= v << 13;
+    v ^= v >> 7;
+    v ^= v << 17;
+    *x = v;
+    return (double)(v >> 11) * (1.0 / 9007199254740992.0);
+}
+
+inline bool valid_probability(double p) { return std::isfinite(p) && p >= 0.0 && p <= 1.0; }  // src/lib.rs:2229-2235
+
+inline double clamp01(double x) { return std::min(1.0, std::max(0.0, x)); }
+
+// StateVector::normalize (src/lib.rs:1005-1014): divide by sqrt(norm_sqr).
+int normalize_state(qf_sv *sv) {
+    double nrm;
+    QF_TRY(reduce_norm_sqr(sv, &nrm));
+    const double norm = std::sqrt(nrm);
+    if (norm == 0.0 || !std::isfinite(norm)) return fail(QF_ERR_INVALID_PROBABILITY, "probability must be in [0, 1], got %g", norm);
+    return collapse(sv, 0, -1, norm);
+}
+
+BGate mat1(uint32_t q, double m00, double m01, double m10, double m11) {
+    BGate g;
+    g.kind = BK_MAT1;
+    g.q0 = q;
+    g.m[0] = m00;
+    g.m[2] = m01;
+    g.m[4] = m10;
+    g.m[6] = m11;
+    g.diag = matrix_is_diag(g.m);
+    return g;
+}
+
+// Circuit::run_shots_impl (src/lib.rs:2842-2916) for circuits with
+// mid-circuit measurements, repeated measurements, ConditionalSingleQubit
+// feed-forward or (allow_noise) channel trajectories.
+//
+// Shots walk a tree: a node is one device state with its classical register
+// and the shots that reached it. Unitary segments (with the conditionals that
+// fire for the node's register) run through the fused engine once per node.
+// At a measurement or a channel every shot of the node draws its own next
+// uniform (shot s starts at draw s * draws-per-shot of SmallRng::seeded(seed),
+// the reference's shot-major stream) and the shots split into children:
+// measurement outcomes (collapse, src/lib.rs:1321-1351) or Kraus branches
+// (apply_channel_trajectory, src/lib.rs:1356-1506; the branch matrix is
+// queued in front of the child's next segment). The tree is walked depth
+// first: a parent's state is shared by its children, copied for all but the
+// last one, so at most one state per level of the current path is alive.
+// The trailing measurements of distinct qubits use the prefix-tree sampler
+// per leaf. Decisions equal the reference's except where a uniform lies
+// within tie_eps of a threshold (counted); complex64 states take P(1)
+// relative to their own norm.
 int run_shots_branching(qf_ctx *ctx, uint32_t n, int dtype, const qf_op *ops, uint64_t n_ops, const double *init,
-                        uint64_t shots, uint64_t seed, double tie_eps, uint64_t *outcomes, uint64_t *n_ties,
-                        const qf_exec_opts *opts) {
+                        uint64_t shots, uint64_t seed, double tie_eps, bool allow_noise, uint64_t *outcomes,
+                        uint64_t *n_ties, const qf_exec_opts *opts) {
     // terminal block: the trailing measurements of distinct qubits
     uint64_t T = n_ops, seen = 0;
     while (T > 0 && ops[T - 1].kind == QF_OP_MEASURE && !((seen >> ops[T - 1].q0) & 1ULL)) {
         seen |= 1ULL << ops[T - 1].q0;
         --T;
     }
-    uint64_t m_total = 0;
-    for (uint64_t k = 0; k < n_ops; ++k) m_total += ops[k].kind == QF_OP_MEASURE;
+    uint64_t draws = 0;  // uniforms per shot
+    for (uint64_t k = 0; k < n_ops; ++k)
+        draws += ops[k].kind == QF_OP_MEASURE || (allow_noise && ops[k].kind == QF_OP_CHANNEL);
     // every shot's generator state at its first draw
     std::vector<uint64_t> st(shots);
     {
@@ -304,142 +347,329 @@ int run_shots_branching(qf_ctx *ctx, uint32_t n, int dtype, const qf_op *ops, ui
         uint64_t x = z == 0 ? 0x9E3779B97F4A7C15ULL : z;
         for (uint64_t s = 0; s < shots; ++s) {
             st[s] = x;
-            for (uint64_t k = 0; k < m_total; ++k) {
-                x ^= x << 13;
-                x ^= x >> 7;
-                x ^= x << 17;
-            }
+            for (uint64_t k = 0; k < draws; ++k) next_uniform(&x);
         }
     }
-    struct Branch {
+    // A state shared by the children of one node; the last child to start
+    // takes it over, the others copy it.
+    struct Shared {
         qf_sv *sv;
-        uint64_t reg;
+        int users;
+    };
+    struct Node {
+        Shared *src;                 // parent state (nullptr: `own` is set)
+        qf_sv *own;
+        uint64_t k;                  // next op
+        uint64_t reg;                // classical register
         std::vector<uint32_t> shots;
+        std::vector<BGate> pre;      // Kraus branch matrix to apply first
+        uint32_t mq;                 // measurement child: collapse q
+        int out;                     //   outcome, or -1 for none
+        double scale;                //   sqrt(probability)
     };
-    std::vector<Branch> br, next;
-    struct Guard {  // the device states of every live branch, on every exit
-        std::vector<Branch> *v, *w;
+    std::vector<Node> stack;
+    std::vector<Shared *> shared;
+    std::vector<qf_sv *> spare;  // finished leaves' states, reused for copies
+    qf_sv *cur = nullptr;
+    struct Guard {
+        std::vector<Shared *> *sh;
+        std::vector<Node> *st;
+        std::vector<qf_sv *> *spare;
+        qf_sv **cur;
         ~Guard() {
-            for (std::vector<Branch> *x : {v, w})
-                for (Branch &b : *x)
-                    if (b.sv) free_state(b.sv);
-        }
-    } guard{&br, &next};
-    {
-        qf_sv *root;
-        QF_TRY(alloc_state(ctx, n, dtype, 0, &root));
-        br.push_back(Branch{root, 0, {}});
-        br[0].shots.resize(shots);
-        for (uint64_t s = 0; s < shots; ++s) br[0].shots[s] = (uint32_t)s;
-        if (init) QF_TRY(convert_from_f64(root, init));
-    }
-    std::vector<qf_op> seg;  // pending gates and conditionals
-    auto flush = [&]() -> int {
-        if (seg.empty()) return QF_OK;
-        for (Branch &b : br) {
-            std::vector<qf_op> run;
-            run.reserve(seg.size());
-            for (const qf_op &o : seg) {
-                if (o.kind == QF_OP_COND) {  // ConditionalSingleQubit: apply when classical[bit] == value
-                    if (((b.reg >> o.param) & 1ULL) != (uint64_t)(o.flags & 1)) continue;
-                    qf_op g = o;
-                    g.kind = QF_OP_GATE;
-                    g.param = 0;
-                    g.flags = 0;
-                    run.push_back(g);
-                } else {
-                    run.push_back(o);
-                }
+            for (Shared *x : *sh) {
+                if (x->sv) free_state(x->sv);
+                delete x;
             }
-            std::vector<BGate> gates;
-            QF_TRY(bind_ops(n, run.data(), run.size(), nullptr, 0, nullptr, 0, -1, 0.0, gates));
-            QF_TRY(execute_gates(b.sv, gates, opts));
+            for (Node &nd : *st)
+                if (nd.own) free_state(nd.own);
+            for (qf_sv *x : *spare) free_state(x);
+            if (*cur) free_state(*cur);
         }
-        seg.clear();
-        return QF_OK;
-    };
+    } guard{&shared, &stack, &spare, &cur};
+    {
+        Node root{};
+        QF_TRY(alloc_state(ctx, n, dtype, 0, &root.own));
+        stack.push_back(std::move(root));
+        Node &r = stack.back();
+        r.out = -1;
+        r.shots.resize(shots);
+        for (uint64_t s = 0; s < shots; ++s) r.shots[s] = (uint32_t)s;
+        if (init) {
+            QF_TRY(convert_from_f64(r.own, init));
+            if (allow_noise) QF_TRY(normalize_state(r.own));
+        } else {
+            QF_TRY(fill_zero_state(r.own));
+        }
+    }
+    std::vector<uint32_t> tq, tc;  // terminal block
+    uint64_t tmask = 0;
+    for (uint64_t k = T; k < n_ops; ++k) {
+        tq.push_back(ops[k].q0);
+        tc.push_back(ops[k].param);
+        tmask |= 1ULL << ops[k].param;
+    }
     uint64_t ties = 0;
-    for (uint64_t k = 0; k < T; ++k) {
-        const qf_op &o = ops[k];
-        if (o.kind != QF_OP_MEASURE) {
-            seg.push_back(o);
+    std::vector<qf_op> run;
+    std::vector<BGate> gates;
+    while (!stack.empty()) {
+        Node nd = std::move(stack.back());
+        stack.pop_back();
+        // take or copy the state
+        if (nd.own) {
+            cur = nd.own;
+            nd.own = nullptr;
+        } else if (--nd.src->users == 0) {
+            cur = nd.src->sv;
+            nd.src->sv = nullptr;
+        } else {
+            if (!spare.empty()) {
+                cur = spare.back();
+                spare.pop_back();
+            } else {
+                QF_TRY(alloc_state(ctx, n, dtype, 0, &cur));
+            }
+            QF_CUDA(cudaMemcpyAsync(cur->d, nd.src->sv->d, cur->bytes(), cudaMemcpyDeviceToDevice, ctx->stream));
+        }
+        if (nd.out >= 0) QF_TRY(collapse(cur, nd.mq, nd.out, nd.scale));
+        // the unitary segment up to the next branch point
+        uint64_t k = nd.k;
+        run.clear();
+        for (; k < T; ++k) {
+            const qf_op &o = ops[k];
+            if (o.kind == QF_OP_MEASURE || (o.kind == QF_OP_CHANNEL && allow_noise)) break;
+            if (o.kind == QF_OP_COND) {  // ConditionalSingleQubit: apply when classical[bit] == value
+                if (((nd.reg >> o.param) & 1ULL) != (uint64_t)(o.flags & 1)) continue;
+                qf_op g = o;
+                g.kind = QF_OP_GATE;
+                g.param = 0;
+                g.flags = 0;
+                run.push_back(g);
+            } else {
+                run.push_back(o);
+            }
+        }
+        gates.clear();
+        QF_TRY(bind_ops(n, run.data(), run.size(), nullptr, 0, nullptr, 0, -1, 0.0, gates));
+        if (!nd.pre.empty()) gates.insert(gates.begin(), nd.pre.begin(), nd.pre.end());
+        if (!gates.empty()) QF_TRY(execute_gates(cur, gates, opts));
+        if (k >= T) {  // leaf: the terminal measurements, or the register as it stands
+            if (!tq.empty()) {
+                std::vector<uint64_t> starts(nd.shots.size()), out(nd.shots.size());
+                for (size_t i = 0; i < nd.shots.size(); ++i) starts[i] = st[nd.shots[i]];
+                uint64_t t = 0;
+                QF_TRY(sample_shots(cur, tq.data(), tc.data(), (uint32_t)tq.size(), nd.shots.size(), seed, tie_eps,
+                                    out.data(), &t, starts.data()));
+                ties += t;
+                if (outcomes)
+                    for (size_t i = 0; i < nd.shots.size(); ++i) outcomes[nd.shots[i]] = (nd.reg & ~tmask) | out[i];
+            } else if (outcomes) {
+                for (uint32_t s : nd.shots) outcomes[s] = nd.reg;
+            }
+            spare.push_back(cur);
+            cur = nullptr;
             continue;
         }
-        QF_TRY(flush());
-        next.clear();
-        for (Branch &b : br) {
+        // a branch point: split the node's shots into up to four children
+        const qf_op &o = ops[k];
+        const uint32_t q = o.q0;
+        if (q >= n) return fail(QF_ERR_QUBIT_OUT_OF_RANGE, "qubit index %u is out of range for %u qubits", q, n);
+        std::vector<uint32_t> go[4];
+        BGate mats[4];
+        bool has_mat[4] = {false, false, false, false};
+        double child_norm[4] = {1.0, 1.0, 1.0, 1.0};  // checked for every child that gets shots
+        bool check_norm = false;
+        double prob[2] = {0.0, 0.0};
+        if (o.kind == QF_OP_MEASURE) {
             double p1;
-            QF_TRY(reduce_p_one(b.sv, o.q0, &p1));
+            QF_TRY(reduce_p_one(cur, q, &p1));
             if (dtype == QF_C64) {  // relative to the state's own norm, which f32 rounding moves off 1
                 double nrm;
-                QF_TRY(reduce_norm_sqr(b.sv, &nrm));
+                QF_TRY(reduce_norm_sqr(cur, &nrm));
                 if (nrm > 0.0) p1 /= nrm;
             }
-            p1 = std::min(1.0, std::max(0.0, p1));
-            std::vector<uint32_t> go[2];
-            for (uint32_t s : b.shots) {
-                uint64_t x = st[s];
-                x ^= x << 13;
-                x ^= x >> 7;
-                x ^= x << 17;
-                st[s] = x;
-                const double u = (double)(x >> 11) * (1.0 / 9007199254740992.0);
-                const int out = u < p1 ? 1 : 0;
+            p1 = clamp01(p1);
+            for (uint32_t s : nd.shots) {
+                const double u = next_uniform(&st[s]);
                 if (std::fabs(u - p1) < tie_eps) ++ties;
-                go[out].push_back(s);
+                go[u < p1 ? 1 : 0].push_back(s);
             }
-            double prob[2] = {1.0 - p1, p1};
-            for (int out = 0; out < 2; ++out)
-                if (!go[out].empty() && prob[out] <= 2.220446049250313e-16)
-                    return fail(QF_ERR_INVALID_PROBABILITY, "measurement probability must be in [0, 1], got %g", prob[out]);
-            const int reuse = go[1].empty() ? 0 : 1;  // the branch's own state goes to this child
-            for (int out = 0; out < 2; ++out) {
-                if (go[out].empty()) continue;
-                qf_sv *c = b.sv;
-                if (out != reuse) {  // a copy taken before the shared state is collapsed
-                    QF_TRY(alloc_state(ctx, n, dtype, 0, &c));
-                    next.push_back(Branch{c, 0, {}});
-                    QF_CUDA(cudaMemcpyAsync(c->d, b.sv->d, b.sv->bytes(), cudaMemcpyDeviceToDevice, ctx->stream));
-                } else {
-                    next.push_back(Branch{c, 0, {}});
-                    b.sv = nullptr;
+            prob[0] = 1.0 - p1;
+            prob[1] = p1;
+            for (int c = 0; c < 2; ++c)
+                if (!go[c].empty() && prob[c] <= 2.220446049250313e-16)
+                    return fail(QF_ERR_INVALID_PROBABILITY, "measurement probability must be in [0, 1], got %g", prob[c]);
+        } else if (o.gate == QF_CHANNEL_DEPOLARIZING) {
+            const double p = o.theta;
+            if (!valid_probability(p)) return fail(QF_ERR_INVALID_PROBABILITY, "probability must be in [0, 1], got %g", p);
+            for (uint32_t s : nd.shots) {
+                const double u = next_uniform(&st[s]);
+                int c = 0;
+                if (u >= 1.0 - p && p > 0.0) {
+                    const double b = std::floor((u - (1.0 - p)) * (3.0 / p));
+                    c = 1 + (b >= 2.0 ? 2 : (int)b);  // X, Y, Z
                 }
-                QF_TRY(collapse(c, o.q0, out, std::sqrt(prob[out])));
-                next.back().reg = (b.reg & ~(1ULL << o.param)) | ((uint64_t)out << o.param);
-                next.back().shots = std::move(go[out]);
+                go[c].push_back(s);
             }
+            for (int c = 1; c < 4; ++c) {
+                mats[c].kind = BK_MAT1;
+                mats[c].q0 = q;
+                QF_TRY(gate_matrix(c == 1 ? QF_GATE_X : c == 2 ? QF_GATE_Y : QF_GATE_Z, 0.0, mats[c].m));
+                mats[c].diag = matrix_is_diag(mats[c].m);
+                has_mat[c] = true;
+            }
+        } else if (o.gate == QF_CHANNEL_AMPLITUDE_DAMPING || o.gate == QF_CHANNEL_PHASE_DAMPING) {
+            const double gamma = o.theta;
+            if (!valid_probability(gamma))
+                return fail(QF_ERR_INVALID_PROBABILITY, "probability must be in [0, 1], got %g", gamma);
+            double norm, p_one;
+            QF_TRY(reduce_norm_sqr(cur, &norm));
+            if (!std::isfinite(norm) || norm <= 2.220446049250313e-16)
+                return fail(QF_ERR_INVALID_PROBABILITY, "probability must be in [0, 1], got %g", norm);
+            QF_TRY(reduce_p_one(cur, q, &p_one));
+            const double jump_p = clamp01(gamma * p_one / norm);
+            for (uint32_t s : nd.shots) {
+                const double u = next_uniform(&st[s]);
+                if (std::fabs(u - jump_p) < tie_eps) ++ties;
+                go[u < jump_p ? 1 : 0].push_back(s);
+            }
+            child_norm[1] = gamma * p_one;
+            child_norm[0] = norm - gamma * p_one;
+            check_norm = true;
+            const double inv1 = 1.0 / std::sqrt(child_norm[1]), inv0 = 1.0 / std::sqrt(child_norm[0]);
+            const double s1 = std::sqrt(gamma) * inv1;
+            mats[1] = o.gate == QF_CHANNEL_AMPLITUDE_DAMPING ? mat1(q, 0.0, s1, 0.0, 0.0) : mat1(q, 0.0, 0.0, 0.0, s1);
+            mats[0] = mat1(q, inv0, 0.0, 0.0, std::sqrt(1.0 - gamma) * inv0);
+            has_mat[0] = has_mat[1] = true;
+        } else if (o.gate == QF_CHANNEL_THERMAL_DAMPING) {
+            const double gd = o.theta, beta = qf_op_aux(&o);
+            if (!valid_probability(gd)) return fail(QF_ERR_INVALID_PROBABILITY, "probability must be in [0, 1], got %g", gd);
+            if (!std::isfinite(beta) || beta < 0.0)
+                return fail(QF_ERR_INVALID_PROBABILITY, "probability must be in [0, 1], got %g", beta);
+            const double gu = gd * std::exp(-beta);  // NoiseChannel::thermal_rates (src/lib.rs:1611-1626)
+            double norm, p_one;
+            QF_TRY(reduce_norm_sqr(cur, &norm));
+            if (!std::isfinite(norm) || norm <= 2.220446049250313e-16)
+                return fail(QF_ERR_INVALID_PROBABILITY, "probability must be in [0, 1], got %g", norm);
+            QF_TRY(reduce_p_one(cur, q, &p_one));
+            const double p1 = clamp01(p_one / norm), p0 = 1.0 - p1;
+            const double down = p1 * gd, up = p0 * gu;
+            const double pd = p0 * (1.0 - gu), pe = p1 * (1.0 - gd);
+            const double stay = pd + pe, du = down + up;
+            for (uint32_t s : nd.shots) {
+                const double u = next_uniform(&st[s]);
+                if (std::fabs(u - down) < tie_eps || std::fabs(u - du) < tie_eps) ++ties;
+                go[u < down ? 1 : (u < du ? 2 : 0)].push_back(s);
+            }
+            child_norm[1] = down;
+            child_norm[2] = up;
+            child_norm[0] = stay;
+            check_norm = true;
+            const double inv1 = 1.0 / std::sqrt(down), inv2 = 1.0 / std::sqrt(up), inv0 = 1.0 / std::sqrt(stay);
+            mats[1] = mat1(q, 0.0, std::sqrt(gd) * inv1, 0.0, 0.0);
+            mats[2] = mat1(q, 0.0, 0.0, std::sqrt(gu) * inv2, 0.0);
+            mats[0] = mat1(q, std::sqrt(1.0 - gu) * inv0, 0.0, 0.0, std::sqrt(1.0 - gd) * inv0);
+            has_mat[0] = has_mat[1] = has_mat[2] = true;
+        } else {
+            return fail(QF_ERR_INVALID_ARGUMENT, "unknown noise channel %u", (unsigned)o.gate);
         }
-        for (Branch &b : br)
-            if (b.sv) free_state(b.sv);
-        br.swap(next);
-        next.clear();
-    }
-    QF_TRY(flush());
-    if (T < n_ops) {  // terminal measurements: the prefix-tree sampler per branch
-        std::vector<uint32_t> tq, tc;
-        uint64_t tmask = 0;
-        for (uint64_t k = T; k < n_ops; ++k) {
-            tq.push_back(ops[k].q0);
-            tc.push_back(ops[k].param);
-            tmask |= 1ULL << ops[k].param;
+        if (check_norm)
+            for (int c = 0; c < 4; ++c)
+                if (!go[c].empty() && (!std::isfinite(child_norm[c]) || child_norm[c] <= 2.220446049250313e-16))
+                    return fail(QF_ERR_INVALID_PROBABILITY, "probability must be in [0, 1], got %g", child_norm[c]);
+        int users = 0;
+        for (int c = 0; c < 4; ++c) users += !go[c].empty();
+        Shared *sh = new Shared{cur, users};
+        shared.push_back(sh);
+        cur = nullptr;
+        // pushed in reverse so that child 0 runs first; the last to run takes the state
+        for (int c = 3; c >= 0; --c) {
+            if (go[c].empty()) continue;
+            Node ch{};
+            ch.src = sh;
+            ch.k = k + 1;
+            ch.reg = nd.reg;
+            ch.shots = std::move(go[c]);
+            ch.out = -1;
+            if (o.kind == QF_OP_MEASURE) {
+                ch.reg = (nd.reg & ~(1ULL << o.param)) | ((uint64_t)c << o.param);
+                ch.mq = q;
+                ch.out = c;
+                ch.scale = std::sqrt(prob[c]);
+            } else if (has_mat[c]) {
+                ch.pre.push_back(mats[c]);
+            }
+            stack.push_back(std::move(ch));
         }
-        for (Branch &b : br) {
-            std::vector<uint64_t> starts(b.shots.size()), out(b.shots.size());
-            for (size_t i = 0; i < b.shots.size(); ++i) starts[i] = st[b.shots[i]];
-            uint64_t t = 0;
-            QF_TRY(sample_shots(b.sv, tq.data(), tc.data(), (uint32_t)tq.size(), b.shots.size(), seed, tie_eps, out.data(), &t,
-                                starts.data()));
-            ties += t;
-            if (outcomes)
-                for (size_t i = 0; i < b.shots.size(); ++i) outcomes[b.shots[i]] = (b.reg & ~tmask) | out[i];
-        }
-    } else if (outcomes) {
-        for (Branch &b : br)
-            for (uint32_t s : b.shots) outcomes[s] = b.reg;
     }
     QF_CUDA(cudaStreamSynchronize(ctx->stream));
     if (n_ties) *n_ties = ties;
     return QF_OK;
+}
+
+// Circuit::run_shots / run_shots_with_noise (src/lib.rs:2822-2916): a
+// unitary prefix then measurements of distinct qubits runs as one state and
+// the prefix-tree sampler; anything else (feed-forward, a measurement
+// followed by gates, a qubit measured twice, a channel trajectory) runs in
+// the branching engine.
+int run_shots_entry(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops, const double *init_amps,
+                    uint64_t shots, uint64_t seed, double tie_eps, bool allow_noise, uint64_t *outcomes,
+                    uint32_t *classical_width, uint64_t *n_ties, const qf_exec_opts *opts) {
+    clear_error();
+    if (!ctx) return fail(QF_ERR_INVALID_ARGUMENT, "context is NULL");
+    QF_TRY(check_dtype(dtype));
+    if (shots == 0) return fail(QF_ERR_INVALID_SHOT_COUNT, "shot count must be greater than zero");
+    if (n_ops && !ops) return fail(QF_ERR_INVALID_ARGUMENT, "ops is NULL");
+    int st;
+    const uint64_t width = classical_bit_check(ops, n_ops, &st);
+    if (st) return st;
+    if (qubits == 0) return fail(QF_ERR_ZERO_QUBITS, "a state vector must contain at least one qubit");
+    uint64_t first = n_ops;
+    for (uint64_t k = 0; k < n_ops; ++k)
+        if (ops[k].kind == QF_OP_MEASURE) { first = k; break; }
+    std::vector<uint32_t> mq, mc;
+    bool branching = false;
+    uint64_t measured = 0;
+    for (uint64_t k = 0; k < n_ops; ++k) {
+        if (ops[k].kind == QF_OP_CHANNEL) {
+            if (!allow_noise)
+                return fail(QF_ERR_OPERATION_REQUIRES_DENSITY_MATRIX, "this circuit operation requires density-matrix simulation");
+            branching = true;
+        }
+        if (ops[k].kind == QF_OP_COND || (k > first && ops[k].kind != QF_OP_MEASURE)) branching = true;
+        if (ops[k].kind == QF_OP_MEASURE || ops[k].kind == QF_OP_COND || ops[k].kind == QF_OP_CHANNEL) {
+            if (ops[k].q0 >= qubits)
+                return fail(QF_ERR_QUBIT_OUT_OF_RANGE, "qubit index %u is out of range for %u qubits", ops[k].q0, qubits);
+        }
+        if (ops[k].kind == QF_OP_MEASURE) {
+            if ((measured >> ops[k].q0) & 1ULL) branching = true;
+            measured |= 1ULL << ops[k].q0;
+            mq.push_back(ops[k].q0);
+            mc.push_back(ops[k].param);
+        }
+    }
+    if (width > 64) return fail(QF_ERR_UNSUPPORTED_OPERATION, "classical registers wider than 64 bits are not packed");
+    if (qubits > 63 && !mq.empty()) return fail(QF_ERR_UNSUPPORTED_OPERATION, "measurement masks cover at most 63 qubits");
+    if (branching) {
+        QF_TRY(bind_device(ctx));
+        if (classical_width) *classical_width = (uint32_t)width;
+        return run_shots_branching(ctx, qubits, dtype, ops, n_ops, init_amps, shots, seed, tie_eps, allow_noise, outcomes,
+                                   n_ties, opts);
+    }
+    std::vector<BGate> gates;
+    QF_TRY(bind_ops(qubits, ops, first, nullptr, 0, nullptr, 0, -1, 0.0, gates));
+    QF_TRY(bind_device(ctx));
+    qf_sv *sv;
+    QF_TRY(scratch_state(ctx, &ctx->scratch_sv, qubits, dtype, &sv));
+    if (init_amps) {
+        QF_TRY(convert_from_f64(sv, init_amps));
+        if (allow_noise) QF_TRY(normalize_state(sv));
+    } else {
+        QF_TRY(fill_zero_state(sv));
+    }
+    QF_TRY(execute_gates(sv, gates, opts));
+    if (classical_width) *classical_width = (uint32_t)width;
+    return sample_shots(sv, mq.data(), mc.data(), (uint32_t)mq.size(), shots, seed, tie_eps, outcomes, n_ties);
 }
 
 }  // namespace
@@ -805,56 +1035,15 @@ int qf_sv_sample(qf_sv *sv, const uint32_t *qubit_order, const uint32_t *classic
 int qf_run_shots(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops, const double *init_amps,
                  uint64_t shots, uint64_t seed, double tie_eps, uint64_t *outcomes, uint32_t *classical_width,
                  uint64_t *n_ties, const qf_exec_opts *opts) {
-    clear_error();
-    if (!ctx) return fail(QF_ERR_INVALID_ARGUMENT, "context is NULL");
-    QF_TRY(check_dtype(dtype));
-    if (shots == 0) return fail(QF_ERR_INVALID_SHOT_COUNT, "shot count must be greater than zero");
-    if (n_ops && !ops) return fail(QF_ERR_INVALID_ARGUMENT, "ops is NULL");
-    int st;
-    const uint64_t width = classical_bit_check(ops, n_ops, &st);
-    if (st) return st;
-    if (qubits == 0) return fail(QF_ERR_ZERO_QUBITS, "a state vector must contain at least one qubit");
-    // a unitary prefix then measurements of distinct qubits: one state, the
-    // prefix-tree sampler; anything else (feed-forward, a measurement followed
-    // by gates, a qubit measured twice): the branching engine
-    uint64_t first = n_ops;
-    for (uint64_t k = 0; k < n_ops; ++k)
-        if (ops[k].kind == QF_OP_MEASURE) { first = k; break; }
-    std::vector<uint32_t> mq, mc;
-    bool branching = false;
-    uint64_t measured = 0;
-    for (uint64_t k = 0; k < n_ops; ++k) {
-        if (ops[k].kind == QF_OP_CHANNEL)
-            return fail(QF_ERR_OPERATION_REQUIRES_DENSITY_MATRIX, "this circuit operation requires density-matrix simulation");
-        if (ops[k].kind == QF_OP_COND || (k > first && ops[k].kind != QF_OP_MEASURE)) branching = true;
-        if (ops[k].kind == QF_OP_MEASURE || ops[k].kind == QF_OP_COND) {
-            if (ops[k].q0 >= qubits)
-                return fail(QF_ERR_QUBIT_OUT_OF_RANGE, "qubit index %u is out of range for %u qubits", ops[k].q0, qubits);
-        }
-        if (ops[k].kind == QF_OP_MEASURE) {
-            if ((measured >> ops[k].q0) & 1ULL) branching = true;
-            measured |= 1ULL << ops[k].q0;
-            mq.push_back(ops[k].q0);
-            mc.push_back(ops[k].param);
-        }
-    }
-    if (width > 64) return fail(QF_ERR_UNSUPPORTED_OPERATION, "classical registers wider than 64 bits are not packed");
-    if (qubits > 63 && !mq.empty()) return fail(QF_ERR_UNSUPPORTED_OPERATION, "measurement masks cover at most 63 qubits");
-    if (branching) {
-        QF_TRY(bind_device(ctx));
-        if (classical_width) *classical_width = (uint32_t)width;
-        return run_shots_branching(ctx, qubits, dtype, ops, n_ops, init_amps, shots, seed, tie_eps, outcomes, n_ties, opts);
-    }
-    std::vector<BGate> gates;
-    QF_TRY(bind_ops(qubits, ops, first, nullptr, 0, nullptr, 0, -1, 0.0, gates));
-    QF_TRY(bind_device(ctx));
-    qf_sv *sv;
-    QF_TRY(scratch_state(ctx, &ctx->scratch_sv, qubits, dtype, &sv));
-    if (init_amps) QF_TRY(convert_from_f64(sv, init_amps));
-    else QF_TRY(fill_zero_state(sv));
-    QF_TRY(execute_gates(sv, gates, opts));
-    if (classical_width) *classical_width = (uint32_t)width;
-    return sample_shots(sv, mq.data(), mc.data(), (uint32_t)mq.size(), shots, seed, tie_eps, outcomes, n_ties);
+    return run_shots_entry(ctx, qubits, dtype, ops, n_ops, init_amps, shots, seed, tie_eps, false, outcomes, classical_width,
+                           n_ties, opts);
+}
+
+int qf_run_shots_with_noise(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops,
+                            const double *init_amps, uint64_t shots, uint64_t seed, double tie_eps, uint64_t *outcomes,
+                            uint32_t *classical_width, uint64_t *n_ties, const qf_exec_opts *opts) {
+    return run_shots_entry(ctx, qubits, dtype, ops, n_ops, init_amps, shots, seed, tie_eps, true, outcomes, classical_width,
+                           n_ties, opts);
 }
 
 int qf_expectation(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops, const double *params,

@@ -316,12 +316,13 @@ int reduce_expect_1q(qf_sv *sv, int obs, uint32_t q, double *out) {
 int reduce_p_one(qf_sv *sv, uint32_t q, double *out) { return pair_reduce(sv, q, 3, out); }
 
 // Collapse after measure (src/lib.rs:1341-1350): amplitudes whose bit differs
-// from the outcome become 0, the others are divided by `scale`.
+// from the outcome become 0, the others are divided by `scale`. outcome < 0
+// divides every amplitude (StateVector::normalize, src/lib.rs:1005-1014).
 template <typename C>
 __global__ void k_collapse(C *__restrict__ a, uint64_t dim, uint32_t q, int outcome, double scale) {
     using R = typename Real<C>::T;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < dim; i += (uint64_t)gridDim.x * blockDim.x) {
-        if ((int)((i >> q) & 1ULL) != outcome) a[i] = mk((R)0, (R)0);
+        if (outcome >= 0 && (int)((i >> q) & 1ULL) != outcome) a[i] = mk((R)0, (R)0);
         else a[i] = mk((R)((double)a[i].x / scale), (R)((double)a[i].y / scale));
     }
 }

@@ -17,8 +17,11 @@ HEADER = Path(__file__).resolve().parent.parent / "include" / "qf.h"
 
 
 def header_functions():
+    """Functions the library exports: declarations, not the header-only
+    `static inline` helpers."""
     text = HEADER.read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"static inline[^{]*\{.*?\n\}", "", text, flags=re.S)
     return sorted(set(re.findall(r"\b(qf_[a-z0-9_]+)\s*\(", text)))
 
 
@@ -48,6 +51,32 @@ def test_struct_layouts_match_header():
     assert A.Op.theta.offset == 16 and A.Op.param.offset == 12
     assert C.sizeof(A.ExecOpts) == 16
     assert C.sizeof(A.GradientOpts) == 48
+
+
+def test_channel_aux_encoding_matches_the_header_helpers(tmp_path):
+    """channel_record's (q1, param) split equals qf_op_set_aux / qf_op_aux."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "aux.c"
+    src.write_text('#include "qf.h"\n'
+                   "double get_aux(const qf_op *op) { return qf_op_aux(op); }\n"
+                   "void set_aux(qf_op *op, double v) { qf_op_set_aux(op, v); }\n")
+    so = tmp_path / "libaux.so"
+    subprocess.run([cc, "-shared", "-fPIC", f"-I{HEADER.parent}", str(src), "-o", str(so)], check=True)
+    lib = C.CDLL(str(so))
+    lib.get_aux.restype = C.c_double
+    lib.get_aux.argtypes = [C.c_void_p]
+    lib.set_aux.argtypes = [C.c_void_p, C.c_double]
+    for beta in (0.0, 0.7, 1.0, 123.456, 1e-300, float("inf")):
+        rec = A.ops_array([A.channel_record(A.CHANNEL_THERMAL_DAMPING, 3, 0.2, beta)])
+        assert lib.get_aux(rec.ctypes.data) == beta
+        other = A.ops_array([(A.OP_CHANNEL, A.CHANNEL_THERMAL_DAMPING, 3, 0, 0, 0.2)])
+        lib.set_aux(other.ctypes.data, beta)
+        assert other.tobytes() == rec.tobytes()
 
 
 @pytest.mark.parametrize("seed,steps", [(0, 0), (1, 1), (42, 7), (721, 64), (991, 1000), (1234, 123457)])

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from quantumforge_gb300 import Circuit, Gate, PauliSum, QuantumError, SmallRng, StateVector
+from quantumforge_gb300 import Circuit, Gate, NoiseChannel, PauliSum, QuantumError, SmallRng, StateVector
 from quantumforge_gb300 import _abi as A
 from quantumforge_gb300 import workloads as W
 
@@ -171,6 +171,140 @@ def test_repeated_measurement_repeats_the_outcome(backend):
     c.measure(0, 1)
     got, width, ties = _shots_vs_oracle(backend, c, 1, 256, 5)
     assert set(got.tolist()) <= {0, 3}
+
+
+# ---- noise trajectories: run_shots_with_noise (src/lib.rs:2829-2916, 1356-1506) ----
+def _noisy_vs_oracle(backend, c, n, shots, seed, dtype="c128", tie_eps=1e-12, init=None):
+    """Per-shot outcomes of the engine's noisy shots against the oracle's
+    literal per-shot trajectories; a shot may differ only where a decision
+    fell within tie_eps of a branch threshold (counted by the engine)."""
+    got, width, ties = c.run_shots_packed(n if init is None else init, shots, seed, dtype=dtype, backend=backend,
+                                          tie_eps=tie_eps, noise=True)
+    want, w2 = O.run_shots(c.ops(), n, shots, seed, init=init, noise=True)
+    assert width == w2
+    assert int((got != want).sum()) <= ties, (int((got != want).sum()), ties)
+    return got, width, ties
+
+
+def test_noisy_shots_match_the_reference_engine(backend):  # tests/quantum_core.rs:678-700
+    c = Circuit()
+    c.push(Gate.H, 0)
+    c.push(Gate.Ry(0.54), 1)
+    c.cnot(0, 1)
+    c.channel(0, NoiseChannel.AmplitudeDamping(0.23))
+    c.channel(1, NoiseChannel.PhaseDamping(0.13))
+    c.channel(0, NoiseChannel.Depolarizing(0.17))
+    c.measure(0, 0)
+    c.if_classical_bit(0, 1, Gate.X, 2)
+    c.measure(2, 1)
+    c.measure(1, 2)
+    got, width, ties = _noisy_vs_oracle(backend, c, 3, 256, 9981)
+    assert ties == 0
+    want = O.counts(O.run_shots(c.ops(), 3, 256, 9981, noise=True)[0], 3)
+    assert backend.run_circuit_shots_batched(3, c, 256, 9981).counts == want
+    with pytest.raises(QuantumError) as e:
+        c.run_shots(3, 1, 5, backend=backend)
+    assert e.value.kind == "OperationRequiresDensityMatrix"
+
+
+@pytest.mark.parametrize("gate,channel,exact", [
+    (Gate.X, NoiseChannel.AmplitudeDamping(0.31), 0.69), (Gate.H, NoiseChannel.PhaseDamping(0.73), 0.5),
+    (Gate.I, NoiseChannel.Depolarizing(0.6), 0.4)])
+def test_noisy_shots_sample_kraus_trajectories(backend, gate, channel, exact):  # tests/quantum_core.rs:768-808
+    init = O.apply(O.zero(2), gate.code, 0.0, 0)
+    c = Circuit()
+    c.channel(0, channel)
+    c.measure(0, 0)
+    c.if_classical_bit(0, 1, Gate.X, 1)
+    c.measure(1, 1)
+    got, width, ties = _noisy_vs_oracle(backend, c, 2, 12_000, 5, init=init)
+    assert abs((got & 1).mean() - exact) < 0.025
+    assert np.array_equal(got & 1, (got >> 1) & 1)
+
+
+def test_thermal_damping_circuit_shots_run(backend):  # tests/noise_thermo.rs:185-203
+    c = Circuit()
+    c.push(Gate.H, 0)
+    c.channel(0, NoiseChannel.ThermalDamping(0.2, 1.0))
+    c.measure(0, 0)
+    got, width, ties = _noisy_vs_oracle(backend, c, 1, 256, 7)
+    res = c.run_shots_with_noise(1, 256, 7, backend=backend)
+    assert sum(res.counts.values()) == 256
+
+
+def _noisy_circuit(n, seed):
+    r = np.random.default_rng(seed)
+    c = Circuit.from_ops(W.random_circuit(n, 2, seed, two_qubit="mixed"))
+    kinds = [NoiseChannel.Depolarizing, NoiseChannel.AmplitudeDamping, NoiseChannel.PhaseDamping,
+             lambda g: NoiseChannel.ThermalDamping(g, float(r.uniform(0.0, 2.0)))]
+    for k in range(3):
+        for q in range(n):  # a noise layer
+            c.channel(q, kinds[int(r.integers(0, 4))](float(r.uniform(0.02, 0.3))))
+        if k == 1:  # a mid-circuit measurement and feed-forward
+            c.measure(int(r.integers(0, n)), 0)
+            c.if_classical_bit(0, 1, Gate.Ry(float(r.uniform(-3, 3))), int(r.integers(0, n)))
+        for op in W.random_circuit(n, 1, seed + 7 * k, two_qubit="ladder"):
+            c.operations.append((int(op["kind"]), int(op["gate"]), int(op["q0"]), int(op["q1"]), 0, float(op["theta"]), 0))
+    for q in range(min(n, 5)):  # a terminal block
+        c.measure(q, 1 + q)
+    return c
+
+
+@pytest.mark.parametrize("n,seed,dtype,tie", [(5, 1, "c128", 1e-12), (8, 2, "c128", 1e-12), (11, 3, "c128", 1e-12),
+                                              (7, 4, "c64", 2e-5), (10, 5, "c64", 2e-5)])
+def test_random_noisy_circuits_match_the_reference_engine(backend, n, seed, dtype, tie):
+    c = _noisy_circuit(n, seed)
+    got, width, ties = _noisy_vs_oracle(backend, c, n, 600, 300 + seed, dtype=dtype, tie_eps=tie)
+    assert len(set(got.tolist())) > 1
+
+
+def test_noisy_shots_normalise_the_initial_state(backend):
+    r = np.random.default_rng(3)
+    init = 3.0 * (r.normal(size=64) + 1j * r.normal(size=64))  # far from unit norm
+    c = Circuit()
+    c.channel(2, NoiseChannel.AmplitudeDamping(0.4))
+    c.push(Gate.H, 1)
+    for q in range(6):
+        c.measure(q, q)
+    _noisy_vs_oracle(backend, c, 6, 2000, 11, init=init)
+    d = Circuit()  # no channel: the sampler path, normalised the same way
+    d.push(Gate.H, 1)
+    for q in range(6):
+        d.measure(q, q)
+    _noisy_vs_oracle(backend, d, 6, 2000, 12, init=init)
+    with pytest.raises(QuantumError) as e:
+        c.run_shots_with_noise(np.zeros(64, complex), 4, 1, backend=backend)
+    assert e.value.kind == "InvalidProbability"
+
+
+@pytest.mark.parametrize("channel", [NoiseChannel.Depolarizing(1.5), NoiseChannel.AmplitudeDamping(-0.1),
+                                     NoiseChannel.ThermalDamping(0.1, -1.0), NoiseChannel.PhaseDamping(float("nan"))])
+def test_invalid_channel_parameters_are_rejected(backend, channel):
+    c = Circuit()
+    c.push(Gate.H, 0)
+    c.channel(0, channel)
+    c.measure(0, 0)
+    with pytest.raises(QuantumError) as e:
+        c.run_shots_with_noise(2, 8, 1, backend=backend)
+    assert e.value.kind == "InvalidProbability"
+
+
+def test_noisy_shots_over_many_branches_stay_within_memory(backend):
+    """Depth-first walk: 16 qubits, 8 noise layers, 4000 shots spread over
+    thousands of trajectories while at most one state per level is alive."""
+    n = 16
+    c = Circuit()
+    for q in range(n):
+        c.push(Gate.H, q)
+    for layer in range(8):
+        for q in range(0, n, 3):
+            c.channel(q, NoiseChannel.Depolarizing(0.3))
+        c.cnot(layer % n, (layer + 1) % n)
+    for q in range(4):
+        c.measure(q, q)
+    got, width, ties = c.run_shots_packed(n, 4000, 21, backend=backend, noise=True)
+    want, _ = O.run_shots(c.ops(), n, 4000, 21, noise=True)
+    assert int((got != want).sum()) <= ties
 
 
 # ---- random circuits -------------------------------------------------------------
