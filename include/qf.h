@@ -202,6 +202,7 @@ typedef struct qf_gradient_info {
 
 typedef struct qf_ctx qf_ctx;  /* CudaBackend: device, stream, workspaces */
 typedef struct qf_sv qf_sv;    /* CudaDeviceState: one resident state vector */
+typedef struct qf_batch qf_batch;  /* CudaDeviceStateBatch: equal-width states in one allocation */
 
 /* ---------------------------------------------------------------------------
  * Errors and build information
@@ -334,6 +335,42 @@ int qf_run_shots_with_noise(qf_ctx *ctx, uint32_t qubits, int dtype,
 int qf_sv_sample(qf_sv *sv, const uint32_t *qubit_order, const uint32_t *classical_bits, uint32_t m,
                  uint64_t shots, uint64_t seed, double tie_eps,
                  uint64_t *outcomes, uint64_t *n_ties);
+
+/* ---------------------------------------------------------------------------
+ * State batches — replace CudaDeviceStateBatch (src/cuda.rs:529-540,
+ * 1486-1992) and CudaBackend::upload_batch / run_circuit_batch
+ * (src/cuda.rs:871-967). State b of a batch occupies amplitudes
+ * [b * 2^qubits, (b + 1) * 2^qubits) of one device allocation; host buffers
+ * hold the states back to back, f64 interleaved.
+ * ------------------------------------------------------------------------- */
+
+/* `batch_size` states |0...0> (0 -> QF_ERR_EMPTY_BATCH). */
+int qf_batch_create(qf_ctx *ctx, uint32_t qubits, int dtype, uint64_t batch_size, qf_batch **out);
+int qf_batch_destroy(qf_batch *batch);
+int qf_batch_qubits(const qf_batch *batch, uint32_t *qubits_out);
+int qf_batch_size(const qf_batch *batch, uint64_t *size_out);
+/* upload_batch (src/cuda.rs:871-955): 2 * batch_size * 2^qubits doubles. */
+int qf_batch_upload(qf_batch *batch, const double *amps, uint64_t n_doubles);
+/* CudaDeviceStateBatch::download (src/cuda.rs:1973-1991). */
+int qf_batch_download(qf_batch *batch, double *amps_out, uint64_t n_doubles);
+/* CudaDeviceStateBatch::copy_from_device (src/cuda.rs:1797-1817). */
+int qf_batch_copy_from(qf_batch *dst, const qf_batch *src);
+/* CudaDeviceStateBatch::run_circuit / apply_gate / apply_cnot / apply_cz /
+ * apply_swap (src/cuda.rs:1821-1969): the same unitary ops on every state;
+ * channels -> QF_ERR_OPERATION_REQUIRES_DENSITY_MATRIX, measurements and
+ * conditionals -> QF_ERR_OPERATION_REQUIRES_SHOT_EXECUTION. */
+int qf_batch_apply_ops(qf_batch *batch, const qf_op *ops, uint64_t n_ops, const qf_exec_opts *opts);
+/* CudaDeviceStateBatch::measure (src/cuda.rs:1497-1623): one uniform per
+ * state in batch order from *rng_state (advanced), P(1) per state, outcome
+ * u < P(1), kept amplitudes multiplied by 1/sqrt(P(outcome)); outcomes[b]
+ * is 0 or 1. */
+int qf_batch_measure(qf_batch *batch, uint32_t qubit, uint64_t *rng_state, uint8_t *outcomes);
+/* CudaBackend::run_circuit_batch (src/cuda.rs:958-967): upload `batch_size`
+ * states from `in_amps`, run the ops on each, download to `out_amps` (both
+ * 2 * batch_size * 2^qubits doubles). */
+int qf_run_circuit_batch(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops,
+                         const double *in_amps, uint64_t batch_size, double *out_amps, uint64_t n_doubles,
+                         const qf_exec_opts *opts);
 
 /* ---------------------------------------------------------------------------
  * Gradients — ParameterizedCircuit::gradient_with_inputs

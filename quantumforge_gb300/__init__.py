@@ -20,12 +20,13 @@ from .core import (
     SingleQubitObservable,
     SmallRng,
     StateVector,
+    StateVectorBatch,
     default_backend,
 )
 from . import gradients
 
 __all__ = [
     "Circuit", "CudaBackend", "Gate", "NoiseChannel", "ParameterizedCircuit", "PauliSum", "QuantumError", "RotationAxis",
-    "ShotResult", "SingleQubitObservable", "SmallRng", "StateVector", "default_backend", "gradients",
+    "ShotResult", "SingleQubitObservable", "SmallRng", "StateVector", "StateVectorBatch", "default_backend", "gradients",
     "load_library",
 ]

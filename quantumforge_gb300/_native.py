@@ -67,6 +67,16 @@ SIGNATURES = {
     "qf_run_circuit": [P, U32, C.c_int, P, U64, P, P, U64, P],
     "qf_run_shots": [P, U32, C.c_int, P, U64, P, U64, U64, F64, P, PU32, PU64, P],
     "qf_run_shots_with_noise": [P, U32, C.c_int, P, U64, P, U64, U64, F64, P, PU32, PU64, P],
+    "qf_batch_create": [P, U32, C.c_int, U64, C.POINTER(P)],
+    "qf_batch_destroy": [P],
+    "qf_batch_qubits": [P, PU32],
+    "qf_batch_size": [P, PU64],
+    "qf_batch_upload": [P, P, U64],
+    "qf_batch_download": [P, P, U64],
+    "qf_batch_copy_from": [P, P],
+    "qf_batch_apply_ops": [P, P, U64, P],
+    "qf_batch_measure": [P, U32, PU64, P],
+    "qf_run_circuit_batch": [P, U32, C.c_int, P, U64, P, U64, P, U64, P],
     "qf_sv_sample": [P, P, P, U32, U64, U64, F64, P, PU64],
     "qf_gradient": [P, U32, P, U64, P, U64, P, U64, P, U64, P, P, P, P],
     "qf_expectation": [P, U32, C.c_int, P, U64, P, U64, P, U64, P, U64, P, PF64],

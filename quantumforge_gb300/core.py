@@ -264,6 +264,25 @@ class CudaBackend:
                                     _exec(exec_opts)))
         return out.view(np.complex128)
 
+    def upload_batch(self, states, dtype="c128") -> "StateVectorBatch":
+        return StateVectorBatch.from_states(states, dtype=dtype, backend=self)
+
+    def run_circuit_batch(self, states, circuit: "Circuit", dtype="c128", exec_opts=None) -> list[np.ndarray]:
+        """CudaBackend::run_circuit_batch (src/cuda.rs:958-967): one upload,
+        one fused sweep over every state, one download."""
+        arrs = [s.amplitudes() if isinstance(s, StateVector) else np.asarray(s, dtype=np.complex128) for s in states]
+        if not arrs:
+            raise QuantumError(_abi.STATUS_CODES["EmptyBatch"], "CUDA state batches must contain at least one state")
+        if any(a.size != arrs[0].size for a in arrs):
+            raise QuantumError(_abi.STATUS_CODES["IncompatibleBatch"], "all states in a CUDA batch must have the same width")
+        n = arrs[0].size.bit_length() - 1
+        src = np.ascontiguousarray(np.concatenate(arrs), dtype=np.complex128).view(np.float64)
+        out = np.empty_like(src)
+        ops = circuit.ops()
+        check(load().qf_run_circuit_batch(self._h, n, _dtype_code(dtype), ptr(ops), len(ops), ptr(src), len(arrs), ptr(out),
+                                          out.size, _exec(exec_opts)))
+        return list(out.view(np.complex128).reshape(len(arrs), 1 << n).copy())
+
     def run_circuit_shots(self, initial_state, circuit: "Circuit", shots: int, seed: int, dtype="c128",
                           tie_eps: float = 0.0) -> "ShotResult":
         return circuit.run_shots(initial_state, shots, seed, dtype=dtype, backend=self, tie_eps=tie_eps)
@@ -433,6 +452,90 @@ class StateVector:
 # ---------------------------------------------------------------------------
 # Circuits
 # ---------------------------------------------------------------------------
+class StateVectorBatch:
+    """`CudaDeviceStateBatch` (src/cuda.rs:529-540, 1486-1992): equal-width
+    states resident in one device allocation, swept together."""
+
+    def __init__(self, handle, qubits: int, size: int, dtype: int, backend: CudaBackend):
+        self._h, self.qubits, self.size, self.dtype, self.backend = handle, qubits, size, dtype, backend
+
+    @classmethod
+    def zero(cls, qubits: int, batch_size: int, dtype="c128", backend: CudaBackend | None = None) -> "StateVectorBatch":
+        backend = backend or default_backend()
+        h = C.c_void_p()
+        code = _dtype_code(dtype)
+        check(load().qf_batch_create(backend.handle, int(qubits), code, int(batch_size), C.byref(h)))
+        return cls(h, int(qubits), int(batch_size), code, backend)
+
+    @classmethod
+    def from_states(cls, states, dtype="c128", backend: CudaBackend | None = None) -> "StateVectorBatch":
+        """CudaBackend::upload_batch (src/cuda.rs:871-955)."""
+        arrs = [s.amplitudes() if isinstance(s, StateVector) else np.asarray(s, dtype=np.complex128) for s in states]
+        if not arrs:
+            raise QuantumError(_abi.STATUS_CODES["EmptyBatch"], "CUDA state batches must contain at least one state")
+        if any(a.size != arrs[0].size for a in arrs):
+            raise QuantumError(_abi.STATUS_CODES["IncompatibleBatch"], "all states in a CUDA batch must have the same width")
+        n = arrs[0].size.bit_length() - 1
+        b = cls.zero(n, len(arrs), dtype=dtype, backend=backend)
+        flat = np.ascontiguousarray(np.concatenate(arrs), dtype=np.complex128).view(np.float64)
+        check(load().qf_batch_upload(b._h, ptr(flat), flat.size))
+        return b
+
+    def __del__(self):
+        try:
+            if self._h and self._h.value:
+                load().qf_batch_destroy(self._h)
+                self._h = C.c_void_p()
+        except Exception:
+            pass
+
+    def batch_size(self) -> int:
+        return self.size
+
+    def num_qubits(self) -> int:
+        return self.qubits
+
+    def apply_ops(self, ops: np.ndarray, exec_opts=None) -> "StateVectorBatch":
+        check(load().qf_batch_apply_ops(self._h, ptr(ops), len(ops), _exec(exec_opts)))
+        return self
+
+    def apply_gate(self, gate: Gate, qubit: int) -> "StateVectorBatch":
+        return self.apply_ops(_abi.ops_array([(_abi.OP_GATE, gate.code, int(qubit), 0, 0, gate.theta)]))
+
+    def apply_cnot(self, control: int, target: int) -> "StateVectorBatch":
+        return self.apply_ops(_abi.ops_array([(_abi.OP_CNOT, 0, int(control), int(target), 0, 0.0)]))
+
+    def apply_cz(self, first: int, second: int) -> "StateVectorBatch":
+        return self.apply_ops(_abi.ops_array([(_abi.OP_CZ, 0, int(first), int(second), 0, 0.0)]))
+
+    def apply_swap(self, first: int, second: int) -> "StateVectorBatch":
+        return self.apply_ops(_abi.ops_array([(_abi.OP_SWAP, 0, int(first), int(second), 0, 0.0)]))
+
+    def run_circuit(self, circuit: "Circuit", exec_opts=None) -> "StateVectorBatch":
+        return self.apply_ops(circuit.ops(), exec_opts)
+
+    def measure(self, qubit: int, rng: SmallRng) -> list[int]:
+        """One uniform per state in batch order; returns the outcomes."""
+        st = C.c_uint64(rng.state)
+        out = np.zeros(self.size, dtype=np.uint8)
+        try:
+            check(load().qf_batch_measure(self._h, int(qubit), C.byref(st), ptr(out)))
+        finally:
+            rng.state = st.value
+        return out.tolist()
+
+    def copy_from_device(self, source: "StateVectorBatch") -> None:
+        check(load().qf_batch_copy_from(self._h, source._h))
+
+    def synchronize(self) -> None:
+        self.backend.synchronize()
+
+    def download(self) -> list[np.ndarray]:
+        out = np.empty(2 * (self.size << self.qubits), dtype=np.float64)
+        check(load().qf_batch_download(self._h, ptr(out), out.size))
+        return list(out.view(np.complex128).reshape(self.size, 1 << self.qubits).copy())
+
+
 @dataclass
 class ShotResult:
     """`ShotResult` (src/lib.rs:2453-2464): counts keyed by LSB-first bit tuples."""

@@ -997,6 +997,149 @@ int qf_sv_measure(qf_sv *sv, uint32_t qubit, uint64_t *rng_state, uint8_t *outco
     return QF_OK;
 }
 
+// ---- state batches (CudaDeviceStateBatch, src/cuda.rs:1486-1992) ------------
+static int check_batch(const qf_batch *b) {
+    if (!b || !b->sv || !b->sv->ctx || !b->sv->d) return fail(QF_ERR_INVALID_ARGUMENT, "batch handle is NULL or released");
+    return QF_OK;
+}
+
+// The first size << n amplitudes of the batch allocation, as a state view for
+// the f64 conversions.
+static qf_sv batch_view(const qf_batch *b) {
+    qf_sv v = *b->sv;
+    v.dim = b->size << b->n;
+    return v;
+}
+
+int qf_batch_create(qf_ctx *ctx, uint32_t qubits, int dtype, uint64_t batch_size, qf_batch **out) {
+    clear_error();
+    if (!ctx || !out) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    QF_TRY(check_dtype(dtype));
+    if (batch_size == 0) return fail(QF_ERR_EMPTY_BATCH, "CUDA state batches must contain at least one state");
+    if (qubits == 0) return fail(QF_ERR_ZERO_QUBITS, "a state vector must contain at least one qubit");
+    uint32_t extra = 0;
+    while (extra < 63 && (1ULL << extra) < batch_size) ++extra;
+    if ((uint64_t)qubits + extra > 40)
+        return fail(QF_ERR_STATE_TOO_LARGE, "a batch of %llu states of %u qubits exceeds the supported device allocation",
+                    (unsigned long long)batch_size, qubits);
+    QF_TRY(bind_device(ctx));
+    qf_sv *sv;
+    QF_TRY(alloc_state(ctx, qubits + extra, dtype, 0, &sv));
+    const int st = batch_set_zero(sv, qubits, batch_size);
+    if (st) {
+        free_state(sv);
+        return st;
+    }
+    *out = new qf_batch{sv, qubits, batch_size};
+    return QF_OK;
+}
+
+int qf_batch_destroy(qf_batch *batch) {
+    if (!batch) return QF_OK;
+    if (batch->sv) qf_sv_destroy(batch->sv);
+    delete batch;
+    return QF_OK;
+}
+
+int qf_batch_qubits(const qf_batch *batch, uint32_t *qubits_out) {
+    QF_TRY(check_batch(batch));
+    if (!qubits_out) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    *qubits_out = batch->n;
+    return QF_OK;
+}
+
+int qf_batch_size(const qf_batch *batch, uint64_t *size_out) {
+    QF_TRY(check_batch(batch));
+    if (!size_out) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    *size_out = batch->size;
+    return QF_OK;
+}
+
+int qf_batch_upload(qf_batch *batch, const double *amps, uint64_t n_doubles) {
+    clear_error();
+    QF_TRY(check_batch(batch));
+    if (!amps) return fail(QF_ERR_INVALID_ARGUMENT, "amplitudes are NULL");
+    qf_sv v = batch_view(batch);
+    if (n_doubles != 2 * v.dim)
+        return fail(QF_ERR_INCOMPATIBLE_BATCH, "expected %llu doubles (%llu states of 2^%u amplitudes), got %llu",
+                    (unsigned long long)(2 * v.dim), (unsigned long long)batch->size, batch->n, (unsigned long long)n_doubles);
+    QF_TRY(bind_device(v.ctx));
+    QF_TRY(convert_from_f64(&v, amps));
+    QF_CUDA(cudaStreamSynchronize(v.ctx->stream));
+    return QF_OK;
+}
+
+int qf_batch_download(qf_batch *batch, double *amps_out, uint64_t n_doubles) {
+    clear_error();
+    QF_TRY(check_batch(batch));
+    if (!amps_out) return fail(QF_ERR_INVALID_ARGUMENT, "output is NULL");
+    qf_sv v = batch_view(batch);
+    if (n_doubles != 2 * v.dim)
+        return fail(QF_ERR_INVALID_ARGUMENT, "expected %llu doubles, got %llu", (unsigned long long)(2 * v.dim),
+                    (unsigned long long)n_doubles);
+    QF_TRY(bind_device(v.ctx));
+    return convert_to_f64(&v, amps_out);
+}
+
+int qf_batch_copy_from(qf_batch *dst, const qf_batch *src) {
+    clear_error();
+    QF_TRY(check_batch(dst));
+    QF_TRY(check_batch(src));
+    if (dst->n != src->n || dst->size != src->size || dst->sv->dtype != src->sv->dtype || dst->sv->ctx != src->sv->ctx)
+        return fail(QF_ERR_INCOMPATIBLE_DEVICE_STATE, "device states must share a backend and have equal dimensions");
+    QF_TRY(bind_device(dst->sv->ctx));
+    QF_CUDA(cudaMemcpyAsync(dst->sv->d, src->sv->d, dst->sv->bytes(), cudaMemcpyDeviceToDevice, dst->sv->ctx->stream));
+    QF_CUDA(cudaStreamSynchronize(dst->sv->ctx->stream));
+    return QF_OK;
+}
+
+int qf_batch_apply_ops(qf_batch *batch, const qf_op *ops, uint64_t n_ops, const qf_exec_opts *opts) {
+    clear_error();
+    QF_TRY(check_batch(batch));
+    if (n_ops && !ops) return fail(QF_ERR_INVALID_ARGUMENT, "ops is NULL");
+    std::vector<BGate> gates;
+    QF_TRY(bind_ops(batch->n, ops, n_ops, nullptr, 0, nullptr, 0, -1, 0.0, gates));
+    QF_TRY(bind_device(batch->sv->ctx));
+    return execute_gates(batch->sv, gates, opts);
+}
+
+int qf_batch_measure(qf_batch *batch, uint32_t qubit, uint64_t *rng_state, uint8_t *outcomes) {
+    clear_error();
+    QF_TRY(check_batch(batch));
+    if (!rng_state || !outcomes) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (qubit >= batch->n) return fail(QF_ERR_QUBIT_OUT_OF_RANGE, "qubit index %u is out of range for %u qubits", qubit, batch->n);
+    std::vector<double> u(batch->size);
+    for (uint64_t b = 0; b < batch->size; ++b) u[b] = next_uniform(rng_state);
+    QF_TRY(bind_device(batch->sv->ctx));
+    return batch_measure(batch->sv, batch->n, batch->size, qubit, u.data(), outcomes);
+}
+
+int qf_run_circuit_batch(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops, const double *in_amps,
+                         uint64_t batch_size, double *out_amps, uint64_t n_doubles, const qf_exec_opts *opts) {
+    clear_error();
+    if (!ctx || !in_amps || !out_amps || (n_ops && !ops)) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (batch_size == 0) return fail(QF_ERR_EMPTY_BATCH, "CUDA state batches must contain at least one state");
+    if (qubits == 0) return fail(QF_ERR_ZERO_QUBITS, "a state vector must contain at least one qubit");
+    if (qubits > 40 || batch_size > (1ULL << (40 - qubits)))
+        return fail(QF_ERR_STATE_TOO_LARGE, "a batch of %llu states of %u qubits exceeds the supported device allocation",
+                    (unsigned long long)batch_size, qubits);
+    if (n_doubles != 2 * (batch_size << qubits))
+        return fail(QF_ERR_INCOMPATIBLE_BATCH, "expected %llu doubles, got %llu",
+                    (unsigned long long)(2 * (batch_size << qubits)), (unsigned long long)n_doubles);
+    std::vector<BGate> gates;
+    QF_TRY(bind_ops(qubits, ops, n_ops, nullptr, 0, nullptr, 0, -1, 0.0, gates));  // validated before any allocation
+    qf_batch *b;
+    QF_TRY(qf_batch_create(ctx, qubits, dtype, batch_size, &b));
+    struct Release {
+        qf_batch *b;
+        ~Release() { qf_batch_destroy(b); }
+    } release{b};
+    qf_sv v = batch_view(b);
+    QF_TRY(convert_from_f64(&v, in_amps));
+    QF_TRY(execute_gates(b->sv, gates, opts));
+    return convert_to_f64(&v, out_amps);
+}
+
 int qf_run_circuit(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops, const double *init_amps,
                    double *out_amps, uint64_t n_doubles, const qf_exec_opts *opts) {
     clear_error();

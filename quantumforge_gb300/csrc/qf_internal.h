@@ -39,6 +39,15 @@ struct qf_sv {
     size_t bytes() const { return dim * (dtype == QF_C64 ? 8u : 16u); }
 };
 
+// A batch of `size` states of `n` qubits: one state of n + ceil(log2 size)
+// qubits whose top bits index the state (padding states stay zero), so the
+// fused engine sweeps every state of the batch in the same passes.
+struct qf_batch {
+    qf_sv *sv = nullptr;
+    uint32_t n = 0;
+    uint64_t size = 0;
+};
+
 namespace qf {
 
 // ---- errors -----------------------------------------------------------------
@@ -279,6 +288,11 @@ int pauli_apply(qf_sv *psi, qf_sv *lambda, const qf_pauli_term *terms, uint64_t 
 int fill_zero_state(qf_sv *sv);
 int convert_from_f64(qf_sv *sv, const double *d_src);
 int convert_to_f64(qf_sv *sv, double *d_dst);
+// Batches: B states of 2^n amplitudes in one allocation (state b at b << n).
+int batch_set_zero(qf_sv *sv, uint32_t n, uint64_t B);
+// Measure qubit q of every state with uniforms[b]; outcomes to host; on an
+// invalid probability nothing is collapsed.
+int batch_measure(qf_sv *sv, uint32_t n, uint64_t B, uint32_t q, const double *uniforms, uint8_t *outcomes);
 // Sampler.
 // start_states: optional per-shot generator states (host, `shots` entries)
 // replacing the shot-major jump from `seed`.

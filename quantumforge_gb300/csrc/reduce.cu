@@ -336,6 +336,119 @@ int collapse(qf_sv *sv, uint32_t q, int outcome, double scale) {
     return QF_OK;
 }
 
+// ---- batches of states --------------------------------------------------------
+// A batch of B states of 2^n amplitudes is one allocation; state b starts at
+// amplitude b << n (CudaDeviceStateBatch, src/cuda.rs:529-540).
+
+// Every state |0...0>, the padding after the last state zero.
+template <typename C>
+__global__ void k_batch_zero(C *__restrict__ a, uint64_t total, uint32_t n, uint64_t B) {
+    using R = typename Real<C>::T;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+        const bool one = (i & ((1ULL << n) - 1)) == 0 && (i >> n) < B;
+        a[i] = mk((R)(one ? 1 : 0), (R)0);
+    }
+}
+
+int batch_set_zero(qf_sv *sv, uint32_t n, uint64_t B) {
+    qf_ctx *ctx = sv->ctx;
+    const int grid = std::max(1, std::min<int>((int)((sv->dim + 255) / 256), ctx->sm_count * 8));
+    if (sv->dtype == QF_C64) k_batch_zero<float2><<<grid, 256, 0, ctx->stream>>>(static_cast<float2 *>(sv->d), sv->dim, n, B);
+    else k_batch_zero<double2><<<grid, 256, 0, ctx->stream>>>(static_cast<double2 *>(sv->d), sv->dim, n, B);
+    QF_CUDA(cudaGetLastError());
+    return QF_OK;
+}
+
+// P(1) of qubit q per state: block (b, c) sums chunk c of state b into
+// partials[b * chunks + c]; k_batch_finish adds each state's chunks in order.
+template <typename C>
+__global__ void k_batch_p_one(const C *__restrict__ a, uint32_t n, uint32_t q, uint32_t chunk_log, double *partials) {
+    __shared__ double red[32];
+    const uint32_t chunks_log = n - chunk_log;
+    const uint64_t b = blockIdx.x >> chunks_log, c = blockIdx.x & ((1ULL << chunks_log) - 1);
+    const uint64_t base = (b << n) + (c << chunk_log), len = 1ULL << chunk_log;
+    double s = 0.0;
+    for (uint64_t j = threadIdx.x; j < len; j += blockDim.x) {
+        const uint64_t i = base + j;
+        if ((i >> q) & 1ULL) {
+            const C v = a[i];
+            s += (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+        }
+    }
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+__global__ void k_batch_finish(const double *__restrict__ partials, uint64_t B, uint32_t chunks, double *out) {
+    const uint64_t b = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    double s = 0.0;
+    for (uint32_t c = 0; c < chunks; ++c) s += partials[b * chunks + c];
+    out[b] = s;
+}
+
+// Collapse state b to outcome[b] on qubit q, multiplying the kept amplitudes
+// by inv[b] (the batch collapse of src/cuda.rs:1582-1621).
+template <typename C>
+__global__ void k_batch_collapse(C *__restrict__ a, uint64_t total, uint32_t n, uint32_t q, const uint8_t *__restrict__ outcome,
+                                 const double *__restrict__ inv) {
+    using R = typename Real<C>::T;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t b = i >> n;
+        if ((uint8_t)((i >> q) & 1ULL) != outcome[b]) {
+            a[i] = mk((R)0, (R)0);
+        } else {
+            const C v = a[i];
+            a[i] = mk((R)((double)v.x * inv[b]), (R)((double)v.y * inv[b]));
+        }
+    }
+}
+
+int batch_measure(qf_sv *sv, uint32_t n, uint64_t B, uint32_t q, const double *uniforms, uint8_t *outcomes) {
+    qf_ctx *ctx = sv->ctx;
+    const uint32_t chunk_log = std::min<uint32_t>(n, 13);  // 8192 amplitudes per block
+    const uint64_t chunks = 1ULL << (n - chunk_log);
+    const uint64_t blocks = B * chunks;
+    if (blocks > 0x7FFFFFFFULL) return fail(QF_ERR_STATE_TOO_LARGE, "batch reduction grid exceeds the launch limit");
+    const size_t part_b = sizeof(double) * blocks, p1_b = sizeof(double) * B, inv_b = sizeof(double) * B;
+    QF_TRY(ensure_device(&ctx->ws_tree, &ctx->ws_tree_bytes, part_b + p1_b + inv_b + B + 16));
+    unsigned char *w = static_cast<unsigned char *>(ctx->ws_tree);
+    double *d_part = reinterpret_cast<double *>(w);
+    double *d_p1 = reinterpret_cast<double *>(w + part_b);
+    double *d_inv = reinterpret_cast<double *>(w + part_b + p1_b);
+    uint8_t *d_out = w + part_b + p1_b + inv_b;
+    if (sv->dtype == QF_C64)
+        k_batch_p_one<float2><<<(unsigned)blocks, 256, 0, ctx->stream>>>(static_cast<const float2 *>(sv->d), n, q, chunk_log, d_part);
+    else
+        k_batch_p_one<double2><<<(unsigned)blocks, 256, 0, ctx->stream>>>(static_cast<const double2 *>(sv->d), n, q, chunk_log, d_part);
+    QF_CUDA(cudaGetLastError());
+    k_batch_finish<<<(unsigned)((B + 255) / 256), 256, 0, ctx->stream>>>(d_part, B, (uint32_t)chunks, d_p1);
+    QF_CUDA(cudaGetLastError());
+    std::vector<double> p1(B), inv(B);
+    QF_CUDA(cudaMemcpyAsync(p1.data(), d_p1, p1_b, cudaMemcpyDeviceToHost, ctx->stream));
+    QF_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (uint64_t b = 0; b < B; ++b) {
+        const double p = std::min(1.0, std::max(0.0, p1[b]));
+        const uint8_t o = uniforms[b] < p ? 1 : 0;
+        const double prob = o ? p : 1.0 - p;
+        if (prob <= 2.220446049250313e-16)
+            return fail(QF_ERR_INVALID_PROBABILITY, "measurement probability must be in [0, 1], got %g", prob);
+        outcomes[b] = o;
+        inv[b] = 1.0 / std::sqrt(prob);
+    }
+    QF_CUDA(cudaMemcpyAsync(d_out, outcomes, B, cudaMemcpyHostToDevice, ctx->stream));
+    QF_CUDA(cudaMemcpyAsync(d_inv, inv.data(), inv_b, cudaMemcpyHostToDevice, ctx->stream));
+    const uint64_t total = B << n;
+    const int grid = std::max(1, std::min<int>((int)((total + 255) / 256), ctx->sm_count * 8));
+    if (sv->dtype == QF_C64)
+        k_batch_collapse<float2><<<grid, 256, 0, ctx->stream>>>(static_cast<float2 *>(sv->d), total, n, q, d_out, d_inv);
+    else
+        k_batch_collapse<double2><<<grid, 256, 0, ctx->stream>>>(static_cast<double2 *>(sv->d), total, n, q, d_out, d_inv);
+    QF_CUDA(cudaGetLastError());
+    QF_CUDA(cudaStreamSynchronize(ctx->stream));  // host outcome/inverse buffers are read by the copies
+    return QF_OK;
+}
+
 // ---- Pauli sums --------------------------------------------------------------
 // Terms are grouped by x-mask. For one group, G_x(i) = sum_t c_t * i^{ny_t} *
 // (-1)^{popcount(i & z_t)} is the phase PauliWord::apply_basis_index gives

@@ -9,7 +9,8 @@ import numpy as np
 import pytest
 
 import oracle as O
-from quantumforge_gb300 import ParameterizedCircuit, PauliSum, QuantumError, RotationAxis, SingleQubitObservable
+from quantumforge_gb300 import (NoiseChannel, ParameterizedCircuit, PauliSum, QuantumError, RotationAxis,
+                                SingleQubitObservable)
 from quantumforge_gb300 import _abi as A
 from quantumforge_gb300 import workloads as W
 from quantumforge_gb300.gradients import (
@@ -130,7 +131,7 @@ def test_auto_selects_and_reports_cost(backend):  # tests/gradients.rs:223-361
     assert sampled.strategy == GradientStrategy.ParameterShift
     noisy = ParameterizedCircuit.new(1)
     noisy.rotation(RotationAxis.Y, 0, 0)
-    noisy.channel(0)
+    noisy.channel(0, NoiseChannel.Depolarizing(0.1))
     with pytest.raises(QuantumError) as e:
         noisy.gradient_auto([0.3], 1, Z, 0, backend=backend)
     assert e.value.kind == "OperationRequiresDensityMatrix"

@@ -9,7 +9,8 @@ import numpy as np
 import pytest
 
 import oracle as O
-from quantumforge_gb300 import Circuit, Gate, NoiseChannel, PauliSum, QuantumError, SmallRng, StateVector
+from quantumforge_gb300 import (Circuit, Gate, NoiseChannel, PauliSum, QuantumError, SmallRng, StateVector,
+                                StateVectorBatch)
 from quantumforge_gb300 import _abi as A
 from quantumforge_gb300 import workloads as W
 
@@ -65,7 +66,15 @@ def test_cuda_executes_the_unitary_circuit_api(backend):  # :488-511
         assert close(got, expected, 1e-12)
 
 
-def test_cuda_batched_inputs_match_independent_cpu_runs(backend):  # :513-600 (states run one by one)
+def _batch_inputs():
+    inputs = [O.zero(3)]
+    inputs.append(O.apply(O.apply(O.zero(3), A.GATE_X, 0, 0), A.GATE_RY, 0.31, 2))
+    inputs.append(O.apply(O.apply(O.zero(3), A.GATE_H, 0, 1), A.GATE_RZ, math.pi / 2, 2))
+    inputs.append(O.apply(O.apply(O.zero(3), A.GATE_X, 0, 1), A.GATE_H, 0, 2))
+    return inputs
+
+
+def test_cuda_batched_circuit_matches_independent_cpu_runs(backend):  # tests/quantum_core.rs:519-600
     c = Circuit()
     c.push(Gate.H, 0)
     c.push(Gate.Rx(0.19), 2)
@@ -74,22 +83,85 @@ def test_cuda_batched_inputs_match_independent_cpu_runs(backend):  # :513-600 (s
     c.cz(1, 2)
     c.swap(0, 1)
     c.push(Gate.Rz(math.pi / 2), 2)
-    inputs = [O.zero(3)]
-    s = O.apply(O.apply(O.zero(3), A.GATE_X, 0, 0), A.GATE_RY, 0.31, 2)
-    inputs.append(s)
-    inputs.append(O.apply(O.apply(O.zero(3), A.GATE_H, 0, 1), A.GATE_RZ, math.pi / 2, 2))
-    inputs.append(O.apply(O.apply(O.zero(3), A.GATE_X, 0, 1), A.GATE_H, 0, 2))
-    for st in inputs:
-        assert close(backend.run_circuit(st, c), O.run(c.ops(), 3, init=st), 1e-12)
-    # shared-RNG measurement of qubit 0 after H, in batch order (seed 7721)
-    rng_gpu, rng_cpu = SmallRng.seeded(7721), O.Rng(7721)
-    for st in inputs:
-        pre = O.apply(st.copy(), A.GATE_H, 0, 0)
-        sv = StateVector.from_amplitudes(pre, backend=backend)
-        cpu = pre.copy()
-        assert sv.measure(0, rng_gpu) == O.measure(cpu, 0, rng_cpu)
-        assert close(sv.amplitudes(), cpu, 1e-12)
+    inputs = _batch_inputs()
+    with pytest.raises(QuantumError) as e:
+        backend.upload_batch([])
+    assert e.value.kind == "EmptyBatch"
+    with pytest.raises(QuantumError) as e:
+        backend.upload_batch([O.zero(2), O.zero(3)])
+    assert e.value.kind == "IncompatibleBatch"
+    got = backend.run_circuit_batch(inputs, c)
+    assert len(got) == len(inputs)
+    for g_, st in zip(got, inputs):
+        assert close(g_, O.run(c.ops(), 3, init=st), 1e-12)
+    # one uniform per state in batch order from the shared SmallRng (seed 7721)
+    pre = [O.apply(st.copy(), A.GATE_H, 0, 0) for st in inputs]
+    cpu = [p.copy() for p in pre]
+    rng_cpu = O.Rng(7721)
+    want = [O.measure(a, 0, rng_cpu) for a in cpu]
+    batch = backend.upload_batch(pre)
+    rng_gpu = SmallRng.seeded(7721)
+    assert batch.measure(0, rng_gpu) == want
     assert rng_gpu.state == rng_cpu.state.value
+    for g_, a in zip(batch.download(), cpu):
+        assert close(g_, a, 1e-12)
+
+
+@pytest.mark.parametrize("n,size,dtype,tol", [(14, 5, "c128", C128_TOL), (10, 1000, "c128", C128_TOL),
+                                              (13, 3, "c64", C64_TOL), (2, 7, "c128", 1e-12)])
+def test_batch_sweeps_every_state_like_independent_runs(backend, n, size, dtype, tol):
+    ops = W.random_circuit(n, 16, 5 + n, two_qubit="mixed")
+    r = np.random.default_rng(n)
+    states = [(lambda v: v / np.linalg.norm(v))(r.normal(size=1 << n) + 1j * r.normal(size=1 << n)) for _ in range(size)]
+    batch = StateVectorBatch.from_states(states, dtype=dtype, backend=backend)
+    batch.apply_ops(ops)
+    got = batch.download()
+    for b in sorted({0, size // 2, size - 1}):
+        assert close(got[b], O.run(ops, n, init=states[b]), tol), b
+    rng_gpu, rng_cpu = SmallRng.seeded(99), O.Rng(99)
+    q = n - 1
+    outs = batch.measure(q, rng_gpu)
+    after = batch.download()
+    for b in sorted({0, size // 2, size - 1}):
+        a = O.run(ops, n, init=states[b])
+        st = O.Rng(0)
+        st.state.value = rng_cpu.state.value
+        for _ in range(b):  # the uniforms of the states before b
+            st.next_f64()
+        assert O.measure(a, q, st) == outs[b]
+        assert close(after[b], a, tol), b
+
+
+def test_batch_copy_errors_and_rejected_ops(backend):
+    src = StateVectorBatch.from_states(_batch_inputs(), backend=backend)
+    dst = StateVectorBatch.zero(3, 4, backend=backend)
+    dst.copy_from_device(src)
+    for a, b in zip(dst.download(), _batch_inputs()):
+        assert np.array_equal(a, b)
+    with pytest.raises(QuantumError) as e:
+        StateVectorBatch.zero(3, 5, backend=backend).copy_from_device(src)
+    assert e.value.kind == "IncompatibleDeviceState"
+    with pytest.raises(QuantumError) as e:
+        StateVectorBatch.zero(3, 0, backend=backend)
+    assert e.value.kind == "EmptyBatch"
+    c = Circuit()
+    c.channel(0, NoiseChannel.Depolarizing(0.1))
+    with pytest.raises(QuantumError) as e:
+        dst.run_circuit(c)
+    assert e.value.kind == "OperationRequiresDensityMatrix"
+    m = Circuit()
+    m.measure(0, 0)
+    with pytest.raises(QuantumError) as e:
+        dst.run_circuit(m)
+    assert e.value.kind == "OperationRequiresShotExecution"
+    with pytest.raises(QuantumError) as e:
+        dst.measure(3, SmallRng.seeded(1))
+    assert e.value.kind == "QubitOutOfRange"
+    with pytest.raises(QuantumError) as e:
+        dst.apply_gate(Gate.H, 5)
+    assert e.value.kind == "QubitOutOfRange"
+    zero = StateVectorBatch.zero(2, 3, backend=backend)
+    assert all(np.array_equal(a, O.zero(2)) for a in zero.download())
 
 
 def test_cuda_resident_measurement_matches_the_cpu_reference(backend):  # :602-622
