@@ -203,6 +203,7 @@ typedef struct qf_gradient_info {
 typedef struct qf_ctx qf_ctx;  /* CudaBackend: device, stream, workspaces */
 typedef struct qf_sv qf_sv;    /* CudaDeviceState: one resident state vector */
 typedef struct qf_batch qf_batch;  /* CudaDeviceStateBatch: equal-width states in one allocation */
+typedef struct qf_dm qf_dm;        /* CudaDeviceDensityMatrix: one resident density matrix */
 
 /* ---------------------------------------------------------------------------
  * Errors and build information
@@ -371,6 +372,47 @@ int qf_batch_measure(qf_batch *batch, uint32_t qubit, uint64_t *rng_state, uint8
 int qf_run_circuit_batch(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops,
                          const double *in_amps, uint64_t batch_size, double *out_amps, uint64_t n_doubles,
                          const qf_exec_opts *opts);
+
+/* ---------------------------------------------------------------------------
+ * Density matrices — replace DensityMatrix (src/lib.rs:1551-2235),
+ * Circuit::run_density (src/lib.rs:2804-2818) and the CUDA density path
+ * (CudaBackend::upload_density / run_density_circuit, CudaDeviceDensityMatrix,
+ * src/cuda.rs:969-1045, 2007-2237). Entries are row-major rho[row * 2^n + col],
+ * f64 interleaved on the host (2 * 4^qubits doubles).
+ * ------------------------------------------------------------------------- */
+
+/* |0...0><0...0| on `qubits` qubits (1..17; the entries take 16 * 4^qubits
+ * bytes in complex128). */
+int qf_dm_create(qf_ctx *ctx, uint32_t qubits, int dtype, qf_dm **out);
+int qf_dm_destroy(qf_dm *dm);
+int qf_dm_qubits(const qf_dm *dm, uint32_t *qubits_out);
+/* upload_density (src/cuda.rs:969-1021) / CudaDeviceDensityMatrix::download. */
+int qf_dm_upload(qf_dm *dm, const double *entries, uint64_t n_doubles);
+int qf_dm_download(qf_dm *dm, double *entries_out, uint64_t n_doubles);
+/* DensityMatrix::from_state (src/lib.rs:1641-1655) from a resident state of
+ * the same width and dtype; maximally_mixed (src/lib.rs:1658-1700). */
+int qf_dm_from_state(qf_dm *dm, const qf_sv *psi);
+int qf_dm_set_maximally_mixed(qf_dm *dm);
+/* Circuit::run_density (src/lib.rs:2804-2818) on the resident matrix: gates
+ * (apply, src/lib.rs:2043-2054; apply_cnot/cz/swap :1983-2031) and channels
+ * (apply_channel, :2056-2143); measurements and conditionals ->
+ * QF_ERR_OPERATION_REQUIRES_SHOT_EXECUTION. The whole list is validated
+ * before anything runs. */
+int qf_dm_apply_ops(qf_dm *dm, const qf_op *ops, uint64_t n_ops, const qf_exec_opts *opts);
+/* trace (src/lib.rs:1732-1736, out[0] re, out[1] im), purity (:1738-1741),
+ * expectation / expectation_z (:1858-1904, observable = enum qf_pauli1),
+ * probability_one (:1906-1920), diagonal probabilities (2^qubits values). */
+int qf_dm_trace(qf_dm *dm, double out[2]);
+int qf_dm_purity(qf_dm *dm, double *out);
+int qf_dm_expectation(qf_dm *dm, int observable, uint32_t qubit, double *out);
+int qf_dm_probability_one(qf_dm *dm, uint32_t qubit, double *out);
+int qf_dm_probabilities(qf_dm *dm, double *out, uint64_t n_out);
+/* DensityMatrix::measure (src/lib.rs:1922-1947), CudaDeviceDensityMatrix::measure. */
+int qf_dm_measure(qf_dm *dm, uint32_t qubit, uint64_t *rng_state, uint8_t *outcome);
+/* CudaBackend::run_density_circuit (src/cuda.rs:1022-1045): upload, run, download. */
+int qf_run_density_circuit(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops,
+                           const double *in_entries, double *out_entries, uint64_t n_doubles,
+                           const qf_exec_opts *opts);
 
 /* ---------------------------------------------------------------------------
  * Gradients — ParameterizedCircuit::gradient_with_inputs

@@ -53,6 +53,17 @@ def lib():
             "qfo_sv_normalize": ([P, U32], C.c_int),
             "qfo_sv_channel_trajectory": ([P, U32, C.c_int, F64, F64, U32, C.POINTER(U64)], C.c_int),
             "qfo_run_shots_tree": ([P, U32, P, U64, U64, U64, P, C.POINTER(U32), C.c_int], C.c_int),
+            "qfo_dm_from_state": ([P, U32, P], None),
+            "qfo_dm_maximally_mixed": ([U32, P], None),
+            "qfo_dm_apply": ([P, U32, C.c_int, F64, U32], C.c_int),
+            "qfo_dm_apply_2q": ([P, U32, C.c_int, U32, U32], C.c_int),
+            "qfo_dm_apply_channel": ([P, U32, C.c_int, F64, F64, U32], C.c_int),
+            "qfo_dm_trace": ([P, U32, P], None),
+            "qfo_dm_purity": ([P, U32], F64),
+            "qfo_dm_expectation": ([P, U32, C.c_int, U32, C.POINTER(F64)], C.c_int),
+            "qfo_dm_probability_one": ([P, U32, U32, C.POINTER(F64)], C.c_int),
+            "qfo_dm_measure": ([P, U32, U32, C.POINTER(U64), C.POINTER(C.c_uint8)], C.c_int),
+            "qfo_run_density": ([P, U32, P, U64], C.c_int),
             "qfo_parameter_shift_gradient": ([U32, P, U64, P, U64, P, U64, P, U64, P, C.c_int], C.c_int),
             "qfo_finite_difference_gradient": ([U32, P, U64, P, U64, P, U64, P, U64, F64, P, C.c_int], C.c_int),
             "qfo_adjoint_gradient_stored": ([U32, P, U64, P, U64, P, U64, P, U64, P], C.c_int),
@@ -200,6 +211,76 @@ def run_shots(ops, n, shots, seed, init=None, literal=False, threads=0, noise=Fa
 def counts(packed: np.ndarray, width: int) -> dict:
     vals, cnts = np.unique(packed, return_counts=True)
     return dict(sorted({tuple(int((int(v) >> b) & 1) for b in range(width)): int(c) for v, c in zip(vals, cnts)}.items()))
+
+
+# ---- density matrices (row-major D x D complex128) ---------------------------
+def _dm_n(rho) -> int:
+    return int(rho.shape[0]).bit_length() - 1
+
+
+def dm_from_state(a) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.complex128)
+    rho = np.empty((a.size, a.size), dtype=np.complex128)
+    lib().qfo_dm_from_state(_p(a), a.size.bit_length() - 1, _p(rho))
+    return rho
+
+
+def dm_maximally_mixed(n: int) -> np.ndarray:
+    rho = np.empty((1 << n, 1 << n), dtype=np.complex128)
+    lib().qfo_dm_maximally_mixed(n, _p(rho))
+    return rho
+
+
+def dm_apply(rho, gate: int, theta: float, q: int) -> np.ndarray:
+    _chk(lib().qfo_dm_apply(_p(rho), _dm_n(rho), gate, theta, q))
+    return rho
+
+
+def dm_apply_2q(rho, kind: int, a: int, b: int) -> np.ndarray:
+    _chk(lib().qfo_dm_apply_2q(_p(rho), _dm_n(rho), kind, a, b))
+    return rho
+
+
+def dm_channel(rho, kind: int, p: float, q: int, beta_delta: float = 0.0) -> np.ndarray:
+    _chk(lib().qfo_dm_apply_channel(_p(rho), _dm_n(rho), kind, p, beta_delta, q))
+    return rho
+
+
+def dm_trace(rho) -> complex:
+    out = np.zeros(2)
+    lib().qfo_dm_trace(_p(rho), _dm_n(rho), _p(out))
+    return complex(out[0], out[1])
+
+
+def dm_purity(rho) -> float:
+    return lib().qfo_dm_purity(_p(rho), _dm_n(rho))
+
+
+def dm_expectation(rho, observable: int, q: int) -> float:
+    v = F64()
+    _chk(lib().qfo_dm_expectation(_p(rho), _dm_n(rho), observable, q, C.byref(v)))
+    return v.value
+
+
+def dm_probability_one(rho, q: int) -> float:
+    v = F64()
+    _chk(lib().qfo_dm_probability_one(_p(rho), _dm_n(rho), q, C.byref(v)))
+    return v.value
+
+
+def dm_measure(rho, q: int, rng: Rng) -> int:
+    o = C.c_uint8()
+    _chk(lib().qfo_dm_measure(_p(rho), _dm_n(rho), q, C.byref(rng.state), C.byref(o)))
+    return o.value
+
+
+def run_density(ops, n: int, rho=None) -> np.ndarray:
+    """Circuit::run_density from `rho` (default |0...0><0...0|)."""
+    if rho is None:
+        rho = dm_from_state(zero(n))
+    rho = np.ascontiguousarray(rho, dtype=np.complex128).copy()
+    _chk(lib().qfo_run_density(_p(rho), n, _p(ops), len(ops)))
+    return rho
 
 
 # ---- gradients --------------------------------------------------------------

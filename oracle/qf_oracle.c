@@ -1009,3 +1009,254 @@ int qfo_random_3_regular(uint32_t n, uint64_t seed, uint32_t *edges_uv) {
     free(stubs); free(eu);
     return found ? 0 : QF_ERR_UNSUPPORTED_OPERATION;
 }
+
+/* ---- DensityMatrix (src/lib.rs:1551-2235) -------------------------------
+ * Row-major entries rho[row * D + col], D = 2^n, interleaved f64. */
+
+/* DensityMatrix::from_state (src/lib.rs:1641-1655): rho = |psi><psi|. */
+void qfo_dm_from_state(const double *amps, uint32_t n, double *rho) {
+    const uint64_t D = 1ULL << n;
+    const cplx *a = (const cplx *)amps;
+    cplx *r = (cplx *)rho;
+    for (uint64_t row = 0; row < D; ++row)
+        for (uint64_t col = 0; col < D; ++col) r[row * D + col] = c_mul(a[row], c_conj(a[col]));
+}
+
+/* DensityMatrix::maximally_mixed_with_memory_budget (src/lib.rs:1668-1700): I / 2^n. */
+void qfo_dm_maximally_mixed(uint32_t n, double *rho) {
+    const uint64_t D = 1ULL << n;
+    cplx *r = (cplx *)rho;
+    const double v = 1.0 / (double)D;
+    for (uint64_t i = 0; i < D * D; ++i) r[i] = c_new(0.0, 0.0);
+    for (uint64_t i = 0; i < D; ++i) r[i * D + i] = c_new(v, 0.0);
+}
+
+/* DensityMatrix::local_transform (src/lib.rs:2169-2206): M rho M^dagger as
+ * a left pass over rows then a right pass over columns, into `out`. */
+static int dm_local_transform(const cplx *e, uint64_t D, const cplx m[4], uint32_t q, cplx *out) {
+    const uint64_t mask = 1ULL << q;
+    cplx *left = (cplx *)malloc(sizeof(cplx) * D * D);
+    if (!left) return QF_ERR_MEMORY_ALLOCATION_FAILED;
+    for (uint64_t row = 0; row < D; ++row) {
+        const uint64_t row0 = row & ~mask, row1 = row0 | mask;
+        for (uint64_t col = 0; col < D; ++col) {
+            const cplx a = e[row0 * D + col], b = e[row1 * D + col];
+            left[row * D + col] = (row & mask) == 0 ? c_add(c_mul(m[0], a), c_mul(m[1], b))
+                                                    : c_add(c_mul(m[2], a), c_mul(m[3], b));
+        }
+    }
+    for (uint64_t row = 0; row < D; ++row) {
+        for (uint64_t col = 0; col < D; ++col) {
+            const uint64_t col0 = col & ~mask, col1 = col0 | mask;
+            const cplx a = left[row * D + col0], b = left[row * D + col1];
+            out[row * D + col] = (col & mask) == 0 ? c_add(c_mul(a, c_conj(m[0])), c_mul(b, c_conj(m[1])))
+                                                   : c_add(c_mul(a, c_conj(m[2])), c_mul(b, c_conj(m[3])));
+        }
+    }
+    free(left);
+    return 0;
+}
+
+/* DensityMatrix::apply (src/lib.rs:2043-2054). */
+int qfo_dm_apply(double *rho, uint32_t n, int gate, double theta, uint32_t q) {
+    if (q >= n) return QF_ERR_QUBIT_OUT_OF_RANGE;
+    cplx m[4];
+    int st = gate_matrix(gate, theta, m);
+    if (st) return st;
+    const uint64_t D = 1ULL << n;
+    cplx *out = (cplx *)malloc(sizeof(cplx) * D * D);
+    if (!out) return QF_ERR_MEMORY_ALLOCATION_FAILED;
+    st = dm_local_transform((cplx *)rho, D, m, q, out);
+    if (!st) memcpy(rho, out, sizeof(cplx) * D * D);
+    free(out);
+    return st;
+}
+
+/* DensityMatrix::apply_basis_permutation (src/lib.rs:2033-2041) for CNOT,
+ * SWAP (src/lib.rs:1983-1997, 2018-2031); CZ flips signs (src/lib.rs:1999-2016). */
+int qfo_dm_apply_2q(double *rho, uint32_t n, int kind, uint32_t a, uint32_t b) {
+    int st = check_pair(n, a, b);
+    if (st) return st;
+    const uint64_t D = 1ULL << n, am = 1ULL << a, bm = 1ULL << b;
+    cplx *e = (cplx *)rho;
+    if (kind == QF_OP_CZ) {
+        for (uint64_t row = 0; row < D; ++row)
+            for (uint64_t col = 0; col < D; ++col) {
+                if ((row & am) && (row & bm)) e[row * D + col] = c_mulf(e[row * D + col], -1.0);
+                if ((col & am) && (col & bm)) e[row * D + col] = c_mulf(e[row * D + col], -1.0);
+            }
+        return 0;
+    }
+    cplx *orig = (cplx *)malloc(sizeof(cplx) * D * D);
+    if (!orig) return QF_ERR_MEMORY_ALLOCATION_FAILED;
+    memcpy(orig, e, sizeof(cplx) * D * D);
+    for (uint64_t row = 0; row < D; ++row) {
+        for (uint64_t col = 0; col < D; ++col) {
+            uint64_t pr = row, pc = col;
+            if (kind == QF_OP_CNOT) {
+                if (row & am) pr ^= bm;
+                if (col & am) pc ^= bm;
+            } else {
+                if (((row & am) == 0) != ((row & bm) == 0)) pr ^= am ^ bm;
+                if (((col & am) == 0) != ((col & bm) == 0)) pc ^= am ^ bm;
+            }
+            e[row * D + col] = orig[pr * D + pc];
+        }
+    }
+    free(orig);
+    return 0;
+}
+
+/* apply_kraus (src/lib.rs:2145-2156): the sum of local_transform(K) in order. */
+static int dm_apply_kraus(double *rho, uint32_t n, const cplx (*ops)[4], int count, uint32_t q) {
+    const uint64_t D = 1ULL << n, E = D * D;
+    cplx *sum = (cplx *)calloc(E, sizeof(cplx));
+    cplx *branch = (cplx *)malloc(sizeof(cplx) * E);
+    int st = 0;
+    if (!sum || !branch) st = QF_ERR_MEMORY_ALLOCATION_FAILED;
+    for (uint64_t i = 0; i < E && !st; ++i) sum[i] = c_new(0.0, 0.0);
+    for (int k = 0; k < count && !st; ++k) {
+        st = dm_local_transform((cplx *)rho, D, ops[k], q, branch);
+        for (uint64_t i = 0; i < E && !st; ++i) sum[i] = c_add(sum[i], branch[i]);
+    }
+    if (!st) memcpy(rho, sum, sizeof(cplx) * E);
+    free(sum);
+    free(branch);
+    return st;
+}
+
+/* DensityMatrix::depolarize (src/lib.rs:2208-2233). */
+static int dm_depolarize(double *rho, uint32_t n, uint32_t q, double p) {
+    const uint64_t D = 1ULL << n, E = D * D;
+    cplx *mixed = (cplx *)malloc(sizeof(cplx) * E);
+    cplx *branch = (cplx *)malloc(sizeof(cplx) * E);
+    int st = 0;
+    if (!mixed || !branch) st = QF_ERR_MEMORY_ALLOCATION_FAILED;
+    for (uint64_t i = 0; i < E && !st; ++i) mixed[i] = c_new(0.0, 0.0);
+    const int gates[3] = {QF_GATE_X, QF_GATE_Y, QF_GATE_Z};
+    for (int g = 0; g < 3 && !st; ++g) {
+        memcpy(branch, rho, sizeof(cplx) * E);
+        st = qfo_dm_apply((double *)branch, n, gates[g], 0.0, q);
+        for (uint64_t i = 0; i < E && !st; ++i) mixed[i] = c_add(mixed[i], c_mulf(branch[i], p / 3.0));
+    }
+    const cplx *orig = (const cplx *)rho;
+    for (uint64_t i = 0; i < E && !st; ++i) mixed[i] = c_add(mixed[i], c_mulf(orig[i], 1.0 - p));
+    if (!st) memcpy(rho, mixed, sizeof(cplx) * E);
+    free(mixed);
+    free(branch);
+    return st;
+}
+
+/* DensityMatrix::apply_channel (src/lib.rs:2056-2143). */
+int qfo_dm_apply_channel(double *rho, uint32_t n, int channel, double p, double beta_delta, uint32_t q) {
+    if (q >= n) return QF_ERR_QUBIT_OUT_OF_RANGE;
+    const cplx z = c_new(0.0, 0.0), one = c_new(1.0, 0.0);
+    if (channel == QF_CHANNEL_DEPOLARIZING) {
+        if (!valid_probability(p)) return QF_ERR_INVALID_PROBABILITY;
+        return dm_depolarize(rho, n, q, p);
+    }
+    if (channel == QF_CHANNEL_AMPLITUDE_DAMPING || channel == QF_CHANNEL_PHASE_DAMPING) {
+        if (!valid_probability(p)) return QF_ERR_INVALID_PROBABILITY;
+        cplx k[2][4] = {{one, z, z, c_new(sqrt(1.0 - p), 0.0)}, {z, z, z, z}};
+        if (channel == QF_CHANNEL_AMPLITUDE_DAMPING) k[1][1] = c_new(sqrt(p), 0.0);
+        else k[1][3] = c_new(sqrt(p), 0.0);
+        return dm_apply_kraus(rho, n, (const cplx (*)[4])k, 2, q);
+    }
+    if (channel == QF_CHANNEL_THERMAL_DAMPING) {
+        if (!valid_probability(p)) return QF_ERR_INVALID_PROBABILITY;
+        if (!isfinite(beta_delta) || beta_delta < 0.0) return QF_ERR_INVALID_PROBABILITY;
+        const double gu = p * exp(-beta_delta), gd = p;
+        cplx k[3][4] = {{c_new(sqrt(1.0 - gu), 0.0), z, z, c_new(sqrt(1.0 - gd), 0.0)},
+                        {z, c_new(sqrt(gd), 0.0), z, z},
+                        {z, z, c_new(sqrt(gu), 0.0), z}};
+        return dm_apply_kraus(rho, n, (const cplx (*)[4])k, 3, q);
+    }
+    return QF_ERR_INVALID_ARGUMENT;
+}
+
+/* trace (src/lib.rs:1732-1736), purity (:1738-1741). */
+void qfo_dm_trace(const double *rho, uint32_t n, double out[2]) {
+    const uint64_t D = 1ULL << n;
+    const cplx *e = (const cplx *)rho;
+    cplx t = c_new(0.0, 0.0);
+    for (uint64_t i = 0; i < D; ++i) t = c_add(t, e[i * D + i]);
+    out[0] = t.re;
+    out[1] = t.im;
+}
+
+double qfo_dm_purity(const double *rho, uint32_t n) {
+    const uint64_t E = (1ULL << n) << n;
+    const cplx *e = (const cplx *)rho;
+    double s = SUM_INIT;
+    for (uint64_t i = 0; i < E; ++i) s += c_norm_sqr(e[i]);
+    return s;
+}
+
+/* expectation_z / expectation (src/lib.rs:1858-1904), probability_one (:1906-1920). */
+int qfo_dm_expectation(const double *rho, uint32_t n, int observable, uint32_t q, double *out) {
+    if (q >= n) return QF_ERR_QUBIT_OUT_OF_RANGE;
+    const uint64_t D = 1ULL << n, mask = 1ULL << q;
+    const cplx *e = (const cplx *)rho;
+    if (observable == QF_PAULI_Z) {
+        double s = SUM_INIT;
+        for (uint64_t i = 0; i < D; ++i) s += ((i & mask) == 0 ? 1.0 : -1.0) * e[i * D + i].re;
+        *out = s;
+        return 0;
+    }
+    if (observable != QF_PAULI_X && observable != QF_PAULI_Y) return QF_ERR_INVALID_ARGUMENT;
+    double v = 0.0;
+    for (uint64_t row = 0; row < D; ++row) {
+        if (row & mask) continue;
+        const cplx c = e[row * D + (row | mask)];
+        v += observable == QF_PAULI_X ? 2.0 * c.re : -2.0 * c.im;
+    }
+    *out = v;
+    return 0;
+}
+
+int qfo_dm_probability_one(const double *rho, uint32_t n, uint32_t q, double *out) {
+    if (q >= n) return QF_ERR_QUBIT_OUT_OF_RANGE;
+    const uint64_t D = 1ULL << n, mask = 1ULL << q;
+    const cplx *e = (const cplx *)rho;
+    double s = SUM_INIT;
+    for (uint64_t i = 0; i < D; ++i)
+        if (i & mask) s += e[i * D + i].re;
+    *out = clamp01(s);
+    return 0;
+}
+
+/* DensityMatrix::measure (src/lib.rs:1922-1947). */
+int qfo_dm_measure(double *rho, uint32_t n, uint32_t q, uint64_t *rng_state, uint8_t *outcome) {
+    double p_one;
+    int st = qfo_dm_probability_one(rho, n, q, &p_one);
+    if (st) return st;
+    const uint8_t o = qfo_rng_next_f64(rng_state) < p_one ? 1 : 0;
+    const double probability = o == 1 ? p_one : 1.0 - p_one;
+    if (probability <= DBL_EPSILON) return QF_ERR_INVALID_PROBABILITY;
+    const uint64_t D = 1ULL << n, mask = 1ULL << q;
+    cplx *e = (cplx *)rho;
+    for (uint64_t row = 0; row < D; ++row)
+        for (uint64_t col = 0; col < D; ++col) {
+            if ((uint8_t)((row & mask) != 0) != o || (uint8_t)((col & mask) != 0) != o) e[row * D + col] = c_new(0.0, 0.0);
+            else e[row * D + col] = c_divf(e[row * D + col], probability);
+        }
+    *outcome = o;
+    return 0;
+}
+
+/* Circuit::run_density (src/lib.rs:2804-2818). */
+int qfo_run_density(double *rho, uint32_t n, const qf_op *ops, uint64_t n_ops) {
+    for (uint64_t k = 0; k < n_ops; ++k) {
+        const qf_op *op = &ops[k];
+        int st;
+        switch (op->kind) {
+        case QF_OP_GATE: st = qfo_dm_apply(rho, n, op->gate, op->theta, op->q0); break;
+        case QF_OP_CNOT: case QF_OP_CZ: case QF_OP_SWAP: st = qfo_dm_apply_2q(rho, n, op->kind, op->q0, op->q1); break;
+        case QF_OP_CHANNEL: st = qfo_dm_apply_channel(rho, n, op->gate, op->theta, qf_op_aux(op), op->q0); break;
+        case QF_OP_MEASURE: case QF_OP_COND: st = QF_ERR_OPERATION_REQUIRES_SHOT_EXECUTION; break;
+        default: st = QF_ERR_INVALID_ARGUMENT; break;
+        }
+        if (st) return st;
+    }
+    return 0;
+}

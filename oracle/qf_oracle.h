@@ -71,6 +71,20 @@ int qfo_run_shots_noisy_literal(const double *init_amps, uint32_t n, const qf_op
 int qfo_run_shots_tree(const double *init_amps, uint32_t n, const qf_op *ops, uint64_t n_ops,
                        uint64_t shots, uint64_t seed, uint64_t *outcomes, uint32_t *width, int threads);
 
+/* DensityMatrix (src/lib.rs:1551-2235): row-major entries rho[row * 2^n + col],
+ * interleaved f64 (2 * 4^n doubles). */
+void qfo_dm_from_state(const double *amps, uint32_t n, double *rho);
+void qfo_dm_maximally_mixed(uint32_t n, double *rho);
+int qfo_dm_apply(double *rho, uint32_t n, int gate, double theta, uint32_t q);
+int qfo_dm_apply_2q(double *rho, uint32_t n, int kind, uint32_t a, uint32_t b);  /* kind: QF_OP_CNOT/CZ/SWAP */
+int qfo_dm_apply_channel(double *rho, uint32_t n, int channel, double p, double beta_delta, uint32_t q);
+void qfo_dm_trace(const double *rho, uint32_t n, double out[2]);
+double qfo_dm_purity(const double *rho, uint32_t n);
+int qfo_dm_expectation(const double *rho, uint32_t n, int observable, uint32_t q, double *out);
+int qfo_dm_probability_one(const double *rho, uint32_t n, uint32_t q, double *out);
+int qfo_dm_measure(double *rho, uint32_t n, uint32_t q, uint64_t *rng_state, uint8_t *outcome);
+int qfo_run_density(double *rho, uint32_t n, const qf_op *ops, uint64_t n_ops);
+
 /* Gradients. `terms` is the observable (one term = SingleQubitObservable). */
 int qfo_parameter_shift_gradient(uint32_t n, const qf_op *ops, uint64_t n_ops,
                                  const double *params, uint64_t n_params,

@@ -11,6 +11,7 @@ from ._native import QuantumError, load as load_library
 from .core import (
     Circuit,
     CudaBackend,
+    DensityMatrix,
     Gate,
     NoiseChannel,
     ParameterizedCircuit,
@@ -26,7 +27,7 @@ from .core import (
 from . import gradients
 
 __all__ = [
-    "Circuit", "CudaBackend", "Gate", "NoiseChannel", "ParameterizedCircuit", "PauliSum", "QuantumError", "RotationAxis",
+    "Circuit", "CudaBackend", "DensityMatrix", "Gate", "NoiseChannel", "ParameterizedCircuit", "PauliSum", "QuantumError", "RotationAxis",
     "ShotResult", "SingleQubitObservable", "SmallRng", "StateVector", "StateVectorBatch", "default_backend", "gradients",
     "load_library",
 ]

@@ -77,6 +77,21 @@ SIGNATURES = {
     "qf_batch_apply_ops": [P, P, U64, P],
     "qf_batch_measure": [P, U32, PU64, P],
     "qf_run_circuit_batch": [P, U32, C.c_int, P, U64, P, U64, P, U64, P],
+    "qf_dm_create": [P, U32, C.c_int, C.POINTER(P)],
+    "qf_dm_destroy": [P],
+    "qf_dm_qubits": [P, PU32],
+    "qf_dm_upload": [P, P, U64],
+    "qf_dm_download": [P, P, U64],
+    "qf_dm_from_state": [P, P],
+    "qf_dm_set_maximally_mixed": [P],
+    "qf_dm_apply_ops": [P, P, U64, P],
+    "qf_dm_trace": [P, P],
+    "qf_dm_purity": [P, PF64],
+    "qf_dm_expectation": [P, C.c_int, U32, PF64],
+    "qf_dm_probability_one": [P, U32, PF64],
+    "qf_dm_probabilities": [P, P, U64],
+    "qf_dm_measure": [P, U32, PU64, P],
+    "qf_run_density_circuit": [P, U32, C.c_int, P, U64, P, P, U64, P],
     "qf_sv_sample": [P, P, P, U32, U64, U64, F64, P, PU64],
     "qf_gradient": [P, U32, P, U64, P, U64, P, U64, P, U64, P, P, P, P],
     "qf_expectation": [P, U32, C.c_int, P, U64, P, U64, P, U64, P, U64, P, PF64],

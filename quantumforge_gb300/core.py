@@ -283,6 +283,24 @@ class CudaBackend:
                                           out.size, _exec(exec_opts)))
         return list(out.view(np.complex128).reshape(len(arrs), 1 << n).copy())
 
+    def upload_density(self, entries, dtype="c128") -> "DensityMatrix":
+        """CudaBackend::upload_density (src/cuda.rs:969-1021)."""
+        return DensityMatrix.from_entries(entries, dtype=dtype, backend=self)
+
+    def run_density_circuit(self, initial, circuit: "Circuit", dtype="c128", exec_opts=None) -> np.ndarray:
+        """CudaBackend::run_density_circuit (src/cuda.rs:1022-1045): host
+        entries in, host entries out."""
+        e = initial.entries() if isinstance(initial, DensityMatrix) else np.asarray(initial, dtype=np.complex128)
+        e = np.ascontiguousarray(e, dtype=np.complex128)
+        d = int(e.shape[0])
+        n = d.bit_length() - 1
+        src = e.reshape(-1).view(np.float64)
+        out = np.empty_like(src)
+        ops = circuit.ops()
+        check(load().qf_run_density_circuit(self._h, n, _dtype_code(dtype), ptr(ops), len(ops), ptr(src), ptr(out),
+                                            out.size, _exec(exec_opts)))
+        return out.view(np.complex128).reshape(d, d)
+
     def run_circuit_shots(self, initial_state, circuit: "Circuit", shots: int, seed: int, dtype="c128",
                           tie_eps: float = 0.0) -> "ShotResult":
         return circuit.run_shots(initial_state, shots, seed, dtype=dtype, backend=self, tie_eps=tie_eps)
@@ -536,6 +554,124 @@ class StateVectorBatch:
         return list(out.view(np.complex128).reshape(self.size, 1 << self.qubits).copy())
 
 
+class DensityMatrix:
+    """`DensityMatrix` (src/lib.rs:1551-2235) resident on the device, the
+    reference's `CudaDeviceDensityMatrix` (src/cuda.rs:2007-2237): row-major
+    entries rho[row, col]; gates act as U rho U^dagger, channels as their Kraus
+    sums."""
+
+    def __init__(self, handle, qubits: int, dtype: int, backend: CudaBackend):
+        self._h, self.n, self.dtype, self.backend = handle, qubits, dtype, backend
+
+    @classmethod
+    def zero(cls, qubits: int, dtype="c128", backend: CudaBackend | None = None) -> "DensityMatrix":
+        backend = backend or default_backend()
+        h = C.c_void_p()
+        code = _dtype_code(dtype)
+        check(load().qf_dm_create(backend.handle, int(qubits), code, C.byref(h)))
+        return cls(h, int(qubits), code, backend)
+
+    @classmethod
+    def from_state(cls, state: "StateVector") -> "DensityMatrix":
+        rho = cls.zero(state.qubits, dtype=state.dtype, backend=state.backend)
+        check(load().qf_dm_from_state(rho._h, state._h))
+        return rho
+
+    @classmethod
+    def maximally_mixed(cls, qubits: int, dtype="c128", backend: CudaBackend | None = None) -> "DensityMatrix":
+        rho = cls.zero(qubits, dtype=dtype, backend=backend)
+        check(load().qf_dm_set_maximally_mixed(rho._h))
+        return rho
+
+    @classmethod
+    def from_entries(cls, entries, dtype="c128", backend: CudaBackend | None = None) -> "DensityMatrix":
+        e = np.ascontiguousarray(entries, dtype=np.complex128)
+        n = int(e.shape[0]).bit_length() - 1
+        rho = cls.zero(n, dtype=dtype, backend=backend)
+        flat = e.reshape(-1).view(np.float64)
+        check(load().qf_dm_upload(rho._h, ptr(flat), flat.size))
+        return rho
+
+    def __del__(self):
+        try:
+            if self._h and self._h.value:
+                load().qf_dm_destroy(self._h)
+                self._h = C.c_void_p()
+        except Exception:
+            pass
+
+    def qubits(self) -> int:
+        return self.n
+
+    def dimension(self) -> int:
+        return 1 << self.n
+
+    def entries(self) -> np.ndarray:
+        d = 1 << self.n
+        out = np.empty(2 * d * d, dtype=np.float64)
+        check(load().qf_dm_download(self._h, ptr(out), out.size))
+        return out.view(np.complex128).reshape(d, d)
+
+    def apply_ops(self, ops: np.ndarray, exec_opts=None) -> "DensityMatrix":
+        check(load().qf_dm_apply_ops(self._h, ptr(ops), len(ops), _exec(exec_opts)))
+        return self
+
+    def apply(self, gate: Gate, qubit: int) -> "DensityMatrix":
+        return self.apply_ops(_abi.ops_array([(_abi.OP_GATE, gate.code, int(qubit), 0, 0, gate.theta)]))
+
+    def apply_cnot(self, control: int, target: int) -> "DensityMatrix":
+        return self.apply_ops(_abi.ops_array([(_abi.OP_CNOT, 0, int(control), int(target), 0, 0.0)]))
+
+    def apply_cz(self, first: int, second: int) -> "DensityMatrix":
+        return self.apply_ops(_abi.ops_array([(_abi.OP_CZ, 0, int(first), int(second), 0, 0.0)]))
+
+    def apply_swap(self, first: int, second: int) -> "DensityMatrix":
+        return self.apply_ops(_abi.ops_array([(_abi.OP_SWAP, 0, int(first), int(second), 0, 0.0)]))
+
+    def apply_channel(self, channel: "NoiseChannel", qubit: int) -> "DensityMatrix":
+        return self.apply_ops(_abi.ops_array([channel.record(int(qubit))]))
+
+    def depolarize(self, qubit: int, probability: float) -> "DensityMatrix":
+        return self.apply_channel(NoiseChannel.Depolarizing(probability), qubit)
+
+    def trace(self) -> complex:
+        out = np.zeros(2)
+        check(load().qf_dm_trace(self._h, ptr(out)))
+        return complex(out[0], out[1])
+
+    def purity(self) -> float:
+        v = C.c_double()
+        check(load().qf_dm_purity(self._h, C.byref(v)))
+        return v.value
+
+    def expectation(self, observable: int, qubit: int) -> float:
+        v = C.c_double()
+        check(load().qf_dm_expectation(self._h, int(observable), int(qubit), C.byref(v)))
+        return v.value
+
+    def expectation_z(self, qubit: int) -> float:
+        return self.expectation(_abi.PAULI_Z, qubit)
+
+    def probability_one(self, qubit: int) -> float:
+        v = C.c_double()
+        check(load().qf_dm_probability_one(self._h, int(qubit), C.byref(v)))
+        return v.value
+
+    def probabilities(self) -> np.ndarray:
+        out = np.empty(1 << self.n, dtype=np.float64)
+        check(load().qf_dm_probabilities(self._h, ptr(out), out.size))
+        return out
+
+    def measure(self, qubit: int, rng: SmallRng) -> int:
+        st = C.c_uint64(rng.state)
+        o = C.c_uint8()
+        try:
+            check(load().qf_dm_measure(self._h, int(qubit), C.byref(st), C.byref(o)))
+        finally:
+            rng.state = st.value
+        return o.value
+
+
 @dataclass
 class ShotResult:
     """`ShotResult` (src/lib.rs:2453-2464): counts keyed by LSB-first bit tuples."""
@@ -658,6 +794,10 @@ class Circuit:
                   tie_eps: float = 0.0, exec_opts=None) -> ShotResult:
         """Circuit::run_shots (src/lib.rs:2822-2916) for terminal measurements."""
         return ShotResult.from_packed(*self.run_shots_packed(initial_state, shots, seed, dtype, backend, tie_eps, exec_opts))
+
+    def run_density(self, state: "DensityMatrix", exec_opts=None) -> "DensityMatrix":
+        """Circuit::run_density (src/lib.rs:2804-2818), in place on the device matrix."""
+        return state.apply_ops(self.ops(), exec_opts)
 
     def run_shots_with_noise(self, initial_state, shots: int, seed: int, dtype="c128", backend: CudaBackend | None = None,
                              tie_eps: float = 0.0, exec_opts=None) -> ShotResult:

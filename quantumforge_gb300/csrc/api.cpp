@@ -1140,6 +1140,296 @@ int qf_run_circuit_batch(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *o
     return convert_to_f64(&v, out_amps);
 }
 
+// ---- density matrices (DensityMatrix, src/lib.rs:1551-2235) ----------------
+}  // extern "C"
+
+namespace {
+
+// One step of a density-matrix op list: a run of 2n-qubit gates for the fused
+// engine, or one local channel.
+struct DmStep {
+    bool channel = false;
+    std::vector<BGate> gates;
+    uint32_t q = 0;
+    double coef[6] = {0, 0, 0, 0, 0, 0};
+};
+
+int check_dm(const qf_dm *dm) {
+    if (!dm || !dm->sv || !dm->sv->ctx || !dm->sv->d) return fail(QF_ERR_INVALID_ARGUMENT, "density handle is NULL or released");
+    return QF_OK;
+}
+
+// U rho U^dagger on an n-qubit density matrix = U on row bit n + q and conj(U)
+// on column bit q; CNOT/CZ/SWAP permute or sign both sides (apply_basis_permutation,
+// src/lib.rs:2033-2041).
+void lower_to_density(const BGate &g, uint32_t n, std::vector<BGate> &out) {
+    BGate row = g, col = g;
+    row.op_index = col.op_index = -1;
+    row.param = col.param = -1;
+    row.axis = col.axis = 255;
+    row.q0 = g.q0 + n;
+    if (g.kind == BK_MAT1) {
+        for (int k = 0; k < 4; ++k) col.m[2 * k + 1] = -g.m[2 * k + 1];
+    } else {
+        row.q1 = g.q1 + n;
+    }
+    out.push_back(row);
+    out.push_back(col);
+}
+
+// apply_channel (src/lib.rs:2056-2143) as the real superoperator of the
+// channel on (row bit, column bit): populations mix, coherences scale.
+int channel_coefficients(const qf_op &o, double coef[6]) {
+    const double p = o.theta;
+    auto bad = [](double v) { return fail(QF_ERR_INVALID_PROBABILITY, "probability must be in [0, 1], got %g", v); };
+    switch (o.gate) {
+    case QF_CHANNEL_DEPOLARIZING: {  // (1-p) rho + p/3 (X rho X + Y rho Y + Z rho Z)
+        if (!valid_probability(p)) return bad(p);
+        const double t = p / 3.0;
+        coef[0] = coef[3] = (1.0 - p) + t;
+        coef[1] = coef[2] = t + t;
+        coef[4] = coef[5] = (1.0 - p) - t;
+        return QF_OK;
+    }
+    case QF_CHANNEL_AMPLITUDE_DAMPING:
+        if (!valid_probability(p)) return bad(p);
+        coef[0] = 1.0, coef[1] = p, coef[2] = 0.0, coef[3] = 1.0 - p;
+        coef[4] = coef[5] = std::sqrt(1.0 - p);
+        return QF_OK;
+    case QF_CHANNEL_PHASE_DAMPING:
+        if (!valid_probability(p)) return bad(p);
+        coef[0] = 1.0, coef[1] = 0.0, coef[2] = 0.0, coef[3] = 1.0;
+        coef[4] = coef[5] = std::sqrt(1.0 - p);
+        return QF_OK;
+    case QF_CHANNEL_THERMAL_DAMPING: {
+        const double beta = qf_op_aux(&o);
+        if (!valid_probability(p)) return bad(p);
+        if (!std::isfinite(beta) || beta < 0.0) return bad(beta);
+        const double gu = p * std::exp(-beta);  // NoiseChannel::thermal_rates (src/lib.rs:1611-1626)
+        coef[0] = 1.0 - gu, coef[1] = p, coef[2] = gu, coef[3] = 1.0 - p;
+        coef[4] = coef[5] = std::sqrt(1.0 - gu) * std::sqrt(1.0 - p);
+        return QF_OK;
+    }
+    default:
+        return fail(QF_ERR_INVALID_ARGUMENT, "unknown noise channel %u", (unsigned)o.gate);
+    }
+}
+
+int lower_density_ops(uint32_t n, const qf_op *ops, uint64_t n_ops, std::vector<DmStep> &steps) {
+    std::vector<qf_op> run;
+    auto close_run = [&]() -> int {
+        if (run.empty()) return QF_OK;
+        std::vector<BGate> g;
+        QF_TRY(bind_ops(n, run.data(), run.size(), nullptr, 0, nullptr, 0, -1, 0.0, g));
+        DmStep st;
+        for (const BGate &x : g) lower_to_density(x, n, st.gates);
+        steps.push_back(std::move(st));
+        run.clear();
+        return QF_OK;
+    };
+    for (uint64_t k = 0; k < n_ops; ++k) {
+        if (ops[k].kind != QF_OP_CHANNEL) {
+            run.push_back(ops[k]);
+            continue;
+        }
+        QF_TRY(close_run());
+        if (ops[k].q0 >= n) return fail(QF_ERR_QUBIT_OUT_OF_RANGE, "qubit index %u is out of range for %u qubits", ops[k].q0, n);
+        DmStep st;
+        st.channel = true;
+        st.q = ops[k].q0;
+        QF_TRY(channel_coefficients(ops[k], st.coef));
+        steps.push_back(std::move(st));
+    }
+    return close_run();
+}
+
+int run_density_steps(qf_sv *sv, uint32_t n, const std::vector<DmStep> &steps, const qf_exec_opts *opts) {
+    for (const DmStep &st : steps) {
+        if (st.channel) QF_TRY(dm_channel(sv, n, st.q, st.coef));
+        else QF_TRY(execute_gates(sv, st.gates, opts));
+    }
+    return QF_OK;
+}
+
+int check_dm_qubits(uint32_t qubits) {
+    if (qubits == 0) return fail(QF_ERR_ZERO_QUBITS, "a state vector must contain at least one qubit");
+    if (qubits > 17) return fail(QF_ERR_STATE_TOO_LARGE, "density matrices of %u qubits exceed the supported allocation", qubits);
+    return QF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qf_dm_create(qf_ctx *ctx, uint32_t qubits, int dtype, qf_dm **out) {
+    clear_error();
+    if (!ctx || !out) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    QF_TRY(check_dtype(dtype));
+    QF_TRY(check_dm_qubits(qubits));
+    QF_TRY(bind_device(ctx));
+    qf_sv *sv;
+    QF_TRY(alloc_state(ctx, 2 * qubits, dtype, 0, &sv));  // entry 0 = 1: |0...0><0...0|
+    *out = new qf_dm{sv, qubits};
+    return QF_OK;
+}
+
+int qf_dm_destroy(qf_dm *dm) {
+    if (!dm) return QF_OK;
+    if (dm->sv) qf_sv_destroy(dm->sv);
+    delete dm;
+    return QF_OK;
+}
+
+int qf_dm_qubits(const qf_dm *dm, uint32_t *qubits_out) {
+    QF_TRY(check_dm(dm));
+    if (!qubits_out) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    *qubits_out = dm->n;
+    return QF_OK;
+}
+
+int qf_dm_upload(qf_dm *dm, const double *entries, uint64_t n_doubles) {
+    clear_error();
+    QF_TRY(check_dm(dm));
+    if (!entries) return fail(QF_ERR_INVALID_ARGUMENT, "entries are NULL");
+    if (n_doubles != 2 * dm->sv->dim)
+        return fail(QF_ERR_STATE_TOO_LARGE, "expected %llu doubles (4^%u complex entries), got %llu",
+                    (unsigned long long)(2 * dm->sv->dim), dm->n, (unsigned long long)n_doubles);
+    QF_TRY(bind_device(dm->sv->ctx));
+    QF_TRY(convert_from_f64(dm->sv, entries));
+    QF_CUDA(cudaStreamSynchronize(dm->sv->ctx->stream));
+    return QF_OK;
+}
+
+int qf_dm_download(qf_dm *dm, double *entries_out, uint64_t n_doubles) {
+    clear_error();
+    QF_TRY(check_dm(dm));
+    if (!entries_out || n_doubles != 2 * dm->sv->dim)
+        return fail(QF_ERR_INVALID_ARGUMENT, "download needs %llu doubles", (unsigned long long)(2 * dm->sv->dim));
+    QF_TRY(bind_device(dm->sv->ctx));
+    return convert_to_f64(dm->sv, entries_out);
+}
+
+int qf_dm_from_state(qf_dm *dm, const qf_sv *psi) {
+    clear_error();
+    QF_TRY(check_dm(dm));
+    QF_TRY(check_sv(psi));
+    if (psi->n != dm->n || psi->dtype != dm->sv->dtype || psi->ctx != dm->sv->ctx)
+        return fail(QF_ERR_INCOMPATIBLE_DEVICE_STATE, "state and density matrix must share a backend, width and dtype");
+    QF_TRY(bind_device(dm->sv->ctx));
+    return dm_from_state(dm->sv, dm->n, psi);
+}
+
+int qf_dm_set_maximally_mixed(qf_dm *dm) {
+    clear_error();
+    QF_TRY(check_dm(dm));
+    QF_TRY(bind_device(dm->sv->ctx));
+    return dm_maximally_mixed(dm->sv, dm->n);
+}
+
+int qf_dm_apply_ops(qf_dm *dm, const qf_op *ops, uint64_t n_ops, const qf_exec_opts *opts) {
+    clear_error();
+    QF_TRY(check_dm(dm));
+    if (n_ops && !ops) return fail(QF_ERR_INVALID_ARGUMENT, "ops is NULL");
+    std::vector<DmStep> steps;
+    QF_TRY(lower_density_ops(dm->n, ops, n_ops, steps));
+    QF_TRY(bind_device(dm->sv->ctx));
+    return run_density_steps(dm->sv, dm->n, steps, opts);
+}
+
+int qf_dm_trace(qf_dm *dm, double out[2]) {
+    clear_error();
+    QF_TRY(check_dm(dm));
+    if (!out) return fail(QF_ERR_INVALID_ARGUMENT, "output is NULL");
+    QF_TRY(bind_device(dm->sv->ctx));
+    return dm_diag_reduce(dm->sv, dm->n, 0, 0, out);
+}
+
+int qf_dm_purity(qf_dm *dm, double *out) {
+    clear_error();
+    QF_TRY(check_dm(dm));
+    if (!out) return fail(QF_ERR_INVALID_ARGUMENT, "output is NULL");
+    QF_TRY(bind_device(dm->sv->ctx));
+    return reduce_norm_sqr(dm->sv, out);  // sum |rho_ij|^2
+}
+
+int qf_dm_expectation(qf_dm *dm, int observable, uint32_t qubit, double *out) {
+    clear_error();
+    QF_TRY(check_dm(dm));
+    if (!out) return fail(QF_ERR_INVALID_ARGUMENT, "output is NULL");
+    if (qubit >= dm->n) return fail(QF_ERR_QUBIT_OUT_OF_RANGE, "qubit index %u is out of range for %u qubits", qubit, dm->n);
+    const int mode = observable == QF_PAULI_Z ? 2 : observable == QF_PAULI_X ? 3 : observable == QF_PAULI_Y ? 4 : -1;
+    if (mode < 0) return fail(QF_ERR_INVALID_ARGUMENT, "unknown observable %d", observable);
+    QF_TRY(bind_device(dm->sv->ctx));
+    double r[2];
+    QF_TRY(dm_diag_reduce(dm->sv, dm->n, qubit, mode, r));
+    *out = r[0];
+    return QF_OK;
+}
+
+int qf_dm_probability_one(qf_dm *dm, uint32_t qubit, double *out) {
+    clear_error();
+    QF_TRY(check_dm(dm));
+    if (!out) return fail(QF_ERR_INVALID_ARGUMENT, "output is NULL");
+    if (qubit >= dm->n) return fail(QF_ERR_QUBIT_OUT_OF_RANGE, "qubit index %u is out of range for %u qubits", qubit, dm->n);
+    QF_TRY(bind_device(dm->sv->ctx));
+    double r[2];
+    QF_TRY(dm_diag_reduce(dm->sv, dm->n, qubit, 1, r));
+    *out = clamp01(r[0]);
+    return QF_OK;
+}
+
+int qf_dm_probabilities(qf_dm *dm, double *out, uint64_t n_out) {
+    clear_error();
+    QF_TRY(check_dm(dm));
+    const uint64_t D = 1ULL << dm->n;
+    if (!out || n_out != D) return fail(QF_ERR_INVALID_ARGUMENT, "probabilities need %llu outputs", (unsigned long long)D);
+    qf_ctx *ctx = dm->sv->ctx;
+    QF_TRY(bind_device(ctx));
+    QF_TRY(ensure_device(&ctx->ws_stage, &ctx->ws_stage_bytes, sizeof(double) * D));
+    QF_TRY(dm_diagonal(dm->sv, dm->n, static_cast<double *>(ctx->ws_stage)));
+    QF_CUDA(cudaMemcpyAsync(out, ctx->ws_stage, sizeof(double) * D, cudaMemcpyDeviceToHost, ctx->stream));
+    QF_CUDA(cudaStreamSynchronize(ctx->stream));
+    return QF_OK;
+}
+
+int qf_dm_measure(qf_dm *dm, uint32_t qubit, uint64_t *rng_state, uint8_t *outcome) {
+    clear_error();
+    QF_TRY(check_dm(dm));
+    if (!rng_state || !outcome) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (qubit >= dm->n) return fail(QF_ERR_QUBIT_OUT_OF_RANGE, "qubit index %u is out of range for %u qubits", qubit, dm->n);
+    QF_TRY(bind_device(dm->sv->ctx));
+    double r[2];
+    QF_TRY(dm_diag_reduce(dm->sv, dm->n, qubit, 1, r));
+    const double p_one = clamp01(r[0]);
+    const uint8_t o = next_uniform(rng_state) < p_one ? 1 : 0;
+    const double prob = o ? p_one : 1.0 - p_one;
+    if (prob <= 2.220446049250313e-16)
+        return fail(QF_ERR_INVALID_PROBABILITY, "measurement probability must be in [0, 1], got %g", prob);
+    QF_TRY(dm_collapse(dm->sv, dm->n, qubit, o, prob));
+    QF_CUDA(cudaStreamSynchronize(dm->sv->ctx->stream));
+    *outcome = o;
+    return QF_OK;
+}
+
+int qf_run_density_circuit(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops, const double *in_entries,
+                           double *out_entries, uint64_t n_doubles, const qf_exec_opts *opts) {
+    clear_error();
+    if (!ctx || !in_entries || !out_entries || (n_ops && !ops)) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    QF_TRY(check_dtype(dtype));
+    QF_TRY(check_dm_qubits(qubits));
+    if (n_doubles != 2 * (1ULL << (2 * qubits)))
+        return fail(QF_ERR_STATE_TOO_LARGE, "expected %llu doubles (4^%u complex entries), got %llu",
+                    (unsigned long long)(2 * (1ULL << (2 * qubits))), qubits, (unsigned long long)n_doubles);
+    std::vector<DmStep> steps;
+    QF_TRY(lower_density_ops(qubits, ops, n_ops, steps));
+    QF_TRY(bind_device(ctx));
+    qf_sv *sv;
+    QF_TRY(scratch_state(ctx, &ctx->scratch_sv, 2 * qubits, dtype, &sv));
+    QF_TRY(convert_from_f64(sv, in_entries));
+    QF_TRY(run_density_steps(sv, qubits, steps, opts));
+    return convert_to_f64(sv, out_entries);
+}
+
 int qf_run_circuit(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops, const double *init_amps,
                    double *out_amps, uint64_t n_doubles, const qf_exec_opts *opts) {
     clear_error();

@@ -1,0 +1,207 @@
+// density.cu — density-matrix kernels (DensityMatrix, src/lib.rs:1551-2235;
+// the reference's CUDA density path, src/cuda.rs:2007-2237).
+//
+// A density matrix of n qubits is stored row-major, rho[row * 2^n + col], as
+// one 2n-qubit vector: column qubit q is index bit q, row qubit q is index bit
+// n + q. Unitaries U rho U^dagger become U on bit n + q and conj(U) on bit q
+// and run through the fused tile engine; the kernels here are the non-unitary
+// pieces: local channels (a real superoperator on the bit pair (n + q, q)),
+// diagonal reductions, measurement collapse and state preparation.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "qf_device.cuh"
+#include "qf_internal.h"
+
+namespace qf {
+
+namespace {
+
+// Insert a zero bit at position p of x.
+__device__ __forceinline__ uint64_t insert0(uint64_t x, uint32_t p) {
+    const uint64_t lo = x & ((1ULL << p) - 1);
+    return ((x >> p) << (p + 1)) | lo;
+}
+
+// One local channel on qubit q: for each (row bit r, col bit c) group
+//   v00' = a v00 + b v11,  v11' = c v00 + d v11,  v01' = e v01,  v10' = f v10
+// (every channel of NoiseChannel has this form: populations mix, coherences scale).
+template <typename C>
+__global__ void k_dm_channel(C *__restrict__ v, uint32_t n, uint32_t q, uint64_t groups, double ca, double cb, double cc,
+                             double cd, double ce, double cf) {
+    using R = typename Real<C>::T;
+    const uint64_t cm = 1ULL << q, rm = 1ULL << (n + q);
+    for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < groups; g += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t i00 = insert0(insert0(g, q), n + q);
+        const C x00 = v[i00], x01 = v[i00 | cm], x10 = v[i00 | rm], x11 = v[i00 | rm | cm];
+        v[i00] = mk((R)(ca * (double)x00.x + cb * (double)x11.x), (R)(ca * (double)x00.y + cb * (double)x11.y));
+        v[i00 | rm | cm] = mk((R)(cc * (double)x00.x + cd * (double)x11.x), (R)(cc * (double)x00.y + cd * (double)x11.y));
+        v[i00 | cm] = mk((R)(ce * (double)x01.x), (R)(ce * (double)x01.y));
+        v[i00 | rm] = mk((R)(cf * (double)x10.x), (R)(cf * (double)x10.y));
+    }
+}
+
+// Diagonal / near-diagonal sums over rows r < 2^n:
+// mode 0: Re and Im of rho[r][r] (trace); 1: Re rho[r][r] where bit q of r is
+// set (P(1)); 2: (+/-) Re rho[r][r] by bit q (<Z_q>); 3: 2 Re rho[r][r|m] and
+// 4: -2 Im rho[r][r|m] over r with bit q clear (<X_q>, <Y_q>).
+template <typename C>
+__global__ void k_dm_diag(const C *__restrict__ v, uint32_t n, uint32_t q, int mode, double *partials) {
+    __shared__ double red[32];
+    const uint64_t D = 1ULL << n, m = 1ULL << q;
+    double s0 = 0.0, s1 = 0.0;
+    for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < D; r += (uint64_t)gridDim.x * blockDim.x) {
+        if (mode <= 2) {
+            const C x = v[(r << n) | r];
+            if (mode == 0) {
+                s0 += (double)x.x;
+                s1 += (double)x.y;
+            } else if (mode == 1) {
+                if (r & m) s0 += (double)x.x;
+            } else {
+                s0 += (r & m) ? -(double)x.x : (double)x.x;
+            }
+        } else if (!(r & m)) {
+            const C x = v[(r << n) | (r | m)];
+            s0 += mode == 3 ? 2.0 * (double)x.x : -2.0 * (double)x.y;
+        }
+    }
+    s0 = block_sum(s0, red);
+    __syncthreads();
+    s1 = block_sum(s1, red);
+    if (threadIdx.x == 0) {
+        partials[2 * blockIdx.x] = s0;
+        partials[2 * blockIdx.x + 1] = s1;
+    }
+}
+
+// Re rho[r][r] for every row (DensityMatrix probabilities).
+template <typename C>
+__global__ void k_dm_diag_out(const C *__restrict__ v, uint32_t n, double *out) {
+    const uint64_t D = 1ULL << n;
+    for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < D; r += (uint64_t)gridDim.x * blockDim.x)
+        out[r] = (double)v[(r << n) | r].x;
+}
+
+// DensityMatrix::measure collapse (src/lib.rs:1937-1946): entries whose row or
+// column bit differs from the outcome become 0, the rest are divided by P.
+template <typename C>
+__global__ void k_dm_collapse(C *__restrict__ v, uint32_t n, uint32_t q, int outcome, double prob) {
+    using R = typename Real<C>::T;
+    const uint64_t total = 1ULL << (2 * n);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+        const int rb = (int)((i >> (n + q)) & 1ULL), cb = (int)((i >> q) & 1ULL);
+        if (rb != outcome || cb != outcome) {
+            v[i] = mk((R)0, (R)0);
+        } else {
+            const C x = v[i];
+            v[i] = mk((R)((double)x.x / prob), (R)((double)x.y / prob));
+        }
+    }
+}
+
+// DensityMatrix::from_state (src/lib.rs:1641-1655): rho[r][c] = a_r conj(a_c).
+template <typename C>
+__global__ void k_dm_outer(const C *__restrict__ a, uint32_t n, C *__restrict__ v) {
+    using R = typename Real<C>::T;
+    const uint64_t total = 1ULL << (2 * n), cmask = (1ULL << n) - 1;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+        const C x = a[i >> n], y = a[i & cmask];
+        v[i] = mk((R)((double)x.x * (double)y.x + (double)x.y * (double)y.y),
+                  (R)((double)x.y * (double)y.x - (double)x.x * (double)y.y));
+    }
+}
+
+// I / 2^n (DensityMatrix::maximally_mixed, src/lib.rs:1668-1700).
+template <typename C>
+__global__ void k_dm_mixed(C *__restrict__ v, uint32_t n) {
+    using R = typename Real<C>::T;
+    const uint64_t total = 1ULL << (2 * n), cmask = (1ULL << n) - 1;
+    const double d = 1.0 / (double)(1ULL << n);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x)
+        v[i] = mk((R)((i >> n) == (i & cmask) ? d : 0.0), (R)0);
+}
+
+int grid_for(const qf_ctx *ctx, uint64_t work) {
+    return (int)std::max<uint64_t>(1, std::min<uint64_t>((work + 255) / 256, (uint64_t)ctx->sm_count * 8));
+}
+
+}  // namespace
+
+int dm_channel(qf_sv *sv, uint32_t n, uint32_t q, const double coef[6]) {
+    qf_ctx *ctx = sv->ctx;
+    const uint64_t groups = 1ULL << (2 * n - 2);
+    const int grid = grid_for(ctx, groups);
+    if (sv->dtype == QF_C64)
+        k_dm_channel<float2><<<grid, 256, 0, ctx->stream>>>(static_cast<float2 *>(sv->d), n, q, groups, coef[0], coef[1],
+                                                            coef[2], coef[3], coef[4], coef[5]);
+    else
+        k_dm_channel<double2><<<grid, 256, 0, ctx->stream>>>(static_cast<double2 *>(sv->d), n, q, groups, coef[0], coef[1],
+                                                             coef[2], coef[3], coef[4], coef[5]);
+    QF_CUDA(cudaGetLastError());
+    return QF_OK;
+}
+
+int dm_diag_reduce(qf_sv *sv, uint32_t n, uint32_t q, int mode, double out[2]) {
+    qf_ctx *ctx = sv->ctx;
+    const uint64_t D = 1ULL << n;
+    const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((D + 255) / 256, (uint64_t)ctx->sm_count * 2));
+    const size_t bytes = sizeof(double) * 2 * grid;
+    QF_TRY(ensure_device(&ctx->ws_red, &ctx->ws_red_bytes, bytes));
+    double *d_part = static_cast<double *>(ctx->ws_red);
+    if (sv->dtype == QF_C64)
+        k_dm_diag<float2><<<grid, 256, 0, ctx->stream>>>(static_cast<const float2 *>(sv->d), n, q, mode, d_part);
+    else
+        k_dm_diag<double2><<<grid, 256, 0, ctx->stream>>>(static_cast<const double2 *>(sv->d), n, q, mode, d_part);
+    QF_CUDA(cudaGetLastError());
+    std::vector<double> part(2 * (size_t)grid);
+    QF_CUDA(cudaMemcpyAsync(part.data(), d_part, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    QF_CUDA(cudaStreamSynchronize(ctx->stream));
+    out[0] = out[1] = 0.0;
+    for (int b = 0; b < grid; ++b) {
+        out[0] += part[2 * (size_t)b];
+        out[1] += part[2 * (size_t)b + 1];
+    }
+    return QF_OK;
+}
+
+int dm_diagonal(qf_sv *sv, uint32_t n, double *d_out) {
+    qf_ctx *ctx = sv->ctx;
+    const int grid = grid_for(ctx, 1ULL << n);
+    if (sv->dtype == QF_C64) k_dm_diag_out<float2><<<grid, 256, 0, ctx->stream>>>(static_cast<const float2 *>(sv->d), n, d_out);
+    else k_dm_diag_out<double2><<<grid, 256, 0, ctx->stream>>>(static_cast<const double2 *>(sv->d), n, d_out);
+    QF_CUDA(cudaGetLastError());
+    return QF_OK;
+}
+
+int dm_collapse(qf_sv *sv, uint32_t n, uint32_t q, int outcome, double prob) {
+    qf_ctx *ctx = sv->ctx;
+    const int grid = grid_for(ctx, sv->dim);
+    if (sv->dtype == QF_C64) k_dm_collapse<float2><<<grid, 256, 0, ctx->stream>>>(static_cast<float2 *>(sv->d), n, q, outcome, prob);
+    else k_dm_collapse<double2><<<grid, 256, 0, ctx->stream>>>(static_cast<double2 *>(sv->d), n, q, outcome, prob);
+    QF_CUDA(cudaGetLastError());
+    return QF_OK;
+}
+
+int dm_from_state(qf_sv *dm, uint32_t n, const qf_sv *psi) {
+    qf_ctx *ctx = dm->ctx;
+    const int grid = grid_for(ctx, dm->dim);
+    if (dm->dtype == QF_C64)
+        k_dm_outer<float2><<<grid, 256, 0, ctx->stream>>>(static_cast<const float2 *>(psi->d), n, static_cast<float2 *>(dm->d));
+    else
+        k_dm_outer<double2><<<grid, 256, 0, ctx->stream>>>(static_cast<const double2 *>(psi->d), n, static_cast<double2 *>(dm->d));
+    QF_CUDA(cudaGetLastError());
+    return QF_OK;
+}
+
+int dm_maximally_mixed(qf_sv *dm, uint32_t n) {
+    qf_ctx *ctx = dm->ctx;
+    const int grid = grid_for(ctx, dm->dim);
+    if (dm->dtype == QF_C64) k_dm_mixed<float2><<<grid, 256, 0, ctx->stream>>>(static_cast<float2 *>(dm->d), n);
+    else k_dm_mixed<double2><<<grid, 256, 0, ctx->stream>>>(static_cast<double2 *>(dm->d), n);
+    QF_CUDA(cudaGetLastError());
+    return QF_OK;
+}
+
+}  // namespace qf

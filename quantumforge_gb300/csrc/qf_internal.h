@@ -48,6 +48,13 @@ struct qf_batch {
     uint64_t size = 0;
 };
 
+// A density matrix of n qubits: row-major rho[row * 2^n + col] held as one
+// 2n-qubit vector (column qubit q = bit q, row qubit q = bit n + q).
+struct qf_dm {
+    qf_sv *sv = nullptr;
+    uint32_t n = 0;
+};
+
 namespace qf {
 
 // ---- errors -----------------------------------------------------------------
@@ -293,6 +300,16 @@ int batch_set_zero(qf_sv *sv, uint32_t n, uint64_t B);
 // Measure qubit q of every state with uniforms[b]; outcomes to host; on an
 // invalid probability nothing is collapsed.
 int batch_measure(qf_sv *sv, uint32_t n, uint64_t B, uint32_t q, const double *uniforms, uint8_t *outcomes);
+// Density matrices (density.cu). coef = (a, b, c, d, e, f) of
+// v00' = a v00 + b v11, v11' = c v00 + d v11, v01' = e v01, v10' = f v10 on
+// the bit pair (row n + q, column q).
+int dm_channel(qf_sv *sv, uint32_t n, uint32_t q, const double coef[6]);
+// mode 0 trace (out[0] re, out[1] im), 1 P(1) of q, 2 <Z_q>, 3 <X_q>, 4 <Y_q>.
+int dm_diag_reduce(qf_sv *sv, uint32_t n, uint32_t q, int mode, double out[2]);
+int dm_diagonal(qf_sv *sv, uint32_t n, double *d_out);
+int dm_collapse(qf_sv *sv, uint32_t n, uint32_t q, int outcome, double prob);
+int dm_from_state(qf_sv *dm, uint32_t n, const qf_sv *psi);
+int dm_maximally_mixed(qf_sv *dm, uint32_t n);
 // Sampler.
 // start_states: optional per-shot generator states (host, `shots` entries)
 // replacing the shot-major jump from `seed`.

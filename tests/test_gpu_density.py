@@ -1,0 +1,150 @@
+"""GPU density matrices (qf_dm_*) against the oracle's restatement of
+DensityMatrix (src/lib.rs:1551-2235): the reference's own CUDA density tests
+(tests/quantum_core.rs:622-647, 702-731) at their 1e-12 tolerance, the
+thermal-channel known answers (tests/noise_thermo.rs:44-124) and random noisy
+circuits. complex128 entries within 1e-11 after tens of fused gates;
+complex64 within 2e-6."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle as O
+from quantumforge_gb300 import Circuit, DensityMatrix, Gate, NoiseChannel, QuantumError, SmallRng, StateVector
+from quantumforge_gb300 import _abi as A
+from quantumforge_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def close(a, b, tol):
+    return np.abs(np.asarray(a) - np.asarray(b)).max() <= tol
+
+
+def test_cuda_density_circuit_matches_cpu_gates_and_noise_channels(backend):  # tests/quantum_core.rs:702-731
+    c = Circuit()
+    for gate, q in ((Gate.H, 0), (Gate.Rx(0.37), 1), (Gate.Ry(-0.81), 2), (Gate.Y, 1), (Gate.Z, 2), (Gate.Rz(-0.44), 0)):
+        c.push(gate, q)
+    c.cnot(0, 2)
+    c.cz(1, 2)
+    c.swap(0, 1)
+    c.channel(0, NoiseChannel.AmplitudeDamping(0.17))
+    c.channel(1, NoiseChannel.PhaseDamping(0.29))
+    c.channel(2, NoiseChannel.Depolarizing(0.13))
+    initial = O.dm_from_state(O.zero(3))
+    expected = O.run_density(c.ops(), 3, initial)
+    actual = backend.run_density_circuit(initial, c)
+    assert close(actual, expected, 1e-12)
+    assert abs(np.trace(actual).real - 1.0) < 1e-12
+    rho = backend.upload_density(initial)
+    c.run_density(rho)
+    assert close(rho.entries(), expected, 1e-12)
+    assert abs(rho.trace().real - 1.0) < 1e-12
+    assert abs(rho.purity() - O.dm_purity(expected)) < 1e-12
+
+
+def test_cuda_resident_density_measurement_matches_cpu_collapse(backend):  # tests/quantum_core.rs:622-647
+    psi = O.cnot(O.apply(O.apply(O.zero(3), A.GATE_H, 0.0, 0), A.GATE_RY, 0.71, 1), 1, 2)
+    initial = O.dm_from_state(psi)
+    cpu = initial.copy()
+    expected = O.dm_measure(cpu, 1, O.Rng(8831))
+    dev = backend.upload_density(initial)
+    rng = SmallRng.seeded(8831)
+    assert dev.measure(1, rng) == expected
+    got = dev.entries()
+    assert close(got, cpu, 1e-12)
+    assert abs(np.trace(got).real - 1.0) < 1e-12
+    r2 = O.Rng(8831)
+    r2.next_f64()
+    assert rng.state == r2.state.value
+
+
+def test_thermal_damping_prepares_the_gibbs_state_on_the_device(backend):  # tests/noise_thermo.rs:44-79
+    gd, beta = 0.10, 1.0
+    gu = gd * math.exp(-beta)
+    target = math.exp(-beta) / (1.0 + math.exp(-beta))
+    rate = 1.0 - gu - gd
+    sv = StateVector.zero(1, backend=backend)
+    sv.apply(Gate.X, 0)
+    rho = DensityMatrix.from_state(sv)
+    ch = NoiseChannel.ThermalDamping(gd, beta)
+    for step in range(21):
+        assert abs(rho.probability_one(0) - (target + (1.0 - target) * rate ** step)) < 1e-12
+        assert abs(rho.trace().real - 1.0) < 1e-12
+        assert rho.purity() <= 1.0 + 1e-12
+        rho.apply_channel(ch, 0)
+    hot = DensityMatrix.from_state(sv)
+    for _ in range(50):
+        hot.apply_channel(NoiseChannel.ThermalDamping(0.3, 0.0), 0)
+    assert abs(hot.probability_one(0) - 0.5) < 1e-12
+
+
+def _noisy_density_circuit(n, seed):
+    r = np.random.default_rng(seed)
+    c = Circuit.from_ops(W.random_circuit(n, 2, seed, two_qubit="mixed"))
+    kinds = [NoiseChannel.Depolarizing, NoiseChannel.AmplitudeDamping, NoiseChannel.PhaseDamping,
+             lambda g: NoiseChannel.ThermalDamping(g, float(r.uniform(0.0, 2.0)))]
+    for k in range(3):
+        for q in range(n):
+            if r.uniform() < 0.6:
+                c.channel(q, kinds[int(r.integers(0, 4))](float(r.uniform(0.02, 0.4))))
+        for op in W.random_circuit(n, 1, seed + 11 * k, two_qubit="mixed"):
+            c.operations.append((int(op["kind"]), int(op["gate"]), int(op["q0"]), int(op["q1"]), 0, float(op["theta"]), 0))
+    return c
+
+
+@pytest.mark.parametrize("n,seed,dtype,tol", [(2, 1, "c128", 1e-12), (5, 2, "c128", 1e-11), (8, 3, "c128", 1e-11),
+                                              (10, 4, "c128", 1e-11), (6, 5, "c64", 2e-6), (9, 6, "c64", 2e-6)])
+@pytest.mark.parametrize("start", ["pure", "mixed"])
+def test_random_noisy_density_circuits_match_the_oracle(backend, n, seed, dtype, tol, start):
+    c = _noisy_density_circuit(n, seed)
+    if start == "pure":
+        psi = O.run(W.random_circuit(n, 2, seed + 100), n)
+        init = O.dm_from_state(psi)
+        sv = StateVector.from_amplitudes(psi, dtype=dtype, backend=backend)
+        rho = DensityMatrix.from_state(sv)
+    else:
+        init = O.dm_maximally_mixed(n)
+        rho = DensityMatrix.maximally_mixed(n, dtype=dtype, backend=backend)
+    want = O.run_density(c.ops(), n, init)
+    c.run_density(rho)
+    assert close(rho.entries(), want, tol)
+    assert abs(rho.trace() - O.dm_trace(want)) < tol * 4
+    assert abs(rho.purity() - O.dm_purity(want)) < tol * 4
+    assert close(rho.probabilities(), np.real(np.diag(want)), tol)
+    for q in (0, n - 1):
+        for obs in (A.PAULI_X, A.PAULI_Y, A.PAULI_Z):
+            assert abs(rho.expectation(obs, q) - O.dm_expectation(want, obs, q)) < tol * 4
+        assert abs(rho.probability_one(q) - O.dm_probability_one(want, q)) < tol * 4
+    r_gpu, r_cpu = SmallRng.seeded(77), O.Rng(77)
+    q = n // 2
+    o = rho.measure(q, r_gpu)
+    assert o == O.dm_measure(want, q, r_cpu)
+    assert close(rho.entries(), want, tol * 4)
+
+
+def test_density_errors(backend):
+    rho = DensityMatrix.zero(3, backend=backend)
+    m = Circuit()
+    m.push(Gate.H, 0)
+    m.measure(0, 0)
+    with pytest.raises(QuantumError) as e:
+        m.run_density(rho)
+    assert e.value.kind == "OperationRequiresShotExecution"
+    assert close(rho.entries(), O.dm_from_state(O.zero(3)), 0.0)  # rejected before anything ran
+    for ch in (NoiseChannel.Depolarizing(1.5), NoiseChannel.ThermalDamping(0.1, -1.0)):
+        with pytest.raises(QuantumError) as e:
+            rho.apply_channel(ch, 0)
+        assert e.value.kind == "InvalidProbability"
+    with pytest.raises(QuantumError) as e:
+        rho.apply_channel(NoiseChannel.AmplitudeDamping(0.1), 3)
+    assert e.value.kind == "QubitOutOfRange"
+    with pytest.raises(QuantumError) as e:
+        rho.measure(5, SmallRng.seeded(1))
+    assert e.value.kind == "QubitOutOfRange"
+    with pytest.raises(QuantumError) as e:
+        DensityMatrix.zero(18, backend=backend)
+    assert e.value.kind == "StateTooLarge"
+    with pytest.raises(QuantumError) as e:
+        DensityMatrix.from_state(StateVector.zero(4, backend=backend)).apply_cnot(0, 0)
+    assert e.value.kind == "InvalidQubitPair"
