@@ -51,7 +51,7 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true")
-    ap.add_argument("--extras", default="vqe24,qaoa4096,shots20,shots_ff,vqe32",
+    ap.add_argument("--extras", default="vqe24,qaoa4096,shots20,shots_ff,noise_shots,density14,vqe32",
                     help="comma-separated extra workloads to run after the headline")
     ap.add_argument("--vqe-qubits", type=int, default=32, help="qubits of the checkpointed-adjoint extra (vqe32)")
     ap.add_argument("--qaoa-instances", type=int, default=4096, help="instances of the batched QAOA extra (qaoa4096)")
@@ -337,6 +337,10 @@ def run_ours(args):
             extra["shots20"] = shots20(backend, cpu=not args.no_cpu_baseline)
         if "shots_ff" in wanted:
             extra["shots_ff"] = shots_feedforward(backend, cpu=not args.no_cpu_baseline)
+        if "density14" in wanted:
+            extra["density14"] = density14(backend, cpu=not args.no_cpu_baseline)
+        if "noise_shots" in wanted:
+            extra["noise_shots"] = noise_shots(backend, cpu=not args.no_cpu_baseline)
         if "vqe32" in wanted:
             extra["vqe32"] = vqe32_checkpointed(backend, args.vqe_qubits)
     if rank == 0 and not args.no_cpu_baseline:
@@ -462,6 +466,133 @@ def shots_feedforward(backend, cpu: bool):
     if cpu:
         out["cpu_literal_shots_per_s"] = k / tl
         out["cpu_sample"] = f"{k} shots of the literal per-shot re-simulation (oracle restating run_shots_impl, one thread)"
+    return out
+
+
+def noisy_layers(n, layers, seed, gamma, dep):
+    """`layers` of random H/RX/RY/RZ + CNOT ladders, each followed by
+    amplitude damping (gamma) on every qubit and depolarizing (dep) on every
+    other qubit."""
+    import quantumforge_gb300 as qf
+    from quantumforge_gb300 import workloads as W
+
+    c = qf.Circuit()
+    for layer in range(layers):
+        for r in W.random_circuit(n, 1, seed + layer):
+            c.operations.append((int(r["kind"]), int(r["gate"]), int(r["q0"]), int(r["q1"]), 0, float(r["theta"]), 0))
+        for q in range(n):
+            c.channel(q, qf.NoiseChannel.AmplitudeDamping(gamma))
+        for q in range(0, n, 2):
+            c.channel(q, qf.NoiseChannel.Depolarizing(dep))
+    return c
+
+
+def density14(backend, cpu: bool, n: int = 14):
+    """A 14-qubit density matrix (4^14 complex128 entries, 4 GiB) through 6
+    noisy layers (`noisy_layers`): Circuit.run_density on the resident matrix,
+    timed with CUDA events on the engine's stream; the channel kernel timed
+    alone; the same workload at 8 qubits against the oracle."""
+    import ctypes as C
+
+    import torch
+
+    import oracle as O
+    import quantumforge_gb300 as qf
+    from quantumforge_gb300 import _abi as A
+    from quantumforge_gb300 import _native
+
+    c = noisy_layers(n, 6, 5, 0.02, 0.01)
+    ops = c.ops()
+    n_ch = int((ops["kind"] == A.OP_CHANNEL).sum())
+    sp = C.c_void_p()
+    _native.load().qf_ctx_stream(backend.handle, C.byref(sp))
+    stream = torch.cuda.ExternalStream(sp.value)
+    rho = qf.DensityMatrix.zero(n, backend=backend)
+    c.run_density(rho)  # warm
+    reps = 3
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        c.run_density(rho)
+    e1.record(stream)
+    e1.synchronize()
+    t = e0.elapsed_time(e1) / 1000.0 / reps
+    chan = qf.Circuit()
+    for q in range(n):
+        chan.channel(q, qf.NoiseChannel.AmplitudeDamping(0.02))
+    chan.run_density(rho)
+    e0.record(stream)
+    chan.run_density(rho)
+    e1.record(stream)
+    e1.synchronize()
+    t_ch = e0.elapsed_time(e1) / 1000.0 / n
+    bytes_ch = 2 * (4 ** n) * 16
+    peak, peak_kind = hbm_peak()
+    tr = rho.trace()
+    out = {"qubits": n, "entries": 4 ** n, "dtype": "complex128", "ops": len(ops), "gates": len(ops) - n_ch,
+           "channels": n_ch, "run_density_s": t, "ops_per_s": len(ops) / t,
+           "channel_kernel": {"kernel": "k_dm_channel<double2>", "avg_launch_ms": 1000 * t_ch,
+                              "bytes_per_launch": bytes_ch, "achieved_gbs": bytes_ch / t_ch / 1e9,
+                              "frac": bytes_ch / t_ch / 1e9 / peak, "peak": peak, "peak_kind": f"of {peak_kind}"},
+           "trace_re": tr.real, "purity": rho.purity()}
+    m = 8
+    cs = noisy_layers(m, 6, 5, 0.02, 0.01)
+    small = qf.DensityMatrix.zero(m, backend=backend)
+    cs.run_density(small)
+    want = O.run_density(cs.ops(), m)
+    out["max_abs_err_vs_oracle_8q"] = float(np.abs(small.entries() - want).max())
+    if cpu:
+        k = 9
+        ck = noisy_layers(k, 6, 5, 0.02, 0.01)
+        t0 = time.perf_counter()
+        O.run_density(ck.ops(), k)
+        tk = time.perf_counter() - t0
+        scale = 4 ** (n - k)
+        out["cpu_ops_per_s_extrapolated"] = len(ck.ops()) / (tk * scale)
+        out["cpu_sample"] = (f"the same layers at {k} qubits through the oracle's DensityMatrix restatement (one thread), "
+                             f"time scaled by 4^{n - k} entries (extrapolated)")
+    return out
+
+
+def noise_shots(backend, cpu: bool, n: int = 12, shots: int = 100_000):
+    """run_shots_with_noise: 12 qubits complex128, 4 noisy layers
+    (`noisy_layers`, gamma 0.01, depolarizing 0.005) then measure(q, q) for
+    every qubit, 10^5 shots through the engine's default (per-shot
+    shared-memory trajectories) and 10^4 through the branch tree; the first
+    shots against the oracle's literal per-shot trajectories."""
+    import oracle as O
+
+    c = noisy_layers(n, 4, 9, 0.01, 0.005)
+    for q in range(n):
+        c.measure(q, q)
+    seed = 42
+    c.run_shots_packed(n, 64, seed, backend=backend, tie_eps=1e-12, noise=True)  # warm
+    t0 = time.perf_counter()
+    got, width, ties = c.run_shots_packed(n, shots, seed, backend=backend, tie_eps=1e-12, noise=True)
+    dt = time.perf_counter() - t0
+    out = {"qubits": n, "ops": len(c.operations), "shots": shots, "engine": "per-shot trajectories (k_trajectories)",
+           "engine_call_s": dt, "engine_shots_per_s": shots / dt, "ties": int(ties),
+           "distinct_outcomes": int(len(np.unique(got)))}
+    t_shots = 10_000
+    t0 = time.perf_counter()
+    tree, _, _ = c.run_shots_packed(n, t_shots, seed, backend=backend, tie_eps=1e-12, noise=True,
+                                    exec_opts={"shots_engine": "tree"})
+    out["tree_engine_shots_per_s"] = t_shots / (time.perf_counter() - t0)
+    out["tree_equals_trajectories"] = bool(np.array_equal(tree, got[:t_shots]))
+    t0 = time.perf_counter()
+    g64, _, ties64 = c.run_shots_packed(n, shots, seed, dtype="c64", backend=backend, tie_eps=2e-5, noise=True)
+    d64 = time.perf_counter() - t0
+    out["c64_engine_shots_per_s"] = shots / d64
+    out["c64_ties"] = int(ties64)
+    out["c64_shots_differing_from_c128"] = int((g64 != got).sum())
+    k = 200
+    t0 = time.perf_counter()
+    want, _ = O.run_shots(c.ops(), n, k, seed, noise=True)
+    tl = time.perf_counter() - t0
+    out["first_shots_equal_oracle"] = bool(np.array_equal(got[:k], want))
+    if cpu:
+        out["cpu_literal_shots_per_s"] = k / tl
+        out["cpu_sample"] = f"{k} shots of the oracle's literal noisy trajectories (run_shots_impl, one thread)"
     return out
 
 

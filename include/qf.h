@@ -162,6 +162,8 @@ enum qf_exec_mode {
 #define QF_EXEC_FLAG_SMEM_TILES 1  /* complex64: use the shared-memory tile kernel instead of register tiles */
 #define QF_EXEC_FLAG_JIT 2         /* complex64: compile the plan's passes (NVRTC) even for small states */
 #define QF_EXEC_FLAG_NO_JIT 4      /* complex64: never compile passes; interpret them */
+#define QF_EXEC_FLAG_SHOTS_TREE 8  /* shots: always walk the branch tree of device states */
+#define QF_EXEC_FLAG_SHOTS_TRAJECTORIES 16  /* shots: per-shot trajectories in shared memory whenever the state fits */
 
 typedef struct qf_exec_opts {
     int32_t mode;          /* enum qf_exec_mode */

@@ -94,11 +94,14 @@ class ExecOpts(C.Structure):
 EXEC_FLAG_SMEM_TILES = 1
 EXEC_FLAG_JIT = 2
 EXEC_FLAG_NO_JIT = 4
+EXEC_FLAG_SHOTS_TREE = 8
+EXEC_FLAG_SHOTS_TRAJECTORIES = 16
 _MODES = {"auto": EXEC_AUTO, "unfused": EXEC_UNFUSED, "fused": EXEC_FUSED}
 
 
 def exec_opts(opts) -> "ExecOpts":
-    """qf_exec_opts from a dict {mode, tile_qubits, block_qubits, smem_tiles, jit}."""
+    """qf_exec_opts from a dict {mode, tile_qubits, block_qubits, smem_tiles, jit,
+    shots_engine ("tree" | "trajectories")}."""
     if isinstance(opts, ExecOpts):
         return opts
     opts = opts or {}
@@ -107,6 +110,13 @@ def exec_opts(opts) -> "ExecOpts":
         flags |= EXEC_FLAG_JIT
     elif opts.get("jit") is False:
         flags |= EXEC_FLAG_NO_JIT
+    engine = opts.get("shots_engine")
+    if engine == "tree":
+        flags |= EXEC_FLAG_SHOTS_TREE
+    elif engine == "trajectories":
+        flags |= EXEC_FLAG_SHOTS_TRAJECTORIES
+    elif engine is not None:
+        raise ValueError("shots_engine must be 'tree' or 'trajectories'")
     return ExecOpts(_MODES[opts.get("mode", "auto")], int(opts.get("tile_qubits", 0)), int(opts.get("block_qubits", 0)),
                     flags)
 

@@ -285,6 +285,35 @@ inline bool valid_probability(double p) { return std::isfinite(p) && p >= 0.0 &&
 
 inline double clamp01(double x) { return std::min(1.0, std::max(0.0, x)); }
 
+// Every shot's generator state at its first draw: shot s starts at draw s * d
+// of SmallRng::seeded(seed) (src/lib.rs:4881-4897), d = measurements (and,
+// with noise, channels) per shot — the reference's shot-major stream.
+std::vector<uint64_t> shot_starts(const qf_op *ops, uint64_t n_ops, uint64_t shots, uint64_t seed, bool allow_noise) {
+    uint64_t draws = 0;
+    for (uint64_t k = 0; k < n_ops; ++k)
+        draws += ops[k].kind == QF_OP_MEASURE || (allow_noise && ops[k].kind == QF_OP_CHANNEL);
+    std::vector<uint64_t> st(shots);
+    uint64_t z = seed + 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    z ^= z >> 31;
+    uint64_t x = z == 0 ? 0x9E3779B97F4A7C15ULL : z;
+    if (draws <= 64) {  // step the stream
+        for (uint64_t s = 0; s < shots; ++s) {
+            st[s] = x;
+            for (uint64_t k = 0; k < draws; ++k) next_uniform(&x);
+        }
+        return st;
+    }
+    uint64_t jump[1][64];  // T^draws: one matrix application per shot
+    rng_jump_matrices(draws, jump, 1);
+    for (uint64_t s = 0; s < shots; ++s) {
+        st[s] = x;
+        x = rng_apply(jump[0], x);
+    }
+    return st;
+}
+
 // StateVector::normalize (src/lib.rs:1005-1014): divide by sqrt(norm_sqr).
 int normalize_state(qf_sv *sv) {
     double nrm;
@@ -334,22 +363,7 @@ int run_shots_branching(qf_ctx *ctx, uint32_t n, int dtype, const qf_op *ops, ui
         seen |= 1ULL << ops[T - 1].q0;
         --T;
     }
-    uint64_t draws = 0;  // uniforms per shot
-    for (uint64_t k = 0; k < n_ops; ++k)
-        draws += ops[k].kind == QF_OP_MEASURE || (allow_noise && ops[k].kind == QF_OP_CHANNEL);
-    // every shot's generator state at its first draw
-    std::vector<uint64_t> st(shots);
-    {
-        uint64_t z = seed + 0x9E3779B97F4A7C15ULL;  // SmallRng::seeded (src/lib.rs:4881-4897)
-        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
-        z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
-        z ^= z >> 31;
-        uint64_t x = z == 0 ? 0x9E3779B97F4A7C15ULL : z;
-        for (uint64_t s = 0; s < shots; ++s) {
-            st[s] = x;
-            for (uint64_t k = 0; k < draws; ++k) next_uniform(&x);
-        }
-    }
+    std::vector<uint64_t> st = shot_starts(ops, n_ops, shots, seed, allow_noise);
     // A state shared by the children of one node; the last child to start
     // takes it over, the others copy it.
     struct Shared {
@@ -653,6 +667,25 @@ int run_shots_entry(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, u
     if (branching) {
         QF_TRY(bind_device(ctx));
         if (classical_width) *classical_width = (uint32_t)width;
+        // Small states with channel trajectories (many distinct branches): one
+        // CTA per shot in shared memory; otherwise the branch tree of device states.
+        const int fl = opts ? opts->flags : 0;
+        bool noisy = false;
+        for (uint64_t k = 0; k < n_ops; ++k) noisy |= ops[k].kind == QF_OP_CHANNEL;
+        const bool traj = trajectories_fit(ctx, qubits, dtype) && !(fl & QF_EXEC_FLAG_SHOTS_TREE) &&
+                          ((fl & QF_EXEC_FLAG_SHOTS_TRAJECTORIES) || noisy);
+        if (traj) {
+            qf_sv *sv;
+            QF_TRY(scratch_state(ctx, &ctx->scratch_sv, qubits, dtype, &sv));
+            if (init_amps) {
+                QF_TRY(convert_from_f64(sv, init_amps));
+                if (allow_noise) QF_TRY(normalize_state(sv));
+            } else {
+                QF_TRY(fill_zero_state(sv));
+            }
+            const std::vector<uint64_t> st = shot_starts(ops, n_ops, shots, seed, allow_noise);
+            return run_trajectories(sv, ops, n_ops, shots, st.data(), tie_eps, allow_noise, outcomes, n_ties);
+        }
         return run_shots_branching(ctx, qubits, dtype, ops, n_ops, init_amps, shots, seed, tie_eps, allow_noise, outcomes,
                                    n_ties, opts);
     }

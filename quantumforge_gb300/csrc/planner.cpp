@@ -552,6 +552,8 @@ uint64_t rng_jump(uint64_t state, uint64_t steps) {
     return mat_apply(m, state);
 }
 
+uint64_t rng_apply(const uint64_t cols[64], uint64_t state) { return mat_apply(cols, state); }
+
 // mats[j] = T^(stride * 2^j), j < count.
 void rng_jump_matrices(uint64_t stride, uint64_t (*mats)[64], int count) {
     if (count <= 0) return;

@@ -310,6 +310,12 @@ int dm_diagonal(qf_sv *sv, uint32_t n, double *d_out);
 int dm_collapse(qf_sv *sv, uint32_t n, uint32_t q, int outcome, double prob);
 int dm_from_state(qf_sv *dm, uint32_t n, const qf_sv *psi);
 int dm_maximally_mixed(qf_sv *dm, uint32_t n);
+// Per-shot trajectories in shared memory (trajectory.cu): whether 2^n
+// amplitudes of the dtype fit one CTA, and the run itself from the initial
+// device state; starts[s] = shot s's generator state at its first draw.
+bool trajectories_fit(const qf_ctx *ctx, uint32_t n, int dtype);
+int run_trajectories(qf_sv *init, const qf_op *ops, uint64_t n_ops, uint64_t shots, const uint64_t *starts, double tie_eps,
+                     bool allow_noise, uint64_t *outcomes, uint64_t *n_ties);
 // Sampler.
 // start_states: optional per-shot generator states (host, `shots` entries)
 // replacing the shot-major jump from `seed`.
@@ -321,6 +327,8 @@ int sample_shots(qf_sv *sv, const uint32_t *qubits, const uint32_t *cbits, uint3
 // SmallRng jump-ahead (host): state advanced by `steps` calls of next_u64.
 uint64_t rng_jump(uint64_t state, uint64_t steps);
 void rng_jump_matrices(uint64_t stride, uint64_t (*mats)[64], int count);
+// A jump matrix (64 columns over GF(2)) applied to a generator state.
+uint64_t rng_apply(const uint64_t cols[64], uint64_t state);
 
 // Dispatcher for a bound gate list on a resident state.
 int execute_gates(qf_sv *sv, const std::vector<BGate> &gates, const qf_exec_opts *opts);

@@ -174,13 +174,15 @@ def test_cuda_resident_measurement_matches_the_cpu_reference(backend):  # :602-6
 
 
 def _shots_vs_oracle(backend, c, n, shots, seed, dtype="c128", tie_eps=1e-12):
-    """Per-shot outcomes of the branching engine against the oracle's literal
+    """Per-shot outcomes of both shot engines against the oracle's literal
     per-shot re-simulation (run_shots_impl); a shot may differ only where a
     decision fell within tie_eps of P(1) (counted by the engine)."""
-    got, width, ties = c.run_shots_packed(n, shots, seed, dtype=dtype, backend=backend, tie_eps=tie_eps)
     want, w2 = O.run_shots(c.ops(), n, shots, seed, literal=True)
-    assert width == w2
-    assert int((got != want).sum()) <= ties, (int((got != want).sum()), ties)
+    for engine in ("tree", "trajectories"):
+        got, width, ties = c.run_shots_packed(n, shots, seed, dtype=dtype, backend=backend, tie_eps=tie_eps,
+                                              exec_opts={"shots_engine": engine})
+        assert width == w2
+        assert int((got != want).sum()) <= ties, (engine, int((got != want).sum()), ties)
     return got, width, ties
 
 
@@ -246,15 +248,17 @@ def test_repeated_measurement_repeats_the_outcome(backend):
 
 
 # ---- noise trajectories: run_shots_with_noise (src/lib.rs:2829-2916, 1356-1506) ----
-def _noisy_vs_oracle(backend, c, n, shots, seed, dtype="c128", tie_eps=1e-12, init=None):
-    """Per-shot outcomes of the engine's noisy shots against the oracle's
-    literal per-shot trajectories; a shot may differ only where a decision
-    fell within tie_eps of a branch threshold (counted by the engine)."""
-    got, width, ties = c.run_shots_packed(n if init is None else init, shots, seed, dtype=dtype, backend=backend,
-                                          tie_eps=tie_eps, noise=True)
+def _noisy_vs_oracle(backend, c, n, shots, seed, dtype="c128", tie_eps=1e-12, init=None, engines=("tree", "trajectories")):
+    """Per-shot outcomes of both shot engines (the branch tree of device states
+    and the per-shot shared-memory trajectories) against the oracle's literal
+    per-shot trajectories; a shot may differ only where a decision fell
+    within tie_eps of a branch threshold (counted by the engine)."""
     want, w2 = O.run_shots(c.ops(), n, shots, seed, init=init, noise=True)
-    assert width == w2
-    assert int((got != want).sum()) <= ties, (int((got != want).sum()), ties)
+    for engine in engines:
+        got, width, ties = c.run_shots_packed(n if init is None else init, shots, seed, dtype=dtype, backend=backend,
+                                              tie_eps=tie_eps, noise=True, exec_opts={"shots_engine": engine})
+        assert width == w2
+        assert int((got != want).sum()) <= ties, (engine, int((got != want).sum()), ties)
     return got, width, ties
 
 
@@ -359,6 +363,12 @@ def test_invalid_channel_parameters_are_rejected(backend, channel):
     with pytest.raises(QuantumError) as e:
         c.run_shots_with_noise(2, 8, 1, backend=backend)
     assert e.value.kind == "InvalidProbability"
+
+
+@pytest.mark.parametrize("n,dtype,tie", [(13, "c128", 1e-12), (14, "c64", 2e-5)])
+def test_trajectory_engine_at_the_largest_shared_memory_state(backend, n, dtype, tie):
+    c = _noisy_circuit(n, 40 + n)
+    _noisy_vs_oracle(backend, c, n, 120, 17, dtype=dtype, tie_eps=tie, engines=("trajectories",))
 
 
 def test_noisy_shots_over_many_branches_stay_within_memory(backend):
