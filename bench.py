@@ -55,6 +55,10 @@ def parse_args():
                     help="comma-separated extra workloads to run after the headline")
     ap.add_argument("--vqe-qubits", type=int, default=32, help="qubits of the checkpointed-adjoint extra (vqe32)")
     ap.add_argument("--qaoa-instances", type=int, default=4096, help="instances of the batched QAOA extra (qaoa4096)")
+    ap.add_argument("--density-qubits", type=int, default=14, help="qubits of the density-matrix extra (density14)")
+    ap.add_argument("--noise-shots", type=int, default=100_000, help="shots of the noisy-shot extra (noise_shots)")
+    ap.add_argument("--extras-only", action="store_true",
+                    help="run only the extras (small profiling runs); prints {\"extra\": ...} instead of the headline")
     return ap.parse_args()
 
 
@@ -338,9 +342,9 @@ def run_ours(args):
         if "shots_ff" in wanted:
             extra["shots_ff"] = shots_feedforward(backend, cpu=not args.no_cpu_baseline)
         if "density14" in wanted:
-            extra["density14"] = density14(backend, cpu=not args.no_cpu_baseline)
+            extra["density14"] = density14(backend, cpu=not args.no_cpu_baseline, n=args.density_qubits)
         if "noise_shots" in wanted:
-            extra["noise_shots"] = noise_shots(backend, cpu=not args.no_cpu_baseline)
+            extra["noise_shots"] = noise_shots(backend, cpu=not args.no_cpu_baseline, shots=args.noise_shots)
         if "vqe32" in wanted:
             extra["vqe32"] = vqe32_checkpointed(backend, args.vqe_qubits)
     if rank == 0 and not args.no_cpu_baseline:
@@ -528,13 +532,30 @@ def density14(backend, cpu: bool, n: int = 14):
     t_ch = e0.elapsed_time(e1) / 1000.0 / n
     bytes_ch = 2 * (4 ** n) * 16
     peak, peak_kind = hbm_peak()
+    rho64 = qf.DensityMatrix.zero(n, dtype="c64", backend=backend)
+    c.run_density(rho64)  # warm (compiles the 2n-qubit passes); one run from |0><0|
+    d64 = None
+    if n <= 12:
+        ref = qf.DensityMatrix.zero(n, backend=backend)
+        c.run_density(ref)
+        d64 = float(np.abs(rho64.entries() - ref.entries()).max())
+        del ref
+    e0.record(stream)
+    c.run_density(rho64)
+    e1.record(stream)
+    e1.synchronize()
+    t64 = e0.elapsed_time(e1) / 1000.0
+    del rho64
     tr = rho.trace()
     out = {"qubits": n, "entries": 4 ** n, "dtype": "complex128", "ops": len(ops), "gates": len(ops) - n_ch,
            "channels": n_ch, "run_density_s": t, "ops_per_s": len(ops) / t,
            "channel_kernel": {"kernel": "k_dm_channel<double2>", "avg_launch_ms": 1000 * t_ch,
                               "bytes_per_launch": bytes_ch, "achieved_gbs": bytes_ch / t_ch / 1e9,
                               "frac": bytes_ch / t_ch / 1e9 / peak, "peak": peak, "peak_kind": f"of {peak_kind}"},
-           "trace_re": tr.real, "purity": rho.purity()}
+           "trace_re": tr.real, "purity": rho.purity(),
+           "c64_run_density_s": t64, "c64_ops_per_s": len(ops) / t64}
+    if d64 is not None:
+        out["c64_max_abs_diff_vs_c128"] = d64
     m = 8
     cs = noisy_layers(m, 6, 5, 0.02, 0.01)
     small = qf.DensityMatrix.zero(m, backend=backend)
@@ -573,7 +594,7 @@ def noise_shots(backend, cpu: bool, n: int = 12, shots: int = 100_000):
     out = {"qubits": n, "ops": len(c.operations), "shots": shots, "engine": "per-shot trajectories (k_trajectories)",
            "engine_call_s": dt, "engine_shots_per_s": shots / dt, "ties": int(ties),
            "distinct_outcomes": int(len(np.unique(got)))}
-    t_shots = 10_000
+    t_shots = min(10_000, shots)
     t0 = time.perf_counter()
     tree, _, _ = c.run_shots_packed(n, t_shots, seed, backend=backend, tie_eps=1e-12, noise=True,
                                     exec_opts={"shots_engine": "tree"})
@@ -720,10 +741,30 @@ def vqe32_checkpointed(backend, n=32):
     return out
 
 
+def extras_only(args):
+    import torch
+
+    import quantumforge_gb300 as qf
+
+    torch.cuda.set_device(0)
+    backend = qf.CudaBackend(0)
+    wanted = set(args.extras.split(","))
+    cpu = not args.no_cpu_baseline
+    extra = {}
+    if "density14" in wanted:
+        extra["density14"] = density14(backend, cpu=cpu, n=args.density_qubits)
+    if "noise_shots" in wanted:
+        extra["noise_shots"] = noise_shots(backend, cpu=cpu, shots=args.noise_shots)
+    print(json.dumps({"extra": extra}), flush=True)
+    backend.close()
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         reference_arm(args)
+    elif args.extras_only:
+        extras_only(args)
     else:
         run_ours(args)
 

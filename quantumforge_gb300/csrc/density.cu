@@ -27,18 +27,31 @@ __device__ __forceinline__ uint64_t insert0(uint64_t x, uint32_t p) {
 // One local channel on qubit q: for each (row bit r, col bit c) group
 //   v00' = a v00 + b v11,  v11' = c v00 + d v11,  v01' = e v01,  v10' = f v10
 // (every channel of NoiseChannel has this form: populations mix, coherences scale).
-template <typename C>
+// SHAPE 0: general; 1: a = 1, c = 0 (amplitude damping: 8 multiplies instead
+// of 12, which matters because complex128 channels run close to the GB300's
+// FP64 issue rate); 2: a = d = 1, b = c = 0 (phase damping: only the
+// coherences are read and written). Arithmetic in the state's precision.
+template <typename C, int SHAPE>
 __global__ void k_dm_channel(C *__restrict__ v, uint32_t n, uint32_t q, uint64_t groups, double ca, double cb, double cc,
                              double cd, double ce, double cf) {
     using R = typename Real<C>::T;
     const uint64_t cm = 1ULL << q, rm = 1ULL << (n + q);
+    const R a = (R)ca, b = (R)cb, c = (R)cc, d = (R)cd, e = (R)ce, f = (R)cf;
     for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < groups; g += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t i00 = insert0(insert0(g, q), n + q);
-        const C x00 = v[i00], x01 = v[i00 | cm], x10 = v[i00 | rm], x11 = v[i00 | rm | cm];
-        v[i00] = mk((R)(ca * (double)x00.x + cb * (double)x11.x), (R)(ca * (double)x00.y + cb * (double)x11.y));
-        v[i00 | rm | cm] = mk((R)(cc * (double)x00.x + cd * (double)x11.x), (R)(cc * (double)x00.y + cd * (double)x11.y));
-        v[i00 | cm] = mk((R)(ce * (double)x01.x), (R)(ce * (double)x01.y));
-        v[i00 | rm] = mk((R)(cf * (double)x10.x), (R)(cf * (double)x10.y));
+        const C x01 = v[i00 | cm], x10 = v[i00 | rm];
+        if (SHAPE != 2) {
+            const C x00 = v[i00], x11 = v[i00 | rm | cm];
+            if (SHAPE == 1) {
+                v[i00] = mk(x00.x + b * x11.x, x00.y + b * x11.y);
+                v[i00 | rm | cm] = mk(d * x11.x, d * x11.y);
+            } else {
+                v[i00] = mk(a * x00.x + b * x11.x, a * x00.y + b * x11.y);
+                v[i00 | rm | cm] = mk(c * x00.x + d * x11.x, c * x00.y + d * x11.y);
+            }
+        }
+        v[i00 | cm] = mk(e * x01.x, e * x01.y);
+        v[i00 | rm] = mk(f * x10.x, f * x10.y);
     }
 }
 
@@ -129,16 +142,22 @@ int grid_for(const qf_ctx *ctx, uint64_t work) {
 
 }  // namespace
 
-int dm_channel(qf_sv *sv, uint32_t n, uint32_t q, const double coef[6]) {
+template <typename C, int SHAPE> void launch_channel(qf_sv *sv, uint32_t n, uint32_t q, const double *k) {
     qf_ctx *ctx = sv->ctx;
     const uint64_t groups = 1ULL << (2 * n - 2);
-    const int grid = grid_for(ctx, groups);
-    if (sv->dtype == QF_C64)
-        k_dm_channel<float2><<<grid, 256, 0, ctx->stream>>>(static_cast<float2 *>(sv->d), n, q, groups, coef[0], coef[1],
-                                                            coef[2], coef[3], coef[4], coef[5]);
-    else
-        k_dm_channel<double2><<<grid, 256, 0, ctx->stream>>>(static_cast<double2 *>(sv->d), n, q, groups, coef[0], coef[1],
-                                                             coef[2], coef[3], coef[4], coef[5]);
+    k_dm_channel<C, SHAPE><<<grid_for(ctx, groups), 256, 0, ctx->stream>>>(static_cast<C *>(sv->d), n, q, groups, k[0], k[1],
+                                                                           k[2], k[3], k[4], k[5]);
+}
+
+template <typename C> void launch_channel_shape(qf_sv *sv, uint32_t n, uint32_t q, const double *k) {
+    if (k[0] == 1.0 && k[1] == 0.0 && k[2] == 0.0 && k[3] == 1.0) launch_channel<C, 2>(sv, n, q, k);
+    else if (k[0] == 1.0 && k[2] == 0.0) launch_channel<C, 1>(sv, n, q, k);
+    else launch_channel<C, 0>(sv, n, q, k);
+}
+
+int dm_channel(qf_sv *sv, uint32_t n, uint32_t q, const double coef[6]) {
+    if (sv->dtype == QF_C64) launch_channel_shape<float2>(sv, n, q, coef);
+    else launch_channel_shape<double2>(sv, n, q, coef);
     QF_CUDA(cudaGetLastError());
     return QF_OK;
 }
