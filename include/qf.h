@@ -417,6 +417,26 @@ int qf_run_density_circuit(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op 
                            const qf_exec_opts *opts);
 
 /* ---------------------------------------------------------------------------
+ * Circuit formats — OpenQASM 2.0 import (qasm::parse_qasm, src/qasm.rs:73),
+ * QASM export (qasm_export::export_qasm / export_qasm_with_qubits,
+ * src/qasm_export.rs), and the JSON form (Circuit::to_json / from_json,
+ * src/serialize.rs:91-170). Ops come back as the qf_op records of the
+ * circuit; pass ops_out = NULL to learn the count (*n_ops), text out = NULL
+ * to learn the length (*len, without the terminating NUL). Parse errors are
+ * QF_ERR_INVALID_ARGUMENT with the reference's message in qf_last_error
+ * ("QASM error at line N: ..."; *error_line = N).
+ * ------------------------------------------------------------------------- */
+int qf_parse_qasm(const char *source, uint64_t len, qf_op *ops_out, uint64_t capacity, uint64_t *n_ops,
+                  uint32_t *qubits, uint32_t *classical_bits, uint64_t *error_line);
+int qf_circuit_from_json(const char *json, uint64_t len, qf_op *ops_out, uint64_t capacity, uint64_t *n_ops,
+                         uint32_t *qubits, uint32_t *classical_bits);
+int qf_circuit_to_json(const qf_op *ops, uint64_t n_ops, char *out, uint64_t capacity, uint64_t *len);
+/* `qubits` < 0: the register spans the highest qubit used (export_qasm);
+ * otherwise the declared register size (export_qasm_with_qubits, an error
+ * when an op uses a qubit outside it). */
+int qf_circuit_to_qasm(const qf_op *ops, uint64_t n_ops, int64_t qubits, char *out, uint64_t capacity, uint64_t *len);
+
+/* ---------------------------------------------------------------------------
  * Gradients — ParameterizedCircuit::gradient_with_inputs
  * (src/gradients.rs:232-330), adjoint_gradient_with_inputs
  * (src/lib.rs:3564-3704), parameter_shift_gradient_with_inputs

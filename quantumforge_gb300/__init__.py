@@ -23,11 +23,15 @@ from .core import (
     StateVector,
     StateVectorBatch,
     default_backend,
+    export_qasm,
+    export_qasm_with_qubits,
+    parse_qasm,
 )
 from . import gradients
 
 __all__ = [
     "Circuit", "CudaBackend", "DensityMatrix", "Gate", "NoiseChannel", "ParameterizedCircuit", "PauliSum", "QuantumError", "RotationAxis",
-    "ShotResult", "SingleQubitObservable", "SmallRng", "StateVector", "StateVectorBatch", "default_backend", "gradients",
+    "ShotResult", "SingleQubitObservable", "SmallRng", "StateVector", "StateVectorBatch", "default_backend", "export_qasm",
+    "export_qasm_with_qubits", "parse_qasm", "gradients",
     "load_library",
 ]

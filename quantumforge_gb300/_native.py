@@ -92,6 +92,10 @@ SIGNATURES = {
     "qf_dm_probabilities": [P, P, U64],
     "qf_dm_measure": [P, U32, PU64, P],
     "qf_run_density_circuit": [P, U32, C.c_int, P, U64, P, P, U64, P],
+    "qf_parse_qasm": [C.c_char_p, U64, P, U64, PU64, PU32, PU32, PU64],
+    "qf_circuit_from_json": [C.c_char_p, U64, P, U64, PU64, PU32, PU32],
+    "qf_circuit_to_json": [P, U64, P, U64, PU64],
+    "qf_circuit_to_qasm": [P, U64, C.c_int64, P, U64, PU64],
     "qf_sv_sample": [P, P, P, U32, U64, U64, F64, P, PU64],
     "qf_gradient": [P, U32, P, U64, P, U64, P, U64, P, U64, P, P, P, P],
     "qf_expectation": [P, U32, C.c_int, P, U64, P, U64, P, U64, P, U64, P, PF64],

@@ -772,6 +772,49 @@ class Circuit:
     def if_classical_bit(self, classical_bit: int, value: int, gate: Gate, target: int) -> None:
         self.operations.append((_abi.OP_COND, gate.code, int(target), 0, int(classical_bit), gate.theta, int(value) & 1))
 
+    # ---- formats (src/serialize.rs, src/qasm.rs, src/qasm_export.rs) ----
+    @classmethod
+    def from_qasm(cls, source: str) -> "Circuit":
+        """qasm::parse_qasm (src/qasm.rs:73): OpenQASM 2.0 text to a circuit."""
+        return cls.from_ops(parse_qasm_ops(source)[0])
+
+    @classmethod
+    def from_json(cls, text: str) -> "Circuit":
+        """Circuit::from_json (src/serialize.rs:150-154)."""
+        return cls.from_json_bytes(text.encode())
+
+    @classmethod
+    def from_json_bytes(cls, data: bytes) -> "Circuit":
+        lib = load()
+        n = C.c_uint64()
+        check(lib.qf_circuit_from_json(data, len(data), None, 0, C.byref(n), None, None))
+        ops = np.zeros(n.value, dtype=_abi.OP_DTYPE)
+        check(lib.qf_circuit_from_json(data, len(data), ptr(ops), n.value, C.byref(n), None, None))
+        return cls.from_ops(ops)
+
+    def to_json(self) -> str:
+        """Circuit::to_json (src/serialize.rs:91-95): serde_json's pretty form."""
+        return self._text(lambda lib, ops, out, cap, ln: lib.qf_circuit_to_json(ptr(ops), len(ops), out, cap, ln))
+
+    def to_json_bytes(self) -> bytes:
+        """Circuit::to_json_bytes (src/serialize.rs:97-101): the same document."""
+        return self.to_json().encode()
+
+    def to_qasm(self, num_qubits: int | None = None) -> str:
+        """qasm_export::export_qasm, or export_qasm_with_qubits when
+        `num_qubits` is given."""
+        nq = -1 if num_qubits is None else int(num_qubits)
+        return self._text(lambda lib, ops, out, cap, ln: lib.qf_circuit_to_qasm(ptr(ops), len(ops), nq, out, cap, ln))
+
+    def _text(self, call) -> str:
+        lib = load()
+        ops = self.ops()
+        n = C.c_uint64()
+        check(call(lib, ops, None, 0, C.byref(n)))
+        buf = C.create_string_buffer(n.value + 1)
+        check(call(lib, ops, C.cast(buf, C.c_void_p), n.value + 1, C.byref(n)))
+        return buf.value.decode()
+
     def has_measurements(self) -> bool:
         return any(op[0] == _abi.OP_MEASURE for op in self.operations)
 
@@ -829,6 +872,32 @@ class Circuit:
         check(fn(backend.handle, n, _dtype_code(dtype), ptr(ops), len(ops), ptr(src), int(shots), int(seed), float(tie_eps),
                  ptr(out), C.byref(width), C.byref(ties), _exec(exec_opts)))
         return out[: int(shots)], width.value, ties.value
+
+
+def parse_qasm_ops(source: str):
+    """qf_parse_qasm: (op records, qubits declared, classical bits declared)."""
+    data = source.encode()
+    lib = load()
+    n, nq, nc, line = C.c_uint64(), C.c_uint32(), C.c_uint32(), C.c_uint64()
+    check(lib.qf_parse_qasm(data, len(data), None, 0, C.byref(n), C.byref(nq), C.byref(nc), C.byref(line)))
+    ops = np.zeros(n.value, dtype=_abi.OP_DTYPE)
+    check(lib.qf_parse_qasm(data, len(data), ptr(ops), n.value, C.byref(n), C.byref(nq), C.byref(nc), C.byref(line)))
+    return ops, nq.value, nc.value
+
+
+def parse_qasm(source: str) -> "Circuit":
+    """qasm::parse_qasm (src/qasm.rs:73)."""
+    return Circuit.from_qasm(source)
+
+
+def export_qasm(circuit: "Circuit") -> str:
+    """qasm_export::export_qasm."""
+    return circuit.to_qasm()
+
+
+def export_qasm_with_qubits(circuit: "Circuit", num_qubits: int) -> str:
+    """qasm_export::export_qasm_with_qubits."""
+    return circuit.to_qasm(num_qubits)
 
 
 class ParameterizedCircuit:
