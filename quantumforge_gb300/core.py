@@ -264,6 +264,24 @@ class CudaBackend:
                                     _exec(exec_opts)))
         return out.view(np.complex128)
 
+    # CudaBackend::apply_ry / apply_rotation / apply_ry_chain /
+    # apply_rotation_chain (src/cuda.rs:794-840): host state in, rotations
+    # applied on the device in one fused sweep, host state out.
+    def apply_rotation_chain(self, state, gates, dtype="c128") -> np.ndarray:
+        sv = StateVector.from_amplitudes(state.amplitudes() if isinstance(state, StateVector) else state, dtype=dtype,
+                                         backend=self)
+        sv.apply_rotation_chain(gates)
+        return sv.amplitudes()
+
+    def apply_rotation(self, state, axis: int, qubit: int, theta: float, dtype="c128") -> np.ndarray:
+        return self.apply_rotation_chain(state, [(axis, qubit, theta)], dtype=dtype)
+
+    def apply_ry_chain(self, state, gates, dtype="c128") -> np.ndarray:
+        return self.apply_rotation_chain(state, [(RotationAxis.Y, q, t) for q, t in gates], dtype=dtype)
+
+    def apply_ry(self, state, qubit: int, theta: float, dtype="c128") -> np.ndarray:
+        return self.apply_rotation(state, RotationAxis.Y, qubit, theta, dtype=dtype)
+
     def upload_batch(self, states, dtype="c128") -> "StateVectorBatch":
         return StateVectorBatch.from_states(states, dtype=dtype, backend=self)
 
@@ -403,6 +421,16 @@ class StateVector:
     def apply_swap(self, first: int, second: int) -> "StateVector":
         check(load().qf_sv_apply_swap(self._h, int(first), int(second)))
         return self
+
+    def apply_rotation_chain(self, gates) -> "StateVector":
+        """CudaDeviceState::apply_rotation_chain (src/cuda.rs:1327-1352):
+        (axis, qubit, theta) rotations, validated first, one fused sweep."""
+        rot = {RotationAxis.X: _abi.GATE_RX, RotationAxis.Y: _abi.GATE_RY, RotationAxis.Z: _abi.GATE_RZ}
+        recs = [(_abi.OP_GATE, rot[int(a)], int(q), 0, 0, float(t)) for a, q, t in gates]
+        return self.apply_ops(_abi.ops_array(recs))
+
+    def apply_rotation(self, axis: int, qubit: int, theta: float) -> "StateVector":
+        return self.apply_rotation_chain([(axis, qubit, theta)])
 
     def apply_ops(self, ops: np.ndarray, params=None, inputs=None, exec_opts=None) -> "StateVector":
         p = None if params is None else np.ascontiguousarray(params, dtype=np.float64)

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from quantumforge_gb300 import (Circuit, Gate, NoiseChannel, PauliSum, QuantumError, SmallRng, StateVector,
+from quantumforge_gb300 import (Circuit, Gate, NoiseChannel, PauliSum, QuantumError, RotationAxis, SmallRng, StateVector,
                                 StateVectorBatch)
 from quantumforge_gb300 import _abi as A
 from quantumforge_gb300 import workloads as W
@@ -33,6 +33,33 @@ def test_cuda_ry_matches_cpu_reference(backend):  # :401-421
         sv.apply(Gate(ax, th), q)
         O.apply(cpu, ax, th, q)
     assert close(sv.amplitudes(), cpu, 1e-12)
+
+
+def test_cuda_rotation_chain_matches_cpu_reference(backend):  # tests/quantum_core.rs:401-422
+    gpu = O.apply(O.apply(O.zero(5), A.GATE_H, 0, 0), A.GATE_RY, -0.2, 3)
+    cpu = gpu.copy()
+    got = backend.apply_rotation_chain(gpu, [(RotationAxis.X, 2, 0.73), (RotationAxis.Y, 4, -0.2), (RotationAxis.Z, 1, 1.1)])
+    for g, q, t in ((A.GATE_RX, 2, 0.73), (A.GATE_RY, 4, -0.2), (A.GATE_RZ, 1, 1.1)):
+        O.apply(cpu, g, t, q)
+    assert close(got, cpu, 1e-12)
+    assert close(backend.apply_ry(gpu, 3, 0.4), O.apply(gpu.copy(), A.GATE_RY, 0.4, 3), 1e-12)
+    assert close(backend.apply_ry_chain(gpu, [(0, 0.1), (1, 0.2)]),
+                 O.apply(O.apply(gpu.copy(), A.GATE_RY, 0.1, 0), A.GATE_RY, 0.2, 1), 1e-12)
+
+
+def test_cuda_device_state_stays_resident_between_dispatches():  # tests/quantum_core.rs:424-446
+    from quantumforge_gb300 import CudaBackend
+
+    initial = O.apply(O.zero(4), A.GATE_H, 0, 0)
+    b = CudaBackend(0)
+    dev = b.upload(initial)
+    dev.apply_rotation(RotationAxis.X, 2, 0.31)
+    dev.apply_rotation_chain([(RotationAxis.Y, 1, -0.83), (RotationAxis.Z, 3, 1.27)])
+    del b  # the state keeps its backend alive, like the reference's Arc
+    want = initial.copy()
+    for g, q, t in ((A.GATE_RX, 2, 0.31), (A.GATE_RY, 1, -0.83), (A.GATE_RZ, 3, 1.27)):
+        O.apply(want, g, t, q)
+    assert close(dev.amplitudes(), want, 1e-12)
 
 
 def test_cuda_entangling_gates_match_cpu_reference(backend):  # :446-486
