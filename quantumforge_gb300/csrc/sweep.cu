@@ -284,15 +284,47 @@ __device__ __forceinline__ void tile_apply(const TileOp &op, C *s0, C *s1, const
         const C m00 = mats[4 * op.mat], m01 = mats[4 * op.mat + 1], m10 = mats[4 * op.mat + 2],
                 m11 = mats[4 * op.mat + 3];
         const uint32_t b = op.b0, mb = 1u << b;
-        for (uint32_t p = tid; p < (T >> 1); p += bd) {
-            const uint32_t i0 = insert0_32(p, b), i1 = i0 | mb;
-            const C a0 = s0[i0], a1 = s0[i1];
-            s0[i0] = cmac2(m00, a0, m01, a1);
-            s0[i1] = cmac2(m10, a0, m11, a1);
-            if (DUAL) {
-                const C c0 = s1[i0], c1 = s1[i1];
-                s1[i0] = cmac2(m00, c0, m01, c1);
-                s1[i1] = cmac2(m10, c0, m11, c1);
+        // Complex128 passes run at the FP64 issue rate, so matrices whose
+        // entries are all real (H, Ry) or real on the diagonal and imaginary
+        // off it (Rx) take half the multiplies of a general 2x2.
+        const bool real = m00.y == 0 && m01.y == 0 && m10.y == 0 && m11.y == 0;
+        const bool xlike = !real && m00.y == 0 && m11.y == 0 && m01.x == 0 && m10.x == 0;
+        if (sizeof(C) == 16 && real) {
+            for (uint32_t p = tid; p < (T >> 1); p += bd) {
+                const uint32_t i0 = insert0_32(p, b), i1 = i0 | mb;
+                const C a0 = s0[i0], a1 = s0[i1];
+                s0[i0] = mk(m00.x * a0.x + m01.x * a1.x, m00.x * a0.y + m01.x * a1.y);
+                s0[i1] = mk(m10.x * a0.x + m11.x * a1.x, m10.x * a0.y + m11.x * a1.y);
+                if (DUAL) {
+                    const C c0 = s1[i0], c1 = s1[i1];
+                    s1[i0] = mk(m00.x * c0.x + m01.x * c1.x, m00.x * c0.y + m01.x * c1.y);
+                    s1[i1] = mk(m10.x * c0.x + m11.x * c1.x, m10.x * c0.y + m11.x * c1.y);
+                }
+            }
+        } else if (sizeof(C) == 16 && xlike) {  // (m00, i u; i v, m11), all four real numbers
+            const auto u = m01.y, v = m10.y;
+            for (uint32_t p = tid; p < (T >> 1); p += bd) {
+                const uint32_t i0 = insert0_32(p, b), i1 = i0 | mb;
+                const C a0 = s0[i0], a1 = s0[i1];
+                s0[i0] = mk(m00.x * a0.x - u * a1.y, m00.x * a0.y + u * a1.x);
+                s0[i1] = mk(m11.x * a1.x - v * a0.y, m11.x * a1.y + v * a0.x);
+                if (DUAL) {
+                    const C c0 = s1[i0], c1 = s1[i1];
+                    s1[i0] = mk(m00.x * c0.x - u * c1.y, m00.x * c0.y + u * c1.x);
+                    s1[i1] = mk(m11.x * c1.x - v * c0.y, m11.x * c1.y + v * c0.x);
+                }
+            }
+        } else {
+            for (uint32_t p = tid; p < (T >> 1); p += bd) {
+                const uint32_t i0 = insert0_32(p, b), i1 = i0 | mb;
+                const C a0 = s0[i0], a1 = s0[i1];
+                s0[i0] = cmac2(m00, a0, m01, a1);
+                s0[i1] = cmac2(m10, a0, m11, a1);
+                if (DUAL) {
+                    const C c0 = s1[i0], c1 = s1[i1];
+                    s1[i0] = cmac2(m00, c0, m01, c1);
+                    s1[i1] = cmac2(m10, c0, m11, c1);
+                }
             }
         }
         break;
