@@ -411,6 +411,20 @@ int qf_dm_probability_one(qf_dm *dm, uint32_t qubit, double *out);
 int qf_dm_probabilities(qf_dm *dm, double *out, uint64_t n_out);
 /* DensityMatrix::measure (src/lib.rs:1922-1947), CudaDeviceDensityMatrix::measure. */
 int qf_dm_measure(qf_dm *dm, uint32_t qubit, uint64_t *rng_state, uint8_t *outcome);
+/* ParameterizedCircuit::expectation_density_with_inputs (src/lib.rs:3175-3186):
+ * the parameterised op list (rotations, encodings, fixed gates, channels)
+ * from |0...0><0...0| through the density matrix, then <P_q> for the
+ * observable P = enum qf_pauli1 on `observable_qubit`. */
+int qf_expectation_density(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops,
+                           const double *params, uint64_t n_params, const double *inputs, uint64_t n_inputs,
+                           int observable, uint32_t observable_qubit, const qf_exec_opts *opts, double *expectation);
+/* parameter_shift_gradient_density_with_inputs (src/lib.rs:3235-3266): two
+ * shifted density runs per rotation occurrence; `expectation` (nullable)
+ * receives the unshifted value. */
+int qf_parameter_shift_gradient_density(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops,
+                                        const double *params, uint64_t n_params, const double *inputs, uint64_t n_inputs,
+                                        int observable, uint32_t observable_qubit, const qf_exec_opts *opts,
+                                        double *expectation, double *gradient);
 /* CudaBackend::run_density_circuit (src/cuda.rs:1022-1045): upload, run, download. */
 int qf_run_density_circuit(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops,
                            const double *in_entries, double *out_entries, uint64_t n_doubles,

@@ -1007,6 +1007,75 @@ class ParameterizedCircuit:
     def run(self, parameters, qubits: int, dtype="c128", backend=None, exec_opts=None) -> StateVector:
         return self.run_with_inputs([], parameters, qubits, dtype=dtype, backend=backend, exec_opts=exec_opts)
 
+    # ---- the density-matrix path (channels; src/lib.rs:3125-3266, 3755-3800) ----
+    def _resolved_ops(self, inputs, parameters) -> np.ndarray:
+        """The op list with rotation and encoding angles bound to fixed gates."""
+        i, p = self._values(inputs, parameters)
+        ops = self.ops().copy()
+        rot = {_abi.PAULI_X: _abi.GATE_RX, _abi.PAULI_Y: _abi.GATE_RY, _abi.PAULI_Z: _abi.GATE_RZ}
+        for k in range(len(ops)):
+            kind = int(ops[k]["kind"])
+            if kind in (_abi.OP_ROTATION, _abi.OP_ENCODING):
+                src = p if kind == _abi.OP_ROTATION else i
+                idx = int(ops[k]["param"])
+                if idx >= src.size:
+                    name = "InvalidParameterCount" if kind == _abi.OP_ROTATION else "InvalidInputCount"
+                    raise QuantumError(_abi.STATUS_CODES[name], f"index {idx} exceeds the {src.size} values given")
+                ops[k]["theta"] = float(src[idx])
+                ops[k]["gate"] = rot[int(ops[k]["gate"])]
+                ops[k]["kind"] = _abi.OP_GATE
+                ops[k]["param"] = 0
+        return ops
+
+    def run_density_with_inputs(self, inputs, parameters, qubits: int, dtype="c128", backend=None,
+                                exec_opts=None) -> "DensityMatrix":
+        """ParameterizedCircuit::run_density_with_inputs (src/lib.rs:3125-3132)."""
+        rho = DensityMatrix.zero(qubits, dtype=dtype, backend=backend)
+        return rho.apply_ops(self._resolved_ops(inputs, parameters), exec_opts)
+
+    def run_density(self, parameters, qubits: int, **kw) -> "DensityMatrix":
+        return self.run_density_with_inputs([], parameters, qubits, **kw)
+
+    def expectation_density_with_inputs(self, inputs, parameters, qubits: int, observable: int, observable_qubit: int,
+                                        dtype="c128", backend=None, exec_opts=None) -> float:
+        """expectation_density_with_inputs (src/lib.rs:3175-3186)."""
+        i, p = self._values(inputs, parameters)
+        be = backend or default_backend()
+        ops = self.ops()
+        v = C.c_double()
+        check(load().qf_expectation_density(be.handle, int(qubits), _dtype_code(dtype), ptr(ops), len(ops), ptr(p), p.size,
+                                            ptr(i), i.size, int(observable), int(observable_qubit), _exec(exec_opts),
+                                            C.byref(v)))
+        return v.value
+
+    def parameter_shift_gradient_density_with_inputs(self, inputs, parameters, qubits: int, observable: int,
+                                                     observable_qubit: int, dtype="c128", backend=None,
+                                                     exec_opts=None) -> np.ndarray:
+        """parameter_shift_gradient_density_with_inputs (src/lib.rs:3235-3266)."""
+        i, p = self._values(inputs, parameters)
+        be = backend or default_backend()
+        ops = self.ops()
+        g = np.zeros(p.size, dtype=np.float64)
+        check(load().qf_parameter_shift_gradient_density(be.handle, int(qubits), _dtype_code(dtype), ptr(ops), len(ops),
+                                                         ptr(p), p.size, ptr(i), i.size, int(observable),
+                                                         int(observable_qubit), _exec(exec_opts), None, ptr(g)))
+        return g
+
+    def mse_loss_and_gradient_density(self, data, parameters, qubits: int, observable: int, observable_qubit: int,
+                                      **kw):
+        """mse_loss_and_gradient_density (src/lib.rs:3755-3800): mean squared
+        error of the density-matrix expectations and its parameter-shift gradient."""
+        if not data or any(len(x) != self.input_count_ or not math.isfinite(y) or not all(math.isfinite(v) for v in x)
+                           for x, y in data):
+            raise QuantumError(_abi.STATUS_CODES["InvalidArgument"], "invalid training data")
+        p = np.ascontiguousarray(parameters, dtype=np.float64)
+        loss, grad = 0.0, np.zeros(self.parameter_count_)
+        for x, y in data:
+            r = self.expectation_density_with_inputs(x, p, qubits, observable, observable_qubit, **kw) - y
+            loss += r * r
+            grad += 2.0 * r * self.parameter_shift_gradient_density_with_inputs(x, p, qubits, observable, observable_qubit, **kw)
+        return loss / len(data), grad / len(data)
+
     def expectation_pauli_sum(self, parameters, qubits: int, hamiltonian, inputs=None, dtype="c128", backend=None,
                               exec_opts=None) -> float:
         i, p = self._values(inputs, parameters)

@@ -1248,12 +1248,21 @@ int channel_coefficients(const qf_op &o, double coef[6]) {
     }
 }
 
-int lower_density_ops(uint32_t n, const qf_op *ops, uint64_t n_ops, std::vector<DmStep> &steps) {
+// Parameterised lists (rotations, encodings; ParameterizedCircuit::
+// run_density_with_shift, src/lib.rs:4742-4806) bind their angles from
+// params/inputs, with `shift` added to op `shift_op`.
+int lower_density_ops(uint32_t n, const qf_op *ops, uint64_t n_ops, std::vector<DmStep> &steps, const double *params = nullptr,
+                      uint64_t n_params = 0, const double *inputs = nullptr, uint64_t n_inputs = 0, int64_t shift_op = -1,
+                      double shift = 0.0) {
     std::vector<qf_op> run;
+    uint64_t run_start = 0;
     auto close_run = [&]() -> int {
         if (run.empty()) return QF_OK;
         std::vector<BGate> g;
-        QF_TRY(bind_ops(n, run.data(), run.size(), nullptr, 0, nullptr, 0, -1, 0.0, g));
+        const int64_t local = shift_op >= (int64_t)run_start && shift_op < (int64_t)(run_start + run.size())
+                                  ? shift_op - (int64_t)run_start
+                                  : -1;
+        QF_TRY(bind_ops(n, run.data(), run.size(), params, n_params, inputs, n_inputs, local, shift, g));
         DmStep st;
         for (const BGate &x : g) lower_to_density(x, n, st.gates);
         steps.push_back(std::move(st));
@@ -1262,6 +1271,7 @@ int lower_density_ops(uint32_t n, const qf_op *ops, uint64_t n_ops, std::vector<
     };
     for (uint64_t k = 0; k < n_ops; ++k) {
         if (ops[k].kind != QF_OP_CHANNEL) {
+            if (run.empty()) run_start = k;
             run.push_back(ops[k]);
             continue;
         }
@@ -1441,6 +1451,82 @@ int qf_dm_measure(qf_dm *dm, uint32_t qubit, uint64_t *rng_state, uint8_t *outco
     QF_TRY(dm_collapse(dm->sv, dm->n, qubit, o, prob));
     QF_CUDA(cudaStreamSynchronize(dm->sv->ctx->stream));
     *outcome = o;
+    return QF_OK;
+}
+
+// ParameterizedCircuit::run_density_with_shift from |0...0><0...0| and the
+// expectation of one Pauli on one qubit (expectation_density_with_inputs,
+// src/lib.rs:3175-3186), on the context's scratch matrix.
+static int density_expectation(qf_ctx *ctx, uint32_t n, int dtype, const qf_op *ops, uint64_t n_ops, const double *params,
+                               uint64_t n_params, const double *inputs, uint64_t n_inputs, int64_t shift_op, double shift,
+                               int mode, uint32_t q, const qf_exec_opts *opts, double *out) {
+    std::vector<DmStep> steps;
+    QF_TRY(lower_density_ops(n, ops, n_ops, steps, params, n_params, inputs, n_inputs, shift_op, shift));
+    qf_sv *sv;
+    QF_TRY(scratch_state(ctx, &ctx->scratch_sv, 2 * n, dtype, &sv));
+    QF_TRY(fill_zero_state(sv));
+    QF_TRY(run_density_steps(sv, n, steps, opts));
+    double r[2];
+    QF_TRY(dm_diag_reduce(sv, n, q, mode, r));
+    *out = r[0];
+    return QF_OK;
+}
+
+static int density_checks(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops, const double *params,
+                          uint64_t n_params, const double *inputs, uint64_t n_inputs, int observable, uint32_t q, int *mode) {
+    if (!ctx || (n_ops && !ops) || (n_params && !params) || (n_inputs && !inputs)) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    QF_TRY(check_dtype(dtype));
+    QF_TRY(check_dm_qubits(qubits));
+    for (uint64_t i = 0; i < n_params; ++i)
+        if (!std::isfinite(params[i])) return fail(QF_ERR_NON_FINITE_PARAMETER, "parameter %llu is not finite", (unsigned long long)i);
+    for (uint64_t i = 0; i < n_inputs; ++i)
+        if (!std::isfinite(inputs[i])) return fail(QF_ERR_NON_FINITE_PARAMETER, "input %llu is not finite", (unsigned long long)i);
+    if (q >= qubits) return fail(QF_ERR_QUBIT_OUT_OF_RANGE, "qubit index %u is out of range for %u qubits", q, qubits);
+    *mode = observable == QF_PAULI_Z ? 2 : observable == QF_PAULI_X ? 3 : observable == QF_PAULI_Y ? 4 : -1;
+    if (*mode < 0) return fail(QF_ERR_INVALID_ARGUMENT, "unknown observable %d", observable);
+    return QF_OK;
+}
+
+int qf_expectation_density(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops, const double *params,
+                           uint64_t n_params, const double *inputs, uint64_t n_inputs, int observable, uint32_t observable_qubit,
+                           const qf_exec_opts *opts, double *expectation) {
+    clear_error();
+    if (!expectation) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    int mode;
+    QF_TRY(density_checks(ctx, qubits, dtype, ops, n_ops, params, n_params, inputs, n_inputs, observable, observable_qubit, &mode));
+    QF_TRY(bind_device(ctx));
+    return density_expectation(ctx, qubits, dtype, ops, n_ops, params, n_params, inputs, n_inputs, -1, 0.0, mode,
+                               observable_qubit, opts, expectation);
+}
+
+// ParameterizedCircuit::parameter_shift_gradient_density_with_inputs
+// (src/lib.rs:3235-3266): every rotation occurrence shifted by +-pi/2 through
+// the density-matrix path, g[param] += (E+ - E-) / 2.
+int qf_parameter_shift_gradient_density(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops,
+                                        const double *params, uint64_t n_params, const double *inputs, uint64_t n_inputs,
+                                        int observable, uint32_t observable_qubit, const qf_exec_opts *opts,
+                                        double *expectation, double *gradient) {
+    clear_error();
+    if (n_params && !gradient) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    int mode;
+    QF_TRY(density_checks(ctx, qubits, dtype, ops, n_ops, params, n_params, inputs, n_inputs, observable, observable_qubit, &mode));
+    QF_TRY(bind_device(ctx));
+    std::vector<double> g(n_params, 0.0);
+    double e;
+    QF_TRY(density_expectation(ctx, qubits, dtype, ops, n_ops, params, n_params, inputs, n_inputs, -1, 0.0, mode,
+                               observable_qubit, opts, &e));  // also validates the whole list before any shift runs
+    const double shift = 1.5707963267948966;  // FRAC_PI_2
+    for (uint64_t k = 0; k < n_ops; ++k) {
+        if (ops[k].kind != QF_OP_ROTATION) continue;
+        double plus, minus;
+        QF_TRY(density_expectation(ctx, qubits, dtype, ops, n_ops, params, n_params, inputs, n_inputs, (int64_t)k, shift, mode,
+                                   observable_qubit, opts, &plus));
+        QF_TRY(density_expectation(ctx, qubits, dtype, ops, n_ops, params, n_params, inputs, n_inputs, (int64_t)k, -shift, mode,
+                                   observable_qubit, opts, &minus));
+        g[ops[k].param] += 0.5 * (plus - minus);
+    }
+    if (expectation) *expectation = e;
+    std::copy(g.begin(), g.end(), gradient);
     return QF_OK;
 }
 

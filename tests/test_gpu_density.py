@@ -148,3 +148,77 @@ def test_density_errors(backend):
     with pytest.raises(QuantumError) as e:
         DensityMatrix.from_state(StateVector.zero(4, backend=backend)).apply_cnot(0, 0)
     assert e.value.kind == "InvalidQubitPair"
+
+
+def _resolve(ops, params, inputs):
+    """Rotation and encoding records bound to fixed gates (the oracle's run_density takes Circuit ops)."""
+    out = ops.copy()
+    rot = {A.PAULI_X: A.GATE_RX, A.PAULI_Y: A.GATE_RY, A.PAULI_Z: A.GATE_RZ}
+    for k in range(len(out)):
+        kind = int(out[k]["kind"])
+        if kind in (A.OP_ROTATION, A.OP_ENCODING):
+            src = params if kind == A.OP_ROTATION else inputs
+            out[k]["theta"] = src[int(out[k]["param"])]
+            out[k]["gate"] = rot[int(out[k]["gate"])]
+            out[k]["kind"] = A.OP_GATE
+            out[k]["param"] = 0
+    return out
+
+
+def test_noisy_parameterized_circuit_uses_density_matrix_parameter_shift(backend):  # tests/quantum_core.rs:125-182
+    from quantumforge_gb300 import ParameterizedCircuit, RotationAxis
+
+    c = ParameterizedCircuit.with_inputs(1, 1)
+    c.encode_rotation(RotationAxis.Y, 0, 0)
+    c.rotation(RotationAxis.X, 0, 0)
+    c.channel(0, NoiseChannel.AmplitudeDamping(0.23))
+    c.channel(0, NoiseChannel.Depolarizing(0.08))
+    inputs, params = [0.39], np.array([0.71])
+    with pytest.raises(QuantumError) as e:
+        c.run_with_inputs(inputs, params, 1, backend=backend)
+    assert e.value.kind == "OperationRequiresDensityMatrix"
+    eps = 1e-6
+    for obs in (A.PAULI_X, A.PAULI_Y, A.PAULI_Z):
+        g = c.parameter_shift_gradient_density_with_inputs(inputs, params, 1, obs, 0, backend=backend)[0]
+        vp = c.expectation_density_with_inputs(inputs, params + eps, 1, obs, 0, backend=backend)
+        vm = c.expectation_density_with_inputs(inputs, params - eps, 1, obs, 0, backend=backend)
+        assert abs(g - (vp - vm) / (2 * eps)) < 1e-8
+        rho = O.run_density(_resolve(c.ops(), params, inputs), 1)
+        assert abs(c.expectation_density_with_inputs(inputs, params, 1, obs, 0, backend=backend)
+                   - O.dm_expectation(rho, obs, 0)) < 1e-13
+    data = [([0.15], 0.62), ([0.71], -0.08), ([-0.32], 0.91)]
+    _, grad = c.mse_loss_and_gradient_density(data, params, 1, A.PAULI_Z, 0, backend=backend)
+    lp = c.mse_loss_and_gradient_density(data, params + eps, 1, A.PAULI_Z, 0, backend=backend)[0]
+    lm = c.mse_loss_and_gradient_density(data, params - eps, 1, A.PAULI_Z, 0, backend=backend)[0]
+    assert abs(grad[0] - (lp - lm) / (2 * eps)) < 1e-8
+
+
+@pytest.mark.parametrize("n,dtype,tol", [(4, "c128", 1e-12), (7, "c128", 1e-11), (6, "c64", 2e-6)])
+def test_density_parameter_shift_matches_the_oracle(backend, n, dtype, tol):
+    from quantumforge_gb300 import ParameterizedCircuit, RotationAxis
+
+    r = np.random.default_rng(n)
+    c = ParameterizedCircuit.with_inputs(5, 2)
+    for q in range(n):
+        c.encode_rotation(RotationAxis.Y, q, q % 2)
+    for layer in range(2):
+        for q in range(n):
+            c.rotation(int(r.integers(0, 3)), q, int(r.integers(0, 5)))
+            c.channel(q, NoiseChannel.AmplitudeDamping(float(r.uniform(0.01, 0.2))))
+        for q in range(n - 1):
+            c.cnot(q, q + 1)
+        c.channel(n // 2, NoiseChannel.ThermalDamping(0.1, 0.5))
+    params, inputs = r.uniform(-np.pi, np.pi, 5), r.uniform(-1, 1, 2)
+    g = c.parameter_shift_gradient_density_with_inputs(inputs, params, n, A.PAULI_Z, 1, dtype=dtype, backend=backend)
+    ops = c.ops()
+    want = np.zeros(5)
+    for k in range(len(ops)):
+        if int(ops[k]["kind"]) != A.OP_ROTATION:
+            continue
+        res = []
+        for d in (np.pi / 2, -np.pi / 2):
+            shifted = _resolve(ops, params, inputs)
+            shifted[k]["theta"] += d
+            res.append(O.dm_expectation(O.run_density(shifted, n), A.PAULI_Z, 1))
+        want[int(ops[k]["param"])] += 0.5 * (res[0] - res[1])
+    assert np.abs(g - want).max() < tol * 10
