@@ -30,15 +30,17 @@ namespace {
 enum : uint8_t { T_GATE = 0, T_CNOT = 1, T_CZ = 2, T_SWAP = 3, T_MEASURE = 4, T_COND = 5, T_DEP = 6, T_AD = 7, T_PD = 8,
                  T_TH = 9, T_DIAG = 10, T_REAL = 11, T_X = 12 };
 
-// One op of a trajectory program. GATE/COND: m = the 2x2 matrix (re, im);
-// channels: m[0] = probability / gamma / gamma_down, m[1] = gamma_up,
-// m[2] = sqrt(m[0]), m[3] = sqrt(1 - m[0]), m[4] = sqrt(m[1]), m[5] = sqrt(1 - m[1]).
+// One op of a trajectory program. GATE/COND: m = the 2x2 matrix (re, im),
+// mf the same in f32 for complex64 states; channels: m[0] = probability /
+// gamma / gamma_down, m[1] = gamma_up, m[2] = sqrt(m[0]), m[3] = sqrt(1 - m[0]),
+// m[4] = sqrt(m[1]), m[5] = sqrt(1 - m[1]).
 struct TOp {
     uint8_t kind;
     uint8_t value;   // COND: required classical value
     uint16_t pad;
     uint32_t q0, q1, cbit;
     double m[8];
+    float mf[8];
 };
 
 constexpr double kEps = 2.220446049250313e-16;
@@ -57,40 +59,21 @@ __device__ __forceinline__ double next_u(uint64_t &x) {
 
 __device__ __forceinline__ double clamp01d(double x) { return fmin(1.0, fmax(0.0, x)); }
 
-// v * s in the state's precision (complex128 stays f64; complex64 keeps its
-// inner loops off the FP64 pipe, which runs at a small fraction of FP32).
-template <typename C> __device__ __forceinline__ C scale(C v, double s) {
-    using R = typename Real<C>::T;
-    const R r = (R)s;
-    return mk(v.x * r, v.y * r);
+template <typename R> __device__ __forceinline__ R warp_sum_r(R v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
 }
 
-// (sum over amplitudes with bit q set, sum over all) of |a|^2, on every
-// thread. Per-thread partial sums in the state's own precision (a complex64
-// state's f32 rounding dominates anyway; FP64 throughput is the bound of the
-// complex128 kernel), added across threads in f64.
-template <typename C>
-__device__ void reduce_p1_norm(const C *a, uint32_t dim, uint32_t q, double *red, double *bc, double &p1, double &norm) {
-    using R = typename Real<C>::T;
-    R xs = 0, ys = 0;
-    for (uint32_t i = threadIdx.x; i < dim; i += blockDim.x) {
-        const C v = a[i];
-        const R w = v.x * v.x + v.y * v.y;
-        ys += w;
-        if ((i >> q) & 1u) xs += w;
-    }
-    double x = (double)xs, y = (double)ys;
-    x = block_sum(x, red);
-    __syncthreads();
-    y = block_sum(y, red);
-    if (threadIdx.x == 0) {
-        bc[0] = x;
-        bc[1] = y;
-    }
-    __syncthreads();
-    p1 = bc[0];
-    norm = bc[1];
-}
+// The per-shot decisions (uniform draw, thresholds, branch weights) are made
+// by thread 0 alone in f64 with round-to-nearest operations and broadcast
+// through shared memory: FP64 issues at a small fraction of FP32 on GB300, so
+// the other 255 threads never touch it for a complex64 state.
+struct Decision {
+    int branch;  // measurement outcome / Kraus branch / Pauli index (-1: none)
+    int fault;
+    double s[4];
+};
 
 template <typename C>
 __global__ void __launch_bounds__(256) k_trajectories(const C *__restrict__ init, uint32_t n, const TOp *__restrict__ ops,
@@ -98,15 +81,16 @@ __global__ void __launch_bounds__(256) k_trajectories(const C *__restrict__ init
                                                       double tie_eps, int rel_norm, uint64_t *__restrict__ out,
                                                       unsigned long long *ties, int *err) {
     using R = typename Real<C>::T;
+    constexpr bool kF32 = sizeof(R) == 4;
     extern __shared__ __align__(16) unsigned char traj_smem[];
     C *a = reinterpret_cast<C *>(traj_smem);
-    __shared__ double red[32];
-    __shared__ double bc[2];
+    __shared__ R wred[2][8];
+    __shared__ Decision dec;
     const uint32_t dim = 1u << n, half = dim >> 1, quarter = dim >> 2;
-    const unsigned tid = threadIdx.x, nt = blockDim.x;
+    const unsigned tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
     for (uint64_t s = blockIdx.x; s < shots; s += gridDim.x) {
         for (uint32_t i = tid; i < dim; i += nt) a[i] = init[i];
-        uint64_t rng = starts[s];
+        uint64_t rng = starts[s];  // used by thread 0
         uint64_t reg = 0;
         unsigned long long my_ties = 0;
         __syncthreads();
@@ -116,19 +100,31 @@ __global__ void __launch_bounds__(256) k_trajectories(const C *__restrict__ init
             const uint32_t q = op.q0;
             const uint32_t qm = 1u << q;
             if (kind == T_COND && ((reg >> op.cbit) & 1ULL) != (uint64_t)op.value) continue;
-            if (kind == T_DIAG) {  // diag(m00, m11): Rz, S, T, Z and their adjoints
-                const C m00 = mk((R)op.m[0], (R)op.m[1]), m11 = mk((R)op.m[6], (R)op.m[7]);
-                for (uint32_t i = tid; i < dim; i += nt) a[i] = cmul((i >> q) & 1u ? m11 : m00, a[i]);
-                __syncthreads();
-                continue;
-            }
-            if (kind == T_REAL) {  // real 2x2: H, Ry
-                const R r00 = (R)op.m[0], r01 = (R)op.m[2], r10 = (R)op.m[4], r11 = (R)op.m[6];
-                for (uint32_t p = tid; p < half; p += nt) {
-                    const uint32_t i0 = ins0(p, q), i1 = i0 | qm;
-                    const C a0 = a[i0], a1 = a[i1];
-                    a[i0] = mk(r00 * a0.x + r01 * a1.x, r00 * a0.y + r01 * a1.y);
-                    a[i1] = mk(r10 * a0.x + r11 * a1.x, r10 * a0.y + r11 * a1.y);
+            if (kind == T_GATE || kind == T_COND || kind == T_DIAG || kind == T_REAL) {
+                C m00, m01, m10, m11;
+                if (kF32) {
+                    m00 = mk((R)op.mf[0], (R)op.mf[1]), m01 = mk((R)op.mf[2], (R)op.mf[3]);
+                    m10 = mk((R)op.mf[4], (R)op.mf[5]), m11 = mk((R)op.mf[6], (R)op.mf[7]);
+                } else {
+                    m00 = mk((R)op.m[0], (R)op.m[1]), m01 = mk((R)op.m[2], (R)op.m[3]);
+                    m10 = mk((R)op.m[4], (R)op.m[5]), m11 = mk((R)op.m[6], (R)op.m[7]);
+                }
+                if (kind == T_DIAG) {  // diag(m00, m11): Rz, S, T, Z and their adjoints
+                    for (uint32_t i = tid; i < dim; i += nt) a[i] = cmul((i >> q) & 1u ? m11 : m00, a[i]);
+                } else if (kind == T_REAL) {  // real 2x2: H, Ry
+                    for (uint32_t p = tid; p < half; p += nt) {
+                        const uint32_t i0 = ins0(p, q), i1 = i0 | qm;
+                        const C a0 = a[i0], a1 = a[i1];
+                        a[i0] = mk(m00.x * a0.x + m01.x * a1.x, m00.x * a0.y + m01.x * a1.y);
+                        a[i1] = mk(m10.x * a0.x + m11.x * a1.x, m10.x * a0.y + m11.x * a1.y);
+                    }
+                } else {
+                    for (uint32_t p = tid; p < half; p += nt) {
+                        const uint32_t i0 = ins0(p, q), i1 = i0 | qm;
+                        const C a0 = a[i0], a1 = a[i1];
+                        a[i0] = cmac2(m00, a0, m01, a1);
+                        a[i1] = cmac2(m10, a0, m11, a1);
+                    }
                 }
                 __syncthreads();
                 continue;
@@ -139,18 +135,6 @@ __global__ void __launch_bounds__(256) k_trajectories(const C *__restrict__ init
                     const C a0 = a[i0];
                     a[i0] = a[i1];
                     a[i1] = a0;
-                }
-                __syncthreads();
-                continue;
-            }
-            if (kind == T_GATE || kind == T_COND) {
-                const C m00 = mk((R)op.m[0], (R)op.m[1]), m01 = mk((R)op.m[2], (R)op.m[3]);
-                const C m10 = mk((R)op.m[4], (R)op.m[5]), m11 = mk((R)op.m[6], (R)op.m[7]);
-                for (uint32_t p = tid; p < half; p += nt) {
-                    const uint32_t i0 = ins0(p, q), i1 = i0 | qm;
-                    const C a0 = a[i0], a1 = a[i1];
-                    a[i0] = cmac2(m00, a0, m01, a1);
-                    a[i1] = cmac2(m10, a0, m11, a1);
                 }
                 __syncthreads();
                 continue;
@@ -177,12 +161,20 @@ __global__ void __launch_bounds__(256) k_trajectories(const C *__restrict__ init
                 continue;
             }
             if (kind == T_DEP) {  // src/lib.rs:1369-1381: one draw, X/Y/Z with probability p/3 each
-                const double pr = op.m[0];
-                const double u = next_u(rng);
-                const double keep = __dsub_rn(1.0, pr);
-                if (u >= keep && pr > 0.0) {
-                    const double b = floor(__dmul_rn(__dsub_rn(u, keep), __ddiv_rn(3.0, pr)));
-                    const int g = b >= 2.0 ? 2 : (int)b;
+                if (tid == 0) {
+                    const double pr = op.m[0];
+                    const double u = next_u(rng);
+                    const double keep = __dsub_rn(1.0, pr);
+                    int g = -1;
+                    if (u >= keep && pr > 0.0) {
+                        const double b = floor(__dmul_rn(__dsub_rn(u, keep), __ddiv_rn(3.0, pr)));
+                        g = b >= 2.0 ? 2 : (int)b;
+                    }
+                    dec.branch = g;
+                }
+                __syncthreads();
+                const int g = dec.branch;
+                if (g >= 0) {
                     for (uint32_t p = tid; p < half; p += nt) {
                         const uint32_t i0 = ins0(p, q), i1 = i0 | qm;
                         const C a0 = a[i0], a1 = a[i1];
@@ -196,102 +188,136 @@ __global__ void __launch_bounds__(256) k_trajectories(const C *__restrict__ init
                             a[i1] = mk(-a1.x, -a1.y);
                         }
                     }
-                    __syncthreads();
                 }
+                __syncthreads();
                 continue;
             }
-            // measurement and damping channels need P(1) and the norm
-            double p_one, norm;
-            reduce_p1_norm(a, dim, q, red, bc, p_one, norm);
-            int fault = 0;
-            if (kind == T_MEASURE) {  // StateVector::measure, src/lib.rs:1321-1351
-                double p = p_one;
-                if (rel_norm && norm > 0.0) p = __ddiv_rn(p_one, norm);
-                p = clamp01d(p);
-                const double u = next_u(rng);
-                const int o = u < p ? 1 : 0;
-                if (tid == 0 && fabs(u - p) < tie_eps) ++my_ties;
-                const double prob = o ? p : __dsub_rn(1.0, p);
-                if (prob <= kEps) {
-                    fault = 1;
-                } else {
-                    const double inv = 1.0 / sqrt(prob);  // one rounding more than the reference's division
-                    for (uint32_t i = tid; i < dim; i += nt)
-                        a[i] = ((int)((i >> q) & 1u) == o) ? scale(a[i], inv) : mk((R)0, (R)0);
-                    reg = (reg & ~(1ULL << op.cbit)) | ((uint64_t)o << op.cbit);
+            // measurement and damping channels: P(1) and the norm, reduced
+            // per thread and per warp in the state's precision
+            {
+                R xs = 0, ys = 0;
+                for (uint32_t i = tid; i < dim; i += nt) {
+                    const C v = a[i];
+                    const R w = v.x * v.x + v.y * v.y;
+                    ys += w;
+                    if ((i >> q) & 1u) xs += w;
                 }
-            } else if (kind == T_AD || kind == T_PD) {  // src/lib.rs:1383-1438
-                const double g = op.m[0];
-                if (!isfinite(norm) || norm <= kEps) {
-                    fault = 1;
-                } else {
-                    const double gp = __dmul_rn(g, p_one);
-                    const double jp = clamp01d(__ddiv_rn(gp, norm));
-                    const double u = next_u(rng);
-                    const bool jump = u < jp;
-                    if (tid == 0 && fabs(u - jp) < tie_eps) ++my_ties;
-                    const double bn = jump ? gp : __dsub_rn(norm, gp);
-                    if (!isfinite(bn) || bn <= kEps) {
-                        fault = 1;
-                    } else {
-                        const double inv = 1.0 / sqrt(bn);
-                        const double s_jump = op.m[2] * inv, s_exc = op.m[3] * inv;
-                        for (uint32_t p = tid; p < half; p += nt) {
-                            const uint32_t i0 = ins0(p, q), i1 = i0 | qm;
-                            const C a0 = a[i0], a1 = a[i1];
-                            if (jump) {
-                                if (kind == T_AD) {
-                                    a[i0] = scale(a1, s_jump);
-                                    a[i1] = mk((R)0, (R)0);
-                                } else {
-                                    a[i0] = mk((R)0, (R)0);
-                                    a[i1] = scale(a1, s_jump);
-                                }
-                            } else {
-                                a[i0] = scale(a0, inv);
-                                a[i1] = scale(a1, s_exc);
-                            }
-                        }
-                    }
-                }
-            } else {  // T_TH, src/lib.rs:1440-1503
-                const double gd = op.m[0], gu = op.m[1];
-                if (!isfinite(norm) || norm <= kEps) {
-                    fault = 1;
-                } else {
-                    const double p1 = clamp01d(__ddiv_rn(p_one, norm)), p0 = __dsub_rn(1.0, p1);
-                    const double down = __dmul_rn(p1, gd), up = __dmul_rn(p0, gu);
-                    const double stay = __dadd_rn(__dmul_rn(p0, __dsub_rn(1.0, gu)), __dmul_rn(p1, __dsub_rn(1.0, gd)));
-                    const double du = __dadd_rn(down, up);
-                    const double u = next_u(rng);
-                    const int br = u < down ? 1 : (u < du ? 2 : 0);
-                    if (tid == 0 && (fabs(u - down) < tie_eps || fabs(u - du) < tie_eps)) ++my_ties;
-                    const double bn = br == 1 ? down : (br == 2 ? up : stay);
-                    if (!isfinite(bn) || bn <= kEps) {
-                        fault = 1;
-                    } else {
-                        const double inv = 1.0 / sqrt(bn);
-                        const double s1 = op.m[2] * inv, s2 = op.m[4] * inv, s0g = op.m[5] * inv, s0e = op.m[3] * inv;
-                        for (uint32_t p = tid; p < half; p += nt) {
-                            const uint32_t i0 = ins0(p, q), i1 = i0 | qm;
-                            const C a0 = a[i0], a1 = a[i1];
-                            if (br == 1) {
-                                a[i0] = scale(a1, s1);
-                                a[i1] = mk((R)0, (R)0);
-                            } else if (br == 2) {
-                                a[i1] = scale(a0, s2);
-                                a[i0] = mk((R)0, (R)0);
-                            } else {
-                                a[i0] = scale(a0, s0g);
-                                a[i1] = scale(a1, s0e);
-                            }
-                        }
-                    }
+                xs = warp_sum_r(xs);
+                ys = warp_sum_r(ys);
+                if (lane == 0) {
+                    wred[0][warp] = xs;
+                    wred[1][warp] = ys;
                 }
             }
-            if (fault) {  // uniform across the CTA: every thread saw the same reduced values
-                if (tid == 0) atomicExch(err, 1);
-                return;
+            __syncthreads();
+            if (tid == 0) {
+                double p_one = 0.0, norm = 0.0;
+                for (unsigned w = 0; w < (nt >> 5); ++w) {
+                    p_one += (double)wred[0][w];
+                    norm += (double)wred[1][w];
+                }
+                Decision d{-1, 0, {0.0, 0.0, 0.0, 0.0}};
+                if (kind == T_MEASURE) {  // StateVector::measure, src/lib.rs:1321-1351
+                    double p = p_one;
+                    if (rel_norm && norm > 0.0) p = __ddiv_rn(p_one, norm);
+                    p = clamp01d(p);
+                    const double u = next_u(rng);
+                    d.branch = u < p ? 1 : 0;
+                    if (fabs(u - p) < tie_eps) ++my_ties;
+                    const double prob = d.branch ? p : __dsub_rn(1.0, p);
+                    if (prob <= kEps) d.fault = 1;
+                    else d.s[0] = 1.0 / sqrt(prob);  // one rounding more than the reference's division
+                } else if (kind == T_AD || kind == T_PD) {  // src/lib.rs:1383-1438
+                    const double g = op.m[0];
+                    if (!isfinite(norm) || norm <= kEps) {
+                        d.fault = 1;
+                    } else {
+                        const double gp = __dmul_rn(g, p_one);
+                        const double jp = clamp01d(__ddiv_rn(gp, norm));
+                        const double u = next_u(rng);
+                        d.branch = u < jp ? 1 : 0;
+                        if (fabs(u - jp) < tie_eps) ++my_ties;
+                        const double bn = d.branch ? gp : __dsub_rn(norm, gp);
+                        if (!isfinite(bn) || bn <= kEps) {
+                            d.fault = 1;
+                        } else {
+                            const double inv = 1.0 / sqrt(bn);
+                            d.s[0] = inv;
+                            d.s[1] = op.m[2] * inv;  // jump
+                            d.s[2] = op.m[3] * inv;  // no jump, excited part
+                        }
+                    }
+                } else {  // T_TH, src/lib.rs:1440-1503
+                    const double gd = op.m[0], gu = op.m[1];
+                    if (!isfinite(norm) || norm <= kEps) {
+                        d.fault = 1;
+                    } else {
+                        const double p1 = clamp01d(__ddiv_rn(p_one, norm)), p0 = __dsub_rn(1.0, p1);
+                        const double down = __dmul_rn(p1, gd), up = __dmul_rn(p0, gu);
+                        const double stay = __dadd_rn(__dmul_rn(p0, __dsub_rn(1.0, gu)), __dmul_rn(p1, __dsub_rn(1.0, gd)));
+                        const double du = __dadd_rn(down, up);
+                        const double u = next_u(rng);
+                        d.branch = u < down ? 1 : (u < du ? 2 : 0);
+                        if (fabs(u - down) < tie_eps || fabs(u - du) < tie_eps) ++my_ties;
+                        const double bn = d.branch == 1 ? down : (d.branch == 2 ? up : stay);
+                        if (!isfinite(bn) || bn <= kEps) {
+                            d.fault = 1;
+                        } else {
+                            const double inv = 1.0 / sqrt(bn);
+                            d.s[0] = op.m[2] * inv;  // down
+                            d.s[1] = op.m[4] * inv;  // up
+                            d.s[2] = op.m[5] * inv;  // stay, ground part
+                            d.s[3] = op.m[3] * inv;  // stay, excited part
+                        }
+                    }
+                }
+                dec = d;
+                if (d.fault) atomicExch(err, 1);
+            }
+            __syncthreads();
+            if (dec.fault) return;  // uniform across the CTA
+            const int br = dec.branch;
+            if (kind == T_MEASURE) {
+                const R inv = (R)dec.s[0];
+                for (uint32_t i = tid; i < dim; i += nt) {
+                    const C v = a[i];
+                    a[i] = ((int)((i >> q) & 1u) == br) ? mk(v.x * inv, v.y * inv) : mk((R)0, (R)0);
+                }
+                reg = (reg & ~(1ULL << op.cbit)) | ((uint64_t)br << op.cbit);
+            } else if (kind == T_AD || kind == T_PD) {
+                const R inv = (R)dec.s[0], s_jump = (R)dec.s[1], s_exc = (R)dec.s[2];
+                for (uint32_t p = tid; p < half; p += nt) {
+                    const uint32_t i0 = ins0(p, q), i1 = i0 | qm;
+                    const C a0 = a[i0], a1 = a[i1];
+                    if (br) {
+                        if (kind == T_AD) {
+                            a[i0] = mk(a1.x * s_jump, a1.y * s_jump);
+                            a[i1] = mk((R)0, (R)0);
+                        } else {
+                            a[i0] = mk((R)0, (R)0);
+                            a[i1] = mk(a1.x * s_jump, a1.y * s_jump);
+                        }
+                    } else {
+                        a[i0] = mk(a0.x * inv, a0.y * inv);
+                        a[i1] = mk(a1.x * s_exc, a1.y * s_exc);
+                    }
+                }
+            } else {
+                const R s1 = (R)dec.s[0], s2 = (R)dec.s[1], s0g = (R)dec.s[2], s0e = (R)dec.s[3];
+                for (uint32_t p = tid; p < half; p += nt) {
+                    const uint32_t i0 = ins0(p, q), i1 = i0 | qm;
+                    const C a0 = a[i0], a1 = a[i1];
+                    if (br == 1) {
+                        a[i0] = mk(a1.x * s1, a1.y * s1);
+                        a[i1] = mk((R)0, (R)0);
+                    } else if (br == 2) {
+                        a[i1] = mk(a0.x * s2, a0.y * s2);
+                        a[i0] = mk((R)0, (R)0);
+                    } else {
+                        a[i0] = mk(a0.x * s0g, a0.y * s0g);
+                        a[i1] = mk(a1.x * s0e, a1.y * s0e);
+                    }
+                }
             }
             __syncthreads();
         }
@@ -351,7 +377,10 @@ int run_trajectories(qf_sv *init, const qf_op *ops, uint64_t n_ops, uint64_t sho
             t.kind = o.kind == QF_OP_GATE ? T_GATE : T_COND;
             t.value = (uint8_t)(o.flags & 1);
             t.cbit = o.param;
-            for (int j = 0; j < 8; ++j) t.m[j] = b[0].m[j];
+            for (int j = 0; j < 8; ++j) {
+                t.m[j] = b[0].m[j];
+                t.mf[j] = (float)b[0].m[j];
+            }
             if (t.kind == T_GATE) {  // structured matrices: fewer floating-point operations per pair
                 const double *m = t.m;
                 if (o.gate == QF_GATE_X) t.kind = T_X;
