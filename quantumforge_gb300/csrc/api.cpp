@@ -3,6 +3,7 @@
 // (src/lib.rs:507-664, src/cuda.rs:3051-3104); all checks run before any
 // launch, and the device state is left untouched when a call is rejected.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -1286,10 +1287,39 @@ int lower_density_ops(uint32_t n, const qf_op *ops, uint64_t n_ops, std::vector<
     return close_run();
 }
 
+// Complex64: consecutive channels go through one fused sweep while their
+// (row, column) bit pairs and the low five column bits fit a 12-bit tile (the
+// single-channel kernel is HBM-bound there). Complex128 channels are bound by
+// the FP64 pipe, which fusing does not relieve: one kernel per channel, as for
+// a lone channel or a matrix under 3 qubits.
 int run_density_steps(qf_sv *sv, uint32_t n, const std::vector<DmStep> &steps, const qf_exec_opts *opts) {
-    for (const DmStep &st : steps) {
-        if (st.channel) QF_TRY(dm_channel(sv, n, st.q, st.coef));
-        else QF_TRY(execute_gates(sv, st.gates, opts));
+    for (size_t i = 0; i < steps.size();) {
+        if (!steps[i].channel) {
+            QF_TRY(execute_gates(sv, steps[i].gates, opts));
+            ++i;
+            continue;
+        }
+        uint64_t mask = 31;
+        std::vector<uint32_t> qs;
+        std::vector<std::array<double, 6>> cf;
+        size_t j = i;
+        while (j < steps.size() && steps[j].channel && qs.size() < 12 && n >= 3 && sv->dtype == QF_C64) {
+            const uint64_t m = mask | (1ULL << steps[j].q) | (1ULL << (n + steps[j].q));
+            if (__builtin_popcountll(m) > 12) break;
+            mask = m;
+            qs.push_back(steps[j].q);
+            std::array<double, 6> c;
+            std::copy(steps[j].coef, steps[j].coef + 6, c.begin());
+            cf.push_back(c);
+            ++j;
+        }
+        if (qs.size() >= 2) {
+            QF_TRY(dm_channels_fused(sv, n, qs.data(), reinterpret_cast<const double(*)[6]>(cf.data()), (uint32_t)qs.size()));
+            i = j;
+        } else {
+            QF_TRY(dm_channel(sv, n, steps[i].q, steps[i].coef));
+            ++i;
+        }
     }
     return QF_OK;
 }

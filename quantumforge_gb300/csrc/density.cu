@@ -136,6 +136,65 @@ __global__ void k_dm_mixed(C *__restrict__ v, uint32_t n) {
         v[i] = mk((R)((i >> n) == (i & cmask) ? d : 0.0), (R)0);
 }
 
+// Several local channels in one sweep: the matrix is walked in tiles of 2^k
+// entries whose bits are the low five column bits (coalesced 32-entry runs)
+// plus the (row, column) bit pairs of the channels; each CTA loads a tile to
+// shared memory, applies the channels in order and stores it back.
+constexpr int kMaxTileChannels = 12;
+struct ChannelTile {
+    uint32_t k;                       // tile bits
+    uint32_t n_hi;                    // tile bits above the low five
+    uint64_t outer_mask;              // bits enumerated by the tile index
+    uint64_t hi_bits[kMaxTileChannels * 2];
+    uint32_t n_ch;
+    uint8_t lc[kMaxTileChannels], lr[kMaxTileChannels], shape[kMaxTileChannels];
+    double coef[kMaxTileChannels][6];
+};
+
+template <typename C>
+__global__ void __launch_bounds__(256) k_dm_channel_tile(C *__restrict__ v, uint64_t n_tiles, const ChannelTile ct) {
+    using R = typename Real<C>::T;
+    extern __shared__ __align__(16) unsigned char dm_smem[];
+    C *s = reinterpret_cast<C *>(dm_smem);
+    uint64_t *hi_off = reinterpret_cast<uint64_t *>(dm_smem + (sizeof(C) << ct.k));
+    const uint32_t T = 1u << ct.k;
+    for (uint32_t h = threadIdx.x; h < (1u << ct.n_hi); h += blockDim.x) {
+        uint64_t off = 0;
+        for (uint32_t r = 0; r < ct.n_hi; ++r)
+            if ((h >> r) & 1u) off |= ct.hi_bits[r];
+        hi_off[h] = off;
+    }
+    __syncthreads();
+    for (uint64_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+        const uint64_t base = deposit(t, ct.outer_mask);
+        for (uint32_t j = threadIdx.x; j < T; j += blockDim.x) s[j] = v[base | hi_off[j >> 5] | (j & 31u)];
+        __syncthreads();
+        for (uint32_t c = 0; c < ct.n_ch; ++c) {
+            const uint32_t lc = ct.lc[c], lr = ct.lr[c], lo = min(lc, lr), hi = max(lc, lr);
+            const uint32_t cm = 1u << lc, rm = 1u << lr;
+            const R a = (R)ct.coef[c][0], b = (R)ct.coef[c][1], cc = (R)ct.coef[c][2], d = (R)ct.coef[c][3];
+            const R e = (R)ct.coef[c][4], f = (R)ct.coef[c][5];
+            const int shape = ct.shape[c];
+            for (uint32_t g = threadIdx.x; g < (T >> 2); g += blockDim.x) {
+                uint32_t i = g;
+                i = ((i >> lo) << (lo + 1)) | (i & ((1u << lo) - 1u));
+                i = ((i >> hi) << (hi + 1)) | (i & ((1u << hi) - 1u));
+                const C x01 = s[i | cm], x10 = s[i | rm];
+                if (shape != 2) {
+                    const C x00 = s[i], x11 = s[i | rm | cm];
+                    s[i] = mk(a * x00.x + b * x11.x, a * x00.y + b * x11.y);
+                    s[i | rm | cm] = mk(cc * x00.x + d * x11.x, cc * x00.y + d * x11.y);
+                }
+                s[i | cm] = mk(e * x01.x, e * x01.y);
+                s[i | rm] = mk(f * x10.x, f * x10.y);
+            }
+            __syncthreads();
+        }
+        for (uint32_t j = threadIdx.x; j < T; j += blockDim.x) v[base | hi_off[j >> 5] | (j & 31u)] = s[j];
+        __syncthreads();
+    }
+}
+
 int grid_for(const qf_ctx *ctx, uint64_t work) {
     return (int)std::max<uint64_t>(1, std::min<uint64_t>((work + 255) / 256, (uint64_t)ctx->sm_count * 8));
 }
@@ -158,6 +217,48 @@ template <typename C> void launch_channel_shape(qf_sv *sv, uint32_t n, uint32_t 
 int dm_channel(qf_sv *sv, uint32_t n, uint32_t q, const double coef[6]) {
     if (sv->dtype == QF_C64) launch_channel_shape<float2>(sv, n, q, coef);
     else launch_channel_shape<double2>(sv, n, q, coef);
+    QF_CUDA(cudaGetLastError());
+    return QF_OK;
+}
+
+int dm_channels_fused(qf_sv *sv, uint32_t n, const uint32_t *qs, const double (*coefs)[6], uint32_t count) {
+    qf_ctx *ctx = sv->ctx;
+    if (count == 0) return QF_OK;
+    if (count > (uint32_t)kMaxTileChannels || 2 * n < 5) return fail(QF_ERR_INVALID_ARGUMENT, "channel group too large");
+    uint64_t tile_mask = 31;  // the low five column bits
+    for (uint32_t c = 0; c < count; ++c) tile_mask |= (1ULL << qs[c]) | (1ULL << (n + qs[c]));
+    ChannelTile ct{};
+    ct.k = (uint32_t)__builtin_popcountll(tile_mask);
+    if (ct.k > 12) return fail(QF_ERR_INVALID_ARGUMENT, "channel group needs %u tile bits", ct.k);
+    ct.n_hi = ct.k - 5;
+    const uint64_t all = (2 * n >= 64) ? ~0ULL : ((1ULL << (2 * n)) - 1);
+    ct.outer_mask = all & ~tile_mask;
+    uint32_t pos[64];
+    uint32_t local = 0;
+    for (uint32_t b = 0; b < 2 * n; ++b)
+        if ((tile_mask >> b) & 1ULL) {
+            pos[b] = local;
+            if (local >= 5) ct.hi_bits[local - 5] = 1ULL << b;
+            ++local;
+        }
+    ct.n_ch = count;
+    for (uint32_t c = 0; c < count; ++c) {
+        ct.lc[c] = (uint8_t)pos[qs[c]];
+        ct.lr[c] = (uint8_t)pos[n + qs[c]];
+        const double *k = coefs[c];
+        ct.shape[c] = (k[0] == 1.0 && k[1] == 0.0 && k[2] == 0.0 && k[3] == 1.0) ? 2 : 0;
+        for (int j = 0; j < 6; ++j) ct.coef[c][j] = k[j];
+    }
+    const uint64_t n_tiles = 1ULL << (2 * n - ct.k);
+    const size_t smem = (sv->dtype == QF_C64 ? 8u : 16u) * (size_t(1) << ct.k) + sizeof(uint64_t) * (size_t(1) << ct.n_hi);
+    const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(n_tiles, (uint64_t)ctx->sm_count * 8));
+    if (sv->dtype == QF_C64) {
+        QF_CUDA(cudaFuncSetAttribute(k_dm_channel_tile<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_dm_channel_tile<float2><<<grid, 256, smem, ctx->stream>>>(static_cast<float2 *>(sv->d), n_tiles, ct);
+    } else {
+        QF_CUDA(cudaFuncSetAttribute(k_dm_channel_tile<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_dm_channel_tile<double2><<<grid, 256, smem, ctx->stream>>>(static_cast<double2 *>(sv->d), n_tiles, ct);
+    }
     QF_CUDA(cudaGetLastError());
     return QF_OK;
 }

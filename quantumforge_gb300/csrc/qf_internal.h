@@ -304,6 +304,9 @@ int batch_measure(qf_sv *sv, uint32_t n, uint64_t B, uint32_t q, const double *u
 // v00' = a v00 + b v11, v11' = c v00 + d v11, v01' = e v01, v10' = f v10 on
 // the bit pair (row n + q, column q).
 int dm_channel(qf_sv *sv, uint32_t n, uint32_t q, const double coef[6]);
+// `count` consecutive channels in one sweep; their bits plus the low five
+// column bits must span at most 12 bits (2n >= 5).
+int dm_channels_fused(qf_sv *sv, uint32_t n, const uint32_t *qs, const double (*coefs)[6], uint32_t count);
 // mode 0 trace (out[0] re, out[1] im), 1 P(1) of q, 2 <Z_q>, 3 <X_q>, 4 <Y_q>.
 int dm_diag_reduce(qf_sv *sv, uint32_t n, uint32_t q, int mode, double out[2]);
 int dm_diagonal(qf_sv *sv, uint32_t n, double *d_out);
