@@ -149,6 +149,7 @@ struct ChannelTile {
     uint32_t n_ch;
     uint8_t lc[kMaxTileChannels], lr[kMaxTileChannels], shape[kMaxTileChannels];
     double coef[kMaxTileChannels][6];
+    float coef_f[kMaxTileChannels][6];  // the same in f32: no f64 -> f32 conversion per tile for complex64
 };
 
 template <typename C>
@@ -172,8 +173,14 @@ __global__ void __launch_bounds__(256) k_dm_channel_tile(C *__restrict__ v, uint
         for (uint32_t c = 0; c < ct.n_ch; ++c) {
             const uint32_t lc = ct.lc[c], lr = ct.lr[c], lo = min(lc, lr), hi = max(lc, lr);
             const uint32_t cm = 1u << lc, rm = 1u << lr;
-            const R a = (R)ct.coef[c][0], b = (R)ct.coef[c][1], cc = (R)ct.coef[c][2], d = (R)ct.coef[c][3];
-            const R e = (R)ct.coef[c][4], f = (R)ct.coef[c][5];
+            R a, b, cc, d, e, f;
+            if (sizeof(R) == 4) {
+                a = (R)ct.coef_f[c][0], b = (R)ct.coef_f[c][1], cc = (R)ct.coef_f[c][2], d = (R)ct.coef_f[c][3];
+                e = (R)ct.coef_f[c][4], f = (R)ct.coef_f[c][5];
+            } else {
+                a = (R)ct.coef[c][0], b = (R)ct.coef[c][1], cc = (R)ct.coef[c][2], d = (R)ct.coef[c][3];
+                e = (R)ct.coef[c][4], f = (R)ct.coef[c][5];
+            }
             const int shape = ct.shape[c];
             for (uint32_t g = threadIdx.x; g < (T >> 2); g += blockDim.x) {
                 uint32_t i = g;
@@ -247,7 +254,10 @@ int dm_channels_fused(qf_sv *sv, uint32_t n, const uint32_t *qs, const double (*
         ct.lr[c] = (uint8_t)pos[n + qs[c]];
         const double *k = coefs[c];
         ct.shape[c] = (k[0] == 1.0 && k[1] == 0.0 && k[2] == 0.0 && k[3] == 1.0) ? 2 : 0;
-        for (int j = 0; j < 6; ++j) ct.coef[c][j] = k[j];
+        for (int j = 0; j < 6; ++j) {
+            ct.coef[c][j] = k[j];
+            ct.coef_f[c][j] = (float)k[j];
+        }
     }
     const uint64_t n_tiles = 1ULL << (2 * n - ct.k);
     const size_t smem = (sv->dtype == QF_C64 ? 8u : 16u) * (size_t(1) << ct.k) + sizeof(uint64_t) * (size_t(1) << ct.n_hi);

@@ -69,10 +69,10 @@ template <typename R> __device__ __forceinline__ R warp_sum_r(R v) {
 // by thread 0 alone in f64 with round-to-nearest operations and broadcast
 // through shared memory: FP64 issues at a small fraction of FP32 on GB300, so
 // the other 255 threads never touch it for a complex64 state.
-struct Decision {
+template <typename R> struct Decision {
     int branch;  // measurement outcome / Kraus branch / Pauli index (-1: none)
     int fault;
-    double s[4];
+    R s[4];      // scales, already in the state's precision (no per-thread f64 -> f32 conversion)
 };
 
 template <typename C>
@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(256) k_trajectories(const C *__restrict__ init
     extern __shared__ __align__(16) unsigned char traj_smem[];
     C *a = reinterpret_cast<C *>(traj_smem);
     __shared__ R wred[2][8];
-    __shared__ Decision dec;
+    __shared__ Decision<R> dec;
     const uint32_t dim = 1u << n, half = dim >> 1, quarter = dim >> 2;
     const unsigned tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
     for (uint64_t s = blockIdx.x; s < shots; s += gridDim.x) {
@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(256) k_trajectories(const C *__restrict__ init
                     p_one += (double)wred[0][w];
                     norm += (double)wred[1][w];
                 }
-                Decision d{-1, 0, {0.0, 0.0, 0.0, 0.0}};
+                Decision<R> d{-1, 0, {(R)0, (R)0, (R)0, (R)0}};
                 if (kind == T_MEASURE) {  // StateVector::measure, src/lib.rs:1321-1351
                     double p = p_one;
                     if (rel_norm && norm > 0.0) p = __ddiv_rn(p_one, norm);
@@ -226,7 +226,7 @@ __global__ void __launch_bounds__(256) k_trajectories(const C *__restrict__ init
                     if (fabs(u - p) < tie_eps) ++my_ties;
                     const double prob = d.branch ? p : __dsub_rn(1.0, p);
                     if (prob <= kEps) d.fault = 1;
-                    else d.s[0] = 1.0 / sqrt(prob);  // one rounding more than the reference's division
+                    else d.s[0] = (R)(1.0 / sqrt(prob));  // one rounding more than the reference's division
                 } else if (kind == T_AD || kind == T_PD) {  // src/lib.rs:1383-1438
                     const double g = op.m[0];
                     if (!isfinite(norm) || norm <= kEps) {
@@ -242,9 +242,9 @@ __global__ void __launch_bounds__(256) k_trajectories(const C *__restrict__ init
                             d.fault = 1;
                         } else {
                             const double inv = 1.0 / sqrt(bn);
-                            d.s[0] = inv;
-                            d.s[1] = op.m[2] * inv;  // jump
-                            d.s[2] = op.m[3] * inv;  // no jump, excited part
+                            d.s[0] = (R)inv;
+                            d.s[1] = (R)(op.m[2] * inv);  // jump
+                            d.s[2] = (R)(op.m[3] * inv);  // no jump, excited part
                         }
                     }
                 } else {  // T_TH, src/lib.rs:1440-1503
@@ -264,10 +264,10 @@ __global__ void __launch_bounds__(256) k_trajectories(const C *__restrict__ init
                             d.fault = 1;
                         } else {
                             const double inv = 1.0 / sqrt(bn);
-                            d.s[0] = op.m[2] * inv;  // down
-                            d.s[1] = op.m[4] * inv;  // up
-                            d.s[2] = op.m[5] * inv;  // stay, ground part
-                            d.s[3] = op.m[3] * inv;  // stay, excited part
+                            d.s[0] = (R)(op.m[2] * inv);  // down
+                            d.s[1] = (R)(op.m[4] * inv);  // up
+                            d.s[2] = (R)(op.m[5] * inv);  // stay, ground part
+                            d.s[3] = (R)(op.m[3] * inv);  // stay, excited part
                         }
                     }
                 }
@@ -278,14 +278,14 @@ __global__ void __launch_bounds__(256) k_trajectories(const C *__restrict__ init
             if (dec.fault) return;  // uniform across the CTA
             const int br = dec.branch;
             if (kind == T_MEASURE) {
-                const R inv = (R)dec.s[0];
+                const R inv = dec.s[0];
                 for (uint32_t i = tid; i < dim; i += nt) {
                     const C v = a[i];
                     a[i] = ((int)((i >> q) & 1u) == br) ? mk(v.x * inv, v.y * inv) : mk((R)0, (R)0);
                 }
                 reg = (reg & ~(1ULL << op.cbit)) | ((uint64_t)br << op.cbit);
             } else if (kind == T_AD || kind == T_PD) {
-                const R inv = (R)dec.s[0], s_jump = (R)dec.s[1], s_exc = (R)dec.s[2];
+                const R inv = dec.s[0], s_jump = dec.s[1], s_exc = dec.s[2];
                 for (uint32_t p = tid; p < half; p += nt) {
                     const uint32_t i0 = ins0(p, q), i1 = i0 | qm;
                     const C a0 = a[i0], a1 = a[i1];
@@ -303,7 +303,7 @@ __global__ void __launch_bounds__(256) k_trajectories(const C *__restrict__ init
                     }
                 }
             } else {
-                const R s1 = (R)dec.s[0], s2 = (R)dec.s[1], s0g = (R)dec.s[2], s0e = (R)dec.s[3];
+                const R s1 = dec.s[0], s2 = dec.s[1], s0g = dec.s[2], s0e = dec.s[3];
                 for (uint32_t p = tid; p < half; p += nt) {
                     const uint32_t i0 = ins0(p, q), i1 = i0 | qm;
                     const C a0 = a[i0], a1 = a[i1];
