@@ -776,10 +776,20 @@ def extras_only(args):
     wanted = set(args.extras.split(","))
     cpu = not args.no_cpu_baseline
     extra = {}
+    if "vqe24" in wanted:
+        extra["vqe24"] = vqe_gradients(backend)
+    if "qaoa4096" in wanted:
+        extra["qaoa4096"] = qaoa_batch(backend, cpu=cpu, count=args.qaoa_instances)
+    if "shots20" in wanted:
+        extra["shots20"] = shots20(backend, cpu=cpu)
+    if "shots_ff" in wanted:
+        extra["shots_ff"] = shots_feedforward(backend, cpu=cpu)
     if "density14" in wanted:
         extra["density14"] = density14(backend, cpu=cpu, n=args.density_qubits)
     if "noise_shots" in wanted:
         extra["noise_shots"] = noise_shots(backend, cpu=cpu, shots=args.noise_shots)
+    if "vqe32" in wanted:
+        extra["vqe32"] = vqe32_checkpointed(backend, args.vqe_qubits)
     print(json.dumps({"extra": extra}), flush=True)
     backend.close()
 

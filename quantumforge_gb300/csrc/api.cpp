@@ -88,7 +88,7 @@ int check_dtype(int dtype) {
 }
 
 // StateVector::zero_with_memory_budget size checks (src/lib.rs:940-966).
-int alloc_state(qf_ctx *ctx, uint32_t qubits, int dtype, uint64_t budget, qf_sv **out) {
+int alloc_state(qf_ctx *ctx, uint32_t qubits, int dtype, uint64_t budget, qf_sv **out, bool fill = true) {
     QF_TRY(check_dtype(dtype));
     if (qubits == 0) return fail(QF_ERR_ZERO_QUBITS, "a state vector must contain at least one qubit");
     if (qubits > 40) return fail(QF_ERR_SIMULATION_SIZE_OVERFLOW, "dense simulation size exceeds the supported addressable range");
@@ -109,7 +109,7 @@ int alloc_state(qf_ctx *ctx, uint32_t qubits, int dtype, uint64_t budget, qf_sv 
         return fail(QF_ERR_MEMORY_ALLOCATION_FAILED, "could not reserve memory for the dense quantum state (%llu bytes)",
                     (unsigned long long)bytes);
     }
-    int st = fill_zero_state(sv);
+    int st = fill ? fill_zero_state(sv) : QF_OK;
     if (st) {
         cudaFree(sv->d);
         delete sv;
@@ -125,6 +125,33 @@ void free_state(qf_sv *sv) {
     if (sv->ctx) sv->ctx->states.erase(sv);
     if (sv->d) cudaFree(sv->d);
     delete sv;
+}
+
+// Checkpoint states for the adjoint: reused across gradients of the same
+// shape instead of a cudaMalloc (and the implicit synchronisation of its
+// cudaFree) per segment per call; at most kCkptPoolBytes stay cached.
+constexpr uint64_t kCkptPoolBytes = 16ULL << 30;
+
+int take_checkpoint(qf_ctx *ctx, uint32_t n, int dtype, qf_sv **out) {
+    for (size_t i = ctx->ckpt_pool.size(); i-- > 0;) {
+        qf_sv *c = ctx->ckpt_pool[i];
+        if (c->n == n && c->dtype == dtype) {
+            ctx->ckpt_pool.erase(ctx->ckpt_pool.begin() + (ptrdiff_t)i);
+            *out = c;
+            return QF_OK;
+        }
+    }
+    return alloc_state(ctx, n, dtype, 0, out, false);  // overwritten by the checkpoint copy
+}
+
+void release_checkpoint(qf_ctx *ctx, qf_sv *c) {
+    uint64_t held = 0;
+    for (qf_sv *x : ctx->ckpt_pool) held += x->bytes();
+    if (held + c->bytes() <= kCkptPoolBytes) {
+        ctx->ckpt_pool.push_back(c);
+        return;
+    }
+    free_state(c);
 }
 
 // A cached context-owned state of the requested shape (whole-circuit calls).
@@ -217,11 +244,12 @@ int adjoint_device(qf_ctx *ctx, uint32_t n, const std::vector<BGate> &gates, con
     QF_TRY(scratch_state(ctx, &ctx->scratch_sv2, n, dtype, &lam));
     std::vector<qf_sv *> ckpt;  // ckpt[s] = psi at the start of segment s+1
     struct Guard {
+        qf_ctx *ctx;
         std::vector<qf_sv *> *v;
         ~Guard() {
-            for (qf_sv *s : *v) free_state(s);
+            for (qf_sv *s : *v) release_checkpoint(ctx, s);
         }
-    } guard{&ckpt};
+    } guard{ctx, &ckpt};
     PlanOpts po;
     default_tiling(n, dtype, o->exec.tile_qubits, &po.tile_qubits, &po.low_qubits);
     QF_TRY(fill_zero_state(psi));
@@ -234,7 +262,7 @@ int adjoint_device(qf_ctx *ctx, uint32_t n, const std::vector<BGate> &gates, con
         QF_TRY(run_plan(psi, plan, o->exec.flags));
         if (s + 1 < n_seg) {
             qf_sv *c;
-            QF_TRY(alloc_state(ctx, n, dtype, 0, &c));
+            QF_TRY(take_checkpoint(ctx, n, dtype, &c));
             ckpt.push_back(c);
             QF_CUDA(cudaMemcpyAsync(c->d, psi->d, psi->bytes(), cudaMemcpyDeviceToDevice, ctx->stream));
         }
@@ -242,32 +270,38 @@ int adjoint_device(qf_ctx *ctx, uint32_t n, const std::vector<BGate> &gates, con
     double e_val = 0.0;
     QF_TRY(pauli_apply(psi, lam, terms, n_terms, &e_val));
     if (energy) *energy = e_val;
-    std::vector<double> g(n_params, 0.0);
+    // every backward segment is planned first, then launched back to back: the
+    // overlap slots of all segments land in one device buffer that is read once
+    std::vector<Plan> bplans(n_seg);
+    std::vector<size_t> slot_off(n_seg, 0);
+    size_t total_slots = 0;
+    po.backward = true;
+    po.merge_1q = true;
     for (size_t s = n_seg; s-- > 0;) {
         const size_t b = seg_begin[s], e = s + 1 < n_seg ? seg_begin[s + 1] : gates.size();
         std::vector<BGate> seg(gates.begin() + b, gates.begin() + e);
-        Plan plan;
-        po.backward = true;
-        po.merge_1q = true;
-        QF_TRY(plan_passes(n, seg, po, plan));
-        if (plan.n_slots) {
-            double *d_sums;
-            const size_t bytes = sizeof(double) * plan.n_slots;
-            if (bytes > kSmallBytes) QF_TRY(ensure_device(&ctx->ws_tree, &ctx->ws_tree_bytes, bytes));
-            d_sums = bytes > kSmallBytes ? static_cast<double *>(ctx->ws_tree) : ctx->d_small;
-            QF_CUDA(cudaMemsetAsync(d_sums, 0, bytes, ctx->stream));
-            QF_TRY(run_plan_dual(psi, lam, plan, d_sums, o->exec.flags));
-            std::vector<double> sums(plan.n_slots);
-            QF_CUDA(cudaMemcpyAsync(sums.data(), d_sums, bytes, cudaMemcpyDeviceToHost, ctx->stream));
-            QF_CUDA(cudaStreamSynchronize(ctx->stream));
-            for (uint32_t k = 0; k < plan.n_slots; ++k) g[(size_t)plan.slot_param[k]] += sums[k];
-        } else {
-            QF_TRY(run_plan_dual(psi, lam, plan, nullptr, o->exec.flags));
-        }
+        QF_TRY(plan_passes(n, seg, po, bplans[s]));
+        slot_off[s] = total_slots;
+        total_slots += bplans[s].n_slots;
+    }
+    double *d_sums = nullptr;
+    const size_t bytes = sizeof(double) * total_slots;
+    if (total_slots) {
+        if (bytes > kSmallBytes) QF_TRY(ensure_device(&ctx->ws_tree, &ctx->ws_tree_bytes, bytes));
+        d_sums = bytes > kSmallBytes ? static_cast<double *>(ctx->ws_tree) : ctx->d_small;
+        QF_CUDA(cudaMemsetAsync(d_sums, 0, bytes, ctx->stream));
+    }
+    for (size_t s = n_seg; s-- > 0;) {
+        QF_TRY(run_plan_dual(psi, lam, bplans[s], bplans[s].n_slots ? d_sums + slot_off[s] : nullptr, o->exec.flags));
         if (s > 0 && !ckpt.empty())
             QF_CUDA(cudaMemcpyAsync(psi->d, ckpt[s - 1]->d, psi->bytes(), cudaMemcpyDeviceToDevice, ctx->stream));
     }
+    std::vector<double> sums(total_slots);
+    if (total_slots) QF_CUDA(cudaMemcpyAsync(sums.data(), d_sums, bytes, cudaMemcpyDeviceToHost, ctx->stream));
     QF_CUDA(cudaStreamSynchronize(ctx->stream));
+    std::vector<double> g(n_params, 0.0);
+    for (size_t s = n_seg; s-- > 0;)
+        for (uint32_t k = 0; k < bplans[s].n_slots; ++k) g[(size_t)bplans[s].slot_param[k]] += sums[slot_off[s] + k];
     std::copy(g.begin(), g.end(), grad);
     return QF_OK;
 }
@@ -777,6 +811,8 @@ int qf_ctx_destroy(qf_ctx *ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     free_state(ctx->scratch_sv);
     free_state(ctx->scratch_sv2);
+    for (qf_sv *c : ctx->ckpt_pool) free_state(c);
+    ctx->ckpt_pool.clear();
     // states the caller still holds: free their memory, keep the handle as an
     // orphan that qf_sv_destroy can release without the context
     for (qf_sv *sv : ctx->states) {

@@ -27,6 +27,7 @@ struct qf_ctx {
     qf_sv *scratch_sv = nullptr;  // cached state for whole-circuit calls
     qf_sv *scratch_sv2 = nullptr; // cached second state (adjoint costate)
     std::set<qf_sv *> states;     // live states; orphaned (memory freed) when the context is destroyed
+    std::vector<qf_sv *> ckpt_pool;  // adjoint checkpoint states kept for the next gradient (bounded bytes)
 };
 constexpr size_t kSmallBytes = 64 * 1024;
 

@@ -19,17 +19,23 @@ constexpr int kRedThreads = 256;
 constexpr int kRedBlocks = 512;  // power of two: the <Z> kernel reads index bits from the thread id
 
 // Sum `n_vals` values per block over `n_blocks` blocks, in block order.
+// out[v] = sum over blocks of partials[b * n_vals + v]: one block, every
+// thread adds a fixed strided subset, then a block reduction (the same order
+// on every run, so results are reproducible).
 __global__ void k_final_sum(const double *__restrict__ partials, uint32_t n_blocks, uint32_t n_vals,
                             double *__restrict__ out) {
-    for (uint32_t v = threadIdx.x; v < n_vals; v += blockDim.x) {
+    __shared__ double red[32];
+    for (uint32_t v = 0; v < n_vals; ++v) {
         double s = 0.0;
-        for (uint32_t b = 0; b < n_blocks; ++b) s += partials[(size_t)b * n_vals + v];
-        out[v] = s;
+        for (uint32_t b = threadIdx.x; b < n_blocks; b += blockDim.x) s += partials[(size_t)b * n_vals + v];
+        s = block_sum(s, red);
+        if (threadIdx.x == 0) out[v] = s;
+        __syncthreads();
     }
 }
 
 static int finish_sum(qf_ctx *ctx, const double *d_partials, uint32_t n_blocks, uint32_t n_vals, double *host_out) {
-    k_final_sum<<<1, 128, 0, ctx->stream>>>(d_partials, n_blocks, n_vals, ctx->d_small);
+    k_final_sum<<<1, 256, 0, ctx->stream>>>(d_partials, n_blocks, n_vals, ctx->d_small);
     QF_CUDA(cudaGetLastError());
     QF_CUDA(cudaMemcpyAsync(ctx->h_small, ctx->d_small, sizeof(double) * n_vals, cudaMemcpyDeviceToHost, ctx->stream));
     QF_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -957,7 +963,7 @@ int run_pauli(qf_sv *psi, qf_sv *lam, PauliPlan &plan, bool apply, double out[2]
     // expectation: every slice; apply: only the slice carrying <psi|lambda>
     const size_t first = apply ? slice - 1 : 0;
     const uint32_t nblk = (uint32_t)(grid * (slice - first));
-    k_final_sum<<<1, 128, 0, ctx->stream>>>(partials + 2 * grid * first, nblk, 2, ctx->d_small);
+    k_final_sum<<<1, 256, 0, ctx->stream>>>(partials + 2 * grid * first, nblk, 2, ctx->d_small);
     QF_CUDA(cudaGetLastError());
     QF_CUDA(cudaMemcpyAsync(ctx->h_small, ctx->d_small, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     QF_CUDA(cudaStreamSynchronize(ctx->stream));
