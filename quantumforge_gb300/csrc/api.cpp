@@ -252,6 +252,24 @@ int adjoint_device(qf_ctx *ctx, uint32_t n, const std::vector<BGate> &gates, con
     } guard{ctx, &ckpt};
     PlanOpts po;
     default_tiling(n, dtype, o->exec.tile_qubits, &po.tile_qubits, &po.low_qubits);
+    // every backward segment is planned before anything launches, then run back
+    // to back: the overlap slots of all segments land in one device buffer that
+    // is read once at the end
+    std::vector<Plan> bplans(n_seg);
+    std::vector<size_t> slot_off(n_seg, 0);
+    size_t total_slots = 0;
+    {
+        PlanOpts bo = po;
+        bo.backward = true;
+        bo.merge_1q = true;
+        for (size_t s = n_seg; s-- > 0;) {
+            const size_t b = seg_begin[s], e = s + 1 < n_seg ? seg_begin[s + 1] : gates.size();
+            std::vector<BGate> seg(gates.begin() + b, gates.begin() + e);
+            QF_TRY(plan_passes(n, seg, bo, bplans[s]));
+            slot_off[s] = total_slots;
+            total_slots += bplans[s].n_slots;
+        }
+    }
     QF_TRY(fill_zero_state(psi));
     for (size_t s = 0; s < n_seg; ++s) {
         const size_t b = seg_begin[s], e = s + 1 < n_seg ? seg_begin[s + 1] : gates.size();
@@ -270,20 +288,6 @@ int adjoint_device(qf_ctx *ctx, uint32_t n, const std::vector<BGate> &gates, con
     double e_val = 0.0;
     QF_TRY(pauli_apply(psi, lam, terms, n_terms, &e_val));
     if (energy) *energy = e_val;
-    // every backward segment is planned first, then launched back to back: the
-    // overlap slots of all segments land in one device buffer that is read once
-    std::vector<Plan> bplans(n_seg);
-    std::vector<size_t> slot_off(n_seg, 0);
-    size_t total_slots = 0;
-    po.backward = true;
-    po.merge_1q = true;
-    for (size_t s = n_seg; s-- > 0;) {
-        const size_t b = seg_begin[s], e = s + 1 < n_seg ? seg_begin[s + 1] : gates.size();
-        std::vector<BGate> seg(gates.begin() + b, gates.begin() + e);
-        QF_TRY(plan_passes(n, seg, po, bplans[s]));
-        slot_off[s] = total_slots;
-        total_slots += bplans[s].n_slots;
-    }
     double *d_sums = nullptr;
     const size_t bytes = sizeof(double) * total_slots;
     if (total_slots) {
