@@ -293,6 +293,15 @@ int qf_sv_expectation_pauli_sum(qf_sv *sv, const qf_pauli_term *terms, uint64_t 
  * (src/cuda.rs:1386-1457): draws one uniform from the SmallRng whose state is
  * *rng_state, collapses the state and returns the bit. */
 int qf_sv_measure(qf_sv *sv, uint32_t qubit, uint64_t *rng_state, uint8_t *outcome);
+/* StateVector::normalize (src/lib.rs:1005-1014): divide by sqrt(norm_sqr);
+ * QF_ERR_INVALID_PROBABILITY for a zero or non-finite norm. */
+int qf_sv_normalize(qf_sv *sv);
+/* StateVector::apply_channel_trajectory (src/lib.rs:1356-1506) on a resident
+ * state: `channel` is a QF_OP_CHANNEL record; one uniform is drawn from
+ * *rng_state (advanced) and the selected Kraus branch applied and
+ * renormalised. *branch_out (nullable): the branch taken (depolarizing: 0
+ * none, 1 X, 2 Y, 3 Z; damping: 1 jump, 0 none; thermal: 1 down, 2 up, 0 stay). */
+int qf_sv_apply_channel_trajectory(qf_sv *sv, const qf_op *channel, uint64_t *rng_state, int *branch_out);
 
 /* ---------------------------------------------------------------------------
  * Whole-circuit calls with host buffers.

@@ -67,6 +67,8 @@ SIGNATURES = {
     "qf_run_circuit": [P, U32, C.c_int, P, U64, P, P, U64, P],
     "qf_run_shots": [P, U32, C.c_int, P, U64, P, U64, U64, F64, P, PU32, PU64, P],
     "qf_run_shots_with_noise": [P, U32, C.c_int, P, U64, P, U64, U64, F64, P, PU32, PU64, P],
+    "qf_sv_normalize": [P],
+    "qf_sv_apply_channel_trajectory": [P, P, PU64, C.POINTER(C.c_int)],
     "qf_batch_create": [P, U32, C.c_int, U64, C.POINTER(P)],
     "qf_batch_destroy": [P],
     "qf_batch_qubits": [P, PU32],

@@ -475,6 +475,23 @@ class StateVector:
         check(load().qf_sv_expectation_pauli_sum(self._h, ptr(t), len(t), ptr(out)))
         return complex(out[0], out[1])
 
+    def normalize(self) -> "StateVector":
+        """StateVector::normalize (src/lib.rs:1005-1014)."""
+        check(load().qf_sv_normalize(self._h))
+        return self
+
+    def apply_channel_trajectory(self, channel: "NoiseChannel", qubit: int, rng: SmallRng) -> int:
+        """StateVector::apply_channel_trajectory (src/lib.rs:1356-1506): one
+        draw from `rng`, the Kraus branch taken (returned) applied and renormalised."""
+        rec = _abi.ops_array([channel.record(int(qubit))])
+        st = C.c_uint64(rng.state)
+        br = C.c_int()
+        try:
+            check(load().qf_sv_apply_channel_trajectory(self._h, ptr(rec), C.byref(st), C.byref(br)))
+        finally:
+            rng.state = st.value
+        return br.value
+
     def measure(self, qubit: int, rng: SmallRng) -> int:
         """StateVector::measure (src/lib.rs:1321-1351), advancing `rng`."""
         st = C.c_uint64(rng.state)

@@ -1047,6 +1047,83 @@ int qf_sv_expectation_pauli_sum(qf_sv *sv, const qf_pauli_term *terms, uint64_t 
 
 // StateVector::measure (src/lib.rs:1321-1351) with the uniform drawn on the
 // host from the caller's SmallRng state, as CudaDeviceState::measure does.
+int qf_sv_normalize(qf_sv *sv) {
+    clear_error();
+    QF_TRY(check_sv(sv));
+    QF_TRY(bind_device(sv->ctx));
+    QF_TRY(normalize_state(sv));
+    QF_CUDA(cudaStreamSynchronize(sv->ctx->stream));
+    return QF_OK;
+}
+
+int qf_sv_apply_channel_trajectory(qf_sv *sv, const qf_op *channel, uint64_t *rng_state, int *branch_out) {
+    clear_error();
+    QF_TRY(check_sv(sv));
+    if (!channel || !rng_state) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    const qf_op &o = *channel;
+    if (o.kind != QF_OP_CHANNEL) return fail(QF_ERR_INVALID_ARGUMENT, "operation is not a noise channel");
+    const uint32_t q = o.q0;
+    if (q >= sv->n) return fail(QF_ERR_QUBIT_OUT_OF_RANGE, "qubit index %u is out of range for %u qubits", q, sv->n);
+    const double p = o.theta, eps = 2.220446049250313e-16;
+    if (!valid_probability(p)) return fail(QF_ERR_INVALID_PROBABILITY, "probability must be in [0, 1], got %g", p);
+    double gu = 0.0;
+    if (o.gate == QF_CHANNEL_THERMAL_DAMPING) {
+        const double beta = qf_op_aux(&o);
+        if (!std::isfinite(beta) || beta < 0.0) return fail(QF_ERR_INVALID_PROBABILITY, "probability must be in [0, 1], got %g", beta);
+        gu = p * std::exp(-beta);
+    } else if (o.gate > QF_CHANNEL_THERMAL_DAMPING) {
+        return fail(QF_ERR_INVALID_ARGUMENT, "unknown noise channel %u", (unsigned)o.gate);
+    }
+    QF_TRY(bind_device(sv->ctx));
+    int branch = 0;
+    BGate m;
+    bool apply = true;
+    if (o.gate == QF_CHANNEL_DEPOLARIZING) {
+        const double u = next_uniform(rng_state);
+        if (u >= 1.0 - p && p > 0.0) {
+            const double b = std::floor((u - (1.0 - p)) * (3.0 / p));
+            branch = 1 + (b >= 2.0 ? 2 : (int)b);
+            m.kind = BK_MAT1;
+            m.q0 = q;
+            QF_TRY(gate_matrix(branch == 1 ? QF_GATE_X : branch == 2 ? QF_GATE_Y : QF_GATE_Z, 0.0, m.m));
+            m.diag = matrix_is_diag(m.m);
+        } else {
+            apply = false;
+        }
+    } else {
+        double norm, p_one;
+        QF_TRY(reduce_norm_sqr(sv, &norm));
+        if (!std::isfinite(norm) || norm <= eps) return fail(QF_ERR_INVALID_PROBABILITY, "probability must be in [0, 1], got %g", norm);
+        QF_TRY(reduce_p_one(sv, q, &p_one));
+        double bn;
+        if (o.gate != QF_CHANNEL_THERMAL_DAMPING) {
+            const double jp = clamp01(p * p_one / norm);
+            branch = next_uniform(rng_state) < jp ? 1 : 0;
+            bn = branch ? p * p_one : norm - p * p_one;
+            if (!std::isfinite(bn) || bn <= eps) return fail(QF_ERR_INVALID_PROBABILITY, "probability must be in [0, 1], got %g", bn);
+            const double inv = 1.0 / std::sqrt(bn);
+            if (branch) m = o.gate == QF_CHANNEL_AMPLITUDE_DAMPING ? mat1(q, 0.0, std::sqrt(p) * inv, 0.0, 0.0)
+                                                                    : mat1(q, 0.0, 0.0, 0.0, std::sqrt(p) * inv);
+            else m = mat1(q, inv, 0.0, 0.0, std::sqrt(1.0 - p) * inv);
+        } else {
+            const double p1 = clamp01(p_one / norm), p0 = 1.0 - p1;
+            const double down = p1 * p, up = p0 * gu, stay = p0 * (1.0 - gu) + p1 * (1.0 - p);
+            const double u = next_uniform(rng_state);
+            branch = u < down ? 1 : (u < down + up ? 2 : 0);
+            bn = branch == 1 ? down : (branch == 2 ? up : stay);
+            if (!std::isfinite(bn) || bn <= eps) return fail(QF_ERR_INVALID_PROBABILITY, "probability must be in [0, 1], got %g", bn);
+            const double inv = 1.0 / std::sqrt(bn);
+            m = branch == 1 ? mat1(q, 0.0, std::sqrt(p) * inv, 0.0, 0.0)
+                : branch == 2 ? mat1(q, 0.0, 0.0, std::sqrt(gu) * inv, 0.0)
+                              : mat1(q, std::sqrt(1.0 - gu) * inv, 0.0, 0.0, std::sqrt(1.0 - p) * inv);
+        }
+    }
+    if (apply) QF_TRY(launch_gate1(sv, m));
+    QF_CUDA(cudaStreamSynchronize(sv->ctx->stream));
+    if (branch_out) *branch_out = branch;
+    return QF_OK;
+}
+
 int qf_sv_measure(qf_sv *sv, uint32_t qubit, uint64_t *rng_state, uint8_t *outcome) {
     clear_error();
     QF_TRY(check_sv(sv));

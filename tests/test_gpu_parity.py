@@ -683,3 +683,40 @@ def test_run_circuit_with_pinned_host_buffers(backend, dtype):
     _native.check(lib.qf_run_circuit(backend.handle, n, code, _native.ptr(ops), len(ops), _native.ptr(src),
                                      _native.ptr(out2), 2 << n, C.byref(eo)))
     assert np.array_equal(out2, h_out.numpy())
+
+
+# ---- single-state trajectory steps and normalisation on a resident state -----------
+@pytest.mark.parametrize("dtype,tol", [("c128", 1e-12), ("c64", 2e-6)])
+def test_apply_channel_trajectory_matches_the_oracle(backend, dtype, tol):  # src/lib.rs:1356-1506
+    r = np.random.default_rng(5)
+    n = 9
+    for trial in range(24):
+        v = r.normal(size=1 << n) + 1j * r.normal(size=1 << n)
+        v /= np.linalg.norm(v)
+        kind = trial % 4
+        p, beta, q, seed = float(r.uniform(0.05, 0.9)), float(r.uniform(0, 2)), int(r.integers(0, n)), int(r.integers(1, 1 << 40))
+        ch = NoiseChannel(kind, p, beta)
+        sv = StateVector.from_amplitudes(v, dtype=dtype, backend=backend)
+        rng = SmallRng.seeded(seed)
+        sv.apply_channel_trajectory(ch, q, rng)
+        a = v.copy()
+        orng = O.Rng(seed)
+        O.channel_trajectory(a, kind, p, q, orng, beta)
+        assert rng.state == orng.state.value
+        assert close(sv.amplitudes(), a, tol), (trial, kind)
+    with pytest.raises(QuantumError) as e:
+        sv.apply_channel_trajectory(NoiseChannel.Depolarizing(1.5), 0, SmallRng.seeded(1))
+    assert e.value.kind == "InvalidProbability"
+    with pytest.raises(QuantumError) as e:
+        sv.apply_channel_trajectory(NoiseChannel.Depolarizing(0.1), n, SmallRng.seeded(1))
+    assert e.value.kind == "QubitOutOfRange"
+
+
+def test_normalize_divides_by_the_norm(backend):  # src/lib.rs:1005-1014
+    v = 3.0 * (np.arange(16) + 1j)
+    sv = StateVector.from_amplitudes(v, backend=backend)
+    sv.normalize()
+    assert close(sv.amplitudes(), v / np.sqrt(np.vdot(v, v).real), 1e-15)
+    with pytest.raises(QuantumError) as e:
+        StateVector.from_amplitudes(np.zeros(4, complex), backend=backend).normalize()
+    assert e.value.kind == "InvalidProbability"
