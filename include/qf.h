@@ -439,6 +439,37 @@ int qf_run_density_circuit(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op 
                            const double *in_entries, double *out_entries, uint64_t n_doubles,
                            const qf_exec_opts *opts);
 
+/* Finite-shot estimates (estimate_observable_shots, src/lib.rs:4806-4838):
+ * the parameterised state prepared, the measured basis rotated, `shots`
+ * single-qubit measurements of SmallRng::seeded(seed); *estimate = 2 p0 - 1
+ * with p0 the outcome-0 fraction (*successes). Draws within tie_eps of P(1)
+ * are counted in *n_ties.
+ * ParameterizedCircuit::expectation_with_inputs_shots (src/lib.rs:3361-3382). */
+int qf_expectation_shots(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops,
+                         const double *params, uint64_t n_params, const double *inputs, uint64_t n_inputs,
+                         int observable, uint32_t observable_qubit, uint64_t shots, uint64_t seed, double tie_eps,
+                         const qf_exec_opts *opts, double *estimate, uint64_t *successes, uint64_t *n_ties);
+/* parameter_shift_gradient_with_inputs_shots (src/lib.rs:3428-3479). */
+int qf_parameter_shift_gradient_shots(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops,
+                                      const double *params, uint64_t n_params, const double *inputs, uint64_t n_inputs,
+                                      int observable, uint32_t observable_qubit, uint64_t shots, uint64_t seed,
+                                      double tie_eps, const qf_exec_opts *opts, double *gradient, uint64_t *n_ties);
+
+/* sample_expectation (src/lib.rs:4840-4850): `shots` Bernoulli draws of
+ * SmallRng::seeded(seed) at P(+1) = clamp((1 + expectation) / 2, 0, 1);
+ * *estimate = 2 (#positive) / shots - 1. Host arithmetic only; the density
+ * shot estimates (src/lib.rs:3188-3320) apply it to the exact density-matrix
+ * expectation. */
+int qf_sample_expectation(double expectation, uint64_t shots, uint64_t seed, double *estimate, uint64_t *positive);
+/* parameter_shift_gradient_density_with_inputs_shots (src/lib.rs:3268-3320):
+ * every rotation occurrence k shifted by +-pi/2 on the density matrix, each
+ * exact expectation passed through qf_sample_expectation with seeds
+ * seed + 2k and seed + 2k + 1. */
+int qf_parameter_shift_gradient_density_shots(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops,
+                                              const double *params, uint64_t n_params, const double *inputs,
+                                              uint64_t n_inputs, int observable, uint32_t observable_qubit,
+                                              uint64_t shots, uint64_t seed, const qf_exec_opts *opts, double *gradient);
+
 /* ---------------------------------------------------------------------------
  * Circuit formats — OpenQASM 2.0 import (qasm::parse_qasm, src/qasm.rs:73),
  * QASM export (qasm_export::export_qasm / export_qasm_with_qubits,

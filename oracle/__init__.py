@@ -64,6 +64,7 @@ def lib():
             "qfo_dm_probability_one": ([P, U32, U32, C.POINTER(F64)], C.c_int),
             "qfo_dm_measure": ([P, U32, U32, C.POINTER(U64), C.POINTER(C.c_uint8)], C.c_int),
             "qfo_run_density": ([P, U32, P, U64], C.c_int),
+            "qfo_estimate_observable_shots": ([P, U32, C.c_int, U32, U64, U64, C.POINTER(U64)], C.c_int),
             "qfo_parameter_shift_gradient": ([U32, P, U64, P, U64, P, U64, P, U64, P, C.c_int], C.c_int),
             "qfo_finite_difference_gradient": ([U32, P, U64, P, U64, P, U64, P, U64, F64, P, C.c_int], C.c_int),
             "qfo_adjoint_gradient_stored": ([U32, P, U64, P, U64, P, U64, P, U64, P], C.c_int),
@@ -281,6 +282,14 @@ def run_density(ops, n: int, rho=None) -> np.ndarray:
     rho = np.ascontiguousarray(rho, dtype=np.complex128).copy()
     _chk(lib().qfo_run_density(_p(rho), n, _p(ops), len(ops)))
     return rho
+
+
+def estimate_observable_shots(a, observable: int, q: int, shots: int, seed: int) -> int:
+    """Outcome-0 count of `shots` literal measurements (src/lib.rs:4806-4838)."""
+    a = np.ascontiguousarray(a, dtype=np.complex128)
+    ok = U64()
+    _chk(lib().qfo_estimate_observable_shots(_p(a), a.size.bit_length() - 1, observable, q, shots, seed, C.byref(ok)))
+    return ok.value
 
 
 # ---- gradients --------------------------------------------------------------

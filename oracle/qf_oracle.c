@@ -1260,3 +1260,32 @@ int qfo_run_density(double *rho, uint32_t n, const qf_op *ops, uint64_t n_ops) {
     }
     return 0;
 }
+
+/* estimate_observable_shots (src/lib.rs:4806-4838): rotate the measured basis
+ * (X: H; Y: Rz(-pi/2) then H), then `shots` measurements of `qubit` on clones
+ * of the state with one shared SmallRng; *successes counts outcome 0. */
+int qfo_estimate_observable_shots(const double *amps, uint32_t n, int observable, uint32_t qubit, uint64_t shots,
+                                  uint64_t seed, uint64_t *successes) {
+    if (shots == 0) return QF_ERR_INVALID_SHOT_COUNT;
+    const uint64_t dim = 1ULL << n;
+    double *state = (double *)malloc(sizeof(double) * 2 * dim);
+    double *sample = (double *)malloc(sizeof(double) * 2 * dim);
+    int st = (!state || !sample) ? QF_ERR_MEMORY_ALLOCATION_FAILED : 0;
+    if (!st) memcpy(state, amps, sizeof(double) * 2 * dim);
+    if (!st && observable == QF_PAULI_X) st = qfo_sv_apply(state, n, QF_GATE_H, 0.0, qubit, 0);
+    if (!st && observable == QF_PAULI_Y) {
+        st = qfo_sv_apply(state, n, QF_GATE_RZ, -1.5707963267948966, qubit, 0);
+        if (!st) st = qfo_sv_apply(state, n, QF_GATE_H, 0.0, qubit, 0);
+    }
+    uint64_t rng = qfo_rng_seeded(seed), ok = 0;
+    for (uint64_t s = 0; s < shots && !st; ++s) {
+        memcpy(sample, state, sizeof(double) * 2 * dim);
+        uint8_t o;
+        st = qfo_sv_measure(sample, n, qubit, &rng, &o);
+        if (!st && o == 0) ++ok;
+    }
+    free(state);
+    free(sample);
+    if (!st) *successes = ok;
+    return st;
+}

@@ -85,6 +85,10 @@ int qfo_dm_probability_one(const double *rho, uint32_t n, uint32_t q, double *ou
 int qfo_dm_measure(double *rho, uint32_t n, uint32_t q, uint64_t *rng_state, uint8_t *outcome);
 int qfo_run_density(double *rho, uint32_t n, const qf_op *ops, uint64_t n_ops);
 
+/* estimate_observable_shots (src/lib.rs:4806-4838): successes = outcome-0 count. */
+int qfo_estimate_observable_shots(const double *amps, uint32_t n, int observable, uint32_t qubit, uint64_t shots,
+                                  uint64_t seed, uint64_t *successes);
+
 /* Gradients. `terms` is the observable (one term = SingleQubitObservable). */
 int qfo_parameter_shift_gradient(uint32_t n, const qf_op *ops, uint64_t n_ops,
                                  const double *params, uint64_t n_params,

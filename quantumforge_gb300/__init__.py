@@ -17,6 +17,7 @@ from .core import (
     ParameterizedCircuit,
     PauliSum,
     RotationAxis,
+    ShotConfig,
     ShotResult,
     SingleQubitObservable,
     SmallRng,
@@ -26,12 +27,14 @@ from .core import (
     export_qasm,
     export_qasm_with_qubits,
     parse_qasm,
+    sample_expectation,
+    wilson_ci,
 )
 from . import gradients
 
 __all__ = [
     "Circuit", "CudaBackend", "DensityMatrix", "Gate", "NoiseChannel", "ParameterizedCircuit", "PauliSum", "QuantumError", "RotationAxis",
-    "ShotResult", "SingleQubitObservable", "SmallRng", "StateVector", "StateVectorBatch", "default_backend", "export_qasm",
-    "export_qasm_with_qubits", "parse_qasm", "gradients",
+    "ShotConfig", "ShotResult", "SingleQubitObservable", "SmallRng", "StateVector", "StateVectorBatch", "default_backend", "export_qasm",
+    "export_qasm_with_qubits", "parse_qasm", "sample_expectation", "wilson_ci", "gradients",
     "load_library",
 ]

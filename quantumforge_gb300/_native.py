@@ -96,6 +96,10 @@ SIGNATURES = {
     "qf_run_density_circuit": [P, U32, C.c_int, P, U64, P, P, U64, P],
     "qf_expectation_density": [P, U32, C.c_int, P, U64, P, U64, P, U64, C.c_int, U32, P, PF64],
     "qf_parameter_shift_gradient_density": [P, U32, C.c_int, P, U64, P, U64, P, U64, C.c_int, U32, P, PF64, P],
+    "qf_expectation_shots": [P, U32, C.c_int, P, U64, P, U64, P, U64, C.c_int, U32, U64, U64, F64, P, PF64, PU64, PU64],
+    "qf_parameter_shift_gradient_shots": [P, U32, C.c_int, P, U64, P, U64, P, U64, C.c_int, U32, U64, U64, F64, P, P, PU64],
+    "qf_sample_expectation": [F64, U64, U64, PF64, PU64],
+    "qf_parameter_shift_gradient_density_shots": [P, U32, C.c_int, P, U64, P, U64, P, U64, C.c_int, U32, U64, U64, P, P],
     "qf_parse_qasm": [C.c_char_p, U64, P, U64, PU64, PU32, PU32, PU64],
     "qf_circuit_from_json": [C.c_char_p, U64, P, U64, PU64, PU32, PU32],
     "qf_circuit_to_json": [P, U64, P, U64, PU64],

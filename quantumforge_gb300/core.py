@@ -919,6 +919,35 @@ class Circuit:
         return out[: int(shots)], width.value, ties.value
 
 
+@dataclass
+class ShotConfig:
+    """`ShotConfig` (src/lib.rs:3019-3026): shots per estimate and the seed."""
+
+    shots: int
+    seed: int = 0
+
+
+def wilson_ci(successes: int, shots: int, confidence: float = 0.95):
+    """Wilson score interval of a binomial proportion (src/lib.rs:2493-2513)."""
+    if shots == 0:
+        return 0.0, 1.0
+    n = float(shots)
+    p = successes / n
+    z = 2.576 if confidence >= 0.99 else 1.96 if confidence >= 0.95 else 1.645 if confidence >= 0.90 else 1.96
+    z2 = z * z
+    denom = 1.0 + z2 / n
+    center = (p + z2 / (2.0 * n)) / denom
+    half = (z / denom) * math.sqrt(p * (1.0 - p) / n + z2 / (4.0 * n * n))
+    return max(center - half, 0.0), min(center + half, 1.0)
+
+
+def sample_expectation(expectation: float, sampling: "ShotConfig") -> float:
+    """sample_expectation (src/lib.rs:4840-4850), computed by the library."""
+    v = C.c_double()
+    check(load().qf_sample_expectation(float(expectation), int(sampling.shots), int(sampling.seed), C.byref(v), None))
+    return v.value
+
+
 def parse_qasm_ops(source: str):
     """qf_parse_qasm: (op records, qubits declared, classical bits declared)."""
     data = source.encode()
@@ -1024,6 +1053,58 @@ class ParameterizedCircuit:
     def run(self, parameters, qubits: int, dtype="c128", backend=None, exec_opts=None) -> StateVector:
         return self.run_with_inputs([], parameters, qubits, dtype=dtype, backend=backend, exec_opts=exec_opts)
 
+    # ---- finite-shot estimates (src/lib.rs:3323-3479, 4806-4838) ----
+    def _shots_call(self, inputs, parameters, qubits, observable, observable_qubit, sampling, dtype, backend, exec_opts,
+                    tie_eps):
+        i, p = self._values(inputs, parameters)
+        be = backend or default_backend()
+        return i, p, be, self.ops(), _dtype_code(dtype), int(sampling.shots), int(sampling.seed)
+
+    def expectation_with_inputs_shots_with_ci(self, inputs, parameters, qubits: int, observable: int,
+                                              observable_qubit: int, sampling: "ShotConfig", dtype="c128",
+                                              backend=None, exec_opts=None, tie_eps: float = 0.0):
+        """(estimate, Wilson 95 % interval on the expectation) from `sampling`
+        shots (src/lib.rs:3384-3405)."""
+        i, p, be, ops, dc, shots, seed = self._shots_call(inputs, parameters, qubits, observable, observable_qubit, sampling,
+                                                          dtype, backend, exec_opts, tie_eps)
+        est, ok, ties = C.c_double(), C.c_uint64(), C.c_uint64()
+        check(load().qf_expectation_shots(be.handle, int(qubits), dc, ptr(ops), len(ops), ptr(p), p.size, ptr(i), i.size,
+                                          int(observable), int(observable_qubit), shots, seed, float(tie_eps),
+                                          _exec(exec_opts), C.byref(est), C.byref(ok), C.byref(ties)))
+        lo, hi = wilson_ci(ok.value, shots, 0.95)
+        return est.value, (2.0 * lo - 1.0, 2.0 * hi - 1.0)
+
+    def expectation_with_inputs_shots(self, inputs, parameters, qubits: int, observable: int, observable_qubit: int,
+                                      sampling: "ShotConfig", **kw) -> float:
+        """expectation_with_inputs_shots (src/lib.rs:3361-3382)."""
+        return self.expectation_with_inputs_shots_with_ci(inputs, parameters, qubits, observable, observable_qubit,
+                                                          sampling, **kw)[0]
+
+    def expectation_shots(self, parameters, qubits: int, observable: int, observable_qubit: int, sampling, **kw) -> float:
+        return self.expectation_with_inputs_shots([], parameters, qubits, observable, observable_qubit, sampling, **kw)
+
+    def expectation_shots_with_ci(self, parameters, qubits: int, observable: int, observable_qubit: int, sampling, **kw):
+        return self.expectation_with_inputs_shots_with_ci([], parameters, qubits, observable, observable_qubit, sampling,
+                                                          **kw)
+
+    def parameter_shift_gradient_with_inputs_shots(self, inputs, parameters, qubits: int, observable: int,
+                                                   observable_qubit: int, sampling: "ShotConfig", dtype="c128",
+                                                   backend=None, exec_opts=None, tie_eps: float = 0.0) -> np.ndarray:
+        """parameter_shift_gradient_with_inputs_shots (src/lib.rs:3428-3479)."""
+        i, p, be, ops, dc, shots, seed = self._shots_call(inputs, parameters, qubits, observable, observable_qubit, sampling,
+                                                          dtype, backend, exec_opts, tie_eps)
+        g = np.zeros(p.size, dtype=np.float64)
+        ties = C.c_uint64()
+        check(load().qf_parameter_shift_gradient_shots(be.handle, int(qubits), dc, ptr(ops), len(ops), ptr(p), p.size, ptr(i),
+                                                       i.size, int(observable), int(observable_qubit), shots, seed,
+                                                       float(tie_eps), _exec(exec_opts), ptr(g), C.byref(ties)))
+        return g
+
+    def parameter_shift_gradient_shots(self, parameters, qubits: int, observable: int, observable_qubit: int, sampling,
+                                       **kw) -> np.ndarray:
+        return self.parameter_shift_gradient_with_inputs_shots([], parameters, qubits, observable, observable_qubit,
+                                                               sampling, **kw)
+
     # ---- the density-matrix path (channels; src/lib.rs:3125-3266, 3755-3800) ----
     def _resolved_ops(self, inputs, parameters) -> np.ndarray:
         """The op list with rotation and encoding angles bound to fixed gates."""
@@ -1082,9 +1163,7 @@ class ParameterizedCircuit:
                                       **kw):
         """mse_loss_and_gradient_density (src/lib.rs:3755-3800): mean squared
         error of the density-matrix expectations and its parameter-shift gradient."""
-        if not data or any(len(x) != self.input_count_ or not math.isfinite(y) or not all(math.isfinite(v) for v in x)
-                           for x, y in data):
-            raise QuantumError(_abi.STATUS_CODES["InvalidArgument"], "invalid training data")
+        self._check_training_data(data)
         p = np.ascontiguousarray(parameters, dtype=np.float64)
         loss, grad = 0.0, np.zeros(self.parameter_count_)
         for x, y in data:
@@ -1092,6 +1171,79 @@ class ParameterizedCircuit:
             loss += r * r
             grad += 2.0 * r * self.parameter_shift_gradient_density_with_inputs(x, p, qubits, observable, observable_qubit, **kw)
         return loss / len(data), grad / len(data)
+
+    def _check_training_data(self, data):
+        if not data or any(len(x) != self.input_count_ or not math.isfinite(y) or not all(math.isfinite(v) for v in x)
+                           for x, y in data):
+            raise QuantumError(_abi.STATUS_CODES["InvalidArgument"], "invalid training data")
+
+    def expectation_density_with_inputs_shots_with_ci(self, inputs, parameters, qubits: int, observable: int,
+                                                      observable_qubit: int, sampling: "ShotConfig", **kw):
+        """(estimate, Wilson 95 % interval) of the density-matrix expectation
+        from `sampling` shots (src/lib.rs:3208-3232): the exact expectation
+        through sample_expectation, the interval from round(P(+1) * shots)."""
+        if int(sampling.shots) == 0:
+            raise QuantumError(_abi.STATUS_CODES["InvalidShotCount"], "shot count must be greater than zero")
+        exact = self.expectation_density_with_inputs(inputs, parameters, qubits, observable, observable_qubit, **kw)
+        est = sample_expectation(exact, sampling)
+        p = min(max((1.0 + exact) * 0.5, 0.0), 1.0)
+        lo, hi = wilson_ci(int(np.round(p * int(sampling.shots))), int(sampling.shots), 0.95)
+        return est, (2.0 * lo - 1.0, 2.0 * hi - 1.0)
+
+    def expectation_density_with_inputs_shots(self, inputs, parameters, qubits: int, observable: int,
+                                              observable_qubit: int, sampling: "ShotConfig", **kw) -> float:
+        """expectation_density_with_inputs_shots (src/lib.rs:3188-3206)."""
+        if int(sampling.shots) == 0:
+            raise QuantumError(_abi.STATUS_CODES["InvalidShotCount"], "shot count must be greater than zero")
+        exact = self.expectation_density_with_inputs(inputs, parameters, qubits, observable, observable_qubit, **kw)
+        return sample_expectation(exact, sampling)
+
+    def parameter_shift_gradient_density_with_inputs_shots(self, inputs, parameters, qubits: int, observable: int,
+                                                           observable_qubit: int, sampling: "ShotConfig", dtype="c128",
+                                                           backend=None, exec_opts=None) -> np.ndarray:
+        """parameter_shift_gradient_density_with_inputs_shots (src/lib.rs:3268-3320)."""
+        i, p = self._values(inputs, parameters)
+        be = backend or default_backend()
+        ops = self.ops()
+        g = np.zeros(p.size, dtype=np.float64)
+        check(load().qf_parameter_shift_gradient_density_shots(be.handle, int(qubits), _dtype_code(dtype), ptr(ops),
+                                                               len(ops), ptr(p), p.size, ptr(i), i.size, int(observable),
+                                                               int(observable_qubit), int(sampling.shots),
+                                                               int(sampling.seed), _exec(exec_opts), ptr(g)))
+        return g
+
+    def _mse_shots(self, data, parameters, sampling, predict, gradient):
+        if int(sampling.shots) == 0:
+            raise QuantumError(_abi.STATUS_CODES["InvalidShotCount"], "shot count must be greater than zero")
+        self._check_training_data(data)
+        p = np.ascontiguousarray(parameters, dtype=np.float64)
+        loss, grad = 0.0, np.zeros(self.parameter_count_)
+        for k, (x, y) in enumerate(data):
+            seed = (int(sampling.seed) + k * 0x9E3779B9) & 0xFFFFFFFFFFFFFFFF
+            r = predict(x, p, ShotConfig(int(sampling.shots), seed)) - y
+            loss += r * r
+            grad += 2.0 * r * gradient(x, p, ShotConfig(int(sampling.shots), (seed + 1) & 0xFFFFFFFFFFFFFFFF))
+        return loss / len(data), grad / len(data)
+
+    def mse_loss_and_gradient_shots(self, data, parameters, qubits: int, observable: int, observable_qubit: int,
+                                    sampling: "ShotConfig", **kw):
+        """mse_loss_and_gradient_shots (src/lib.rs:3866-3927): sample k uses
+        seed + k * 0x9e3779b9 for its prediction and that + 1 for its gradient."""
+        return self._mse_shots(
+            data, parameters, sampling,
+            lambda x, p, sc: self.expectation_with_inputs_shots(x, p, qubits, observable, observable_qubit, sc, **kw),
+            lambda x, p, sc: self.parameter_shift_gradient_with_inputs_shots(x, p, qubits, observable, observable_qubit,
+                                                                             sc, **kw))
+
+    def mse_loss_and_gradient_density_shots(self, data, parameters, qubits: int, observable: int, observable_qubit: int,
+                                            sampling: "ShotConfig", **kw):
+        """mse_loss_and_gradient_density_shots (src/lib.rs:3802-3864)."""
+        return self._mse_shots(
+            data, parameters, sampling,
+            lambda x, p, sc: self.expectation_density_with_inputs_shots(x, p, qubits, observable, observable_qubit, sc,
+                                                                        **kw),
+            lambda x, p, sc: self.parameter_shift_gradient_density_with_inputs_shots(x, p, qubits, observable,
+                                                                                     observable_qubit, sc, **kw))
 
     def expectation_pauli_sum(self, parameters, qubits: int, hamiltonian, inputs=None, dtype="c128", backend=None,
                               exec_opts=None) -> float:

@@ -324,6 +324,16 @@ inline bool valid_probability(double p) { return std::isfinite(p) && p >= 0.0 &&
 
 inline double clamp01(double x) { return std::min(1.0, std::max(0.0, x)); }
 
+// SmallRng::seeded (src/lib.rs:4881-4897): splitmix64 of the seed, a zero
+// state replaced by the golden-ratio constant.
+inline uint64_t smallrng_seeded(uint64_t seed) {
+    uint64_t z = seed + 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    z ^= z >> 31;
+    return z == 0 ? 0x9E3779B97F4A7C15ULL : z;
+}
+
 // Every shot's generator state at its first draw: shot s starts at draw s * d
 // of SmallRng::seeded(seed) (src/lib.rs:4881-4897), d = measurements (and,
 // with noise, channels) per shot — the reference's shot-major stream.
@@ -332,11 +342,7 @@ std::vector<uint64_t> shot_starts(const qf_op *ops, uint64_t n_ops, uint64_t sho
     for (uint64_t k = 0; k < n_ops; ++k)
         draws += ops[k].kind == QF_OP_MEASURE || (allow_noise && ops[k].kind == QF_OP_CHANNEL);
     std::vector<uint64_t> st(shots);
-    uint64_t z = seed + 0x9E3779B97F4A7C15ULL;
-    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
-    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
-    z ^= z >> 31;
-    uint64_t x = z == 0 ? 0x9E3779B97F4A7C15ULL : z;
+    uint64_t x = smallrng_seeded(seed);
     if (draws <= 64) {  // step the stream
         for (uint64_t s = 0; s < shots; ++s) {
             st[s] = x;
@@ -1649,10 +1655,13 @@ int qf_expectation_density(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op 
 // ParameterizedCircuit::parameter_shift_gradient_density_with_inputs
 // (src/lib.rs:3235-3266): every rotation occurrence shifted by +-pi/2 through
 // the density-matrix path, g[param] += (E+ - E-) / 2.
-int qf_parameter_shift_gradient_density(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops,
-                                        const double *params, uint64_t n_params, const double *inputs, uint64_t n_inputs,
-                                        int observable, uint32_t observable_qubit, const qf_exec_opts *opts,
-                                        double *expectation, double *gradient) {
+// Per rotation occurrence k: g[p_k] += (E(+pi/2 at k) - E(-pi/2 at k)) / 2 on
+// the density matrix. With shots > 0 each E goes through sample_expectation
+// with seed + 2k and seed + 2k + 1 (src/lib.rs:3268-3320).
+static int density_shift_gradient(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops,
+                                  const double *params, uint64_t n_params, const double *inputs, uint64_t n_inputs,
+                                  int observable, uint32_t observable_qubit, const qf_exec_opts *opts, uint64_t shots,
+                                  uint64_t seed, double *expectation, double *gradient) {
     clear_error();
     if (n_params && !gradient) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
     int mode;
@@ -1670,11 +1679,35 @@ int qf_parameter_shift_gradient_density(qf_ctx *ctx, uint32_t qubits, int dtype,
                                    observable_qubit, opts, &plus));
         QF_TRY(density_expectation(ctx, qubits, dtype, ops, n_ops, params, n_params, inputs, n_inputs, (int64_t)k, -shift, mode,
                                    observable_qubit, opts, &minus));
+        if (shots) {
+            const uint64_t occ_seed = seed + 2 * k;
+            QF_TRY(qf_sample_expectation(plus, shots, occ_seed, &plus, nullptr));
+            QF_TRY(qf_sample_expectation(minus, shots, occ_seed + 1, &minus, nullptr));
+        }
         g[ops[k].param] += 0.5 * (plus - minus);
     }
     if (expectation) *expectation = e;
     std::copy(g.begin(), g.end(), gradient);
     return QF_OK;
+}
+
+int qf_parameter_shift_gradient_density(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops,
+                                        const double *params, uint64_t n_params, const double *inputs, uint64_t n_inputs,
+                                        int observable, uint32_t observable_qubit, const qf_exec_opts *opts,
+                                        double *expectation, double *gradient) {
+    return density_shift_gradient(ctx, qubits, dtype, ops, n_ops, params, n_params, inputs, n_inputs, observable,
+                                  observable_qubit, opts, 0, 0, expectation, gradient);
+}
+
+// ParameterizedCircuit::parameter_shift_gradient_density_with_inputs_shots (src/lib.rs:3268-3320).
+int qf_parameter_shift_gradient_density_shots(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops,
+                                              const double *params, uint64_t n_params, const double *inputs,
+                                              uint64_t n_inputs, int observable, uint32_t observable_qubit,
+                                              uint64_t shots, uint64_t seed, const qf_exec_opts *opts, double *gradient) {
+    clear_error();
+    if (shots == 0) return fail(QF_ERR_INVALID_SHOT_COUNT, "shot count must be greater than zero");
+    return density_shift_gradient(ctx, qubits, dtype, ops, n_ops, params, n_params, inputs, n_inputs, observable,
+                                  observable_qubit, opts, shots, seed, nullptr, gradient);
 }
 
 int qf_run_density_circuit(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops, const double *in_entries,
@@ -1756,6 +1789,129 @@ int qf_expectation(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, ui
     QF_TRY(bind_device(ctx));
     return forward_expectation(ctx, qubits, dtype, ops, n_ops, params, n_params, inputs, n_inputs, -1, 0.0, terms, n_terms,
                                opts, expectation);
+}
+
+// estimate_observable_shots (src/lib.rs:4806-4838) on the state the op list
+// prepares (with `shift` on op `shift_op`): the measured basis rotated (X: H;
+// Y: Rz(-pi/2) then H), P(1) of the qubit reduced once, then `shots` draws of
+// SmallRng::seeded(seed) compared against it (each clone-and-measure of the
+// reference draws one uniform against the same P(1)); *successes counts
+// outcome 0. Draws within tie_eps of P(1) are counted.
+static int shots_estimate(qf_ctx *ctx, uint32_t n, int dtype, const qf_op *ops, uint64_t n_ops, const double *params,
+                          uint64_t n_params, const double *inputs, uint64_t n_inputs, int64_t shift_op, double shift,
+                          int observable, uint32_t q, uint64_t shots, uint64_t seed, double tie_eps,
+                          const qf_exec_opts *opts, uint64_t *successes, uint64_t *ties) {
+    std::vector<BGate> gates;
+    QF_TRY(bind_ops(n, ops, n_ops, params, n_params, inputs, n_inputs, shift_op, shift, gates));
+    auto add = [&](int gate, double theta) -> int {
+        BGate g;
+        g.kind = BK_MAT1;
+        g.q0 = q;
+        QF_TRY(gate_matrix(gate, theta, g.m));
+        g.diag = matrix_is_diag(g.m);
+        gates.push_back(g);
+        return QF_OK;
+    };
+    if (observable == QF_PAULI_X) QF_TRY(add(QF_GATE_H, 0.0));
+    if (observable == QF_PAULI_Y) {
+        QF_TRY(add(QF_GATE_RZ, -1.5707963267948966));
+        QF_TRY(add(QF_GATE_H, 0.0));
+    }
+    qf_sv *sv;
+    QF_TRY(scratch_state(ctx, &ctx->scratch_sv, n, dtype, &sv));
+    QF_TRY(fill_zero_state(sv));
+    QF_TRY(execute_gates(sv, gates, opts));
+    double p1;
+    QF_TRY(reduce_p_one(sv, q, &p1));
+    p1 = clamp01(p1);
+    uint64_t x = smallrng_seeded(seed), ok = 0, t = 0;
+    for (uint64_t k = 0; k < shots; ++k) {
+        const double u = next_uniform(&x);
+        const int o = u < p1 ? 1 : 0;
+        if (std::fabs(u - p1) < tie_eps) ++t;
+        const double prob = o ? p1 : 1.0 - p1;
+        if (prob <= 2.220446049250313e-16)
+            return fail(QF_ERR_INVALID_PROBABILITY, "measurement probability must be in [0, 1], got %g", prob);
+        ok += o == 0;
+    }
+    *successes = ok;
+    if (ties) *ties += t;
+    return QF_OK;
+}
+
+int qf_sample_expectation(double expectation, uint64_t shots, uint64_t seed, double *estimate, uint64_t *positive) {
+    if (!estimate) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (shots == 0) return fail(QF_ERR_INVALID_SHOT_COUNT, "shot count must be greater than zero");
+    const double p = clamp01((1.0 + expectation) * 0.5);
+    uint64_t x = smallrng_seeded(seed), k = 0;
+    for (uint64_t s = 0; s < shots; ++s) k += next_uniform(&x) < p;
+    *estimate = (double)(2 * k) / (double)shots - 1.0;
+    if (positive) *positive = k;
+    return QF_OK;
+}
+
+static int shots_checks(qf_ctx *ctx, uint32_t qubits, int dtype, uint64_t n_ops, const qf_op *ops, const double *params,
+                        uint64_t n_params, const double *inputs, uint64_t n_inputs, int observable, uint32_t q,
+                        uint64_t shots) {
+    if (!ctx || (n_ops && !ops) || (n_params && !params) || (n_inputs && !inputs)) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    QF_TRY(check_dtype(dtype));
+    if (shots == 0) return fail(QF_ERR_INVALID_SHOT_COUNT, "shot count must be greater than zero");
+    if (qubits == 0) return fail(QF_ERR_ZERO_QUBITS, "a state vector must contain at least one qubit");
+    if (q >= qubits) return fail(QF_ERR_QUBIT_OUT_OF_RANGE, "qubit index %u is out of range for %u qubits", q, qubits);
+    if (observable != QF_PAULI_X && observable != QF_PAULI_Y && observable != QF_PAULI_Z)
+        return fail(QF_ERR_INVALID_ARGUMENT, "unknown observable %d", observable);
+    return QF_OK;
+}
+
+// ParameterizedCircuit::expectation_with_inputs_shots (src/lib.rs:3361-3382).
+int qf_expectation_shots(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops, const double *params,
+                         uint64_t n_params, const double *inputs, uint64_t n_inputs, int observable, uint32_t observable_qubit,
+                         uint64_t shots, uint64_t seed, double tie_eps, const qf_exec_opts *opts, double *estimate,
+                         uint64_t *successes, uint64_t *n_ties) {
+    clear_error();
+    QF_TRY(shots_checks(ctx, qubits, dtype, n_ops, ops, params, n_params, inputs, n_inputs, observable, observable_qubit, shots));
+    QF_TRY(bind_device(ctx));
+    uint64_t ok = 0, t = 0;
+    QF_TRY(shots_estimate(ctx, qubits, dtype, ops, n_ops, params, n_params, inputs, n_inputs, -1, 0.0, observable,
+                          observable_qubit, shots, seed, tie_eps, opts, &ok, &t));
+    if (estimate) *estimate = 2.0 * ((double)ok / (double)shots) - 1.0;
+    if (successes) *successes = ok;
+    if (n_ties) *n_ties = t;
+    return QF_OK;
+}
+
+// ParameterizedCircuit::parameter_shift_gradient_with_inputs_shots
+// (src/lib.rs:3428-3479): rotation occurrence k shifted by +-pi/2, each side
+// estimated from `shots` draws, seeds seed + 2k and seed + 2k + 1.
+int qf_parameter_shift_gradient_shots(qf_ctx *ctx, uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops,
+                                      const double *params, uint64_t n_params, const double *inputs, uint64_t n_inputs,
+                                      int observable, uint32_t observable_qubit, uint64_t shots, uint64_t seed,
+                                      double tie_eps, const qf_exec_opts *opts, double *gradient, uint64_t *n_ties) {
+    clear_error();
+    if (n_params && !gradient) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    QF_TRY(shots_checks(ctx, qubits, dtype, n_ops, ops, params, n_params, inputs, n_inputs, observable, observable_qubit, shots));
+    {  // the whole list validated before any launch
+        std::vector<BGate> g;
+        QF_TRY(bind_ops(qubits, ops, n_ops, params, n_params, inputs, n_inputs, -1, 0.0, g));
+    }
+    QF_TRY(bind_device(ctx));
+    std::vector<double> g(n_params, 0.0);
+    uint64_t t = 0;
+    const double shift = 1.5707963267948966;  // FRAC_PI_2
+    for (uint64_t k = 0; k < n_ops; ++k) {
+        if (ops[k].kind != QF_OP_ROTATION) continue;
+        const uint64_t occ_seed = seed + k * 2;
+        uint64_t okp, okm;
+        QF_TRY(shots_estimate(ctx, qubits, dtype, ops, n_ops, params, n_params, inputs, n_inputs, (int64_t)k, shift, observable,
+                              observable_qubit, shots, occ_seed, tie_eps, opts, &okp, &t));
+        QF_TRY(shots_estimate(ctx, qubits, dtype, ops, n_ops, params, n_params, inputs, n_inputs, (int64_t)k, -shift, observable,
+                              observable_qubit, shots, occ_seed + 1, tie_eps, opts, &okm, &t));
+        const double plus = 2.0 * ((double)okp / (double)shots) - 1.0, minus = 2.0 * ((double)okm / (double)shots) - 1.0;
+        g[ops[k].param] += 0.5 * (plus - minus);
+    }
+    std::copy(g.begin(), g.end(), gradient);
+    if (n_ties) *n_ties = t;
+    return QF_OK;
 }
 
 // ParameterizedCircuit::gradient_with_inputs (src/gradients.rs:232-330).

@@ -227,3 +227,137 @@ def test_expectation_entry_point(backend):
     pc = pc_from_ops(ops, params.size)
     e = pc.expectation_pauli_sum(params, n, H, backend=backend)
     assert abs(e - O.energy(ops, n, params, H.array())) < 1e-10
+
+
+def _shots_circuit(n):
+    r = np.random.default_rng(40 + n)
+    c = ParameterizedCircuit.with_inputs(4, 2)
+    for q in range(n):
+        c.encode_rotation(RotationAxis.Y, q, q % 2)
+    for layer in range(2):
+        for q in range(n):
+            c.rotation(int(r.integers(0, 3)), q, int(r.integers(0, 4)))
+        for q in range(n - 1):
+            c.cnot(q, q + 1)
+    return c, r.uniform(-np.pi, np.pi, 4), r.uniform(-1, 1, 2)
+
+
+@pytest.mark.parametrize("n", [1, 5, 9])
+def test_shot_estimates_match_the_oracle_draw_for_draw(backend, n):  # src/lib.rs:3361-3479, 4806-4838
+    """complex128: every shot's outcome is the oracle's literal
+    clone-and-measure outcome, so estimates and gradients are equal."""
+    from quantumforge_gb300 import ShotConfig
+
+    c, params, inputs = _shots_circuit(n)
+    ops = c.ops()
+    shots, seed = 3000, 1234 + n
+    for obs in (A.PAULI_X, A.PAULI_Y, A.PAULI_Z):
+        q = n - 1
+        est, (lo, hi) = c.expectation_with_inputs_shots_with_ci(inputs, params, n, obs, q, ShotConfig(shots, seed),
+                                                                backend=backend)
+        ok = O.estimate_observable_shots(O.run(ops, n, params, inputs), obs, q, shots, seed)
+        assert est == 2.0 * ok / shots - 1.0
+        assert lo <= est <= hi and hi - lo < 0.1
+        assert c.expectation_with_inputs_shots(inputs, params, n, obs, q, ShotConfig(shots, seed), backend=backend) == est
+        g = c.parameter_shift_gradient_with_inputs_shots(inputs, params, n, obs, q, ShotConfig(shots, seed),
+                                                         backend=backend)
+        want = np.zeros(4)
+        for k in range(len(ops)):
+            if int(ops[k]["kind"]) != A.OP_ROTATION:
+                continue
+            e = []
+            for sh, sd in ((np.pi / 2, seed + 2 * k), (-np.pi / 2, seed + 2 * k + 1)):
+                okk = O.estimate_observable_shots(O.run(ops, n, params, inputs, shift_op=k, shift=sh), obs, q, shots, sd)
+                e.append(2.0 * okk / shots - 1.0)
+            want[int(ops[k]["param"])] += 0.5 * (e[0] - e[1])
+        assert np.array_equal(g, want)
+        exact = c.parameter_shift_gradient_with_inputs(inputs, params, n, obs, q, backend=backend)
+        assert np.abs(g - exact).max() < 0.2
+
+
+def test_shot_estimates_validate_like_the_reference(backend):
+    from quantumforge_gb300 import ShotConfig
+
+    c, params, inputs = _shots_circuit(3)
+    for call in (lambda: c.expectation_with_inputs_shots(inputs, params, 3, Z, 0, ShotConfig(0, 1), backend=backend),
+                 lambda: c.parameter_shift_gradient_with_inputs_shots(inputs, params, 3, Z, 0, ShotConfig(0, 1),
+                                                                      backend=backend),
+                 lambda: c.expectation_density_with_inputs_shots(inputs, params, 3, Z, 0, ShotConfig(0, 1),
+                                                                 backend=backend),
+                 lambda: c.parameter_shift_gradient_density_with_inputs_shots(inputs, params, 3, Z, 0,
+                                                                              ShotConfig(0, 1), backend=backend)):
+        with pytest.raises(QuantumError) as e:
+            call()
+        assert e.value.kind == "InvalidShotCount"
+    with pytest.raises(QuantumError) as e:
+        c.expectation_with_inputs_shots(inputs, params, 3, Z, 3, ShotConfig(10, 1), backend=backend)
+    assert e.value.kind == "QubitOutOfRange"
+    # complex64 state: the same draws, outcomes equal except within float32 distance of P(1)
+    est64 = c.expectation_with_inputs_shots(inputs, params, 3, Z, 1, ShotConfig(4000, 9), dtype="c64", backend=backend)
+    est128 = c.expectation_with_inputs_shots(inputs, params, 3, Z, 1, ShotConfig(4000, 9), backend=backend)
+    assert abs(est64 - est128) <= 2 * 3 / 4000
+
+
+def test_density_shot_estimates_sample_the_exact_expectation(backend):  # src/lib.rs:3188-3320, 4840-4850
+    from quantumforge_gb300 import ShotConfig, sample_expectation
+
+    c, params, inputs = _shots_circuit(4)
+    c.channel(2, NoiseChannel.AmplitudeDamping(0.2))
+    c.rotation(RotationAxis.X, 2, 3)
+    c.channel(1, NoiseChannel.Depolarizing(0.05))
+    sc = ShotConfig(5000, 77)
+    exact = c.expectation_density_with_inputs(inputs, params, 4, A.PAULI_Z, 2, backend=backend)
+    est, (lo, hi) = c.expectation_density_with_inputs_shots_with_ci(inputs, params, 4, A.PAULI_Z, 2, sc,
+                                                                   backend=backend)
+    assert est == sample_expectation(exact, sc)
+    assert c.expectation_density_with_inputs_shots(inputs, params, 4, A.PAULI_Z, 2, sc, backend=backend) == est
+    assert lo <= exact <= hi
+    g = c.parameter_shift_gradient_density_with_inputs_shots(inputs, params, 4, A.PAULI_Z, 2, sc, backend=backend)
+    ops = c.ops()
+    want = np.zeros(4)
+    for k in range(len(ops)):
+        if int(ops[k]["kind"]) != A.OP_ROTATION:
+            continue
+        e = []
+        for sh, sd in ((np.pi / 2, 77 + 2 * k), (-np.pi / 2, 77 + 2 * k + 1)):
+            ex = _density_shifted(c, params, inputs, k, sh)
+            e.append(sample_expectation(ex, ShotConfig(5000, sd)))
+        want[int(ops[k]["param"])] += 0.5 * (e[0] - e[1])
+    assert np.abs(g - want).max() < 1e-12
+    exact_g = c.parameter_shift_gradient_density_with_inputs(inputs, params, 4, A.PAULI_Z, 2, backend=backend)
+    assert np.abs(g - exact_g).max() < 0.15
+
+
+def _density_shifted(c, params, inputs, k, shift):
+    """Exact density expectation <Z_2> with rotation occurrence k shifted, from the oracle."""
+    ops = c.ops().copy()
+    rot = {A.PAULI_X: A.GATE_RX, A.PAULI_Y: A.GATE_RY, A.PAULI_Z: A.GATE_RZ}
+    for j in range(len(ops)):
+        kind = int(ops[j]["kind"])
+        if kind in (A.OP_ROTATION, A.OP_ENCODING):
+            src = params if kind == A.OP_ROTATION else inputs
+            ops[j]["theta"] = src[int(ops[j]["param"])] + (shift if j == k else 0.0)
+            ops[j]["gate"] = rot[int(ops[j]["gate"])]
+            ops[j]["kind"] = A.OP_GATE
+            ops[j]["param"] = 0
+    return O.dm_expectation(O.run_density(ops, 4), A.PAULI_Z, 2)
+
+
+def test_shot_mse_composes_the_per_sample_estimates(backend):  # src/lib.rs:3802-3927
+    from quantumforge_gb300 import ShotConfig
+
+    c, params, _ = _shots_circuit(3)
+    data = [([0.1, -0.4], 0.3), ([0.7, 0.2], -0.5), ([-0.9, 0.5], 0.05)]
+    sc = ShotConfig(2000, 31)
+    for dens in (False, True):
+        f = c.mse_loss_and_gradient_density_shots if dens else c.mse_loss_and_gradient_shots
+        pred = c.expectation_density_with_inputs_shots if dens else c.expectation_with_inputs_shots
+        grad = c.parameter_shift_gradient_density_with_inputs_shots if dens else c.parameter_shift_gradient_with_inputs_shots
+        loss, g = f(data, params, 3, Z, 0, sc, backend=backend)
+        want_l, want_g = 0.0, np.zeros(4)
+        for k, (x, y) in enumerate(data):
+            s = 31 + k * 0x9E3779B9
+            r = pred(x, params, 3, Z, 0, ShotConfig(2000, s), backend=backend) - y
+            want_l += r * r
+            want_g += 2 * r * grad(x, params, 3, Z, 0, ShotConfig(2000, s + 1), backend=backend)
+        assert loss == want_l / 3 and np.array_equal(g, want_g / 3)

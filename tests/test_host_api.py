@@ -3,7 +3,9 @@ ShotResult, NoiseChannel records and the package's exported names."""
 import math
 
 import numpy as np
+import pytest
 
+import oracle as O
 import quantumforge_gb300 as qf
 from quantumforge_gb300 import _abi as A
 from quantumforge_gb300.core import NoiseChannel, ShotResult
@@ -34,3 +36,29 @@ def test_noise_channel_records():
 def test_package_exports():
     for name in ("Circuit", "NoiseChannel", "StateVector", "StateVectorBatch", "ShotResult", "CudaBackend"):
         assert hasattr(qf, name), name
+
+
+def test_wilson_interval_matches_the_reference_formula():  # src/lib.rs:2493-2513
+    from quantumforge_gb300 import wilson_ci
+
+    assert wilson_ci(0, 0, 0.95) == (0.0, 1.0)
+    lo, hi = wilson_ci(5, 10, 0.95)
+    assert abs(lo - 0.2365895936154873) < 1e-15 and abs(hi - 0.7634104063845127) < 1e-15
+    lo, hi = wilson_ci(10, 10, 0.95)
+    assert hi == 1.0 and 0.7 < lo < 0.73
+    # the z of each confidence band: 2.576, 1.96, 1.645, and 1.96 below 0.90
+    widths = [wilson_ci(50, 100, c)[1] - wilson_ci(50, 100, c)[0] for c in (0.99, 0.95, 0.90, 0.5)]
+    assert widths[0] > widths[1] > widths[2] and widths[3] == widths[1]
+
+
+def test_sample_expectation_draws_the_seeded_stream():  # src/lib.rs:4840-4850
+    from quantumforge_gb300 import QuantumError, ShotConfig, sample_expectation
+
+    for e, shots, seed in [(0.3, 1000, 5), (-1.0, 7, 0), (1.0, 10, 3), (0.0, 4321, 2**64 - 1), (1.7, 9, 1)]:
+        r = O.Rng(seed)
+        p = min(max((1 + e) / 2, 0.0), 1.0)
+        k = sum(r.next_f64() < p for _ in range(shots))
+        assert sample_expectation(e, ShotConfig(shots, seed)) == 2 * k / shots - 1
+    with pytest.raises(QuantumError) as err:
+        sample_expectation(0.2, ShotConfig(0, 1))
+    assert err.value.kind == "InvalidShotCount"
