@@ -164,6 +164,8 @@ enum qf_exec_mode {
 #define QF_EXEC_FLAG_NO_JIT 4      /* complex64: never compile passes; interpret them */
 #define QF_EXEC_FLAG_SHOTS_TREE 8  /* shots: always walk the branch tree of device states */
 #define QF_EXEC_FLAG_SHOTS_TRAJECTORIES 16  /* shots: per-shot trajectories in shared memory whenever the state fits */
+#define QF_EXEC_FLAG_PLAN_FIRST_COME 32  /* fused sweeps: fill each pass's tile in gate order (no look-ahead choice of
+                                            its resident qubits) */
 
 typedef struct qf_exec_opts {
     int32_t mode;          /* enum qf_exec_mode */

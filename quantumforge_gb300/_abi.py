@@ -96,6 +96,7 @@ EXEC_FLAG_JIT = 2
 EXEC_FLAG_NO_JIT = 4
 EXEC_FLAG_SHOTS_TREE = 8
 EXEC_FLAG_SHOTS_TRAJECTORIES = 16
+EXEC_FLAG_PLAN_FIRST_COME = 32
 _MODES = {"auto": EXEC_AUTO, "unfused": EXEC_UNFUSED, "fused": EXEC_FUSED}
 
 
@@ -110,6 +111,10 @@ def exec_opts(opts) -> "ExecOpts":
         flags |= EXEC_FLAG_JIT
     elif opts.get("jit") is False:
         flags |= EXEC_FLAG_NO_JIT
+    if opts.get("plan") == "first_come":
+        flags |= EXEC_FLAG_PLAN_FIRST_COME
+    elif opts.get("plan", "lookahead") != "lookahead":
+        raise ValueError("plan must be 'lookahead' or 'first_come'")
     engine = opts.get("shots_engine")
     if engine == "tree":
         flags |= EXEC_FLAG_SHOTS_TREE

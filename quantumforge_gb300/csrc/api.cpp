@@ -252,6 +252,7 @@ int adjoint_device(qf_ctx *ctx, uint32_t n, const std::vector<BGate> &gates, con
     } guard{ctx, &ckpt};
     PlanOpts po;
     default_tiling(n, dtype, o->exec.tile_qubits, &po.tile_qubits, &po.low_qubits);
+    po.search = !(o->exec.flags & QF_EXEC_FLAG_PLAN_FIRST_COME);
     // every backward segment is planned before anything launches, then run back
     // to back: the overlap slots of all segments land in one device buffer that
     // is read once at the end
@@ -1993,6 +1994,7 @@ int qf_plan_stats(uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops, 
     }
     PlanOpts po;
     forward_tiling(qubits, dtype, opts ? opts->tile_qubits : 0, opts ? opts->flags : 0, &po.tile_qubits, &po.low_qubits);
+    po.search = !(opts && (opts->flags & QF_EXEC_FLAG_PLAN_FIRST_COME));
     Plan plan;
     QF_TRY(plan_passes(qubits, gates, po, plan));
     *n_passes = plan.passes.size();

@@ -220,6 +220,59 @@ int popc(uint64_t x) { return __builtin_popcountll(x); }
 // it. Gates on different qubits commute, so the reordering is exact.
 // Diagonal gates, CZ and a CNOT's control never need residency: within a tile
 // their non-resident bits are constant and become per-tile scalars/conditions.
+namespace {
+// Items of `remaining` (in order) that one pass over resident set S runs: an
+// item runs when none of its qubits is blocked and its needed qubits are in
+// S; an item that cannot run blocks its qubits for everything after it.
+int pass_closure(const std::vector<Item> &items, const std::vector<int> &remaining, uint64_t S, uint64_t all,
+                 int max_items) {
+    uint64_t blocked = 0;
+    int cnt = 0;
+    for (int idx : remaining) {
+        if (blocked == all || cnt >= max_items) break;
+        const Item &it = items[idx];
+        if ((it.touch & blocked) || (it.need & ~S)) {
+            blocked |= it.touch;
+            continue;
+        }
+        ++cnt;
+    }
+    return cnt;
+}
+
+// Resident set of the next pass: from `base`, add one qubit at a time, each
+// time the one that lets the pass run the most items (lowest index on ties).
+// Stops when no single qubit adds an item; the first-come fill completes it.
+uint64_t choose_resident(const std::vector<Item> &items, const std::vector<int> &remaining, uint64_t base, int k,
+                         uint32_t n, uint64_t all, int max_items) {
+    uint64_t S = base;
+    int cur = pass_closure(items, remaining, S, all, max_items);
+    while (popc(S) < k) {
+        // candidates: qubits some runnable-so-far frontier item needs
+        uint64_t cand = 0, blocked = 0;
+        for (int idx : remaining) {
+            if (blocked == all) break;
+            const Item &it = items[idx];
+            if (it.touch & blocked) { blocked |= it.touch; continue; }
+            if (it.need & ~S) {
+                if (popc(it.need & ~S) == 1) cand |= it.need & ~S;
+                blocked |= it.touch;
+            }
+        }
+        int best = -1, best_cnt = cur;
+        for (uint32_t q = 0; q < n; ++q) {
+            if (!((cand >> q) & 1ULL)) continue;
+            const int c = pass_closure(items, remaining, S | (1ULL << q), all, max_items);
+            if (c > best_cnt) { best_cnt = c; best = (int)q; }
+        }
+        if (best < 0) break;
+        S |= 1ULL << best;
+        cur = best_cnt;
+    }
+    return S;
+}
+}  // namespace
+
 int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, Plan &plan) {
     plan = Plan();
     plan.n = n;
@@ -251,6 +304,7 @@ int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, 
         uint64_t L = low_mask;
         const uint64_t first_need = items[remaining[0]].need;
         for (int b = low - 1; b >= 1 && popc(L | first_need) > k; --b) L &= ~(1ULL << b);
+        if (o.search) L = choose_resident(items, remaining, L | first_need, k, n, all, o.max_items);
         uint64_t blocked = 0;
         std::vector<Item> taken;
         std::vector<int> last_on(n, -1);  // index into taken of the last item touching q

@@ -241,6 +241,7 @@ struct PlanOpts {
     bool merge_1q = true;   // multiply consecutive 1q gates on one qubit
     bool backward = false;  // adjoint reverse sweep: inverse gates + overlaps
     int max_items = 768;    // bound on ops per pass (shared-memory budget)
+    bool search = true;     // choose each pass's resident qubits by look-ahead
 };
 
 int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, Plan &plan);

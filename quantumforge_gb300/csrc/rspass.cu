@@ -137,6 +137,12 @@ __global__ void __launch_bounds__(32 << WB, (WB == 3 ? 2 : 1))
             sw |= 1ULL << pa.store_q[4 + w];
         }
     }
+    // SWAP relabels can leave other qubits in the warp positions at the store
+    // than at the load: a warp then stores into amplitudes another warp of the
+    // CTA loads, so every warp must have loaded the tile before any stores
+    bool cross_warp = false;
+#pragma unroll
+    for (int w = 0; w < WB; ++w) cross_warp |= pa.load_q[4 + w] != pa.store_q[4 + w];
 
     for (uint64_t t = blockIdx.x; t < pa.n_tiles; t += gridDim.x) {
         const uint64_t tb = deposit(t, pa.nonlocal_mask);
@@ -274,6 +280,7 @@ __global__ void __launch_bounds__(32 << WB, (WB == 3 ? 2 : 1))
             }
             }
         }
+        if (cross_warp) __syncthreads();
         {
             const uint64_t base = tb | lane | sw;
 #pragma unroll

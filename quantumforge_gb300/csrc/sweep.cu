@@ -631,6 +631,7 @@ int execute_gates(qf_sv *sv, const std::vector<BGate> &gates, const qf_exec_opts
         return fail(QF_ERR_INVALID_ARGUMENT, "unknown execution mode %d", mode);
     PlanOpts po;
     forward_tiling(sv->n, sv->dtype, opts ? opts->tile_qubits : 0, opts ? opts->flags : 0, &po.tile_qubits, &po.low_qubits);
+    po.search = !(opts && (opts->flags & QF_EXEC_FLAG_PLAN_FIRST_COME));
     Plan plan;
     QF_TRY(plan_passes(sv->n, gates, po, plan));
     return run_plan(sv, plan, opts ? opts->flags : 0);

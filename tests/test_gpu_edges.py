@@ -100,3 +100,38 @@ def test_largest_ghz_state(backend, n, dtype):
     finally:
         del sv
         gc.collect()
+
+
+def _inverse(ops):
+    """C† of a gate list: reversed, S/T swapped with their adjoints, angles negated."""
+    inv = ops[::-1].copy()
+    swap = {A.GATE_S: A.GATE_SDG, A.GATE_SDG: A.GATE_S, A.GATE_T: A.GATE_TDG, A.GATE_TDG: A.GATE_T}
+    for r in inv:
+        if int(r["kind"]) == A.OP_GATE:
+            g = int(r["gate"])
+            r["gate"] = swap.get(g, g)
+            if g in (A.GATE_RX, A.GATE_RY, A.GATE_RZ):
+                r["theta"] = -r["theta"]
+    return inv
+
+
+@pytest.mark.parametrize("plan", ["lookahead", "first_come"])
+def test_headline_circuit_round_trip_at_full_size(backend, plan):
+    """The 30-qubit depth-40 mixed circuit (1798 gates) and its inverse through
+    the compiled complex64 passes return |0...0>: a size-independent check of
+    the headline workload's planner and kernels (f32 error over 3596 gates)."""
+    from quantumforge_gb300 import workloads as W
+
+    gc.collect()
+    ops = W.random_circuit(30, 40, 1, two_qubit="mixed")
+    sv = StateVector.zero(30, dtype="c64", backend=backend)
+    try:
+        sv.apply_ops(ops, exec_opts={"plan": plan})
+        z = sv.expectation_z_all()
+        assert np.abs(z).max() < 0.01  # a scrambled state
+        sv.apply_ops(_inverse(ops), exec_opts={"plan": plan})
+        assert abs(sv.norm_sqr() - 1.0) < 1e-4
+        assert np.abs(sv.expectation_z_all() - 1.0).max() < 1e-4
+    finally:
+        del sv
+        gc.collect()
