@@ -263,6 +263,10 @@ int adjoint_device(qf_ctx *ctx, uint32_t n, const std::vector<BGate> &gates, con
         PlanOpts bo = po;
         bo.backward = true;
         bo.merge_1q = true;
+        // the dual passes (psi and lambda per tile) are bound by arithmetic, not
+        // HBM: fewer, heavier passes from the look-ahead measured 3 % slower
+        // on the 24-qubit VQE, so the backward sweep fills passes first-come
+        bo.search = false;
         for (size_t s = n_seg; s-- > 0;) {
             const size_t b = seg_begin[s], e = s + 1 < n_seg ? seg_begin[s + 1] : gates.size();
             std::vector<BGate> seg(gates.begin() + b, gates.begin() + e);
