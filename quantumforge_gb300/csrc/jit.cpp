@@ -123,6 +123,16 @@ struct Gen {
     std::vector<std::complex<double>> consts;  // 4 complex per matrix slot (float2 M[...])
     std::complex<double> gphase{1.0, 0.0};
     bool any_diag = false;
+    // factors pulled out of the gates of the current forward pass (one
+    // multiply per amplitude at the pass's end)
+    std::complex<double> pscale{1.0, 0.0};
+    bool pscale_imag = false;  // an odd number of imaginary factors
+    bool any_scale = false;
+    void reset_scale() {
+        pscale = {1.0, 0.0};
+        pscale_imag = false;
+        any_scale = false;
+    }
     int tmp = 0;
 
     std::string pfx = "r";  // register array: r = psi, l = lambda (backward passes)
@@ -199,6 +209,76 @@ void emit_mat2(Gen &g, int slot, int mk, const std::string &A, const std::string
         s << B << ".y=" << m10 << ".x*x.y+" << m10 << ".y*x.x+" << m11 << ".x*y.y+" << m11 << ".y*y.x;";
     }
     s << "}\n";
+}
+
+// A unitary 2x2 whose entries are real (kind 1) or real on the diagonal and
+// imaginary off it (kind 2) has |m00| = |m11| and |m01| = |m10|. Pulling the
+// larger of m00, m01 (g) out of the gate leaves one unit coefficient per
+// output: out0 = g (p0 + r0 q0), out1 = g (sigma p1 + r1 q1) with sigma = +-1
+// and |r| <= 1, which is two packed FMAs per amplitude pair instead of four
+// (real) or eight scalar FMAs (kind 2). The factors g of a pass multiply into
+// one scalar applied when the pass stores its tile. Non-unitary matrices
+// (Kraus operators of the shot engine) keep the plain form.
+struct Factored {
+    bool ok = false;
+    int pivot = 0;        // 0: output 0 pivots on x (|m00| >= |m01|); 1: on y
+    bool neg = false;     // sigma = -1
+    bool imag_r = false;  // r0, r1 purely imaginary (kind 2), else real
+    bool imag_g = false;  // g purely imaginary (kind 2 with pivot 1)
+    std::complex<double> g, r0, r1;
+};
+Factored factor_gate(const std::complex<double> m[4], int mk) {
+    Factored f;
+    if (mk != 1 && mk != 2) return f;
+    f.pivot = std::abs(m[0]) >= std::abs(m[1]) ? 0 : 1;
+    const std::complex<double> g = f.pivot ? m[1] : m[0];
+    const std::complex<double> h = f.pivot ? m[2] : m[3];
+    if (!(std::abs(g) > 1e-150)) return f;
+    const std::complex<double> sig = h / g;
+    if (std::abs(sig.imag()) > 1e-12 || std::abs(std::abs(sig.real()) - 1.0) > 1e-12) return f;
+    f.neg = sig.real() < 0.0;
+    f.g = g;
+    f.r0 = (f.pivot ? m[0] : m[1]) / g;
+    f.r1 = (f.pivot ? m[3] : m[2]) / g;
+    f.imag_r = mk == 2;
+    f.imag_g = mk == 2 && f.pivot == 1;
+    f.ok = true;
+    return f;
+}
+// the splatted constant of r: (r, r) when real, (-Im r, Im r) when imaginary
+std::complex<double> factored_const(const Factored &f, std::complex<double> r) {
+    return f.imag_r ? std::complex<double>(-r.imag(), r.imag()) : std::complex<double>(r.real(), r.real());
+}
+// structure code of a factored gate for the module cache key (0: plain form)
+uint8_t factored_code(const Factored &f) {
+    return f.ok ? (uint8_t)(1 + f.pivot + 2 * f.neg) : 0;
+}
+int slot_factored(Gen &g, const Factored &f) {
+    g.pscale *= f.g;
+    g.pscale_imag ^= f.imag_g;
+    g.any_scale = true;
+    return g.slot(factored_const(f, f.r0), factored_const(f, f.r1), 0.0, 0.0);
+}
+void emit_factored(Gen &g, int slot, const Factored &f, const std::string &A, const std::string &B) {
+    const std::string k0 = Mref(slot, 0), k1 = Mref(slot, 1);
+    auto S = [&](const char *v) { return f.imag_r ? std::string("make_float2(") + v + ".y," + v + ".x)" : std::string(v); };
+    auto N = [&](const char *v) { return f.neg ? std::string("make_float2(-") + v + ".x,-" + v + ".y)" : std::string(v); };
+    auto &s = g.s;
+    s << "{const float2 x=" << A << ",y=" << B << ";";
+    if (f.pivot == 0) {
+        s << A << "=qf_ffma2(" << k0 << "," << S("y") << ",x);";
+        s << B << "=qf_ffma2(" << k1 << "," << S("x") << "," << N("y") << ");";
+    } else {
+        s << A << "=qf_ffma2(" << k0 << "," << S("x") << ",y);";
+        s << B << "=qf_ffma2(" << k1 << "," << S("y") << "," << N("x") << ");";
+    }
+    s << "}\n";
+}
+
+// the pass factor as a packed multiplier: (G, G) when real, (-Im G, Im G) when imaginary
+std::complex<double> scale_const(const Gen &g) {
+    return g.pscale_imag ? std::complex<double>(-g.pscale.imag(), g.pscale.imag())
+                         : std::complex<double>(g.pscale.real(), g.pscale.real());
 }
 
 // One pass -> one kernel.
@@ -522,6 +602,7 @@ struct PassGen {
     void emit_kernel(int index, bool last_pass) {
         auto &s = g.s;
         for (int i = 0; i < kR; ++i) g.v[i] = i;
+        g.reset_scale();
         const std::string dep_t = deposit_code(p.a.nonlocal_mask, "t");
         const std::string dep_t2 = deposit_code(p.a.nonlocal_mask, "t2");
         if (dual && n_acc() > kMaxAcc) {
@@ -691,8 +772,11 @@ struct PassGen {
                 }
             } else {
                 const int mk = matrix_kind_of(m);
+                const Factored fg = dual ? Factored() : factor_gate(m, mk);
                 int sl;
-                if (mk == 1)  // splatted real entries for packed f32x2 arithmetic
+                if (fg.ok)
+                    sl = slot_factored(g, fg);
+                else if (mk == 1)  // splatted real entries for packed f32x2 arithmetic
                     sl = g.slot({m[0].real(), m[0].real()}, {m[1].real(), m[1].real()}, {m[2].real(), m[2].real()},
                                 {m[3].real(), m[3].real()});
                 else
@@ -701,7 +785,10 @@ struct PassGen {
                 for (int a = 0; a < n_arrays(); ++a) {
                     g.pfx = reg_pfx(a);
                     for (int i = 0; i < kR; ++i)
-                        if (!((i >> rb) & 1)) emit_mat2(g, sl, mk, g.R(i), g.R(i | (1 << rb)));
+                        if (!((i >> rb) & 1)) {
+                            if (fg.ok) emit_factored(g, sl, fg, g.R(i), g.R(i | (1 << rb)));
+                            else emit_mat2(g, sl, mk, g.R(i), g.R(i | (1 << rb)));
+                        }
                 }
             }
             break;
@@ -761,13 +848,21 @@ struct PassGen {
 
     void finish(bool last_pass, const std::string &dep_t2) {
         auto &s = g.s;
-        if (last_pass && g.any_diag) {  // the plan's global phase, once, at the very end
-            const int sl = g.slot(g.gphase, 0.0, 0.0, 0.0);
+        if (last_pass && g.any_diag) {  // the plan's global phase, once, at the very end (with this pass's factors)
+            const int sl = g.slot(g.gphase * g.pscale, 0.0, 0.0, 0.0);
             for (int a = 0; a < n_arrays(); ++a) {
                 g.pfx = reg_pfx(a);
                 for (int i = 0; i < kR; ++i) emit_cmul_const(g, g.R(i), sl, 0);
             }
             g.pfx = "r";
+        } else if (g.any_scale) {  // the factors pulled out of this pass's gates: real or imaginary
+            const int sl = g.slot(scale_const(g), 0.0, 0.0, 0.0);
+            const std::string f = Mref(sl, 0);
+            for (int i = 0; i < kR; ++i) {
+                const std::string R = g.R(i);
+                if (g.pscale_imag) s << R << "=qf_fmul2(" << f << ",make_float2(" << R << ".y," << R << ".x));\n";
+                else s << R << "=qf_fmul2(" << f << "," << R << ");\n";
+            }
         }
         const std::string prefetch = "{const unsigned long long t2 = t + gridDim.x; if (t2 < nt) {const unsigned long long tq = " +
                                      dep_t2 + ";\n";
@@ -954,6 +1049,10 @@ std::string plan_key(const Plan &plan, bool dual) {
                 mk = matrix_kind_of(m);
             }
             put(x.kind | (x.diag << 3) | (mk << 4), 1);
+            if (!dual && x.kind == BK_MAT1 && !x.diag) {
+                const std::complex<double> m[4] = {{x.m[0], x.m[1]}, {x.m[2], x.m[3]}, {x.m[4], x.m[5]}, {x.m[6], x.m[7]}};
+                put(factored_code(factor_gate(m, mk)), 1);
+            }
             put(x.q0, 1);
             put(x.q1, 1);
             if (x.kind == BK_OVL) {
@@ -967,13 +1066,15 @@ std::string plan_key(const Plan &plan, bool dual) {
 
 // The constant banks of modules generated for `plan`, rebuilt from the gates
 // in each pass's emission order exactly as emit_gate / finish allocate them.
-void replay_consts(const Plan &plan, const std::vector<std::vector<int>> &orders, std::vector<ModulePlan> &mods) {
+void replay_consts(const Plan &plan, const std::vector<std::vector<int>> &orders, std::vector<ModulePlan> &mods,
+                   bool dual) {
     Gen g;
     const size_t npass = plan.passes.size();
     for (ModulePlan &mp : mods) {
         g.consts.clear();
         for (int pi : mp.pass_index) {
             const Pass &p = plan.passes[pi];
+            g.reset_scale();
             for (int j : orders[pi]) {
                 const BGate &x = p.gates[j];
                 if (x.kind != BK_MAT1) continue;
@@ -983,14 +1084,20 @@ void replay_consts(const Plan &plan, const std::vector<std::vector<int>> &orders
                     g.gphase *= m[0];
                     const std::complex<double> f = m[3] / m[0];
                     g.slot(f, 0.0, 0.0, f);
-                } else if (matrix_kind_of(m) == 1) {
-                    g.slot({m[0].real(), m[0].real()}, {m[1].real(), m[1].real()}, {m[2].real(), m[2].real()},
-                           {m[3].real(), m[3].real()});
                 } else {
-                    g.slot(m[0], m[1], m[2], m[3]);
+                    const int mk = matrix_kind_of(m);
+                    const Factored fg = dual ? Factored() : factor_gate(m, mk);
+                    if (fg.ok)
+                        slot_factored(g, fg);
+                    else if (mk == 1)
+                        g.slot({m[0].real(), m[0].real()}, {m[1].real(), m[1].real()}, {m[2].real(), m[2].real()},
+                               {m[3].real(), m[3].real()});
+                    else
+                        g.slot(m[0], m[1], m[2], m[3]);
                 }
             }
-            if ((size_t)pi + 1 == npass && g.any_diag) g.slot(g.gphase, 0.0, 0.0, 0.0);
+            if ((size_t)pi + 1 == npass && g.any_diag) g.slot(g.gphase * g.pscale, 0.0, 0.0, 0.0);
+            else if (g.any_scale) g.slot(scale_const(g), 0.0, 0.0, 0.0);
         }
         mp.consts.clear();
         mp.consts.reserve(g.consts.size() * 2);
@@ -1062,7 +1169,7 @@ bool gen_modules(const Plan &plan, std::vector<ModulePlan> &mods, bool dual = fa
     }
     if (hit) {
         mods = hit->mods;
-        replay_consts(plan, hit->orders, mods);
+        replay_consts(plan, hit->orders, mods, dual);
         return true;
     }
     auto e = std::make_shared<GenEntry>();
