@@ -217,8 +217,10 @@ void emit_mat2(Gen &g, int slot, int mk, const std::string &A, const std::string
 // output: out0 = g (p0 + r0 q0), out1 = g (sigma p1 + r1 q1) with sigma = +-1
 // and |r| <= 1, which is two packed FMAs per amplitude pair instead of four
 // (real) or eight scalar FMAs (kind 2). The factors g of a pass multiply into
-// one scalar applied when the pass stores its tile. Non-unitary matrices
-// (Kraus operators of the shot engine) keep the plain form.
+// one scalar applied when the pass stores its tile; in the adjoint's dual
+// passes psi and lambda carry the same factor G, so an overlap read mid-pass
+// is scaled by |G|^2. Non-unitary matrices (Kraus operators of the shot
+// engine) keep the plain form.
 struct Factored {
     bool ok = false;
     int pivot = 0;        // 0: output 0 pivots on x (|m00| >= |m01|); 1: on y
@@ -743,6 +745,10 @@ struct PassGen {
                       << ".x + " << l1 << ".y * " << p0 << ".y);\n";
             }
         }
+        if (g.any_scale) {  // psi and lambda both carry the factor G pulled out so far: <l|P|p> scales by |G|^2
+            const int sl = g.slot(std::norm(g.pscale), 0.0, 0.0, 0.0);
+            s << "ov *= " << Mref(sl, 0) << ".x;\n";
+        }
         for (int o = 16; o >= 1; o >>= 1) s << "ov += __shfl_xor_sync(0xffffffffu, ov, " << o << ");\n";
         s << "if (lane == " << (ls & 31) << "u) acc" << (ls >> 5) << " += (double)ov;}\n";
     }
@@ -772,7 +778,7 @@ struct PassGen {
                 }
             } else {
                 const int mk = matrix_kind_of(m);
-                const Factored fg = dual ? Factored() : factor_gate(m, mk);
+                const Factored fg = factor_gate(m, mk);
                 int sl;
                 if (fg.ok)
                     sl = slot_factored(g, fg);
@@ -858,11 +864,15 @@ struct PassGen {
         } else if (g.any_scale) {  // the factors pulled out of this pass's gates: real or imaginary
             const int sl = g.slot(scale_const(g), 0.0, 0.0, 0.0);
             const std::string f = Mref(sl, 0);
-            for (int i = 0; i < kR; ++i) {
-                const std::string R = g.R(i);
-                if (g.pscale_imag) s << R << "=qf_fmul2(" << f << ",make_float2(" << R << ".y," << R << ".x));\n";
-                else s << R << "=qf_fmul2(" << f << "," << R << ");\n";
+            for (int a = 0; a < n_arrays(); ++a) {  // psi and lambda went through the same gates
+                g.pfx = reg_pfx(a);
+                for (int i = 0; i < kR; ++i) {
+                    const std::string R = g.R(i);
+                    if (g.pscale_imag) s << R << "=qf_fmul2(" << f << ",make_float2(" << R << ".y," << R << ".x));\n";
+                    else s << R << "=qf_fmul2(" << f << "," << R << ");\n";
+                }
             }
+            g.pfx = "r";
         }
         const std::string prefetch = "{const unsigned long long t2 = t + gridDim.x; if (t2 < nt) {const unsigned long long tq = " +
                                      dep_t2 + ";\n";
@@ -1049,7 +1059,7 @@ std::string plan_key(const Plan &plan, bool dual) {
                 mk = matrix_kind_of(m);
             }
             put(x.kind | (x.diag << 3) | (mk << 4), 1);
-            if (!dual && x.kind == BK_MAT1 && !x.diag) {
+            if (x.kind == BK_MAT1 && !x.diag) {
                 const std::complex<double> m[4] = {{x.m[0], x.m[1]}, {x.m[2], x.m[3]}, {x.m[4], x.m[5]}, {x.m[6], x.m[7]}};
                 put(factored_code(factor_gate(m, mk)), 1);
             }
@@ -1066,8 +1076,7 @@ std::string plan_key(const Plan &plan, bool dual) {
 
 // The constant banks of modules generated for `plan`, rebuilt from the gates
 // in each pass's emission order exactly as emit_gate / finish allocate them.
-void replay_consts(const Plan &plan, const std::vector<std::vector<int>> &orders, std::vector<ModulePlan> &mods,
-                   bool dual) {
+void replay_consts(const Plan &plan, const std::vector<std::vector<int>> &orders, std::vector<ModulePlan> &mods) {
     Gen g;
     const size_t npass = plan.passes.size();
     for (ModulePlan &mp : mods) {
@@ -1077,6 +1086,7 @@ void replay_consts(const Plan &plan, const std::vector<std::vector<int>> &orders
             g.reset_scale();
             for (int j : orders[pi]) {
                 const BGate &x = p.gates[j];
+                if (x.kind == BK_OVL && g.any_scale) g.slot(std::norm(g.pscale), 0.0, 0.0, 0.0);
                 if (x.kind != BK_MAT1) continue;
                 const std::complex<double> m[4] = {{x.m[0], x.m[1]}, {x.m[2], x.m[3]}, {x.m[4], x.m[5]}, {x.m[6], x.m[7]}};
                 if (x.diag) {
@@ -1086,7 +1096,7 @@ void replay_consts(const Plan &plan, const std::vector<std::vector<int>> &orders
                     g.slot(f, 0.0, 0.0, f);
                 } else {
                     const int mk = matrix_kind_of(m);
-                    const Factored fg = dual ? Factored() : factor_gate(m, mk);
+                    const Factored fg = factor_gate(m, mk);
                     if (fg.ok)
                         slot_factored(g, fg);
                     else if (mk == 1)
@@ -1169,7 +1179,7 @@ bool gen_modules(const Plan &plan, std::vector<ModulePlan> &mods, bool dual = fa
     }
     if (hit) {
         mods = hit->mods;
-        replay_consts(plan, hit->orders, mods, dual);
+        replay_consts(plan, hit->orders, mods);
         return true;
     }
     auto e = std::make_shared<GenEntry>();
