@@ -109,6 +109,29 @@ def test_plan_fuses_a_random_circuit(engine_lib):
     assert counts == sorted(counts, reverse=True), counts
 
 
+def test_lookahead_residency_needs_fewer_passes_than_first_come(engine_lib):
+    """The 30-qubit depth-40 headline circuit on 12-qubit tiles: 52 passes when
+    each pass's resident qubits are chosen by look-ahead, 74 first-come."""
+    ops = W.random_circuit(30, 40, 1, two_qubit="mixed")
+    npass = C.c_uint64()
+    counts = {}
+    for flags, name in ((0, "lookahead"), (A.EXEC_FLAG_PLAN_FIRST_COME, "first_come")):
+        o = A.ExecOpts(A.EXEC_AUTO, 12, 0, flags)
+        ng = C.c_uint64()
+        assert engine_lib.qf_plan_stats(30, A.C64, _native.ptr(ops), len(ops), None, 0, None, 0, C.byref(o),
+                                        C.byref(npass), C.byref(ng)) == 0
+        counts[name] = npass.value
+    assert counts == {"lookahead": 52, "first_come": 74}
+    for seed in (2, 3):
+        ops = W.random_circuit(26, 30, seed, two_qubit="mixed")
+        la = plan_stats(engine_lib, 26, ops)[1]
+        o = A.ExecOpts(A.EXEC_AUTO, 0, 0, A.EXEC_FLAG_PLAN_FIRST_COME)
+        ng = C.c_uint64()
+        engine_lib.qf_plan_stats(26, A.C64, _native.ptr(ops), len(ops), None, 0, None, 0, C.byref(o), C.byref(npass),
+                                 C.byref(ng))
+        assert la < npass.value, (seed, la, npass.value)
+
+
 def test_plan_small_state_is_one_pass(engine_lib):
     ops = W.random_circuit(10, 20, 3, two_qubit="mixed")
     st, npass, _ = plan_stats(engine_lib, 10, ops)
