@@ -128,10 +128,12 @@ struct Gen {
     std::complex<double> pscale{1.0, 0.0};
     bool pscale_imag = false;  // an odd number of imaginary factors
     bool any_scale = false;
+    int n_factored = 0;  // factors in pscale: each |g| >= 1/sqrt(2), so 96 keep |pscale| >= 2^-48
     void reset_scale() {
         pscale = {1.0, 0.0};
         pscale_imag = false;
         any_scale = false;
+        n_factored = 0;
     }
     int tmp = 0;
 
@@ -255,8 +257,15 @@ std::complex<double> factored_const(const Factored &f, std::complex<double> r) {
 uint8_t factored_code(const Factored &f) {
     return f.ok ? (uint8_t)(1 + f.pivot + 2 * f.neg) : 0;
 }
+// Factors pulled out before the tile values are rescaled mid-pass: 96 of them
+// keep the amplitudes below 2^48 times their size and the scale above 2^-48,
+// far inside float32's range, however deep a pass is (a pass holds up to 768
+// gates).
+constexpr int kMaxFactors = 96;
+
 int slot_factored(Gen &g, const Factored &f) {
     g.pscale *= f.g;
+    ++g.n_factored;
     g.pscale_imag ^= f.imag_g;
     g.any_scale = true;
     return g.slot(factored_const(f, f.r0), factored_const(f, f.r1), 0.0, 0.0);
@@ -779,6 +788,7 @@ struct PassGen {
             } else {
                 const int mk = matrix_kind_of(m);
                 const Factored fg = factor_gate(m, mk);
+                if (fg.ok && g.n_factored >= kMaxFactors) emit_scale();
                 int sl;
                 if (fg.ok)
                     sl = slot_factored(g, fg);
@@ -852,6 +862,24 @@ struct PassGen {
         g.pfx = "r";
     }
 
+    // multiply the tile (psi and lambda alike) by the factors pulled out so
+    // far, a real or an imaginary scalar, and start a new product
+    void emit_scale() {
+        auto &s = g.s;
+        const int sl = g.slot(scale_const(g), 0.0, 0.0, 0.0);
+        const std::string f = Mref(sl, 0);
+        for (int a = 0; a < n_arrays(); ++a) {
+            g.pfx = reg_pfx(a);
+            for (int i = 0; i < kR; ++i) {
+                const std::string R = g.R(i);
+                if (g.pscale_imag) s << R << "=qf_fmul2(" << f << ",make_float2(" << R << ".y," << R << ".x));\n";
+                else s << R << "=qf_fmul2(" << f << "," << R << ");\n";
+            }
+        }
+        g.pfx = "r";
+        g.reset_scale();
+    }
+
     void finish(bool last_pass, const std::string &dep_t2) {
         auto &s = g.s;
         if (last_pass && g.any_diag) {  // the plan's global phase, once, at the very end (with this pass's factors)
@@ -861,18 +889,8 @@ struct PassGen {
                 for (int i = 0; i < kR; ++i) emit_cmul_const(g, g.R(i), sl, 0);
             }
             g.pfx = "r";
-        } else if (g.any_scale) {  // the factors pulled out of this pass's gates: real or imaginary
-            const int sl = g.slot(scale_const(g), 0.0, 0.0, 0.0);
-            const std::string f = Mref(sl, 0);
-            for (int a = 0; a < n_arrays(); ++a) {  // psi and lambda went through the same gates
-                g.pfx = reg_pfx(a);
-                for (int i = 0; i < kR; ++i) {
-                    const std::string R = g.R(i);
-                    if (g.pscale_imag) s << R << "=qf_fmul2(" << f << ",make_float2(" << R << ".y," << R << ".x));\n";
-                    else s << R << "=qf_fmul2(" << f << "," << R << ");\n";
-                }
-            }
-            g.pfx = "r";
+        } else if (g.any_scale) {  // the factors pulled out of this pass's gates
+            emit_scale();
         }
         const std::string prefetch = "{const unsigned long long t2 = t + gridDim.x; if (t2 < nt) {const unsigned long long tq = " +
                                      dep_t2 + ";\n";
@@ -1097,6 +1115,10 @@ void replay_consts(const Plan &plan, const std::vector<std::vector<int>> &orders
                 } else {
                     const int mk = matrix_kind_of(m);
                     const Factored fg = factor_gate(m, mk);
+                    if (fg.ok && g.n_factored >= kMaxFactors) {
+                        g.slot(scale_const(g), 0.0, 0.0, 0.0);
+                        g.reset_scale();
+                    }
                     if (fg.ok)
                         slot_factored(g, fg);
                     else if (mk == 1)

@@ -646,6 +646,51 @@ def test_compiled_13_qubit_tiles_match_oracle(backend, n, seed, kinds):
         assert close(sv.amplitudes(), expected, C64_TOL), trial
 
 
+@pytest.mark.parametrize("dual", [False, True])
+def test_compiled_pass_with_hundreds_of_factored_gates(backend, dual):
+    """A pass of 768 gates on 12 qubits (60 layers of RY/RX and a CNOT chain):
+    the scale pulled out of ~400 unitary gates is applied every 96 of them, so
+    float32 neither overflows nor underflows. Forward against the oracle; the
+    adjoint's dual passes against the oracle's parameter shift."""
+    r = np.random.default_rng(77)
+    n, layers = 14, 60
+    if not dual:
+        recs = []
+        for layer in range(layers):
+            g = A.GATE_RY if layer % 2 == 0 else A.GATE_RX
+            recs += [(A.OP_GATE, g, q, 0, 0, float(r.uniform(1.2, 1.9))) for q in range(12)]
+            recs += [(A.OP_CNOT, 0, q, q + 1, 0, 0.0) for q in range(11)]
+        ops = A.ops_array(recs)
+        sv = StateVector.zero(n, dtype="c64", backend=backend)
+        sv.apply_ops(ops, exec_opts={"jit": True})
+        got = sv.amplitudes()
+        assert np.isfinite(got).all()
+        assert close(got, O.run(ops, n), 2e-5)
+        return
+    from quantumforge_gb300 import ParameterizedCircuit, RotationAxis
+    from quantumforge_gb300.gradients import GradientOptions, GradientStrategy, gradient_with_inputs
+
+    pc = ParameterizedCircuit(24)
+    for layer in range(20):  # 240 rotations + their overlaps + 220 CNOTs: one backward pass
+        for q in range(12):
+            pc.rotation(RotationAxis.Y if layer % 2 == 0 else RotationAxis.X, q, (layer * 12 + q) % 24)
+        for q in range(11):
+            pc.cnot(q, q + 1)
+    params = r.uniform(1.2, 1.9, 24)
+    n = 12  # one 4096-amplitude tile keeps the oracle's 480 shifted runs short
+    H = PauliSum()
+    H.add_term(0, 1 | (1 << 11), 1.0)
+    H.add_term(1 << 3, 0, 0.5)
+    est = gradient_with_inputs(pc, GradientOptions(strategy=GradientStrategy.Adjoint), [], params, n, H, dtype="c64",
+                               backend=backend, exec_opts={"jit": True})
+    want = O.parameter_shift(pc.ops(), n, params, A.terms_array([(0, 1 | (1 << 11), 1.0), (1 << 3, 0, 0.5)]), threads=8)
+    smem = gradient_with_inputs(pc, GradientOptions(strategy=GradientStrategy.Adjoint), [], params, n, H, dtype="c64",
+                                backend=backend, exec_opts={"jit": False})
+    assert np.isfinite(est.gradient).all()
+    assert np.abs(est.gradient - want).max() < 2e-4
+    assert np.abs(est.gradient - smem.gradient).max() < 2e-4
+
+
 def test_state_outliving_its_context_is_released_safely(engine_lib):
     from quantumforge_gb300 import CudaBackend
 
