@@ -234,6 +234,9 @@ struct Factored {
 Factored factor_gate(const std::complex<double> m[4], int mk) {
     Factored f;
     if (mk != 1 && mk != 2) return f;
+    // unit rows: |g| >= 1/sqrt(2), which bounds the product of a pass's factors
+    if (std::abs(std::norm(m[0]) + std::norm(m[1]) - 1.0) > 1e-9 || std::abs(std::norm(m[2]) + std::norm(m[3]) - 1.0) > 1e-9)
+        return f;
     f.pivot = std::abs(m[0]) >= std::abs(m[1]) ? 0 : 1;
     const std::complex<double> g = f.pivot ? m[1] : m[0];
     const std::complex<double> h = f.pivot ? m[2] : m[3];
