@@ -219,7 +219,11 @@ void emit_mat2(Gen &g, int slot, int mk, const std::string &A, const std::string
 // output: out0 = g (p0 + r0 q0), out1 = g (sigma p1 + r1 q1) with sigma = +-1
 // and |r| <= 1, which is two packed FMAs per amplitude pair instead of four
 // (real) or eight scalar FMAs (kind 2). The factors g of a pass multiply into
-// one scalar applied when the pass stores its tile; in the adjoint's dual
+// one scalar applied when the pass stores its tile. The pivot choice is part of
+// a module's structure, so gates whose matrices come from circuit parameters
+// or encoded inputs (they change between calls: training steps, shifted
+// evaluations) keep the plain form and new angles never recompile. In the
+// adjoint's dual
 // passes psi and lambda carry the same factor G, so an overlap read mid-pass
 // is scaled by |G|^2. Non-unitary matrices (Kraus operators of the shot
 // engine) keep the plain form.
@@ -790,7 +794,7 @@ struct PassGen {
                 }
             } else {
                 const int mk = matrix_kind_of(m);
-                const Factored fg = factor_gate(m, mk);
+                const Factored fg = x.varying ? Factored() : factor_gate(m, mk);
                 if (fg.ok && g.n_factored >= kMaxFactors) emit_scale();
                 int sl;
                 if (fg.ok)
@@ -1082,7 +1086,7 @@ std::string plan_key(const Plan &plan, bool dual) {
             put(x.kind | (x.diag << 3) | (mk << 4), 1);
             if (x.kind == BK_MAT1 && !x.diag) {
                 const std::complex<double> m[4] = {{x.m[0], x.m[1]}, {x.m[2], x.m[3]}, {x.m[4], x.m[5]}, {x.m[6], x.m[7]}};
-                put(factored_code(factor_gate(m, mk)), 1);
+                put(x.varying ? 0 : factored_code(factor_gate(m, mk)), 1);
             }
             put(x.q0, 1);
             put(x.q1, 1);
@@ -1117,7 +1121,7 @@ void replay_consts(const Plan &plan, const std::vector<std::vector<int>> &orders
                     g.slot(f, 0.0, 0.0, f);
                 } else {
                     const int mk = matrix_kind_of(m);
-                    const Factored fg = factor_gate(m, mk);
+                    const Factored fg = x.varying ? Factored() : factor_gate(m, mk);
                     if (fg.ok && g.n_factored >= kMaxFactors) {
                         g.slot(scale_const(g), 0.0, 0.0, 0.0);
                         g.reset_scale();

@@ -88,6 +88,7 @@ int bind_ops(uint32_t n, const qf_op *ops, uint64_t n_ops, const double *params,
             } else {
                 if (op.gate > QF_PAULI_Z) return fail(QF_ERR_INVALID_ARGUMENT, "rotation axis %u is invalid", op.gate);
                 gate = rotation_gate(op.gate);
+                g.varying = 1;
                 if (op.kind == QF_OP_ROTATION) {
                     if (op.param >= n_params)
                         return fail(QF_ERR_INVALID_PARAMETER_COUNT, "expected %llu circuit parameters, got %llu",
@@ -325,6 +326,7 @@ int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, 
                     double c[8];
                     mat_mul(it.g.m, taken[prev].g.m, c);
                     std::memcpy(taken[prev].g.m, c, sizeof c);
+                    taken[prev].g.varying |= it.g.varying;
                     taken[prev].g.diag = matrix_is_diag(c);
                     taken[prev].g.op_index = -1;
                     continue;

@@ -101,7 +101,7 @@ struct BGate {
     uint8_t kind = BK_MAT1;
     uint8_t diag = 0;        // MAT1 only: m01 == m10 == 0
     uint8_t axis = 255;      // rotation occurrence: generator axis (QF_PAULI_*), else 255
-    uint8_t pad = 0;
+    uint8_t varying = 0;     // matrix from a circuit parameter or an encoded input (changes between calls)
     uint32_t q0 = 0, q1 = 0;
     int64_t op_index = -1;   // index into the caller's op list
     int64_t param = -1;      // parameter index of a rotation occurrence

@@ -651,7 +651,8 @@ def test_compiled_pass_with_hundreds_of_factored_gates(backend, dual):
     """A pass of 768 gates on 12 qubits (60 layers of RY/RX and a CNOT chain):
     the scale pulled out of ~400 unitary gates is applied every 96 of them, so
     float32 neither overflows nor underflows. Forward against the oracle; the
-    adjoint's dual passes against the oracle's parameter shift."""
+    adjoint's dual passes (overlaps scaled by |G|^2) against the oracle's
+    parameter shift."""
     r = np.random.default_rng(77)
     n, layers = 14, 60
     if not dual:
@@ -670,14 +671,22 @@ def test_compiled_pass_with_hundreds_of_factored_gates(backend, dual):
     from quantumforge_gb300 import ParameterizedCircuit, RotationAxis
     from quantumforge_gb300.gradients import GradientOptions, GradientStrategy, gradient_with_inputs
 
+    # fixed-angle RY/RX gates (factored; parameterised rotations keep the plain
+    # form) between CNOT chains and the trainable rotations: 10 layers of 58
+    # items (120 factored gates, 120 overlap slots) make one backward pass
     pc = ParameterizedCircuit(24)
-    for layer in range(20):  # 240 rotations + their overlaps + 220 CNOTs: one backward pass
+    for layer in range(10):
+        fixed = A.GATE_RY if layer % 2 == 0 else A.GATE_RX
+        for q in range(12):
+            pc.operations.append((A.OP_GATE, fixed, q, 0, 0, float(r.uniform(1.2, 1.9))))
+        for q in range(11):
+            pc.cnot(q, q + 1)
         for q in range(12):
             pc.rotation(RotationAxis.Y if layer % 2 == 0 else RotationAxis.X, q, (layer * 12 + q) % 24)
         for q in range(11):
             pc.cnot(q, q + 1)
     params = r.uniform(1.2, 1.9, 24)
-    n = 12  # one 4096-amplitude tile keeps the oracle's 480 shifted runs short
+    n = 12  # one 4096-amplitude tile keeps the oracle's 240 shifted runs short
     H = PauliSum()
     H.add_term(0, 1 | (1 << 11), 1.0)
     H.add_term(1 << 3, 0, 0.5)
