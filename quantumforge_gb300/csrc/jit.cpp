@@ -213,48 +213,19 @@ void emit_mat2(Gen &g, int slot, int mk, const std::string &A, const std::string
     s << "}\n";
 }
 
-// A unitary 2x2 whose entries are real (kind 1) or real on the diagonal and
-// imaginary off it (kind 2) has |m00| = |m11| and |m01| = |m10|. Pulling the
-// larger of m00, m01 (g) out of the gate leaves one unit coefficient per
-// output: out0 = g (p0 + r0 q0), out1 = g (sigma p1 + r1 q1) with sigma = +-1
-// and |r| <= 1, which is two packed FMAs per amplitude pair instead of four
-// (real) or eight scalar FMAs (kind 2). The factors g of a pass multiply into
+// Gates factored as out0 = g (p0 + r0 q0), out1 = g (sigma p1 + r1 q1)
+// (factor_unitary_2x2) take two packed FMAs per amplitude pair instead of four
+// (real) or eight scalar FMAs (RX type). The factors g of a pass multiply into
 // one scalar applied when the pass stores its tile. The pivot choice is part of
 // a module's structure, so gates whose matrices come from circuit parameters
 // or encoded inputs (they change between calls: training steps, shifted
 // evaluations) keep the plain form and new angles never recompile. In the
-// adjoint's dual
-// passes psi and lambda carry the same factor G, so an overlap read mid-pass
-// is scaled by |G|^2. Non-unitary matrices (Kraus operators of the shot
-// engine) keep the plain form.
-struct Factored {
-    bool ok = false;
-    int pivot = 0;        // 0: output 0 pivots on x (|m00| >= |m01|); 1: on y
-    bool neg = false;     // sigma = -1
-    bool imag_r = false;  // r0, r1 purely imaginary (kind 2), else real
-    bool imag_g = false;  // g purely imaginary (kind 2 with pivot 1)
-    std::complex<double> g, r0, r1;
-};
-Factored factor_gate(const std::complex<double> m[4], int mk) {
-    Factored f;
-    if (mk != 1 && mk != 2) return f;
-    // unit rows: |g| >= 1/sqrt(2), which bounds the product of a pass's factors
-    if (std::abs(std::norm(m[0]) + std::norm(m[1]) - 1.0) > 1e-9 || std::abs(std::norm(m[2]) + std::norm(m[3]) - 1.0) > 1e-9)
-        return f;
-    f.pivot = std::abs(m[0]) >= std::abs(m[1]) ? 0 : 1;
-    const std::complex<double> g = f.pivot ? m[1] : m[0];
-    const std::complex<double> h = f.pivot ? m[2] : m[3];
-    if (!(std::abs(g) > 1e-150)) return f;
-    const std::complex<double> sig = h / g;
-    if (std::abs(sig.imag()) > 1e-12 || std::abs(std::abs(sig.real()) - 1.0) > 1e-12) return f;
-    f.neg = sig.real() < 0.0;
-    f.g = g;
-    f.r0 = (f.pivot ? m[0] : m[1]) / g;
-    f.r1 = (f.pivot ? m[3] : m[2]) / g;
-    f.imag_r = mk == 2;
-    f.imag_g = mk == 2 && f.pivot == 1;
-    f.ok = true;
-    return f;
+// adjoint's dual passes psi and lambda carry the same factor G, so an overlap
+// read mid-pass is scaled by |G|^2.
+Factored factor_gate(const std::complex<double> m[4], int) {
+    const double d[8] = {m[0].real(), m[0].imag(), m[1].real(), m[1].imag(),
+                         m[2].real(), m[2].imag(), m[3].real(), m[3].imag()};
+    return factor_unitary_2x2(d);
 }
 // the splatted constant of r: (r, r) when real, (-Im r, Im r) when imaginary
 std::complex<double> factored_const(const Factored &f, std::complex<double> r) {

@@ -149,6 +149,32 @@ BGate inverse_gate(const BGate &g) {
     return r;
 }
 
+Factored factor_unitary_2x2(const double md[8]) {
+    Factored f;
+    const std::complex<double> m[4] = {{md[0], md[1]}, {md[2], md[3]}, {md[4], md[5]}, {md[6], md[7]}};
+    bool real = true;
+    for (int k = 0; k < 4; ++k) real = real && m[k].imag() == 0.0;
+    const bool xlike = !real && m[0].imag() == 0 && m[3].imag() == 0 && m[1].real() == 0 && m[2].real() == 0;
+    if (!real && !xlike) return f;
+    // unit rows: |g| >= 1/sqrt(2), which bounds the product of a pass's factors
+    if (std::abs(std::norm(m[0]) + std::norm(m[1]) - 1.0) > 1e-9 || std::abs(std::norm(m[2]) + std::norm(m[3]) - 1.0) > 1e-9)
+        return f;
+    f.pivot = std::abs(m[0]) >= std::abs(m[1]) ? 0 : 1;
+    const std::complex<double> g = f.pivot ? m[1] : m[0];
+    const std::complex<double> h = f.pivot ? m[2] : m[3];
+    if (!(std::abs(g) > 1e-150)) return f;
+    const std::complex<double> sig = h / g;
+    if (std::abs(sig.imag()) > 1e-12 || std::abs(std::abs(sig.real()) - 1.0) > 1e-12) return f;
+    f.neg = sig.real() < 0.0;
+    f.g = g;
+    f.r0 = (f.pivot ? m[0] : m[1]) / g;
+    f.r1 = (f.pivot ? m[3] : m[2]) / g;
+    f.imag_r = xlike;
+    f.imag_g = xlike && f.pivot == 1;
+    f.ok = true;
+    return f;
+}
+
 // c = a * b for 2x2 complex (row-major, interleaved).
 static void mat_mul(const double a[8], const double b[8], double c[8]) {
     for (int i = 0; i < 2; ++i)
@@ -366,6 +392,22 @@ int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, 
         p.op_begin = (uint32_t)plan.ops.size();
         p.mat_begin = (uint32_t)(plan.mats.size() / 8);
         p.a.slot_base = plan.n_slots;
+        // factors pulled out of T_MAT1F gates (forward plans), applied by a
+        // T_SCALE op at the end of the pass, or earlier once they get small
+        std::complex<double> pscale(1.0, 0.0);
+        bool any_factored = false;
+        auto push_scale = [&]() {
+            TileOp sc;
+            std::memset(&sc, 0, sizeof sc);
+            sc.slot = -1;
+            sc.kind = T_SCALE;
+            sc.mat = (uint32_t)(plan.mats.size() / 8) - p.mat_begin;
+            const double e[8] = {pscale.real(), pscale.imag(), 0, 0, 0, 0, 0, 0};
+            plan.mats.insert(plan.mats.end(), e, e + 8);
+            plan.ops.push_back(sc);
+            pscale = 1.0;
+            any_factored = false;
+        };
         for (const Item &it : taken) {
             TileOp t;
             std::memset(&t, 0, sizeof t);
@@ -390,6 +432,19 @@ int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, 
             p.gates.push_back(g);
             switch (g.kind) {
             case BK_MAT1: {
+                const Factored f = (!g.diag && !o.backward) ? factor_unitary_2x2(g.m) : Factored();
+                if (f.ok) {
+                    if (std::abs(pscale) < 0x1p-40) push_scale();  // keep float32 tiles far from overflow
+                    t.mat = (uint32_t)(plan.mats.size() / 8) - p.mat_begin;
+                    const double e[8] = {f.r0.real(), f.r0.imag(), f.r1.real(), f.r1.imag(), 0, 0, 0, 0};
+                    plan.mats.insert(plan.mats.end(), e, e + 8);
+                    t.kind = T_MAT1F;
+                    t.b0 = (uint8_t)lb0;
+                    t.b1 = (uint8_t)(f.pivot | (f.neg ? 2 : 0) | (f.imag_r ? 4 : 0));
+                    pscale *= f.g;
+                    any_factored = true;
+                    break;
+                }
                 t.mat = (uint32_t)(plan.mats.size() / 8) - p.mat_begin;
                 plan.mats.insert(plan.mats.end(), g.m, g.m + 8);
                 if (!g.diag) { t.kind = T_MAT1; t.b0 = (uint8_t)lb0; }
@@ -413,6 +468,7 @@ int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, 
             }
             plan.ops.push_back(t);
         }
+        if (any_factored) push_scale();
         p.a.n_ops = (uint32_t)plan.ops.size() - p.op_begin;
         p.a.n_mats = (uint32_t)(plan.mats.size() / 8) - p.mat_begin;
         p.a.n_slots = plan.n_slots - p.a.slot_base;

@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <complex>
 #include <cstdint>
 #include <set>
 #include <string>
@@ -120,6 +121,22 @@ int bind_ops(uint32_t n, const qf_op *ops, uint64_t n_ops, const double *params,
 // The inverse of a bound gate (U^dagger).
 BGate inverse_gate(const BGate &g);
 
+// A unitary 2x2 whose entries are real (kind 1) or real on the diagonal and
+// imaginary off it (kind 2) has |m00| = |m11| and |m01| = |m10|. Pulling the
+// larger of m00, m01 (g) out of the gate leaves one unit coefficient per
+// output: out0 = g (p0 + r0 q0), out1 = g (sigma p1 + r1 q1) with sigma = +-1
+// and |r| <= 1 — half the multiplies of the plain form. ok = false for other
+// matrices (general complex, non-unitary Kraus operators).
+struct Factored {
+    bool ok = false;
+    int pivot = 0;        // 0: output 0 pivots on x (|m00| >= |m01|); 1: on y
+    bool neg = false;     // sigma = -1
+    bool imag_r = false;  // r0, r1 purely imaginary (kind 2), else real
+    bool imag_g = false;  // g purely imaginary (kind 2 with pivot 1)
+    std::complex<double> g, r0, r1;
+};
+Factored factor_unitary_2x2(const double m[8]);
+
 // ---- tile-pass plans --------------------------------------------------------
 enum TKind : uint8_t {
     T_MAT1 = 0,     // dense 2x2 on local bit b0
@@ -134,7 +151,10 @@ enum TKind : uint8_t {
     T_OVL_X = 9,    // adjoint overlap Im<lambda|X_b0 psi>, slot
     T_OVL_Y = 10,   // adjoint overlap Im<lambda|Y_b0 psi>
     T_OVL_ZL = 11,  // adjoint overlap Im<lambda|Z_b0 psi>, b0 local
-    T_OVL_ZG = 12   // adjoint overlap with Z on non-local g0
+    T_OVL_ZG = 12,  // adjoint overlap with Z on non-local g0
+    T_MAT1F = 13,   // factored unitary on local bit b0: mats[mat] = (r0, r1, -, -); b1 bit 0 pivot, bit 1 sigma < 0,
+                    // bit 2 r imaginary
+    T_SCALE = 14    // every amplitude times mats[mat].m00 (the factors pulled out by T_MAT1F)
 };
 
 struct TileOp {

@@ -275,6 +275,31 @@ __device__ __forceinline__ void tile_store(const C *s, C *__restrict__ g, uint64
     }
 }
 
+// A factored unitary (T_MAT1F): out0 = P + r0 Q, out1 = sigma Q + r1 P with
+// (P, Q) = (x, y) for pivot 0 and (y, x) for pivot 1, r real or imaginary;
+// the pass's factor comes with T_SCALE.
+template <typename C, bool PIV, bool NEG, bool IM>
+__device__ __forceinline__ void mat1f_pair(C *s, uint32_t i0, uint32_t i1, C r0, C r1) {
+    const C x = s[i0], y = s[i1];
+    const C P = PIV ? y : x, Q = PIV ? x : y;
+    const C sq = NEG ? mk(-Q.x, -Q.y) : Q;
+    if (IM) {  // r = i rho: r v = (-rho v.y, rho v.x)
+        s[i0] = mk(P.x - r0.y * Q.y, P.y + r0.y * Q.x);
+        s[i1] = mk(sq.x - r1.y * P.y, sq.y + r1.y * P.x);
+    } else {
+        s[i0] = mk(P.x + r0.x * Q.x, P.y + r0.x * Q.y);
+        s[i1] = mk(sq.x + r1.x * P.x, sq.y + r1.x * P.y);
+    }
+}
+template <typename C, bool DUAL, bool PIV, bool NEG, bool IM>
+__device__ __forceinline__ void mat1f_tile(C *s0, C *s1, uint32_t b, C r0, C r1, uint32_t T) {
+    for (uint32_t p = threadIdx.x; p < (T >> 1); p += blockDim.x) {
+        const uint32_t i0 = insert0_32(p, b), i1 = i0 | (1u << b);
+        mat1f_pair<C, PIV, NEG, IM>(s0, i0, i1, r0, r1);
+        if (DUAL) mat1f_pair<C, PIV, NEG, IM>(s1, i0, i1, r0, r1);
+    }
+}
+
 template <typename C, bool DUAL>
 __device__ __forceinline__ void tile_apply(const TileOp &op, C *s0, C *s1, const C *mats, uint64_t base,
                                            uint32_t T) {
@@ -326,6 +351,28 @@ __device__ __forceinline__ void tile_apply(const TileOp &op, C *s0, C *s1, const
                     s1[i1] = cmac2(m10, c0, m11, c1);
                 }
             }
+        }
+        break;
+    }
+    case T_MAT1F: {
+        const C r0 = mats[4 * op.mat], r1 = mats[4 * op.mat + 1];
+        switch (op.b1 & 7u) {
+        case 0: mat1f_tile<C, DUAL, false, false, false>(s0, s1, op.b0, r0, r1, T); break;
+        case 1: mat1f_tile<C, DUAL, true, false, false>(s0, s1, op.b0, r0, r1, T); break;
+        case 2: mat1f_tile<C, DUAL, false, true, false>(s0, s1, op.b0, r0, r1, T); break;
+        case 3: mat1f_tile<C, DUAL, true, true, false>(s0, s1, op.b0, r0, r1, T); break;
+        case 4: mat1f_tile<C, DUAL, false, false, true>(s0, s1, op.b0, r0, r1, T); break;
+        case 5: mat1f_tile<C, DUAL, true, false, true>(s0, s1, op.b0, r0, r1, T); break;
+        case 6: mat1f_tile<C, DUAL, false, true, true>(s0, s1, op.b0, r0, r1, T); break;
+        default: mat1f_tile<C, DUAL, true, true, true>(s0, s1, op.b0, r0, r1, T); break;
+        }
+        break;
+    }
+    case T_SCALE: {
+        const C f = mats[4 * op.mat];
+        for (uint32_t i = threadIdx.x; i < T; i += blockDim.x) {
+            s0[i] = cmul(s0[i], f);
+            if (DUAL) s1[i] = cmul(s1[i], f);
         }
         break;
     }
@@ -483,7 +530,7 @@ __global__ void __launch_bounds__(kThreads)
         __syncthreads();
         for (uint32_t o = 0; o < pa.n_ops; ++o) {
             const TileOp op = ops[o];
-            if (op.kind >= T_OVL_X) {
+            if (op.kind >= T_OVL_X && op.kind <= T_OVL_ZG) {
                 if (DUAL) {
                     const double v = block_sum(tile_overlap(op, s0, s1, base, T), red);
                     if (threadIdx.x == 0) acc[op.slot - (int32_t)pa.slot_base] += v;
