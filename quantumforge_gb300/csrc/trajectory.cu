@@ -28,7 +28,7 @@ namespace qf {
 namespace {
 
 enum : uint8_t { T_GATE = 0, T_CNOT = 1, T_CZ = 2, T_SWAP = 3, T_MEASURE = 4, T_COND = 5, T_DEP = 6, T_AD = 7, T_PD = 8,
-                 T_TH = 9, T_DIAG = 10, T_REAL = 11, T_X = 12 };
+                 T_TH = 9, T_DIAG = 10, T_REAL = 11, T_X = 12, T_XLIKE = 13 };
 
 // One op of a trajectory program. GATE/COND: m = the 2x2 matrix (re, im),
 // mf the same in f32 for complex64 states; channels: m[0] = probability /
@@ -100,7 +100,7 @@ __global__ void __launch_bounds__(256) k_trajectories(const C *__restrict__ init
             const uint32_t q = op.q0;
             const uint32_t qm = 1u << q;
             if (kind == T_COND && ((reg >> op.cbit) & 1ULL) != (uint64_t)op.value) continue;
-            if (kind == T_GATE || kind == T_COND || kind == T_DIAG || kind == T_REAL) {
+            if (kind == T_GATE || kind == T_COND || kind == T_DIAG || kind == T_REAL || kind == T_XLIKE) {
                 C m00, m01, m10, m11;
                 if (kF32) {
                     m00 = mk((R)op.mf[0], (R)op.mf[1]), m01 = mk((R)op.mf[2], (R)op.mf[3]);
@@ -117,6 +117,13 @@ __global__ void __launch_bounds__(256) k_trajectories(const C *__restrict__ init
                         const C a0 = a[i0], a1 = a[i1];
                         a[i0] = mk(m00.x * a0.x + m01.x * a1.x, m00.x * a0.y + m01.x * a1.y);
                         a[i1] = mk(m10.x * a0.x + m11.x * a1.x, m10.x * a0.y + m11.x * a1.y);
+                    }
+                } else if (kind == T_XLIKE) {  // real diagonal, imaginary off-diagonal: Rx
+                    for (uint32_t p = tid; p < half; p += nt) {
+                        const uint32_t i0 = ins0(p, q), i1 = i0 | qm;
+                        const C a0 = a[i0], a1 = a[i1];
+                        a[i0] = mk(m00.x * a0.x - m01.y * a1.y, m00.x * a0.y + m01.y * a1.x);
+                        a[i1] = mk(m11.x * a1.x - m10.y * a0.y, m11.x * a1.y + m10.y * a0.x);
                     }
                 } else {
                     for (uint32_t p = tid; p < half; p += nt) {
@@ -386,6 +393,7 @@ int run_trajectories(qf_sv *init, const qf_op *ops, uint64_t n_ops, uint64_t sho
                 if (o.gate == QF_GATE_X) t.kind = T_X;
                 else if (b[0].diag) t.kind = T_DIAG;
                 else if (m[1] == 0.0 && m[3] == 0.0 && m[5] == 0.0 && m[7] == 0.0) t.kind = T_REAL;
+                else if (m[1] == 0.0 && m[7] == 0.0 && m[2] == 0.0 && m[4] == 0.0) t.kind = T_XLIKE;
             }
             break;
         }
