@@ -662,11 +662,16 @@ def test_compiled_pass_with_hundreds_of_factored_gates(backend, dual):
             recs += [(A.OP_GATE, g, q, 0, 0, float(r.uniform(1.2, 1.9))) for q in range(12)]
             recs += [(A.OP_CNOT, 0, q, q + 1, 0, 0.0) for q in range(11)]
         ops = A.ops_array(recs)
-        sv = StateVector.zero(n, dtype="c64", backend=backend)
-        sv.apply_ops(ops, exec_opts={"jit": True})
-        got = sv.amplitudes()
-        assert np.isfinite(got).all()
-        assert close(got, O.run(ops, n), 2e-5)
+        want = O.run(ops, n)
+        # compiled passes; shared-memory passes (factored T_MAT1F ops with T_SCALE
+        # rescaling) in complex64 and complex128
+        for dtype, opts, tol in (("c64", {"jit": True}, 2e-5), ("c64", {"smem_tiles": True}, 2e-5),
+                                 ("c128", {}, 1e-10)):
+            sv = StateVector.zero(n, dtype=dtype, backend=backend)
+            sv.apply_ops(ops, exec_opts=opts)
+            got = sv.amplitudes()
+            assert np.isfinite(got).all(), (dtype, opts)
+            assert close(got, want, tol), (dtype, opts)
         return
     from quantumforge_gb300 import ParameterizedCircuit, RotationAxis
     from quantumforge_gb300.gradients import GradientOptions, GradientStrategy, gradient_with_inputs
