@@ -168,7 +168,15 @@ __global__ void __launch_bounds__(256) k_dm_channel_tile(C *__restrict__ v, uint
     __syncthreads();
     for (uint64_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
         const uint64_t base = deposit(t, ct.outer_mask);
-        for (uint32_t j = threadIdx.x; j < T; j += blockDim.x) s[j] = v[base | hi_off[j >> 5] | (j & 31u)];
+        if (sizeof(C) == 8) {  // complex64: 16-byte accesses (2 amplitudes of a 32-amplitude run), all in flight
+#pragma unroll 8
+            for (uint32_t w = threadIdx.x; w < (T >> 1); w += blockDim.x) {
+                const uint32_t j = w << 1;
+                *reinterpret_cast<float4 *>(s + j) = *reinterpret_cast<const float4 *>(v + (base | hi_off[j >> 5] | (j & 31u)));
+            }
+        } else {
+            for (uint32_t j = threadIdx.x; j < T; j += blockDim.x) s[j] = v[base | hi_off[j >> 5] | (j & 31u)];
+        }
         __syncthreads();
         for (uint32_t c = 0; c < ct.n_ch; ++c) {
             const uint32_t lc = ct.lc[c], lr = ct.lr[c], lo = min(lc, lr), hi = max(lc, lr);
@@ -197,7 +205,15 @@ __global__ void __launch_bounds__(256) k_dm_channel_tile(C *__restrict__ v, uint
             }
             __syncthreads();
         }
-        for (uint32_t j = threadIdx.x; j < T; j += blockDim.x) v[base | hi_off[j >> 5] | (j & 31u)] = s[j];
+        if (sizeof(C) == 8) {
+#pragma unroll 8
+            for (uint32_t w = threadIdx.x; w < (T >> 1); w += blockDim.x) {
+                const uint32_t j = w << 1;
+                *reinterpret_cast<float4 *>(v + (base | hi_off[j >> 5] | (j & 31u))) = *reinterpret_cast<const float4 *>(s + j);
+            }
+        } else {
+            for (uint32_t j = threadIdx.x; j < T; j += blockDim.x) v[base | hi_off[j >> 5] | (j & 31u)] = s[j];
+        }
         __syncthreads();
     }
 }
@@ -234,6 +250,9 @@ int dm_channels_fused(qf_sv *sv, uint32_t n, const uint32_t *qs, const double (*
     if (count > (uint32_t)kMaxTileChannels || 2 * n < 5) return fail(QF_ERR_INVALID_ARGUMENT, "channel group too large");
     uint64_t tile_mask = 31;  // the low five column bits
     for (uint32_t c = 0; c < count; ++c) tile_mask |= (1ULL << qs[c]) | (1ULL << (n + qs[c]));
+    // widen to 12 tile bits with the lowest free bits: fewer, larger tiles
+    // (per-tile index work and barriers amortised) and longer contiguous runs
+    for (uint32_t b = 5; b < 2 * n && __builtin_popcountll(tile_mask) < 12; ++b) tile_mask |= 1ULL << b;
     ChannelTile ct{};
     ct.k = (uint32_t)__builtin_popcountll(tile_mask);
     if (ct.k > 12) return fail(QF_ERR_INVALID_ARGUMENT, "channel group needs %u tile bits", ct.k);
@@ -261,12 +280,22 @@ int dm_channels_fused(qf_sv *sv, uint32_t n, const uint32_t *qs, const double (*
     }
     const uint64_t n_tiles = 1ULL << (2 * n - ct.k);
     const size_t smem = (sv->dtype == QF_C64 ? 8u : 16u) * (size_t(1) << ct.k) + sizeof(uint64_t) * (size_t(1) << ct.n_hi);
-    const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(n_tiles, (uint64_t)ctx->sm_count * 8));
+    // one wave of resident CTAs (a grid past the resident count leaves a tail
+    // wave running on part of the GPU)
+    auto grid_of = [&](const void *k, int *grid) -> int {
+        int per_sm = 0;
+        QF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, smem));
+        *grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(n_tiles, (uint64_t)std::max(per_sm, 1) * ctx->sm_count));
+        return QF_OK;
+    };
+    int grid;
     if (sv->dtype == QF_C64) {
         QF_CUDA(cudaFuncSetAttribute(k_dm_channel_tile<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        QF_TRY(grid_of((const void *)k_dm_channel_tile<float2>, &grid));
         k_dm_channel_tile<float2><<<grid, 256, smem, ctx->stream>>>(static_cast<float2 *>(sv->d), n_tiles, ct);
     } else {
         QF_CUDA(cudaFuncSetAttribute(k_dm_channel_tile<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        QF_TRY(grid_of((const void *)k_dm_channel_tile<double2>, &grid));
         k_dm_channel_tile<double2><<<grid, 256, smem, ctx->stream>>>(static_cast<double2 *>(sv->d), n_tiles, ct);
     }
     QF_CUDA(cudaGetLastError());
