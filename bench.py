@@ -51,6 +51,8 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extra", action="store_true")
+    ap.add_argument("--no-parity", dest="parity", action="store_false",
+                    help="skip the complex128 run of the headline circuit (error of the complex64 result)")
     ap.add_argument("--extras", default="vqe24,qaoa4096,shots20,shots_ff,noise_shots,density14,vqe32",
                     help="comma-separated extra workloads to run after the headline")
     ap.add_argument("--vqe-qubits", type=int, default=32, help="qubits of the checkpointed-adjoint extra (vqe32)")
@@ -329,12 +331,16 @@ def run_ours(args):
                "api": "qf_run_circuit (CudaBackend::run_circuit): f64 host amplitudes in and out, pinned"}
         del host_in, host_out
 
+    parity = None
+    if rank == 0 and args.parity and dcode == A.C64:
+        del sv
+        parity = c128_parity(backend, n, ops, exec_opts)
     extra = {}
     cpu = None
     if rank == 0 and not args.no_extra:
         wanted = set(args.extras.split(","))
         if "vqe24" in wanted:
-            extra["vqe24"] = vqe_gradients(backend)
+            extra["vqe24"] = vqe_gradients(backend, cpu=not args.no_cpu_baseline)
         if "qaoa4096" in wanted:
             extra["qaoa4096"] = qaoa_batch(backend, cpu=not args.no_cpu_baseline, count=args.qaoa_instances)
         if "shots20" in wanted:
@@ -365,12 +371,70 @@ def run_ours(args):
                          "traffic": traffic, "peak_kind": f"of {peak_kind}", "kernel": kernel,
                          "bytes_per_launch": bytes_per_launch, "avg_launch_ms": 1000 * avg_launch_s},
             "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches,
-            "extra": extra,
+            "parity_vs_c128": parity, "extra": extra,
         }
         print(json.dumps(line), flush=True)
     backend.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+class _DeviceArray:
+    """A flat device buffer seen by torch through __cuda_array_interface__."""
+
+    def __init__(self, ptr: int, count: int, typestr: str):
+        self.__cuda_array_interface__ = {"shape": (count,), "typestr": typestr, "data": (ptr, False), "version": 3}
+
+
+def state_tensor(sv):
+    """The interleaved (re, im) reals of a device state as a torch tensor (no copy)."""
+    import ctypes as C
+
+    import torch
+
+    from quantumforge_gb300 import _native
+
+    p = C.c_void_p()
+    _native.check(_native.load().qf_sv_device_ptr(sv._h, C.byref(p)))
+    typestr = "<f4" if sv.dtype in ("c64", "complex64") else "<f8"
+    return torch.as_tensor(_DeviceArray(p.value, 2 << sv.qubits, typestr), device="cuda")
+
+
+def c128_parity(backend, n, ops, exec_opts):
+    """The headline circuit once from |0...0> on a complex64 and on a
+    complex128 state (the reference's precision; the complex128 tile passes
+    agree with the oracle to 1e-10 where it can run): the largest amplitude
+    and <Z_q> differences, computed on the device in chunks."""
+    import torch
+
+    import quantumforge_gb300 as qf
+
+    sv64 = qf.StateVector.zero(n, dtype="c64", backend=backend)
+    sv64.apply_ops(ops, exec_opts=exec_opts)
+    z64 = np.asarray(sv64.expectation_z_all())
+    sv128 = qf.StateVector.zero(n, dtype="c128", backend=backend)
+    sv128.apply_ops(ops)  # warm (plans the passes)
+    sv128 = qf.StateVector.zero(n, dtype="c128", backend=backend)
+    backend.synchronize()
+    t0 = time.perf_counter()
+    sv128.apply_ops(ops)
+    backend.synchronize()
+    t128 = time.perf_counter() - t0
+    z128 = np.asarray(sv128.expectation_z_all())
+    a, b = state_tensor(sv64), state_tensor(sv128)
+    err, norm_err, chunk = 0.0, 0.0, 1 << 26
+    for i in range(0, a.numel(), chunk):
+        d = (a[i:i + chunk].double() - b[i:i + chunk]).view(-1, 2)
+        err = max(err, float(torch.sqrt((d * d).sum(1)).max()))
+    max_amp = 0.0
+    for i in range(0, b.numel(), chunk):
+        v = b[i:i + chunk].view(-1, 2)
+        max_amp = max(max_amp, float(torch.sqrt((v * v).sum(1)).max()))
+    torch.cuda.synchronize()
+    del a, b, sv64, sv128
+    return {"reference": "the same circuit on a complex128 state", "max_abs_amp_err_vs_c128": err,
+            "max_abs_amp_c128": max_amp, "max_z_err_vs_c128": float(np.abs(z64 - z128).max()),
+            "c128_step_s": t128, "c128_gates_per_s": len(ops) / t128}
 
 
 def shots20(backend, cpu: bool):
@@ -408,6 +472,14 @@ def shots20(backend, cpu: bool):
            "ties": res.ties, "distinct_outcomes": len(res.counts)}
     exp_packed, width = O.run_shots(mops, n, shots, seed, threads=os.cpu_count() or 1)
     out["counts_bit_exact_vs_oracle"] = res.counts == O.counts(exp_packed, width)
+    out["more_seeds"] = {}
+    for s2 in (43, 44):  # two more seeds of the same circuit
+        t0 = time.perf_counter()
+        r2 = circ.run_shots(n, shots, s2, dtype="c128", backend=backend, tie_eps=1e-12)
+        t2 = time.perf_counter() - t0
+        e2, w2 = O.run_shots(mops, n, shots, s2, threads=os.cpu_count() or 1)
+        out["more_seeds"][str(s2)] = {"api_shots_per_s": shots / t2, "ties": r2.ties,
+                                      "counts_bit_exact_vs_oracle": r2.counts == O.counts(e2, w2)}
     a = O.run(ops, n, threads=os.cpu_count() or 1)
     out["max_prob_err_vs_oracle"] = float(np.abs(probs - O.probabilities(a)).max())
     out["max_z_err_vs_oracle"] = float(max(abs(zs[q] - O.expectation(a, 2, q)) for q in range(n)))
@@ -701,9 +773,14 @@ def qaoa_cpu_estimate(problems):
             "eval_s": {str(k): v for k, v in t_eval.items()}}
 
 
-def vqe_gradients(backend):
+def vqe_gradients(backend, cpu: bool = True):
     """24-qubit VQE (RY.RZ per qubit + CZ ring, 8 layers, 384 params, TFIM
-    ring h = 1): adjoint (checkpoint per layer) vs GPU parameter shift."""
+    ring h = 1): adjoint (checkpoint per layer) vs GPU parameter shift, both
+    complex64; the energy and gradient error against a complex128 adjoint run
+    of the same circuit (the reference's precision), and central finite
+    differences (h = 1e-4, complex128 energies) on a few parameters. The CPU
+    baseline is the oracle's parameter shift (two energy evaluations timed,
+    scaled to the 2 x 384 evaluations of one gradient)."""
     import numpy as np
 
     import quantumforge_gb300 as qf
@@ -728,10 +805,50 @@ def vqe_gradients(backend):
     sh = gradient_with_inputs(pc, GradientOptions(strategy=GradientStrategy.ParameterShift), [], params, n, H,
                               dtype="c64", backend=backend)
     t_sh = time.perf_counter() - t0
-    return {"qubits": n, "params": int(params.size), "ops": len(ops), "adjoint_grads_per_s": 1.0 / t_adj,
-            "param_shift_grads_per_s": 1.0 / t_sh, "ratio": t_sh / t_adj,
-            "max_abs_grad_diff_adjoint_vs_shift": float(np.abs(adj.gradient - sh.gradient).max()),
-            "energy_adjoint": adj.expectation, "energy_shift_run": sh.expectation, "dtype": "complex64"}
+    # complex128 reference run and finite differences
+    t0 = time.perf_counter()
+    ref = gradient_with_inputs(pc, GradientOptions(strategy=GradientStrategy.Adjoint), [], params, n, H,
+                               dtype="c128", backend=backend, checkpoint_every=3 * n)
+    t_ref = time.perf_counter() - t0
+    g64, g128 = np.asarray(adj.gradient), np.asarray(ref.gradient)
+    h = 1e-4
+    fd_params = [0, 97, 191, 288, 383]
+    fd = []
+    for k in fd_params:
+        pp, pm = params.copy(), params.copy()
+        pp[k] += h
+        pm[k] -= h
+        ep = pc.expectation_pauli_sum(pp, n, H, dtype="c128", backend=backend)
+        em = pc.expectation_pauli_sum(pm, n, H, dtype="c128", backend=backend)
+        fd.append((ep - em) / (2 * h))
+    fd = np.asarray(fd)
+    out = {"qubits": n, "params": int(params.size), "ops": len(ops), "adjoint_grads_per_s": 1.0 / t_adj,
+           "param_shift_grads_per_s": 1.0 / t_sh, "ratio": t_sh / t_adj,
+           "max_abs_grad_diff_adjoint_vs_shift": float(np.abs(adj.gradient - sh.gradient).max()),
+           "energy_adjoint": adj.expectation, "energy_shift_run": sh.expectation, "dtype": "complex64",
+           "vs_c128": {"energy_c128": ref.expectation, "energy_err_vs_c128": abs(adj.expectation - ref.expectation),
+                       "max_abs_grad_err_vs_c128": float(np.abs(g64 - g128).max()),
+                       "shift_max_abs_grad_err_vs_c128": float(np.abs(np.asarray(sh.gradient) - g128).max()),
+                       "target": 1e-6, "c128_adjoint_s": t_ref},
+           "central_fd": {"step": h, "params": fd_params, "energies": "complex128",
+                          "max_abs_diff_vs_c128_adjoint": float(np.abs(fd - g128[fd_params]).max()),
+                          "max_abs_diff_vs_c64_adjoint": float(np.abs(fd - g64[fd_params]).max())}}
+    if cpu:
+        import oracle as O
+
+        threads = os.cpu_count() or 1
+        m = 20  # one 24-qubit evaluation takes about a minute on the host: time the same ansatz at 20 qubits
+        ops_m, params_m, H_m = W.vqe_tfim(m, 8, seed=3)
+        t0 = time.perf_counter()
+        O.energy(ops_m, m, params_m, H_m.array(), threads=threads)
+        te = (time.perf_counter() - t0) * (1 << (n - m))
+        out["cpu_baseline"] = {"value": 1.0 / (2 * params.size * te), "unit": "gradients/s", "cores": threads,
+                               "kind": "port",
+                               "sample": f"one energy evaluation of the same 8-layer ansatz at {m} qubits through the "
+                                         f"oracle (complex128, {threads} threads), scaled by 2^{n - m} amplitudes and "
+                                         f"by the 2 x {params.size} evaluations of a parameter-shift gradient "
+                                         f"(extrapolated)"}
+    return out
 
 
 def vqe32_checkpointed(backend, n=32):
@@ -779,7 +896,7 @@ def extras_only(args):
     cpu = not args.no_cpu_baseline
     extra = {}
     if "vqe24" in wanted:
-        extra["vqe24"] = vqe_gradients(backend)
+        extra["vqe24"] = vqe_gradients(backend, cpu=not args.no_cpu_baseline)
     if "qaoa4096" in wanted:
         extra["qaoa4096"] = qaoa_batch(backend, cpu=cpu, count=args.qaoa_instances)
     if "shots20" in wanted:

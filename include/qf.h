@@ -580,11 +580,15 @@ uint64_t qf_rng_jump(uint64_t state, uint64_t steps);
  * allocating routine: its only scratch is a fixed array in the library's
  * device image (about 84 KB, held on every GPU that loads the library until
  * the process exits), which limits `qubits` to 1..40 (QF_ERR_STATE_TOO_LARGE
- * beyond). `stream` is a cudaStream_t (NULL = the legacy default stream); the
- * call returns after the result is on the host. The first call on a device
- * looks up the scratch array's device address, so make it before any stream
- * capture. Every call reuses the same scratch, so calls that overlap on the
- * GPU race: serialise them.
+ * beyond). `stream` is a cudaStream_t of `device` (NULL = the legacy default
+ * stream; a stream of another device is QF_ERR_INVALID_ARGUMENT); the call
+ * returns after the result is on the host, with the calling thread's current
+ * device as it was before the call. The first call on a device looks up the
+ * scratch array's device address, so make it before any stream capture; the
+ * address is kept for the life of the process, so do not call this entry
+ * point again after destroying the device's primary context
+ * (cudaDeviceReset). Every call reuses the same scratch, so calls that
+ * overlap on the GPU race: serialise them.
  * ------------------------------------------------------------------------- */
 int qf_expectation_z_all_noalloc(int device, const void *d_amps, uint32_t qubits, int dtype, void *stream,
                                  double *out, uint64_t n_out);

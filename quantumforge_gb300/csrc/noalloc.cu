@@ -13,9 +13,13 @@
 // address is looked up once per device with cudaGetSymbolAddress (with that
 // device current) by the first call on the device, and passed to the
 // kernels. That first call should therefore come before any stream capture.
+// The address is cached for the life of the process: it belongs to the
+// device's primary context, so a caller that destroys that context
+// (cudaDeviceReset) must not call this entry point again in the same process.
 // All calls share the array and every call overwrites the part it reads, so
 // calls that overlap on the GPU (different streams, or different host
-// threads) race and must be serialised by the caller.
+// threads) race and must be serialised by the caller. The calling thread's
+// current device is the same after the call as before it.
 #include <algorithm>
 #include <mutex>
 
@@ -116,6 +120,25 @@ __global__ void k_na_final(const double *__restrict__ partial, uint32_t blocks, 
     }
 }
 
+// Makes `device` current for the call and gives the caller's device back on
+// every return path: the hosts this entry point serves manage their own
+// current device.
+struct DeviceGuard {
+    int saved = -1;
+    cudaError_t enter(int device) {
+        cudaError_t e = cudaGetDevice(&saved);
+        if (e != cudaSuccess) {
+            saved = -1;
+            return e;
+        }
+        return saved == device ? cudaSuccess : cudaSetDevice(device);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        if (saved >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != saved) cudaSetDevice(saved);
+    }
+};
+
 template <typename C>
 int na_launch(const C *a, uint32_t n, cudaStream_t stream, double *scratch, uint32_t *blocks_out) {
     uint32_t blocks = 1;
@@ -153,10 +176,17 @@ extern "C" int qf_expectation_z_all_noalloc(int device, const void *d_amps, uint
     if (reinterpret_cast<uintptr_t>(d_amps) % align)
         return fail(QF_ERR_INVALID_ARGUMENT, "amplitudes must be %zu-byte aligned", align);
     if (device < 0 || device >= 64) return fail(QF_ERR_INVALID_ARGUMENT, "device %d is out of range", device);
-    QF_CUDA(cudaSetDevice(device));
+    DeviceGuard guard;
+    QF_CUDA(guard.enter(device));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (s) {  // a stream of another device would fail later with a generic launch error
+        int sdev = -1;
+        QF_CUDA(cudaStreamGetDevice(s, &sdev));
+        if (sdev != device)
+            return fail(QF_ERR_INVALID_ARGUMENT, "the stream belongs to device %d, not to device %d", sdev, device);
+    }
     double *scratch = nullptr;
     QF_TRY(na_scratch(device, &scratch));
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     uint32_t blocks = 1;
     if (dtype == QF_C64) QF_TRY(na_launch(static_cast<const float2 *>(d_amps), qubits, s, scratch, &blocks));
     else QF_TRY(na_launch(static_cast<const double2 *>(d_amps), qubits, s, scratch, &blocks));

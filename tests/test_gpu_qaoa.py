@@ -73,6 +73,34 @@ def test_batched_passes_match_oracle(backend, graph):
             assert np.abs(grad[i] - g_ref).max() < 1e-4 * max(1.0, np.abs(g_ref).max()), (i, n, grad[i], g_ref)
 
 
+def test_config_sizes_at_depth_four_match_oracle(backend):
+    """Every qubit count of the 4096-instance workload (12..20, p = 4, gamma in
+    [0, pi], beta in [0, pi/2]), the 20-qubit class included, at non-zero
+    angles against the oracle's complex128 adjoint; with and without the
+    captured graph."""
+    import os
+
+    rng = np.random.default_rng(20)
+    sizes = [20, 12, 14, 16, 18, 20]
+    problems = [(n, O.random_3_regular(n, 900 + i)) for i, n in enumerate(sizes)]
+    p = 4
+    gam = rng.uniform(0, np.pi, (len(problems), p))
+    bet = rng.uniform(0, np.pi / 2, (len(problems), p))
+    threads = os.cpu_count() or 1
+    refs = []
+    for i, (n, edges) in enumerate(problems):
+        ops = W.qaoa_param_circuit(n, edges, p)
+        params = np.concatenate([2 * gam[i], 2 * bet[i]])
+        e_ref, g_ref = O.adjoint_uncompute(ops, n, params, PauliSum.maxcut(edges).array(), threads=threads)
+        refs.append((e_ref, 2 * g_ref))
+    for graph in (False, True):
+        cost, grad = QaoaBatch(problems, p, backend=backend, use_graph=graph).run(gam, bet)
+        for i, (n, _) in enumerate(problems):
+            e_ref, g_ref = refs[i]
+            assert abs(cost[i] - e_ref) < 1e-5 * max(1.0, abs(e_ref)), (graph, i, n, cost[i], e_ref)
+            assert np.abs(grad[i] - g_ref).max() < 1e-4 * max(1.0, np.abs(g_ref).max()), (graph, i, n, grad[i], g_ref)
+
+
 def test_uniform_superposition_cuts_half_the_edges(backend):
     # gamma = beta = 0: the state is H^n |0>, every edge is cut with probability 1/2
     problems = [(n, O.random_3_regular(n, n)) for n in (12, 14, 16, 20, 22, 24)]

@@ -13,6 +13,8 @@ import ctypes as C
 import numpy as np
 import pytest
 
+import oracle as O
+
 from quantumforge_gb300 import StateVector
 from quantumforge_gb300 import _abi as A
 from quantumforge_gb300 import _native
@@ -29,22 +31,34 @@ def _noalloc(lib, device, ptr, n, dtype, stream):
 
 
 @pytest.mark.parametrize("dtype,code,tol", [("c64", A.C64, 1e-5), ("c128", A.C128, 1e-11)])
-@pytest.mark.parametrize("n", [1, 5, 9, 21])
+@pytest.mark.parametrize("n", [1, 5, 8, 9, 14, 21])
 def test_noalloc_matches_the_allocating_reduction(backend, dtype, code, tol, n):
+    """n = 8 is the smallest state on the chunked kernel (one warp); n = 14
+    runs several blocks of 256 threads whose thread-id bits meet the
+    block-index bits."""
+    import torch
+
     lib = _native.load()
     ops = W.random_circuit(n, 6, 300 + n, two_qubit="mixed" if n > 3 else "ladder")
     sv = StateVector.zero(n, dtype=dtype, backend=backend)
     sv.apply_ops(ops)
     expected = sv.expectation_z_all()
+    amps = sv.amplitudes()
+    oracle_z = np.array([O.expectation(amps, 2, q) for q in range(n)])
     dptr, stream = C.c_void_p(), C.c_void_p()
     _native.check(lib.qf_sv_device_ptr(sv._h, C.byref(dptr)))
     _native.check(lib.qf_ctx_stream(backend.handle, C.byref(stream)))
     backend.synchronize()
+    device_before = torch.cuda.current_device()
     # two calls in a row share the scratch array: both must be right
     first = _noalloc(lib, backend.ordinal, dptr, n, code, stream)
     second = _noalloc(lib, backend.ordinal, dptr, n, code, stream)
-    assert np.abs(first - expected).max() <= tol
-    assert np.abs(second - expected).max() <= tol
+    # the legacy default stream (NULL) as well
+    third = _noalloc(lib, backend.ordinal, dptr, n, code, None)
+    assert torch.cuda.current_device() == device_before
+    for got in (first, second, third):
+        assert np.abs(got - expected).max() <= tol
+        assert np.abs(got - oracle_z).max() <= tol
 
 
 def test_noalloc_rejects_states_beyond_its_scratch(backend):
