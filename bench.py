@@ -53,7 +53,7 @@ def parse_args():
     ap.add_argument("--no-extra", action="store_true")
     ap.add_argument("--no-parity", dest="parity", action="store_false",
                     help="skip the complex128 run of the headline circuit (error of the complex64 result)")
-    ap.add_argument("--extras", default="vqe24,qaoa4096,shots20,shots_ff,noise_shots,density14,vqe32",
+    ap.add_argument("--extras", default="vqe24,qaoa4096,shots20,shots_ff,noise_shots,density14,vqe32,c2_matrix",
                     help="comma-separated extra workloads to run after the headline")
     ap.add_argument("--vqe-qubits", type=int, default=32, help="qubits of the checkpointed-adjoint extra (vqe32)")
     ap.add_argument("--qaoa-instances", type=int, default=4096, help="instances of the batched QAOA extra (qaoa4096)")
@@ -353,6 +353,8 @@ def run_ours(args):
             extra["noise_shots"] = noise_shots(backend, cpu=not args.no_cpu_baseline, shots=args.noise_shots)
         if "vqe32" in wanted:
             extra["vqe32"] = vqe32_checkpointed(backend, args.vqe_qubits)
+        if "c2_matrix" in wanted:
+            extra["c2_matrix"] = c2_matrix(backend)
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, sample = time_cpu_oracle(n, ops, args.cpu_seconds, threads)
@@ -396,7 +398,9 @@ def state_tensor(sv):
 
     p = C.c_void_p()
     _native.check(_native.load().qf_sv_device_ptr(sv._h, C.byref(p)))
-    typestr = "<f4" if sv.dtype in ("c64", "complex64") else "<f8"
+    from quantumforge_gb300 import _abi as A
+
+    typestr = "<f4" if sv.dtype == A.C64 else "<f8"  # StateVector.dtype holds the qf_dtype code
     return torch.as_tensor(_DeviceArray(p.value, 2 << sv.qubits, typestr), device="cuda")
 
 
@@ -435,6 +439,105 @@ def c128_parity(backend, n, ops, exec_opts):
     return {"reference": "the same circuit on a complex128 state", "max_abs_amp_err_vs_c128": err,
             "max_abs_amp_c128": max_amp, "max_z_err_vs_c128": float(np.abs(z64 - z128).max()),
             "c128_step_s": t128, "c128_gates_per_s": len(ops) / t128}
+
+
+def max_amp_diff(sv_a, sv_b) -> float:
+    """max_i |a_i - b_i| over two device states of the same size (on the device, in chunks)."""
+    import torch
+
+    a, b = state_tensor(sv_a), state_tensor(sv_b)
+    err, chunk = 0.0, 1 << 26
+    for i in range(0, a.numel(), chunk):
+        d = (a[i:i + chunk].double() - b[i:i + chunk].double()).view(-1, 2)
+        err = max(err, float(torch.sqrt((d * d).sum(1)).max()))
+    return err
+
+
+def unfused_bytes(ops, n, amp_bytes) -> int:
+    """Algorithmic bytes of one gate per sweep (dense or RZ-type 2Nb, Z/S/T Nb,
+    CNOT/SWAP Nb, CZ Nb/2) summed over the circuit."""
+    from quantumforge_gb300 import _abi as A
+
+    N = 1 << n
+    tot = 0
+    for r in ops:
+        k, g = int(r["kind"]), int(r["gate"])
+        if k == A.OP_GATE:
+            tot += N * amp_bytes if g in (A.GATE_Z, A.GATE_S, A.GATE_SDG, A.GATE_T, A.GATE_TDG) else 2 * N * amp_bytes
+        elif k in (A.OP_CNOT, A.OP_SWAP):
+            tot += N * amp_bytes
+        else:
+            tot += N * amp_bytes // 2
+    return tot
+
+
+def c2_matrix(backend, n64: int = 30, n128: int = 26, depth: int = 40, seed: int = 1):
+    """The headline circuit generator run unfused (one sweep per gate, the
+    reference's structure), as per-gate tile passes (the default), and fused
+    into dense k-qubit blocks for k = 2..5 (k = 5 on the tensor cores and on
+    the FP32 pipe), in complex64 at 30 qubits and complex128 at 26 qubits
+    (FP64 dense blocks of 5 qubits take minutes at 30). Per mode: gates/s, HBM
+    passes, the fraction of the measured copy peak over the passes'
+    algorithmic bytes, and the largest amplitude error against the complex128
+    per-gate result of the same circuit."""
+    import ctypes as C
+
+    import torch
+
+    import quantumforge_gb300 as qf
+    from quantumforge_gb300 import _abi as A
+    from quantumforge_gb300 import _native
+    from quantumforge_gb300 import workloads as W
+
+    lib = _native.load()
+    peak, peak_kind = hbm_peak()
+    sp = C.c_void_p()
+    lib.qf_ctx_stream(backend.handle, C.byref(sp))
+    stream = torch.cuda.ExternalStream(sp.value)
+    modes = [("unfused", {"mode": "unfused"}), ("passes", {}), ("k2", {"block_qubits": 2}), ("k3", {"block_qubits": 3}),
+             ("k4", {"block_qubits": 4}), ("k5", {"block_qubits": 5}),
+             ("k5_simt", {"block_qubits": 5, "blocks_engine": "simt"})]
+    out = {"metric": "gates/s", "peak": peak, "peak_kind": f"of {peak_kind}",
+           "reference_state": "complex128 per-gate tile passes of the same circuit"}
+    for dtype, n in (("c64", n64), ("c128", n128)):
+        ops = W.random_circuit(n, depth, seed, two_qubit="mixed")
+        b = 8 if dtype == "c64" else 16
+        ref = qf.StateVector.zero(n, dtype="c128", backend=backend)
+        ref.apply_ops(ops)
+        rows = {}
+        for name, eo in modes:
+            if dtype == "c128" and name == "k5_simt":
+                continue  # complex128 blocks always run on the FP64 pipe
+            npass, ngate = C.c_uint64(), C.c_uint64()
+            o = A.exec_opts(eo)
+            _native.check(lib.qf_plan_stats(n, A.C64 if dtype == "c64" else A.C128, _native.ptr(ops), len(ops), None, 0,
+                                            None, 0, C.byref(o), C.byref(npass), C.byref(ngate)))
+            sv = qf.StateVector.zero(n, dtype=dtype, backend=backend)
+            try:
+                sv.apply_ops(ops, exec_opts=eo)  # from |0...0>: plans, compiles; the error check
+            except Exception as e:  # a mode that fails is reported, not fatal to the bench
+                rows[name] = {"error": str(e)[:300]}
+                del sv
+                continue
+            backend.synchronize()
+            err = max_amp_diff(sv, ref)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            t0 = time.perf_counter()
+            e0.record(stream)
+            sv.apply_ops(ops, exec_opts=eo)
+            e1.record(stream)
+            e1.synchronize()
+            t_wall = time.perf_counter() - t0
+            t = e0.elapsed_time(e1) / 1000.0
+            algo = unfused_bytes(ops, n, b) if name == "unfused" else npass.value * 2 * (1 << n) * b
+            rows[name] = {"gates_per_s": len(ops) / t, "step_s": t, "wall_s": t_wall, "hbm_passes": npass.value,
+                          "algorithmic_gb": algo / 1e9, "frac": algo / t / 1e9 / peak,
+                          "max_abs_amp_err_vs_c128": err}
+            del sv
+        out[f"{dtype}_{n}q"] = {"gates": len(ops), **rows}
+        del ref
+        torch.cuda.empty_cache()
+    return out
 
 
 def shots20(backend, cpu: bool):
@@ -909,6 +1012,8 @@ def extras_only(args):
         extra["noise_shots"] = noise_shots(backend, cpu=cpu, shots=args.noise_shots)
     if "vqe32" in wanted:
         extra["vqe32"] = vqe32_checkpointed(backend, args.vqe_qubits)
+    if "c2_matrix" in wanted:
+        extra["c2_matrix"] = c2_matrix(backend, n64=args.qubits, n128=min(args.qubits, 26))
     print(json.dumps({"extra": extra}), flush=True)
     backend.close()
 

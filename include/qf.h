@@ -166,11 +166,17 @@ enum qf_exec_mode {
 #define QF_EXEC_FLAG_SHOTS_TRAJECTORIES 16  /* shots: per-shot trajectories in shared memory whenever the state fits */
 #define QF_EXEC_FLAG_PLAN_FIRST_COME 32  /* fused sweeps: fill each pass's tile in gate order (no look-ahead choice of
                                             its resident qubits) */
+#define QF_EXEC_FLAG_BLOCKS_SIMT 64      /* block_qubits = 5, complex64: apply the blocks on the FP32 pipe (shared-memory
+                                            interpreter) instead of the tensor cores */
 
 typedef struct qf_exec_opts {
     int32_t mode;          /* enum qf_exec_mode */
     int32_t tile_qubits;   /* qubits resident per tile (0 = auto) */
-    int32_t block_qubits;  /* dense fused-block width k (0/1 = apply gates one by one, 2..5 = fuse into k-qubit blocks) */
+    int32_t block_qubits;  /* dense fused-block width k: 0/1 = apply gates one by one (default); 2..5 = multiply the
+                              gates of each tile pass into dense blocks of up to k qubits (f64 on the host) and apply
+                              one 2^m x 2^m matrix per block. complex64: compiled register passes for k <= 4, the
+                              tensor cores (tcgen05, 3xTF32) for k = 5; complex128: the shared-memory interpreter.
+                              Every qubit a gate touches is then resident in the pass's tile. */
     int32_t flags;         /* QF_EXEC_FLAG_* */
 } qf_exec_opts;
 

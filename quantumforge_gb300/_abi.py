@@ -97,12 +97,13 @@ EXEC_FLAG_NO_JIT = 4
 EXEC_FLAG_SHOTS_TREE = 8
 EXEC_FLAG_SHOTS_TRAJECTORIES = 16
 EXEC_FLAG_PLAN_FIRST_COME = 32
+EXEC_FLAG_BLOCKS_SIMT = 64
 _MODES = {"auto": EXEC_AUTO, "unfused": EXEC_UNFUSED, "fused": EXEC_FUSED}
 
 
 def exec_opts(opts) -> "ExecOpts":
     """qf_exec_opts from a dict {mode, tile_qubits, block_qubits, smem_tiles, jit,
-    shots_engine ("tree" | "trajectories")}."""
+    shots_engine ("tree" | "trajectories"), blocks_engine ("auto" | "simt")}."""
     if isinstance(opts, ExecOpts):
         return opts
     opts = opts or {}
@@ -115,6 +116,11 @@ def exec_opts(opts) -> "ExecOpts":
         flags |= EXEC_FLAG_PLAN_FIRST_COME
     elif opts.get("plan", "lookahead") != "lookahead":
         raise ValueError("plan must be 'lookahead' or 'first_come'")
+    blocks = opts.get("blocks_engine")
+    if blocks == "simt":
+        flags |= EXEC_FLAG_BLOCKS_SIMT
+    elif blocks not in (None, "auto"):
+        raise ValueError("blocks_engine must be 'auto' or 'simt'")
     engine = opts.get("shots_engine")
     if engine == "tree":
         flags |= EXEC_FLAG_SHOTS_TREE

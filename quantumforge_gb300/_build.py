@@ -19,7 +19,7 @@ LIBDIR = PKG / "_lib"
 LIB = LIBDIR / "libqf_gb300.so"
 INCLUDE = PKG.parent / "include"
 
-SOURCES = ["api.cpp", "planner.cpp", "sweep.cu", "reduce.cu", "rspass.cu", "jit.cpp", "noalloc.cu", "qaoa.cu", "density.cu", "trajectory.cu", "ingest.cpp"]
+SOURCES = ["api.cpp", "planner.cpp", "sweep.cu", "reduce.cu", "rspass.cu", "jit.cpp", "noalloc.cu", "qaoa.cu", "density.cu", "trajectory.cu", "ingest.cpp", "blockmma.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O3,-ffp-contract=off", "--expt-relaxed-constexpr",
               "-Xptxas", "-O3", f"-I{INCLUDE}"]

@@ -1997,8 +1997,7 @@ int qf_plan_stats(uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops, 
         return QF_OK;
     }
     PlanOpts po;
-    forward_tiling(qubits, dtype, opts ? opts->tile_qubits : 0, opts ? opts->flags : 0, &po.tile_qubits, &po.low_qubits);
-    po.search = !(opts && (opts->flags & QF_EXEC_FLAG_PLAN_FIRST_COME));
+    QF_TRY(plan_opts_for(qubits, dtype, opts, po));
     Plan plan;
     QF_TRY(plan_passes(qubits, gates, po, plan));
     *n_passes = plan.passes.size();

@@ -270,6 +270,16 @@ std::complex<double> scale_const(const Gen &g) {
                          : std::complex<double>(g.pscale.real(), g.pscale.real());
 }
 
+// A dense block's D x D matrix in the constant bank (row-major, from complex
+// offset `boff` of the plan's block matrices); returns its first slot (entry
+// (r, c) is M[4 * slot + r * D + c]).
+int block_slots(Gen &g, const std::vector<double> &bm, uint32_t boff, int D) {
+    const int first = (int)g.consts.size() / 4;
+    for (int e = 0; e < D * D; ++e) g.consts.push_back({bm[2 * ((size_t)boff + e)], bm[2 * ((size_t)boff + e) + 1]});
+    while (g.consts.size() % 4) g.consts.push_back(0.0);
+    return first;
+}
+
 // One pass -> one kernel.
 struct PassGen {
     Gen &g;
@@ -282,8 +292,10 @@ struct PassGen {
     int WB = 3;           // warp bits: K - 9
 
     bool dual;  // backward pass: psi (A, r*) and lambda (B, l*) with overlap slots
+    const std::vector<double> *bmats = nullptr;  // the plan's dense block matrices (BK_BLOCK)
 
-    PassGen(Gen &gen, const Pass &pass, uint32_t nq, bool dual_ = false) : g(gen), p(pass), n(nq), dual(dual_) {
+    PassGen(Gen &gen, const Pass &pass, uint32_t nq, bool dual_ = false, const std::vector<double> *bm = nullptr)
+        : g(gen), p(pass), n(nq), dual(dual_), bmats(bm) {
         for (int q = 0; q < 64; ++q) slot_of[q] = -1;
         int s = 0;
         for (uint32_t q = 0; q < n; ++q)
@@ -334,11 +346,22 @@ struct PassGen {
         case BK_CNOT: return q == x.q0;
         case BK_CZ: return true;
         case BK_OVL: return x.axis == QF_PAULI_Z;
-        default: return false;
+        default: return false;  // SWAP, dense block
         }
     }
-    static int arity(const BGate &x) { return (x.kind == BK_MAT1 || x.kind == BK_OVL) ? 1 : 2; }
-    static uint32_t qubit(const BGate &x, int k) { return k ? x.q1 : x.q0; }
+    static int arity(const BGate &x) {
+        if (x.kind == BK_BLOCK) return x.nq;
+        return (x.kind == BK_MAT1 || x.kind == BK_OVL) ? 1 : 2;
+    }
+    static uint32_t qubit(const BGate &x, int k) {
+        if (x.kind == BK_BLOCK) return x.bq[k];
+        return k ? x.q1 : x.q0;
+    }
+    static uint64_t block_mask(const BGate &x) {
+        uint64_t m = 0;
+        for (int i = 0; i < x.nq; ++i) m |= 1ULL << x.bq[i];
+        return m;
+    }
     void build_deps() {
         const auto &G = p.gates;
         preds.assign(G.size(), {});
@@ -360,9 +383,14 @@ struct PassGen {
         return true;
     }
     static bool strict_need(const BGate &x) {
-        return (x.kind == BK_MAT1 && !x.diag) || x.kind == BK_CNOT || (x.kind == BK_OVL && x.axis != QF_PAULI_Z);
+        return (x.kind == BK_MAT1 && !x.diag) || x.kind == BK_CNOT || (x.kind == BK_OVL && x.axis != QF_PAULI_Z) ||
+               x.kind == BK_BLOCK;
     }
     bool runnable(const BGate &x, uint64_t regs, bool force_diag) const {
+        if (x.kind == BK_BLOCK) {  // every qubit of a dense block in a register position
+            const uint64_t bm = block_mask(x);
+            return (regs & bm) == bm;
+        }
         if (x.kind == BK_MAT1)  // a diagonal gate on a qubit outside the tile never reaches a register
             return ((regs >> x.q0) & 1ULL) || (x.diag && (force_diag || !((p.resident >> x.q0) & 1ULL)));
         if (x.kind == BK_CNOT) return (regs >> x.q1) & 1ULL;
@@ -394,14 +422,46 @@ struct PassGen {
     // register qubits for the next layout: greedily the qubits that let the
     // most dense gates (then gates) run
     std::vector<uint32_t> choose_regs() const {
-        std::vector<uint32_t> S;
+        std::vector<uint32_t> best = greedy_regs({});
+        bool any_block = false;
+        for (size_t j = 0; j < p.gates.size(); ++j) any_block = any_block || (!done[j] && p.gates[j].kind == BK_BLOCK);
+        if (!any_block) return best;
+        // a dense block runs only with all its qubits in registers: try each
+        // ready block's qubits as the start of the register set
+        auto score = [&](const std::vector<uint32_t> &S, int *dn) {
+            uint64_t m = 0;
+            for (uint32_t q : S) m |= 1ULL << q;
+            std::vector<char> d = done;
+            return simulate(m, d, false, dn);
+        };
+        int bd = 0;
+        int ba = score(best, &bd);
+        for (size_t j = 0; j < p.gates.size(); ++j) {
+            const BGate &x = p.gates[j];
+            if (done[j] || x.kind != BK_BLOCK || !ready(j, done)) continue;
+            std::vector<uint32_t> base(x.bq, x.bq + x.nq);
+            std::vector<uint32_t> S = greedy_regs(base);
+            int dn = 0;
+            const int all = score(S, &dn);
+            if (dn > bd || (dn == bd && all > ba)) {
+                best = S;
+                bd = dn;
+                ba = all;
+            }
+        }
+        return best;
+    }
+    // from `base`, add the qubit that lets the most dense gates (then gates)
+    // run, until four register qubits are chosen or no qubit adds a gate
+    std::vector<uint32_t> greedy_regs(std::vector<uint32_t> S) const {
         uint64_t mask = 0;
+        for (uint32_t q : S) mask |= 1ULL << q;
         int best_dense = -1, best_all = -1;
         {
             std::vector<char> d = done;
-            best_all = simulate(0, d, false, &best_dense);
+            best_all = simulate(mask, d, false, &best_dense);
         }
-        for (int k = 0; k < 4; ++k) {
+        for (int k = (int)S.size(); k < 4; ++k) {
             int pick = -1, pd = best_dense, pa = best_all;
             for (int s = K - 1; s >= 0; --s) {  // ties keep qubits 0..4 for the lanes
                 const uint32_t q = slot_q[s];
@@ -599,7 +659,8 @@ struct PassGen {
             return;
         }
         if (!dual)
-            s << "extern \"C\" __global__ void __launch_bounds__(" << threads_of(K) << ", " << (K == 12 ? 3 : 1) << ") p" << index
+            s << "extern \"C\" __global__ void __launch_bounds__(" << threads_of(K) << ", "
+              << (K == 12 ? (p.max_block >= 2 ? 2 : 3) : 1) << ") p" << index
               << "(float2* __restrict__ A, unsigned long long nt) {\n";
         else
             s << "extern \"C\" __global__ void __launch_bounds__(" << threads_of(K) << ", 2) b" << index
@@ -831,6 +892,7 @@ struct PassGen {
             break;
         }
         case BK_OVL: emit_overlap(x); break;
+        case BK_BLOCK: emit_block(x); break;
         default: {  // SWAP of two resident qubits: relabel
             const int a = pos_of(x.q0), b = pos_of(x.q1);
             std::swap(L[a], L[b]);
@@ -838,6 +900,44 @@ struct PassGen {
         }
         }
         g.pfx = "r";
+    }
+
+    // A dense 2^m x 2^m block (m <= 4) whose qubits all sit in register
+    // positions: for every setting of the other register bits, the thread's
+    // 2^m amplitudes times the block's matrix (row-major in the constant
+    // bank), four FMAs per complex multiply-add.
+    void emit_block(const BGate &x) {
+        auto &s = g.s;
+        const int m = x.nq, D = 1 << m;
+        int rb[kMaxBlockQubits];
+        uint32_t bits = 0;
+        for (int i = 0; i < m; ++i) {
+            rb[i] = pos_of(x.bq[i]) - 5;
+            bits |= 1u << rb[i];
+        }
+        const int base = block_slots(g, *bmats, x.boff, D);
+        for (int i0 = 0; i0 < kR; ++i0) {
+            if (i0 & (int)bits) continue;
+            auto idx = [&](int c) {
+                int r = i0;
+                for (int i = 0; i < m; ++i)
+                    if ((c >> i) & 1) r |= 1 << rb[i];
+                return r;
+            };
+            s << "{";
+            for (int c = 0; c < D; ++c) s << "const float2 x" << c << "=" << g.R(idx(c)) << ";";
+            s << "\n";
+            for (int r = 0; r < D; ++r) {
+                std::ostringstream re, im;
+                for (int c = 0; c < D; ++c) {
+                    const std::string e = "M[" + std::to_string(4 * base + r * D + c) + "]";
+                    re << (c ? "+" : "") << e << ".x*x" << c << ".x-" << e << ".y*x" << c << ".y";
+                    im << (c ? "+" : "") << e << ".x*x" << c << ".y+" << e << ".y*x" << c << ".x";
+                }
+                s << g.R(idx(r)) << ".x=" << re.str() << ";" << g.R(idx(r)) << ".y=" << im.str() << ";\n";
+            }
+            s << "}\n";
+        }
     }
 
     // multiply the tile (psi and lambda alike) by the factors pulled out so
@@ -1061,6 +1161,10 @@ std::string plan_key(const Plan &plan, bool dual) {
             }
             put(x.q0, 1);
             put(x.q1, 1);
+            if (x.kind == BK_BLOCK) {
+                put(x.nq, 1);
+                for (int i = 0; i < x.nq; ++i) put(x.bq[i], 1);
+            }
             if (x.kind == BK_OVL) {
                 put(x.axis, 1);
                 put((uint64_t)x.op_index, 4);
@@ -1083,6 +1187,7 @@ void replay_consts(const Plan &plan, const std::vector<std::vector<int>> &orders
             for (int j : orders[pi]) {
                 const BGate &x = p.gates[j];
                 if (x.kind == BK_OVL && g.any_scale) g.slot(std::norm(g.pscale), 0.0, 0.0, 0.0);
+                if (x.kind == BK_BLOCK) block_slots(g, plan.bmats, x.boff, 1 << x.nq);
                 if (x.kind != BK_MAT1) continue;
                 const std::complex<double> m[4] = {{x.m[0], x.m[1]}, {x.m[2], x.m[3]}, {x.m[4], x.m[5]}, {x.m[6], x.m[7]}};
                 if (x.diag) {
@@ -1131,6 +1236,16 @@ GenCache &gen_cache() {
     return c;
 }
 
+// Upper bound of the constant-bank bytes one pass adds.
+size_t pass_const_bytes(const Pass &p) {
+    size_t b = 64;
+    for (const BGate &x : p.gates) {
+        if (x.kind == BK_BLOCK) b += (size_t)8 << (2 * x.nq);
+        else b += 2 * 32;  // a matrix (plus a possible mid-pass scale)
+    }
+    return b;
+}
+
 bool gen_modules_uncached(const Plan &plan, std::vector<ModulePlan> &mods, std::vector<std::vector<int>> &orders,
                           bool dual) {
     Gen g;
@@ -1143,10 +1258,10 @@ bool gen_modules_uncached(const Plan &plan, std::vector<ModulePlan> &mods, std::
         std::ostringstream body;
         g.consts.clear();
         int local = 0;
-        while (pi < npass && local < 8 && g.consts.size() * 8 < 56 * 1024) {
+        while (pi < npass && local < 8 && (local == 0 || g.consts.size() * 8 + pass_const_bytes(plan.passes[pi]) < 60 * 1024)) {
             g.s.str("");
             g.s.clear();
-            PassGen pg(g, plan.passes[pi], plan.n, dual);
+            PassGen pg(g, plan.passes[pi], plan.n, dual, &plan.bmats);
             pg.emit_kernel(local, pi + 1 == npass);
             if (pg.failed) return false;
             body << g.s.str();
@@ -1285,10 +1400,11 @@ int grid_of(qf_ctx *ctx, cudaKernel_t k, int K, uint64_t n_tiles, uint64_t *grid
 // Generate, compile (or fetch) and launch the plan's passes.
 int run_plan_jit(qf_sv *sv, const Plan &plan, int) {
     const int wb = (int)plan.passes[0].a.k - 9;
-    if (!jit_plan_fits(plan)) return run_plan_rs(sv, plan, wb);  // interpreted (falls back to shared memory)
+    // interpreted when the plan does not fit the compiled layout
+    if (!jit_plan_fits(plan)) return plan.block_qubits ? run_plan_blocks(sv, plan) : run_plan_rs(sv, plan, wb);
     qf_ctx *ctx = sv->ctx;
     std::vector<ModulePlan> mods;
-    if (!gen_modules(plan, mods)) return run_plan_rs(sv, plan, wb);
+    if (!gen_modules(plan, mods)) return plan.block_qubits ? run_plan_blocks(sv, plan) : run_plan_rs(sv, plan, wb);
     std::vector<std::shared_ptr<JitModule>> handles;
     QF_TRY(fetch_modules(ctx, mods, handles));
     for (size_t m = 0; m < mods.size(); ++m) {

@@ -3,6 +3,7 @@
 // CPU-only test-suite through qf_plan_stats / qf_rng_jump.
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <cstring>
 
 #include "qf_internal.h"
@@ -300,6 +301,212 @@ uint64_t choose_resident(const std::vector<Item> &items, const std::vector<int> 
 }
 }  // namespace
 
+// ---- k-qubit dense-block fusion --------------------------------------------
+// The reference applies every gate as its own sweep (StateVector::apply,
+// src/lib.rs:1017-1059; kernel per gate in src/cuda.rs:114-128) and fuses
+// nothing but same-axis rotation angles (src/optimizer.rs:767). Here the gates
+// of one tile pass are multiplied into dense blocks of up to k qubits on the
+// host in f64; the device then applies one 2^m x 2^m matrix per block.
+using cd = std::complex<double>;
+
+namespace {
+struct FBlock {
+    uint64_t mask = 0;
+    std::vector<uint32_t> qs;  // ascending; bit i of the local index is qubit qs[i]
+    std::vector<cd> M;         // row-major 2^m x 2^m
+    int gates = 0;
+    BGate first;               // the gate, when the block holds exactly one
+    bool varying = false;
+};
+
+}  // namespace
+
+std::vector<uint32_t> qubits_of_mask(uint64_t m) {
+    std::vector<uint32_t> q;
+    for (uint32_t b = 0; b < 64; ++b)
+        if ((m >> b) & 1ULL) q.push_back(b);
+    return q;
+}
+static int local_of(const std::vector<uint32_t> &qs, uint32_t q) {
+    for (size_t i = 0; i < qs.size(); ++i)
+        if (qs[i] == q) return (int)i;
+    return -1;
+}
+
+// A matrix on ascending qubits `qs` widened to the ascending superset `nq`:
+// M (x) identity on the added qubits.
+std::vector<cd> widen_matrix(const std::vector<uint32_t> &qs, const std::vector<cd> &M, const std::vector<uint32_t> &nq) {
+    const int m = (int)nq.size(), d = 1 << m, od = 1 << qs.size();
+    std::vector<int> old(m);
+    for (int i = 0; i < m; ++i) old[i] = local_of(qs, nq[i]);
+    std::vector<cd> N((size_t)d * d, cd(0.0, 0.0));
+    for (int r = 0; r < d; ++r)
+        for (int c = 0; c < d; ++c) {
+            uint32_t ro = 0, co = 0;
+            bool ok = true;
+            for (int i = 0; i < m && ok; ++i) {
+                const int rb = (r >> i) & 1, cb = (c >> i) & 1;
+                if (old[i] < 0) ok = rb == cb;
+                else {
+                    ro |= (uint32_t)rb << old[i];
+                    co |= (uint32_t)cb << old[i];
+                }
+            }
+            if (ok) N[(size_t)r * d + c] = M[(size_t)ro * od + co];
+        }
+    return N;
+}
+
+// v <- G v for one gate on local bits l0 (l1), the semantics of
+// StateVector::apply / apply_cnot / apply_cz / apply_swap (src/lib.rs:1017-1122).
+static void vec_apply(std::vector<cd> &v, int d, const BGate &g, int l0, int l1) {
+    switch (g.kind) {
+    case BK_MAT1: {
+        const cd m00(g.m[0], g.m[1]), m01(g.m[2], g.m[3]), m10(g.m[4], g.m[5]), m11(g.m[6], g.m[7]);
+        for (int i = 0; i < d; ++i)
+            if (!((i >> l0) & 1)) {
+                const int j = i | (1 << l0);
+                const cd a = v[i], b = v[j];
+                v[i] = m00 * a + m01 * b;
+                v[j] = m10 * a + m11 * b;
+            }
+        break;
+    }
+    case BK_CNOT:
+        for (int i = 0; i < d; ++i)
+            if (((i >> l0) & 1) && !((i >> l1) & 1)) std::swap(v[i], v[i | (1 << l1)]);
+        break;
+    case BK_CZ:
+        for (int i = 0; i < d; ++i)
+            if (((i >> l0) & 1) && ((i >> l1) & 1)) v[i] = -v[i];
+        break;
+    default:  // SWAP
+        for (int i = 0; i < d; ++i)
+            if (((i >> l0) & 1) && !((i >> l1) & 1)) std::swap(v[i], v[(i & ~(1 << l0)) | (1 << l1)]);
+        break;
+    }
+}
+
+// M <- G M for a one- or two-qubit gate on qubits within `qs`: the gate
+// applied to every column.
+void apply_gate_to_matrix(const std::vector<uint32_t> &qs, std::vector<cd> &M, const BGate &g) {
+    const int d = 1 << qs.size();
+    const int l0 = local_of(qs, g.q0), l1 = g.kind == BK_MAT1 ? -1 : local_of(qs, g.q1);
+    std::vector<cd> v(d);
+    for (int c = 0; c < d; ++c) {
+        for (int r = 0; r < d; ++r) v[r] = M[(size_t)r * d + c];
+        vec_apply(v, d, g, l0, l1);
+        for (int r = 0; r < d; ++r) M[(size_t)r * d + c] = v[r];
+    }
+}
+
+// Dense matrix of a gate or a fused block over its qubits (ascending).
+void dense_matrix(const BGate &g, const std::vector<double> &bmats, std::vector<uint32_t> &qs, std::vector<cd> &M) {
+    if (g.kind == BK_BLOCK) {
+        qs.assign(g.bq, g.bq + g.nq);
+        const size_t dd = (size_t)1 << (2 * g.nq);
+        M.resize(dd);
+        for (size_t e = 0; e < dd; ++e) M[e] = cd(bmats[2 * (g.boff + e)], bmats[2 * (g.boff + e) + 1]);
+        return;
+    }
+    qs.clear();
+    qs.push_back(g.q0);
+    if (g.kind != BK_MAT1) qs.push_back(g.q1);
+    std::sort(qs.begin(), qs.end());
+    const int d = 1 << qs.size();
+    M.assign((size_t)d * d, cd(0.0, 0.0));
+    for (int i = 0; i < d; ++i) M[(size_t)i * d + i] = 1.0;
+    apply_gate_to_matrix(qs, M, g);
+}
+
+namespace {
+// The tensor product of open blocks on disjoint qubits, over `nq` (their union).
+std::vector<cd> kron_blocks(const std::vector<const FBlock *> &bs, const std::vector<uint32_t> &nq) {
+    const int m = (int)nq.size(), d = 1 << m;
+    std::vector<cd> P((size_t)d * d);
+    std::vector<std::vector<int>> pos(bs.size());
+    int covered = 0;
+    for (size_t b = 0; b < bs.size(); ++b)
+        for (uint32_t q : bs[b]->qs) {
+            pos[b].push_back(local_of(nq, q));
+            covered |= 1 << pos[b].back();
+        }
+    for (int r = 0; r < d; ++r)
+        for (int c = 0; c < d; ++c) {
+            if ((r ^ c) & ~covered) {  // qubits of nq outside every block: identity
+                P[(size_t)r * d + c] = 0.0;
+                continue;
+            }
+            cd v(1.0, 0.0);
+            for (size_t b = 0; b < bs.size() && v != cd(0.0, 0.0); ++b) {
+                uint32_t rb = 0, cb = 0;
+                for (size_t i = 0; i < pos[b].size(); ++i) {
+                    rb |= (uint32_t)((r >> pos[b][i]) & 1) << i;
+                    cb |= (uint32_t)((c >> pos[b][i]) & 1) << i;
+                }
+                v *= bs[b]->M[(size_t)rb * (1u << pos[b].size()) + cb];
+            }
+            P[(size_t)r * d + c] = v;
+        }
+    return P;
+}
+
+// Greedy fusion of a pass's gates (in order) into blocks of at most k qubits.
+// Open blocks act on disjoint qubits. A gate joins the open blocks it touches
+// when their union with its qubits has at most k qubits; otherwise the widest
+// of those blocks are closed (emitted) until the rest fits. Every block that
+// touches a qubit is emitted after the blocks holding earlier gates on that
+// qubit, so the emitted product equals the gate sequence.
+std::vector<FBlock> fuse_gates(const std::vector<BGate> &gates, int k) {
+    std::vector<FBlock> open, out;
+    for (const BGate &g : gates) {
+        const uint64_t gm = g.kind == BK_MAT1 ? (1ULL << g.q0) : ((1ULL << g.q0) | (1ULL << g.q1));
+        std::vector<size_t> I;
+        for (size_t j = 0; j < open.size(); ++j)
+            if (open[j].mask & gm) I.push_back(j);
+        auto width = [&]() {
+            uint64_t u = gm;
+            for (size_t j : I) u |= open[j].mask;
+            return popc(u);
+        };
+        std::vector<size_t> closing;
+        while (width() > k) {
+            size_t wi = 0;
+            for (size_t t = 1; t < I.size(); ++t)
+                if (popc(open[I[t]].mask) > popc(open[I[wi]].mask)) wi = t;
+            closing.push_back(I[wi]);
+            I.erase(I.begin() + (long)wi);
+        }
+        FBlock nb;
+        nb.mask = gm;
+        for (size_t j : I) nb.mask |= open[j].mask;
+        nb.qs = qubits_of_mask(nb.mask);
+        std::vector<const FBlock *> parts;
+        for (size_t j : I) {  // disjoint blocks commute: their tensor product (identity elsewhere)
+            parts.push_back(&open[j]);
+            nb.gates += open[j].gates;
+            nb.varying = nb.varying || open[j].varying;
+            if (open[j].gates == 1) nb.first = open[j].first;
+        }
+        nb.M = kron_blocks(parts, nb.qs);
+        apply_gate_to_matrix(nb.qs, nb.M, g);
+        if (nb.gates == 0) nb.first = g;
+        ++nb.gates;
+        nb.varying = nb.varying || g.varying;
+        // emit the closed blocks, then replace the merged ones by the new block
+        std::sort(closing.begin(), closing.end());
+        for (size_t j : closing) out.push_back(open[j]);
+        std::vector<size_t> gone = closing;
+        gone.insert(gone.end(), I.begin(), I.end());
+        std::sort(gone.begin(), gone.end());
+        for (size_t t = gone.size(); t-- > 0;) open.erase(open.begin() + (long)gone[t]);
+        open.push_back(std::move(nb));
+    }
+    for (FBlock &b : open) out.push_back(std::move(b));
+    return out;
+}
+}  // namespace
+
 int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, Plan &plan) {
     plan = Plan();
     plan.n = n;
@@ -311,10 +518,16 @@ int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, 
     const uint64_t all = n >= 64 ? ~0ULL : ((1ULL << n) - 1);
     const uint64_t low_mask = (low >= 64) ? ~0ULL : ((1ULL << low) - 1);
 
+    const int kb = (!o.backward && o.block_qubits >= 2) ? std::min(o.block_qubits, kMaxBlockQubits) : 0;
+    if (kb && kb > k) return fail(QF_ERR_INVALID_ARGUMENT, "blocks of %d qubits do not fit a %d-qubit tile", kb, k);
+    plan.block_qubits = (uint32_t)kb;
     std::vector<Item> items;
     items.reserve(gates.size() * (o.backward ? 2 : 1));
     if (!o.backward) {
-        for (const BGate &g : gates) items.push_back(make_item(g, false));
+        for (const BGate &g : gates) {
+            items.push_back(make_item(g, false));
+            if (kb) items.back().need = items.back().touch;  // a dense block needs all its qubits in the tile
+        }
     } else {
         for (size_t i = gates.size(); i-- > 0;) {
             if (gates[i].axis != 255) items.push_back(make_item(gates[i], true));
@@ -365,6 +578,49 @@ int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, 
         }
         if (taken.empty()) return fail(QF_ERR_INVALID_ARGUMENT, "planner made no progress");
         remaining.swap(rest);
+        uint32_t n_blocks = 0, max_block = 0;
+        if (kb) {  // the pass's gates as dense blocks of up to kb qubits
+            std::vector<BGate> seq;
+            seq.reserve(taken.size());
+            for (const Item &it : taken) seq.push_back(it.g);
+            std::vector<Item> fused;
+            for (FBlock &b : fuse_gates(seq, kb)) {
+                if (b.gates == 1) {  // a lone gate keeps its own (cheaper) form
+                    fused.push_back(make_item(b.first, false));
+                } else if (b.qs.size() == 1) {  // a product of one-qubit gates
+                    BGate g;
+                    g.kind = BK_MAT1;
+                    g.q0 = b.qs[0];
+                    for (int e = 0; e < 4; ++e) {
+                        g.m[2 * e] = b.M[e].real();
+                        g.m[2 * e + 1] = b.M[e].imag();
+                    }
+                    g.diag = matrix_is_diag(g.m);
+                    g.varying = b.varying;
+                    fused.push_back(make_item(g, false));
+                } else {
+                    BGate g;
+                    g.kind = BK_BLOCK;
+                    g.nq = (uint8_t)b.qs.size();
+                    for (size_t i = 0; i < b.qs.size(); ++i) g.bq[i] = (uint8_t)b.qs[i];
+                    g.q0 = b.qs[0];
+                    g.q1 = b.qs[1];
+                    g.varying = b.varying;
+                    g.boff = (uint32_t)(plan.bmats.size() / 2);
+                    for (const cd &z : b.M) {
+                        plan.bmats.push_back(z.real());
+                        plan.bmats.push_back(z.imag());
+                    }
+                    Item it;
+                    it.g = g;
+                    it.touch = it.need = b.mask;
+                    fused.push_back(it);
+                    ++n_blocks;
+                    max_block = std::max<uint32_t>(max_block, g.nq);
+                }
+            }
+            taken.swap(fused);
+        }
 
         // widen the tile with the lowest free qubits: longer contiguous runs
         for (uint32_t q = 0; q < n && popc(L) < k; ++q) L |= 1ULL << q;
@@ -389,6 +645,8 @@ int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, 
         p.a.nonlocal_mask = all & ~L;
         p.a.n_tiles = 1ULL << (n - p.a.k);
         p.resident = L;
+        p.n_blocks = n_blocks;
+        p.max_block = max_block;
         p.op_begin = (uint32_t)plan.ops.size();
         p.mat_begin = (uint32_t)(plan.mats.size() / 8);
         p.a.slot_base = plan.n_slots;
@@ -431,6 +689,13 @@ int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, 
             }
             p.gates.push_back(g);
             switch (g.kind) {
+            case BK_BLOCK: {
+                t.kind = T_BLOCK;
+                t.b0 = g.nq;
+                for (int i = 0; i < g.nq; ++i) t.g0 |= (uint32_t)local_bit[g.bq[i]] << (5 * i);
+                t.mat = g.boff;
+                break;
+            }
             case BK_MAT1: {
                 const Factored f = (!g.diag && !o.backward) ? factor_unitary_2x2(g.m) : Factored();
                 if (f.ok) {

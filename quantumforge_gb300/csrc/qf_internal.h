@@ -96,7 +96,11 @@ int ensure_pinned(void **ptr, size_t *bytes, size_t need);
 // A gate list with parameters resolved to matrices (host, f64).
 // BK_OVL marks an adjoint overlap Im<lambda|P_q0 psi> in a backward pass:
 // P = X/Y/Z from `axis`, op_index = the overlap slot.
-enum BKind : uint8_t { BK_MAT1 = 0, BK_CNOT = 1, BK_CZ = 2, BK_SWAP = 3, BK_OVL = 4 };
+// BK_BLOCK is a dense 2^nq x 2^nq block on qubits bq[0..nq-1] (ascending; bit
+// i of the block's local index is qubit bq[i]) made by k-qubit fusion; its
+// matrix is row-major complex at Plan::bmats[2 * boff ...].
+enum BKind : uint8_t { BK_MAT1 = 0, BK_CNOT = 1, BK_CZ = 2, BK_SWAP = 3, BK_OVL = 4, BK_BLOCK = 5 };
+constexpr int kMaxBlockQubits = 5;
 
 struct BGate {
     uint8_t kind = BK_MAT1;
@@ -107,6 +111,9 @@ struct BGate {
     int64_t op_index = -1;   // index into the caller's op list
     int64_t param = -1;      // parameter index of a rotation occurrence
     double m[8] = {0};       // m00, m01, m10, m11 as (re, im)
+    uint8_t nq = 0;          // BK_BLOCK: qubits of the block
+    uint8_t bq[kMaxBlockQubits] = {0};
+    uint32_t boff = 0;       // BK_BLOCK: complex offset of the matrix in Plan::bmats
 };
 
 // Gate::matrix (src/lib.rs:2267-2333) evaluated on the host in f64.
@@ -154,7 +161,9 @@ enum TKind : uint8_t {
     T_OVL_ZG = 12,  // adjoint overlap with Z on non-local g0
     T_MAT1F = 13,   // factored unitary on local bit b0: mats[mat] = (r0, r1, -, -); b1 bit 0 pivot, bit 1 sigma < 0,
                     // bit 2 r imaginary
-    T_SCALE = 14    // every amplitude times mats[mat].m00 (the factors pulled out by T_MAT1F)
+    T_SCALE = 14,   // every amplitude times mats[mat].m00 (the factors pulled out by T_MAT1F)
+    T_BLOCK = 15    // dense 2^b0 x 2^b0 block on local bits (g0 >> 5i) & 31, i < b0; matrix at complex offset
+                    // `mat` of the plan's block matrices (row-major)
 };
 
 struct TileOp {
@@ -190,6 +199,8 @@ struct Pass {
     uint32_t mat_begin = 0;   // into Plan::mats (matrix index)
     uint64_t resident = 0;    // qubits resident in the tile
     std::vector<BGate> gates; // the pass's gates in order (after 1q merging, overlaps as BK_OVL), global qubits
+    uint32_t n_blocks = 0;    // BK_BLOCK items among `gates`
+    uint32_t max_block = 0;   // widest of them (qubits)
 };
 
 // ---- register-tiled passes (complex64) -------------------------------------
@@ -253,6 +264,8 @@ struct Plan {
     std::vector<double> mats;        // 8 doubles per matrix
     std::vector<int64_t> slot_param; // overlap slot -> parameter index
     uint32_t n_slots = 0;
+    std::vector<double> bmats;       // dense block matrices (interleaved complex), see BK_BLOCK
+    uint32_t block_qubits = 0;       // fusion width the plan was made with (0: gates one by one)
 };
 
 struct PlanOpts {
@@ -262,9 +275,19 @@ struct PlanOpts {
     bool backward = false;  // adjoint reverse sweep: inverse gates + overlaps
     int max_items = 768;    // bound on ops per pass (shared-memory budget)
     bool search = true;     // choose each pass's resident qubits by look-ahead
+    int block_qubits = 0;   // forward plans: fuse each pass's gates into dense blocks of up to this many
+                            // qubits (2..5); every qubit a gate touches is then tile-resident
 };
 
 int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, Plan &plan);
+// Dense matrices of gates and fused blocks (host, f64, row-major, bit i of
+// the local index = i-th qubit of the ascending list `qs`).
+void dense_matrix(const BGate &g, const std::vector<double> &bmats, std::vector<uint32_t> &qs,
+                  std::vector<std::complex<double>> &M);
+std::vector<std::complex<double>> widen_matrix(const std::vector<uint32_t> &qs, const std::vector<std::complex<double>> &M,
+                                               const std::vector<uint32_t> &nq);
+void apply_gate_to_matrix(const std::vector<uint32_t> &qs, std::vector<std::complex<double>> &M, const BGate &g);
+std::vector<uint32_t> qubits_of_mask(uint64_t m);
 // Lower a forward plan to register-tiled passes; passes whose tile is not
 // {qubits 0..4} plus 4 + wb more qubits are marked fallback.
 int lower_rs(const Plan &plan, int wb, RsPlan &out);
@@ -280,6 +303,12 @@ int launch_gate2(qf_sv *sv, const BGate &g);
 // (register-tiled for complex64 where the tile fits, shared memory otherwise).
 int run_plan(qf_sv *sv, const Plan &plan, int flags = 0);
 int run_plan_smem(qf_sv *sv, const Plan &plan);
+// Plans with dense blocks: the shared-memory block interpreter (any width,
+// complex64 and complex128) and, for complex64 blocks of 5 qubits, the
+// tensor-core pass (blockmma.cu).
+int run_plan_blocks(qf_sv *sv, const Plan &plan);
+bool mma_blocks_fit(const Plan &plan);
+int run_plan_blocks_mma(qf_sv *sv, const Plan &plan);
 int run_plan_rs(qf_sv *sv, const Plan &plan, int wb);
 // Compiled register-tiled passes (jit.cpp); states of at least kJitMinQubits
 // qubits use them by default.
@@ -357,5 +386,7 @@ uint64_t rng_apply(const uint64_t cols[64], uint64_t state);
 
 // Dispatcher for a bound gate list on a resident state.
 int execute_gates(qf_sv *sv, const std::vector<BGate> &gates, const qf_exec_opts *opts);
+// Planning options of a forward sweep (tile widths, look-ahead, block width).
+int plan_opts_for(uint32_t n, int dtype, const qf_exec_opts *opts, PlanOpts &po);
 
 }  // namespace qf

@@ -488,13 +488,23 @@ struct PGroup {
     uint32_t t_begin;  // into the pass's term array
     uint32_t t_count;
     uint32_t real;     // every coefficient of the group is real
+    // Groups of many terms (the register-tiled pass) are evaluated from two
+    // per-tile tables: their terms are ordered [z only on local bits 0..5 |
+    // only on local bits 6.. | only off the tile | both halves], and
+    // G(j) = TL[j & 63] + TH[j >> 6] + the terms spanning both halves.
+    uint32_t tab;      // table slot, or kNoTable
+    uint32_t n_lo, n_hi, n_const;
 };
+constexpr uint32_t kNoTable = 0xFFFFFFFFu;
+constexpr uint32_t kTableTerms = 6;     // groups with at least this many terms get tables
+constexpr uint32_t kTableEntries = 192;  // 64 (bits 0..5) + up to 128 (bits 6..12)
 struct PPassArgs {
     uint64_t nonlocal_mask;
     uint64_t n_tiles;
     uint32_t k, low, n_groups, n_terms;
     uint32_t mode;  // 0 = expectation, 1 = write lambda, 2 = accumulate lambda
     uint32_t last;  // accumulate <psi|lambda> (mode 1/2)
+    uint32_t n_tables;  // groups evaluated from per-tile tables (register-tiled pass)
     uint8_t hi_q[kMaxLocal];
 };
 
@@ -598,7 +608,8 @@ __global__ void __launch_bounds__(kRedThreads)
     constexpr uint32_t T = 256u * NR;
     const uint32_t nhi = pa.k - pa.low, tid = threadIdx.x;
     C *s = reinterpret_cast<C *>(smem);
-    uint64_t *hi_off = reinterpret_cast<uint64_t *>(smem + (size_t)T * sizeof(C));
+    C *tabs = s + T;  // pa.n_tables x kTableEntries
+    uint64_t *hi_off = reinterpret_cast<uint64_t *>(tabs + (size_t)pa.n_tables * kTableEntries);
     PGroup *groups = reinterpret_cast<PGroup *>(hi_off + (1u << nhi));
     PTermT<R> *terms = reinterpret_cast<PTermT<R> *>(groups + pa.n_groups);
     __shared__ double red[32];
@@ -619,6 +630,27 @@ __global__ void __launch_bounds__(kRedThreads)
     for (uint64_t t = blockIdx.x; t < pa.n_tiles; t += gridDim.x) {
         const uint64_t base = deposit(t, pa.nonlocal_mask);
         for (uint32_t j = tid; j < T; j += blockDim.x) s[j] = psi[base | hi_off[j >> pa.low] | (j & lowmask)];
+        // this tile's tables of the many-term groups: each coefficient signed
+        // by the tile's own bits, then summed per 6-bit half of the local index
+        for (uint32_t g = 0; g < pa.n_groups; ++g) {
+            const PGroup G = groups[g];
+            if (G.tab == kNoTable) continue;
+            C *tb = tabs + (size_t)G.tab * kTableEntries;
+            const uint32_t n_hi_entries = 1u << (pa.k - 6);
+            for (uint32_t e = tid; e < 64u + n_hi_entries; e += blockDim.x) {
+                R vr = 0, vi = 0;
+                const bool lo = e < 64u;
+                const uint32_t a = lo ? e : ((e - 64u) << 6);
+                const uint32_t q0 = G.t_begin + (lo ? 0u : G.n_lo), q1 = G.t_begin + (lo ? G.n_lo : G.n_lo + G.n_hi + G.n_const);
+                for (uint32_t q = q0; q < q1; ++q) {
+                    const PTermT<R> P = terms[q];
+                    const bool odd = (__popc(a & P.zl) + __popcll(base & P.zo)) & 1u;
+                    vr += odd ? -P.cre : P.cre;
+                    vi += odd ? -P.cim : P.cim;
+                }
+                tb[e] = mk(vr, vi);
+            }
+        }
         __syncthreads();
         R tile_re = 0, tile_im = 0;
 #pragma unroll 1
@@ -630,9 +662,22 @@ __global__ void __launch_bounds__(kRedThreads)
                 const PGroup G = groups[g];
                 const uint32_t xo = pa.mode == 0 ? 0u : G.xl;  // phase at the source index of the element
                 R gr[RC], gim[RC];
+                uint32_t q_first = 0;
+                if (G.tab != kNoTable) {  // table lookups, then the terms spanning both halves
+                    const C *tb = tabs + (size_t)G.tab * kTableEntries;
 #pragma unroll
-                for (int r = 0; r < RC; ++r) gr[r] = gim[r] = 0;
-                for (uint32_t q = 0; q < G.t_count; ++q) {
+                    for (int r = 0; r < RC; ++r) {
+                        const uint32_t src = (tid + 256u * (rc + r)) ^ xo;
+                        const C lo = tb[src & 63u], hi = tb[64u + (src >> 6)];
+                        gr[r] = lo.x + hi.x;
+                        gim[r] = lo.y + hi.y;
+                    }
+                    q_first = G.n_lo + G.n_hi + G.n_const;
+                } else {
+#pragma unroll
+                    for (int r = 0; r < RC; ++r) gr[r] = gim[r] = 0;
+                }
+                for (uint32_t q = q_first; q < G.t_count; ++q) {
                     const PTermT<R> P = terms[G.t_begin + q];
                     const uint32_t par = (__popc((tid ^ xo) & P.zl & 0xFFu) + __popc(xo & P.zl & ~0xFFu) + __popcll(base & P.zo)) & 1u;
                     const uint32_t m = (P.q >> rc) ^ (0u - par);
@@ -844,6 +889,9 @@ int plan_pauli(uint32_t n, int dtype, const qf_pauli_term *terms, uint64_t n_ter
             G.t_begin = (uint32_t)P.terms.size();
             G.t_count = (uint32_t)groups[g].second.size();
             G.real = 1;
+            G.tab = kNoTable;
+            G.n_lo = G.n_hi = G.n_const = 0;
+            std::vector<PTerm> part[4];  // low half, high half, off the tile, both halves
             for (PTerm T : groups[g].second) {
                 // the term's z on the resident qubits in tile bits, on the rest as is
                 T.zo = T.z & P.a.nonlocal_mask;
@@ -854,8 +902,19 @@ int plan_pauli(uint32_t n, int dtype, const qf_pauli_term *terms, uint64_t n_ter
                 const uint32_t nr = P.a.k > 8 ? 1u << (P.a.k - 8) : 1u;
                 for (uint32_t r = 0; r < nr && r < 32; ++r) T.q |= (uint32_t)(__builtin_popcount(r & (T.zl >> 8)) & 1) << r;
                 if (T.cim != 0.0) G.real = 0;
-                P.terms.push_back(T);
+                const int kind = (T.zl & 63u) && (T.zl >> 6) ? 3 : (T.zl & 63u) ? 0 : (T.zl >> 6) ? 1 : 2;
+                part[kind].push_back(T);
             }
+            // the register-tiled pass (tiles of 2^9..2^13) evaluates a group of many
+            // terms from two tables unless most of its terms span both halves
+            if (P.a.k >= 9 && P.a.k <= 13 && G.t_count >= kTableTerms && part[3].size() * 2 < G.t_count) {
+                G.tab = P.a.n_tables++;
+                G.n_lo = (uint32_t)part[0].size();
+                G.n_hi = (uint32_t)part[1].size();
+                G.n_const = (uint32_t)part[2].size();
+            }
+            for (int kind = 0; kind < 4; ++kind)
+                for (const PTerm &T : part[kind]) P.terms.push_back(T);
             P.groups.push_back(G);
         }
         P.a.n_groups = (uint32_t)P.groups.size();
@@ -920,7 +979,8 @@ int run_pauli(qf_sv *psi, qf_sv *lam, PauliPlan &plan, bool apply, double out[2]
         QF_CUDA(cudaMemcpyAsync(dt, P.terms.data(), P.terms.size() * sizeof(PTerm), cudaMemcpyHostToDevice, ctx->stream));
         off += (P.terms.size() * sizeof(PTerm) + 15) / 16 * 16;
         auto rk = PauliRKernel<C>::get(P.a.k);
-        const size_t head = ((size_t)1 << P.a.k) * sizeof(C) + (8u << (P.a.k - P.a.low)) + P.groups.size() * sizeof(PGroup);
+        const size_t head = ((size_t)1 << P.a.k) * sizeof(C) + (size_t)P.a.n_tables * kTableEntries * sizeof(C) +
+                            (8u << (P.a.k - P.a.low)) + P.groups.size() * sizeof(PGroup);
         const size_t smem = head + P.terms.size() * (rk ? sizeof(PTermT<R>) : sizeof(PTermR<R>));
         if (smem > dyn_limit[ctx->device & 63])
             return fail(QF_ERR_UNSUPPORTED_OPERATION, "Pauli pass needs too much shared memory");

@@ -549,6 +549,172 @@ __global__ void __launch_bounds__(kThreads)
             partials[(size_t)(pa.slot_base + s) * partial_stride + blockIdx.x] = acc[s];
 }
 
+// ---------------------------------------------------------------------------
+// Dense-block passes (k-qubit fusion, any width up to 5): the shared-memory
+// interpreter. A T_BLOCK op multiplies every group of 2^m amplitudes (the
+// tile indices that differ only in the block's m local bits) by the block's
+// 2^m x 2^m matrix. Thread (group, part) holds the group's inputs in
+// registers and computes outputs part, part + S, ... into the other tile
+// buffer; the buffers then swap, so no output overwrites an input another
+// thread still reads. S (a power of two up to 2^m) spreads small group counts
+// over the CTA. Lanes of a warp share `part` and so read the same matrix
+// entries (broadcast loads).
+// ---------------------------------------------------------------------------
+template <typename C, int M>
+__device__ __forceinline__ void block_apply(const C *__restrict__ in, C *__restrict__ out, const TileOp &op,
+                                            const C *__restrict__ bm, uint32_t T) {
+    using R = typename Real<C>::T;
+    constexpr int D = 1 << M;
+    uint32_t bit[M];
+#pragma unroll
+    for (int i = 0; i < M; ++i) bit[i] = (op.g0 >> (5 * i)) & 31u;
+    uint32_t off[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+        uint32_t o = 0;
+#pragma unroll
+        for (int i = 0; i < M; ++i)
+            if ((c >> i) & 1) o |= 1u << bit[i];
+        off[c] = o;
+    }
+    const uint32_t groups = T >> M;
+    uint32_t S = 1;
+    while (S < (uint32_t)D && groups * (S << 1) <= blockDim.x) S <<= 1;
+    const uint32_t items = groups * S;
+    const C *mx = bm + op.mat;
+    for (uint32_t it = threadIdx.x; it < items; it += blockDim.x) {
+        const uint32_t g = it % groups, part = it / groups;
+        uint32_t base = g;  // insert a zero at every block bit, lowest first
+        uint32_t sorted[M];
+#pragma unroll
+        for (int i = 0; i < M; ++i) sorted[i] = bit[i];
+#pragma unroll
+        for (int i = 0; i < M; ++i)
+#pragma unroll
+            for (int j = 0; j + 1 < M - i; ++j)
+                if (sorted[j] > sorted[j + 1]) {
+                    const uint32_t t = sorted[j];
+                    sorted[j] = sorted[j + 1];
+                    sorted[j + 1] = t;
+                }
+#pragma unroll
+        for (int i = 0; i < M; ++i) base = insert0_32(base, sorted[i]);
+        C x[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) x[c] = in[base | off[c]];
+        for (uint32_t r = part; r < (uint32_t)D; r += S) {
+            R yr = 0, yi = 0;
+#pragma unroll
+            for (int c = 0; c < D; ++c) {
+                const C m = mx[r * D + c];
+                yr += m.x * x[c].x - m.y * x[c].y;
+                yi += m.x * x[c].y + m.y * x[c].x;
+            }
+            out[base | off[r]] = mk(yr, yi);
+        }
+    }
+}
+
+template <typename C>
+__global__ void __launch_bounds__(kThreads)
+    k_block_pass(C *__restrict__ psi, const PassArgs pa, const TileOp *__restrict__ g_ops,
+                 const double *__restrict__ g_mats, const C *__restrict__ g_bmats) {
+    using R = typename Real<C>::T;
+    extern __shared__ __align__(16) unsigned char smem[];
+    // the dual layout gives the second tile buffer
+    const TileSmem L = tile_smem(pa.k, pa.low, pa.n_ops, pa.n_mats, 0, true, sizeof(C));
+    C *buf[2] = {reinterpret_cast<C *>(smem + L.s0), reinterpret_cast<C *>(smem + L.s1)};
+    uint64_t *hi_off = reinterpret_cast<uint64_t *>(smem + L.hi);
+    TileOp *ops = reinterpret_cast<TileOp *>(smem + L.ops);
+    C *mats = reinterpret_cast<C *>(smem + L.mats);
+
+    const uint32_t T = 1u << pa.k, nhi = pa.k - pa.low;
+    for (uint32_t h = threadIdx.x; h < (1u << nhi); h += blockDim.x) {
+        uint64_t off = 0;
+        for (uint32_t r = 0; r < nhi; ++r)
+            if ((h >> r) & 1u) off |= 1ULL << pa.hi_q[r];
+        hi_off[h] = off;
+    }
+    for (uint32_t o = threadIdx.x; o < pa.n_ops; o += blockDim.x) ops[o] = g_ops[o];
+    for (uint32_t e = threadIdx.x; e < 4 * pa.n_mats; e += blockDim.x)
+        mats[e] = mk((R)g_mats[2 * e], (R)g_mats[2 * e + 1]);
+    __syncthreads();
+
+    for (uint64_t t = blockIdx.x; t < pa.n_tiles; t += gridDim.x) {
+        const uint64_t base = deposit(t, pa.nonlocal_mask);
+        int cur = 0;
+        tile_load(buf[0], psi, base, hi_off, T, pa.low);
+        __syncthreads();
+        for (uint32_t o = 0; o < pa.n_ops; ++o) {
+            const TileOp op = ops[o];
+            if (op.kind == T_BLOCK) {
+                switch (op.b0) {
+                case 2: block_apply<C, 2>(buf[cur], buf[cur ^ 1], op, g_bmats, T); break;
+                case 3: block_apply<C, 3>(buf[cur], buf[cur ^ 1], op, g_bmats, T); break;
+                case 4: block_apply<C, 4>(buf[cur], buf[cur ^ 1], op, g_bmats, T); break;
+                default: block_apply<C, 5>(buf[cur], buf[cur ^ 1], op, g_bmats, T); break;
+                }
+                cur ^= 1;
+            } else {
+                tile_apply<C, false>(op, buf[cur], nullptr, mats, base, T);
+            }
+            __syncthreads();
+        }
+        tile_store(buf[cur], psi, base, hi_off, T, pa.low);
+        __syncthreads();
+    }
+}
+
+template <typename C> static int launch_block_passes(qf_sv *sv, const Plan &plan) {
+    qf_ctx *ctx = sv->ctx;
+    static size_t dyn[64] = {0};
+    const int dev = ctx->device & 63;
+    if (!dyn[dev]) QF_TRY(allow_max_dynamic_smem(k_block_pass<C>, ctx, &dyn[dev]));
+    // upload ops, 2x2 matrices (f64) and block matrices (in the state's precision)
+    const size_t ops_bytes = align_up((uint32_t)(plan.ops.size() * sizeof(TileOp)), 16);
+    const size_t mats_bytes = align_up((uint32_t)(plan.mats.size() * sizeof(double)), 16);
+    const size_t n_bm = plan.bmats.size() / 2;
+    std::vector<C> bm(n_bm);
+    for (size_t i = 0; i < n_bm; ++i) bm[i] = to_c<C>(&plan.bmats[2 * i]);
+    const size_t bm_bytes = n_bm * sizeof(C);
+    QF_TRY(ensure_device(&ctx->ws_plan, &ctx->ws_plan_bytes, ops_bytes + mats_bytes + bm_bytes + 16));
+    unsigned char *d_plan = static_cast<unsigned char *>(ctx->ws_plan);
+    if (!plan.ops.empty())
+        QF_CUDA(cudaMemcpyAsync(d_plan, plan.ops.data(), plan.ops.size() * sizeof(TileOp), cudaMemcpyHostToDevice,
+                                ctx->stream));
+    if (!plan.mats.empty())
+        QF_CUDA(cudaMemcpyAsync(d_plan + ops_bytes, plan.mats.data(), plan.mats.size() * sizeof(double),
+                                cudaMemcpyHostToDevice, ctx->stream));
+    if (bm_bytes)
+        QF_CUDA(cudaMemcpyAsync(d_plan + ops_bytes + mats_bytes, bm.data(), bm_bytes, cudaMemcpyHostToDevice, ctx->stream));
+    const TileOp *d_ops = reinterpret_cast<const TileOp *>(d_plan);
+    const double *d_mats = reinterpret_cast<const double *>(d_plan + ops_bytes);
+    const C *d_bm = reinterpret_cast<const C *>(d_plan + ops_bytes + mats_bytes);
+    uint32_t max_smem = 0;
+    for (const Pass &p : plan.passes)
+        max_smem = std::max(max_smem, tile_smem(p.a.k, p.a.low, p.a.n_ops, p.a.n_mats, 0, true, sizeof(C)).total);
+    if (max_smem > dyn[dev])
+        return fail(QF_ERR_UNSUPPORTED_OPERATION, "block pass needs %u bytes of shared memory (limit %zu)", max_smem,
+                    dyn[dev]);
+    int per_sm = 0;
+    QF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_block_pass<C>, kThreads, max_smem));
+    const uint32_t grid = (uint32_t)std::max(per_sm, 1) * (uint32_t)ctx->sm_count;
+    for (const Pass &p : plan.passes) {
+        const TileSmem L = tile_smem(p.a.k, p.a.low, p.a.n_ops, p.a.n_mats, 0, true, sizeof(C));
+        const uint32_t g = (uint32_t)std::min<uint64_t>(grid, p.a.n_tiles);
+        k_block_pass<C><<<g, kThreads, L.total, ctx->stream>>>(static_cast<C *>(sv->d), p.a, d_ops + p.op_begin,
+                                                               d_mats + 8 * (size_t)p.mat_begin, d_bm);
+        QF_CUDA(cudaGetLastError());
+    }
+    return QF_OK;
+}
+
+int run_plan_blocks(qf_sv *sv, const Plan &plan) {
+    if (plan.passes.empty()) return QF_OK;
+    if (sv->dtype == QF_C64) return launch_block_passes<float2>(sv, plan);
+    return launch_block_passes<double2>(sv, plan);
+}
+
 // slot_sums[s] += sum over blocks of partials[s * stride + b], in block order.
 __global__ void k_reduce_slots(const double *__restrict__ partials, uint32_t stride, uint32_t n_slots,
                                double *__restrict__ slot_sums) {
@@ -630,6 +796,16 @@ int run_plan_smem(qf_sv *sv, const Plan &plan) {
 // (complex128, small states, QF_EXEC_FLAG_SMEM_TILES) in shared memory.
 int run_plan(qf_sv *sv, const Plan &plan, int flags) {
     if (plan.passes.empty()) return QF_OK;
+    if (plan.block_qubits) {  // dense k-qubit blocks
+        if (sv->dtype == QF_C64 && !(flags & QF_EXEC_FLAG_SMEM_TILES)) {
+            if (plan.block_qubits == 5 && !(flags & QF_EXEC_FLAG_BLOCKS_SIMT) && mma_blocks_fit(plan))
+                return run_plan_blocks_mma(sv, plan);
+            if (plan.block_qubits <= 4 && sv->n >= 12 && plan.passes[0].a.k == 12 && !(flags & QF_EXEC_FLAG_NO_JIT) &&
+                ((flags & QF_EXEC_FLAG_JIT) || sv->n >= kJitMinQubits) && jit_available())
+                return run_plan_jit(sv, plan, 3);
+        }
+        return run_plan_blocks(sv, plan);
+    }
     if (sv->dtype == QF_C64 && !(flags & QF_EXEC_FLAG_SMEM_TILES) && sv->n >= 12) {
         const uint32_t k = plan.passes[0].a.k;
         // compiled passes for large states (the compile is amortised over many
@@ -677,11 +853,22 @@ int execute_gates(qf_sv *sv, const std::vector<BGate> &gates, const qf_exec_opts
     if (mode != QF_EXEC_AUTO && mode != QF_EXEC_FUSED)
         return fail(QF_ERR_INVALID_ARGUMENT, "unknown execution mode %d", mode);
     PlanOpts po;
-    forward_tiling(sv->n, sv->dtype, opts ? opts->tile_qubits : 0, opts ? opts->flags : 0, &po.tile_qubits, &po.low_qubits);
-    po.search = !(opts && (opts->flags & QF_EXEC_FLAG_PLAN_FIRST_COME));
+    QF_TRY(plan_opts_for(sv->n, sv->dtype, opts, po));
     Plan plan;
     QF_TRY(plan_passes(sv->n, gates, po, plan));
     return run_plan(sv, plan, opts ? opts->flags : 0);
+}
+
+// Forward-sweep planning options from a caller's qf_exec_opts.
+int plan_opts_for(uint32_t n, int dtype, const qf_exec_opts *opts, PlanOpts &po) {
+    forward_tiling(n, dtype, opts ? opts->tile_qubits : 0, opts ? opts->flags : 0, &po.tile_qubits, &po.low_qubits);
+    po.search = !(opts && (opts->flags & QF_EXEC_FLAG_PLAN_FIRST_COME));
+    const int kb = opts ? opts->block_qubits : 0;
+    if (kb < 0 || kb > kMaxBlockQubits)
+        return fail(QF_ERR_INVALID_ARGUMENT, "block_qubits must be 0..%d, got %d", kMaxBlockQubits, kb);
+    po.block_qubits = kb >= 2 ? std::min<int>(kb, (int)n) : 0;
+    if (po.block_qubits < 2) po.block_qubits = 0;
+    return QF_OK;
 }
 
 }  // namespace qf

@@ -15,6 +15,8 @@ same op list for the same seed. Ops are ``qf_op`` records (``_abi.OP_DTYPE``).
   in [-pi, pi).
 * ``qaoa_maxcut`` — the reference's ``algorithms::qaoa_maxcut``
   (src/algorithms.rs:110-137) as a parameterised op list.
+* ``inverse_circuit`` — C^dagger of a fixed gate list (round-trip checks at
+  sizes the oracle cannot run).
 """
 from __future__ import annotations
 
@@ -179,3 +181,19 @@ def qaoa_maxcut(n: int, edges, p: int, betas, gammas) -> np.ndarray:
         for q in range(n):
             recs.append((_abi.OP_GATE, _abi.GATE_RX, q, 0, 0, 2.0 * betas[layer]))
     return _abi.ops_array(recs)
+
+
+def inverse_circuit(ops: np.ndarray) -> np.ndarray:
+    """C^dagger of a fixed gate list: reversed, S/T swapped with their
+    adjoints, rotation angles negated (``adjoint_gate``, src/lib.rs:2363-2382);
+    CNOT, CZ, SWAP and the other gates are self-inverse."""
+    inv = ops[::-1].copy()
+    swap = {_abi.GATE_S: _abi.GATE_SDG, _abi.GATE_SDG: _abi.GATE_S, _abi.GATE_T: _abi.GATE_TDG,
+            _abi.GATE_TDG: _abi.GATE_T}
+    for r in inv:
+        if int(r["kind"]) == _abi.OP_GATE:
+            g = int(r["gate"])
+            r["gate"] = swap.get(g, g)
+            if g in (_abi.GATE_RX, _abi.GATE_RY, _abi.GATE_RZ):
+                r["theta"] = -r["theta"]
+    return inv

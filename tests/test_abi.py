@@ -177,3 +177,32 @@ def test_context_creation_reports_missing_gpu_cleanly(engine_lib):
     h = C.c_void_p()
     st = engine_lib.qf_ctx_create(0, C.byref(h))
     assert A.STATUS_NAMES[st] == "Cuda" and not h.value
+
+
+def _block_plan(engine_lib, n, ops, k, dtype=A.C64, flags=0):
+    npass, ngate = C.c_uint64(), C.c_uint64()
+    o = A.ExecOpts(A.EXEC_AUTO, 0, k, flags)
+    st = engine_lib.qf_plan_stats(n, dtype, _native.ptr(ops), len(ops), None, 0, None, 0, C.byref(o), C.byref(npass),
+                                  C.byref(ngate))
+    return st, npass.value
+
+
+@pytest.mark.parametrize("dtype", [A.C64, A.C128])
+def test_dense_block_plans(engine_lib, dtype):
+    """k-qubit block fusion plans every width 2..5 (every touched qubit is then
+    tile-resident, so a block plan never has fewer passes than the plain one
+    on the same tiles), and rejects widths outside 0..5."""
+    ops = W.random_circuit(30, 40, 1, two_qubit="mixed")
+    st, plain = _block_plan(engine_lib, 30, ops, 0, dtype)
+    assert st == 0
+    for k in (2, 3, 4, 5):
+        st, npass = _block_plan(engine_lib, 30, ops, k, dtype)
+        assert st == 0 and npass >= plain, (k, npass, plain)
+        assert npass * 8 < len(ops)
+    assert _block_plan(engine_lib, 30, ops, 1, dtype) == (0, plain)  # width 1: gates one by one
+    for bad in (6, -1):
+        st, _ = _block_plan(engine_lib, 30, ops, bad, dtype)
+        assert A.STATUS_NAMES[st] == "InvalidArgument"
+    # a small state is one pass whatever the width
+    small = W.random_circuit(4, 6, 2, two_qubit="mixed")
+    assert _block_plan(engine_lib, 4, small, 5, dtype) == (0, 1)

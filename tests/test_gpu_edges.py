@@ -103,16 +103,9 @@ def test_largest_ghz_state(backend, n, dtype):
 
 
 def _inverse(ops):
-    """C† of a gate list: reversed, S/T swapped with their adjoints, angles negated."""
-    inv = ops[::-1].copy()
-    swap = {A.GATE_S: A.GATE_SDG, A.GATE_SDG: A.GATE_S, A.GATE_T: A.GATE_TDG, A.GATE_TDG: A.GATE_T}
-    for r in inv:
-        if int(r["kind"]) == A.OP_GATE:
-            g = int(r["gate"])
-            r["gate"] = swap.get(g, g)
-            if g in (A.GATE_RX, A.GATE_RY, A.GATE_RZ):
-                r["theta"] = -r["theta"]
-    return inv
+    from quantumforge_gb300 import workloads as W
+
+    return W.inverse_circuit(ops)
 
 
 @pytest.mark.parametrize("plan", ["lookahead", "first_come"])
