@@ -59,6 +59,9 @@ def parse_args():
     ap.add_argument("--qaoa-instances", type=int, default=4096, help="instances of the batched QAOA extra (qaoa4096)")
     ap.add_argument("--density-qubits", type=int, default=14, help="qubits of the density-matrix extra (density14)")
     ap.add_argument("--noise-shots", type=int, default=100_000, help="shots of the noisy-shot extra (noise_shots)")
+    ap.add_argument("--c2-modes", default="unfused,passes,k2,k3,k4,k5,k5_simt",
+                    help="modes of the c2_matrix extra (unfused, passes, k2..k5, k5_simt)")
+    ap.add_argument("--c2-dtypes", default="c64,c128", help="state types of the c2_matrix extra")
     ap.add_argument("--extras-only", action="store_true",
                     help="run only the extras (small profiling runs); prints {\"extra\": ...} instead of the headline")
     return ap.parse_args()
@@ -354,7 +357,7 @@ def run_ours(args):
         if "vqe32" in wanted:
             extra["vqe32"] = vqe32_checkpointed(backend, args.vqe_qubits)
         if "c2_matrix" in wanted:
-            extra["c2_matrix"] = c2_matrix(backend)
+            extra["c2_matrix"] = c2_matrix(backend, modes_wanted=args.c2_modes.split(","), dtypes=args.c2_dtypes.split(","))
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, sample = time_cpu_oracle(n, ops, args.cpu_seconds, threads)
@@ -471,7 +474,7 @@ def unfused_bytes(ops, n, amp_bytes) -> int:
     return tot
 
 
-def c2_matrix(backend, n64: int = 30, n128: int = 26, depth: int = 40, seed: int = 1):
+def c2_matrix(backend, n64: int = 30, n128: int = 26, depth: int = 40, seed: int = 1, modes_wanted=None, dtypes=("c64", "c128")):
     """The headline circuit generator run unfused (one sweep per gate, the
     reference's structure), as per-gate tile passes (the default), and fused
     into dense k-qubit blocks for k = 2..5 (k = 5 on the tensor cores and on
@@ -499,7 +502,11 @@ def c2_matrix(backend, n64: int = 30, n128: int = 26, depth: int = 40, seed: int
              ("k5_simt", {"block_qubits": 5, "blocks_engine": "simt"})]
     out = {"metric": "gates/s", "peak": peak, "peak_kind": f"of {peak_kind}",
            "reference_state": "complex128 per-gate tile passes of the same circuit"}
+    if modes_wanted:
+        modes = [m for m in modes if m[0] in modes_wanted]
     for dtype, n in (("c64", n64), ("c128", n128)):
+        if dtype not in dtypes:
+            continue
         ops = W.random_circuit(n, depth, seed, two_qubit="mixed")
         b = 8 if dtype == "c64" else 16
         ref = qf.StateVector.zero(n, dtype="c128", backend=backend)
@@ -830,7 +837,9 @@ def qaoa_batch(backend, cpu: bool, count: int = 4096):
     from quantumforge_gb300.qaoa import QaoaBatch, autotune_tiles
 
     problems, gam, bet = W.qaoa_batch_problems(count)
-    tiles = autotune_tiles(problems, 4, candidates=(9, 10, 11, 12), reps=1, backend=backend)
+    t0 = time.perf_counter()
+    tiles = autotune_tiles(problems, 4, candidates=(9, 10, 11, 12), large_candidates=(0, 12), reps=1, backend=backend)
+    t_tune = time.perf_counter() - t0
     batch = QaoaBatch(problems, 4, tile_qubits=tiles, backend=backend, use_graph=True)
     batch.run(gam, bet)
     reps = 3
@@ -838,9 +847,26 @@ def qaoa_batch(backend, cpu: bool, count: int = 4096):
     for _ in range(reps):
         cost, grad = batch.run(gam, bet)
     dt = (time.perf_counter() - t0) / reps
+    # algorithmic HBM bytes of the instances in batched passes (above 12
+    # qubits, tiles of 0 = batched): per layer a forward pass A (psi + cost
+    # bytes) and B, one lambda write, per reverse layer passes B and A on psi
+    # and lambda (+ cost bytes); smaller instances stay in L2 / shared memory
+    p = 4
+    algo = 0
+    for n, _ in problems:
+        if n > 12 and tiles.get(n, 0) == 0:
+            N = 1 << n
+            algo += p * (2 * 16 * N + N) + 8 * N + p * (2 * 32 * N + N)
+    peak, peak_kind = hbm_peak()
     out = {"instances": len(problems), "sizes": [12, 14, 16, 18, 20], "p": 4, "batch_s": dt,
            "instances_per_s": len(problems) / dt, "gradient_params_per_instance": 8, "tiles": tiles,
-           "dtype": "complex64", "host_copies_in_timing": True, "mean_cost": float(np.mean(cost))}
+           "tiles_meaning": "per qubit count: up to 12 the tile width of the one-CTA-per-instance kernel; above 12, "
+                            "0 = batched tile passes, else one CTA per instance with that tile width",
+           "autotune_s": t_tune, "dtype": "complex64", "host_copies_in_timing": True, "mean_cost": float(np.mean(cost)),
+           "roofline": {"bound": "hbm", "algorithmic_gb": algo / 1e9, "achieved_gbs": algo / dt / 1e9, "peak": peak,
+                        "frac": algo / dt / 1e9 / peak, "peak_kind": f"of {peak_kind}",
+                        "note": "batched-pass bytes over the whole batch time (small instances, host copies and "
+                                "launch gaps included): a lower bound of the passes' own fraction"}}
     if cpu:
         out["cpu_estimate"] = qaoa_cpu_estimate(problems)
     return out
@@ -1013,7 +1039,8 @@ def extras_only(args):
     if "vqe32" in wanted:
         extra["vqe32"] = vqe32_checkpointed(backend, args.vqe_qubits)
     if "c2_matrix" in wanted:
-        extra["c2_matrix"] = c2_matrix(backend, n64=args.qubits, n128=min(args.qubits, 26))
+        extra["c2_matrix"] = c2_matrix(backend, n64=args.qubits, n128=min(args.qubits, 26),
+                                       modes_wanted=args.c2_modes.split(","), dtypes=args.c2_dtypes.split(","))
     print(json.dumps({"extra": extra}), flush=True)
     backend.close()
 

@@ -546,7 +546,10 @@ typedef struct qf_qaoa_instance {
 
 typedef struct qf_qaoa_opts {
     int32_t use_graph;         /* capture the launch in a CUDA graph once per batch layout, then replay */
-    int32_t tile_qubits[33];   /* tile width per qubit count (0 = default) */
+    int32_t tile_qubits[33];   /* per qubit count: up to 12 qubits the tile width of the one-CTA-per-instance
+                                  kernel (0 = 10); above 12 qubits 0 = batched tile passes over every instance
+                                  of that count (the default), 4..12 = one CTA per instance with tiles of that
+                                  width instead */
 } qf_qaoa_opts;
 
 /* gammas/betas: n_inst x p (row = instance). cost_out: n_inst values;

@@ -12,10 +12,11 @@
 // one M = 128, N = 64, K = 64 product per block.
 //
 // Precision (complex64 state, FP32 results): A and B are split into a TF32
-// head (low 13 mantissa bits cleared) and an FP32 tail, and D = Ah Bh + Al Bh
-// + Ah Bl accumulates in FP32 in tensor memory (the dropped Al Bl term is
-// below 2^-20 of the product). Each block is 24 tcgen05.mma instructions of
-// K = 8.
+// head and a TF32 tail, both rounded to nearest (truncating either biased
+// every block toward zero: 30-qubit error vs complex128 2e-8 instead of
+// 1e-10), and D = Ah Bh + Al Bh + Ah Bl accumulates in FP32 in tensor memory
+// (the dropped Al Bl term is below 2^-24 of the product). Each block is 24
+// tcgen05.mma instructions of K = 8.
 //
 // Data path of one CTA (128 threads; thread r owns TMEM lane r = group row r):
 //   * the tile streams into a 32 KB staging buffer (16-byte cp.async, one
@@ -68,7 +69,9 @@ constexpr uint32_t kSmHiOff = kSmB + kBlockMatBytes;    // 128 x u64
 constexpr uint32_t kSmBars = kSmHiOff + 128 * 8;        // 2 mbarriers
 constexpr uint32_t kSmTmem = kSmBars + 16;              // TMEM base address
 constexpr uint32_t kSmFlag = kSmTmem + 4;               // abort flag
-constexpr uint32_t kSmBytes = (kSmFlag + 4 + 127) / 128 * 128;
+constexpr uint32_t kMaxPassBlocks = 64;                 // block descriptors kept in shared memory
+constexpr uint32_t kSmDesc = kSmFlag + 12;              // kMaxPassBlocks x 16 bytes
+constexpr uint32_t kSmBytes = (kSmDesc + kMaxPassBlocks * 16 + 127) / 128 * 128;
 
 // Instruction descriptor of kind::tf32: D f32 (bits 4-5 = 1), A and B tf32
 // (bits 7-9, 10-12 = 2), both K-major, N >> 3 at bits 17-22, M >> 4 at 24-28.
@@ -141,6 +144,13 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
                  "l"(src), "r"(bytes), "r"(bar)
                  : "memory");
+}
+
+// f32 -> tf32, round to nearest (ties away from zero); low 13 bits zero.
+__device__ __forceinline__ uint32_t tf32_rna(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;\n" : "=r"(r) : "f"(x));
+    return r;
 }
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
@@ -225,6 +235,8 @@ __global__ void __launch_bounds__(kMmaThreads, 2)
             if ((h >> r) & 1u) off |= 1ULL << pa.hi_q[r];
         hi_off[h] = off;
     }
+    MmaBlock *sblocks = reinterpret_cast<MmaBlock *>(sm + kSmDesc);
+    for (uint32_t b = tid; b < pa.n_blocks; b += kMmaThreads) sblocks[b] = blocks[b];
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -265,7 +277,7 @@ __global__ void __launch_bounds__(kMmaThreads, 2)
         __syncthreads();
         float2 *S = stage[cur];
         for (uint32_t b = 0; b < nb; ++b) {
-            const MmaBlock blk = blocks[b];
+            const MmaBlock blk = sblocks[b];
             // this thread's row (group) and the swizzled offsets of its 32 amplitudes
             uint32_t tm = 0;
 #pragma unroll
@@ -288,9 +300,10 @@ __global__ void __launch_bounds__(kMmaThreads, 2)
                 }
                 uint32_t lo[64];
 #pragma unroll
-                for (int e = 0; e < 64; ++e) {
-                    const uint32_t h = v[e] & 0xFFFFE000u;
-                    lo[e] = __float_as_uint(__uint_as_float(v[e]) - __uint_as_float(h));
+                for (int e = 0; e < 64; ++e) {  // head and tail both rounded to nearest: unbiased
+                    const float x = __uint_as_float(v[e]);
+                    const uint32_t h = tf32_rna(x) & 0xFFFFE000u;
+                    lo[e] = tf32_rna(x - __uint_as_float(h)) & 0xFFFFE000u;
                     v[e] = h;
                 }
                 tmem_st64(tmem + lane_base + kColAh, v);
@@ -412,11 +425,12 @@ void choose_rows(const uint8_t jbit[5], uint8_t mbit[7]) {
     for (int i = 0; i < 7; ++i) mbit[i] = (uint8_t)order[i];
 }
 
-float tf32_head(double w) {
+// w rounded to TF32 (nearest, ties away from zero), as a float.
+float tf32_rn(double w) {
     float f = (float)w;
     uint32_t u;
     std::memcpy(&u, &f, 4);
-    u &= 0xFFFFE000u;
+    u = (u + 0x1000u) & 0xFFFFE000u;
     std::memcpy(&f, &u, 4);
     return f;
 }
@@ -433,8 +447,8 @@ void pack_block(const std::vector<cd> &U, float *head, float *tail) {
             if ((n & 1) == 0) w = (k & 1) == 0 ? u.real() : -u.imag();
             else w = (k & 1) == 0 ? u.imag() : u.real();
             const size_t at = (size_t)(n >> 3) * 512 + (size_t)(k >> 2) * 32 + (size_t)(n & 7) * 4 + (size_t)(k & 3);
-            head[at] = tf32_head(w);
-            tail[at] = (float)(w - (double)head[at]);
+            head[at] = tf32_rn(w);
+            tail[at] = tf32_rn(w - (double)head[at]);
         }
 }
 
@@ -524,6 +538,8 @@ int lower_mma(const Plan &plan, MmaPlan &out) {
         }
         emit();
         a.n_blocks = (uint32_t)(out.blocks.size() - out.block_begin.back());
+        if (a.n_blocks > kMaxPassBlocks)
+            return fail(QF_ERR_UNSUPPORTED_OPERATION, "a pass of %u tensor-core blocks (at most %u)", a.n_blocks, kMaxPassBlocks);
         out.passes.push_back(a);
     }
     return QF_OK;
@@ -605,9 +621,18 @@ int run_plan_blocks_mma(qf_sv *sv, const Plan &plan) {
         QF_CUDA(cudaMemcpyAsync(d_blocks, mp.blocks.data(), mp.blocks.size() * sizeof(MmaBlock), cudaMemcpyHostToDevice,
                                 ctx->stream));
     if (mats_bytes) QF_CUDA(cudaMemcpyAsync(d_mats, mp.mats.data(), mats_bytes, cudaMemcpyHostToDevice, ctx->stream));
-    int per_sm = 0;
-    QF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mma_pass, kMmaThreads, kSmBytes));
-    per_sm = std::min(std::max(per_sm, 1), 2);  // two CTAs hold all 512 TMEM columns of an SM
+    // two CTAs per SM: together they hold all 512 TMEM columns, and one
+    // CTA's gathers and scatters overlap the other's MMAs (the occupancy
+    // query answered one here, although two fit by registers and shared
+    // memory, as the launch's own occupancy limits show)
+    int smem_sm = 0, regs_sm = 0;
+    QF_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx->device));
+    QF_CUDA(cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, ctx->device));
+    cudaFuncAttributes fa;
+    QF_CUDA(cudaFuncGetAttributes(&fa, k_mma_pass));
+    const int regs_cta = ((fa.numRegs + 7) / 8) * 8 * kMmaThreads;
+    int per_sm = std::min(smem_sm / (int)(kSmBytes + 1024), regs_sm / std::max(1, regs_cta));
+    per_sm = std::min(std::max(per_sm, 1), 2);
     const uint64_t grid_max = (uint64_t)per_sm * (uint64_t)ctx->sm_count;
     for (size_t i = 0; i < mp.passes.size(); ++i) {
         const MmaPassArgs &a = mp.passes[i];

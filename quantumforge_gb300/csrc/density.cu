@@ -152,38 +152,13 @@ struct ChannelTile {
     float coef_f[kMaxTileChannels][6];  // the same in f32: no f64 -> f32 conversion per tile for complex64
 };
 
-// One channel on the entries (x00, x01, x10, x11) of a (row, column) bit
-// pair: populations mix, coherences scale.
-template <typename C, typename R>
-__device__ __forceinline__ void dm_chan4(C &x00, C &x01, C &x10, C &x11, R a, R b, R cc, R d, R e, R f, bool mix) {
-    if (mix) {
-        const C p = x00, q = x11;
-        x00 = mk(a * p.x + b * q.x, a * p.y + b * q.y);
-        x11 = mk(cc * p.x + d * q.x, cc * p.y + d * q.y);
-    }
-    x01 = mk(e * x01.x, e * x01.y);
-    x10 = mk(f * x10.x, f * x10.y);
-}
-
 template <typename C>
-__device__ __forceinline__ void dm_coefs(const ChannelTile &ct, uint32_t c, typename Real<C>::T (&k)[6]) {
-    using R = typename Real<C>::T;
-#pragma unroll
-    for (int j = 0; j < 6; ++j) k[j] = sizeof(R) == 4 ? (R)ct.coef_f[c][j] : (R)ct.coef[c][j];
-}
-
-// The channels of a tile are applied two at a time in registers: a thread
-// holds the 16 entries that differ in the two channels' four bits, applies
-// both and writes them back (one shared-memory round trip per two channels).
-// complex64 tiles stream in one tile ahead (16-byte cp.async, two buffers).
-template <typename C>
-__global__ void __launch_bounds__(256, 2) k_dm_channel_tile(C *__restrict__ v, uint64_t n_tiles, const ChannelTile ct) {
+__global__ void __launch_bounds__(256) k_dm_channel_tile(C *__restrict__ v, uint64_t n_tiles, const ChannelTile ct) {
     using R = typename Real<C>::T;
     extern __shared__ __align__(16) unsigned char dm_smem[];
+    C *s = reinterpret_cast<C *>(dm_smem);
+    uint64_t *hi_off = reinterpret_cast<uint64_t *>(dm_smem + (sizeof(C) << ct.k));
     const uint32_t T = 1u << ct.k;
-    C *buf[2] = {reinterpret_cast<C *>(dm_smem), reinterpret_cast<C *>(dm_smem) + T};
-    const bool two = sizeof(C) == 8;  // double-buffered (complex64)
-    uint64_t *hi_off = reinterpret_cast<uint64_t *>(buf[two ? 1 : 0] + T);
     for (uint32_t h = threadIdx.x; h < (1u << ct.n_hi); h += blockDim.x) {
         uint64_t off = 0;
         for (uint32_t r = 0; r < ct.n_hi; ++r)
@@ -191,98 +166,46 @@ __global__ void __launch_bounds__(256, 2) k_dm_channel_tile(C *__restrict__ v, u
         hi_off[h] = off;
     }
     __syncthreads();
-    auto issue = [&](uint64_t t, C *dst) {  // complex64: asynchronous 16-byte copies of tile t
-        const uint64_t base = deposit(t, ct.outer_mask);
-        const uint32_t sd = (uint32_t)__cvta_generic_to_shared(dst);
-        for (uint32_t w = threadIdx.x; w < (T >> 1); w += blockDim.x) {
-            const uint32_t j = w << 1;
-            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sd + j * 8u),
-                         "l"(v + (base | hi_off[j >> 5] | (j & 31u)))
-                         : "memory");
-        }
-        asm volatile("cp.async.commit_group;\n" ::: "memory");
-    };
-    int cur = 0;
-    if (two && blockIdx.x < n_tiles) issue(blockIdx.x, buf[0]);
     for (uint64_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
         const uint64_t base = deposit(t, ct.outer_mask);
-        C *s = buf[cur];
-        if (two) {
-            const uint64_t t2 = t + gridDim.x;
-            if (t2 < n_tiles) issue(t2, buf[cur ^ 1]);
-            else asm volatile("cp.async.commit_group;\n" ::: "memory");
-            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        if (sizeof(C) == 8) {  // complex64: 16-byte accesses (2 amplitudes of a 32-amplitude run), all in flight
+#pragma unroll 8
+            for (uint32_t w = threadIdx.x; w < (T >> 1); w += blockDim.x) {
+                const uint32_t j = w << 1;
+                *reinterpret_cast<float4 *>(s + j) = *reinterpret_cast<const float4 *>(v + (base | hi_off[j >> 5] | (j & 31u)));
+            }
         } else {
             for (uint32_t j = threadIdx.x; j < T; j += blockDim.x) s[j] = v[base | hi_off[j >> 5] | (j & 31u)];
         }
         __syncthreads();
-        uint32_t c = 0;
-        for (; c + 1 < ct.n_ch; c += 2) {  // two channels per shared-memory round trip
-            uint32_t bit[4] = {ct.lc[c], ct.lr[c], ct.lc[c + 1], ct.lr[c + 1]};
-            uint32_t srt[4] = {bit[0], bit[1], bit[2], bit[3]};
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-#pragma unroll
-                for (int j = 0; j < 3 - i; ++j)
-                    if (srt[j] > srt[j + 1]) {
-                        const uint32_t tmp = srt[j];
-                        srt[j] = srt[j + 1];
-                        srt[j + 1] = tmp;
-                    }
-            R ka[6], kb[6];
-            dm_coefs<C>(ct, c, ka);
-            dm_coefs<C>(ct, c + 1, kb);
-            const bool mixa = ct.shape[c] != 2, mixb = ct.shape[c + 1] != 2;
-            for (uint32_t g = threadIdx.x; g < (T >> 4); g += blockDim.x) {
-                uint32_t i = g;
-#pragma unroll
-                for (int b = 0; b < 4; ++b) i = ((i >> srt[b]) << (srt[b] + 1)) | (i & ((1u << srt[b]) - 1u));
-                C x[16];
-#pragma unroll
-                for (int e = 0; e < 16; ++e) {
-                    uint32_t o = 0;
-#pragma unroll
-                    for (int b = 0; b < 4; ++b)
-                        if ((e >> b) & 1) o |= 1u << bit[b];
-                    x[e] = s[i | o];
-                }
-#pragma unroll
-                for (int h = 0; h < 4; ++h)  // first channel: entry bits 0 (column), 1 (row)
-                    dm_chan4(x[4 * h], x[4 * h + 1], x[4 * h + 2], x[4 * h + 3], ka[0], ka[1], ka[2], ka[3], ka[4], ka[5], mixa);
-#pragma unroll
-                for (int l = 0; l < 4; ++l)  // second channel: entry bits 2 (column), 3 (row)
-                    dm_chan4(x[l], x[l + 4], x[l + 8], x[l + 12], kb[0], kb[1], kb[2], kb[3], kb[4], kb[5], mixb);
-#pragma unroll
-                for (int e = 0; e < 16; ++e) {
-                    uint32_t o = 0;
-#pragma unroll
-                    for (int b = 0; b < 4; ++b)
-                        if ((e >> b) & 1) o |= 1u << bit[b];
-                    s[i | o] = x[e];
-                }
-            }
-            __syncthreads();
-        }
-        if (c < ct.n_ch) {  // an odd channel out
+        for (uint32_t c = 0; c < ct.n_ch; ++c) {
             const uint32_t lc = ct.lc[c], lr = ct.lr[c], lo = min(lc, lr), hi = max(lc, lr);
             const uint32_t cm = 1u << lc, rm = 1u << lr;
-            R k[6];
-            dm_coefs<C>(ct, c, k);
-            const bool mix = ct.shape[c] != 2;
+            R a, b, cc, d, e, f;
+            if (sizeof(R) == 4) {
+                a = (R)ct.coef_f[c][0], b = (R)ct.coef_f[c][1], cc = (R)ct.coef_f[c][2], d = (R)ct.coef_f[c][3];
+                e = (R)ct.coef_f[c][4], f = (R)ct.coef_f[c][5];
+            } else {
+                a = (R)ct.coef[c][0], b = (R)ct.coef[c][1], cc = (R)ct.coef[c][2], d = (R)ct.coef[c][3];
+                e = (R)ct.coef[c][4], f = (R)ct.coef[c][5];
+            }
+            const int shape = ct.shape[c];
             for (uint32_t g = threadIdx.x; g < (T >> 2); g += blockDim.x) {
                 uint32_t i = g;
                 i = ((i >> lo) << (lo + 1)) | (i & ((1u << lo) - 1u));
                 i = ((i >> hi) << (hi + 1)) | (i & ((1u << hi) - 1u));
-                C x00 = s[i], x01 = s[i | cm], x10 = s[i | rm], x11 = s[i | rm | cm];
-                dm_chan4(x00, x01, x10, x11, k[0], k[1], k[2], k[3], k[4], k[5], mix);
-                s[i] = x00;
-                s[i | cm] = x01;
-                s[i | rm] = x10;
-                s[i | rm | cm] = x11;
+                const C x01 = s[i | cm], x10 = s[i | rm];
+                if (shape != 2) {
+                    const C x00 = s[i], x11 = s[i | rm | cm];
+                    s[i] = mk(a * x00.x + b * x11.x, a * x00.y + b * x11.y);
+                    s[i | rm | cm] = mk(cc * x00.x + d * x11.x, cc * x00.y + d * x11.y);
+                }
+                s[i | cm] = mk(e * x01.x, e * x01.y);
+                s[i | rm] = mk(f * x10.x, f * x10.y);
             }
             __syncthreads();
         }
-        if (two) {
+        if (sizeof(C) == 8) {
 #pragma unroll 8
             for (uint32_t w = threadIdx.x; w < (T >> 1); w += blockDim.x) {
                 const uint32_t j = w << 1;
@@ -292,9 +215,7 @@ __global__ void __launch_bounds__(256, 2) k_dm_channel_tile(C *__restrict__ v, u
             for (uint32_t j = threadIdx.x; j < T; j += blockDim.x) v[base | hi_off[j >> 5] | (j & 31u)] = s[j];
         }
         __syncthreads();
-        cur ^= two ? 1 : 0;
     }
-    if (two) asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 }
 
 int grid_for(const qf_ctx *ctx, uint64_t work) {
@@ -358,8 +279,7 @@ int dm_channels_fused(qf_sv *sv, uint32_t n, const uint32_t *qs, const double (*
         }
     }
     const uint64_t n_tiles = 1ULL << (2 * n - ct.k);
-    // complex64: two tile buffers (the next tile streams in); complex128: one
-    const size_t smem = (sv->dtype == QF_C64 ? 16u : 16u) * (size_t(1) << ct.k) + sizeof(uint64_t) * (size_t(1) << ct.n_hi);
+    const size_t smem = (sv->dtype == QF_C64 ? 8u : 16u) * (size_t(1) << ct.k) + sizeof(uint64_t) * (size_t(1) << ct.n_hi);
     // one wave of resident CTAs (a grid past the resident count leaves a tail
     // wave running on part of the GPU)
     auto grid_of = [&](const void *k, int *grid) -> int {

@@ -674,7 +674,17 @@ extern "C" int qf_qaoa_maxcut_batch(qf_ctx *ctx, const qf_qaoa_instance *inst, u
     for (uint64_t e = 0; e < n_edges; ++e) masks[e] = (1ULL << edges_uv[2 * e]) | (1ULL << edges_uv[2 * e + 1]);
     for (uint64_t i = 0; i < n_inst * p; ++i)
         if (!std::isfinite(gammas[i]) || !std::isfinite(betas[i])) return fail(QF_ERR_NON_FINITE_PARAMETER, "circuit parameters must be finite");
-    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return inst[a].qubits > inst[b].qubits; });
+    // an instance above 12 qubits runs in the batched passes unless a tile
+    // width is given for it (then one CTA per instance, like the small ones)
+    auto tile_req = [&](const qf_qaoa_instance &I) -> int {
+        return I.tile_qubits ? (int)I.tile_qubits : (opts && I.qubits <= 32 ? opts->tile_qubits[I.qubits] : 0);
+    };
+    auto batched = [&](const qf_qaoa_instance &I) { return I.qubits > (uint32_t)kQBTile && tile_req(I) == 0; };
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+        const bool ba = batched(inst[a]), bb = batched(inst[b]);
+        if (ba != bb) return ba;
+        return inst[a].qubits > inst[b].qubits;
+    });
     // rows [0, r_small): batched passes per qubit count (13..24 qubits); the
     // rest: one CTA per instance
     uint64_t amp_off = 0, cost_off = 0, ptab_off = 0, part_off = 0;
@@ -685,7 +695,7 @@ extern "C" int qf_qaoa_maxcut_batch(qf_ctx *ctx, const qf_qaoa_instance *inst, u
         std::memset(&D, 0, sizeof D);
         D.n = I.qubits;
         if (D.n > 24) return fail(QF_ERR_UNSUPPORTED_OPERATION, "batched QAOA supports up to 24 qubits, got %u", D.n);
-        if (D.n > (uint32_t)kQBTile) {
+        if (batched(I)) {
             r_small = (uint32_t)r + 1;
             D.k = kQBTile;
             D.ptab = ptab_off;
@@ -693,7 +703,7 @@ extern "C" int qf_qaoa_maxcut_batch(qf_ctx *ctx, const qf_qaoa_instance *inst, u
             D.part = part_off;
             part_off += (uint64_t)(1 + 3 * p) << (D.n - kQBTile);
         } else {
-            const int kt = I.tile_qubits ? (int)I.tile_qubits : (opts && opts->tile_qubits[I.qubits] ? opts->tile_qubits[I.qubits] : 10);
+            const int kt = tile_req(I) ? tile_req(I) : 10;
             D.k = (uint32_t)std::max(4, std::min(kQMaxTile, kt));
             if (D.n > D.k && D.n - D.k > D.k - 1) D.k = (D.n + 1) / 2 + 1;  // pass B needs n-k+1 <= k
             D.k = std::min<uint32_t>(D.k, (uint32_t)kQMaxTile);

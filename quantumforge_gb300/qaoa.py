@@ -6,8 +6,10 @@ expected cut of the QAOA state
 ``algorithms::qaoa_maxcut``, src/algorithms.rs:110-137, unit weights) and its
 exact gradient with respect to every gamma_l and beta_l: instances of up to 12
 qubits one CTA each, larger ones (up to 24) as tile passes batched over all
-instances of a qubit count. ``autotune_tiles`` picks the shared-memory tile
-width of the small instances per qubit count by timing sub-batches.
+instances of a qubit count, or one CTA each when asked. ``autotune_tiles``
+picks, per qubit count, the shared-memory tile width of the small instances
+and, above 12 qubits, batched passes or one CTA per instance, by timing
+sub-batches; ``save_tiles`` / ``load_tiles`` persist the table.
 """
 from __future__ import annotations
 
@@ -80,23 +82,27 @@ class QaoaBatch:
         return cost, grad
 
 
-def autotune_tiles(problems, p: int, candidates=(8, 9, 10, 11, 12), reps: int = 2, backend=None) -> dict:
-    """Best tile width per qubit count (up to 12 qubits: larger instances run as
-    batched passes with fixed 12-qubit tiles), timed on the sub-batch of that
-    count."""
+def autotune_tiles(problems, p: int, candidates=(8, 9, 10, 11, 12), reps: int = 2, backend=None,
+                   large_candidates=(0, 12, 11), max_large: int = 24) -> dict:
+    """Best execution per qubit count, timed on the sub-batch of that count
+    (at most 256 instances). Up to 12 qubits: the tile width of the
+    one-CTA-per-instance kernel, from `candidates`. Above 12 (up to
+    `max_large`): 0 = batched tile passes over every instance of the count, or
+    one CTA per instance with tiles of a width in `large_candidates`."""
     rng = np.random.default_rng(0)
     best = {}
     by_n: dict[int, list] = {}
     for prob in problems:
-        if int(prob[0]) <= 12:
+        if int(prob[0]) <= max_large:
             by_n.setdefault(int(prob[0]), []).append(prob)
     for n, probs in sorted(by_n.items()):
         probs = probs[: max(8, min(len(probs), 256))]
         g = rng.uniform(0, np.pi, (len(probs), p))
         b = rng.uniform(0, np.pi / 2, (len(probs), p))
         timings = {}
-        for k in candidates:
-            if k > n and k != candidates[0]:
+        cands = candidates if n <= 12 else large_candidates
+        for k in cands:
+            if n <= 12 and k > n and k != cands[0]:
                 continue
             batch = QaoaBatch(probs, p, tile_qubits={n: k}, backend=backend, use_graph=False)
             batch.run(g, b)
@@ -106,3 +112,19 @@ def autotune_tiles(problems, p: int, candidates=(8, 9, 10, 11, 12), reps: int = 
             timings[k] = (time.perf_counter() - t0) / reps
         best[n] = min(timings, key=timings.get)
     return best
+
+
+def save_tiles(tiles: dict, path) -> None:
+    """Persist an autotuned table ({qubits: tile}) as JSON."""
+    import json
+    from pathlib import Path
+
+    Path(path).write_text(json.dumps({str(k): int(v) for k, v in sorted(tiles.items())}))
+
+
+def load_tiles(path) -> dict:
+    """A table written by save_tiles."""
+    import json
+    from pathlib import Path
+
+    return {int(k): int(v) for k, v in json.loads(Path(path).read_text()).items()}

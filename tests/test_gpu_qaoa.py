@@ -117,8 +117,29 @@ def test_more_than_24_qubits_is_rejected(backend):
         QaoaBatch([(26, O.random_3_regular(26, 1))], 1, backend=backend).run(np.zeros((1, 1)), np.zeros((1, 1)))
 
 
-def test_autotune_returns_a_tile_per_small_size(backend):
-    # instances above 12 qubits run as batched passes with fixed tiles: not tuned
+def test_autotune_returns_a_choice_per_size(backend, tmp_path):
+    from quantumforge_gb300.qaoa import load_tiles, save_tiles
+
     problems = [(n, O.random_3_regular(n, n + 7)) for n in (10, 12, 14) for _ in range(8)]
-    best = autotune_tiles(problems, 2, candidates=(8, 10, 12), reps=1, backend=backend)
-    assert set(best) == {10, 12} and all(k in (8, 10, 12) for k in best.values())
+    best = autotune_tiles(problems, 2, candidates=(8, 10, 12), large_candidates=(0, 12), reps=1, backend=backend)
+    assert set(best) == {10, 12, 14} and best[10] in (8, 10, 12) and best[12] in (8, 10, 12) and best[14] in (0, 12)
+    save_tiles(best, tmp_path / "tiles.json")
+    assert load_tiles(tmp_path / "tiles.json") == best
+
+
+@pytest.mark.parametrize("k", [12, 11])
+def test_one_cta_per_large_instance_matches_oracle(backend, k):
+    """Instances above 12 qubits on the one-CTA-per-instance kernel (a tile
+    width given for their qubit count) instead of the batched passes."""
+    rng = np.random.default_rng(31)
+    sizes = [14, 16, 18, 12, 14]
+    problems = [(n, O.random_3_regular(n, 500 + i)) for i, n in enumerate(sizes)]
+    p = 2
+    gam = rng.uniform(0, np.pi, (len(problems), p))
+    bet = rng.uniform(0, np.pi / 2, (len(problems), p))
+    batch = QaoaBatch(problems, p, tile_qubits={14: k, 16: k, 18: k}, backend=backend)
+    cost, grad = batch.run(gam, bet)
+    for i, (n, edges) in enumerate(problems):
+        e_ref, g_ref = oracle_cost_grad(n, edges, gam[i], bet[i])
+        assert abs(cost[i] - e_ref) < 1e-5 * max(1.0, abs(e_ref)), (i, n, cost[i], e_ref)
+        assert np.abs(grad[i] - g_ref).max() < 1e-4 * max(1.0, np.abs(g_ref).max()), (i, n, grad[i], g_ref)
