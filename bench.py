@@ -922,13 +922,40 @@ def vqe_gradients(backend, cpu: bool = True):
     for r in ops:
         pc.operations.append((int(r["kind"]), int(r["gate"]), int(r["q0"]), int(r["q1"]), int(r["param"]),
                               float(r["theta"])))
-    kw = dict(dtype="c64", backend=backend, checkpoint_every=3 * n)
-    adj = gradient_with_inputs(pc, GradientOptions(strategy=GradientStrategy.Adjoint), [], params, n, H, **kw)
-    reps = 5
-    t0 = time.perf_counter()
-    for _ in range(reps):
+    # checkpoint policies: psi stored at every layer, every four layers, or
+    # never (pure uncompute); each timed over 5 gradients, with its algorithmic
+    # HBM bytes from the adjoint's own plan (qf_adjoint_plan_stats)
+    import ctypes as C
+
+    from quantumforge_gb300 import _abi as A
+    from quantumforge_gb300 import _native
+
+    peak, peak_kind = hbm_peak()
+    policies = {}
+    for name, every in (("per_layer", 3 * n), ("every_4_layers", 12 * n), ("uncompute", 0)):
+        kw = dict(dtype="c64", backend=backend, checkpoint_every=every)
         adj = gradient_with_inputs(pc, GradientOptions(strategy=GradientStrategy.Adjoint), [], params, n, H, **kw)
-    t_adj = (time.perf_counter() - t0) / reps
+        reps = 5
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            adj = gradient_with_inputs(pc, GradientOptions(strategy=GradientStrategy.Adjoint), [], params, n, H, **kw)
+        t = (time.perf_counter() - t0) / reps
+        o = A.GradientOpts()
+        o.strategy, o.dtype, o.checkpoint_every = A.GRAD_ADJOINT, A.C64, every
+        st = A.AdjointStats()
+        pp = np.ascontiguousarray(params, dtype=np.float64)
+        terms = H.array()
+        _native.check(_native.load().qf_adjoint_plan_stats(n, A.C64, _native.ptr(ops), len(ops), _native.ptr(pp), pp.size,
+                                                           None, 0, _native.ptr(terms), len(terms), C.byref(o),
+                                                           C.byref(st)))
+        policies[name] = {"checkpoint_every_ops": every, "grads_per_s": 1.0 / t, "s_per_gradient": t,
+                          "launches": {"forward": st.forward_passes, "pauli": st.pauli_passes,
+                                       "backward": st.backward_passes, "state_copies": st.state_copies},
+                          "algorithmic_gb": st.hbm_bytes / 1e9,
+                          "roofline_frac": st.hbm_bytes / t / 1e9 / peak, "grad": np.asarray(adj.gradient), "est": adj}
+    best = min(policies, key=lambda k: policies[k]["s_per_gradient"])
+    adj = policies[best]["est"]
+    t_adj = policies[best]["s_per_gradient"]
     pc.expectation_pauli_sum(params, n, H, dtype="c64", backend=backend)  # warm: compiles the forward passes
     t0 = time.perf_counter()
     sh = gradient_with_inputs(pc, GradientOptions(strategy=GradientStrategy.ParameterShift), [], params, n, H,
@@ -951,7 +978,17 @@ def vqe_gradients(backend, cpu: bool = True):
         em = pc.expectation_pauli_sum(pm, n, H, dtype="c128", backend=backend)
         fd.append((ep - em) / (2 * h))
     fd = np.asarray(fd)
+    pol = {}
+    for name, v in policies.items():
+        pol[name] = {k: v[k] for k in ("checkpoint_every_ops", "grads_per_s", "launches", "algorithmic_gb", "roofline_frac")}
+        pol[name]["max_abs_grad_err_vs_c128"] = float(np.abs(v["grad"] - g128).max())
     out = {"qubits": n, "params": int(params.size), "ops": len(ops), "adjoint_grads_per_s": 1.0 / t_adj,
+           "adjoint_policy": best, "adjoint_policies": pol,
+           "roofline": {"bound": "hbm", "algorithmic_gb_per_gradient": policies[best]["algorithmic_gb"],
+                        "achieved_gbs": policies[best]["algorithmic_gb"] / t_adj, "peak": peak,
+                        "frac": policies[best]["roofline_frac"], "peak_kind": f"of {peak_kind}",
+                        "note": "the gradient's algorithmic HBM bytes (forward, Pauli and backward passes, checkpoint "
+                                "copies) over its wall time, host work included"},
            "param_shift_grads_per_s": 1.0 / t_sh, "ratio": t_sh / t_adj,
            "max_abs_grad_diff_adjoint_vs_shift": float(np.abs(adj.gradient - sh.gradient).max()),
            "energy_adjoint": adj.expectation, "energy_shift_run": sh.expectation, "dtype": "complex64",

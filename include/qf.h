@@ -569,6 +569,25 @@ int qf_plan_stats(uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops,
                   const double *inputs, uint64_t n_inputs,
                   const qf_exec_opts *opts, uint64_t *n_passes, uint64_t *n_gates);
 
+/* What one adjoint gradient (qf_gradient with QF_GRAD_ADJOINT and these
+ * options) launches, and its algorithmic HBM bytes: |0> written, forward
+ * passes (read + write psi), the Pauli passes of lambda = H psi, backward
+ * passes (psi and lambda read and written), checkpoint copies. Host only, no
+ * GPU needed; the measurement helper behind the gradient's roofline fraction
+ * (the reference's adjoint_gradient_with_inputs, src/lib.rs:3564-3704, stores
+ * every intermediate state instead). */
+typedef struct qf_adjoint_stats {
+    uint64_t forward_passes;
+    uint64_t backward_passes;
+    uint64_t pauli_passes;
+    uint64_t state_copies;
+    double hbm_bytes;
+} qf_adjoint_stats;
+int qf_adjoint_plan_stats(uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops,
+                          const double *params, uint64_t n_params, const double *inputs, uint64_t n_inputs,
+                          const qf_pauli_term *terms, uint64_t n_terms, const qf_gradient_opts *opts,
+                          qf_adjoint_stats *out);
+
 /* SmallRng::next_u64 (src/lib.rs:4898-4905) advanced `steps` times, computed
  * by GF(2) matrix powers: the generator state from which the shot-major
  * stream of run_shots_impl (src/lib.rs:2874-2912) draws its `steps`-th value.

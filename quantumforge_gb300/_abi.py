@@ -144,6 +144,12 @@ class GradientOpts(C.Structure):
     ]
 
 
+class AdjointStats(C.Structure):
+    """qf_adjoint_stats: launches and algorithmic HBM bytes of one adjoint gradient."""
+    _fields_ = [("forward_passes", C.c_uint64), ("backward_passes", C.c_uint64), ("pauli_passes", C.c_uint64),
+                ("state_copies", C.c_uint64), ("hbm_bytes", C.c_double)]
+
+
 class GradientInfo(C.Structure):
     _fields_ = [("strategy", C.c_int32), ("reserved", C.c_int32), ("evaluations", C.c_uint64)]
 

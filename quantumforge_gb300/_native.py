@@ -108,6 +108,7 @@ SIGNATURES = {
     "qf_gradient": [P, U32, P, U64, P, U64, P, U64, P, U64, P, P, P, P],
     "qf_expectation": [P, U32, C.c_int, P, U64, P, U64, P, U64, P, U64, P, PF64],
     "qf_plan_stats": [U32, C.c_int, P, U64, P, U64, P, U64, P, PU64, PU64],
+    "qf_adjoint_plan_stats": [U32, C.c_int, P, U64, P, U64, P, U64, P, U64, P, P],
     "qf_qaoa_maxcut_batch": [P, P, U64, P, U64, U32, P, P, P, P, P],
     "qf_rng_jump": [U64, U64],
     "qf_expectation_z_all_noalloc": [C.c_int, P, U32, C.c_int, P, P, U64],

@@ -1983,6 +1983,61 @@ int qf_gradient(qf_ctx *ctx, uint32_t qubits, const qf_op *ops, uint64_t n_ops, 
 
 uint64_t qf_rng_jump(uint64_t state, uint64_t steps) { return rng_jump(state, steps); }
 
+int qf_adjoint_plan_stats(uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops, const double *params,
+                          uint64_t n_params, const double *inputs, uint64_t n_inputs, const qf_pauli_term *terms,
+                          uint64_t n_terms, const qf_gradient_opts *opts, qf_adjoint_stats *out) {
+    clear_error();
+    QF_TRY(check_dtype(dtype));
+    if (!out || !opts) return fail(QF_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (qubits == 0) return fail(QF_ERR_ZERO_QUBITS, "a state vector must contain at least one qubit");
+    std::vector<BGate> gates;
+    QF_TRY(bind_ops(qubits, ops, n_ops, params, n_params, inputs, n_inputs, -1, 0.0, gates));
+    std::memset(out, 0, sizeof *out);
+    // the planning of adjoint_device, without launches
+    const int every = std::max(0, opts->checkpoint_every);
+    std::vector<size_t> seg_begin;
+    if (every > 0 && !gates.empty()) {
+        for (size_t s = 0; s < gates.size(); s += (size_t)every) seg_begin.push_back(s);
+    } else {
+        seg_begin.push_back(0);
+    }
+    const size_t n_seg = seg_begin.size();
+    PlanOpts po;
+    default_tiling(qubits, dtype, opts->exec.tile_qubits, &po.tile_qubits, &po.low_qubits);
+    po.search = !(opts->exec.flags & QF_EXEC_FLAG_PLAN_FIRST_COME);
+    PlanOpts bo = po;
+    bo.backward = true;
+    bo.merge_1q = true;
+    bo.search = false;
+    for (size_t s = 0; s < n_seg; ++s) {
+        const size_t b = seg_begin[s], e = s + 1 < n_seg ? seg_begin[s + 1] : gates.size();
+        std::vector<BGate> seg(gates.begin() + b, gates.begin() + e);
+        Plan fp, bp;
+        QF_TRY(plan_passes(qubits, seg, po, fp));
+        QF_TRY(plan_passes(qubits, seg, bo, bp));
+        out->forward_passes += fp.passes.size();
+        out->backward_passes += bp.passes.size();
+    }
+    uint64_t tiles = 0, wide = 0;
+    QF_TRY(pauli_plan_stats(qubits, dtype, terms, n_terms, &tiles, &wide));
+    out->pauli_passes = tiles + wide;
+    out->state_copies = 2 * (n_seg - 1);  // checkpoints taken forward, restored backward
+    // algorithmic bytes: |0> written; a forward pass reads and writes psi; the
+    // first Pauli tile pass reads psi and writes lambda, later ones also read
+    // lambda (as every wide group does); a separate <psi|lambda> follows wide
+    // groups; a backward pass reads and writes psi and lambda; a copy reads
+    // and writes one state
+    const double N = (double)(1ULL << qubits) * (dtype == QF_C64 ? 8.0 : 16.0);
+    double bytes = N + 2.0 * N * (double)out->forward_passes + 4.0 * N * (double)out->backward_passes +
+                   2.0 * N * (double)out->state_copies;
+    if (tiles) bytes += 2.0 * N + 3.0 * N * (double)(tiles - 1);
+    bytes += 3.0 * N * (double)wide;
+    if (wide && tiles == 0) bytes -= N;  // lambda is zeroed, not read, before the first wide sweep
+    if (wide) bytes += 2.0 * N;
+    out->hbm_bytes = bytes;
+    return QF_OK;
+}
+
 int qf_plan_stats(uint32_t qubits, int dtype, const qf_op *ops, uint64_t n_ops, const double *params, uint64_t n_params,
                   const double *inputs, uint64_t n_inputs, const qf_exec_opts *opts, uint64_t *n_passes, uint64_t *n_gates) {
     clear_error();

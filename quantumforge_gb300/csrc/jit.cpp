@@ -704,6 +704,8 @@ struct PassGen {
             s << "float2* S = SB;\nfloat2* SL = SB + " << tile_of(K) << "u;\n";
         }
         s << "const unsigned long long tb = " << dep_t << ";\n";
+        if (!dual) s << "float2 tph = make_float2(1.f, 0.f);\n";  // deferred per-thread phase
+        phase_pending = false;
         for (int a = 0; a < n_arrays(); ++a)
             for (int i = 0; i < kR; ++i) s << "float2 " << reg_pfx(a) << i << ";\n";
         build_deps();
@@ -748,6 +750,7 @@ struct PassGen {
                 continue;
             }
             s << "{\n";  // remap: a new layout with the chosen qubits in register positions
+            flush_phase();
             emit_write();
             s << "__syncthreads();\n";
             relayout(choose_regs());
@@ -818,6 +821,15 @@ struct PassGen {
                         const int rb = d - 8;
                         for (int i = 0; i < kR; ++i)
                             if ((i >> rb) & 1) emit_cmul_const(g, g.R(i), sl, 0);
+                    } else if (!dual) {
+                        // a lane, warp or outside-the-tile bit is constant over the thread's
+                        // registers: the factor goes into the thread's deferred phase
+                        // (applied once, before the next remap or the store)
+                        if (a == 0) {
+                            s << "if (" << cbit(d) << ") ";
+                            emit_cmul_const(g, "tph", sl, 0);
+                            phase_pending = true;
+                        }
                     } else {
                         s << "if (" << cbit(d) << ") {\n";
                         for (int i = 0; i < kR; ++i) emit_cmul_const(g, g.R(i), sl, 0);
@@ -940,6 +952,20 @@ struct PassGen {
         }
     }
 
+    // the deferred per-thread phase of diagonal gates on lane, warp and
+    // outside-the-tile bits, multiplied into the registers (forward passes)
+    bool phase_pending = false;
+    void flush_phase() {
+        if (!phase_pending) return;
+        auto &s = g.s;
+        for (int i = 0; i < kR; ++i) {
+            const std::string R = g.R(i);
+            s << "{const float2 x=" << R << ";" << R << ".x=tph.x*x.x-tph.y*x.y;" << R << ".y=tph.x*x.y+tph.y*x.x;}\n";
+        }
+        s << "tph = make_float2(1.f, 0.f);\n";
+        phase_pending = false;
+    }
+
     // multiply the tile (psi and lambda alike) by the factors pulled out so
     // far, a real or an imaginary scalar, and start a new product
     void emit_scale() {
@@ -960,6 +986,7 @@ struct PassGen {
 
     void finish(bool last_pass, const std::string &dep_t2) {
         auto &s = g.s;
+        flush_phase();
         if (last_pass && g.any_diag) {  // the plan's global phase, once, at the very end (with this pass's factors)
             const int sl = g.slot(g.gphase * g.pscale, 0.0, 0.0, 0.0);
             for (int a = 0; a < n_arrays(); ++a) {

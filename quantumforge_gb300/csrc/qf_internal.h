@@ -342,6 +342,10 @@ int collapse(qf_sv *sv, uint32_t q, int outcome, double scale);
 // Pauli sums: <psi|H|psi> (complex), and lambda = H psi with <psi|lambda>.
 int pauli_expectation(qf_sv *sv, const qf_pauli_term *terms, uint64_t n_terms, double out[2]);
 int pauli_apply(qf_sv *psi, qf_sv *lambda, const qf_pauli_term *terms, uint64_t n_terms, double *energy);
+// Launch counts of the Pauli-sum passes (host only): tile passes and sweeps of
+// groups whose x-mask does not fit a tile.
+int pauli_plan_stats(uint32_t n, int dtype, const qf_pauli_term *terms, uint64_t n_terms, uint64_t *tile_passes,
+                     uint64_t *wide_passes);
 // Fill/convert.
 int fill_zero_state(qf_sv *sv);
 int convert_from_f64(qf_sv *sv, const double *d_src);

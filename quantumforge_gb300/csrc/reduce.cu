@@ -1033,6 +1033,15 @@ int run_pauli(qf_sv *psi, qf_sv *lam, PauliPlan &plan, bool apply, double out[2]
 }
 }  // namespace
 
+int pauli_plan_stats(uint32_t n, int dtype, const qf_pauli_term *terms, uint64_t n_terms, uint64_t *tile_passes,
+                     uint64_t *wide_passes) {
+    PauliPlan plan;
+    if (n_terms) QF_TRY(plan_pauli(n, dtype, terms, n_terms, plan));
+    *tile_passes = plan.tiles.size();
+    *wide_passes = plan.wide.size();
+    return QF_OK;
+}
+
 int pauli_expectation(qf_sv *sv, const qf_pauli_term *terms, uint64_t n_terms, double out[2]) {
     out[0] = out[1] = 0.0;
     if (n_terms == 0) return QF_OK;

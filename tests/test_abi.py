@@ -207,3 +207,24 @@ def test_dense_block_plans(engine_lib, dtype):
     # a small state is one pass whatever the width
     small = W.random_circuit(4, 6, 2, two_qubit="mixed")
     assert _block_plan(engine_lib, 4, small, 5, dtype) == (0, 1)
+
+
+def test_adjoint_plan_stats(engine_lib):
+    """Launch counts and algorithmic bytes of one adjoint gradient (host only):
+    a checkpoint per layer adds state copies and never removes passes."""
+    ops, params, H = W.vqe_tfim(24, 8, seed=3)
+    t = H.array()
+    out = {}
+    for every in (0, 72):
+        o = A.GradientOpts()
+        o.strategy, o.dtype, o.checkpoint_every = A.GRAD_ADJOINT, A.C64, every
+        st = A.AdjointStats()
+        p = np.ascontiguousarray(params, dtype=np.float64)
+        assert engine_lib.qf_adjoint_plan_stats(24, A.C64, _native.ptr(ops), len(ops), _native.ptr(p), p.size, None, 0,
+                                                _native.ptr(t), len(t), C.byref(o), C.byref(st)) == 0
+        out[every] = st
+        N = (1 << 24) * 8
+        assert st.forward_passes >= 1 and st.backward_passes >= 1 and st.pauli_passes >= 1
+        assert st.hbm_bytes >= N * (1 + 2 * st.forward_passes + 4 * st.backward_passes + 2)
+    assert out[0].state_copies == 0 and out[72].state_copies == 2 * (8 - 1)
+    assert out[72].forward_passes >= out[0].forward_passes
