@@ -5,6 +5,9 @@
 #include <cmath>
 #include <complex>
 #include <cstring>
+#include <string>
+#include <mutex>
+#include <map>
 
 #include "qf_internal.h"
 
@@ -546,6 +549,55 @@ std::vector<FBlock> fuse_gates(const std::vector<BGate> &gates, int k) {
 }
 }  // namespace
 
+namespace {
+// A pass's choice: its resident qubits (before the lowest free qubits widen the
+// tile) and the items it runs, in order.
+struct PassChoice {
+    uint64_t L;
+    std::vector<int> sel;
+};
+std::string plan_key_of(uint32_t n, int k, int low, const PlanOpts &o, const std::vector<Item> &items) {
+    std::string key;
+    auto put = [&](uint64_t v, int bytes) {
+        for (int b = 0; b < bytes; ++b) key.push_back((char)((v >> (8 * b)) & 0xFF));
+    };
+    put(n, 1);
+    put((uint64_t)k, 1);
+    put((uint64_t)low, 1);
+    put(o.merge_1q | (o.backward << 1) | (o.search << 2), 1);
+    put((uint64_t)o.max_items, 4);
+    put((uint64_t)o.block_qubits, 1);
+    put(items.size(), 4);
+    for (const Item &it : items) {
+        put(it.g.kind | (it.overlap << 3) | ((it.g.axis == QF_PAULI_Z) << 4), 1);
+        put(it.g.q0, 1);
+        put(it.g.q1, 1);
+        put(it.need, 8);
+    }
+    return key;
+}
+struct PlanCache {
+    std::mutex mu;
+    std::map<std::string, std::vector<PassChoice>> entries;
+};
+PlanCache &plan_cache() {
+    static PlanCache c;
+    return c;
+}
+bool plan_cache_get(const std::string &key, std::vector<PassChoice> &out) {
+    std::lock_guard<std::mutex> lk(plan_cache().mu);
+    auto it = plan_cache().entries.find(key);
+    if (it == plan_cache().entries.end()) return false;
+    out = it->second;
+    return true;
+}
+void plan_cache_put(const std::string &key, std::vector<PassChoice> &&v) {
+    std::lock_guard<std::mutex> lk(plan_cache().mu);
+    if (plan_cache().entries.size() >= 64) plan_cache().entries.clear();  // bound the host memory
+    plan_cache().entries[key] = std::move(v);
+}
+}  // namespace
+
 int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, Plan &plan) {
     plan = Plan();
     plan.n = n;
@@ -577,27 +629,22 @@ int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, 
     std::vector<int> remaining(items.size());
     for (size_t i = 0; i < items.size(); ++i) remaining[i] = (int)i;
 
-    while (!remaining.empty()) {
-        // The first remaining item must fit: shrink the always-resident low
-        // block from the top until it does (qubit 0 stays resident, k >= 3).
-        uint64_t L = low_mask;
-        const uint64_t first_need = items[remaining[0]].need;
-        for (int b = low - 1; b >= 1 && popc(L | first_need) > k; --b) L &= ~(1ULL << b);
-        if (o.search) L = choose_resident(items, remaining, L | first_need, k, n, all, o.max_items);
-        uint64_t blocked = 0;
+    // The choice of every pass (resident qubits and items) depends only on the
+    // list's structure: a list of the same gate kinds, qubits, diagonal flags
+    // and overlaps (new angles, shifted parameters, another optimiser step)
+    // replays the recorded choices instead of searching again.
+    const std::string key = plan_key_of(n, k, low, o, items);
+    std::vector<PassChoice> replay;
+    const bool hit = plan_cache_get(key, replay);
+    std::vector<PassChoice> record;
+    size_t pass_i = 0;
+
+    while (hit ? pass_i < replay.size() : !remaining.empty()) {
+        uint64_t L;
         std::vector<Item> taken;
         std::vector<int> last_on(n, -1);  // index into taken of the last item touching q
-        std::vector<int> rest;
-        rest.reserve(remaining.size());
-        for (size_t r = 0; r < remaining.size(); ++r) {
-            const int idx = remaining[r];
-            const Item &it = items[idx];
-            if (blocked == all || taken.size() >= (size_t)o.max_items) { rest.push_back(idx); continue; }
-            if (it.touch & blocked) { blocked |= it.touch; rest.push_back(idx); continue; }
-            const uint64_t nl = L | it.need;
-            if (popc(nl) > k) { blocked |= it.touch; rest.push_back(idx); continue; }
-            L = nl;
-            // merge consecutive 1q gates on one qubit into one matrix
+        // merge consecutive 1q gates on one qubit into one matrix
+        auto take = [&](const Item &it) {
             if (o.merge_1q && !it.overlap && it.g.kind == BK_MAT1) {
                 int prev = last_on[it.g.q0];
                 if (prev >= 0 && !taken[prev].overlap && taken[prev].g.kind == BK_MAT1) {
@@ -607,16 +654,43 @@ int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, 
                     taken[prev].g.varying |= it.g.varying;
                     taken[prev].g.diag = matrix_is_diag(c);
                     taken[prev].g.op_index = -1;
-                    continue;
+                    return;
                 }
             }
             taken.push_back(it);
             const int ti = (int)taken.size() - 1;
             for (uint32_t q = 0; q < n; ++q)
                 if ((it.touch >> q) & 1ULL) last_on[q] = ti;
+        };
+        if (hit) {
+            L = replay[pass_i].L;
+            for (int idx : replay[pass_i].sel) take(items[idx]);
+            ++pass_i;
+        } else {
+            // The first remaining item must fit: shrink the always-resident low
+            // block from the top until it does (qubit 0 stays resident, k >= 3).
+            L = low_mask;
+            const uint64_t first_need = items[remaining[0]].need;
+            for (int b = low - 1; b >= 1 && popc(L | first_need) > k; --b) L &= ~(1ULL << b);
+            if (o.search) L = choose_resident(items, remaining, L | first_need, k, n, all, o.max_items);
+            uint64_t blocked = 0;
+            std::vector<int> rest, sel;
+            rest.reserve(remaining.size());
+            for (size_t r = 0; r < remaining.size(); ++r) {
+                const int idx = remaining[r];
+                const Item &it = items[idx];
+                if (blocked == all || taken.size() >= (size_t)o.max_items) { rest.push_back(idx); continue; }
+                if (it.touch & blocked) { blocked |= it.touch; rest.push_back(idx); continue; }
+                const uint64_t nl = L | it.need;
+                if (popc(nl) > k) { blocked |= it.touch; rest.push_back(idx); continue; }
+                L = nl;
+                sel.push_back(idx);
+                take(it);
+            }
+            if (taken.empty()) return fail(QF_ERR_INVALID_ARGUMENT, "planner made no progress");
+            remaining.swap(rest);
+            record.push_back(PassChoice{L, std::move(sel)});
         }
-        if (taken.empty()) return fail(QF_ERR_INVALID_ARGUMENT, "planner made no progress");
-        remaining.swap(rest);
         uint32_t n_blocks = 0, max_block = 0;
         if (kb) {  // the pass's gates as dense blocks of up to kb qubits
             std::vector<BGate> seq;
@@ -778,6 +852,7 @@ int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, 
         p.a.n_slots = plan.n_slots - p.a.slot_base;
         plan.passes.push_back(p);
     }
+    if (!hit) plan_cache_put(key, std::move(record));
     return QF_OK;
 }
 
