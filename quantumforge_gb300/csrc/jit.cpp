@@ -1491,4 +1491,254 @@ int run_plan_jit_dual(qf_sv *psi, qf_sv *lam, const Plan &plan, double *d_slot_s
     return QF_OK;
 }
 
+
+// ---- compiled Pauli-sum passes ----------------------------------------------
+// A Pauli pass (terms grouped by x-mask, every x-bit of its groups resident in
+// a 12-bit tile whose low five bits are qubits 0..4) as one generated kernel.
+// Thread t holds the 16 amplitudes j = lane | i << 5 | warp << 9 (i < 16);
+// the tile arrives by 16-byte cp.async one tile ahead. For a group of x-mask
+// x, the partner of j is j ^ x: in the thread's own registers when x has only
+// register bits, otherwise read from shared memory. The phase of term t at the
+// source index splits into a per-thread bit (lane and warp bits of its z-mask,
+// computed once per kernel), a per-tile bit (its z-mask off the tile), a
+// compile-time bit (the x-mask's lane and warp bits) and the register bits:
+// terms with the same register part of z add into one class sum per tile, and
+// G_i = sum over classes of (-1)^parity((i ^ x_reg) & class) * sum (a
+// Walsh-Hadamard transform when the classes are many). Coefficients live in the
+// constant bank, so a Hamiltonian with new coefficients reuses its kernels.
+namespace {
+
+struct PauliPassDesc {
+    const PPassArgs *a;
+    const std::vector<PGroup> *groups;
+    const std::vector<PTerm> *terms;
+};
+
+bool pauli_pass_fits(const PPassArgs &a) { return a.k == 12 && a.low >= 5 && a.n_terms > 0; }
+
+void gen_pauli_kernel(std::ostringstream &s, const PauliPassDesc &d, int index, int coef_base) {
+    const PPassArgs &a = *d.a;
+    const uint32_t mode = a.mode;
+    uint32_t qb[12];
+    for (uint32_t b = 0; b < 12; ++b) qb[b] = b < a.low ? b : a.hi_q[b - a.low];
+    auto bitq = [&](uint32_t b) { return hex64(1ULL << qb[b]); };
+    s << "extern \"C\" __global__ void __launch_bounds__(256, 2) h" << index
+      << "(const float2* __restrict__ P, float2* __restrict__ L, unsigned long long nt, double* __restrict__ partials) {\n";
+    s << "extern __shared__ __align__(16) float2 SB[];\n";
+    s << "__shared__ double red[32];\n";
+    s << "const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, tid = threadIdx.x;\n";
+    s << "const unsigned sbase = (unsigned)__cvta_generic_to_shared(SB);\n";
+    s << "const unsigned jb = lane | (warp << 9);\n";
+    s << "const unsigned long long ow = ((warp & 1u) ? " << bitq(9) << " : 0ull) | ((warp & 2u) ? " << bitq(10)
+      << " : 0ull) | ((warp & 4u) ? " << bitq(11) << " : 0ull);\n";
+    // cp.async chunk c = tid + 256 k holds tile indices 2c, 2c + 1
+    s << "const unsigned long long toff = (unsigned long long)((2u * tid) & 31u)";
+    for (int b = 0; b < 4; ++b) s << " | ((tid & " << (16u << b) << "u) ? " << bitq(5 + b) << " : 0ull)";
+    s << ";\n";
+    const std::string dep_t = deposit_code(a.nonlocal_mask, "t"), dep_t2 = deposit_code(a.nonlocal_mask, "t2");
+    auto issue = [&](const std::string &tq, const std::string &buf) {
+        for (int k = 0; k < 8; ++k) {
+            uint64_t ck = 0;
+            for (int b = 0; b < 3; ++b)
+                if ((k >> b) & 1) ck |= 1ULL << qb[9 + b];
+            s << "qf_cpa16(sbase + ((" << buf << ") * 4096u + 2u * tid + " << 512 * k << "u) * 8u, P + (" << tq
+              << " | toff | " << hex64(ck) << "));\n";
+        }
+    };
+    // per-thread parity bits of every term (lane and warp bits of its z-mask)
+    const auto &T = *d.terms;
+    const size_t nt_ = T.size();
+    const int n_words = (int)((nt_ + 63) / 64);
+    for (int w = 0; w < n_words; ++w) {
+        s << "unsigned long long tpar" << w << " = 0ull";
+        for (size_t t = 64 * (size_t)w; t < std::min(nt_, 64 * (size_t)w + 64); ++t) {
+            const uint32_t zl = T[t].zl & 31u, zw = (T[t].zl >> 9) & 7u;
+            if (zl || zw)
+                s << " | ((unsigned long long)((__popc(lane & " << zl << "u) + __popc(warp & " << zw << "u)) & 1u) << "
+                  << (t - 64 * w) << ")";
+        }
+        s << ";\n";
+    }
+    s << "double acc_re = 0.0, acc_im = 0.0;\n";
+    s << "unsigned long long t = blockIdx.x;\n";
+    s << "if (t < nt) {const unsigned long long tq = " << dep_t << ";\n";
+    issue("tq", "0u");
+    s << "}\nasm volatile(\"cp.async.commit_group;\\n\" ::: \"memory\");\n";
+    s << "for (unsigned it = 0; t < nt; t += gridDim.x, ++it) {\n";
+    s << "const unsigned cur = it & 1u;\n";
+    s << "{const unsigned long long t2 = t + gridDim.x; if (t2 < nt) {const unsigned long long tq = " << dep_t2 << ";\n";
+    issue("tq", "cur ^ 1u");
+    s << "}}\nasm volatile(\"cp.async.commit_group;\\n\" ::: \"memory\");\n";
+    s << "asm volatile(\"cp.async.wait_group 1;\\n\" ::: \"memory\");\n__syncthreads();\n";
+    s << "const float2* S = SB + cur * 4096u;\n";
+    s << "const unsigned long long base = " << dep_t << ";\n";
+    if (mode != 0) s << "const unsigned long long gb = base | lane | ow;\n";
+    for (int i = 0; i < 16; ++i) s << "const float2 r" << i << " = S[jb | " << (i << 5) << "u];\n";
+    if (mode != 0)
+        for (int i = 0; i < 16; ++i) s << "float2 l" << i << " = make_float2(0.f, 0.f);\n";
+    else
+        s << "float e_re = 0.f, e_im = 0.f;\n";
+    int k = coef_base;
+    for (const PGroup &G : *d.groups) {
+        const uint32_t x = G.xl;
+        const uint32_t xsrc = mode == 0 ? 0u : x;
+        const uint32_t xr = (xsrc >> 5) & 15u;
+        const bool real = G.real != 0;
+        // class sums
+        std::map<uint32_t, int> cls;
+        for (uint32_t q = 0; q < G.t_count; ++q) cls.emplace((T[G.t_begin + q].zl >> 5) & 15u, (int)cls.size());
+        s << "{\n";
+        for (auto &c : cls) s << "float sr" << c.second << " = 0.f" << (real ? "" : std::string(", si") + std::to_string(c.second) + " = 0.f") << ";\n";
+        for (uint32_t q = 0; q < G.t_count; ++q, ++k) {
+            const PTerm &P = T[G.t_begin + q];
+            const size_t ti = G.t_begin + q;
+            const uint32_t zl = P.zl & 31u, zw = (P.zl >> 9) & 7u;
+            const uint32_t cflip = (uint32_t)((__builtin_popcount((xsrc & 31u) & zl) + __builtin_popcount(((xsrc >> 9) & 7u) & zw)) & 1);
+            std::ostringstream bit;
+            bit << "(unsigned)((tpar" << ti / 64 << " >> " << ti % 64 << ") & 1ull)";
+            if (P.zo) bit << " ^ (unsigned)(__popcll(base & " << hex64(P.zo) << ") & 1)";
+            if (cflip) bit << " ^ 1u";
+            const int c = cls[(P.zl >> 5) & 15u];
+            s << "{const unsigned b = " << bit.str() << "; const float2 c = M[" << k << "]; sr" << c << " += b ? -c.x : c.x;";
+            if (!real) s << " si" << c << " += b ? -c.y : c.y;";
+            s << "}\n";
+        }
+        // G_i for every register index, then the multiply-add with the partner
+        const bool fwht = cls.size() > 4;
+        if (fwht) {  // W[c] for all 16 classes, then the butterflies: H[i] = sum_c (-1)^popc(i & c) W[c]
+            for (int c = 0; c < 16; ++c) {
+                auto it = cls.find((uint32_t)c);
+                s << "float wr" << c << " = " << (it == cls.end() ? std::string("0.f") : "sr" + std::to_string(it->second)) << ";";
+                if (!real) s << "float wi" << c << " = " << (it == cls.end() ? std::string("0.f") : "si" + std::to_string(it->second)) << ";";
+            }
+            s << "\n";
+            for (int h = 1; h < 16; h <<= 1)
+                for (int c = 0; c < 16; ++c)
+                    if (!(c & h)) {
+                        s << "{const float u = wr" << c << ", v = wr" << (c | h) << "; wr" << c << " = u + v; wr" << (c | h) << " = u - v;}";
+                        if (!real)
+                            s << "{const float u = wi" << c << ", v = wi" << (c | h) << "; wi" << c << " = u + v; wi" << (c | h) << " = u - v;}";
+                    }
+            s << "\n";
+        }
+        const bool in_regs = (x & 31u) == 0 && ((x >> 9) & 7u) == 0;
+        for (int i = 0; i < 16; ++i) {
+            const uint32_t isrc = (uint32_t)i ^ xr;
+            std::ostringstream gr, gi;
+            if (fwht) {
+                gr << "wr" << isrc;
+                gi << "wi" << isrc;
+            } else {
+                bool first = true;
+                for (auto &c : cls) {
+                    const bool neg = __builtin_popcount(isrc & c.first) & 1;
+                    gr << (first ? (neg ? "-" : "") : (neg ? "-" : "+")) << "sr" << c.second;
+                    gi << (first ? (neg ? "-" : "") : (neg ? "-" : "+")) << "si" << c.second;
+                    first = false;
+                }
+            }
+            std::string part;
+            if (in_regs) part = "r" + std::to_string(i ^ (int)((x >> 5) & 15u));
+            else part = "S[(jb | " + std::to_string(i << 5) + "u) ^ " + std::to_string(x) + "u]";
+            s << "{const float g_r = " << gr.str() << ";";
+            if (!real) s << "const float g_i = " << gi.str() << ";";
+            s << "const float2 p = " << part << ";";
+            if (mode != 0) {
+                const std::string l = "l" + std::to_string(i);
+                if (real) s << l << ".x = fmaf(g_r, p.x, " << l << ".x); " << l << ".y = fmaf(g_r, p.y, " << l << ".y);";
+                else
+                    s << l << ".x = fmaf(g_r, p.x, fmaf(-g_i, p.y, " << l << ".x)); " << l << ".y = fmaf(g_r, p.y, fmaf(g_i, p.x, "
+                      << l << ".y));";
+            } else {  // conj(psi_{j^x}) * G(j) * psi_j
+                const std::string r = "r" + std::to_string(i);
+                if (real) s << "const float tr = g_r * " << r << ".x, ti = g_r * " << r << ".y;";
+                else s << "const float tr = g_r * " << r << ".x - g_i * " << r << ".y, ti = g_r * " << r << ".y + g_i * " << r << ".x;";
+                s << "e_re = fmaf(p.x, tr, fmaf(p.y, ti, e_re)); e_im = fmaf(p.x, ti, fmaf(-p.y, tr, e_im));";
+            }
+            s << "}\n";
+        }
+        s << "}\n";
+    }
+    if (mode != 0) {
+        s << "float e_re = 0.f, e_im = 0.f;\n";
+        for (int i = 0; i < 16; ++i) {
+            uint64_t off = 0;
+            for (int b = 0; b < 4; ++b)
+                if ((i >> b) & 1) off |= 1ULL << qb[5 + b];
+            const std::string l = "l" + std::to_string(i), r = "r" + std::to_string(i);
+            s << "{float2* q = L + (gb | " << hex64(off) << ");";
+            if (mode == 2) s << "const float2 o = *q; " << l << ".x += o.x; " << l << ".y += o.y;";
+            s << "*q = " << l << ";";
+            if (a.last) s << "e_re = fmaf(" << r << ".x, " << l << ".x, fmaf(" << r << ".y, " << l << ".y, e_re)); e_im = fmaf(" << r
+                          << ".x, " << l << ".y, fmaf(-" << r << ".y, " << l << ".x, e_im));";
+            s << "}\n";
+        }
+    }
+    s << "acc_re += (double)e_re; acc_im += (double)e_im;\n";
+    s << "__syncthreads();\n}\n";  // tile loop
+    s << "asm volatile(\"cp.async.wait_group 0;\\n\" ::: \"memory\");\n";
+    s << "for (int o = 16; o > 0; o >>= 1) {acc_re += __shfl_xor_sync(0xffffffffu, acc_re, o); acc_im += __shfl_xor_sync(0xffffffffu, acc_im, o);}\n";
+    s << "if (lane == 0) {red[warp] = acc_re; red[8 + warp] = acc_im;}\n__syncthreads();\n";
+    s << "if (tid == 0) {double a = 0.0, b = 0.0; for (int w = 0; w < 8; ++w) {a += red[w]; b += red[8 + w];} partials[2 * blockIdx.x] = a; "
+         "partials[2 * blockIdx.x + 1] = b;}\n";
+    s << "}\n";
+}
+
+struct PauliModule {
+    std::shared_ptr<JitModule> mod;
+    std::vector<float> consts;
+};
+
+}  // namespace
+
+int run_pauli_jit(qf_sv *psi, qf_sv *lam, const std::vector<const PPassArgs *> &args,
+                  const std::vector<const std::vector<PGroup> *> &groups, const std::vector<const std::vector<PTerm> *> &terms,
+                  double *partials, uint32_t slice_stride, uint32_t max_grid, bool *ran) {
+    *ran = false;
+    if (psi->dtype != QF_C64 || !jit_available() || args.empty()) return QF_OK;
+    for (const PPassArgs *a : args)
+        if (!pauli_pass_fits(*a)) return QF_OK;
+    qf_ctx *ctx = psi->ctx;
+    // source text (structure only) and constants (the coefficients)
+    ModulePlan mp;
+    mp.prefix = 'h';
+    std::ostringstream body;
+    std::vector<float> consts;
+    for (size_t p = 0; p < args.size(); ++p) {
+        PauliPassDesc d{args[p], groups[p], terms[p]};
+        gen_pauli_kernel(body, d, (int)p, (int)(consts.size() / 2));
+        for (const PGroup &G : *groups[p])
+            for (uint32_t q = 0; q < G.t_count; ++q) {
+                consts.push_back((float)(*terms[p])[G.t_begin + q].cre);
+                consts.push_back((float)(*terms[p])[G.t_begin + q].cim);
+            }
+        mp.pass_index.push_back((int)p);
+    }
+    if (consts.size() * 4 > 60 * 1024) return QF_OK;  // the constant bank holds at most ~7500 terms
+    std::ostringstream head;
+    head << "__constant__ float2 M[" << std::max<size_t>(1, consts.size() / 2) << "];\n" << kPrelude;
+    mp.src = std::make_shared<const std::string>(head.str() + body.str());
+    mp.consts = consts;
+    std::vector<ModulePlan> mods{mp};
+    std::vector<std::shared_ptr<JitModule>> handles;
+    QF_TRY(fetch_modules(ctx, mods, handles));
+    JitModule &jm = *handles[0];
+    QF_TRY(upload_consts(ctx, jm, mods[0]));
+    for (size_t p = 0; p < args.size(); ++p) {
+        const PPassArgs &a = *args[p];
+        int per_sm = 0;
+        QF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)jm.kernels[p], 256, dyn_smem_of(12)));
+        const uint64_t grid = std::min<uint64_t>(std::min<uint64_t>((uint64_t)std::max(per_sm, 1) * ctx->sm_count, max_grid),
+                                                 a.n_tiles);
+        const float2 *P = static_cast<const float2 *>(psi->d);
+        float2 *Lp = lam ? static_cast<float2 *>(lam->d) : nullptr;
+        unsigned long long nt = a.n_tiles;
+        double *parts = partials + (size_t)slice_stride * p;
+        void *kargs[] = {&P, &Lp, &nt, &parts};
+        QF_CUDA(cudaLaunchKernel((const void *)jm.kernels[p], dim3((unsigned)grid), dim3(256), kargs, dyn_smem_of(12), ctx->stream));
+    }
+    *ran = true;
+    return QF_OK;
+}
+
 }  // namespace qf

@@ -342,6 +342,48 @@ int collapse(qf_sv *sv, uint32_t q, int outcome, double scale);
 // Pauli sums: <psi|H|psi> (complex), and lambda = H psi with <psi|lambda>.
 int pauli_expectation(qf_sv *sv, const qf_pauli_term *terms, uint64_t n_terms, double out[2]);
 int pauli_apply(qf_sv *psi, qf_sv *lambda, const qf_pauli_term *terms, uint64_t n_terms, double *energy);
+// ---- Pauli-sum passes (reduce.cu, compiled form in jit.cpp) --------------
+struct PTerm {
+    uint64_t z;
+    double cre, cim;  // coefficient times i^{ny}
+    uint64_t zo;      // z on the pass's non-resident qubits
+    uint32_t zl;      // z on the resident qubits, in tile-local bits
+    uint32_t q;       // bit r: parity of r & (zl >> 8) (the register part of a thread's amplitudes)
+};
+struct PGroup {
+    uint64_t x;        // global x-mask
+    uint32_t xl;       // the same mask in local tile bits
+    uint32_t t_begin;  // into the pass's term array
+    uint32_t t_count;
+    uint32_t real;     // every coefficient of the group is real
+    // Groups of many terms (the register-tiled pass) are evaluated from two
+    // per-tile tables: their terms are ordered [z only on local bits 0..5 |
+    // only on local bits 6.. | only off the tile | both halves], and
+    // G(j) = TL[j & 63] + TH[j >> 6] + the terms spanning both halves.
+    uint32_t tab;      // table slot, or kNoTable
+    uint32_t n_lo, n_hi, n_const;
+};
+constexpr uint32_t kNoTable = 0xFFFFFFFFu;
+constexpr uint32_t kTableTerms = 6;     // groups with at least this many terms get tables
+constexpr uint32_t kTableEntries = 192;  // 64 (bits 0..5) + up to 128 (bits 6..12)
+struct PPassArgs {
+    uint64_t nonlocal_mask;
+    uint64_t n_tiles;
+    uint32_t k, low, n_groups, n_terms;
+    uint32_t mode;  // 0 = expectation, 1 = write lambda, 2 = accumulate lambda
+    uint32_t last;  // accumulate <psi|lambda> (mode 1/2)
+    uint32_t n_tables;  // groups evaluated from per-tile tables (register-tiled pass)
+    uint8_t hi_q[kMaxLocal];
+};
+
+
+// Compiled Pauli-sum passes (jit.cpp): complex64, every pass a 12-bit tile whose
+// low five bits are qubits 0..4; pass p writes its partial sums to
+// partials[p * slice_stride ...] (2 doubles per CTA, at most max_grid CTAs).
+// *ran is false (and nothing launched) when a pass does not fit.
+int run_pauli_jit(qf_sv *psi, qf_sv *lam, const std::vector<const PPassArgs *> &args,
+                  const std::vector<const std::vector<PGroup> *> &groups, const std::vector<const std::vector<PTerm> *> &terms,
+                  double *partials, uint32_t slice_stride, uint32_t max_grid, bool *ran);
 // Launch counts of the Pauli-sum passes (host only): tile passes and sweeps of
 // groups whose x-mask does not fit a tile.
 int pauli_plan_stats(uint32_t n, int dtype, const qf_pauli_term *terms, uint64_t n_terms, uint64_t *tile_passes,

@@ -462,13 +462,6 @@ int batch_measure(qf_sv *sv, uint32_t n, uint64_t B, uint32_t q, const double *u
 //   <psi|H_x|psi> = sum_i conj(psi_{i^x}) G_x(i) psi_i,  (H_x psi)_j = G_x(j^x) psi_{j^x}.
 // A pass keeps every x-bit of its groups tile-resident, so each partner
 // amplitude is in shared memory.
-struct PTerm {
-    uint64_t z;
-    double cre, cim;  // coefficient times i^{ny}
-    uint64_t zo;      // z on the pass's non-resident qubits
-    uint32_t zl;      // z on the resident qubits, in tile-local bits
-    uint32_t q;       // bit r: parity of r & (zl >> 8) (the register part of a thread's amplitudes)
-};
 // a term staged in shared memory with its coefficient in the state's real
 // type: converted once per CTA, not once per amplitude
 template <typename R>
@@ -482,32 +475,6 @@ struct PTermT {
     uint32_t zl, q;
     R cre, cim;
 };
-struct PGroup {
-    uint64_t x;        // global x-mask
-    uint32_t xl;       // the same mask in local tile bits
-    uint32_t t_begin;  // into the pass's term array
-    uint32_t t_count;
-    uint32_t real;     // every coefficient of the group is real
-    // Groups of many terms (the register-tiled pass) are evaluated from two
-    // per-tile tables: their terms are ordered [z only on local bits 0..5 |
-    // only on local bits 6.. | only off the tile | both halves], and
-    // G(j) = TL[j & 63] + TH[j >> 6] + the terms spanning both halves.
-    uint32_t tab;      // table slot, or kNoTable
-    uint32_t n_lo, n_hi, n_const;
-};
-constexpr uint32_t kNoTable = 0xFFFFFFFFu;
-constexpr uint32_t kTableTerms = 6;     // groups with at least this many terms get tables
-constexpr uint32_t kTableEntries = 192;  // 64 (bits 0..5) + up to 128 (bits 6..12)
-struct PPassArgs {
-    uint64_t nonlocal_mask;
-    uint64_t n_tiles;
-    uint32_t k, low, n_groups, n_terms;
-    uint32_t mode;  // 0 = expectation, 1 = write lambda, 2 = accumulate lambda
-    uint32_t last;  // accumulate <psi|lambda> (mode 1/2)
-    uint32_t n_tables;  // groups evaluated from per-tile tables (register-tiled pass)
-    uint8_t hi_q[kMaxLocal];
-};
-
 template <typename C>
 __global__ void __launch_bounds__(kRedThreads)
     k_pauli_pass(const C *__restrict__ psi, C *__restrict__ lam, const PPassArgs pa, const PGroup *__restrict__ g_groups,
@@ -968,10 +935,27 @@ int run_pauli(qf_sv *psi, qf_sv *lam, PauliPlan &plan, bool apply, double out[2]
     unsigned char *dmeta = static_cast<unsigned char *>(ctx->ws_plan);
     size_t off = 0, slice = 0;
     if (apply && plan.tiles.empty()) QF_CUDA(cudaMemsetAsync(lam->d, 0, lam->bytes(), ctx->stream));
-    for (size_t i = 0; i < plan.tiles.size(); ++i, ++slice) {
+    for (size_t i = 0; i < plan.tiles.size(); ++i) {
         PPassHost &P = plan.tiles[i];
         P.a.mode = apply ? (i == 0 ? 1u : 2u) : 0u;
         P.a.last = (apply && !need_dot && i + 1 == plan.tiles.size()) ? 1u : 0u;
+    }
+    // complex64 tile passes: compiled kernels (one per pass) when every pass fits
+    bool compiled = false;
+    if (sizeof(C) == 8 && !plan.tiles.empty()) {
+        std::vector<const PPassArgs *> pa;
+        std::vector<const std::vector<PGroup> *> pg;
+        std::vector<const std::vector<PTerm> *> pt;
+        for (const PPassHost &P : plan.tiles) {
+            pa.push_back(&P.a);
+            pg.push_back(&P.groups);
+            pt.push_back(&P.terms);
+        }
+        QF_TRY(run_pauli_jit(psi, lam, pa, pg, pt, partials, 2 * grid, grid, &compiled));
+        if (compiled) slice += plan.tiles.size();
+    }
+    for (size_t i = 0; i < plan.tiles.size() && !compiled; ++i, ++slice) {
+        PPassHost &P = plan.tiles[i];
         PGroup *dg = reinterpret_cast<PGroup *>(dmeta + off);
         QF_CUDA(cudaMemcpyAsync(dg, P.groups.data(), P.groups.size() * sizeof(PGroup), cudaMemcpyHostToDevice, ctx->stream));
         off += (P.groups.size() * sizeof(PGroup) + 15) / 16 * 16;
