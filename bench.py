@@ -479,7 +479,8 @@ def c2_matrix(backend, n64: int = 30, n128: int = 26, depth: int = 40, seed: int
     reference's structure), as per-gate tile passes (the default), and fused
     into dense k-qubit blocks for k = 2..5 (k = 5 on the tensor cores and on
     the FP32 pipe), in complex64 at 30 qubits and complex128 at 26 qubits
-    (FP64 dense blocks of 5 qubits take minutes at 30). Per mode: gates/s, HBM
+    (FP64 dense blocks of 5 qubits take minutes at 30; complex128 unfused and
+    per-gate passes also at 30). Per mode: gates/s, HBM
     passes, the fraction of the measured copy peak over the passes'
     algorithmic bytes, and the largest amplitude error against the complex128
     per-gate result of the same circuit."""
@@ -504,9 +505,14 @@ def c2_matrix(backend, n64: int = 30, n128: int = 26, depth: int = 40, seed: int
            "reference_state": "complex128 per-gate tile passes of the same circuit"}
     if modes_wanted:
         modes = [m for m in modes if m[0] in modes_wanted]
-    for dtype, n in (("c64", n64), ("c128", n128)):
+    runs = [("c64", n64), ("c128", n128)]
+    if n128 < n64:  # complex128 at the full size too, for the unfused sweeps and the per-gate passes
+        runs.append(("c128", n64))
+    all_modes = modes
+    for dtype, n in runs:
         if dtype not in dtypes:
             continue
+        modes = [m for m in all_modes if m[0] in ("unfused", "passes")] if (dtype == "c128" and n > n128) else all_modes
         ops = W.random_circuit(n, depth, seed, two_qubit="mixed")
         b = 8 if dtype == "c64" else 16
         ref = qf.StateVector.zero(n, dtype="c128", backend=backend)

@@ -695,7 +695,11 @@ struct PassGen {
         } else {
             // one psi + lambda buffer; the next tile streams in after the last
             // shared-memory read of the current one
-            for (int a = 0; a < n_acc(); ++a) s << "double acc" << a << " = 0.0;\n";
+            // overlap sums per lane as an unevaluated pair of floats (hi + lo,
+            // every addition's rounding error carried in lo): the precision of
+            // an f64 accumulator without the FP64 pipe, which GB300 runs at a
+            // small fraction of its FP32 rate
+            for (int a = 0; a < n_acc(); ++a) s << "float acc" << a << "h = 0.f, acc" << a << "l = 0.f;\n";
             s << "if (t < nt) {const unsigned long long tq = " << dep_t << ";\n";
             emit_issue("tq");
             s << "}\nasm volatile(\"cp.async.commit_group;\\n\" ::: \"memory\");\n";
@@ -801,7 +805,9 @@ struct PassGen {
             s << "ov *= " << Mref(sl, 0) << ".x;\n";
         }
         for (int o = 16; o >= 1; o >>= 1) s << "ov += __shfl_xor_sync(0xffffffffu, ov, " << o << ");\n";
-        s << "if (lane == " << (ls & 31) << "u) acc" << (ls >> 5) << " += (double)ov;}\n";
+        const std::string ah = "acc" + std::to_string(ls >> 5) + "h", al = "acc" + std::to_string(ls >> 5) + "l";
+        s << "if (lane == " << (ls & 31) << "u) {const float sm = " << ah << " + ov, bb = sm - " << ah << "; " << al << " += ("
+          << ah << " - (sm - bb)) + (ov - bb); " << ah << " = sm;}}\n";
     }
 
     void emit_gate(const BGate &x) {
@@ -1047,8 +1053,8 @@ struct PassGen {
             s << "asm volatile(\"cp.async.wait_group 0;\\n\" ::: \"memory\");\n__syncthreads();\n";
             s << "double* RD = reinterpret_cast<double*>(SB);\n";
             for (int a = 0; a < n_acc(); ++a)
-                s << "if (lane + " << 32 * a << "u < " << p.a.n_slots << "u) RD[(lane + " << 32 * a << "u) * 8u + warp] = acc" << a
-                  << ";\n";
+                s << "if (lane + " << 32 * a << "u < " << p.a.n_slots << "u) RD[(lane + " << 32 * a << "u) * 8u + warp] = (double)acc"
+                  << a << "h + (double)acc" << a << "l;\n";
             s << "__syncthreads();\n";
             s << "for (unsigned k = tid; k < " << p.a.n_slots << "u; k += " << threads_of(K) << "u) {double v = 0.0;"
               << " for (unsigned w = 0; w < 8u; ++w) v += RD[k * 8u + w];"
