@@ -248,6 +248,10 @@ int dm_channels_fused(qf_sv *sv, uint32_t n, const uint32_t *qs, const double (*
     qf_ctx *ctx = sv->ctx;
     if (count == 0) return QF_OK;
     if (count > (uint32_t)kMaxTileChannels || 2 * n < 5) return fail(QF_ERR_INVALID_ARGUMENT, "channel group too large");
+    // the kernel moves complex64 entries two at a time (16-byte accesses): the
+    // tile's low five bits are column bits 0..4 and the matrix is 16-byte aligned
+    if (reinterpret_cast<uintptr_t>(sv->d) % 16)
+        return fail(QF_ERR_INVALID_ARGUMENT, "density matrix storage is not 16-byte aligned");
     uint64_t tile_mask = 31;  // the low five column bits
     for (uint32_t c = 0; c < count; ++c) tile_mask |= (1ULL << qs[c]) | (1ULL << (n + qs[c]));
     // widen to 12 tile bits with the lowest free bits: fewer, larger tiles

@@ -74,3 +74,18 @@ def test_blocks_keep_the_state_normalised_at_scale(backend):
         sv.apply_ops(inv, exec_opts={"block_qubits": k})
         a = sv.amplitudes()
         assert abs(a[0] - 1.0) < 1e-4 and float(np.abs(a[1:]).max()) < 1e-4, k
+
+
+def test_autotuner_picks_a_runnable_fastest_option(backend):
+    """The execution autotuner times every candidate (per-gate passes, 13-qubit
+    tiles, fusion widths 2..5) and returns the fastest; the choice reproduces
+    the oracle's state."""
+    from quantumforge_gb300.autotune import autotune_exec
+
+    n = 16
+    ops = W.random_circuit(n, 6, 12, two_qubit="mixed")
+    best, times = autotune_exec(ops, n, backend=backend, reps=1)
+    assert len(times) >= 4 and min(times.values()) > 0
+    sv = StateVector.zero(n, dtype="c64", backend=backend)
+    sv.apply_ops(ops, exec_opts=best)
+    assert float(np.abs(sv.amplitudes() - O.run(ops, n)).max()) < TOL["c64"]

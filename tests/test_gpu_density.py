@@ -94,7 +94,8 @@ def _noisy_density_circuit(n, seed):
 
 
 @pytest.mark.parametrize("n,seed,dtype,tol", [(2, 1, "c128", 1e-12), (5, 2, "c128", 1e-11), (8, 3, "c128", 1e-11),
-                                              (10, 4, "c128", 1e-11), (6, 5, "c64", 2e-6), (9, 6, "c64", 2e-6)])
+                                              (10, 4, "c128", 1e-11), (3, 7, "c64", 2e-6), (4, 8, "c64", 2e-6),
+                                              (6, 5, "c64", 2e-6), (9, 6, "c64", 2e-6)])
 @pytest.mark.parametrize("start", ["pure", "mixed"])
 def test_random_noisy_density_circuits_match_the_oracle(backend, n, seed, dtype, tol, start):
     c = _noisy_density_circuit(n, seed)
