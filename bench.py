@@ -547,7 +547,8 @@ def c2_matrix(backend, n64: int = 30, n128: int = 26, depth: int = 40, seed: int
                           "algorithmic_gb": algo / 1e9, "frac": algo / t / 1e9 / peak,
                           "max_abs_amp_err_vs_c128": err}
             del sv
-        out[f"{dtype}_{n}q"] = {"gates": len(ops), **rows}
+        timed = {m: r["gates_per_s"] for m, r in rows.items() if "gates_per_s" in r}
+        out[f"{dtype}_{n}q"] = {"gates": len(ops), "fastest": max(timed, key=timed.get) if timed else None, **rows}
         del ref
         torch.cuda.empty_cache()
     return out

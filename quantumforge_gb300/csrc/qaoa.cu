@@ -52,17 +52,64 @@ struct QShared {
     float2 tp[1 << kQMaxTile];
     float2 tl[1 << kQMaxTile];
     float2 phase[kQMaxEdges + 1];  // exp(-iγ(W - 2c)) for the current layer
-    uint64_t emask[kQMaxEdges];
+    uint32_t emask[kQMaxEdges];
     double red[32];
     double acc[2 * kQMaxP];
     double energy;
     uint32_t inst;
 };
 
-__device__ __forceinline__ uint32_t cut_value(uint64_t x, const uint64_t *emask, uint32_t ne) {
+// Edge masks hold both endpoints as bits; instances have at most 24 qubits.
+__device__ __forceinline__ uint32_t cut_value(uint32_t x, const uint32_t *emask, uint32_t ne) {
     uint32_t c = 0;
-    for (uint32_t e = 0; e < ne; ++e) c += __popcll(x & emask[e]) & 1u;
+    for (uint32_t e = 0; e < ne; ++e) c += __popc(x & emask[e]) & 1u;
     return c;
+}
+
+// bit b < 4 of k = 4q + r as bytes r = 0..3 of a word (0 or 1 each)
+__device__ __forceinline__ uint32_t cut_bit_bytes(uint32_t b, uint32_t q) {
+    return b == 0 ? 0x01000100u : b == 1 ? 0x01010000u : ((q >> (b - 2)) & 1u) ? 0x01010101u : 0u;
+}
+
+// C(base | k) for k = 0..15, byte k & 3 of word k >> 2 (base has bits 0..3
+// clear). An edge above bit 3 adds the constant parity of base; an edge from
+// bit b < 4 to a bit w above adds bit b of k, or 1 minus it where bit w of
+// base is set; an edge inside bits 0..3 adds a fixed byte pattern. Per k the
+// sum is c + the D_b of the bits b set in k (D_b = edges at b with bit w clear
+// minus those with it set), plus the pattern: one pass over the edges per 16
+// amplitudes.
+__device__ __forceinline__ uint4 cut16(uint32_t base, const uint32_t *emask, uint32_t ne) {
+    uint32_t c = 0, dp = 0, dm = 0;
+    uint32_t t2[4] = {0u, 0u, 0u, 0u};
+    for (uint32_t e = 0; e < ne; ++e) {
+        const uint32_t m = emask[e], lo = m & 15u;
+        if (lo == 0) {
+            c += __popc(base & m) & 1u;
+        } else if (lo != m) {
+            const uint32_t f = 1u << (8 * (__ffs(lo) - 1));
+            if (base & m) {
+                ++c;
+                dm += f;
+            } else {
+                dp += f;
+            }
+        } else {
+            const uint32_t u = __ffs(m) - 1, v = 31 - __clz(m);
+#pragma unroll
+            for (uint32_t q = 0; q < 4; ++q) t2[q] += cut_bit_bytes(u, q) ^ cut_bit_bytes(v, q);
+        }
+    }
+    int d[4];
+#pragma unroll
+    for (uint32_t b = 0; b < 4; ++b) d[b] = (int)((dp >> (8 * b)) & 0xFFu) - (int)((dm >> (8 * b)) & 0xFFu);
+    uint32_t w[4];
+#pragma unroll
+    for (uint32_t q = 0; q < 4; ++q) {
+        const int h = (int)c + ((q & 1u) ? d[2] : 0) + ((q & 2u) ? d[3] : 0);
+        w[q] = t2[q] + ((uint32_t)h | ((uint32_t)(h + d[0]) << 8) | ((uint32_t)(h + d[1]) << 16) |
+                        ((uint32_t)(h + d[0] + d[1]) << 24));
+    }
+    return make_uint4(w[0], w[1], w[2], w[3]);
 }
 
 // Local tile index j <-> amplitude index for a tile whose qubits are the low
@@ -212,12 +259,12 @@ __global__ void __launch_bounds__(kQThreads)
         const uint32_t n = D.n, ne = D.e_count;
         float2 *psi = arena + D.psi, *lam = arena + D.lam;
         uint8_t *cost = costs + D.cost;
-        for (uint32_t e = threadIdx.x; e < ne; e += blockDim.x) S.emask[e] = emasks[D.e_begin + e];
+        for (uint32_t e = threadIdx.x; e < ne; e += blockDim.x) S.emask[e] = (uint32_t)emasks[D.e_begin + e];
         if (threadIdx.x < 2 * kQMaxP) S.acc[threadIdx.x] = 0.0;
         __syncthreads();
         const uint64_t dim = 1ULL << n;
         const float amp0 = (float)(1.0 / sqrt((double)dim));
-        for (uint64_t x = threadIdx.x; x < dim; x += blockDim.x) {  // H on every qubit of |0>; C(x)
+        for (uint32_t x = threadIdx.x; x < (uint32_t)dim; x += blockDim.x) {  // H on every qubit of |0>; C(x)
             psi[x] = make_float2(amp0, 0.f);
             cost[x] = (uint8_t)cut_value(x, S.emask, ne);
         }
@@ -314,10 +361,6 @@ __device__ __forceinline__ void qb_cp16(void *dst, const void *src) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
                  : "memory");
 }
-__device__ __forceinline__ void qb_cp_wait() {
-    asm volatile("cp.async.commit_group;\n" ::: "memory");
-    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-}
 // Shared-memory position of tile amplitude j: bits 1..3 XOR bits 4..6, so
 // that the mixer round on tile bits 0..3 (16-byte pair accesses, 8 lanes per
 // phase) and the rounds on higher bits (8-byte accesses, 16 lanes per phase)
@@ -333,30 +376,6 @@ __device__ __forceinline__ void qb_load(float2 *dst, const float2 *src, bool pas
     for (uint32_t c = threadIdx.x; c < kQBT / 2; c += blockDim.x)
         qb_cp16(dst + qb_phys(2 * c), src + qb_index(pass_b, L, t, 2 * c));
 }
-// the 16 amplitudes base | (i << b0) of a mixer round, and back
-__device__ __forceinline__ void qb_read(const float2 *tile, uint32_t base, uint32_t b0, float2 (&v)[16]) {
-    if (b0 == 0) {
-#pragma unroll
-        for (uint32_t i = 0; i < 16; i += 2) {
-            const float4 t = *reinterpret_cast<const float4 *>(tile + qb_phys(base | i));
-            v[i] = make_float2(t.x, t.y);
-            v[i + 1] = make_float2(t.z, t.w);
-        }
-    } else {
-#pragma unroll
-        for (uint32_t i = 0; i < 16; ++i) v[i] = tile[qb_phys(base | (i << b0))];
-    }
-}
-__device__ __forceinline__ void qb_write(float2 *tile, uint32_t base, uint32_t b0, const float2 (&v)[16]) {
-    if (b0 == 0) {
-#pragma unroll
-        for (uint32_t i = 0; i < 16; i += 2)
-            *reinterpret_cast<float4 *>(tile + qb_phys(base | i)) = make_float4(v[i].x, v[i].y, v[i + 1].x, v[i + 1].y);
-    } else {
-#pragma unroll
-        for (uint32_t i = 0; i < 16; ++i) tile[qb_phys(base | (i << b0))] = v[i];
-    }
-}
 // the cost bytes of a pass-A tile (contiguous)
 __device__ __forceinline__ void qb_load_cost(uint8_t *dst, const uint8_t *src, uint64_t t) {
     for (uint32_t c = threadIdx.x; c < kQBT / 16; c += blockDim.x) qb_cp16(dst + 16 * c, src + (t << kQBTile) + 16 * c);
@@ -367,80 +386,159 @@ __device__ __forceinline__ void qb_load_cost(uint8_t *dst, const uint8_t *src, u
 // kernel computes them
 __global__ void __launch_bounds__(kQThreads)
     k_qaoa_costs(const QBArgs a, const QDesc *__restrict__ desc, const uint64_t *__restrict__ emasks, uint8_t *__restrict__ costs) {
-    __shared__ uint64_t em[kQMaxEdges];
+    __shared__ uint32_t em[kQMaxEdges];
     const uint64_t items = (uint64_t)a.m * a.tiles;
     for (uint64_t w = blockIdx.x; w < items; w += gridDim.x) {
         const uint32_t ci = (uint32_t)(w / a.tiles);
         const uint64_t t = w % a.tiles;
         const QDesc D = desc[a.r0 + ci];
         __syncthreads();
-        for (uint32_t e = threadIdx.x; e < D.e_count; e += blockDim.x) em[e] = emasks[D.e_begin + e];
+        for (uint32_t e = threadIdx.x; e < D.e_count; e += blockDim.x) em[e] = (uint32_t)emasks[D.e_begin + e];
         __syncthreads();
-        uint8_t *cost = costs + D.cost;
-        for (uint32_t j = threadIdx.x; j < kQBT; j += blockDim.x) {
-            const uint64_t x = (t << kQBTile) | j;
-            cost[x] = (uint8_t)cut_value(x, em, D.e_count);
-        }
+        uint8_t *cost = costs + D.cost + (t << kQBTile);  // 16-byte aligned: batched rows come first, 2^n >= 2^13 each
+        for (uint32_t g = threadIdx.x; g < kQBT / 16; g += blockDim.x)
+            *reinterpret_cast<uint4 *>(cost + 16 * g) = cut16((uint32_t)(t << kQBTile) | (g << 4), em, D.e_count);
     }
 }
 
+// Per (instance, layer) mixer constants of the batched passes. Each gate
+// exp(-i beta X) is applied divided by a real factor F, which leaves four FMAs
+// per amplitude pair: form C (|cos beta| >= |sin beta|) divides by cos beta
+// (k = tan beta), form S by sin beta (k = cot beta); the inverse gate has -k
+// and F' = cos beta or -sin beta. The factors a state picks up in a layer
+// (F^n, or F'^n in reverse) are multiplied back where a pass already touches
+// every amplitude (the next layer's cost phase, the last forward write, the
+// inverse cost phase) and into the gradient sums as scalars.
+struct QMix {
+    float kf, kr;   // forward / inverse gate constant
+    float f2;       // F^2
+    float fn_f;     // F^n
+    float fn_r;     // F'^n
+    float f2_a0;    // F^(2(n-12)): a reverse pass A starts after the n-12 gates of pass B
+    uint32_t form_c;
+    uint32_t pad;
+};
+
+// Phase tables per (instance, layer): forward exp(-i gamma_l (W - 2c)) times
+// the factor its input carries (2^(-n/2) in layer 0, F_{l-1}^n after), at
+// ptab + l * span; the reverse table, times F'_l^n, at ptab + (p + l) * span.
 __global__ void k_qaoa_tables(const QDesc *__restrict__ desc, uint32_t rows, const double *__restrict__ gammas,
-                              const double *__restrict__ betas, uint32_t p, float2 *__restrict__ ptab, float2 *__restrict__ mtab) {
+                              const double *__restrict__ betas, uint32_t p, float2 *__restrict__ ptab, QMix *__restrict__ mtab) {
     const uint32_t span = kQMaxEdges + 1;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < (uint64_t)rows * p * span;
          i += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t r = (uint32_t)(i / ((uint64_t)p * span)), l = (uint32_t)((i / span) % p), c = (uint32_t)(i % span);
         const QDesc D = desc[r];
-        const double gm = gammas[(size_t)D.out * p + l];
+        const int n = (int)D.n;
+        auto factor = [&](uint32_t layer, bool inverse) {  // F or F' of a layer's mixer
+            const double bt = betas[(size_t)D.out * p + layer], cb = cos(bt), sb = sin(bt);
+            return fabs(cb) >= fabs(sb) ? cb : (inverse ? -sb : sb);
+        };
         if (c <= D.e_count) {
+            const double gm = gammas[(size_t)D.out * p + l];
             const double ang = -gm * ((double)D.e_count - 2.0 * (double)c);
-            ptab[D.ptab + (uint64_t)l * span + c] = make_float2((float)cos(ang), (float)sin(ang));
+            const double hin = l == 0 ? 1.0 / sqrt((double)(1ULL << n)) : pow(factor(l - 1, false), n);
+            const double hrev = pow(factor(l, true), n);
+            const double ca = cos(ang), sa = sin(ang);
+            ptab[D.ptab + (uint64_t)l * span + c] = make_float2((float)(hin * ca), (float)(hin * sa));
+            ptab[D.ptab + (uint64_t)(p + l) * span + c] = make_float2((float)(hrev * ca), (float)(hrev * sa));
         }
         if (c == 0) {
-            const double bt = betas[(size_t)D.out * p + l];
-            mtab[(uint64_t)r * p + l] = make_float2((float)cos(bt), (float)sin(bt));
+            const double bt = betas[(size_t)D.out * p + l], cb = cos(bt), sb = sin(bt);
+            const bool fc = fabs(cb) >= fabs(sb);
+            const double f = fc ? cb : sb, k = fc ? sb / cb : cb / sb;
+            QMix M;
+            M.kf = (float)k;
+            M.kr = (float)-k;
+            M.f2 = (float)(f * f);
+            M.fn_f = (float)pow(f, n);
+            M.fn_r = (float)pow(fc ? cb : -sb, n);
+            M.f2_a0 = (float)pow(f * f, n - kQBTile);
+            M.form_c = fc ? 1u : 0u;
+            M.pad = 0;
+            mtab[(uint64_t)r * p + l] = M;
         }
     }
 }
 
-// Mixer rounds of a batched pass: a round applies exp(-i beta X) to the bits
-// of a 4-bit window [b0, b0 + 4) selected by `mask`, with the 16 amplitudes
-// j = base(tid) | (i << b0) of each thread in registers; pass A has windows
-// 0, 4, 8, pass B the windows at and above its first high bit L (top first).
-struct QBRounds {
-    uint32_t n;
-    uint32_t b0[3];
-    uint32_t mask[3];
-};
-__device__ __forceinline__ QBRounds qb_rounds(bool pass_b, uint32_t L) {
-    QBRounds R;
-    R.n = 0;
-    if (!pass_b) {
-        for (uint32_t w = 0; w < 3; ++w) {
-            R.b0[R.n] = 4 * w;
-            R.mask[R.n++] = 0xFu;
-        }
-    } else {
-        for (int w = 2; w >= 0; --w) {
-            const uint32_t b0 = 4u * (uint32_t)w;
-            if (b0 + 4 <= L) break;
-            uint32_t m = 0;
-            for (uint32_t b = 0; b < 4; ++b)
-                if (b0 + b >= L) m |= 1u << b;
-            R.b0[R.n] = b0;
-            R.mask[R.n++] = m;
-        }
-    }
-    return R;
+// Mixer windows of a batched pass: round k applies the mixer to the tile bits
+// [b0, b0 + 4) selected by a mask, with the 16 amplitudes j = base | (i << b0)
+// of each thread in registers. Pass A: b0 = 0, 4, 8 (all bits); pass B: b0 =
+// 8, 4, 0 (top first) while the window holds a bit at or above L, the bits
+// below L masked out. The round count is a template argument, so b0, the
+// shared-memory offsets of the 16 amplitudes and the global offsets of pass A
+// fold to constants.
+__host__ __device__ constexpr int qb_rounds_b(uint32_t L) { return L <= 3 ? 3 : (L <= 7 ? 2 : 1); }
+__device__ __forceinline__ uint32_t qb_mask(bool pass_b, uint32_t b0, uint32_t L) {
+    if (!pass_b || L <= b0) return 0xFu;
+    return L >= b0 + 4 ? 0u : (0xFu & ~((1u << (L - b0)) - 1u));
 }
 __device__ __forceinline__ uint32_t qb_base(uint32_t b0) {  // thread's group with the window bits cleared
     const uint32_t g = threadIdx.x;
     return (g & ((1u << b0) - 1)) | ((g >> b0) << (b0 + 4));
 }
-// exp(-i beta X) (c = cos, s = sin) on the window bits in `mask`; dual: the
-// same on l, with 2 Im<l|X_b|a> before each gate added to gsum
-template <bool DUAL>
-__device__ __forceinline__ void qb_mix(float2 (&a)[16], float2 (&l)[16], uint32_t mask, float c, float s, float &gsum) {
+// v, opaque to the compiler: the addresses derived from it are formed where
+// they are used instead of being hoisted out of the tile loop into registers
+__device__ __forceinline__ uint32_t qb_opaque(uint32_t v) {
+    uint32_t r;
+    asm volatile("mov.b32 %0, %1;" : "=r"(r) : "r"(v));
+    return r;
+}
+// the 16 amplitudes base | (i << b0), pb = qb_phys(base) (qb_phys is linear
+// over XOR and the two parts have no common bit), and back
+__device__ __forceinline__ void qb_read(const float2 *tile, uint32_t pb, uint32_t b0, float2 (&v)[16]) {
+    if (b0 == 0) {
+#pragma unroll
+        for (uint32_t i = 0; i < 16; i += 2) {
+            const float4 t = *reinterpret_cast<const float4 *>(tile + (pb ^ i));
+            v[i] = make_float2(t.x, t.y);
+            v[i + 1] = make_float2(t.z, t.w);
+        }
+    } else {
+#pragma unroll
+        for (uint32_t i = 0; i < 16; ++i) v[i] = tile[pb ^ qb_phys(i << b0)];
+    }
+}
+__device__ __forceinline__ void qb_write(float2 *tile, uint32_t pb, uint32_t b0, const float2 (&v)[16]) {
+    if (b0 == 0) {
+#pragma unroll
+        for (uint32_t i = 0; i < 16; i += 2)
+            *reinterpret_cast<float4 *>(tile + (pb ^ i)) = make_float4(v[i].x, v[i].y, v[i + 1].x, v[i + 1].y);
+    } else {
+#pragma unroll
+        for (uint32_t i = 0; i < 16; ++i) tile[pb ^ qb_phys(i << b0)] = v[i];
+    }
+}
+// one scaled gate on the pair (x, y): form C (x - i k y, y - i k x), form S
+// (k x - i y, k y - i x)
+template <bool FORM_C>
+__device__ __forceinline__ void qb_gate(float2 &x, float2 &y, float k) {
+    float2 a, b;
+    if (FORM_C) {
+        a = make_float2(fmaf(k, y.y, x.x), fmaf(-k, y.x, x.y));
+        b = make_float2(fmaf(k, x.y, y.x), fmaf(-k, x.x, y.y));
+    } else {
+        a = make_float2(fmaf(k, x.x, y.y), fmaf(k, x.y, -y.x));
+        b = make_float2(fmaf(k, y.x, x.y), fmaf(k, y.y, -x.x));
+    }
+    x = a;
+    y = b;
+}
+template <bool FORM_C>
+__device__ __forceinline__ void qb_mix(float2 (&a)[16], uint32_t mask, float k) {
+#pragma unroll
+    for (uint32_t b = 0; b < 4; ++b) {
+        if (!((mask >> b) & 1u)) continue;
+#pragma unroll
+        for (uint32_t i = 0; i < 16; ++i)
+            if (!(i & (1u << b))) qb_gate<FORM_C>(a[i], a[i | (1u << b)], k);
+    }
+}
+// sum over the window bits in mask of Im<l|X_b|a> on the thread's amplitudes
+// (taken before the window's gates: they commute with every X_b, so the sum is
+// the same at any point of the mixer)
+__device__ __forceinline__ float qb_grad(const float2 (&a)[16], const float2 (&l)[16], uint32_t mask) {
+    float g[2] = {0.f, 0.f}, h[2] = {0.f, 0.f};
 #pragma unroll
     for (uint32_t b = 0; b < 4; ++b) {
         if (!((mask >> b) & 1u)) continue;
@@ -448,17 +546,25 @@ __device__ __forceinline__ void qb_mix(float2 (&a)[16], float2 (&l)[16], uint32_
         for (uint32_t i = 0; i < 16; ++i) {
             if (i & (1u << b)) continue;
             const uint32_t j = i | (1u << b);
-            if (DUAL) gsum += (l[i].x * a[j].y - l[i].y * a[j].x) + (l[j].x * a[i].y - l[j].y * a[i].x);
-            const float2 x = a[i], y = a[j];
-            a[i] = make_float2(c * x.x + s * y.y, c * x.y - s * y.x);
-            a[j] = make_float2(c * y.x + s * x.y, c * y.y - s * x.x);
-            if (DUAL) {
-                const float2 u = l[i], v = l[j];
-                l[i] = make_float2(c * u.x + s * v.y, c * u.y - s * v.x);
-                l[j] = make_float2(c * v.x + s * u.y, c * v.y - s * u.x);
-            }
+            g[b & 1] = fmaf(l[i].x, a[j].y, g[b & 1]);
+            h[b & 1] = fmaf(l[i].y, a[j].x, h[b & 1]);
+            g[b & 1] = fmaf(l[j].x, a[i].y, g[b & 1]);
+            h[b & 1] = fmaf(l[j].y, a[i].x, h[b & 1]);
         }
     }
+    return (g[0] - h[0]) + (g[1] - h[1]);
+}
+// block sum of a per-thread float: warps in float, warps' totals in double;
+// valid in thread 0; red is free again on return
+__device__ __forceinline__ double qb_block_sum(float v, double *red) {
+    v = warp_sum(v);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = (double)v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (uint32_t w = 0; w < (blockDim.x >> 5); ++w) s += red[w];
+    __syncthreads();
+    return s;
 }
 __device__ __forceinline__ void qb_issue(bool dual, bool pass_b, bool with_cost, const QBArgs &a, const QDesc *desc,
                                          float2 *arena, const uint8_t *costs, uint64_t w, float2 *tp, float2 *tl,
@@ -472,20 +578,33 @@ __device__ __forceinline__ void qb_issue(bool dual, bool pass_b, bool with_cost,
     if (with_cost) qb_load_cost(tc, costs + D.cost, t);
     asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
+// the element offsets of the last round's amplitudes base | (i << b0) in the
+// state: pass A contiguous tiles, pass B through qb_index (a bit permutation,
+// so the offset of i is the sum of those of its bits)
+template <bool PASS_B>
+__device__ __forceinline__ void qb_offsets(const QBArgs &a, uint64_t t, uint32_t base, uint32_t b0, uint64_t &x0,
+                                           uint32_t (&off)[16]) {
+    x0 = qb_index(PASS_B, a.L, t, base);
+    uint32_t o[4];
+#pragma unroll
+    for (uint32_t b = 0; b < 4; ++b) o[b] = PASS_B ? (uint32_t)qb_index(true, a.L, 0, 1u << (b0 + b)) : (1u << (b0 + b));
+#pragma unroll
+    for (uint32_t i = 0; i < 16; ++i)
+        off[i] = ((i & 1u) ? o[0] : 0u) + ((i & 2u) ? o[1] : 0u) + ((i & 4u) ? o[2] : 0u) + ((i & 8u) ? o[3] : 0u);
+}
 
 // forward pass: [pass A: cost phase] + mixer; the last pass B of the last
 // layer also writes lambda = C psi and the per-tile energy
-template <bool PASS_B>
-__global__ void __launch_bounds__(kQThreads)
+template <bool PASS_B, int NR>
+__global__ void __launch_bounds__(kQThreads, 4)
     k_qaoa_fwd(const QBArgs a, const QDesc *__restrict__ desc, float2 *__restrict__ arena, const uint8_t *__restrict__ costs,
-               const float2 *__restrict__ ptab, const float2 *__restrict__ mtab, double *__restrict__ part) {
+               const float2 *__restrict__ ptab, const QMix *__restrict__ mtab, double *__restrict__ part) {
     extern __shared__ __align__(16) float2 qb_tile[];
     uint8_t *tc = reinterpret_cast<uint8_t *>(qb_tile + kQBT);
     __shared__ double red[32];
+    __shared__ float2 spt[kQMaxEdges + 1];  // the item's phase table
     const uint64_t items = (uint64_t)a.m * a.tiles;
     const bool last = PASS_B && a.layer + 1 == a.p;
-    const QBRounds R = qb_rounds(PASS_B, a.L);
-    const float amp0 = (float)(1.0 / sqrt((double)(1ULL << a.n)));
     uint64_t w = blockIdx.x;
     if (w < items) qb_issue(false, PASS_B, !PASS_B, a, desc, arena, costs, w, qb_tile, nullptr, tc);
     for (; w < items; w += gridDim.x) {
@@ -493,48 +612,62 @@ __global__ void __launch_bounds__(kQThreads)
         const uint64_t t = w % a.tiles;
         const uint32_t r = a.r0 + ci;
         const QDesc D = desc[r];
-        const float2 *ph = ptab + D.ptab + (uint64_t)a.layer * (kQMaxEdges + 1);
-        const float2 cs = mtab[(uint64_t)r * a.p + a.layer];
+        const QMix M = mtab[(uint64_t)r * a.p + a.layer];
+        if (!PASS_B) {  // the previous item's reads of spt ended before its last barrier
+            const float2 *ph = ptab + D.ptab + (uint64_t)a.layer * (kQMaxEdges + 1);
+            for (uint32_t c = threadIdx.x; c <= D.e_count; c += blockDim.x) spt[c] = ph[c];
+        }
         asm volatile("cp.async.wait_group 0;\n" ::: "memory");
         __syncthreads();
-        float2 v[16], dummy[16];
-        float gs = 0.f;
-        uint32_t base = 0;
-        for (uint32_t k = 0; k < R.n; ++k) {
-            base = qb_base(R.b0[k]);
-            if (!PASS_B && k == 0) {  // the cost layer (layer 0 starts from H on every qubit of |0>); window 0..3
-                if (a.layer > 0) qb_read(qb_tile, base, 0, v);
+        float2 v[16];
+        uint32_t base = 0, pb = 0, b0 = 0;
+#pragma unroll
+        for (int k = 0; k < NR; ++k) {
+            b0 = PASS_B ? 8u - 4u * (uint32_t)k : 4u * (uint32_t)k;
+            base = qb_opaque(qb_base(b0));
+            pb = qb_phys(base);
+            const uint32_t mask = qb_mask(PASS_B, b0, a.L);
+            if (!PASS_B && k == 0) {  // the cost phase on window 0..3 (layer 0: the table holds H|0> times the phase)
+                if (a.layer > 0) qb_read(qb_tile, pb, 0, v);
                 const uint4 cb = *reinterpret_cast<const uint4 *>(tc + base);
                 const uint32_t cw[4] = {cb.x, cb.y, cb.z, cb.w};
 #pragma unroll
-                for (uint32_t i = 0; i < 16; ++i)
-                    v[i] = cm(a.layer == 0 ? make_float2(amp0, 0.f) : v[i], ph[(cw[i >> 2] >> (8 * (i & 3))) & 0xFFu]);
+                for (uint32_t i = 0; i < 16; ++i) {
+                    const float2 f = spt[(cw[i >> 2] >> (8 * (i & 3))) & 0xFFu];
+                    v[i] = a.layer == 0 ? f : cm(v[i], f);
+                }
             } else {
-                qb_read(qb_tile, base, R.b0[k], v);
+                qb_read(qb_tile, pb, b0, v);
             }
-            qb_mix<false>(v, dummy, R.mask[k], cs.x, cs.y, gs);
-            if (k + 1 < R.n) {
-                qb_write(qb_tile, base, R.b0[k], v);
+            if (M.form_c) qb_mix<true>(v, mask, M.kf);
+            else qb_mix<false>(v, mask, M.kf);
+            if (k + 1 < NR) {
+                qb_write(qb_tile, pb, b0, v);
                 __syncthreads();
             }
         }
-        const uint32_t b0 = R.b0[R.n - 1];
         __syncthreads();  // every read of this tile is done: stream the next one in
         if (w + gridDim.x < items) qb_issue(false, PASS_B, !PASS_B, a, desc, arena, costs, w + gridDim.x, qb_tile, nullptr, tc);
-        float2 *psi = arena + D.psi;
-        float e = 0.f;
+        uint64_t x0;
+        uint32_t off[16];
+        qb_offsets<PASS_B>(a, t, base, b0, x0, off);
+        float2 *psi = arena + D.psi + x0;
+        if (!last) {
 #pragma unroll
-        for (uint32_t i = 0; i < 16; ++i) {
-            const uint64_t x = qb_index(PASS_B, a.L, t, base | (i << b0));
-            psi[x] = v[i];
-            if (last) {  // lambda = C psi and <C>
-                const float cv = (float)costs[D.cost + x];
-                arena[D.lam + x] = make_float2(cv * v[i].x, cv * v[i].y);
-                e += cv * (v[i].x * v[i].x + v[i].y * v[i].y);
+            for (uint32_t i = 0; i < 16; ++i) psi[off[i]] = v[i];
+        } else {  // psi with the layer's factor F^n back in, lambda = C psi and <C>
+            float2 *lam = arena + D.lam + x0;
+            const uint8_t *cst = costs + D.cost + x0;
+            float e = 0.f;
+#pragma unroll
+            for (uint32_t i = 0; i < 16; ++i) {
+                const float2 u = make_float2(v[i].x * M.fn_f, v[i].y * M.fn_f);
+                const float cv = (float)cst[off[i]];
+                psi[off[i]] = u;
+                lam[off[i]] = make_float2(cv * u.x, cv * u.y);
+                e = fmaf(cv, fmaf(u.x, u.x, u.y * u.y), e);
             }
-        }
-        if (last) {
-            const double et = block_sum((double)e, red);
+            const double et = qb_block_sum(e, red);
             if (threadIdx.x == 0) part[D.part + t] = et;
         }
     }
@@ -542,16 +675,16 @@ __global__ void __launch_bounds__(kQThreads)
 
 // reverse pass: the inverse mixer on psi and lambda with the dE/dbeta terms;
 // pass A then the cost layer's dE/dgamma term and the inverse phase
-template <bool PASS_B>
-__global__ void __launch_bounds__(kQThreads)
+template <bool PASS_B, int NR>
+__global__ void __launch_bounds__(kQThreads, 2)
     k_qaoa_rev(const QBArgs a, const QDesc *__restrict__ desc, float2 *__restrict__ arena, const uint8_t *__restrict__ costs,
-               const float2 *__restrict__ ptab, const float2 *__restrict__ mtab, double *__restrict__ part) {
+               const float2 *__restrict__ ptab, const QMix *__restrict__ mtab, double *__restrict__ part) {
     extern __shared__ __align__(16) float2 qb_tile[];
     float2 *tp = qb_tile, *tl = qb_tile + kQBT;
     uint8_t *tc = reinterpret_cast<uint8_t *>(qb_tile + 2 * kQBT);
     __shared__ double red[32];
+    __shared__ float2 spt[kQMaxEdges + 1];  // the item's inverse phase table
     const uint64_t items = (uint64_t)a.m * a.tiles;
-    const QBRounds R = qb_rounds(PASS_B, a.L);
     uint64_t w = blockIdx.x;
     if (w < items) qb_issue(true, PASS_B, !PASS_B, a, desc, arena, costs, w, tp, tl, tc);
     for (; w < items; w += gridDim.x) {
@@ -559,51 +692,71 @@ __global__ void __launch_bounds__(kQThreads)
         const uint64_t t = w % a.tiles;
         const uint32_t r = a.r0 + ci;
         const QDesc D = desc[r];
-        const float2 *ph = ptab + D.ptab + (uint64_t)a.layer * (kQMaxEdges + 1);
-        const float2 cs = mtab[(uint64_t)r * a.p + a.layer];
+        const QMix M = mtab[(uint64_t)r * a.p + a.layer];
+        if (!PASS_B) {  // the previous item's reads of spt ended before its block sums' barriers
+            const float2 *ph = ptab + D.ptab + (uint64_t)(a.p + a.layer) * (kQMaxEdges + 1);
+            for (uint32_t c = threadIdx.x; c <= D.e_count; c += blockDim.x) spt[c] = ph[c];
+        }
         asm volatile("cp.async.wait_group 0;\n" ::: "memory");
         __syncthreads();
         float2 v[16], l[16];
-        uint8_t cv[16];
+        uint32_t cw[4] = {0u, 0u, 0u, 0u};  // the last round's cost bytes, four per word
         float gb = 0.f;
-        uint32_t base = 0;
-        for (uint32_t k = 0; k < R.n; ++k) {
-            base = qb_base(R.b0[k]);
-            qb_read(tp, base, R.b0[k], v);
-            qb_read(tl, base, R.b0[k], l);
-            if (!PASS_B && k + 1 == R.n)
+        float sc = PASS_B ? 1.f : M.f2_a0;  // F'^(2m) after the m gates of this layer undone so far
+        uint32_t base = 0, pb = 0, b0 = 0;
 #pragma unroll
-                for (uint32_t i = 0; i < 16; ++i) cv[i] = tc[base | (i << R.b0[k])];
-            qb_mix<true>(v, l, R.mask[k], cs.x, -cs.y, gb);  // the inverse mixer, gradient before each gate
-            if (k + 1 < R.n) {
-                qb_write(tp, base, R.b0[k], v);
-                qb_write(tl, base, R.b0[k], l);
+        for (int k = 0; k < NR; ++k) {
+            b0 = PASS_B ? 8u - 4u * (uint32_t)k : 4u * (uint32_t)k;
+            base = qb_opaque(qb_base(b0));
+            pb = qb_phys(base);
+            const uint32_t mask = qb_mask(PASS_B, b0, a.L);
+            qb_read(tp, pb, b0, v);
+            qb_read(tl, pb, b0, l);
+            if (!PASS_B && k + 1 == NR)
+#pragma unroll
+                for (uint32_t i = 0; i < 16; ++i) cw[i >> 2] |= (uint32_t)tc[base | (i << b0)] << (8 * (i & 3));
+            gb = fmaf(qb_grad(v, l, mask), sc, gb);
+#pragma unroll
+            for (uint32_t b = 0; b < 4; ++b)
+                if ((mask >> b) & 1u) sc *= M.f2;
+            if (M.form_c) {
+                qb_mix<true>(v, mask, M.kr);
+                qb_mix<true>(l, mask, M.kr);
+            } else {
+                qb_mix<false>(v, mask, M.kr);
+                qb_mix<false>(l, mask, M.kr);
+            }
+            if (k + 1 < NR) {
+                qb_write(tp, pb, b0, v);
+                qb_write(tl, pb, b0, l);
                 __syncthreads();
             }
         }
-        const uint32_t b0 = R.b0[R.n - 1];
         __syncthreads();  // every read of this tile is done: stream the next one in
         if (w + gridDim.x < items) qb_issue(true, PASS_B, !PASS_B, a, desc, arena, costs, w + gridDim.x, tp, tl, tc);
-        float2 *psi = arena + D.psi, *lam = arena + D.lam;
+        uint64_t x0;
+        uint32_t off[16];
+        qb_offsets<PASS_B>(a, t, base, b0, x0, off);
+        float2 *psi = arena + D.psi + x0, *lam = arena + D.lam + x0;
         const float W = (float)D.e_count;
         float gg = 0.f;
 #pragma unroll
         for (uint32_t i = 0; i < 16; ++i) {
-            const uint64_t x = qb_index(PASS_B, a.L, t, base | (i << b0));
             float2 pv = v[i], lv = l[i];
-            if (!PASS_B) {  // the cost layer: its gradient term, then undo its phase
-                const float2 f = ph[cv[i]];
-                gg += (W - 2.f * (float)cv[i]) * (lv.x * pv.y - lv.y * pv.x);
+            if (!PASS_B) {  // the cost layer: its gradient term, then undo its phase (the table holds F'^n)
+                const uint32_t cv = (cw[i >> 2] >> (8 * (i & 3))) & 0xFFu;
+                const float2 f = spt[cv];
+                gg = fmaf(W - 2.f * (float)cv, lv.x * pv.y - lv.y * pv.x, gg);
                 pv = cmc(pv, f);
                 lv = cmc(lv, f);
             }
-            psi[x] = pv;
-            lam[x] = lv;
+            psi[off[i]] = pv;
+            lam[off[i]] = lv;
         }
-        const double gbt = block_sum((double)gb, red);
+        const double gbt = qb_block_sum(gb, red);
         if (threadIdx.x == 0) part[D.part + (uint64_t)(1 + (PASS_B ? a.p : 0) + a.layer) * a.tiles + t] = gbt;
         if (!PASS_B) {
-            const double ggt = block_sum((double)gg, red);
+            const double ggt = qb_block_sum(gg, red) * (double)M.fn_r * (double)M.fn_r;
             if (threadIdx.x == 0) part[D.part + (uint64_t)(1 + 2 * a.p + a.layer) * a.tiles + t] = ggt;
         }
     }
@@ -699,7 +852,7 @@ extern "C" int qf_qaoa_maxcut_batch(qf_ctx *ctx, const qf_qaoa_instance *inst, u
             r_small = (uint32_t)r + 1;
             D.k = kQBTile;
             D.ptab = ptab_off;
-            ptab_off += (uint64_t)p * (kQMaxEdges + 1);
+            ptab_off += 2ULL * p * (kQMaxEdges + 1);  // forward and reverse tables
             D.part = part_off;
             part_off += (uint64_t)(1 + 3 * p) << (D.n - kQBTile);
         } else {
@@ -726,7 +879,7 @@ extern "C" int qf_qaoa_maxcut_batch(qf_ctx *ctx, const qf_qaoa_instance *inst, u
     const size_t b_desc = al(sizeof(QDesc) * n_inst), b_mask = al(8 * std::max<uint64_t>(1, n_edges));
     const size_t b_par = al(8 * n_inst * p), b_cost = al(8 * n_inst), b_grad = al(16 * n_inst * p), b_cnt = 256;
     const size_t b_arena = al(8 * amp_off), b_costs = al(cost_off);
-    const size_t b_ptab = al(8 * std::max<uint64_t>(1, ptab_off)), b_mtab = al(8 * std::max<uint64_t>(1, (uint64_t)r_small * p));
+    const size_t b_ptab = al(8 * std::max<uint64_t>(1, ptab_off)), b_mtab = al(sizeof(QMix) * std::max<uint64_t>(1, (uint64_t)r_small * p));
     const size_t b_part = al(8 * std::max<uint64_t>(1, part_off));
     const size_t total = b_desc + b_mask + 2 * b_par + b_cost + b_grad + b_cnt + b_arena + b_costs + b_ptab + b_mtab + b_part;
     QF_TRY(ensure_device(&ctx->ws_tree, &ctx->ws_tree_bytes, total));
@@ -742,7 +895,7 @@ extern "C" int qf_qaoa_maxcut_batch(qf_ctx *ctx, const qf_qaoa_instance *inst, u
     uint8_t *d_costs = reinterpret_cast<uint8_t *>(w + b_desc + b_mask + 2 * b_par + b_cost + b_grad + b_cnt + b_arena);
     unsigned char *w2 = w + b_desc + b_mask + 2 * b_par + b_cost + b_grad + b_cnt + b_arena + b_costs;
     float2 *d_ptab = reinterpret_cast<float2 *>(w2);
-    float2 *d_mtab = reinterpret_cast<float2 *>(w2 + b_ptab);
+    QMix *d_mtab = reinterpret_cast<QMix *>(w2 + b_ptab);
     double *d_part = reinterpret_cast<double *>(w2 + b_ptab + b_mtab);
     cudaStream_t st = ctx->stream;
     QF_CUDA(cudaMemcpyAsync(d_desc, desc.data(), sizeof(QDesc) * n_inst, cudaMemcpyHostToDevice, st));
@@ -750,24 +903,30 @@ extern "C" int qf_qaoa_maxcut_batch(qf_ctx *ctx, const qf_qaoa_instance *inst, u
     QF_CUDA(cudaMemcpyAsync(d_gam, gammas, 8 * n_inst * p, cudaMemcpyHostToDevice, st));
     QF_CUDA(cudaMemcpyAsync(d_bet, betas, 8 * n_inst * p, cudaMemcpyHostToDevice, st));
     static bool attr[64] = {false};
+    static int pass_occ[64][8];
     const size_t smem = sizeof(QShared);
     const size_t smem_f = sizeof(float2) * kQBT + kQBT, smem_r = 2 * sizeof(float2) * kQBT + kQBT;  // tiles + cost bytes
-    if (!attr[ctx->device & 63]) {
+    // passes: forward A, forward B with 1..3 rounds, reverse A, reverse B with 1..3 rounds
+    using QPass = void (*)(QBArgs, const QDesc *, float2 *, const uint8_t *, const float2 *, const QMix *, double *);
+    const QPass passes[8] = {k_qaoa_fwd<false, 3>, k_qaoa_fwd<true, 1>, k_qaoa_fwd<true, 2>, k_qaoa_fwd<true, 3>,
+                             k_qaoa_rev<false, 3>, k_qaoa_rev<true, 1>, k_qaoa_rev<true, 2>, k_qaoa_rev<true, 3>};
+    const int dev = ctx->device & 63;
+    if (!attr[dev]) {
         QF_CUDA(cudaFuncSetAttribute(k_qaoa_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        QF_CUDA(cudaFuncSetAttribute(k_qaoa_rev<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r));
-        QF_CUDA(cudaFuncSetAttribute(k_qaoa_rev<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_r));
-        QF_CUDA(cudaFuncSetAttribute(k_qaoa_fwd<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_f));
-        QF_CUDA(cudaFuncSetAttribute(k_qaoa_fwd<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_f));
-        attr[ctx->device & 63] = true;
+        for (int i = 0; i < 8; ++i) {
+            const size_t sm_i = i < 4 ? smem_f : smem_r;
+            QF_CUDA(cudaFuncSetAttribute(passes[i], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_i));
+            QF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pass_occ[dev][i], passes[i], kQThreads, sm_i));
+        }
+        attr[dev] = true;
     }
     const uint32_t n_small = (uint32_t)n_inst - r_small;
     int per_sm = 0;
     QF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_qaoa_batch, kQThreads, smem));
     const uint32_t grid = (uint32_t)std::min<uint64_t>(std::max(1u, n_small), (uint64_t)std::max(1, per_sm) * ctx->sm_count);
-    int occ_f = 0, occ_r = 0;
-    QF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, k_qaoa_fwd<false>, kQThreads, smem_f));
-    QF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_r, k_qaoa_rev<false>, kQThreads, smem_r));
-    const uint64_t cap_f = (uint64_t)std::max(1, occ_f) * ctx->sm_count, cap_r = (uint64_t)std::max(1, occ_r) * ctx->sm_count;
+    auto pass_grid = [&](int i, uint64_t items) {
+        return (unsigned)std::min<uint64_t>(items, (uint64_t)std::max(1, pass_occ[dev][i]) * ctx->sm_count);
+    };
     auto enqueue = [&](cudaStream_t s) -> int {
         if (r_small) {
             k_qaoa_tables<<<(unsigned)std::min<uint64_t>(4096, ((uint64_t)r_small * p * (kQMaxEdges + 1) + 255) / 256), 256, 0, s>>>(
@@ -785,18 +944,20 @@ extern "C" int qf_qaoa_maxcut_batch(qf_ctx *ctx, const qf_qaoa_instance *inst, u
             A.p = p;
             A.tiles = 1ULL << (A.n - kQBTile);
             const uint64_t items = (uint64_t)A.m * A.tiles;
-            const unsigned gf = (unsigned)std::min(items, cap_f), gr = (unsigned)std::min(items, cap_r);
+            const int rb = qb_rounds_b(A.L);  // pass B rounds: 3, 2 or 1
+            const unsigned gfa = pass_grid(0, items), gfb = pass_grid(rb, items);
+            const unsigned gra = pass_grid(4, items), grb = pass_grid(4 + rb, items);
             A.layer = 0;
-            k_qaoa_costs<<<gf, kQThreads, 0, s>>>(A, d_desc, d_mask, d_costs);
+            k_qaoa_costs<<<gfa, kQThreads, 0, s>>>(A, d_desc, d_mask, d_costs);
             for (uint32_t l = 0; l < p; ++l) {
                 A.layer = l;
-                k_qaoa_fwd<false><<<gf, kQThreads, smem_f, s>>>(A, d_desc, d_arena, d_costs, d_ptab, d_mtab, d_part);
-                k_qaoa_fwd<true><<<gf, kQThreads, smem_f, s>>>(A, d_desc, d_arena, d_costs, d_ptab, d_mtab, d_part);
+                passes[0]<<<gfa, kQThreads, smem_f, s>>>(A, d_desc, d_arena, d_costs, d_ptab, d_mtab, d_part);
+                passes[rb]<<<gfb, kQThreads, smem_f, s>>>(A, d_desc, d_arena, d_costs, d_ptab, d_mtab, d_part);
             }
             for (uint32_t l = p; l-- > 0;) {
                 A.layer = l;
-                k_qaoa_rev<true><<<gr, kQThreads, smem_r, s>>>(A, d_desc, d_arena, d_costs, d_ptab, d_mtab, d_part);
-                k_qaoa_rev<false><<<gr, kQThreads, smem_r, s>>>(A, d_desc, d_arena, d_costs, d_ptab, d_mtab, d_part);
+                passes[4 + rb]<<<grb, kQThreads, smem_r, s>>>(A, d_desc, d_arena, d_costs, d_ptab, d_mtab, d_part);
+                passes[4]<<<gra, kQThreads, smem_r, s>>>(A, d_desc, d_arena, d_costs, d_ptab, d_mtab, d_part);
             }
             k_qaoa_reduce<<<(unsigned)std::max<uint64_t>(1, ((uint64_t)A.m * (1 + 2 * p) + 127) / 128), 128, 0, s>>>(
                 A, d_desc, d_part, d_cost, d_grad);

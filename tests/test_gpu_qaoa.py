@@ -143,3 +143,24 @@ def test_one_cta_per_large_instance_matches_oracle(backend, k):
         e_ref, g_ref = oracle_cost_grad(n, edges, gam[i], bet[i])
         assert abs(cost[i] - e_ref) < 1e-5 * max(1.0, abs(e_ref)), (i, n, cost[i], e_ref)
         assert np.abs(grad[i] - g_ref).max() < 1e-4 * max(1.0, np.abs(g_ref).max()), (i, n, grad[i], g_ref)
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_dense_graphs_in_batched_passes_match_oracle(backend, graph):
+    """Cut tables of graphs with many edges among the low qubits (edges inside
+    qubits 0..3, from them to higher qubits and above them): the complete graph
+    on 14 qubits (91 edges), a clique on qubits 0..7 with a path to qubit 12,
+    a star from qubit 0 over 16 qubits with a ring."""
+    k14 = [(u, v, 1.0) for u in range(14) for v in range(u + 1, 14)]
+    clique = [(u, v, 1.0) for u in range(8) for v in range(u + 1, 8)] + [(q, q + 1, 1.0) for q in range(7, 12)]
+    star = [(0, v, 1.0) for v in range(1, 16)] + [(q, q + 1, 1.0) for q in range(1, 15)]
+    problems = [(14, k14), (13, clique), (16, star), (13, clique)]
+    rng = np.random.default_rng(31)
+    p = 2
+    gam = rng.uniform(0, np.pi, (len(problems), p))
+    bet = rng.uniform(0, np.pi / 2, (len(problems), p))
+    cost, grad = QaoaBatch(problems, p, backend=backend, use_graph=graph).run(gam, bet)
+    for i, (n, edges) in enumerate(problems):
+        e_ref, g_ref = oracle_cost_grad(n, edges, gam[i], bet[i])
+        assert abs(cost[i] - e_ref) < 1e-5 * max(1.0, abs(e_ref)), (i, n, cost[i], e_ref)
+        assert np.abs(grad[i] - g_ref).max() < 1e-4 * max(1.0, np.abs(g_ref).max()), (i, n, grad[i], g_ref)
