@@ -767,7 +767,7 @@ def density14(backend, cpu: bool, n: int = 14):
            "channel_kernel": {"kernel": "k_dm_channel<double2>", "avg_launch_ms": 1000 * t_ch,
                               "bytes_per_launch": bytes_ch, "achieved_gbs": bytes_ch / t_ch / 1e9,
                               "frac": bytes_ch / t_ch / 1e9 / peak, "peak": peak, "peak_kind": f"of {peak_kind}"},
-           "fused_channel_passes": {"kernel": "k_dm_channel_tile", **fused},
+           "fused_channel_passes": {"kernel": "k_dm_channel_pairs (complex64, two channels per shared-memory round)", **fused},
            "trace_re": tr.real, "purity": rho.purity(),
            "c64_run_density_s": t64, "c64_ops_per_s": len(ops) / t64}
     if d64 is not None:

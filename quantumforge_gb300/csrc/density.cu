@@ -150,6 +150,14 @@ struct ChannelTile {
     uint8_t lc[kMaxTileChannels], lr[kMaxTileChannels], shape[kMaxTileChannels];
     double coef[kMaxTileChannels][6];
     float coef_f[kMaxTileChannels][6];  // the same in f32: no f64 -> f32 conversion per tile for complex64
+    // complex64 paired rounds (k = 12): per round its channels (0xFF: none),
+    // the tile bits of the thread's eight index bits, the swizzled offsets of
+    // its 16 entries and whether entries i, i + 1 share a 16-byte slot
+    uint8_t rch[kMaxTileChannels / 2][2];
+    uint8_t rpos[kMaxTileChannels / 2][8];
+    uint16_t roff[kMaxTileChannels / 2][16];
+    uint8_t rwide[kMaxTileChannels / 2];
+    uint32_t n_rounds;
 };
 
 template <typename C>
@@ -214,6 +222,118 @@ __global__ void __launch_bounds__(256) k_dm_channel_tile(C *__restrict__ v, uint
         } else {
             for (uint32_t j = threadIdx.x; j < T; j += blockDim.x) v[base | hi_off[j >> 5] | (j & 31u)] = s[j];
         }
+        __syncthreads();
+    }
+}
+
+// Complex64 tiles of 12 bits, channels applied two per shared-memory round
+// trip: in a round each thread holds the 16 entries base | (i over the bits
+// lc, lr of its first channel and lc, lr of its second) in registers (a lone
+// channel takes two other tile bits as bits 2, 3 of i). Tiles stream in by
+// 16-byte cp.async into one of two buffers while the other is worked on (the
+// next tile's copies are issued before the current tile's rounds). In shared
+// memory entry j sits at dm_swz(j): bits 1..3 XOR bits 4..6, 7..9 and 10..11,
+// bit 0 kept (a copied 16-byte pair stays whole). The host puts the lane bits
+// of a round on tile bits whose bank-pair vectors dm_swz(1 << b) & 15 are
+// independent (16 distinct bank pairs per half warp); a round holding tile bit
+// 0 reads and writes its pairs as 16-byte words.
+__host__ __device__ inline uint32_t dm_swz(uint32_t j) { return j ^ ((((j >> 4) ^ (j >> 7) ^ (j >> 10)) & 7u) << 1); }
+template <bool GENERAL>
+__device__ __forceinline__ void dm_quad(float2 &x00, float2 &x01, float2 &x10, float2 &x11, const float *k) {
+    if (GENERAL) {
+        const float2 p = x00, q = x11;
+        x00 = make_float2(k[0] * p.x + k[1] * q.x, k[0] * p.y + k[1] * q.y);
+        x11 = make_float2(k[2] * p.x + k[3] * q.x, k[2] * p.y + k[3] * q.y);
+    }
+    x01 = make_float2(k[4] * x01.x, k[4] * x01.y);
+    x10 = make_float2(k[5] * x10.x, k[5] * x10.y);
+}
+// channel on bits (sel, sel << 1) of the 16-entry index: sel = 1 for bits 0, 1
+// (quads over bits 2, 3), sel = 4 for bits 2, 3
+template <uint32_t SEL>
+__device__ __forceinline__ void dm_apply(float2 (&e)[16], int shape, const float *k) {
+    constexpr uint32_t O = SEL == 1 ? 4u : 1u;  // step between the four quads
+#pragma unroll
+    for (uint32_t q = 0; q < 4; ++q) {
+        const uint32_t b = q * O;
+        if (shape == 2) dm_quad<false>(e[b], e[b | SEL], e[b | (SEL << 1)], e[b | (SEL * 3)], k);
+        else dm_quad<true>(e[b], e[b | SEL], e[b | (SEL << 1)], e[b | (SEL * 3)], k);
+    }
+}
+__device__ __forceinline__ void dm_cp16(float2 *dst, const float2 *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__global__ void __launch_bounds__(256, 3) k_dm_channel_pairs(float2 *__restrict__ v, uint64_t n_tiles, const ChannelTile ct) {
+    extern __shared__ __align__(16) unsigned char dm_smem[];
+    float2 *buf = reinterpret_cast<float2 *>(dm_smem);  // two tiles of 4096 entries
+    uint64_t *hi_off = reinterpret_cast<uint64_t *>(dm_smem + 2 * (sizeof(float2) << 12));
+    uint64_t *dep = hi_off + 128;  // the tile index's bits on outer_mask, per byte of the index
+    for (uint32_t h = threadIdx.x; h < 128u; h += blockDim.x) {
+        uint64_t off = 0;
+        for (uint32_t r = 0; r < ct.n_hi; ++r)
+            if ((h >> r) & 1u) off |= ct.hi_bits[r];
+        hi_off[h] = off;
+    }
+    for (uint32_t h = threadIdx.x; h < 3u * 256u; h += blockDim.x)
+        dep[h] = deposit((uint64_t)(h & 255u) << (8 * (h >> 8)), ct.outer_mask);
+    __syncthreads();
+    // copy k of a thread holds the entries j, j + 1 for j = 2 (tid + 256 k)
+    const uint32_t tid = threadIdx.x, j0 = tid << 1, slot0 = dm_swz(j0);
+    auto tile_base = [&](uint64_t t) { return dep[t & 255u] | dep[256u + ((t >> 8) & 255u)] | dep[512u + ((t >> 16) & 255u)]; };
+    auto issue = [&](uint64_t t, float2 *dst) {
+        const float2 *src = v + (tile_base(t) | (j0 & 31u));
+#pragma unroll
+        for (uint32_t k = 0; k < 8; ++k) dm_cp16(dst + (slot0 ^ dm_swz(512u * k)), src + hi_off[(tid >> 4) + 16 * k]);
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+    uint64_t t = blockIdx.x;
+    uint32_t cur = 0;
+    if (t < n_tiles) issue(t, buf);
+    for (; t < n_tiles; t += gridDim.x, cur ^= 1u) {
+        float2 *s = buf + (cur << 12);
+        if (t + gridDim.x < n_tiles) {  // the other buffer's last reads ended before the previous tile's final barrier
+            issue(t + gridDim.x, buf + ((cur ^ 1u) << 12));
+            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        }
+        __syncthreads();
+        for (uint32_t r = 0; r < ct.n_rounds; ++r) {
+            const uint32_t c1 = ct.rch[r][0], c2 = ct.rch[r][1];
+            uint32_t g = 0;
+#pragma unroll
+            for (uint32_t b = 0; b < 8; ++b) g |= ((tid >> b) & 1u) << ct.rpos[r][b];
+            const uint32_t pb = dm_swz(g);
+            float2 e[16];
+            if (ct.rwide[r]) {
+#pragma unroll
+                for (uint32_t i = 0; i < 16; i += 2) {
+                    const float4 x = *reinterpret_cast<const float4 *>(s + (pb ^ ct.roff[r][i]));
+                    e[i] = make_float2(x.x, x.y);
+                    e[i + 1] = make_float2(x.z, x.w);
+                }
+            } else {
+#pragma unroll
+                for (uint32_t i = 0; i < 16; ++i) e[i] = s[pb ^ ct.roff[r][i]];
+            }
+            dm_apply<1>(e, ct.shape[c1], ct.coef_f[c1]);
+            if (c2 < ct.n_ch) dm_apply<4>(e, ct.shape[c2], ct.coef_f[c2]);
+            if (ct.rwide[r]) {
+#pragma unroll
+                for (uint32_t i = 0; i < 16; i += 2)
+                    *reinterpret_cast<float4 *>(s + (pb ^ ct.roff[r][i])) = make_float4(e[i].x, e[i].y, e[i + 1].x, e[i + 1].y);
+            } else {
+#pragma unroll
+                for (uint32_t i = 0; i < 16; ++i) s[pb ^ ct.roff[r][i]] = e[i];
+            }
+            __syncthreads();
+        }
+        float2 *dst = v + (tile_base(t) | (j0 & 31u));
+#pragma unroll
+        for (uint32_t k = 0; k < 8; ++k)
+            *reinterpret_cast<float4 *>(dst + hi_off[(tid >> 4) + 16 * k]) =
+                *reinterpret_cast<const float4 *>(s + (slot0 ^ dm_swz(512u * k)));
         __syncthreads();
     }
 }
@@ -283,7 +403,66 @@ int dm_channels_fused(qf_sv *sv, uint32_t n, const uint32_t *qs, const double (*
         }
     }
     const uint64_t n_tiles = 1ULL << (2 * n - ct.k);
-    const size_t smem = (sv->dtype == QF_C64 ? 8u : 16u) * (size_t(1) << ct.k) + sizeof(uint64_t) * (size_t(1) << ct.n_hi);
+    const bool pairs = sv->dtype == QF_C64 && ct.k == 12 && 2 * n - ct.k <= 24;
+    if (pairs) {
+        // channels in pairs (they act on disjoint bits and commute); a channel
+        // whose column bit is tile bit 0 goes first in its round, so the
+        // round's entries i, i + 1 are 16-byte neighbours
+        std::vector<uint32_t> order;
+        for (uint32_t c = 0; c < count; ++c)
+            if (ct.lc[c] == 0) order.push_back(c);
+        for (uint32_t c = 0; c < count; ++c)
+            if (ct.lc[c] != 0) order.push_back(c);
+        ct.n_rounds = (count + 1) / 2;
+        for (uint32_t r = 0; r < ct.n_rounds; ++r) {
+            const uint32_t c1 = order[2 * r], c2 = 2 * r + 1 < count ? order[2 * r + 1] : 0xFFu;
+            ct.rch[r][0] = (uint8_t)c1;
+            ct.rch[r][1] = (uint8_t)c2;
+            uint32_t P[4] = {ct.lc[c1], ct.lr[c1], 0, 0};
+            if (c2 != 0xFFu) {
+                P[2] = ct.lc[c2];
+                P[3] = ct.lr[c2];
+            } else {  // two filler bits, not tile bit 0 (it stays a lane bit)
+                uint32_t f = 0;
+                for (uint32_t b = 1; b < 12 && f < 2; ++b)
+                    if (b != P[0] && b != P[1]) P[2 + f++] = b;
+            }
+            ct.rwide[r] = P[0] == 0 ? 1 : 0;
+            // lane bits: free tile bits, taken in ascending order when their
+            // bank-pair vector is independent of those taken (GF(2) basis by
+            // leading bit), until four; then the rest in ascending order
+            uint32_t taken = (1u << P[0]) | (1u << P[1]) | (1u << P[2]) | (1u << P[3]), nb = 0;
+            uint32_t basis[4] = {0, 0, 0, 0};
+            for (uint32_t b = 0; b < 12 && nb < 4; ++b) {
+                if ((taken >> b) & 1u) continue;
+                uint32_t x = dm_swz(1u << b) & 15u;
+                for (int h = 3; h >= 0 && x; --h)
+                    if ((x >> h) & 1u) {
+                        if (!basis[h]) break;
+                        x ^= basis[h];
+                    }
+                if (!x) continue;
+                int h = 3;
+                while (!((x >> h) & 1u)) --h;
+                basis[h] = x;
+                ct.rpos[r][nb++] = (uint8_t)b;
+                taken |= 1u << b;
+            }
+            for (uint32_t b = 0; b < 12; ++b)
+                if (!((taken >> b) & 1u)) {
+                    ct.rpos[r][nb++] = (uint8_t)b;
+                    taken |= 1u << b;
+                }
+            for (uint32_t i = 0; i < 16; ++i) {
+                uint32_t off = 0;
+                for (uint32_t b = 0; b < 4; ++b)
+                    if ((i >> b) & 1u) off |= 1u << P[b];
+                ct.roff[r][i] = (uint16_t)dm_swz(off);
+            }
+        }
+    }
+    const size_t smem = pairs ? 2 * sizeof(float2) * 4096 + sizeof(uint64_t) * (128 + 3 * 256)
+                              : (sv->dtype == QF_C64 ? 8u : 16u) * (size_t(1) << ct.k) + sizeof(uint64_t) * (size_t(1) << ct.n_hi);
     // one wave of resident CTAs (a grid past the resident count leaves a tail
     // wave running on part of the GPU)
     auto grid_of = [&](const void *k, int *grid) -> int {
@@ -293,7 +472,11 @@ int dm_channels_fused(qf_sv *sv, uint32_t n, const uint32_t *qs, const double (*
         return QF_OK;
     };
     int grid;
-    if (sv->dtype == QF_C64) {
+    if (pairs) {
+        QF_CUDA(cudaFuncSetAttribute(k_dm_channel_pairs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        QF_TRY(grid_of((const void *)k_dm_channel_pairs, &grid));
+        k_dm_channel_pairs<<<grid, 256, smem, ctx->stream>>>(static_cast<float2 *>(sv->d), n_tiles, ct);
+    } else if (sv->dtype == QF_C64) {
         QF_CUDA(cudaFuncSetAttribute(k_dm_channel_tile<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         QF_TRY(grid_of((const void *)k_dm_channel_tile<float2>, &grid));
         k_dm_channel_tile<float2><<<grid, 256, smem, ctx->stream>>>(static_cast<float2 *>(sv->d), n_tiles, ct);

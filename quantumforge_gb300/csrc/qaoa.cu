@@ -566,6 +566,23 @@ __device__ __forceinline__ double qb_block_sum(float v, double *red) {
     __syncthreads();
     return s;
 }
+// the same for two values at once (one pair of barriers)
+__device__ __forceinline__ void qb_block_sum2(float v, float u, double *red, double &sv, double &su) {
+    v = warp_sum(v);
+    u = warp_sum(u);
+    if ((threadIdx.x & 31) == 0) {
+        red[threadIdx.x >> 5] = (double)v;
+        red[16 + (threadIdx.x >> 5)] = (double)u;
+    }
+    __syncthreads();
+    sv = su = 0.0;
+    if (threadIdx.x == 0)
+        for (uint32_t w = 0; w < (blockDim.x >> 5); ++w) {
+            sv += red[w];
+            su += red[16 + w];
+        }
+    __syncthreads();
+}
 __device__ __forceinline__ void qb_issue(bool dual, bool pass_b, bool with_cost, const QBArgs &a, const QDesc *desc,
                                          float2 *arena, const uint8_t *costs, uint64_t w, float2 *tp, float2 *tl,
                                          uint8_t *tc) {
@@ -753,11 +770,16 @@ __global__ void __launch_bounds__(kQThreads, 2)
             psi[off[i]] = pv;
             lam[off[i]] = lv;
         }
-        const double gbt = qb_block_sum(gb, red);
-        if (threadIdx.x == 0) part[D.part + (uint64_t)(1 + (PASS_B ? a.p : 0) + a.layer) * a.tiles + t] = gbt;
-        if (!PASS_B) {
-            const double ggt = qb_block_sum(gg, red) * (double)M.fn_r * (double)M.fn_r;
-            if (threadIdx.x == 0) part[D.part + (uint64_t)(1 + 2 * a.p + a.layer) * a.tiles + t] = ggt;
+        if (PASS_B) {
+            const double gbt = qb_block_sum(gb, red);
+            if (threadIdx.x == 0) part[D.part + (uint64_t)(1 + a.p + a.layer) * a.tiles + t] = gbt;
+        } else {
+            double gbt, ggt;
+            qb_block_sum2(gb, gg, red, gbt, ggt);
+            if (threadIdx.x == 0) {
+                part[D.part + (uint64_t)(1 + a.layer) * a.tiles + t] = gbt;
+                part[D.part + (uint64_t)(1 + 2 * a.p + a.layer) * a.tiles + t] = ggt * (double)M.fn_r * (double)M.fn_r;
+            }
         }
     }
 }
