@@ -348,6 +348,7 @@ struct QBArgs {
     uint32_t n, L;   // qubits; low bits of a pass-B tile (24 - n)
     uint32_t p, layer;
     uint64_t tiles;  // tiles per instance: 2^(n-12)
+    uint64_t chunk;  // items (instance, tile) per CTA, consecutive: CTA b takes [b chunk, (b + 1) chunk)
 };
 
 // part slots per tile: 0 energy, 1+l dE/dbeta (pass A), 1+p+l dE/dbeta
@@ -389,8 +390,8 @@ __global__ void __launch_bounds__(kQThreads)
     __shared__ uint32_t em[kQMaxEdges];
     const uint64_t items = (uint64_t)a.m * a.tiles;
     for (uint64_t w = blockIdx.x; w < items; w += gridDim.x) {
-        const uint32_t ci = (uint32_t)(w / a.tiles);
-        const uint64_t t = w % a.tiles;
+        const uint32_t ci = (uint32_t)(w >> (a.n - kQBTile));
+        const uint64_t t = (w & (a.tiles - 1));
         const QDesc D = desc[a.r0 + ci];
         __syncthreads();
         for (uint32_t e = threadIdx.x; e < D.e_count; e += blockDim.x) em[e] = (uint32_t)emasks[D.e_begin + e];
@@ -583,19 +584,21 @@ __device__ __forceinline__ void qb_block_sum2(float v, float u, double *red, dou
         }
     __syncthreads();
 }
-__device__ __forceinline__ void qb_issue(bool dual, bool pass_b, bool with_cost, const QBArgs &a, const QDesc *desc,
-                                         float2 *arena, const uint8_t *costs, uint64_t w, float2 *tp, float2 *tl,
+// the cp.async copies of item tile t of instance D (psi, lambda for dual
+// passes, the cost bytes for pass A), one commit group
+__device__ __forceinline__ void qb_issue(bool dual, bool pass_b, bool with_cost, const QBArgs &a, const QDesc &D,
+                                         float2 *arena, const uint8_t *costs, uint64_t t, float2 *tp, float2 *tl,
                                          uint8_t *tc) {
-    const uint32_t ci = (uint32_t)(w / a.tiles);
-    const uint64_t t = w % a.tiles;
-    const QDesc D = desc[a.r0 + ci];
     const bool load_psi = pass_b || dual || a.layer > 0;
     if (load_psi) qb_load(tp, arena + D.psi, pass_b, a.L, t);
     if (dual) qb_load(tl, arena + D.lam, pass_b, a.L, t);
     if (with_cost) qb_load_cost(tc, costs + D.cost, t);
     asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
-// the element offsets of the last round's amplitudes base | (i << b0) in the
+// a phase table into shared memory (visible after the caller's next barrier)
+__device__ __forceinline__ void qb_table(float2 *spt, const float2 *ph, uint32_t e_count) {
+    for (uint32_t c = threadIdx.x; c <= e_count; c += blockDim.x) spt[c] = ph[c];
+}// the element offsets of the last round's amplitudes base | (i << b0) in the
 // state: pass A contiguous tiles, pass B through qb_index (a bit permutation,
 // so the offset of i is the sum of those of its bits)
 template <bool PASS_B>
@@ -610,32 +613,63 @@ __device__ __forceinline__ void qb_offsets(const QBArgs &a, uint64_t t, uint32_t
         off[i] = ((i & 1u) ? o[0] : 0u) + ((i & 2u) ? o[1] : 0u) + ((i & 4u) ? o[2] : 0u) + ((i & 8u) ? o[3] : 0u);
 }
 
+// Item order of the batched passes. Pass A: each CTA walks a run of
+// consecutive items (the instance's descriptor stays in L1 and its phase table
+// in shared memory across the run). Pass B: grid-stride, so the CTAs at work
+// hold neighbouring tiles of one instance (a pass-B tile is 2^(12-L) runs of
+// 2^L amplitudes, and neighbouring tiles' runs are adjacent in memory).
+struct QItems {
+    uint64_t w, end, step;
+};
+template <bool PASS_B>
+__device__ __forceinline__ QItems qb_items(const QBArgs &a) {
+    const uint64_t items = (uint64_t)a.m * a.tiles;
+    if (PASS_B) return QItems{blockIdx.x, items, gridDim.x};
+    const uint64_t w0 = blockIdx.x * a.chunk;
+    return QItems{w0, min(items, w0 + a.chunk), 1};
+}
+
 // forward pass: [pass A: cost phase] + mixer; the last pass B of the last
-// layer also writes lambda = C psi and the per-tile energy
+// layer also writes lambda = C psi and the per-tile energy. Two tile buffers:
+// the next item's copies are issued before the current item's rounds.
 template <bool PASS_B, int NR>
-__global__ void __launch_bounds__(kQThreads, 4)
+__global__ void __launch_bounds__(kQThreads, 3)
     k_qaoa_fwd(const QBArgs a, const QDesc *__restrict__ desc, float2 *__restrict__ arena, const uint8_t *__restrict__ costs,
                const float2 *__restrict__ ptab, const QMix *__restrict__ mtab, double *__restrict__ part) {
-    extern __shared__ __align__(16) float2 qb_tile[];
-    uint8_t *tc = reinterpret_cast<uint8_t *>(qb_tile + kQBT);
+    extern __shared__ __align__(16) float2 qb_tile[];  // two tiles, then two cost-byte tiles
+    uint8_t *tcs = reinterpret_cast<uint8_t *>(qb_tile + 2 * kQBT);
     __shared__ double red[32];
-    __shared__ float2 spt[kQMaxEdges + 1];  // the item's phase table
-    const uint64_t items = (uint64_t)a.m * a.tiles;
+    __shared__ float2 spt[kQMaxEdges + 1];  // the instance's phase table
+    const QItems it = qb_items<PASS_B>(a);
+    if (it.w >= it.end) return;
     const bool last = PASS_B && a.layer + 1 == a.p;
-    uint64_t w = blockIdx.x;
-    if (w < items) qb_issue(false, PASS_B, !PASS_B, a, desc, arena, costs, w, qb_tile, nullptr, tc);
-    for (; w < items; w += gridDim.x) {
-        const uint32_t ci = (uint32_t)(w / a.tiles);
-        const uint64_t t = w % a.tiles;
-        const uint32_t r = a.r0 + ci;
-        const QDesc D = desc[r];
-        const QMix M = mtab[(uint64_t)r * a.p + a.layer];
-        if (!PASS_B) {  // the previous item's reads of spt ended before its last barrier
-            const float2 *ph = ptab + D.ptab + (uint64_t)a.layer * (kQMaxEdges + 1);
-            for (uint32_t c = threadIdx.x; c <= D.e_count; c += blockDim.x) spt[c] = ph[c];
+    // pass A keeps the run's descriptor and constants in registers and reloads
+    // them (and the phase table) between instances; pass B reads them per item
+    uint32_t ci = (uint32_t)(it.w >> (a.n - kQBTile));
+    QDesc Dc = desc[a.r0 + ci];
+    QMix Mc = mtab[(uint64_t)(a.r0 + ci) * a.p + a.layer];
+    qb_issue(false, PASS_B, !PASS_B, a, Dc, arena, costs, (it.w & (a.tiles - 1)), qb_tile, nullptr, tcs);
+    if (!PASS_B) qb_table(spt, ptab + Dc.ptab + (uint64_t)a.layer * (kQMaxEdges + 1), Dc.e_count);
+    uint32_t cur = 0;
+    for (uint64_t w = it.w; w < it.end; w += it.step, cur ^= 1u) {
+        const uint64_t t = (w & (a.tiles - 1));
+        if (PASS_B) ci = (uint32_t)(w >> (a.n - kQBTile));
+        const QDesc D = PASS_B ? desc[a.r0 + ci] : Dc;
+        const QMix M = PASS_B ? mtab[(uint64_t)(a.r0 + ci) * a.p + a.layer] : Mc;
+        const uint64_t wn = w + it.step;
+        const uint32_t cn = (uint32_t)(wn >> (a.n - kQBTile));
+        QDesc Dn = D;
+        if (wn < it.end) {
+            if (cn != ci) Dn = desc[a.r0 + cn];
+            qb_issue(false, PASS_B, !PASS_B, a, Dn, arena, costs, (wn & (a.tiles - 1)), qb_tile + ((cur ^ 1u) << kQBTile), nullptr,
+                     tcs + ((cur ^ 1u) << kQBTile));
+            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
         }
-        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
         __syncthreads();
+        float2 *tile = qb_tile + (cur << kQBTile);
+        const uint8_t *tc = tcs + (cur << kQBTile);
         float2 v[16];
         uint32_t base = 0, pb = 0, b0 = 0;
 #pragma unroll
@@ -645,7 +679,7 @@ __global__ void __launch_bounds__(kQThreads, 4)
             pb = qb_phys(base);
             const uint32_t mask = qb_mask(PASS_B, b0, a.L);
             if (!PASS_B && k == 0) {  // the cost phase on window 0..3 (layer 0: the table holds H|0> times the phase)
-                if (a.layer > 0) qb_read(qb_tile, pb, 0, v);
+                if (a.layer > 0) qb_read(tile, pb, 0, v);
                 const uint4 cb = *reinterpret_cast<const uint4 *>(tc + base);
                 const uint32_t cw[4] = {cb.x, cb.y, cb.z, cb.w};
 #pragma unroll
@@ -654,17 +688,15 @@ __global__ void __launch_bounds__(kQThreads, 4)
                     v[i] = a.layer == 0 ? f : cm(v[i], f);
                 }
             } else {
-                qb_read(qb_tile, pb, b0, v);
+                qb_read(tile, pb, b0, v);
             }
             if (M.form_c) qb_mix<true>(v, mask, M.kf);
             else qb_mix<false>(v, mask, M.kf);
             if (k + 1 < NR) {
-                qb_write(qb_tile, pb, b0, v);
+                qb_write(tile, pb, b0, v);
                 __syncthreads();
             }
         }
-        __syncthreads();  // every read of this tile is done: stream the next one in
-        if (w + gridDim.x < items) qb_issue(false, PASS_B, !PASS_B, a, desc, arena, costs, w + gridDim.x, qb_tile, nullptr, tc);
         uint64_t x0;
         uint32_t off[16];
         qb_offsets<PASS_B>(a, t, base, b0, x0, off);
@@ -687,11 +719,20 @@ __global__ void __launch_bounds__(kQThreads, 4)
             const double et = qb_block_sum(e, red);
             if (threadIdx.x == 0) part[D.part + t] = et;
         }
+        __syncthreads();  // every read of this tile buffer and of spt is done before they are refilled
+        if (!PASS_B && wn < it.end && cn != ci) {
+            ci = cn;
+            Dc = Dn;
+            Mc = mtab[(uint64_t)(a.r0 + ci) * a.p + a.layer];
+            qb_table(spt, ptab + Dc.ptab + (uint64_t)a.layer * (kQMaxEdges + 1), Dc.e_count);
+        }
     }
 }
 
 // reverse pass: the inverse mixer on psi and lambda with the dE/dbeta terms;
-// pass A then the cost layer's dE/dgamma term and the inverse phase
+// pass A then the cost layer's dE/dgamma term and the inverse phase. One
+// buffer per tile (psi and lambda): the next item's copies are issued after
+// the last round's reads.
 template <bool PASS_B, int NR>
 __global__ void __launch_bounds__(kQThreads, 2)
     k_qaoa_rev(const QBArgs a, const QDesc *__restrict__ desc, float2 *__restrict__ arena, const uint8_t *__restrict__ costs,
@@ -700,19 +741,22 @@ __global__ void __launch_bounds__(kQThreads, 2)
     float2 *tp = qb_tile, *tl = qb_tile + kQBT;
     uint8_t *tc = reinterpret_cast<uint8_t *>(qb_tile + 2 * kQBT);
     __shared__ double red[32];
-    __shared__ float2 spt[kQMaxEdges + 1];  // the item's inverse phase table
-    const uint64_t items = (uint64_t)a.m * a.tiles;
-    uint64_t w = blockIdx.x;
-    if (w < items) qb_issue(true, PASS_B, !PASS_B, a, desc, arena, costs, w, tp, tl, tc);
-    for (; w < items; w += gridDim.x) {
-        const uint32_t ci = (uint32_t)(w / a.tiles);
-        const uint64_t t = w % a.tiles;
-        const uint32_t r = a.r0 + ci;
-        const QDesc D = desc[r];
-        const QMix M = mtab[(uint64_t)r * a.p + a.layer];
-        if (!PASS_B) {  // the previous item's reads of spt ended before its block sums' barriers
-            const float2 *ph = ptab + D.ptab + (uint64_t)(a.p + a.layer) * (kQMaxEdges + 1);
-            for (uint32_t c = threadIdx.x; c <= D.e_count; c += blockDim.x) spt[c] = ph[c];
+    __shared__ float2 spt[kQMaxEdges + 1];  // the instance's inverse phase table
+    const QItems it = qb_items<PASS_B>(a);
+    if (it.w >= it.end) return;
+    uint32_t ci_tab = ~0u;
+    {
+        const QDesc D = desc[a.r0 + (uint32_t)(it.w >> (a.n - kQBTile))];
+        qb_issue(true, PASS_B, !PASS_B, a, D, arena, costs, (it.w & (a.tiles - 1)), tp, tl, tc);
+    }
+    for (uint64_t w = it.w; w < it.end; w += it.step) {
+        const uint32_t ci = (uint32_t)(w >> (a.n - kQBTile));
+        const uint64_t t = (w & (a.tiles - 1));
+        const QDesc D = desc[a.r0 + ci];
+        const QMix M = mtab[(uint64_t)(a.r0 + ci) * a.p + a.layer];
+        if (!PASS_B && ci != ci_tab) {  // the previous item's reads of spt ended before its block sums' barriers
+            qb_table(spt, ptab + D.ptab + (uint64_t)(a.p + a.layer) * (kQMaxEdges + 1), D.e_count);
+            ci_tab = ci;
         }
         asm volatile("cp.async.wait_group 0;\n" ::: "memory");
         __syncthreads();
@@ -749,8 +793,12 @@ __global__ void __launch_bounds__(kQThreads, 2)
                 __syncthreads();
             }
         }
-        __syncthreads();  // every read of this tile is done: stream the next one in
-        if (w + gridDim.x < items) qb_issue(true, PASS_B, !PASS_B, a, desc, arena, costs, w + gridDim.x, tp, tl, tc);
+        __syncthreads();  // every read of the tile buffers is done: stream the next item in
+        const uint64_t wn = w + it.step;
+        if (wn < it.end) {
+            const uint32_t cn = (uint32_t)(wn >> (a.n - kQBTile));
+            qb_issue(true, PASS_B, !PASS_B, a, cn == ci ? D : desc[a.r0 + cn], arena, costs, (wn & (a.tiles - 1)), tp, tl, tc);
+        }
         uint64_t x0;
         uint32_t off[16];
         qb_offsets<PASS_B>(a, t, base, b0, x0, off);
@@ -927,7 +975,8 @@ extern "C" int qf_qaoa_maxcut_batch(qf_ctx *ctx, const qf_qaoa_instance *inst, u
     static bool attr[64] = {false};
     static int pass_occ[64][8];
     const size_t smem = sizeof(QShared);
-    const size_t smem_f = sizeof(float2) * kQBT + kQBT, smem_r = 2 * sizeof(float2) * kQBT + kQBT;  // tiles + cost bytes
+    // forward: two tiles + two cost-byte tiles; reverse: psi and lambda tiles + cost bytes
+    const size_t smem_f = 2 * (sizeof(float2) * kQBT + kQBT), smem_r = 2 * sizeof(float2) * kQBT + kQBT;
     // passes: forward A, forward B with 1..3 rounds, reverse A, reverse B with 1..3 rounds
     using QPass = void (*)(QBArgs, const QDesc *, float2 *, const uint8_t *, const float2 *, const QMix *, double *);
     const QPass passes[8] = {k_qaoa_fwd<false, 3>, k_qaoa_fwd<true, 1>, k_qaoa_fwd<true, 2>, k_qaoa_fwd<true, 3>,
@@ -946,8 +995,11 @@ extern "C" int qf_qaoa_maxcut_batch(qf_ctx *ctx, const qf_qaoa_instance *inst, u
     int per_sm = 0;
     QF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_qaoa_batch, kQThreads, smem));
     const uint32_t grid = (uint32_t)std::min<uint64_t>(std::max(1u, n_small), (uint64_t)std::max(1, per_sm) * ctx->sm_count);
-    auto pass_grid = [&](int i, uint64_t items) {
-        return (unsigned)std::min<uint64_t>(items, (uint64_t)std::max(1, pass_occ[dev][i]) * ctx->sm_count);
+    // one wave of resident CTAs, each on a run of consecutive items
+    auto pass_grid = [&](int i, uint64_t items, uint64_t *chunk) {
+        const uint64_t g = std::min<uint64_t>(items, (uint64_t)std::max(1, pass_occ[dev][i]) * ctx->sm_count);
+        *chunk = (items + g - 1) / g;
+        return (unsigned)((items + *chunk - 1) / *chunk);
     };
     auto enqueue = [&](cudaStream_t s) -> int {
         if (r_small) {
@@ -967,18 +1019,24 @@ extern "C" int qf_qaoa_maxcut_batch(qf_ctx *ctx, const qf_qaoa_instance *inst, u
             A.tiles = 1ULL << (A.n - kQBTile);
             const uint64_t items = (uint64_t)A.m * A.tiles;
             const int rb = qb_rounds_b(A.L);  // pass B rounds: 3, 2 or 1
-            const unsigned gfa = pass_grid(0, items), gfb = pass_grid(rb, items);
-            const unsigned gra = pass_grid(4, items), grb = pass_grid(4 + rb, items);
+            uint64_t cfa, cfb, cra, crb;
+            const unsigned gfa = pass_grid(0, items, &cfa), gfb = pass_grid(rb, items, &cfb);
+            const unsigned gra = pass_grid(4, items, &cra), grb = pass_grid(4 + rb, items, &crb);
             A.layer = 0;
+            A.chunk = 0;
             k_qaoa_costs<<<gfa, kQThreads, 0, s>>>(A, d_desc, d_mask, d_costs);
             for (uint32_t l = 0; l < p; ++l) {
                 A.layer = l;
+                A.chunk = cfa;
                 passes[0]<<<gfa, kQThreads, smem_f, s>>>(A, d_desc, d_arena, d_costs, d_ptab, d_mtab, d_part);
+                A.chunk = cfb;
                 passes[rb]<<<gfb, kQThreads, smem_f, s>>>(A, d_desc, d_arena, d_costs, d_ptab, d_mtab, d_part);
             }
             for (uint32_t l = p; l-- > 0;) {
                 A.layer = l;
+                A.chunk = crb;
                 passes[4 + rb]<<<grb, kQThreads, smem_r, s>>>(A, d_desc, d_arena, d_costs, d_ptab, d_mtab, d_part);
+                A.chunk = cra;
                 passes[4]<<<gra, kQThreads, smem_r, s>>>(A, d_desc, d_arena, d_costs, d_ptab, d_mtab, d_part);
             }
             k_qaoa_reduce<<<(unsigned)std::max<uint64_t>(1, ((uint64_t)A.m * (1 + 2 * p) + 127) / 128), 128, 0, s>>>(
