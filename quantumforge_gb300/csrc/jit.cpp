@@ -723,7 +723,7 @@ struct PassGen {
         while (left) {
             bool progress = false;
             for (size_t j = 0; j < G.size() && left; ++j) {
-                if (done[j] || !ready(j, done) || !runnable(G[j], reg_mask(), false)) continue;
+                if (done[j] || is_zovl(G[j]) || !ready(j, done) || !runnable(G[j], reg_mask(), false)) continue;
                 emit_gate(G[j]);
                 order.push_back((int)j);
                 done[j] = 1;
@@ -733,6 +733,21 @@ struct PassGen {
             }
             if (progress) remapped = false;
             if (!left || progress) continue;
+            if (dual) {  // nothing else runs: every ready Z-axis overlap at once
+                std::vector<int> zs;
+                for (size_t j = 0; j < G.size(); ++j)
+                    if (!done[j] && is_zovl(G[j]) && ready(j, done)) zs.push_back((int)j);
+                if (!zs.empty()) {
+                    emit_overlap_group(zs);
+                    for (int j : zs) {
+                        order.push_back(j);
+                        done[j] = 1;
+                        --left;
+                    }
+                    remapped = false;
+                    continue;
+                }
+            }
             bool dense_left = false;
             for (size_t j = 0; j < G.size(); ++j) dense_left = dense_left || (!done[j] && strict_need(G[j]));
             if (!dense_left || remapped) {  // only diagonal gates hold things up: run one where its qubit is
@@ -770,9 +785,67 @@ struct PassGen {
     // src/lib.rs:3648-3664, summed as the shared-memory kernel does), reduced
     // over the warp in f32 and added to the slot's f64 accumulator (held by
     // lane slot % 32).
-    void emit_overlap(const BGate &x) {
+    // Z-axis overlaps of a backward pass are held back until nothing else can
+    // run, then evaluated together: Im<lambda|Z_q psi> commutes with every gate
+    // still pending before it (none of them acts off-diagonal on q), and all of
+    // them share the per-amplitude products w_i = Im(conj(l_i) r_i).
+    bool is_zovl(const BGate &x) const { return dual && x.kind == BK_OVL && x.axis == QF_PAULI_Z; }
+    static std::string tree_sum(const std::vector<std::string> &v, size_t b, size_t e) {
+        if (e - b == 1) return v[b];
+        const size_t m = b + (e - b) / 2;
+        return "(" + tree_sum(v, b, m) + " + " + tree_sum(v, m, e) + ")";
+    }
+    void emit_overlap_group(const std::vector<int> &js) {
+        auto &s = g.s;
+        const auto &G = p.gates;
+        s << "{\n";
+        std::vector<std::string> w;
+        for (int i = 0; i < kR; ++i) {
+            const std::string l = "l" + std::to_string(g.v[i]), r = "r" + std::to_string(g.v[i]);
+            s << "const float w" << i << " = " << l << ".x * " << r << ".y - " << l << ".y * " << r << ".x;\n";
+            w.push_back("w" + std::to_string(i));
+        }
+        s << "const float wt = " << tree_sum(w, 0, w.size()) << ";\n";
+        uint32_t rbits = 0;
+        for (int j : js) {
+            const uint8_t d = desc(G[j].q0);
+            if (is_reg(d)) rbits |= 1u << (d - 8);
+        }
+        for (int rb = 0; rb < 4; ++rb) {  // sum over register bit rb clear minus bit set = 2 (clear) - total
+            if (!((rbits >> rb) & 1u)) continue;
+            std::vector<std::string> c;
+            for (int i = 0; i < kR; ++i)
+                if (!((i >> rb) & 1)) c.push_back(w[i]);
+            s << "const float wz" << rb << " = 2.f * " << tree_sum(c, 0, c.size()) << " - wt;\n";
+        }
+        for (int j : js) {
+            const BGate &x = G[j];
+            const uint8_t d = desc(x.q0);
+            s << "{float ov = ";
+            if (is_reg(d)) s << "wz" << (d - 8) << ";\n";
+            else s << "(" << cbit(d) << ") ? -wt : wt;\n";
+            emit_overlap_sum(x);
+            s << "}\n";
+        }
+        s << "}\n";
+    }
+    // the overlap value `ov` of x (psi and lambda scale by |G|^2), reduced over
+    // the warp and added to the slot's float-pair accumulator
+    void emit_overlap_sum(const BGate &x) {
         auto &s = g.s;
         const int ls = (int)x.op_index - (int)p.a.slot_base;
+        if (g.any_scale) {
+            const int sl = g.slot(std::norm(g.pscale), 0.0, 0.0, 0.0);
+            s << "ov *= " << Mref(sl, 0) << ".x;\n";
+        }
+        for (int o = 16; o >= 1; o >>= 1) s << "ov += __shfl_xor_sync(0xffffffffu, ov, " << o << ");\n";
+        const std::string ah = "acc" + std::to_string(ls >> 5) + "h", al = "acc" + std::to_string(ls >> 5) + "l";
+        s << "if (lane == " << (ls & 31) << "u) {const float sm = " << ah << " + ov, bb = sm - " << ah << "; " << al << " += ("
+          << ah << " - (sm - bb)) + (ov - bb); " << ah << " = sm;}\n";
+    }
+
+    void emit_overlap(const BGate &x) {
+        auto &s = g.s;
         auto R_ = [&](int i) { return "r" + std::to_string(g.v[i]); };
         auto L_ = [&](int i) { return "l" + std::to_string(g.v[i]); };
         s << "{float ov = 0.f;\n";
@@ -800,14 +873,8 @@ struct PassGen {
                       << ".x + " << l1 << ".y * " << p0 << ".y);\n";
             }
         }
-        if (g.any_scale) {  // psi and lambda both carry the factor G pulled out so far: <l|P|p> scales by |G|^2
-            const int sl = g.slot(std::norm(g.pscale), 0.0, 0.0, 0.0);
-            s << "ov *= " << Mref(sl, 0) << ".x;\n";
-        }
-        for (int o = 16; o >= 1; o >>= 1) s << "ov += __shfl_xor_sync(0xffffffffu, ov, " << o << ");\n";
-        const std::string ah = "acc" + std::to_string(ls >> 5) + "h", al = "acc" + std::to_string(ls >> 5) + "l";
-        s << "if (lane == " << (ls & 31) << "u) {const float sm = " << ah << " + ov, bb = sm - " << ah << "; " << al << " += ("
-          << ah << " - (sm - bb)) + (ov - bb); " << ah << " = sm;}}\n";
+        emit_overlap_sum(x);  // psi and lambda both carry the factor G pulled out so far
+        s << "}\n";
     }
 
     void emit_gate(const BGate &x) {
