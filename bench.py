@@ -57,6 +57,8 @@ def parse_args():
                     help="comma-separated extra workloads to run after the headline")
     ap.add_argument("--vqe-qubits", type=int, default=32, help="qubits of the checkpointed-adjoint extra (vqe32)")
     ap.add_argument("--qaoa-instances", type=int, default=4096, help="instances of the batched QAOA extra (qaoa4096)")
+    ap.add_argument("--vqe24-adjoint-only", action="store_true",
+                    help="vqe24 extra: only the adjoint gradient with a checkpoint every four layers, twice (profiling runs)")
     ap.add_argument("--density-qubits", type=int, default=14, help="qubits of the density-matrix extra (density14)")
     ap.add_argument("--noise-shots", type=int, default=100_000, help="shots of the noisy-shot extra (noise_shots)")
     ap.add_argument("--c2-modes", default="unfused,passes,k2,k3,k4,k5,k5_simt",
@@ -343,7 +345,7 @@ def run_ours(args):
     if rank == 0 and not args.no_extra:
         wanted = set(args.extras.split(","))
         if "vqe24" in wanted:
-            extra["vqe24"] = vqe_gradients(backend, cpu=not args.no_cpu_baseline)
+            extra["vqe24"] = vqe_gradients(backend, cpu=not args.no_cpu_baseline, adjoint_only=args.vqe24_adjoint_only)
         if "qaoa4096" in wanted:
             extra["qaoa4096"] = qaoa_batch(backend, cpu=not args.no_cpu_baseline, count=args.qaoa_instances)
         if "shots20" in wanted:
@@ -909,7 +911,7 @@ def qaoa_cpu_estimate(problems):
             "eval_s": {str(k): v for k, v in t_eval.items()}}
 
 
-def vqe_gradients(backend, cpu: bool = True):
+def vqe_gradients(backend, cpu: bool = True, adjoint_only: bool = False):
     """24-qubit VQE (RY.RZ per qubit + CZ ring, 8 layers, 384 params, TFIM
     ring h = 1): adjoint (checkpoint per layer) vs GPU parameter shift, both
     complex64; the energy and gradient error against a complex128 adjoint run
@@ -937,6 +939,13 @@ def vqe_gradients(backend, cpu: bool = True):
     from quantumforge_gb300 import _abi as A
     from quantumforge_gb300 import _native
 
+    if adjoint_only:  # a warm-up and one timed gradient, nothing else launched
+        kw = dict(dtype="c64", backend=backend, checkpoint_every=12 * n)
+        gradient_with_inputs(pc, GradientOptions(strategy=GradientStrategy.Adjoint), [], params, n, H, **kw)
+        t0 = time.perf_counter()
+        gradient_with_inputs(pc, GradientOptions(strategy=GradientStrategy.Adjoint), [], params, n, H, **kw)
+        return {"qubits": n, "params": int(params.size), "adjoint_policy": "every_4_layers",
+                "s_per_gradient": time.perf_counter() - t0}
     peak, peak_kind = hbm_peak()
     policies = {}
     for name, every in (("per_layer", 3 * n), ("every_4_layers", 12 * n), ("uncompute", 0)):
@@ -1069,7 +1078,7 @@ def extras_only(args):
     cpu = not args.no_cpu_baseline
     extra = {}
     if "vqe24" in wanted:
-        extra["vqe24"] = vqe_gradients(backend, cpu=not args.no_cpu_baseline)
+        extra["vqe24"] = vqe_gradients(backend, cpu=not args.no_cpu_baseline, adjoint_only=args.vqe24_adjoint_only)
     if "qaoa4096" in wanted:
         extra["qaoa4096"] = qaoa_batch(backend, cpu=cpu, count=args.qaoa_instances)
     if "shots20" in wanted:
