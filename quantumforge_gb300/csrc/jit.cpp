@@ -708,7 +708,7 @@ struct PassGen {
             s << "float2* S = SB;\nfloat2* SL = SB + " << tile_of(K) << "u;\n";
         }
         s << "const unsigned long long tb = " << dep_t << ";\n";
-        if (!dual) s << "float2 tph = make_float2(1.f, 0.f);\n";  // deferred per-thread phase
+        s << "float2 tph = make_float2(1.f, 0.f);\n";  // deferred per-thread phase (psi and lambda alike)
         phase_pending = false;
         for (int a = 0; a < n_arrays(); ++a)
             for (int i = 0; i < kR; ++i) s << "float2 " << reg_pfx(a) << i << ";\n";
@@ -834,6 +834,8 @@ struct PassGen {
     void emit_overlap_sum(const BGate &x) {
         auto &s = g.s;
         const int ls = (int)x.op_index - (int)p.a.slot_base;
+        // psi and lambda both wait for the deferred phase: <l|P|p> carries |tph|^2
+        if (phase_pending) s << "ov *= tph.x * tph.x + tph.y * tph.y;\n";
         if (g.any_scale) {
             const int sl = g.slot(std::norm(g.pscale), 0.0, 0.0, 0.0);
             s << "ov *= " << Mref(sl, 0) << ".x;\n";
@@ -894,19 +896,14 @@ struct PassGen {
                         const int rb = d - 8;
                         for (int i = 0; i < kR; ++i)
                             if ((i >> rb) & 1) emit_cmul_const(g, g.R(i), sl, 0);
-                    } else if (!dual) {
+                    } else if (a == 0) {
                         // a lane, warp or outside-the-tile bit is constant over the thread's
                         // registers: the factor goes into the thread's deferred phase
-                        // (applied once, before the next remap or the store)
-                        if (a == 0) {
-                            s << "if (" << cbit(d) << ") ";
-                            emit_cmul_const(g, "tph", sl, 0);
-                            phase_pending = true;
-                        }
-                    } else {
-                        s << "if (" << cbit(d) << ") {\n";
-                        for (int i = 0; i < kR; ++i) emit_cmul_const(g, g.R(i), sl, 0);
-                        s << "}\n";
+                        // (applied once, before the next remap or the store; backward
+                        // passes apply the same factor to psi and lambda)
+                        s << "if (" << cbit(d) << ") ";
+                        emit_cmul_const(g, "tph", sl, 0);
+                        phase_pending = true;
                     }
                 }
             } else {
@@ -968,10 +965,9 @@ struct PassGen {
                     for (int i = 0; i < kR; ++i)
                         if ((i >> b) & 1) neg(i);
                     s << "}\n";
-                } else {
-                    s << "if (" << cbit(da) << " & " << cbit(db) << ") {\n";
-                    for (int i = 0; i < kR; ++i) neg(i);
-                    s << "}\n";
+                } else if (a == 0) {  // both bits constant over the thread's registers: the deferred phase
+                    s << "if (" << cbit(da) << " & " << cbit(db) << ") {tph.x = -tph.x; tph.y = -tph.y;}\n";
+                    phase_pending = true;
                 }
             }
             break;
@@ -1031,10 +1027,15 @@ struct PassGen {
     void flush_phase() {
         if (!phase_pending) return;
         auto &s = g.s;
-        for (int i = 0; i < kR; ++i) {
-            const std::string R = g.R(i);
-            s << "{const float2 x=" << R << ";" << R << ".x=tph.x*x.x-tph.y*x.y;" << R << ".y=tph.x*x.y+tph.y*x.x;}\n";
+        const std::string keep = g.pfx;
+        for (int a = 0; a < n_arrays(); ++a) {
+            g.pfx = reg_pfx(a);
+            for (int i = 0; i < kR; ++i) {
+                const std::string R = g.R(i);
+                s << "{const float2 x=" << R << ";" << R << ".x=tph.x*x.x-tph.y*x.y;" << R << ".y=tph.x*x.y+tph.y*x.x;}\n";
+            }
         }
+        g.pfx = keep;
         s << "tph = make_float2(1.f, 0.f);\n";
         phase_pending = false;
     }
