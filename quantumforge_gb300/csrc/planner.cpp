@@ -50,6 +50,12 @@ int gate_matrix(int gate, double theta, double m[8]) {
 }
 
 bool matrix_is_diag(const double m[8]) { return m[2] == 0 && m[3] == 0 && m[4] == 0 && m[5] == 0; }
+// all entries real, or real diagonal with an imaginary off-diagonal (RX type):
+// the compiled passes' two cheap dense forms
+bool matrix_is_cheap(const double m[8]) {
+    if (m[1] == 0 && m[3] == 0 && m[5] == 0 && m[7] == 0) return true;
+    return m[1] == 0 && m[7] == 0 && m[2] == 0 && m[4] == 0;
+}
 
 static int rotation_gate(int axis) {
     return axis == QF_PAULI_X ? QF_GATE_RX : axis == QF_PAULI_Y ? QF_GATE_RY : QF_GATE_RZ;
@@ -650,11 +656,20 @@ int plan_passes(uint32_t n, const std::vector<BGate> &gates, const PlanOpts &o, 
                 if (prev >= 0 && !taken[prev].overlap && taken[prev].g.kind == BK_MAT1) {
                     double c[8];
                     mat_mul(it.g.m, taken[prev].g.m, c);
-                    std::memcpy(taken[prev].g.m, c, sizeof c);
-                    taken[prev].g.varying |= it.g.varying;
-                    taken[prev].g.diag = matrix_is_diag(c);
-                    taken[prev].g.op_index = -1;
-                    return;
+                    // Gates from circuit parameters keep the plain matrix form (no
+                    // factoring, so new angles never recompile): their product is
+                    // merged only while it stays diagonal, real or RX-type. A
+                    // general complex product (RZ after RY, RY after RX) costs 16
+                    // FMAs per amplitude pair, the two apart a real rotation and a
+                    // diagonal phase (deferred when its qubit is off the registers).
+                    const bool varying = taken[prev].g.varying || it.g.varying;
+                    if (!varying || matrix_is_diag(c) || matrix_is_cheap(c)) {
+                        std::memcpy(taken[prev].g.m, c, sizeof c);
+                        taken[prev].g.varying = varying;
+                        taken[prev].g.diag = matrix_is_diag(c);
+                        taken[prev].g.op_index = -1;
+                        return;
+                    }
                 }
             }
             taken.push_back(it);

@@ -119,6 +119,7 @@ struct BGate {
 // Gate::matrix (src/lib.rs:2267-2333) evaluated on the host in f64.
 int gate_matrix(int gate, double theta, double m[8]);
 bool matrix_is_diag(const double m[8]);
+bool matrix_is_cheap(const double m[8]);
 
 // Validate an op list for state-vector execution and bind it.
 // `shift_op`/`shift` add `shift` to the angle of op `shift_op` (parameter shift).
