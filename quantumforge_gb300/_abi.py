@@ -167,11 +167,8 @@ assert OP_DTYPE.itemsize == 24 and TERM_DTYPE.itemsize == 32
 
 def ops_array(records) -> np.ndarray:
     """Build a contiguous ``qf_op`` array from (kind, gate, q0, q1, param, theta[, flags]) tuples."""
-    arr = np.zeros(len(records), dtype=OP_DTYPE)
-    for i, r in enumerate(records):
-        kind, gate, q0, q1, param, theta = r[:6]
-        arr[i] = (kind, gate, r[6] if len(r) > 6 else 0, q0, q1, param, theta)
-    return arr
+    rows = [(r[0], r[1], r[6] if len(r) > 6 else 0, r[2], r[3], r[4], r[5]) for r in records]
+    return np.array(rows, dtype=OP_DTYPE) if rows else np.zeros(0, dtype=OP_DTYPE)
 
 
 def aux_fields(value: float) -> tuple[int, int]:

@@ -781,6 +781,20 @@ class NoiseChannel:
         return f"NoiseChannel.{names[self.kind]}({self.p}{extra})"
 
 
+def _cached_ops(owner) -> np.ndarray:
+    """The ``qf_op`` array of ``owner.operations``, rebuilt only when the list
+    differs from the one it was built from (records are tuples; the array is
+    read-only and shared between calls)."""
+    src = getattr(owner, "_ops_src", None)
+    if src is not None and src == owner.operations:
+        return owner._ops_arr
+    arr = _abi.ops_array(owner.operations)
+    arr.flags.writeable = False
+    owner._ops_src = list(owner.operations)
+    owner._ops_arr = arr
+    return arr
+
+
 class Circuit:
     """`Circuit` (src/lib.rs:2517-2916): an op list executed on a device state."""
 
@@ -872,7 +886,7 @@ class Circuit:
         return m + 1
 
     def ops(self) -> np.ndarray:
-        return _abi.ops_array(self.operations)
+        return _cached_ops(self)
 
     def run(self, state: StateVector, exec_opts=None) -> StateVector:
         """Circuit::run (src/lib.rs:2786-2802), in place on the device state."""
@@ -1027,7 +1041,7 @@ class ParameterizedCircuit:
         self.operations.append(channel.record(int(target)))
 
     def ops(self) -> np.ndarray:
-        return _abi.ops_array(self.operations)
+        return _cached_ops(self)
 
     # validate_parameters / validate_inputs (src/lib.rs:4651-4675)
     def _values(self, inputs, parameters):
