@@ -290,24 +290,23 @@ int adjoint_device(qf_ctx *ctx, uint32_t n, const std::vector<BGate> &gates, con
             QF_CUDA(cudaMemcpyAsync(c->d, psi->d, psi->bytes(), cudaMemcpyDeviceToDevice, ctx->stream));
         }
     }
-    double e_val = 0.0;
-    QF_TRY(pauli_apply(psi, lam, terms, n_terms, &e_val));
-    if (energy) *energy = e_val;
-    double *d_sums = nullptr;
+    // the slot sums and, behind them, the energy stay on the device until the
+    // single synchronize at the end: the host prepares the backward passes
+    // while lambda = H psi runs
     const size_t bytes = sizeof(double) * total_slots;
-    if (total_slots) {
-        if (bytes > kSmallBytes) QF_TRY(ensure_device(&ctx->ws_tree, &ctx->ws_tree_bytes, bytes));
-        d_sums = bytes > kSmallBytes ? static_cast<double *>(ctx->ws_tree) : ctx->d_small;
-        QF_CUDA(cudaMemsetAsync(d_sums, 0, bytes, ctx->stream));
-    }
+    QF_TRY(ensure_device(&ctx->ws_tree, &ctx->ws_tree_bytes, bytes + 2 * sizeof(double)));
+    double *d_sums = static_cast<double *>(ctx->ws_tree);
+    QF_TRY(pauli_apply(psi, lam, terms, n_terms, nullptr, d_sums + total_slots));
+    if (total_slots) QF_CUDA(cudaMemsetAsync(d_sums, 0, bytes, ctx->stream));
     for (size_t s = n_seg; s-- > 0;) {
         QF_TRY(run_plan_dual(psi, lam, bplans[s], bplans[s].n_slots ? d_sums + slot_off[s] : nullptr, o->exec.flags));
         if (s > 0 && !ckpt.empty())
             QF_CUDA(cudaMemcpyAsync(psi->d, ckpt[s - 1]->d, psi->bytes(), cudaMemcpyDeviceToDevice, ctx->stream));
     }
-    std::vector<double> sums(total_slots);
-    if (total_slots) QF_CUDA(cudaMemcpyAsync(sums.data(), d_sums, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    std::vector<double> sums(total_slots + 2);
+    QF_CUDA(cudaMemcpyAsync(sums.data(), d_sums, bytes + 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     QF_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (energy) *energy = sums[total_slots];
     std::vector<double> g(n_params, 0.0);
     for (size_t s = n_seg; s-- > 0;)
         for (uint32_t k = 0; k < bplans[s].n_slots; ++k) g[(size_t)bplans[s].slot_param[k]] += sums[slot_off[s] + k];

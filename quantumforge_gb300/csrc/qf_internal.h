@@ -342,7 +342,10 @@ int reduce_p_one(qf_sv *sv, uint32_t q, double *out);
 int collapse(qf_sv *sv, uint32_t q, int outcome, double scale);
 // Pauli sums: <psi|H|psi> (complex), and lambda = H psi with <psi|lambda>.
 int pauli_expectation(qf_sv *sv, const qf_pauli_term *terms, uint64_t n_terms, double out[2]);
-int pauli_apply(qf_sv *psi, qf_sv *lambda, const qf_pauli_term *terms, uint64_t n_terms, double *energy);
+// lambda = H psi and <psi|H|psi>: into *energy after a stream synchronize, or,
+// with d_energy, left in device memory (two doubles: real, imaginary part)
+int pauli_apply(qf_sv *psi, qf_sv *lambda, const qf_pauli_term *terms, uint64_t n_terms, double *energy,
+                double *d_energy = nullptr);
 // ---- Pauli-sum passes (reduce.cu, compiled form in jit.cpp) --------------
 struct PTerm {
     uint64_t z;

@@ -911,7 +911,9 @@ struct PauliRKernel {
 };
 
 template <typename C>
-int run_pauli(qf_sv *psi, qf_sv *lam, PauliPlan &plan, bool apply, double out[2]) {
+// The sums land in out[] after a stream synchronize, or, with d_out, in
+// device memory (two doubles) with nothing waited for.
+int run_pauli(qf_sv *psi, qf_sv *lam, PauliPlan &plan, bool apply, double out[2], double *d_out = nullptr) {
     qf_ctx *ctx = psi->ctx;
     using R = typename Real<C>::T;
     static size_t dyn_limit[64] = {0};
@@ -1007,8 +1009,9 @@ int run_pauli(qf_sv *psi, qf_sv *lam, PauliPlan &plan, bool apply, double out[2]
     // expectation: every slice; apply: only the slice carrying <psi|lambda>
     const size_t first = apply ? slice - 1 : 0;
     const uint32_t nblk = (uint32_t)(grid * (slice - first));
-    k_final_sum<<<1, 256, 0, ctx->stream>>>(partials + 2 * grid * first, nblk, 2, ctx->d_small);
+    k_final_sum<<<1, 256, 0, ctx->stream>>>(partials + 2 * grid * first, nblk, 2, d_out ? d_out : ctx->d_small);
     QF_CUDA(cudaGetLastError());
+    if (d_out) return QF_OK;
     QF_CUDA(cudaMemcpyAsync(ctx->h_small, ctx->d_small, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     QF_CUDA(cudaStreamSynchronize(ctx->stream));
     out[0] = ctx->h_small[0];
@@ -1035,18 +1038,19 @@ int pauli_expectation(qf_sv *sv, const qf_pauli_term *terms, uint64_t n_terms, d
     return run_pauli<double2>(sv, nullptr, plan, false, out);
 }
 
-int pauli_apply(qf_sv *psi, qf_sv *lam, const qf_pauli_term *terms, uint64_t n_terms, double *energy) {
+int pauli_apply(qf_sv *psi, qf_sv *lam, const qf_pauli_term *terms, uint64_t n_terms, double *energy, double *d_energy) {
     if (n_terms == 0) {
         QF_CUDA(cudaMemsetAsync(lam->d, 0, lam->bytes(), psi->ctx->stream));
+        if (d_energy) QF_CUDA(cudaMemsetAsync(d_energy, 0, 2 * sizeof(double), psi->ctx->stream));
         if (energy) *energy = 0.0;
         return QF_OK;
     }
     PauliPlan plan;
     QF_TRY(plan_pauli(psi->n, psi->dtype, terms, n_terms, plan));
-    double out[2];
-    if (psi->dtype == QF_C64) QF_TRY(run_pauli<float2>(psi, lam, plan, true, out));
-    else QF_TRY(run_pauli<double2>(psi, lam, plan, true, out));
-    if (energy) *energy = out[0];
+    double out[2] = {0.0, 0.0};
+    if (psi->dtype == QF_C64) QF_TRY(run_pauli<float2>(psi, lam, plan, true, out, d_energy));
+    else QF_TRY(run_pauli<double2>(psi, lam, plan, true, out, d_energy));
+    if (energy && !d_energy) *energy = out[0];
     return QF_OK;
 }
 
