@@ -715,13 +715,17 @@ int run_plan_blocks(qf_sv *sv, const Plan &plan) {
     return launch_block_passes<double2>(sv, plan);
 }
 
-// slot_sums[s] += sum over blocks of partials[s * stride + b], in block order.
+// slot_sums[s] += sum over blocks of partials[s * stride + b]: one warp per
+// slot, lane l adding blocks l, l + 32, ... in order, then the warp's tree (the
+// same order on every run). Launch with 256-thread blocks, 8 slots per block.
 __global__ void k_reduce_slots(const double *__restrict__ partials, uint32_t stride, uint32_t n_slots,
                                double *__restrict__ slot_sums) {
-    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < n_slots; s += gridDim.x * blockDim.x) {
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < n_slots; s += (gridDim.x * blockDim.x) >> 5) {
         double v = 0.0;
-        for (uint32_t b = 0; b < stride; ++b) v += partials[(size_t)s * stride + b];
-        slot_sums[s] += v;
+        for (uint32_t b = lane; b < stride; b += 32) v += partials[(size_t)s * stride + b];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) slot_sums[s] += v;
     }
 }
 
@@ -779,8 +783,7 @@ static int launch_passes(qf_sv *psi, qf_sv *lam, const Plan &plan, double *d_slo
         QF_CUDA(cudaGetLastError());
     }
     if (DUAL && plan.n_slots) {
-        k_reduce_slots<<<(plan.n_slots + 127) / 128, 128, 0, ctx->stream>>>(d_partials, grid, plan.n_slots,
-                                                                            d_slot_sums);
+        k_reduce_slots<<<(plan.n_slots + 7) / 8, 256, 0, ctx->stream>>>(d_partials, grid, plan.n_slots, d_slot_sums);
         QF_CUDA(cudaGetLastError());
     }
     return QF_OK;
@@ -835,7 +838,7 @@ int run_plan_dual(qf_sv *psi, qf_sv *lambda, const Plan &plan, double *d_slot_su
 
 int reduce_slots(qf_ctx *ctx, const double *partials, uint32_t stride, uint32_t n_slots, double *d_slot_sums) {
     if (!n_slots) return QF_OK;
-    k_reduce_slots<<<(n_slots + 127) / 128, 128, 0, ctx->stream>>>(partials, stride, n_slots, d_slot_sums);
+    k_reduce_slots<<<(n_slots + 7) / 8, 256, 0, ctx->stream>>>(partials, stride, n_slots, d_slot_sums);
     QF_CUDA(cudaGetLastError());
     return QF_OK;
 }
