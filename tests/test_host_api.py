@@ -62,3 +62,40 @@ def test_sample_expectation_draws_the_seeded_stream():  # src/lib.rs:4840-4850
     with pytest.raises(QuantumError) as err:
         sample_expectation(0.2, ShotConfig(0, 1))
     assert err.value.kind == "InvalidShotCount"
+
+
+def test_op_arrays_are_cached_read_only_and_follow_edits():
+    """Circuit.ops() / ParameterizedCircuit.ops() return one read-only record
+    array while the operation list is unchanged, rebuilt after any edit, equal
+    byte for byte to a record-by-record construction."""
+    def by_record(records):
+        arr = np.zeros(len(records), dtype=A.OP_DTYPE)
+        for i, r in enumerate(records):
+            arr[i] = (r[0], r[1], r[6] if len(r) > 6 else 0, r[2], r[3], r[4], r[5])
+        return arr
+
+    c = qf.Circuit()
+    assert c.ops().shape == (0,)
+    c.operations.append((A.OP_GATE, A.GATE_H, 0, 0, 0, 0.0))
+    c.operations.append((A.OP_CNOT, 0, 0, 1, 0, 0.0))
+    c.channel(1, NoiseChannel.Depolarizing(0.1))
+    a = c.ops()
+    assert c.ops() is a and not a.flags.writeable
+    assert a.tobytes() == by_record(c.operations).tobytes()
+    with pytest.raises(ValueError):
+        a[0]["q0"] = 3
+    c.operations.append((A.OP_GATE, A.GATE_X, 1, 0, 0, 0.0))
+    b = c.ops()
+    assert b is not a and len(b) == 4 and b.tobytes() == by_record(c.operations).tobytes()
+    c.operations[0] = (A.OP_GATE, A.GATE_Z, 1, 0, 0, 0.0)
+    assert int(c.ops()[0]["gate"]) == A.GATE_Z and int(c.ops()[0]["q0"]) == 1
+    del c.operations[1]
+    assert c.ops().tobytes() == by_record(c.operations).tobytes()
+
+    pc = qf.ParameterizedCircuit(2)
+    pc.operations.append((A.OP_ROTATION, A.PAULI_Y, 0, 0, 0, 0.0))
+    pc.operations.append((A.OP_ROTATION, A.PAULI_Z, 0, 0, 1, 0.0))
+    p = pc.ops()
+    assert pc.ops() is p and p.tobytes() == by_record(pc.operations).tobytes()
+    pc.operations.pop()
+    assert len(pc.ops()) == 1
