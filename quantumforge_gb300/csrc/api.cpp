@@ -1452,9 +1452,8 @@ int run_density_steps(qf_sv *sv, uint32_t n, const std::vector<DmStep> &steps, c
             continue;
         }
         // as many sweeps as the widest grouping needs, with the channels spread
-        // evenly over them (the shared-memory work of a sweep grows with its
-        // channel count: a 6-channel sweep of a 14-qubit matrix took 1.6 ms, a
-        // 3-channel one 0.9 ms)
+        // evenly over them (for complex64 the sweeps apply two channels per
+        // shared-memory round, so a sweep's time hardly depends on its count)
         auto groups = group_run(i, e, 12);
         const size_t cap = (e - i + groups.size() - 1) / groups.size();
         auto even = group_run(i, e, cap);

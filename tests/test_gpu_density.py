@@ -223,3 +223,36 @@ def test_density_parameter_shift_matches_the_oracle(backend, n, dtype, tol):
             res.append(O.dm_expectation(O.run_density(shifted, n), A.PAULI_Z, 1))
         want[int(ops[k]["param"])] += 0.5 * (res[0] - res[1])
     assert np.abs(g - want).max() < tol * 10
+
+
+def test_fifteen_qubit_complex64_channel_groups_match_complex128(backend):
+    """Channel groups of a 15-qubit complex64 matrix (4^15 entries, 8 GiB: more
+    than 16 tile-index bits, all three bytes of the paired kernel's deposit
+    tables) against the complex128 matrix, whose channels run one kernel each:
+    trace, purity, P(1) and <X>, <Y>, <Z> of every qubit."""
+    n = 15
+    c = Circuit()
+    for q in range(n):
+        c.push(Gate.Ry(0.3 + 0.1 * q), q)
+    for q in range(0, n - 1, 2):
+        c.cnot(q, q + 1)
+    kinds = (NoiseChannel.AmplitudeDamping, NoiseChannel.Depolarizing, NoiseChannel.PhaseDamping)
+    for q in range(n):
+        c.channel(q, kinds[q % 3](0.05 + 0.02 * q))
+    for q in range(n):
+        c.push(Gate.Rx(0.2 * q - 1.0), q)
+    for q in range(n - 1, 0, -3):
+        c.channel(q, NoiseChannel.AmplitudeDamping(0.11))
+    got, want = {}, {}
+    for dtype, out in (("c64", got), ("c128", want)):
+        rho = DensityMatrix.zero(n, dtype=dtype, backend=backend)
+        c.run_density(rho)
+        out["trace"] = rho.trace().real
+        out["purity"] = rho.purity()
+        out["p1"] = np.array([rho.probability_one(q) for q in range(n)])
+        out["xyz"] = np.array([[rho.expectation(o, q) for o in (A.PAULI_X, A.PAULI_Y, A.PAULI_Z)] for q in range(n)])
+        del rho
+    assert abs(want["trace"] - 1.0) < 1e-9 and abs(got["trace"] - 1.0) < 1e-5
+    assert abs(got["purity"] - want["purity"]) < 1e-5 * max(1.0, want["purity"])
+    assert np.abs(got["p1"] - want["p1"]).max() < 1e-5
+    assert np.abs(got["xyz"] - want["xyz"]).max() < 1e-5

@@ -164,3 +164,29 @@ def test_dense_graphs_in_batched_passes_match_oracle(backend, graph):
         e_ref, g_ref = oracle_cost_grad(n, edges, gam[i], bet[i])
         assert abs(cost[i] - e_ref) < 1e-5 * max(1.0, abs(e_ref)), (i, n, cost[i], e_ref)
         assert np.abs(grad[i] - g_ref).max() < 1e-4 * max(1.0, np.abs(g_ref).max()), (i, n, grad[i], g_ref)
+
+
+@pytest.mark.parametrize("n", [22, 24])
+def test_batched_passes_above_twenty_qubits_match_oracle(backend, n):
+    """Pass B of a 21..24-qubit class has windows at tile bits 8, 4 and 0 with
+    the bits below L = 24 - n masked out (at 24 qubits, L = 0, its tiles load
+    with plain copies): one instance at depth 1 against the oracle (22 qubits:
+    a 3-regular graph; 24 qubits: a sparse graph with edges across pass A's and
+    pass B's qubits, to keep the oracle's run short)."""
+    import os
+
+    rng = np.random.default_rng(40 + n)
+    if n == 22:
+        edges = O.random_3_regular(n, 1200)
+    else:
+        pairs = [(0, 23), (1, 12), (2, 20), (5, 17), (11, 12), (13, 22), (3, 7), (8, 15), (18, 21), (6, 9)]
+        edges = [(u, v, 1.0) for u, v in pairs]
+    p = 1
+    gam = rng.uniform(0, np.pi, (1, p))
+    bet = rng.uniform(0, np.pi / 2, (1, p))
+    cost, grad = QaoaBatch([(n, edges)], p, backend=backend, use_graph=False).run(gam, bet)
+    ops = W.qaoa_param_circuit(n, edges, p)
+    params = np.concatenate([2 * gam[0], 2 * bet[0]])
+    e_ref, g_ref = O.adjoint_uncompute(ops, n, params, PauliSum.maxcut(edges).array(), threads=os.cpu_count() or 1)
+    assert abs(cost[0] - e_ref) < 1e-5 * max(1.0, abs(e_ref)), (cost[0], e_ref)
+    assert np.abs(grad[0] - 2 * g_ref).max() < 1e-4 * max(1.0, np.abs(2 * g_ref).max()), (grad[0], 2 * g_ref)
