@@ -471,7 +471,7 @@ int dm_channels_fused(qf_sv *sv, uint32_t n, const uint32_t *qs, const double (*
         *grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(n_tiles, (uint64_t)std::max(per_sm, 1) * ctx->sm_count));
         return QF_OK;
     };
-    int grid;
+    int grid = 1;
     if (pairs) {
         QF_CUDA(cudaFuncSetAttribute(k_dm_channel_pairs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         QF_TRY(grid_of((const void *)k_dm_channel_pairs, &grid));
