@@ -3,7 +3,8 @@
 ctypes wrapper over ``oracle/_build/libqf_oracle.so``, the plain-C restatement
 of the reference's complex128 CPU simulator (see qf_oracle.h). Only the
 test-suite, the smoke check and the benchmark's CPU legs use it, and only as
-the checker / CPU baseline; the engine never links or calls it.
+the reference the engine's results are compared with and as the timed CPU
+baseline; the engine never links or calls it.
 """
 from __future__ import annotations
 

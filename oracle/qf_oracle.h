@@ -4,8 +4,8 @@
  * TEST INFRASTRUCTURE ONLY. This is a plain-C restatement of QuantumForge's
  * complex128 CPU simulator (the reference crate's `src/lib.rs`,
  * `src/gradients.rs`, `src/analytic.rs`, `src/qaoa_transfer.rs`,
- * `src/mps_qaoa.rs`). It is the checker for the CUDA engine and the timed CPU
- * baseline; nothing in the product links it. Each function cites the
+ * `src/mps_qaoa.rs`). The CUDA engine's results are compared with it and it is
+ * the timed CPU baseline; nothing in the product links it. Each function cites the
  * reference file:line it follows.
  *
  * Parity pin: the reference (Rust, crates.io dependencies) cannot be built in

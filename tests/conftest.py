@@ -26,7 +26,7 @@ def engine_lib():
 
 @pytest.fixture(scope="session")
 def backend(engine_lib):
-    import torch  # noqa: F401  (the GPU machine's torch initialises the driver quickly)
+    import torch  # noqa: F401  (torch brings the CUDA driver up first)
 
     from quantumforge_gb300 import CudaBackend
 
