@@ -253,9 +253,24 @@ int adjoint_device(qf_ctx *ctx, uint32_t n, const std::vector<BGate> &gates, con
     PlanOpts po;
     default_tiling(n, dtype, o->exec.tile_qubits, &po.tile_qubits, &po.low_qubits);
     po.search = !(o->exec.flags & QF_EXEC_FLAG_PLAN_FIRST_COME);
-    // every backward segment is planned before anything launches, then run back
-    // to back: the overlap slots of all segments land in one device buffer that
-    // is read once at the end
+    QF_TRY(fill_zero_state(psi));
+    for (size_t s = 0; s < n_seg; ++s) {
+        const size_t b = seg_begin[s], e = s + 1 < n_seg ? seg_begin[s + 1] : gates.size();
+        std::vector<BGate> seg(gates.begin() + b, gates.begin() + e);
+        Plan plan;
+        po.backward = false;
+        QF_TRY(plan_passes(n, seg, po, plan));
+        QF_TRY(run_plan(psi, plan, o->exec.flags));
+        if (s + 1 < n_seg) {
+            qf_sv *c;
+            QF_TRY(take_checkpoint(ctx, n, dtype, &c));
+            ckpt.push_back(c);
+            QF_CUDA(cudaMemcpyAsync(c->d, psi->d, psi->bytes(), cudaMemcpyDeviceToDevice, ctx->stream));
+        }
+    }
+    // every backward segment is planned while the forward passes run (after
+    // their launches), then run back to back: the overlap slots of all segments
+    // land in one device buffer that is read once at the end
     std::vector<Plan> bplans(n_seg);
     std::vector<size_t> slot_off(n_seg, 0);
     size_t total_slots = 0;
@@ -273,21 +288,6 @@ int adjoint_device(qf_ctx *ctx, uint32_t n, const std::vector<BGate> &gates, con
             QF_TRY(plan_passes(n, seg, bo, bplans[s]));
             slot_off[s] = total_slots;
             total_slots += bplans[s].n_slots;
-        }
-    }
-    QF_TRY(fill_zero_state(psi));
-    for (size_t s = 0; s < n_seg; ++s) {
-        const size_t b = seg_begin[s], e = s + 1 < n_seg ? seg_begin[s + 1] : gates.size();
-        std::vector<BGate> seg(gates.begin() + b, gates.begin() + e);
-        Plan plan;
-        po.backward = false;
-        QF_TRY(plan_passes(n, seg, po, plan));
-        QF_TRY(run_plan(psi, plan, o->exec.flags));
-        if (s + 1 < n_seg) {
-            qf_sv *c;
-            QF_TRY(take_checkpoint(ctx, n, dtype, &c));
-            ckpt.push_back(c);
-            QF_CUDA(cudaMemcpyAsync(c->d, psi->d, psi->bytes(), cudaMemcpyDeviceToDevice, ctx->stream));
         }
     }
     // the slot sums and, behind them, the energy stay on the device until the
